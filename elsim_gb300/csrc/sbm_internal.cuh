@@ -1,0 +1,274 @@
+// sbm_internal.cuh -- shared declarations of the GB300 SBM library.
+//
+// Device layout: every field lives in HBM in the reference's halo-padded
+// Fortran layout A(0:ny+1, 0:nx+1, 0:nz+1), y fastest, so host arrays are
+// uploaded and downloaded with one contiguous copy and no transpose.  The
+// MPI decomposition of the reference (MyDmnCmpn_YZ / BcMpiYZ in
+// SBMES_3D_MPI_CH_Gr_CONJG_VD_T05_01_BQ_hx3.f90) collapses into this one
+// device-resident domain; physical-boundary ghost rules are applied inside
+// the kernels that read the ghosts.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/sbm_capi.h"
+
+namespace sbm {
+
+// ------------------------------------------------------------ geometry
+struct Geo {
+  int ny, nx, nz;
+  int64_t sx;  // stride of the x index j   = ny+2
+  int64_t sz;  // stride of the z index k   = (ny+2)(nx+2)
+  int64_t nh;  // halo-padded element count = (ny+2)(nx+2)(nz+2)
+  __host__ __device__ __forceinline__ int64_t ix(int i, int j, int k) const {
+    return (int64_t)i + sx * j + sz * k;
+  }
+  __host__ __device__ __forceinline__ int64_t ninterior() const {
+    return (int64_t)ny * nx * nz;
+  }
+};
+
+inline Geo make_geo(int ny, int nx, int nz) {
+  Geo g;
+  g.ny = ny;
+  g.nx = nx;
+  g.nz = nz;
+  g.sx = ny + 2;
+  g.sz = (int64_t)(ny + 2) * (nx + 2);
+  g.nh = g.sz * (nz + 2);
+  return g;
+}
+
+// ------------------------------------------------------- launch shape
+// Stencil-family kernels map threadIdx.x to y (the contiguous axis) and
+// threadIdx.y to x; each thread marches `zc` planes in z and keeps the
+// z-neighbours in registers.
+constexpr int BX = 32;
+constexpr int BY = 8;
+constexpr int kMaxPartials = 1 << 16;  // >= blocks of any reduction launch
+
+struct Shape {
+  dim3 grid, block;
+  int zc;
+  int nblocks() const { return (int)(grid.x * grid.y * grid.z); }
+};
+
+inline Shape stencil_shape(const Geo& g, int zc) {
+  Shape s;
+  s.zc = zc < 1 ? 1 : zc;
+  s.block = dim3(BX, BY, 1);
+  s.grid = dim3((g.ny + BX - 1) / BX, (g.nx + BY - 1) / BY, (g.nz + s.zc - 1) / s.zc);
+  return s;
+}
+
+// Picks the z-chunk so that a launch covers the 152 SMs in several full
+// waves; `tuned` > 0 overrides (set by the autotuner).
+int pick_zc(const Geo& g, int tuned);
+
+// -------------------------------------------------------- CG state
+// One per solve, in device memory.  Scalars are produced by the last block
+// of each reduction kernel and consumed by the next kernel, so the loop
+// needs no host round trip; `done` turns remaining launches of a captured
+// chunk into no-ops.
+struct CgState {
+  double rho;     // CG scalar of the current residual: r.z (r.r without preconditioner)
+  double rr;      // r.r of the current residual (stopping test)
+  double rr0;     // r.r of the initial residual
+  double pq;      // p.Ap
+  double alpha, beta;
+  double rms;     // value of the stopping norm after the last iteration
+  double tol;
+  double wsum;    // sum of the stopping weight (tPP / tPE)
+  double aux[4];
+  int iter;
+  int max_it;
+  int done;       // 0 running, 1 converged, 2 iteration cap, 3 non-finite, 4 breakdown
+  int stop_rule;
+  unsigned int counter[8];
+};
+
+// ------------------------------------------------------ errors, counters
+extern std::atomic<int64_t> g_launches;
+void set_error(const char* where, cudaError_t e);
+const char* last_error();
+
+#define SBM_CUDA_TRY(call)                                    \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) {                                  \
+      ::sbm::set_error(#call, e_);                            \
+      return SBM_ERR_CUDA;                                    \
+    }                                                         \
+  } while (0)
+
+#define SBM_LAUNCHED(n) ::sbm::g_launches.fetch_add((n), std::memory_order_relaxed)
+
+// ---------------------------------------------------- device helpers
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of `v` for up to 1024 threads; result valid in thread 0.
+__device__ __forceinline__ double block_sum(double v, double* smem32) {
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthr = blockDim.x * blockDim.y * blockDim.z;
+  v = warp_sum(v);
+  if ((tid & 31) == 0) smem32[tid >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (tid < 32) {
+    r = (tid < (nthr + 31) / 32) ? smem32[tid] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// Deterministic grid reduction of NV values per thread: block sums go to
+// partials[v * nblocks + block]; the last block to finish sums them in a
+// fixed order and returns true with the totals in `tot` (valid in every
+// thread of that block).  The counter is re-armed for the next launch.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(const double (&v)[NV], double* partials,
+                                            unsigned int* counter, double (&tot)[NV]) {
+  __shared__ double sm[32];
+  __shared__ bool is_last;
+  __shared__ double res[NV];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthr = blockDim.x * blockDim.y * blockDim.z;
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const double b = block_sum(v[q], sm);
+    if (tid == 0) partials[q * nb + bid] = b;
+  }
+  if (tid == 0) {
+    __threadfence();
+    const unsigned int t = atomicAdd(counter, 1u);
+    is_last = (t == (unsigned int)nb - 1u);
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  __threadfence();
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    double s = 0.0;
+    for (int b = tid; b < nb; b += nthr) s += __ldcg(partials + q * nb + b);
+    s = block_sum(s, sm);
+    if (tid == 0) res[q] = s;
+  }
+  if (tid == 0) *counter = 0u;
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NV; ++q) tot[q] = res[q];
+  return true;
+}
+
+// ------------------------------------------------------ operator args
+// q = scale*S(p)            (FORM 0: the phP / phE form, SBMES:670-676)
+// q = diag*p - scale*S(p)   (FORM 1: the CnE form,       SBMES:515-521)
+// with S(p) = sum_f c_f (p_nb - p_c), c_f = hk_nb + hk_c, hk = K/2.
+template <typename T>
+struct OpArgs {
+  Geo g;
+  const T* hk;    // half node coefficient, halo-padded
+  const T* diag;  // FORM 1 diagonal field (psE), halo-padded, else null
+  T scale;
+  int form;       // 0 or 1
+  int bcx0, bcx1; // SBM_BC_COPY / SBM_BC_ZERO for the search direction
+};
+
+// ------------------------------------------------------- launchers
+// q = A x with x's ghosts read from memory (no reduction), FP64.  Used for
+// RHE = (1/dx^2) div(pce grad CnE), SBMES:591-596.
+cudaError_t launch_apply_mem64(const OpArgs<double>& op, const double* x, double* q,
+                               cudaStream_t s);
+// hk = 0.5 * K over the padded array.
+cudaError_t launch_half(const Geo& g, const double* k, double* hk, cudaStream_t s);
+
+struct SolveSpec {
+  int op;             // SBM_OP_*
+  int bcx0, bcx1;
+  int form;
+  double scale;
+  const double* hk64; // FP64 half coefficient
+  const double* diag64;
+  const double* rhs;  // halo layout, interior used
+  double* x;          // halo layout, ghosts hold Dirichlet / flux data
+  const double* w;    // stop weight
+  double wsum;
+  int stop_rule;
+  double tol;
+  int max_it;
+  int precision;
+  int precond;
+  // FP32 copies for the mixed path (may be null -> built on demand)
+  const float* hk32;
+  const float* diag32;
+};
+
+struct SolveResult {
+  int iters;
+  int outer;
+  double final_res;
+  float ms;
+  int status;
+};
+
+}  // namespace sbm
+
+// ------------------------------------------------------------ context
+#include <map>
+#include <vector>
+
+struct sbm_ctx {
+  sbm::Geo g;
+  sbm_params p;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evq[2] = {nullptr, nullptr};
+  // public fields (halo-padded FP64)
+  double* f[SBM_F_COUNT] = {};
+  // half node coefficients of the four operators (FP64)
+  double *hk_kap = nullptr, *hk_pce = nullptr, *hk_pcc = nullptr, *hk_gen = nullptr;
+  // step work fields (halo-padded FP64)
+  double *dab = nullptr, *dab1 = nullptr, *mu = nullptr, *mb = nullptr, *pmn = nullptr;
+  double *rhs = nullptr, *rhe = nullptr, *rxc = nullptr, *kfw = nullptr, *kbw = nullptr;
+  double *ppo = nullptr, *peo = nullptr, *tmp = nullptr;
+  // FP64 CG work: residual, direction, A*direction, IR correction, IR r0
+  double *r64 = nullptr, *p64 = nullptr, *q64 = nullptr, *d64 = nullptr, *r0 = nullptr;
+  // FP32 work: half coefficient, diagonal, residual, direction, A*direction, correction, z
+  float *hk32 = nullptr, *dg32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr,
+        *x32 = nullptr, *z32 = nullptr, *rold32 = nullptr;
+  // reductions
+  double* partials = nullptr;
+  sbm::CgState* st = nullptr;      // device: outer / FP64 state
+  sbm::CgState* st32 = nullptr;    // device: inner FP32 state
+  sbm::CgState* h_st = nullptr;    // pinned host copies [4]
+  double* d_scal = nullptr;        // device scalar scratch [64]
+  double* h_scal = nullptr;        // pinned host scalar scratch [64]
+  // electrochemical scalars (host mirror)
+  sbm_scalars sc{};
+  // tuning
+  int zc64 = 0, zc32 = 0, chunk = 0;
+  double inner_tol = 0.0;
+  int inner_max = 0;
+  // CUDA graphs of captured CG chunks, keyed by solve signature
+  std::map<std::string, std::pair<cudaGraphExec_t, int>> graphs;
+  // learned preconditioner (opaque; owned by sbm_learned.cu)
+  void* net = nullptr;
+};
+
+namespace sbm {
+int solve(sbm_ctx* ctx, const SolveSpec& spec, SolveResult* out);
+int ensure_fp32_work(sbm_ctx* ctx);
+void release_graphs(sbm_ctx* ctx);
+}  // namespace sbm

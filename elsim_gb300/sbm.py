@@ -1,0 +1,359 @@
+"""Host-side mirror of the reference's SBM solver interface over the C-ABI.
+
+The reference (AffanMalik90/Elsim, src/frtrn/SBMES_3D_MPI_CH_Gr_CONJG_VD_T05_01_BQ_hx3.f90,
+called SBMES here) is one Fortran program whose solver loops are inline; its
+only subroutines on the path are Tbl_Chk_Pln_3DA (SBMES:987), ReDist3D_XYZ
+(LevelSet_3D.f90:194) and the AccDiff sweep (AccDiff_3D.f90:111).  This
+module binds ``libsbm_gb300.so`` with ctypes exactly as a Fortran
+``bind(C)`` interface would, and offers:
+
+* ``Context`` -- one device-resident domain: field upload/download in the
+  reference's halo-padded (y, x, z) layout, ``setup_domain`` (SBMES:154-341),
+  ``cg_solve`` (the inline CG loops), and the time-step stages;
+* ``tbl_chk_pln_3da``, ``redist3d_xyz``, ``accdiff``, ``rm_mask``, ``sign``
+  -- one-for-one replacements of the reference subroutines/blocks.
+
+Arrays are numpy arrays in Fortran order, indexed ``A[i, j, k]`` with the
+halo at index 0 and n+1, as in the reference.  Errors raise ``SbmError``
+carrying the C status code.  There is no CPU fallback: if the CUDA library
+is missing the import of a ``Context`` fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libsbm_gb300.so"
+
+# status codes (include/sbm_capi.h)
+OK, ERR_ARG, ERR_CUDA, ERR_MAXIT, ERR_NONFINITE, ERR_BREAKDOWN, ERR_NOMEM, ERR_STATE = (
+    0, -1, -2, -3, -4, -5, -6, -7)
+BC_COPY, BC_ZERO = 0, 1
+OP_CNE, OP_PHP, OP_PHE, OP_GENERIC = 0, 1, 2, 3
+STOP_REF_UPDATE, STOP_REF_RESID, STOP_REL_RES = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+PC_NONE, PC_JACOBI, PC_LEARNED = 0, 1, 2
+BV_EXP, BV_LINEAR = 0, 1
+F_PSP, F_PSE, F_AVP, F_AVPX, F_CNP, F_CNE, F_PHP, F_PHE, F_RXN, F_COEF, F_RHS, F_X, F_WEIGHT = range(13)
+FIELDS = dict(psP=F_PSP, psE=F_PSE, AvP=F_AVP, AvPx=F_AVPX, CnP=F_CNP, CnE=F_CNE, phP=F_PHP,
+              phE=F_PHE, Rxn=F_RXN, coef=F_COEF, rhs=F_RHS, x=F_X, weight=F_WEIGHT)
+TBL_MAX = 128
+
+_ERRNAMES = {ERR_ARG: "bad argument", ERR_CUDA: "CUDA error", ERR_MAXIT: "iteration cap",
+             ERR_NONFINITE: "non-finite value", ERR_BREAKDOWN: "CG breakdown",
+             ERR_NOMEM: "out of device memory", ERR_STATE: "invalid state"}
+
+
+class SbmError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str = ""):
+        self.code = code
+        msg = f"{where}: {_ERRNAMES.get(code, 'error')} ({code})"
+        if detail:
+            msg += f" [{detail}]"
+        super().__init__(msg)
+
+
+class Params(C.Structure):
+    """Mirror of ``sbm_params`` (include/sbm_capi.h)."""
+    _fields_ = [(n, C.c_double) for n in (
+        "dx", "rho", "eps", "ch_mask", "d0", "tc1", "tc2", "t_minus", "dab_c0", "dab_c1", "dab_c2",
+        "dab_c3", "cne_ref", "cst1", "frd", "bvp", "bve", "kap_scale", "avp_mask", "i0_scale",
+        "kfw_c", "crt_cne", "crt_php", "crt_phe", "crt_picard")] + [
+        (n, C.c_int) for n in ("max_it_cne", "max_it_php", "max_it_phe", "max_picard",
+                               "cne_mean_every", "bv_mode", "tbl_n", "pad_")] + [
+        (n, C.c_double * TBL_MAX) for n in ("tbl_x", "tbl_mu", "tbl_mb", "tbl_i0", "tbl_ocv")]
+
+    def set_table(self, name: str, values) -> None:
+        v = np.asarray(values, dtype=np.float64)
+        if v.size > TBL_MAX:
+            raise ValueError("table longer than SBM_TBL_MAX")
+        arr = getattr(self, name)
+        for t, x in enumerate(v):
+            arr[t] = float(x)
+        if name == "tbl_x":
+            self.tbl_n = int(v.size)
+
+    def table(self, name: str) -> np.ndarray:
+        return np.array(getattr(self, name)[: self.tbl_n])
+
+
+class Scalars(C.Structure):
+    """Mirror of ``sbm_scalars``."""
+    _fields_ = [(n, C.c_double) for n in ("tPP", "tPE", "xrf", "infx", "scrnt", "trgI", "bve",
+                                          "cvgp", "cvgl")] + [
+        (n, C.c_int) for n in ("it_cne", "it_php", "it_phe", "n_picard")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: os.PathLike | None = None) -> C.CDLL:
+    """Loads the CUDA library (fails loudly when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(
+            f"{p} not built: run `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the SBM path has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    dp, fp, ip, vp = C.POINTER(C.c_double), C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_void_p
+    i64 = C.c_int64
+    sig = {
+        "sbm_version": (C.c_char_p, []),
+        "sbm_launch_count": (i64, []),
+        "sbm_last_error": (C.c_char_p, []),
+        "sbm_params_reference": (C.c_int, [C.POINTER(Params)]),
+        "sbm_ctx_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(vp)]),
+        "sbm_ctx_destroy": (C.c_int, [vp]),
+        "sbm_ctx_set_params": (C.c_int, [vp, C.POINTER(Params)]),
+        "sbm_ctx_set_tuning": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]),
+        "sbm_ctx_stream": (C.c_int, [vp, C.POINTER(vp)]),
+        "sbm_ctx_sync": (C.c_int, [vp]),
+        "sbm_upload": (C.c_int, [vp, C.c_int, dp, C.c_int]),
+        "sbm_download": (C.c_int, [vp, C.c_int, dp, C.c_int]),
+        "sbm_field_ptr": (C.c_int, [vp, C.c_int, C.POINTER(dp)]),
+        "sbm_setup_domain": (C.c_int, [vp, fp, fp, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.POINTER(Scalars)]),
+        "sbm_cg_solve": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                   C.c_int, C.c_int, C.c_int, ip, dp, fp]),
+        "sbm_time_step": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_int,
+                                    C.POINTER(Scalars)]),
+        "sbm_ch_step": (C.c_int, [vp, C.c_double, C.POINTER(Scalars)]),
+        "sbm_cne_step": (C.c_int, [vp, C.c_int, C.c_double, C.c_int, C.POINTER(Scalars)]),
+        "sbm_bv_update": (C.c_int, [vp, C.c_int, C.POINTER(Scalars)]),
+        "sbm_voltage_step": (C.c_int, [vp, C.c_double, C.c_double, C.POINTER(Scalars)]),
+        "sbm_table_lookup": (C.c_int, [i64, C.c_int, dp, dp, dp, dp]),
+        "sbm_redist": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]),
+        "sbm_accdiff": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, C.c_int]),
+        "sbm_rm_mask": (C.c_int, [i64, dp, dp, dp]),
+        "sbm_sign": (C.c_int, [i64, dp, C.c_double, dp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def declared_symbols() -> list[str]:
+    """Every function name declared in include/sbm_capi.h."""
+    import re
+    hdr = (_PKG.parent / "include" / "sbm_capi.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[\w]+\**\s+\**(sbm_\w+)\s*\(", hdr, re.M)))
+
+
+def _check(rc: int, where: str) -> int:
+    if rc != OK:
+        detail = ""
+        if rc == ERR_CUDA and _lib is not None:
+            detail = _lib.sbm_last_error().decode(errors="replace")
+        raise SbmError(rc, where, detail)
+    return rc
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f64(a, shape=None) -> np.ndarray:
+    a = np.asarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return np.asfortranarray(a)
+
+
+def reference_params() -> Params:
+    """The reference's constants (SBMES:90-136) with flat synthetic tables."""
+    p = Params()
+    _check(load_library().sbm_params_reference(C.byref(p)), "sbm_params_reference")
+    return p
+
+
+def launch_count() -> int:
+    return int(load_library().sbm_launch_count())
+
+
+class Context:
+    """One device-resident SBM domain of ny x nx x nz interior voxels."""
+
+    def __init__(self, ny: int, nx: int, nz: int, params: Params | None = None):
+        self.lib = load_library()
+        self.shape = (ny, nx, nz)
+        self.hshape = (ny + 2, nx + 2, nz + 2)
+        self.params = params if params is not None else reference_params()
+        h = C.c_void_p()
+        _check(self.lib.sbm_ctx_create(ny, nx, nz, C.byref(self.params), C.byref(h)),
+               "sbm_ctx_create")
+        self._h = h
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.sbm_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- configuration
+    def set_params(self, params: Params) -> None:
+        self.params = params
+        _check(self.lib.sbm_ctx_set_params(self._h, C.byref(params)), "sbm_ctx_set_params")
+
+    def set_tuning(self, zc64=0, zc32=0, chunk=0, inner_tol=0.0, inner_max=0) -> None:
+        _check(self.lib.sbm_ctx_set_tuning(self._h, zc64, zc32, chunk, inner_tol, inner_max),
+               "sbm_ctx_set_tuning")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(self.lib.sbm_ctx_stream(self._h, C.byref(s)), "sbm_ctx_stream")
+        return s.value or 0
+
+    def sync(self) -> None:
+        _check(self.lib.sbm_ctx_sync(self._h), "sbm_ctx_sync")
+
+    # -- fields
+    def upload(self, field, a, haloed: bool = True) -> None:
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        a = _f64(a, self.hshape if haloed else self.shape)
+        _check(self.lib.sbm_upload(self._h, fid, _dptr(a), int(haloed)), "sbm_upload")
+
+    def download(self, field, haloed: bool = True) -> np.ndarray:
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        out = np.zeros(self.hshape if haloed else self.shape, dtype=np.float64, order="F")
+        _check(self.lib.sbm_download(self._h, fid, _dptr(out), int(haloed)), "sbm_download")
+        return out
+
+    def field_ptr(self, field) -> int:
+        fid = FIELDS[field] if isinstance(field, str) else int(field)
+        p = C.POINTER(C.c_double)()
+        _check(self.lib.sbm_field_ptr(self._h, fid, C.byref(p)), "sbm_field_ptr")
+        return C.cast(p, C.c_void_p).value
+
+    # -- set-up and solves
+    def setup_domain(self, dist_p, dist_e, zeta=0.5, cnp0=2.02e-2, cne0=1.0e-3, cr=6.0) -> dict:
+        """SBMES:154-341 from two REAL(4) distance fields (interior shape)."""
+        dp = np.asfortranarray(np.asarray(dist_p, dtype=np.float32))
+        de = np.asfortranarray(np.asarray(dist_e, dtype=np.float32))
+        if dp.shape != self.shape or de.shape != self.shape:
+            raise ValueError("distance fields must have the interior shape")
+        s = Scalars()
+        fpt = C.POINTER(C.c_float)
+        _check(self.lib.sbm_setup_domain(self._h, dp.ctypes.data_as(fpt), de.ctypes.data_as(fpt),
+                                         zeta, cnp0, cne0, cr, C.byref(s)), "sbm_setup_domain")
+        return s.as_dict()
+
+    def cg_solve(self, op=OP_GENERIC, bc_x0=BC_COPY, bc_x1=BC_COPY, scale=1.0, tol=1e-8,
+                 max_it=100000, stop_rule=STOP_REL_RES, precision=PREC_FP64, precond=PC_NONE,
+                 raise_on_maxit: bool = True) -> dict:
+        it = C.c_int(0)
+        res = C.c_double(0)
+        ms = C.c_float(0)
+        rc = self.lib.sbm_cg_solve(self._h, op, bc_x0, bc_x1, scale, tol, max_it, stop_rule,
+                                   precision, precond, C.byref(it), C.byref(res), C.byref(ms))
+        if rc != OK and not (rc == ERR_MAXIT and not raise_on_maxit):
+            _check(rc, "sbm_cg_solve")
+        return dict(iters=it.value, final_res=res.value, ms=ms.value, status=rc)
+
+    def time_step(self, it: int, dt: float, vsr: float, precision=PREC_FP64) -> dict:
+        s = Scalars()
+        _check(self.lib.sbm_time_step(self._h, it, dt, vsr, precision, C.byref(s)),
+               "sbm_time_step")
+        return s.as_dict()
+
+    def ch_step(self, dt: float) -> dict:
+        s = Scalars()
+        _check(self.lib.sbm_ch_step(self._h, dt, C.byref(s)), "sbm_ch_step")
+        return s.as_dict()
+
+    def cne_step(self, it: int, dt: float, precision=PREC_FP64) -> dict:
+        s = Scalars()
+        _check(self.lib.sbm_cne_step(self._h, it, dt, precision, C.byref(s)), "sbm_cne_step")
+        return s.as_dict()
+
+    def bv_update(self, precision=PREC_FP64) -> dict:
+        s = Scalars()
+        _check(self.lib.sbm_bv_update(self._h, precision, C.byref(s)), "sbm_bv_update")
+        return s.as_dict()
+
+    def voltage_step(self, dt: float, vsr: float) -> dict:
+        s = Scalars()
+        _check(self.lib.sbm_voltage_step(self._h, dt, vsr, C.byref(s)), "sbm_voltage_step")
+        return s.as_dict()
+
+
+# ------------------------------------------------------- stateless routines
+
+def tbl_chk_pln_3da(cord, vals, cn) -> np.ndarray:
+    """Tbl_Chk_Pln_3DA (SBMES:987-1028) on the GPU; any array shape."""
+    lib = load_library()
+    cord = np.ascontiguousarray(cord, dtype=np.float64)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    c = np.asarray(cn, dtype=np.float64)
+    flat = np.ascontiguousarray(c).ravel()
+    out = np.empty_like(flat)
+    _check(lib.sbm_table_lookup(flat.size, cord.size, _dptr(cord), _dptr(vals), _dptr(flat),
+                                _dptr(out)), "sbm_table_lookup")
+    return out.reshape(c.shape)
+
+
+def redist3d_xyz(lit: int, sg, f, dt: float = 1.0e-1) -> np.ndarray:
+    """ReDist3D_XYZ (LevelSet_3D.f90:194-261) on the GPU; returns the new f.
+
+    ``dt`` is 1.0d-1 in LevelSet_3D.f90 and the REAL(4) 1.0e-1 (pass
+    ``float(np.float32(0.1))``) in RM_UCNCT_3D.f90."""
+    lib = load_library()
+    sg = _f64(sg)
+    f = _f64(f).copy(order="F")
+    py, px, pz = (s - 2 for s in sg.shape)
+    _check(lib.sbm_redist(lit, py, px, pz, dt, _dptr(sg), _dptr(f)), "sbm_redist")
+    return f
+
+
+def accdiff(psi, cn, term: int = 1501, dirichlet_x: int = 1) -> np.ndarray:
+    """One AccDiff_3D phase (AccDiff_3D.f90:111-169 solid with dirichlet_x=1,
+    :185-243 electrolyte with dirichlet_x=0) on the GPU; returns the new Cn."""
+    lib = load_library()
+    psi = _f64(psi)
+    cn = _f64(cn).copy(order="F")
+    py, px, pz = (s - 2 for s in psi.shape)
+    _check(lib.sbm_accdiff(py, px, pz, _dptr(psi), _dptr(cn), term, dirichlet_x), "sbm_accdiff")
+    return cn
+
+
+def rm_mask(psA, cn) -> np.ndarray:
+    """RM_UCNCT_3D.f90:79-82: psB = psA, 0 where Cn < 1e-4 (REAL(4))."""
+    lib = load_library()
+    a = np.ascontiguousarray(psA, dtype=np.float64)
+    c = np.ascontiguousarray(cn, dtype=np.float64)
+    out = np.empty_like(a)
+    _check(lib.sbm_rm_mask(a.size, _dptr(a), _dptr(c), _dptr(out)), "sbm_rm_mask")
+    return out
+
+
+def sign(ds, thr: float = 0.5) -> np.ndarray:
+    """LevelSet_3D.f90:140-144: 1 where ds > thr, else -1."""
+    lib = load_library()
+    d = np.ascontiguousarray(ds, dtype=np.float64)
+    out = np.empty_like(d)
+    _check(lib.sbm_sign(d.size, _dptr(d), thr, _dptr(out)), "sbm_sign")
+    return out

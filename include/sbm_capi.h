@@ -1,0 +1,244 @@
+/*
+ * sbm_capi.h -- C-ABI of the GB300 smoothed-boundary-method (SBM) hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers, sizes and a plain
+ * parameter struct, and returns an `int` status (SBM_OK == 0, negative on
+ * error).  Nothing here aborts the process.  The types are bind(C)
+ * compatible, so a Fortran host can declare them in an ISO_C_BINDING
+ * interface block (INTEGER(C_INT), REAL(C_DOUBLE), TYPE(C_PTR)).
+ *
+ * Array layout is the reference's: Fortran column-major (y, x, z), y fastest.
+ * A halo-padded field A(0:ny+1, 0:nx+1, 0:nz+1) has element (i, j, k) at
+ *     i + (ny+2) * (j + (nx+2) * k)
+ * and an interior-only field B(1:ny, 1:nx, 1:nz) has element (i, j, k) at
+ *     (i-1) + ny * ((j-1) + nx * (k-1)).
+ * The x axis (2nd index) carries the Dirichlet / flux faces, exactly as in
+ * SBMES_3D_MPI_CH_Gr_CONJG_VD_T05_01_BQ_hx3.f90 (called SBMES below).
+ *
+ * The reference has no FFI of its own: its solver loops are inline in the
+ * main program.  Each declaration below names the reference lines it
+ * replaces.
+ */
+#ifndef SBM_CAPI_H
+#define SBM_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define SBM_OK                 0
+#define SBM_ERR_ARG           -1   /* bad dimension, null pointer, unknown id */
+#define SBM_ERR_CUDA          -2   /* a CUDA runtime call failed               */
+#define SBM_ERR_MAXIT         -3   /* iteration cap hit before tolerance       */
+#define SBM_ERR_NONFINITE     -4   /* NaN/Inf in a reduction                   */
+#define SBM_ERR_BREAKDOWN     -5   /* p.Ap == 0 in CG                          */
+#define SBM_ERR_NOMEM         -6   /* device allocation failed                 */
+#define SBM_ERR_STATE         -7   /* call made in a state that forbids it     */
+
+/* ---------------------------------------------------------- enumerations */
+/* Ghost rule applied to the CG search direction at an x face
+ * (SBMES:512-513, :667-668, :748-749).  y and z faces are always Neumann
+ * (edge copy), as BcMpiYZ does at the physical boundary (SBMES:1043-1088). */
+#define SBM_BC_COPY   0   /* PRJ(ghost) = PRJ(edge)   (Neumann)  */
+#define SBM_BC_ZERO   1   /* PRJ(ghost) = 0           (Dirichlet) */
+
+/* Operator families (SBMES:515-521 CnE, :670-676 phP, :751-757 phE).
+ * GENERIC is the phP form on the context's COEF field with the x-face ghost
+ * rules taken from the solve call (used for the plain potential solve). */
+#define SBM_OP_CNE      0
+#define SBM_OP_PHP      1
+#define SBM_OP_PHE      2
+#define SBM_OP_GENERIC  3
+
+/* Stopping rules.  REF_UPDATE: sqrt(sum(w*dx^2)/sum(w)) < tol, the
+ * potential loops (SBMES:699-705, :780-786).  REF_RESID:
+ * sqrt(sum(w*r^2)/sum(w)) < tol, the CnE loop (SBMES:545-547).
+ * REL_RES: ||r||_2 / ||r_0||_2 <= tol. */
+#define SBM_STOP_REF_UPDATE  0
+#define SBM_STOP_REF_RESID   1
+#define SBM_STOP_REL_RES     2
+
+/* Solver variants (no counterpart in the reference). */
+#define SBM_PREC_FP64   0   /* plain FP64 CG: the drop-in                    */
+#define SBM_PREC_MIXED  1   /* FP32 inner CG inside FP64 iterative refinement */
+
+#define SBM_PC_NONE     0
+#define SBM_PC_JACOBI   1
+#define SBM_PC_LEARNED  2
+
+/* Butler-Volmer forms (SBMES:636-637). */
+#define SBM_BV_EXP      0   /* reference exponential form        */
+#define SBM_BV_LINEAR   1   /* first-order expansion in dPh      */
+
+/* Device-resident fields of a context.  All are halo-padded FP64. */
+enum sbm_field {
+  SBM_F_PSP = 0,   /* psP  particle domain parameter      SBMES:143 */
+  SBM_F_PSE,       /* psE  electrolyte domain parameter   SBMES:144 */
+  SBM_F_AVP,       /* AvP  interface measure              SBMES:273-289 */
+  SBM_F_AVPX,      /* AvPx = AvP/dx                        SBMES:291 */
+  SBM_F_CNP,       /* CnP  particle Li fraction           SBMES:295 */
+  SBM_F_CNE,       /* CnE  salt concentration             SBMES:306 */
+  SBM_F_PHP,       /* phP  particle potential             SBMES:316 */
+  SBM_F_PHE,       /* phE  electrolyte potential          SBMES:336 */
+  SBM_F_RXN,       /* Rxn  reaction rate                  SBMES:310 */
+  SBM_F_COEF,      /* node coefficient of the GENERIC operator */
+  SBM_F_RHS,       /* right-hand side of a GENERIC solve       */
+  SBM_F_X,         /* unknown of a GENERIC solve (ghosts = Dirichlet data) */
+  SBM_F_WEIGHT,    /* psi weight of the GENERIC stopping norm  */
+  SBM_F_COUNT
+};
+
+#define SBM_TBL_MAX 128
+
+/* Physical and numerical parameters of the electrochemical step.  Field
+ * names follow the reference's variables; defaults (sbm_params_reference)
+ * carry the reference's Fortran literals with their kinds preserved. */
+typedef struct sbm_params {
+  double dx;              /* SBMES:90 */
+  double rho;             /* SBMES:100 (REAL(4) literal)     */
+  double eps;             /* SBMES:136                        */
+  double ch_mask;         /* 1e-5 update mask, SBMES:430      */
+  double d0, tc1, tc2, t_minus;   /* SBMES:118-126 */
+  double dab_c0, dab_c1, dab_c2, dab_c3; /* Dab = D0*EXP(c0 - c1*c + c2*(c3*c)**2), SBMES:474 */
+  double cne_ref;         /* mean CnE target 1e-3, SBMES:567  */
+  double cst1, frd;       /* SBMES:101-102                    */
+  double bvp, bve;        /* SBMES:106-107                    */
+  double kap_scale;       /* 3.3, SBMES:324                   */
+  double avp_mask;        /* 1e-2, SBMES:287, :631            */
+  double i0_scale;        /* 1e-3, SBMES:617                  */
+  double kfw_c;           /* 0.001 in Kfw, SBMES:621          */
+  double crt_cne, crt_php, crt_phe, crt_picard; /* SBMES:96-98, :627 */
+  int    max_it_cne, max_it_php, max_it_phe, max_picard;
+  int    cne_mean_every;  /* 100, SBMES:562 */
+  int    bv_mode;         /* SBM_BV_EXP or SBM_BV_LINEAR */
+  int    tbl_n;           /* table length (101), SBMES:210-242 */
+  int    pad_;
+  double tbl_x[SBM_TBL_MAX];    /* Tbl(1,:)  coordinates   */
+  double tbl_mu[SBM_TBL_MAX];   /* Tbl(2,:)  chemical potential, C_Li_M6 */
+  double tbl_mb[SBM_TBL_MAX];   /* DTbl(2,:) mobility, C_Li_Mb5 (already scaled) */
+  double tbl_i0[SBM_TBL_MAX];   /* iTbl(2,:) exchange current, C_Li_J2 */
+  double tbl_ocv[SBM_TBL_MAX];  /* OTbl(2,:) open-circuit voltage, C_Li_O3 */
+} sbm_params;
+
+/* Scalars of the electrochemical state that the reference keeps in
+ * program variables (SBMES:248-262, :303, :341, :351, :443, :828). */
+typedef struct sbm_scalars {
+  double tPP, tPE;        /* sums of psP, psE */
+  double xrf;             /* mean particle Li fraction */
+  double infx;            /* Li influx */
+  double scrnt, trgI;     /* current and target current */
+  double bve;             /* electrolyte boundary potential (moves) */
+  double cvgp, cvgl;      /* Picard convergence norms of the last step */
+  int    it_cne, it_php, it_phe, n_picard; /* CG iterations of the last step */
+} sbm_scalars;
+
+typedef struct sbm_ctx sbm_ctx;
+
+/* Fills *p with the reference's constants (SBMES:90-136) and flat tables. */
+int sbm_params_reference(sbm_params* p);
+
+/* Context: one device-resident domain (replaces the MPI decomposition
+ * MyDmnCmpn_YZ, SBMES:947-982, and the halo exchange BcMpiYZ,
+ * SBMES:1031-1090).  Owns device buffers and one CUDA stream. */
+int sbm_ctx_create(int ny, int nx, int nz, const sbm_params* p, sbm_ctx** out);
+int sbm_ctx_destroy(sbm_ctx* ctx);
+int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p);
+/* Launch-shape and mixed-precision knobs (0 = built-in choice): z planes
+ * per thread of the FP64 / FP32 stencil kernels, CG iterations per captured
+ * graph chunk, relative tolerance and iteration cap of the inner FP32 solve.
+ * No counterpart in the reference. */
+int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double inner_tol,
+                       int inner_max);
+/* The context's CUDA stream as an opaque handle (cudaStream_t). */
+int sbm_ctx_stream(sbm_ctx* ctx, void** stream);
+int sbm_ctx_sync(sbm_ctx* ctx);
+
+/* Host <-> device copies of a field.  `haloed` = 1: h has the halo-padded
+ * shape (ny+2)(nx+2)(nz+2); 0: interior shape ny*nx*nz (ghosts untouched). */
+int sbm_upload(sbm_ctx* ctx, int field, const double* h, int haloed);
+int sbm_download(sbm_ctx* ctx, int field, double* h, int haloed);
+/* Raw device pointer of a field (halo-padded FP64), for device-resident use. */
+int sbm_field_ptr(sbm_ctx* ctx, int field, double** dptr);
+
+/* Domain set-up, SBMES:154-168 + :173-176 + :247-262 + :273-291 +
+ * :297-341: psi from two REAL(4) distance fields (interior shape), clamp,
+ * edge ghosts, the 1e-7 / 1e-6 floors, AvP/AvPx, tPP/tPE, initial
+ * concentrations and potentials, Kap, Xrf and the target current
+ * (rate `cr`, SBMES:109, :341).  zeta: SBMES:94. */
+int sbm_setup_domain(sbm_ctx* ctx, const float* dist_p, const float* dist_e,
+                     double zeta, double cnp0, double cne0, double cr,
+                     sbm_scalars* s);
+
+/* CG solve on device-resident fields (SBMES:492-555, :647-714, :729-795).
+ * op: SBM_OP_*.  For CNE/PHP/PHE the right-hand side is the context's
+ * internal RHS buffer filled by the step routines; GENERIC uses
+ * SBM_F_RHS, SBM_F_X, SBM_F_COEF and SBM_F_WEIGHT with x-face ghost rules
+ * bc_x0 / bc_x1 and operator scale `scale` (q = scale * div(K grad p)).
+ * precision: SBM_PREC_*; precond: SBM_PC_*.  `iters` receives the number
+ * of CG iterations executed (inner iterations for MIXED); `final_res`
+ * the last value of the stopping norm; `ms` the device time. */
+int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale,
+                 double tol, int max_it, int stop_rule, int precision,
+                 int precond, int* iters, double* final_res, float* ms);
+
+/* One electrochemical time step, the body of the reference's time loop
+ * (SBMES:397-840) for a given dt, voltage-scan rate vsr and step index
+ * iter: Cahn-Hilliard, CnE implicit solve with the flux BC and mean
+ * correction, Dab/pce/pcN, tables, Butler-Volmer Picard loop with the phP
+ * and phE solves, current sum and voltage control. */
+int sbm_time_step(sbm_ctx* ctx, int iter, double dt, double vsr,
+                  int precision, sbm_scalars* s);
+
+/* Stages of the same step, callable one at a time. */
+int sbm_ch_step(sbm_ctx* ctx, double dt, sbm_scalars* s);            /* SBMES:397-443 */
+int sbm_cne_step(sbm_ctx* ctx, int iter, double dt, int precision,
+                 sbm_scalars* s);                                     /* SBMES:461-572 */
+int sbm_bv_update(sbm_ctx* ctx, int precision, sbm_scalars* s);      /* SBMES:577-812 */
+int sbm_voltage_step(sbm_ctx* ctx, double dt, double vsr,
+                     sbm_scalars* s);                                 /* SBMES:826-835 */
+
+/* ---------------------------------------------------- stateless kernels
+ * These take HOST arrays, copy to the device, run, and copy back, so a
+ * Fortran host can swap them in for the named subroutines one for one. */
+
+/* Tbl_Chk_Pln_3DA(py,px,pz,sz,Cord,Vals,Cn,fn), SBMES:987-1028.
+ * n = py*px*pz voxels. */
+int sbm_table_lookup(int64_t n, int sz, const double* cord, const double* vals,
+                     const double* cn, double* fn);
+
+/* ReDist3D_XYZ(lit,py,px,pz,sg,f), LevelSet_3D.f90:194-261 (dt = 1.0d-1)
+ * and RM_UCNCT_3D.f90:209-276 (dt = 1.0e-1 REAL(4)): in place on f,
+ * halo-padded.  Bit-exact with the reference arithmetic. */
+int sbm_redist(int lit, int py, int px, int pz, double dt,
+               const double* sg, double* f);
+
+/* One phase of the AccDiff_3D connectivity sweep, AccDiff_3D.f90:111-169
+ * (solid, dirichlet_x = 1: Dirichlet 1 at x = px+1) and :185-243
+ * (electrolyte, dirichlet_x = 0: Dirichlet 1 at x = 0), for iterations
+ * 2..term.  psi and cn halo-padded; cn in/out.  Bit-exact. */
+int sbm_accdiff(int py, int px, int pz, const double* psi, double* cn,
+                int term, int dirichlet_x);
+
+/* RM_UCNCT_3D.f90:78-82 / :127-130: psB = psA, psB = 0 where Cn < 1e-4
+ * (REAL(4) literal).  n voxels, bit-exact. */
+int sbm_rm_mask(int64_t n, const double* psA, const double* cn, double* psB);
+
+/* Sign function, LevelSet_3D.f90:140-144 / RM_UCNCT_3D.f90:92-96:
+ * sg = 1 where ds > thr else -1; n values (halo-padded array). */
+int sbm_sign(int64_t n, const double* ds, double thr, double* sg);
+
+/* Text of the last CUDA error seen by this thread. */
+const char* sbm_last_error(void);
+/* Version string of the compiled library. */
+const char* sbm_version(void);
+/* Number of kernel launches this process has issued through the library. */
+int64_t sbm_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SBM_CAPI_H */
