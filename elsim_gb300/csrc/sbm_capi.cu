@@ -59,12 +59,12 @@ int ensure_fp32_work(sbm_ctx* ctx) {
   float** bufs[] = {&ctx->hk32, &ctx->dg32, &ctx->r32, &ctx->p32,
                     &ctx->q32,  &ctx->x32,  &ctx->z32, &ctx->rold32};
   for (float** b : bufs) {
-    cudaError_t e = cudaMalloc(b, sizeof(float) * (size_t)ctx->g.nh);
+    cudaError_t e = cudaMalloc(b, sizeof(float) * (size_t)ctx->g32.nh);
     if (e != cudaSuccess) {
       set_error("cudaMalloc fp32", e);
       return SBM_ERR_NOMEM;
     }
-    if (cudaMemset(*b, 0, sizeof(float) * (size_t)ctx->g.nh) != cudaSuccess) return SBM_ERR_CUDA;
+    if (cudaMemset(*b, 0, sizeof(float) * (size_t)ctx->g32.nh) != cudaSuccess) return SBM_ERR_CUDA;
   }
   return SBM_OK;
 }
@@ -138,6 +138,7 @@ int sbm_ctx_create(int ny, int nx, int nz, const sbm_params* p, sbm_ctx** out) {
   sbm_ctx* ctx = new (std::nothrow) sbm_ctx();
   if (!ctx) return SBM_ERR_NOMEM;
   ctx->g = make_geo(ny, nx, nz);
+  ctx->g32 = make_geo32(ny, nx, nz);
   if (p) ctx->p = *p;
   else sbm_params_reference(&ctx->p);
   int rc = SBM_OK;

@@ -45,6 +45,24 @@ inline Geo make_geo(int ny, int nx, int nz) {
   return g;
 }
 
+// Internal FP32 layout of the mixed-precision solver: rows padded to a
+// multiple of 4 floats and shifted by kOff32 elements, so the first
+// interior element (i = 1) of every row is 16-byte aligned and a row of
+// ny (a multiple of 4) interior values is read with float4 loads.  Kernels
+// get `buffer + kOff32` as base and index it like the Fortran layout with
+// these strides; nh counts the floats to allocate (including the shift).
+constexpr int kOff32 = 3;
+inline Geo make_geo32(int ny, int nx, int nz) {
+  Geo g;
+  g.ny = ny;
+  g.nx = nx;
+  g.nz = nz;
+  g.sx = ((int64_t)ny + 2 + kOff32 + 3) / 4 * 4;
+  g.sz = g.sx * (nx + 2);
+  g.nh = g.sz * (nz + 2) + 4;
+  return g;
+}
+
 // ------------------------------------------------------- launch shape
 // Stencil-family kernels map threadIdx.x to y (the contiguous axis) and
 // threadIdx.y to x; each thread marches `zc` planes in z and keeps the
@@ -85,11 +103,17 @@ struct CgState {
   double rms;     // value of the stopping norm after the last iteration
   double tol;
   double wsum;    // sum of the stopping weight (tPP / tPE)
+  double maxrr;   // mixed: largest FP32 r.r since the last reliable update
+  double delta2;  // mixed: reliable update when r.r < delta2 * maxrr
   double aux[4];
   int iter;
   int max_it;
   int done;       // 0 running, 1 converged, 2 iteration cap, 3 non-finite, 4 breakdown
   int stop_rule;
+  int reliable;       // mixed: recompute the FP64 residual in this iteration
+  int accum_pending;  // mixed: fold the FP32 correction into the FP64 one
+  int initial;        // mixed: first residual of the solve (beta = 0)
+  int n_reliable;     // mixed: number of FP64 residual replacements
   unsigned int counter[8];
 };
 
@@ -232,6 +256,7 @@ struct SolveResult {
 
 struct sbm_ctx {
   sbm::Geo g;
+  sbm::Geo g32;  // internal FP32 layout of the mixed-precision solver
   sbm_params p;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evq[2] = {nullptr, nullptr};

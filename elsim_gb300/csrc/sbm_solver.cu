@@ -16,10 +16,11 @@
 //
 // Two precisions:
 //   FP64  the drop-in: the reference's CG and stopping rules.
-//   MIXED FP32 inner CG (FP32 stencil, FP32 vectors, per-thread FP32 partial
-//         sums promoted to FP64 for the grid reduction) inside an FP64
-//         iterative-refinement loop whose residual r = r0 - A d is always
-//         recomputed in FP64.
+//   MIXED FP32 CG (FP32 stencil and vectors on a 16-byte-aligned internal
+//         layout, per-thread FP32 partial sums promoted to FP64 for the grid
+//         reduction) with FP64 iterative refinement by reliable updates: the
+//         residual is periodically recomputed in FP64 and the correction
+//         accumulated in FP64, without restarting the Krylov space.
 #include <cmath>
 #include <cstring>
 
@@ -272,65 +273,6 @@ __global__ void __launch_bounds__(BX* BY)
   }
 }
 
-// Iterative refinement step: r = r0 - A_h d64 in FP64 (ghost rules on d64),
-// rr = r.r and the outer stopping test; then start the inner FP32 solve:
-// r32 = (float)r, x32 = 0, p32 = z32 (Jacobi) or r32, inner rho/rr/rr0.
-template <int FORM, bool PC>
-__global__ void __launch_bounds__(BX* BY)
-    k_ir_resid(OpArgs<double> op, int zc, const double* __restrict__ d64,
-               const double* __restrict__ r0, float* __restrict__ r32, float* __restrict__ p32,
-               float* __restrict__ x32, const float* __restrict__ invd32, double* partials,
-               CgState* st, CgState* st32, int max_outer) {
-  const Geo g = op.g;
-  SBM_COLUMN_PROLOGUE(g, zc)
-  double a_rr = 0.0, a_r32 = 0.0, a_rz32 = 0.0;
-  if (active && k0 <= k1) {
-    int64_t c = g.ix(i, j, k0);
-    double pc = d64[c], kc = op.hk[c];
-    double pzm = d64[c - g.sz], kzm = op.hk[c - g.sz];
-    if (k0 == 1) pzm = pc;
-    for (int k = k0; k <= k1; ++k) {
-      const double pzp_raw = d64[c + g.sz], kzp = op.hk[c + g.sz];
-      const double pzp = (k == g.nz) ? pc : pzp_raw;
-      const double s = stencil_at<double, true>(g, op.hk, d64, c, i, j, pc, kc, pzm, pzp, kzm,
-                                                kzp, op.bcx0, op.bcx1);
-      const double ad = (FORM == 0) ? op.scale * s : op.diag[c] * pc - op.scale * s;
-      const double rv = r0[c] - ad;
-      a_rr += rv * rv;
-      const float rf = (float)rv;
-      r32[c] = rf;
-      x32[c] = 0.0f;
-      const float zf = PC ? invd32[c] * rf : rf;
-      p32[c] = zf;
-      a_r32 += (double)rf * (double)rf;
-      a_rz32 += (double)rf * (double)zf;
-      pzm = pc;
-      kzm = kc;
-      pc = pzp_raw;
-      kc = kzp;
-      c += g.sz;
-    }
-  }
-  double v[3] = {a_rr, a_r32, a_rz32}, tot[3];
-  if (grid_reduce<3>(v, partials, &st->counter[3], tot)) {
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-      st->rr = tot[0];
-      const double rms = sqrt(tot[0]) / sqrt(st->rr0);
-      st->rms = rms;
-      if (!isfinite(rms)) st->done = 3;
-      else if (!(rms > st->tol) || st->rr0 == 0.0) st->done = 1;
-      else if (st->iter >= max_outer) st->done = 2;
-      st->iter = st->iter + 1;
-      st32->rr = tot[1];
-      st32->rr0 = tot[1];
-      st32->rho = tot[2];
-      st32->iter = 0;
-      st32->rms = 1.0;
-      st32->done = (tot[1] == 0.0 || st->done) ? 1 : 0;
-    }
-  }
-}
-
 template <typename T>
 __global__ void k_accum(Geo g, int zc, double* __restrict__ acc, const T* __restrict__ v) {
   SBM_COLUMN_PROLOGUE(g, zc)
@@ -422,11 +364,11 @@ int chunk_len(const sbm_ctx* ctx) {
   return 32;
 }
 
-// Captures (once) and returns a graph of `len` iterations.
-template <typename T>
-int get_graph(sbm_ctx* ctx, const std::string& key, const OpArgs<T>& op, const Shape& sh,
-              int stop, bool pc, T* x, T* p, T* r, T* q, const double* w, const T* invd,
-              CgState* st, cudaGraphExec_t* exec, int* nodes) {
+// Captures (once per key) a graph of chunk_len(ctx) iterations, each
+// issued by body(stream), and returns it with its kernel-node count.
+template <typename Body>
+int capture_graph(sbm_ctx* ctx, const std::string& key, int nodes_per_iter, Body&& body,
+                  cudaGraphExec_t* exec, int* nodes) {
   auto it = ctx->graphs.find(key);
   if (it != ctx->graphs.end()) {
     *exec = it->second.first;
@@ -436,8 +378,7 @@ int get_graph(sbm_ctx* ctx, const std::string& key, const OpArgs<T>& op, const S
   const int len = chunk_len(ctx);
   cudaGraph_t graph = nullptr;
   SBM_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  for (int c = 0; c < len; ++c)
-    launch_iteration<T>(op, sh, stop, pc, x, p, r, q, w, invd, ctx->partials, st, ctx->stream);
+  for (int c = 0; c < len; ++c) body(ctx->stream);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
   if (e != cudaSuccess) {
     set_error("cudaStreamEndCapture", e);
@@ -456,9 +397,9 @@ int get_graph(sbm_ctx* ctx, const std::string& key, const OpArgs<T>& op, const S
     set_error("cudaGraphInstantiate", e);
     return SBM_ERR_CUDA;
   }
-  ctx->graphs[key] = {ex, 3 * len};
+  ctx->graphs[key] = {ex, nodes_per_iter * len};
   *exec = ex;
-  *nodes = 3 * len;
+  *nodes = nodes_per_iter * len;
   return SBM_OK;
 }
 
@@ -548,8 +489,13 @@ int solve_fp64(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
              sp.form, sp.bcx0, sp.bcx1, sp.stop_rule, pc, sh.zc, chunk_len(ctx));
   cudaGraphExec_t ex = nullptr;
   int nodes = 0;
-  int rc = get_graph<double>(ctx, key, op, sh, sp.stop_rule, pc, sp.x, ctx->p64, ctx->r64,
-                             ctx->q64, sp.w, invd, ctx->st, &ex, &nodes);
+  int rc = capture_graph(
+      ctx, key, 3,
+      [&](cudaStream_t s2) {
+        launch_iteration<double>(op, sh, sp.stop_rule, pc, sp.x, ctx->p64, ctx->r64, ctx->q64,
+                                 sp.w, invd, ctx->partials, ctx->st, s2);
+      },
+      &ex, &nodes);
   if (rc) return rc;
   CgState fin;
   rc = run_chunks(ctx, ex, nodes, ctx->st, ctx->h_st, &fin);
@@ -566,101 +512,446 @@ int solve_fp64(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   return SBM_OK;
 }
 
+}  // namespace
+
+// =================================================================== MIXED
+// FP32 CG with FP64 iterative refinement by reliable updates (residual
+// replacement).  The FP32 iteration runs on an internal 16-byte-aligned
+// layout (make_geo32); every time the FP32 recursive residual has dropped
+// by delta^2 since the last replacement -- and whenever it claims
+// convergence or the cap is reached -- the true residual
+//     r = r0 - A (d64 + x32)
+// is recomputed in FP64 from the FP64 correction d64 and the FP32 partial
+// correction x32, converted to FP32 and substituted for the recursive
+// residual; x32 is then folded into d64.  The FP32 search direction is kept
+// across replacements, so the Krylov space is not restarted (unlike
+// restarted iterative refinement).  Convergence is decided only on the FP64
+// true residual: on return ||b - A x||_2 / ||b - A x0||_2 <= tol.
+
+namespace {
+
+__device__ __forceinline__ float4 ld4(const float* p) {
+  return *reinterpret_cast<const float4*>(p);
+}
+__device__ __forceinline__ void st4(float* p, const float4& v) {
+  *reinterpret_cast<float4*>(p) = v;
+}
+
+// q = A p on the FP32 layout, four y-consecutive voxels per thread (float4),
+// threads flattened over (y-chunk, x-row) so warps never idle on short rows;
+// y-neighbours come from the adjacent lanes by shuffle, x- and
+// z-neighbours by float4 loads (z kept in registers while marching).
+template <int FORM, bool DOT>
+__global__ void __launch_bounds__(256)
+    k32v_apply(OpArgs<float> op, int nchunk, int zc, const float* __restrict__ p,
+               float* __restrict__ q, double* partials, CgState* st) {
+  if (DOT && st->done) return;
+  const Geo g = op.g;
+  const unsigned FULL = 0xffffffffu;
+  const int64_t rows = (int64_t)nchunk * g.nx;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = t < rows;
+  const int64_t tt = active ? t : rows - 1;
+  const int lane = threadIdx.x & 31;
+  const int chunk = (int)(tt % nchunk);
+  const int j = (int)(tt / nchunk) + 1;
+  const int k0 = blockIdx.y * zc + 1;
+  const int k1 = min(k0 + zc - 1, g.nz);
+  const bool lin = (lane > 0) && (chunk > 0);
+  const bool rin = (lane < 31) && (chunk < nchunk - 1) && (t + 1 < rows);
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  int64_t c = g.ix(4 * chunk + 1, j, k0);
+  float4 pc = ld4(p + c), kc = ld4(op.hk + c);
+  float4 pzm = ld4(p + c - g.sz), kzm = ld4(op.hk + c - g.sz);
+  if (k0 == 1) pzm = pc;
+  float acc = 0.f;
+  for (int k = k0; k <= k1; ++k) {
+    const float4 pzp_raw = ld4(p + c + g.sz), kzp = ld4(op.hk + c + g.sz);
+    const float4 pzp = (k == g.nz) ? pc : pzp_raw;
+    float4 pxm = ld4(p + c - g.sx), pxp = ld4(p + c + g.sx);
+    const float4 kxm = ld4(op.hk + c - g.sx), kxp = ld4(op.hk + c + g.sx);
+    if (j == 1) pxm = op.bcx0 ? zero4 : pc;
+    if (j == g.nx) pxp = op.bcx1 ? zero4 : pc;
+    float pl = __shfl_up_sync(FULL, pc.w, 1), kl = __shfl_up_sync(FULL, kc.w, 1);
+    float pr = __shfl_down_sync(FULL, pc.x, 1), kr = __shfl_down_sync(FULL, kc.x, 1);
+    if (!lin) {
+      kl = op.hk[c - 1];
+      pl = (chunk == 0) ? pc.x : p[c - 1];
+    }
+    if (!rin) {
+      kr = op.hk[c + 4];
+      pr = (chunk == nchunk - 1) ? pc.w : p[c + 4];
+    }
+    const float pa[6] = {pl, pc.x, pc.y, pc.z, pc.w, pr};
+    const float ka[6] = {kl, kc.x, kc.y, kc.z, kc.w, kr};
+    const float pxa[4] = {pxm.x, pxm.y, pxm.z, pxm.w}, pxb[4] = {pxp.x, pxp.y, pxp.z, pxp.w};
+    const float kxa[4] = {kxm.x, kxm.y, kxm.z, kxm.w}, kxb[4] = {kxp.x, kxp.y, kxp.z, kxp.w};
+    const float pza[4] = {pzm.x, pzm.y, pzm.z, pzm.w}, pzb[4] = {pzp.x, pzp.y, pzp.z, pzp.w};
+    const float kza[4] = {kzm.x, kzm.y, kzm.z, kzm.w}, kzb[4] = {kzp.x, kzp.y, kzp.z, kzp.w};
+    float dg[4] = {0.f, 0.f, 0.f, 0.f};
+    if (FORM == 1) {
+      const float4 d4 = ld4(op.diag + c);
+      dg[0] = d4.x; dg[1] = d4.y; dg[2] = d4.z; dg[3] = d4.w;
+    }
+    float qa[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float s = face_sum<float>(ka[e + 1], pa[e + 1], ka[e + 2], pa[e + 2], ka[e], pa[e],
+                                      kxb[e], pxb[e], kxa[e], pxa[e], kzb[e], pzb[e], kza[e],
+                                      pza[e]);
+      qa[e] = (FORM == 0) ? op.scale * s : dg[e] * pa[e + 1] - op.scale * s;
+    }
+    if (active) {
+      st4(q + c, make_float4(qa[0], qa[1], qa[2], qa[3]));
+      if (DOT) acc += (pa[1] * qa[0] + pa[2] * qa[1]) + (pa[3] * qa[2] + pa[4] * qa[3]);
+    }
+    pzm = pc;
+    kzm = kc;
+    pc = pzp_raw;
+    kc = kzp;
+    c += g.sz;
+  }
+  if (DOT) {
+    double v[1] = {(double)acc}, tot[1];
+    if (grid_reduce<1>(v, partials, &st->counter[0], tot)) {
+      if (threadIdx.x == 0) {
+        const double pq = tot[0];
+        st->pq = pq;
+        st->alpha = st->rho / pq;
+        if (pq == 0.0) st->done = 4;
+        else if (!isfinite(pq)) st->done = 3;
+      }
+    }
+  }
+}
+
+// Interior work item u -> index of its first voxel on layout g (VEC voxels
+// along y per item).
+template <int VEC>
+__device__ __forceinline__ int64_t item_ix(const Geo& g, int nchunk, int64_t u, int* pi, int* pj,
+                                           int* pk) {
+  const int chunk = (int)(u % nchunk);
+  const int64_t r = u / nchunk;
+  const int j = (int)(r % g.nx) + 1;
+  const int k = (int)(r / g.nx) + 1;
+  *pi = VEC * chunk + 1;
+  *pj = j;
+  *pk = k;
+  return g.ix(*pi, j, k);
+}
+
+// x32 += alpha p; r32 -= alpha q; r.r and r.z (FP32 per thread, FP64 across
+// threads); decides whether the next step is a reliable update.
+template <bool PC, int VEC>
+__global__ void __launch_bounds__(256)
+    k32_update(Geo g, int nchunk, float* __restrict__ x, const float* __restrict__ p,
+               float* __restrict__ r, const float* __restrict__ q, const float* __restrict__ invd,
+               double* partials, CgState* st) {
+  if (st->done) return;
+  const float alpha = (float)st->alpha;
+  const int64_t n = (int64_t)nchunk * g.nx * g.nz;
+  float a_rr = 0.f, a_rz = 0.f;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const int64_t c = item_ix<VEC>(g, nchunk, u, &i, &j, &k);
+    if (VEC == 4) {
+      float4 xv = ld4(x + c), pv = ld4(p + c), rv = ld4(r + c), qv = ld4(q + c);
+      xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+      rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
+      st4(x + c, xv);
+      st4(r + c, rv);
+      a_rr += (rv.x * rv.x + rv.y * rv.y) + (rv.z * rv.z + rv.w * rv.w);
+      if (PC) {
+        const float4 d = ld4(invd + c);
+        a_rz += (rv.x * (d.x * rv.x) + rv.y * (d.y * rv.y)) +
+                (rv.z * (d.z * rv.z) + rv.w * (d.w * rv.w));
+      }
+    } else {
+      x[c] += alpha * p[c];
+      const float rn = r[c] - alpha * q[c];
+      r[c] = rn;
+      a_rr += rn * rn;
+      if (PC) a_rz += rn * (invd[c] * rn);
+    }
+  }
+  double v[2] = {(double)a_rr, PC ? (double)a_rz : (double)a_rr}, tot[2];
+  if (grid_reduce<2>(v, partials, &st->counter[1], tot)) {
+    if (threadIdx.x == 0) {
+      const double rr_new = tot[0], rho_new = tot[1];
+      const int it = st->iter + 1;
+      st->iter = it;
+      if (!isfinite(rho_new) || !isfinite(st->alpha)) {
+        st->done = 3;
+      } else {
+        const double maxrr = fmax(st->maxrr, rr_new);
+        const bool trig = (rr_new < st->delta2 * maxrr) ||
+                          (rr_new <= st->tol * st->tol * st->aux[0]) || (it >= st->max_it);
+        if (trig) {
+          st->reliable = 1;
+        } else {
+          st->beta = rho_new / st->rho;
+          st->rho = rho_new;
+        }
+        st->rr = rr_new;
+        st->maxrr = maxrr;
+      }
+    }
+  }
+}
+
+// Reliable update: r = r0 - A_h (d64 + x32) in FP64 (ghost rules of the
+// search direction on the correction), r32 = (float) r, z = invd*r32;
+// convergence on the FP64 norm, new rho / beta.  No-op unless flagged.
+template <int FORM, bool PC>
+__global__ void __launch_bounds__(BX* BY)
+    k_rel_resid(OpArgs<double> op, Geo g32, int zc, const double* __restrict__ d64,
+                const float* __restrict__ x32, const double* __restrict__ r0,
+                float* __restrict__ r32, const float* __restrict__ invd32, double* partials,
+                CgState* st) {
+  if (!st->reliable || st->done) return;
+  const Geo g = op.g;
+  SBM_COLUMN_PROLOGUE(g, zc)
+  double a_rr = 0.0, a_r32 = 0.0, a_rz = 0.0;
+  if (active && k0 <= k1) {
+    for (int k = k0; k <= k1; ++k) {
+      const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
+#define V(o64, o32) (d64[c + (o64)] + (double)x32[c3 + (o32)])
+      const double pc = V(0, 0);
+      const double pym = (i == 1) ? pc : V(-1, -1);
+      const double pyp = (i == g.ny) ? pc : V(1, 1);
+      const double pxm = (j == 1) ? (op.bcx0 ? 0.0 : pc) : V(-g.sx, -g32.sx);
+      const double pxp = (j == g.nx) ? (op.bcx1 ? 0.0 : pc) : V(g.sx, g32.sx);
+      const double pzm = (k == 1) ? pc : V(-g.sz, -g32.sz);
+      const double pzp = (k == g.nz) ? pc : V(g.sz, g32.sz);
+#undef V
+      const double* hk = op.hk;
+      const double s = face_sum<double>(hk[c], pc, hk[c + 1], pyp, hk[c - 1], pym, hk[c + g.sx],
+                                        pxp, hk[c - g.sx], pxm, hk[c + g.sz], pzp, hk[c - g.sz],
+                                        pzm);
+      const double ad = (FORM == 0) ? op.scale * s : op.diag[c] * pc - op.scale * s;
+      const double rv = r0[c] - ad;
+      const float rf = (float)rv;
+      r32[c3] = rf;
+      const float zf = PC ? invd32[c3] * rf : rf;
+      a_rr += rv * rv;
+      a_r32 += (double)rf * (double)rf;
+      a_rz += (double)rf * (double)zf;
+    }
+  }
+  double v[3] = {a_rr, a_r32, a_rz}, tot[3];
+  if (grid_reduce<3>(v, partials, &st->counter[3], tot)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      const double rms = (st->rr0 > 0.0) ? sqrt(tot[0] / st->rr0) : 0.0;
+      st->rms = rms;
+      st->n_reliable += 1;
+      if (!isfinite(rms)) st->done = 3;
+      else if (!(rms > st->tol)) st->done = 1;
+      else if (st->iter >= st->max_it) st->done = 2;
+      st->beta = st->initial ? 0.0 : tot[2] / st->rho;
+      if (st->initial) st->aux[0] = tot[1];
+      st->rho = tot[2];
+      st->rr = tot[1];
+      st->maxrr = tot[1];
+      st->initial = 0;
+      st->reliable = 0;
+      st->accum_pending = 1;
+    }
+  }
+}
+
+// After a reliable update d64 += x32, x32 = 0 (the last block clears the
+// flag); then, unless done, p = z + beta p.
+template <bool PC, int VEC>
+__global__ void __launch_bounds__(256)
+    k32_direction(Geo g, Geo g64, int nchunk, const float* __restrict__ r, float* __restrict__ p,
+                  const float* __restrict__ invd, float* __restrict__ x32,
+                  double* __restrict__ d64, CgState* st) {
+  const bool acc = st->accum_pending != 0;
+  const bool done = st->done != 0;
+  if (!acc && done) return;
+  const float beta = (float)st->beta;
+  const int64_t n = (int64_t)nchunk * g.nx * g.nz;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const int64_t c = item_ix<VEC>(g, nchunk, u, &i, &j, &k);
+    if (acc) {
+      const int64_t c64 = g64.ix(i, j, k);
+#pragma unroll
+      for (int e = 0; e < VEC; ++e) {
+        d64[c64 + e] += (double)x32[c + e];
+        x32[c + e] = 0.f;
+      }
+    }
+    if (!done) {
+      if (VEC == 4) {
+        const float4 rv = ld4(r + c);
+        float4 pv = ld4(p + c);
+        float4 z = rv;
+        if (PC) {
+          const float4 d = ld4(invd + c);
+          z = make_float4(d.x * rv.x, d.y * rv.y, d.z * rv.z, d.w * rv.w);
+        }
+        pv = make_float4(z.x + beta * pv.x, z.y + beta * pv.y, z.z + beta * pv.z,
+                         z.w + beta * pv.w);
+        st4(p + c, pv);
+      } else {
+        const float z = PC ? invd[c] * r[c] : r[c];
+        p[c] = z + beta * p[c];
+      }
+    }
+  }
+  if (acc) {
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last = atomicAdd(&st->counter[4], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+      st->accum_pending = 0;
+      st->counter[4] = 0u;
+    }
+  }
+}
+
+// hk32/dg32 = (float) hk64/diag64 over the padded domain, FP64 layout ->
+// FP32 layout.
+__global__ void k_to32(Geo g64, Geo g32, const double* __restrict__ hk, float* __restrict__ hk32,
+                       const double* __restrict__ dg, float* __restrict__ dg32) {
+  const int64_t n = g64.nh;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g64.sx);
+    const int64_t rr = c / g64.sx;
+    const int j = (int)(rr % (g64.nx + 2));
+    const int k = (int)(rr / (g64.nx + 2));
+    const int64_t c3 = g32.ix(i, j, k);
+    hk32[c3] = (float)hk[c];
+    if (dg) dg32[c3] = (float)dg[c];
+  }
+}
+
+int flat_blocks(int64_t items) {
+  int64_t b = (items + 256 * 8 - 1) / (256 * 8);
+  if (b < 1) b = 1;
+  if (b > 152 * 16) b = 152 * 16;
+  return (int)b;
+}
+
+}  // namespace
+
 int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   if (sp.stop_rule != SBM_STOP_REL_RES) return SBM_ERR_ARG;
   int rc = ensure_fp32_work(ctx);
   if (rc) return rc;
   const Geo& g = ctx->g;
+  const Geo& g32 = ctx->g32;
   cudaStream_t s = ctx->stream;
   const Shape sh64 = stencil_shape(g, pick_zc(g, ctx->zc64));
-  const Shape sh32 = stencil_shape(g, pick_zc(g, ctx->zc32));
+  const int vec = (g.ny % 4 == 0) ? 4 : 1;
+  const int nchunk = g.ny / vec;
+  const int zc32 = ctx->zc32 > 0 ? ctx->zc32 : 8;
+  const Shape sh32 = stencil_shape(g32, pick_zc(g32, ctx->zc32));
+  float* const hk32 = ctx->hk32 + kOff32;
+  float* const dg32 = ctx->dg32 + kOff32;
+  float* const r32 = ctx->r32 + kOff32;
+  float* const p32 = ctx->p32 + kOff32;
+  float* const q32 = ctx->q32 + kOff32;
+  float* const x32 = ctx->x32 + kOff32;
+  float* const iv32 = ctx->z32 + kOff32;
   OpArgs<double> op64{g, sp.hk64, sp.diag64, sp.scale, sp.form, sp.bcx0, sp.bcx1};
-  OpArgs<float> op32{g, ctx->hk32, sp.form ? ctx->dg32 : nullptr, (float)sp.scale, sp.form,
-                     sp.bcx0, sp.bcx1};
+  OpArgs<float> op32{g32, hk32, sp.form ? dg32 : nullptr, (float)sp.scale, sp.form, sp.bcx0,
+                     sp.bcx1};
   const bool pc = sp.precond == SBM_PC_JACOBI;
-  const int max_outer = 40;
-  const double inner_tol = ctx->inner_tol > 0 ? ctx->inner_tol : 2e-5;
+  const double delta = ctx->inner_tol > 0 ? ctx->inner_tol : 0.1;
   CgState* h = &ctx->h_st[2];
   memset(h, 0, sizeof(CgState));
   h->tol = sp.tol;
-  h->max_it = max_outer;
+  h->max_it = sp.max_it;
   h->stop_rule = SBM_STOP_REL_RES;
-  CgState* h32 = &ctx->h_st[3];
-  memset(h32, 0, sizeof(CgState));
-  h32->tol = inner_tol;
-  h32->max_it = ctx->inner_max > 0 ? ctx->inner_max : sp.max_it;
-  h32->stop_rule = SBM_STOP_REL_RES;
+  h->delta2 = delta * delta;
+  h->reliable = 1;
+  h->initial = 1;
   SBM_CUDA_TRY(cudaEventRecord(ctx->ev0, s));
   SBM_CUDA_TRY(cudaMemcpyAsync(ctx->st, h, sizeof(CgState), cudaMemcpyHostToDevice, s));
-  SBM_CUDA_TRY(cudaMemcpyAsync(ctx->st32, h32, sizeof(CgState), cudaMemcpyHostToDevice, s));
-  // FP32 copies of the operator
-  k_to_f32<<<flat_grid(g.nh), 256, 0, s>>>(g.nh, sp.hk64, ctx->hk32, sp.form ? sp.diag64 : nullptr,
-                                           ctx->dg32);
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->d64, 0, sizeof(double) * g.nh, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->x32, 0, sizeof(float) * g32.nh, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->p32, 0, sizeof(float) * g32.nh, s));
+  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
+                                         dg32);
   SBM_LAUNCHED(1);
-  float* invd32 = ctx->z32;
   if (pc) {
-    k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, invd32);
+    k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
     SBM_LAUNCHED(1);
   }
-  // r0 = b - A x (FP64, stored ghosts); the outer state's rr0.
+  // r0 = b - A x0 with x0's stored ghosts (FP64); sets rr0.
   if (sp.form == 0)
-    k_residual_mem<0, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x, ctx->r0,
-                                                              ctx->p64, nullptr, ctx->partials,
-                                                              ctx->st);
+    k_residual_mem<0, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x,
+                                                              ctx->r0, ctx->p64, nullptr,
+                                                              ctx->partials, ctx->st);
   else
-    k_residual_mem<1, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x, ctx->r0,
-                                                              ctx->p64, nullptr, ctx->partials,
-                                                              ctx->st);
+    k_residual_mem<1, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x,
+                                                              ctx->r0, ctx->p64, nullptr,
+                                                              ctx->partials, ctx->st);
   SBM_LAUNCHED(1);
-  SBM_CUDA_TRY(cudaMemsetAsync(ctx->d64, 0, sizeof(double) * g.nh, s));
+  const int64_t items = (int64_t)nchunk * g.nx * g.nz;
+  const dim3 fgrid(flat_blocks(items));
+  const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
+  auto rel = [&](cudaStream_t s2) {
+#define SBM_REL(F, P)                                                                          \
+  k_rel_resid<F, P><<<sh64.grid, sh64.block, 0, s2>>>(op64, g32, sh64.zc, ctx->d64, x32,      \
+                                                       ctx->r0, r32, iv32, ctx->partials,      \
+                                                       ctx->st)
+    if (sp.form == 0) {
+      if (pc) SBM_REL(0, true); else SBM_REL(0, false);
+    } else {
+      if (pc) SBM_REL(1, true); else SBM_REL(1, false);
+    }
+#undef SBM_REL
+  };
+  auto dir = [&](cudaStream_t s2) {
+    if (vec == 4) {
+      if (pc) k32_direction<true, 4><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, r32, p32, iv32, x32, ctx->d64, ctx->st);
+      else k32_direction<false, 4><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, r32, p32, iv32, x32, ctx->d64, ctx->st);
+    } else {
+      if (pc) k32_direction<true, 1><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, r32, p32, iv32, x32, ctx->d64, ctx->st);
+      else k32_direction<false, 1><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, r32, p32, iv32, x32, ctx->d64, ctx->st);
+    }
+  };
+  auto body = [&](cudaStream_t s2) {
+    if (vec == 4) {
+      if (sp.form == 0) k32v_apply<0, true><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, p32, q32, ctx->partials, ctx->st);
+      else k32v_apply<1, true><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, p32, q32, ctx->partials, ctx->st);
+      if (pc) k32_update<true, 4><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, p32, r32, q32, iv32, ctx->partials, ctx->st);
+      else k32_update<false, 4><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, p32, r32, q32, iv32, ctx->partials, ctx->st);
+    } else {
+      if (sp.form == 0) k_apply<float, 0, true, true><<<sh32.grid, sh32.block, 0, s2>>>(op32, sh32.zc, p32, q32, ctx->partials, ctx->st);
+      else k_apply<float, 1, true, true><<<sh32.grid, sh32.block, 0, s2>>>(op32, sh32.zc, p32, q32, ctx->partials, ctx->st);
+      if (pc) k32_update<true, 1><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, p32, r32, q32, iv32, ctx->partials, ctx->st);
+      else k32_update<false, 1><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, p32, r32, q32, iv32, ctx->partials, ctx->st);
+    }
+    rel(s2);
+    dir(s2);
+  };
+  // first residual replacement (r32 = r0, beta = 0) and p = z
+  rel(s);
+  dir(s);
+  SBM_LAUNCHED(2);
   SBM_CUDA_TRY(cudaGetLastError());
   const std::string key =
-      key_of("mix32", ctx->hk32, ctx->dg32, ctx->x32, ctx->r32, ctx->p32, ctx->q32, invd32,
-             sp.scale, sp.form, sp.bcx0, sp.bcx1, SBM_STOP_REL_RES, pc, sh32.zc, chunk_len(ctx));
+      key_of("mixrel", hk32, dg32, x32, r32, p32, q32, iv32, sp.scale, sp.form, sp.bcx0,
+             sp.bcx1, vec * 16 + zc32, pc, sh64.zc, chunk_len(ctx));
   cudaGraphExec_t ex = nullptr;
   int nodes = 0;
-  rc = get_graph<float>(ctx, key, op32, sh32, SBM_STOP_REL_RES, pc, ctx->x32, ctx->p32,
-                        ctx->r32, ctx->q32, nullptr, invd32, ctx->st32, &ex, &nodes);
+  rc = capture_graph(ctx, key, 4, body, &ex, &nodes);
   if (rc) return rc;
-  int inner_total = 0, outer = 0;
-  CgState fin{}, fin32{};
-  for (;;) {
-    if (sp.form == 0) {
-      if (pc)
-        k_ir_resid<0, true><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, ctx->d64, ctx->r0,
-                                                            ctx->r32, ctx->p32, ctx->x32, invd32,
-                                                            ctx->partials, ctx->st, ctx->st32,
-                                                            max_outer);
-      else
-        k_ir_resid<0, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, ctx->d64, ctx->r0,
-                                                             ctx->r32, ctx->p32, ctx->x32, invd32,
-                                                             ctx->partials, ctx->st, ctx->st32,
-                                                             max_outer);
-    } else {
-      if (pc)
-        k_ir_resid<1, true><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, ctx->d64, ctx->r0,
-                                                            ctx->r32, ctx->p32, ctx->x32, invd32,
-                                                            ctx->partials, ctx->st, ctx->st32,
-                                                            max_outer);
-      else
-        k_ir_resid<1, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, ctx->d64, ctx->r0,
-                                                             ctx->r32, ctx->p32, ctx->x32, invd32,
-                                                             ctx->partials, ctx->st, ctx->st32,
-                                                             max_outer);
-    }
-    SBM_LAUNCHED(1);
-    SBM_CUDA_TRY(cudaMemcpyAsync(&ctx->h_st[0], ctx->st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
-    SBM_CUDA_TRY(cudaStreamSynchronize(s));
-    fin = ctx->h_st[0];
-    if (fin.done) break;
-    ++outer;
-    rc = run_chunks(ctx, ex, nodes, ctx->st32, ctx->h_st, &fin32);
-    if (rc) return rc;
-    inner_total += fin32.iter;
-    k_accum<float><<<sh64.grid, sh64.block, 0, s>>>(g, sh64.zc, ctx->d64, ctx->x32);
-    SBM_LAUNCHED(1);
-  }
-  // x += d (interior): the ghosts of x keep their Dirichlet / flux data.
+  CgState fin;
+  rc = run_chunks(ctx, ex, nodes, ctx->st, ctx->h_st, &fin);
+  if (rc) return rc;
+  // x += d64 (interior): the ghosts of x keep their Dirichlet / flux data.
   k_accum<double><<<sh64.grid, sh64.block, 0, s>>>(g, sh64.zc, sp.x, ctx->d64);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
@@ -668,15 +959,14 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   SBM_CUDA_TRY(cudaEventSynchronize(ctx->ev1));
   float ms = 0.f;
   SBM_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  out->iters = inner_total;
-  out->outer = outer;
+  out->iters = fin.iter;
+  out->outer = fin.n_reliable;
   out->final_res = fin.rms;
   out->ms = ms;
   out->status = status_of(fin.done);
   return SBM_OK;
 }
 
-}  // namespace
 
 int solve(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   if (sp.precision == SBM_PREC_FP64) return solve_fp64(ctx, sp, out);

@@ -149,10 +149,11 @@ int sbm_ctx_destroy(sbm_ctx* ctx);
 int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p);
 /* Launch-shape and mixed-precision knobs (0 = built-in choice): z planes
  * per thread of the FP64 / FP32 stencil kernels, CG iterations per captured
- * graph chunk, relative tolerance and iteration cap of the inner FP32 solve.
- * No counterpart in the reference. */
-int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double inner_tol,
-                       int inner_max);
+ * graph chunk, and `delta` of the mixed solver (its FP64 residual is
+ * recomputed whenever the FP32 residual norm has fallen by this factor;
+ * default 0.1).  `reserved` must be 0.  No counterpart in the reference. */
+int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta,
+                       int reserved);
 /* The context's CUDA stream as an opaque handle (cudaStream_t). */
 int sbm_ctx_stream(sbm_ctx* ctx, void** stream);
 int sbm_ctx_sync(sbm_ctx* ctx);

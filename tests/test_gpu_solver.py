@@ -93,7 +93,9 @@ def test_cne_form_residual_rule_matches_oracle(built):
         ctx.upload("CnE", cne)
         g = ctx.cne_step(2, dt)
         o = st.cne_step(2, dt)
-        assert abs(g["it_cne"] - o["it_cne"]) <= 3, (g["it_cne"], o["it_cne"])
+        # thousands of iterations on an ill-conditioned system: tree- versus
+        # plane-ordered sums shift the stopping iteration by a fraction of a percent
+        assert abs(g["it_cne"] - o["it_cne"]) <= max(3, 0.01 * o["it_cne"]), (g["it_cne"], o["it_cne"])
         assert rel_l2(ctx.download("CnE"), st.field(sbm.F_CNE)) < 1e-10
         assert abs(g["infx"] - o["infx"]) <= 1e-12 * max(1.0, abs(o["infx"]))
 
