@@ -537,16 +537,22 @@ __device__ __forceinline__ void st4(float* p, const float4& v) {
   *reinterpret_cast<float4*>(p) = v;
 }
 
-// q = A p on the FP32 layout, four y-consecutive voxels per thread (float4),
-// threads flattened over (y-chunk, x-row) so warps never idle on short rows;
-// y-neighbours come from the adjacent lanes by shuffle, x- and
-// z-neighbours by float4 loads (z kept in registers while marching).
-template <int FORM, bool DOT>
-__global__ void __launch_bounds__(256)
-    k32v_apply(OpArgs<float> op, int nchunk, int zc, const float* __restrict__ p,
-               float* __restrict__ q, double* partials, CgState* st) {
-  if (DOT && st->done) return;
+// p_new = z + beta p_old (z = invd*r with Jacobi, else r) at the centre
+// and at the six neighbours (so p never needs a separate pass), then
+// q = A p_new and p_new.q -> alpha.  p is double-buffered (p_old read at
+// neighbours, p_new written at the centre).  Four y-consecutive voxels per
+// thread (float4), threads flattened over (y-chunk, x-row) so short rows do
+// not idle lanes; y-neighbours come from the adjacent lanes by shuffle, x-
+// and z-neighbours by float4 loads, z kept in registers while marching.
+template <int FORM, bool PC>
+__global__ void __launch_bounds__(256, 4)
+    k32v_apply_dir(OpArgs<float> op, int nchunk, int zc, const float* __restrict__ r,
+                   const float* __restrict__ pold, const float* __restrict__ invd,
+                   float* __restrict__ pnew, float* __restrict__ q, double* partials,
+                   CgState* st) {
+  if (st->done) return;
   const Geo g = op.g;
+  const float beta = (float)st->beta;
   const unsigned FULL = 0xffffffffu;
   const int64_t rows = (int64_t)nchunk * g.nx;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -560,27 +566,41 @@ __global__ void __launch_bounds__(256)
   const bool lin = (lane > 0) && (chunk > 0);
   const bool rin = (lane < 31) && (chunk < nchunk - 1) && (t + 1 < rows);
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto P4 = [&](int64_t idx) -> float4 {
+    const float4 rv = ld4(r + idx), pv = ld4(pold + idx);
+    float4 z = rv;
+    if (PC) {
+      const float4 d = ld4(invd + idx);
+      z = make_float4(d.x * rv.x, d.y * rv.y, d.z * rv.z, d.w * rv.w);
+    }
+    return make_float4(z.x + beta * pv.x, z.y + beta * pv.y, z.z + beta * pv.z,
+                       z.w + beta * pv.w);
+  };
+  auto P1 = [&](int64_t idx) -> float {
+    const float z = PC ? invd[idx] * r[idx] : r[idx];
+    return z + beta * pold[idx];
+  };
   int64_t c = g.ix(4 * chunk + 1, j, k0);
-  float4 pc = ld4(p + c), kc = ld4(op.hk + c);
-  float4 pzm = ld4(p + c - g.sz), kzm = ld4(op.hk + c - g.sz);
-  if (k0 == 1) pzm = pc;
+  float4 pc = P4(c), kc = ld4(op.hk + c);
+  float4 pzm = (k0 == 1) ? pc : P4(c - g.sz);
+  float4 kzm = ld4(op.hk + c - g.sz);
   float acc = 0.f;
   for (int k = k0; k <= k1; ++k) {
-    const float4 pzp_raw = ld4(p + c + g.sz), kzp = ld4(op.hk + c + g.sz);
-    const float4 pzp = (k == g.nz) ? pc : pzp_raw;
-    float4 pxm = ld4(p + c - g.sx), pxp = ld4(p + c + g.sx);
+    const bool top = (k == g.nz);
+    const float4 pzp = top ? pc : P4(c + g.sz);
+    const float4 kzp = ld4(op.hk + c + g.sz);
+    const float4 pxm = (j == 1) ? (op.bcx0 ? zero4 : pc) : P4(c - g.sx);
+    const float4 pxp = (j == g.nx) ? (op.bcx1 ? zero4 : pc) : P4(c + g.sx);
     const float4 kxm = ld4(op.hk + c - g.sx), kxp = ld4(op.hk + c + g.sx);
-    if (j == 1) pxm = op.bcx0 ? zero4 : pc;
-    if (j == g.nx) pxp = op.bcx1 ? zero4 : pc;
     float pl = __shfl_up_sync(FULL, pc.w, 1), kl = __shfl_up_sync(FULL, kc.w, 1);
     float pr = __shfl_down_sync(FULL, pc.x, 1), kr = __shfl_down_sync(FULL, kc.x, 1);
     if (!lin) {
       kl = op.hk[c - 1];
-      pl = (chunk == 0) ? pc.x : p[c - 1];
+      pl = (chunk == 0) ? pc.x : P1(c - 1);
     }
     if (!rin) {
       kr = op.hk[c + 4];
-      pr = (chunk == nchunk - 1) ? pc.w : p[c + 4];
+      pr = (chunk == nchunk - 1) ? pc.w : P1(c + 4);
     }
     const float pa[6] = {pl, pc.x, pc.y, pc.z, pc.w, pr};
     const float ka[6] = {kl, kc.x, kc.y, kc.z, kc.w, kr};
@@ -602,25 +622,76 @@ __global__ void __launch_bounds__(256)
       qa[e] = (FORM == 0) ? op.scale * s : dg[e] * pa[e + 1] - op.scale * s;
     }
     if (active) {
+      st4(pnew + c, pc);
       st4(q + c, make_float4(qa[0], qa[1], qa[2], qa[3]));
-      if (DOT) acc += (pa[1] * qa[0] + pa[2] * qa[1]) + (pa[3] * qa[2] + pa[4] * qa[3]);
+      acc += (pa[1] * qa[0] + pa[2] * qa[1]) + (pa[3] * qa[2] + pa[4] * qa[3]);
     }
     pzm = pc;
     kzm = kc;
-    pc = pzp_raw;
+    pc = pzp;
     kc = kzp;
     c += g.sz;
   }
-  if (DOT) {
-    double v[1] = {(double)acc}, tot[1];
-    if (grid_reduce<1>(v, partials, &st->counter[0], tot)) {
-      if (threadIdx.x == 0) {
-        const double pq = tot[0];
-        st->pq = pq;
-        st->alpha = st->rho / pq;
-        if (pq == 0.0) st->done = 4;
-        else if (!isfinite(pq)) st->done = 3;
-      }
+  double v[1] = {(double)acc}, tot[1];
+  if (grid_reduce<1>(v, partials, &st->counter[0], tot)) {
+    if (threadIdx.x == 0) {
+      const double pq = tot[0];
+      st->pq = pq;
+      st->alpha = st->rho / pq;
+      if (pq == 0.0) st->done = 4;
+      else if (!isfinite(pq)) st->done = 3;
+    }
+  }
+}
+
+// Scalar form of k32v_apply_dir for rows whose length is not a multiple of
+// four (one voxel per thread, column z-march).
+template <int FORM, bool PC>
+__global__ void __launch_bounds__(BX* BY)
+    k32s_apply_dir(OpArgs<float> op, int zc, const float* __restrict__ r,
+                   const float* __restrict__ pold, const float* __restrict__ invd,
+                   float* __restrict__ pnew, float* __restrict__ q, double* partials,
+                   CgState* st) {
+  if (st->done) return;
+  const Geo g = op.g;
+  const float beta = (float)st->beta;
+  SBM_COLUMN_PROLOGUE(g, zc)
+  auto P1 = [&](int64_t idx) -> float {
+    const float z = PC ? invd[idx] * r[idx] : r[idx];
+    return z + beta * pold[idx];
+  };
+  float acc = 0.f;
+  if (active && k0 <= k1) {
+    int64_t c = g.ix(i, j, k0);
+    float pc = P1(c), kc = op.hk[c];
+    float pzm = (k0 == 1) ? pc : P1(c - g.sz), kzm = op.hk[c - g.sz];
+    for (int k = k0; k <= k1; ++k) {
+      const float pzp = (k == g.nz) ? pc : P1(c + g.sz), kzp = op.hk[c + g.sz];
+      const float pym = (i == 1) ? pc : P1(c - 1), pyp = (i == g.ny) ? pc : P1(c + 1);
+      const float pxm = (j == 1) ? (op.bcx0 ? 0.f : pc) : P1(c - g.sx);
+      const float pxp = (j == g.nx) ? (op.bcx1 ? 0.f : pc) : P1(c + g.sx);
+      const float s = face_sum<float>(kc, pc, op.hk[c + 1], pyp, op.hk[c - 1], pym,
+                                      op.hk[c + g.sx], pxp, op.hk[c - g.sx], pxm, kzp, pzp, kzm,
+                                      pzm);
+      const float qv = (FORM == 0) ? op.scale * s : op.diag[c] * pc - op.scale * s;
+      pnew[c] = pc;
+      q[c] = qv;
+      acc += pc * qv;
+      pzm = pc;
+      kzm = kc;
+      pc = pzp;
+      kc = kzp;
+      c += g.sz;
+    }
+  }
+  double v[1] = {(double)acc}, tot[1];
+  if (grid_reduce<1>(v, partials, &st->counter[0], tot)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      const double pq = tot[0];
+      st->pq = pq;
+      st->alpha = st->rho / pq;
+      if (pq == 0.0) st->done = 4;
+      else if (!isfinite(pq)) st->done = 3;
     }
   }
 }
@@ -631,9 +702,9 @@ template <int VEC>
 __device__ __forceinline__ int64_t item_ix(const Geo& g, int nchunk, int64_t u, int* pi, int* pj,
                                            int* pk) {
   const int chunk = (int)(u % nchunk);
-  const int64_t r = u / nchunk;
-  const int j = (int)(r % g.nx) + 1;
-  const int k = (int)(r / g.nx) + 1;
+  const int64_t rr = u / nchunk;
+  const int j = (int)(rr % g.nx) + 1;
+  const int k = (int)(rr / g.nx) + 1;
   *pi = VEC * chunk + 1;
   *pj = j;
   *pk = k;
@@ -641,13 +712,16 @@ __device__ __forceinline__ int64_t item_ix(const Geo& g, int nchunk, int64_t u, 
 }
 
 // x32 += alpha p; r32 -= alpha q; r.r and r.z (FP32 per thread, FP64 across
-// threads); decides whether the next step is a reliable update.
+// threads); decides whether the next step is a reliable update.  After a
+// reliable update the FP32 correction accumulated so far is first folded
+// into the FP64 one (d64 += x32, x32 = alpha p).
 template <bool PC, int VEC>
 __global__ void __launch_bounds__(256)
-    k32_update(Geo g, int nchunk, float* __restrict__ x, const float* __restrict__ p,
+    k32_update(Geo g, Geo g64, int nchunk, float* __restrict__ x, const float* __restrict__ p,
                float* __restrict__ r, const float* __restrict__ q, const float* __restrict__ invd,
-               double* partials, CgState* st) {
+               double* __restrict__ d64, double* partials, CgState* st) {
   if (st->done) return;
+  const bool fold = st->accum_pending != 0;
   const float alpha = (float)st->alpha;
   const int64_t n = (int64_t)nchunk * g.nx * g.nz;
   float a_rr = 0.f, a_rz = 0.f;
@@ -656,8 +730,19 @@ __global__ void __launch_bounds__(256)
     int i, j, k;
     const int64_t c = item_ix<VEC>(g, nchunk, u, &i, &j, &k);
     if (VEC == 4) {
-      float4 xv = ld4(x + c), pv = ld4(p + c), rv = ld4(r + c), qv = ld4(q + c);
-      xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+      float4 xv = ld4(x + c);
+      const float4 pv = ld4(p + c), qv = ld4(q + c);
+      float4 rv = ld4(r + c);
+      if (fold) {
+        const int64_t c64 = g64.ix(i, j, k);
+        d64[c64] += (double)xv.x;
+        d64[c64 + 1] += (double)xv.y;
+        d64[c64 + 2] += (double)xv.z;
+        d64[c64 + 3] += (double)xv.w;
+        xv = make_float4(alpha * pv.x, alpha * pv.y, alpha * pv.z, alpha * pv.w);
+      } else {
+        xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+      }
       rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
       st4(x + c, xv);
       st4(r + c, rv);
@@ -668,7 +753,14 @@ __global__ void __launch_bounds__(256)
                 (rv.z * (d.z * rv.z) + rv.w * (d.w * rv.w));
       }
     } else {
-      x[c] += alpha * p[c];
+      float xv = x[c];
+      if (fold) {
+        d64[g64.ix(i, j, k)] += (double)xv;
+        xv = alpha * p[c];
+      } else {
+        xv += alpha * p[c];
+      }
+      x[c] = xv;
       const float rn = r[c] - alpha * q[c];
       r[c] = rn;
       a_rr += rn * rn;
@@ -681,6 +773,7 @@ __global__ void __launch_bounds__(256)
       const double rr_new = tot[0], rho_new = tot[1];
       const int it = st->iter + 1;
       st->iter = it;
+      st->accum_pending = 0;
       if (!isfinite(rho_new) || !isfinite(st->alpha)) {
         st->done = 3;
       } else {
@@ -760,60 +853,14 @@ __global__ void __launch_bounds__(BX* BY)
   }
 }
 
-// After a reliable update d64 += x32, x32 = 0 (the last block clears the
-// flag); then, unless done, p = z + beta p.
-template <bool PC, int VEC>
-__global__ void __launch_bounds__(256)
-    k32_direction(Geo g, Geo g64, int nchunk, const float* __restrict__ r, float* __restrict__ p,
-                  const float* __restrict__ invd, float* __restrict__ x32,
-                  double* __restrict__ d64, CgState* st) {
-  const bool acc = st->accum_pending != 0;
-  const bool done = st->done != 0;
-  if (!acc && done) return;
-  const float beta = (float)st->beta;
-  const int64_t n = (int64_t)nchunk * g.nx * g.nz;
-  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
-       u += (int64_t)gridDim.x * blockDim.x) {
-    int i, j, k;
-    const int64_t c = item_ix<VEC>(g, nchunk, u, &i, &j, &k);
-    if (acc) {
-      const int64_t c64 = g64.ix(i, j, k);
-#pragma unroll
-      for (int e = 0; e < VEC; ++e) {
-        d64[c64 + e] += (double)x32[c + e];
-        x32[c + e] = 0.f;
-      }
-    }
-    if (!done) {
-      if (VEC == 4) {
-        const float4 rv = ld4(r + c);
-        float4 pv = ld4(p + c);
-        float4 z = rv;
-        if (PC) {
-          const float4 d = ld4(invd + c);
-          z = make_float4(d.x * rv.x, d.y * rv.y, d.z * rv.z, d.w * rv.w);
-        }
-        pv = make_float4(z.x + beta * pv.x, z.y + beta * pv.y, z.z + beta * pv.z,
-                         z.w + beta * pv.w);
-        st4(p + c, pv);
-      } else {
-        const float z = PC ? invd[c] * r[c] : r[c];
-        p[c] = z + beta * p[c];
-      }
-    }
-  }
-  if (acc) {
-    __shared__ bool last;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      last = atomicAdd(&st->counter[4], 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-      st->accum_pending = 0;
-      st->counter[4] = 0u;
-    }
+// x += d64 + x32 on the interior (the total correction of the mixed solve).
+__global__ void k_finish(Geo g, Geo g32, int zc, double* __restrict__ x,
+                         const double* __restrict__ d64, const float* __restrict__ x32) {
+  SBM_COLUMN_PROLOGUE(g, zc)
+  if (!active) return;
+  for (int k = k0; k <= k1; ++k) {
+    const int64_t c = g.ix(i, j, k);
+    x[c] = x[c] + (d64[c] + (double)x32[g32.ix(i, j, k)]);
   }
 }
 
@@ -880,6 +927,7 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->d64, 0, sizeof(double) * g.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->x32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->p32, 0, sizeof(float) * g32.nh, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->rold32, 0, sizeof(float) * g32.nh, s));
   k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
                                          dg32);
   SBM_LAUNCHED(1);
@@ -900,6 +948,7 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   const int64_t items = (int64_t)nchunk * g.nx * g.nz;
   const dim3 fgrid(flat_blocks(items));
   const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
+  float* const pbuf[2] = {p32, ctx->rold32 + kOff32};  // alternating direction buffers
   auto rel = [&](cudaStream_t s2) {
 #define SBM_REL(F, P)                                                                          \
   k_rel_resid<F, P><<<sh64.grid, sh64.block, 0, s2>>>(op64, g32, sh64.zc, ctx->d64, x32,      \
@@ -912,47 +961,57 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
     }
 #undef SBM_REL
   };
-  auto dir = [&](cudaStream_t s2) {
-    if (vec == 4) {
-      if (pc) k32_direction<true, 4><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, r32, p32, iv32, x32, ctx->d64, ctx->st);
-      else k32_direction<false, 4><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, r32, p32, iv32, x32, ctx->d64, ctx->st);
+  // one iteration reading direction buffer `in` and writing `out`
+  auto iter = [&](cudaStream_t s2, const float* in, float* out) {
+#define SBM_AD(F, P)                                                                           \
+  do {                                                                                         \
+    if (vec == 4)                                                                              \
+      k32v_apply_dir<F, P><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, r32, in, iv32, out, q32, \
+                                                   ctx->partials, ctx->st);                    \
+    else                                                                                       \
+      k32s_apply_dir<F, P><<<sh32.grid, sh32.block, 0, s2>>>(op32, sh32.zc, r32, in, iv32,     \
+                                                              out, q32, ctx->partials,         \
+                                                              ctx->st);                        \
+  } while (0)
+    if (sp.form == 0) {
+      if (pc) SBM_AD(0, true); else SBM_AD(0, false);
     } else {
-      if (pc) k32_direction<true, 1><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, r32, p32, iv32, x32, ctx->d64, ctx->st);
-      else k32_direction<false, 1><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, r32, p32, iv32, x32, ctx->d64, ctx->st);
+      if (pc) SBM_AD(1, true); else SBM_AD(1, false);
     }
-  };
-  auto body = [&](cudaStream_t s2) {
+#undef SBM_AD
+#define SBM_UP(P, V)                                                                         \
+  k32_update<P, V><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, x32, out, r32, q32, iv32, ctx->d64, \
+                                          ctx->partials, ctx->st)
     if (vec == 4) {
-      if (sp.form == 0) k32v_apply<0, true><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, p32, q32, ctx->partials, ctx->st);
-      else k32v_apply<1, true><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, p32, q32, ctx->partials, ctx->st);
-      if (pc) k32_update<true, 4><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, p32, r32, q32, iv32, ctx->partials, ctx->st);
-      else k32_update<false, 4><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, p32, r32, q32, iv32, ctx->partials, ctx->st);
+      if (pc) SBM_UP(true, 4); else SBM_UP(false, 4);
     } else {
-      if (sp.form == 0) k_apply<float, 0, true, true><<<sh32.grid, sh32.block, 0, s2>>>(op32, sh32.zc, p32, q32, ctx->partials, ctx->st);
-      else k_apply<float, 1, true, true><<<sh32.grid, sh32.block, 0, s2>>>(op32, sh32.zc, p32, q32, ctx->partials, ctx->st);
-      if (pc) k32_update<true, 1><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, p32, r32, q32, iv32, ctx->partials, ctx->st);
-      else k32_update<false, 1><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, p32, r32, q32, iv32, ctx->partials, ctx->st);
+      if (pc) SBM_UP(true, 1); else SBM_UP(false, 1);
     }
+#undef SBM_UP
     rel(s2);
-    dir(s2);
   };
-  // first residual replacement (r32 = r0, beta = 0) and p = z
+  // two iterations per captured unit so the direction buffers alternate
+  auto body = [&](cudaStream_t s2) {
+    iter(s2, pbuf[0], pbuf[1]);
+    iter(s2, pbuf[1], pbuf[0]);
+  };
+  // first residual replacement: r32 = r0, rho, beta = 0 (p32 = 0 so the
+  // first p_new = z)
   rel(s);
-  dir(s);
-  SBM_LAUNCHED(2);
+  SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   const std::string key =
-      key_of("mixrel", hk32, dg32, x32, r32, p32, q32, iv32, sp.scale, sp.form, sp.bcx0,
+      key_of("mixrel2", hk32, dg32, x32, r32, pbuf[0], pbuf[1], iv32, sp.scale, sp.form, sp.bcx0,
              sp.bcx1, vec * 16 + zc32, pc, sh64.zc, chunk_len(ctx));
   cudaGraphExec_t ex = nullptr;
   int nodes = 0;
-  rc = capture_graph(ctx, key, 4, body, &ex, &nodes);
+  rc = capture_graph(ctx, key, 6, body, &ex, &nodes);
   if (rc) return rc;
   CgState fin;
   rc = run_chunks(ctx, ex, nodes, ctx->st, ctx->h_st, &fin);
   if (rc) return rc;
-  // x += d64 (interior): the ghosts of x keep their Dirichlet / flux data.
-  k_accum<double><<<sh64.grid, sh64.block, 0, s>>>(g, sh64.zc, sp.x, ctx->d64);
+  // x += d64 + x32 (interior): the ghosts of x keep their Dirichlet / flux data.
+  k_finish<<<sh64.grid, sh64.block, 0, s>>>(g, g32, sh64.zc, sp.x, ctx->d64, x32);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   SBM_CUDA_TRY(cudaEventRecord(ctx->ev1, s));
