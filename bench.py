@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 SBM hot path: 256^3 potential solve to rel-res 1e-8.
+
+Workload (one "step" = one full solve): a 256^3 seeded synthetic
+microstructure -- overlapping spheres, radii U[4,10] voxels, solid fraction
+0.6, plus one random cylindrical tunnel of radius 6 -- whose signed distance
+comes from 175 ReDist3D_XYZ steps and psi = 0.5(1 + tanh(d/(sqrt(2)*1.5))).
+Node conductivity psi*1 + (1-psi)*0.1, Dirichlet phi = 0 / 1 on the two x
+ghost planes, Neumann elsewhere, zero right-hand side; solved until
+||r||/||r0|| <= 1e-8 (r recomputed in FP64).
+
+Our arm (default): the production solver -- FP32 CG with Jacobi
+preconditioning and FP64 reliable-update refinement -- with fields resident
+in HBM; `value` is the mean device time of one solve (CUDA events on the
+solver stream), `e2e` the same solve through the C-ABI from pinned host
+buffers (coef/x/rhs uploaded, x downloaded) timed on the wall clock.  The
+plain FP64 CG (the drop-in) is timed beside it for the speed-up.
+
+--impl reference: the reference's algorithm (plain FP64 CG, its own
+restatement in C with OpenMP -- the Fortran reference has no compiler here)
+timed on all host cores, each step a bounded sample of CG iterations
+extrapolated to the 2038 iterations the FP64 CG needs on this workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N = 256
+SEED = 1
+TOL = 1e-8
+# FP64 CG iterations to rel-res 1e-8 on this workload: the oracle (plain
+# FP64 CG in C) and the GPU FP64 CG both stop at 2038.
+FP64_ITERS = 2038
+METRIC = "sbm_potential_solve_time_256^3_relres_1e-8"
+UNIT = "s"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=N)
+    return ap.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _config(n, extra=None):
+    cfg = {"workload": f"SBM potential solve {n}^3, spheres r~U[4,10] + tunnel r=6, "
+                       f"solid 0.6, k=psi+0.1(1-psi), Dirichlet 0/1 on x faces, rel-res 1e-8",
+           "grid": [n, n, n], "seed": SEED, "tol": TOL,
+           "l2": "working set > L2 (>= 8 fields of 67-134 MB each) and an L2 flush "
+                 "(256 MB write) between timed solves"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi in the background."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        lines = [ln.strip() for ln in open(self.f.name) if ln.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------- CPU side
+
+def cpu_sample(prob, budget_s: float):
+    """Oracle FP64 CG on the host cores for a bounded number of iterations,
+    extrapolated to the FP64 iteration count; returns (seconds, info)."""
+    from oracle import sbm_oracle as orc
+    from elsim_gb300 import sbm
+    threads = orc.lib().orc_num_threads()
+    t = time.perf_counter()
+    orc.cg(prob["coef"], prob["rhs"], prob["x"], 1.0, sbm.BC_ZERO, sbm.BC_ZERO, sbm.STOP_REL_RES,
+           TOL, 5)
+    per = (time.perf_counter() - t) / 5
+    iters = int(max(5, min(FP64_ITERS, budget_s / max(per, 1e-6))))
+    t = time.perf_counter()
+    _, info = orc.cg(prob["coef"], prob["rhs"], prob["x"], 1.0, sbm.BC_ZERO, sbm.BC_ZERO,
+                     sbm.STOP_REL_RES, TOL, iters)
+    el = time.perf_counter() - t
+    return el / info["iters"] * FP64_ITERS, {"iters": info["iters"], "seconds": el,
+                                              "threads": threads}
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    from elsim_gb300 import synth
+    from oracle import sbm_oracle as orc
+    n = args.size
+    m = synth.microstructure((n, n, n), seed=SEED, tunnel=True, redist=orc.redist)
+    prob = synth.potential_problem(m["psi"])
+    budget = 8.0
+    for _ in range(args.warmup):
+        cpu_sample(prob, budget / 4)
+    vals, infos = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, info = cpu_sample(prob, budget)
+        vals.append(v)
+        infos.append(info)
+    wall = time.perf_counter() - t0
+    value = statistics.mean(vals)
+    threads = infos[0]["threads"]
+    sample = (f"{infos[0]['iters']} FP64 CG iterations of the {n}^3 solve per step on {threads} "
+              f"OpenMP threads (oracle port of the reference CG), extrapolated x{FP64_ITERS}/"
+              f"{infos[0]['iters']} to the full solve")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded spheres + tunnel; reference inputs are not public)",
+            "impl": "reference", "config": _config(n),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# --------------------------------------------------------------- GPU side
+
+def run_ours(args):
+    import torch
+    ws, rank = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    import __graft_entry__
+    __graft_entry__.build()
+    from elsim_gb300 import sbm, synth
+
+    n = args.size
+    dev = torch.device("cuda", torch.cuda.current_device())
+    m = synth.microstructure((n, n, n), seed=SEED, tunnel=True)
+    prob = synth.potential_problem(m["psi"])
+    hshape = prob["x"].shape
+    nh = int(np.prod(hshape))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    ctx = sbm.Context(n, n, n)
+    for k in ("coef", "x", "rhs", "weight"):
+        ctx.upload(k, prob[k])
+
+    def solve(prec, pc):
+        ctx.upload("x", prob["x"])
+        flush.zero_()
+        torch.cuda.synchronize()
+        return ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO, scale=1.0,
+                            tol=TOL, max_it=200000, stop_rule=sbm.STOP_REL_RES, precision=prec,
+                            precond=pc)
+
+    # the drop-in: plain FP64 CG (reference algorithm on the GPU)
+    fp64 = solve(sbm.PREC_FP64, sbm.PC_NONE)
+    x64 = ctx.download("x")[1:-1, 1:-1, 1:-1].copy()
+    fp64_ms = ctx.bench_kernel(2, 10)
+    plain = solve(sbm.PREC_MIXED, sbm.PC_NONE)
+    for _ in range(args.warmup):
+        solve(sbm.PREC_MIXED, sbm.PC_JACOBI)
+    # timed region: K solves, each timed on the device with CUDA events on the
+    # solver stream (x reset and L2 flush happen between solves, untimed)
+    clocks = Clocks()
+    barrier()
+    clocks.start()
+    l0 = sbm.launch_count()
+    t0 = time.perf_counter()
+    times = []
+    for _ in range(args.steps):
+        info = solve(sbm.PREC_MIXED, sbm.PC_JACOBI)
+        times.append(info["ms"] / 1e3)
+    barrier()
+    wall = time.perf_counter() - t0
+    launches = sbm.launch_count() - l0
+    clk = clocks.stop()
+    xm = ctx.download("x")[1:-1, 1:-1, 1:-1]
+    rel_err = float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))
+    t_local = max(times)
+    if ws > 1:
+        tt = torch.tensor([t_local], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_local = float(tt.item())
+    value = statistics.mean(times) if ws == 1 else t_local
+    # roofline of the dominant kernel (fused direction + stencil), timed live
+    ms_k, bytes_k = ctx.bench_kernel(0, 20)
+    ms_u, bytes_u = ctx.bench_kernel(1, 20)
+    peak, peak_kind = _peaks()
+    achieved = bytes_k / (ms_k * 1e-3) / 1e9
+    # e2e through the C-ABI with pinned host buffers
+    pin = {}
+    for k in ("coef", "x", "rhs"):
+        t = torch.empty(nh, dtype=torch.float64, pin_memory=True)
+        a = np.ndarray(hshape, dtype=np.float64, buffer=t.numpy(), order="F")
+        a[...] = prob[k]
+        pin[k] = (t, a)
+    xout_t = torch.empty(nh, dtype=torch.float64, pin_memory=True)
+    e2e = []
+    for step in range(max(1, args.steps)):
+        flush.zero_()
+        barrier()
+        t1 = time.perf_counter()
+        for k in ("coef", "x", "rhs"):
+            ctx.upload(k, pin[k][1])
+        ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO, scale=1.0, tol=TOL,
+                     max_it=200000, stop_rule=sbm.STOP_REL_RES, precision=sbm.PREC_MIXED,
+                     precond=sbm.PC_JACOBI)
+        xo = np.ndarray(hshape, dtype=np.float64, buffer=xout_t.numpy(), order="F")
+        lib = sbm.load_library()
+        rc = lib.sbm_download(ctx._h, sbm.F_X, xo.ctypes.data_as(sbm.C.POINTER(sbm.C.c_double)), 1)
+        assert rc == 0
+        e2e.append(time.perf_counter() - t1)
+    e2e_v = statistics.mean(e2e)
+    cpu = None
+    if rank == 0 and ws == 1:
+        cv, ci = cpu_sample(prob, 12.0)
+        cpu = {"value": cv, "unit": UNIT, "cores": ci["threads"], "kind": "port",
+               "sample": f"{ci['iters']} oracle FP64 CG iterations of the same {n}^3 solve "
+                         f"({ci['seconds']:.1f} s on {ci['threads']} threads), extrapolated "
+                         f"x{FP64_ITERS}/{ci['iters']}"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded spheres + tunnel; reference inputs are not public)",
+            "config": _config(n, {
+                "method": "FP32 Jacobi-PCG, FP64 reliable-update refinement",
+                "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
+                "iterations": info["iters"],
+                "relL2_vs_fp64_cg": rel_err,
+                "fp64_cg_s": fp64["ms"] / 1e3, "fp64_cg_iterations": fp64["iters"],
+                "mixed_no_pc_s": plain["ms"] / 1e3, "mixed_no_pc_iterations": plain["iters"],
+                "speedup_vs_fp64_cg": fp64["ms"] / 1e3 / value,
+                "voxel_updates_per_s": n ** 3 * info["iters"] / value,
+                "wall_s_timed_region": wall,
+                "update_kernel": {"ms": ms_u, "GB/s": bytes_u / (ms_u * 1e-3) / 1e9},
+                "fp64_stencil_kernel": {"ms": fp64_ms[0],
+                                        "GB/s": fp64_ms[1] / (fp64_ms[0] * 1e-3) / 1e9,
+                                        "bound": "fp64 alu"},
+            }),
+            "roofline": {"bound": "hbm", "kernel": "k32v_apply_dir (FP32 direction+stencil)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": 441.7e6,
+                         "algorithmic_bytes": bytes_k, "ms": ms_k},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": 3 * nh * 8,
+                    "d2h_bytes_per_step": nh * 8},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

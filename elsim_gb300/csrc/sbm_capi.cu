@@ -361,6 +361,12 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, doubl
   return r.status;
 }
 
+int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
+                     double* bytes_per_launch) {
+  if (!ctx) return SBM_ERR_ARG;
+  return bench_kernel(ctx, which, reps, ms_per_launch, bytes_per_launch);
+}
+
 int sbm_ch_step(sbm_ctx* ctx, double dt, sbm_scalars* s) {
   if (!ctx) return SBM_ERR_ARG;
   if (!ctx->hk_kap) return SBM_ERR_STATE;

@@ -288,12 +288,16 @@ struct sbm_ctx {
   int inner_max = 0;
   // CUDA graphs of captured CG chunks, keyed by solve signature
   std::map<std::string, std::pair<cudaGraphExec_t, int>> graphs;
+  // arguments of the last mixed solve, replayed by sbm_bench_kernel
+  sbm::OpArgs<float> last_op32{};
+  int last_pc = -1;
   // learned preconditioner (opaque; owned by sbm_learned.cu)
   void* net = nullptr;
 };
 
 namespace sbm {
 int solve(sbm_ctx* ctx, const SolveSpec& spec, SolveResult* out);
+int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double* bytes_per_launch);
 int ensure_fp32_work(sbm_ctx* ctx);
 void release_graphs(sbm_ctx* ctx);
 }  // namespace sbm

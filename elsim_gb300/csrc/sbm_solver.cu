@@ -1007,6 +1007,8 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   int nodes = 0;
   rc = capture_graph(ctx, key, 6, body, &ex, &nodes);
   if (rc) return rc;
+  ctx->last_op32 = op32;
+  ctx->last_pc = pc ? 1 : 0;
   CgState fin;
   rc = run_chunks(ctx, ex, nodes, ctx->st, ctx->h_st, &fin);
   if (rc) return rc;
@@ -1026,6 +1028,88 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   return SBM_OK;
 }
 
+
+// Times `reps` back-to-back launches of one solver kernel on the context
+// stream with CUDA events, on the buffers of the last mixed solve:
+//   which 0: the FP32 fused direction + stencil kernel (the dominant kernel)
+//   which 1: the FP32 vector update kernel
+//   which 2: the FP64 stencil + dot kernel of the plain CG
+// and reports the algorithmic bytes one launch moves.
+int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double* bytes_per_launch) {
+  if (reps < 1 || which < 0 || which > 2) return SBM_ERR_ARG;
+  if (which < 2 && ctx->last_pc < 0) return SBM_ERR_STATE;
+  const Geo& g = ctx->g;
+  const Geo& g32 = ctx->g32;
+  cudaStream_t s = ctx->stream;
+  const double n = (double)g.ninterior();
+  CgState* h = &ctx->h_st[3];
+  memset(h, 0, sizeof(CgState));
+  h->rho = 1.0;
+  h->alpha = 1e-30;
+  h->beta = 0.5;
+  h->max_it = 1 << 30;
+  h->tol = 0.0;
+  h->delta2 = 0.0;
+  h->aux[0] = 1.0;
+  SBM_CUDA_TRY(cudaMemcpyAsync(ctx->st32, h, sizeof(CgState), cudaMemcpyHostToDevice, s));
+  const OpArgs<float> op32 = ctx->last_op32;
+  const bool pc = ctx->last_pc == 1;
+  const int vec = (g.ny % 4 == 0) ? 4 : 1;
+  const int nchunk = g.ny / vec;
+  const int zc32 = ctx->zc32 > 0 ? ctx->zc32 : 8;
+  const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
+  const dim3 fgrid(flat_blocks((int64_t)nchunk * g.nx * g.nz));
+  const Shape sh32 = stencil_shape(g32, pick_zc(g32, ctx->zc32));
+  const Shape sh64 = stencil_shape(g, pick_zc(g, ctx->zc64));
+  float* r32 = ctx->r32 + kOff32;
+  float* pa = ctx->p32 + kOff32;
+  float* pb = ctx->rold32 + kOff32;
+  float* q32 = ctx->q32 + kOff32;
+  float* x32 = ctx->x32 + kOff32;
+  float* iv = ctx->z32 + kOff32;
+  auto launch = [&]() {
+    if (which == 0) {
+      if (vec == 4) {
+        if (op32.form == 0) {
+          if (pc) k32v_apply_dir<0, true><<<vgrid, 256, 0, s>>>(op32, nchunk, zc32, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);
+          else k32v_apply_dir<0, false><<<vgrid, 256, 0, s>>>(op32, nchunk, zc32, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);
+        } else {
+          if (pc) k32v_apply_dir<1, true><<<vgrid, 256, 0, s>>>(op32, nchunk, zc32, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);
+          else k32v_apply_dir<1, false><<<vgrid, 256, 0, s>>>(op32, nchunk, zc32, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);
+        }
+      } else {
+        if (op32.form == 0) k32s_apply_dir<0, false><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);
+        else k32s_apply_dir<1, false><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);
+      }
+    } else if (which == 1) {
+      if (vec == 4) {
+        if (pc) k32_update<true, 4><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);
+        else k32_update<false, 4><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);
+      } else {
+        k32_update<false, 1><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);
+      }
+    } else {
+      OpArgs<double> op{g, ctx->hk_gen, nullptr, 1.0, 0, SBM_BC_ZERO, SBM_BC_ZERO};
+      k_apply<double, 0, true, true><<<sh64.grid, sh64.block, 0, s>>>(op, sh64.zc, ctx->p64, ctx->q64, ctx->partials, ctx->st32);
+    }
+  };
+  launch();  // warm
+  SBM_CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+  for (int r = 0; r < reps; ++r) launch();
+  SBM_CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+  SBM_CUDA_TRY(cudaEventSynchronize(ctx->ev1));
+  SBM_CUDA_TRY(cudaGetLastError());
+  SBM_LAUNCHED(reps + 1);
+  float ms = 0.f;
+  SBM_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  if (ms_per_launch) *ms_per_launch = ms / reps;
+  double words;
+  if (which == 0) words = 5.0 + (pc ? 1.0 : 0.0) + (op32.form ? 1.0 : 0.0);  // r,p_old,hk,[invd],[diag] -> p_new,q
+  else if (which == 1) words = 6.0 + (pc ? 1.0 : 0.0);                       // x,p,r,q,[invd] -> x,r
+  else words = 3.0;                                                          // p,hk -> q (FP64)
+  if (bytes_per_launch) *bytes_per_launch = words * (which == 2 ? 8.0 : 4.0) * n;
+  return SBM_OK;
+}
 
 int solve(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   if (sp.precision == SBM_PREC_FP64) return solve_fp64(ctx, sp, out);

@@ -125,6 +125,7 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
                                        C.c_double, C.POINTER(Scalars)]),
         "sbm_cg_solve": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
                                    C.c_int, C.c_int, C.c_int, ip, dp, fp]),
+        "sbm_bench_kernel": (C.c_int, [vp, C.c_int, C.c_int, fp, dp]),
         "sbm_time_step": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_int,
                                     C.POINTER(Scalars)]),
         "sbm_ch_step": (C.c_int, [vp, C.c_double, C.POINTER(Scalars)]),
@@ -219,9 +220,18 @@ class Context:
         self.params = params
         _check(self.lib.sbm_ctx_set_params(self._h, C.byref(params)), "sbm_ctx_set_params")
 
-    def set_tuning(self, zc64=0, zc32=0, chunk=0, inner_tol=0.0, inner_max=0) -> None:
-        _check(self.lib.sbm_ctx_set_tuning(self._h, zc64, zc32, chunk, inner_tol, inner_max),
+    def set_tuning(self, zc64=0, zc32=0, chunk=0, delta=0.0) -> None:
+        """Launch-shape knobs (0 = built-in) and the reliable-update factor."""
+        _check(self.lib.sbm_ctx_set_tuning(self._h, zc64, zc32, chunk, delta, 0),
                "sbm_ctx_set_tuning")
+
+    def bench_kernel(self, which: int, reps: int = 20) -> tuple[float, float]:
+        """(ms per launch, algorithmic bytes per launch) of a solver kernel."""
+        ms = C.c_float(0)
+        b = C.c_double(0)
+        _check(self.lib.sbm_bench_kernel(self._h, which, reps, C.byref(ms), C.byref(b)),
+               "sbm_bench_kernel")
+        return ms.value, b.value
 
     def stream(self) -> int:
         s = C.c_void_p()

@@ -186,6 +186,14 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale,
                  double tol, int max_it, int stop_rule, int precision,
                  int precond, int* iters, double* final_res, float* ms);
 
+/* Benchmark hook (no counterpart in the reference): times `reps` launches
+ * of one solver kernel on the context stream with CUDA events, replaying the
+ * arguments of the last mixed-precision solve.  which 0: FP32 fused
+ * direction + stencil kernel; 1: FP32 vector update; 2: FP64 stencil + dot.
+ * Reports the mean launch time and the algorithmic bytes one launch moves. */
+int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
+                     double* bytes_per_launch);
+
 /* One electrochemical time step, the body of the reference's time loop
  * (SBMES:397-840) for a given dt, voltage-scan rate vsr and step index
  * iter: Cahn-Hilliard, CnE implicit solve with the flux BC and mean
