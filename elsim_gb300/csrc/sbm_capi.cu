@@ -19,6 +19,7 @@ static thread_local char g_err[256] = "";
 void set_error(const char* where, cudaError_t e) {
   snprintf(g_err, sizeof(g_err), "%s: %s", where, cudaGetErrorString(e));
 }
+void set_error_msg(const char* msg) { snprintf(g_err, sizeof(g_err), "%s", msg); }
 const char* last_error() { return g_err; }
 
 // defined in sbm_fields.cu / sbm_levelset.cu

@@ -120,6 +120,7 @@ struct CgState {
 // ------------------------------------------------------ errors, counters
 extern std::atomic<int64_t> g_launches;
 void set_error(const char* where, cudaError_t e);
+void set_error_msg(const char* msg);
 const char* last_error();
 
 #define SBM_CUDA_TRY(call)                                    \

@@ -239,3 +239,71 @@ int sign_dev(cudaStream_t s, int64_t n, const double* ds, double thr, double* sg
 }
 
 }  // namespace sbm
+
+// ================================================ no-allocation ReDist3D_XYZ
+// sbm_redist_noalloc runs the same ReDist3D_XYZ iterations as sbm_redist on
+// caller-owned device buffers, for callers that must not allocate device
+// memory themselves or through this library.  Its only scratch -- the
+// ping-pong field of the Jacobi sweep -- is the fixed array below: every GPU
+// that loads this library holds it (SBM_NOALLOC_REDIST_MAX_CELLS doubles,
+// 8 MiB) until the process exits.  All calls share it: two calls whose work
+// overlaps on the GPU (different streams or host threads) race on it.  The
+// sweep writes every cell of the scratch before reading it, so the contents
+// a previous call left behind never matter and nothing is cleared.
+
+#include <mutex>
+
+namespace sbm {
+
+static __device__ __align__(256) double g_redist_scratch[SBM_NOALLOC_REDIST_MAX_CELLS];
+
+namespace {
+
+std::mutex g_redist_scratch_mu;
+double* g_redist_scratch_ptr[64] = {};
+
+// Device address of the scratch array on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is asked of
+// the runtime once per device (with that device current) and cached.
+int redist_scratch(double** out) {
+  int dev = 0;
+  SBM_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return SBM_ERR_STATE;
+  std::lock_guard<std::mutex> lock(g_redist_scratch_mu);
+  if (!g_redist_scratch_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_redist_scratch);
+    if (e != cudaSuccess) {
+      set_error("cudaGetSymbolAddress", e);
+      return SBM_ERR_CUDA;
+    }
+    g_redist_scratch_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_redist_scratch_ptr[dev];
+  return SBM_OK;
+}
+
+}  // namespace
+}  // namespace sbm
+
+extern "C" int sbm_redist_noalloc(int lit, int py, int px, int pz, double dt, const double* sg,
+                                  double* f, void* stream) {
+  if (lit < 0 || py < 1 || px < 1 || pz < 1 || !sg || !f) return SBM_ERR_ARG;
+  const int64_t cells = (int64_t)(py + 2) * (px + 2) * (pz + 2);
+  if (cells > SBM_NOALLOC_REDIST_MAX_CELLS) {
+    char msg[160];
+    snprintf(msg, sizeof(msg),
+             "sbm_redist_noalloc: %lld padded cells exceed the %d-cell built-in scratch",
+             (long long)cells, SBM_NOALLOC_REDIST_MAX_CELLS);
+    sbm::set_error_msg(msg);
+    return SBM_ERR_ARG;
+  }
+  double* scratch = nullptr;
+  int rc = sbm::redist_scratch(&scratch);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  rc = sbm::redist_dev(s, sbm::make_geo(py, px, pz), sg, f, scratch, lit, dt);
+  if (rc) return rc;
+  SBM_CUDA_TRY(cudaStreamSynchronize(s));
+  return SBM_OK;
+}

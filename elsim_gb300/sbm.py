@@ -135,6 +135,8 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_table_lookup": (C.c_int, [i64, C.c_int, dp, dp, dp, dp]),
         "sbm_redist": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]),
         "sbm_accdiff": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, C.c_int]),
+        "sbm_redist_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
         "sbm_rm_mask": (C.c_int, [i64, dp, dp, dp]),
         "sbm_sign": (C.c_int, [i64, dp, C.c_double, dp]),
     }

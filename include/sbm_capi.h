@@ -232,6 +232,23 @@ int sbm_redist(int lit, int py, int px, int pz, double dt,
 int sbm_accdiff(int py, int px, int pz, const double* psi, double* cn,
                 int term, int dirichlet_x);
 
+/* ReDist3D_XYZ without any device allocation.  No counterpart in the
+ * reference.  Some callers cannot allocate device memory: a host program
+ * whose GPU memory is all owned by another allocator or framework, or one
+ * that runs under a fixed memory budget set at start-up.  This variant takes
+ * DEVICE pointers sg and f (halo-padded, f in/out), enqueues the lit
+ * iterations on `stream` (a cudaStream_t; NULL = the default stream), waits
+ * for them, and uses as scratch a fixed array built into the library
+ * (SBM_NOALLOC_REDIST_MAX_CELLS doubles, 8 MiB, held on every GPU that loads
+ * the library until exit); grids of more padded cells are rejected with
+ * SBM_ERR_ARG and a message in sbm_last_error().  It calls no cudaMalloc or cudaFree.  The first call on a
+ * device looks up the scratch address on that device, so make that first
+ * call before any stream capture.  All calls share the scratch: calls that
+ * overlap on the GPU race.  Results are bit-identical to sbm_redist. */
+#define SBM_NOALLOC_REDIST_MAX_CELLS (1 << 20)
+int sbm_redist_noalloc(int lit, int py, int px, int pz, double dt, const double* sg, double* f,
+                       void* stream);
+
 /* RM_UCNCT_3D.f90:78-82 / :127-130: psB = psA, psB = 0 where Cn < 1e-4
  * (REAL(4) literal).  n voxels, bit-exact. */
 int sbm_rm_mask(int64_t n, const double* psA, const double* cn, double* psB);
@@ -240,7 +257,7 @@ int sbm_rm_mask(int64_t n, const double* psA, const double* cn, double* psB);
  * sg = 1 where ds > thr else -1; n values (halo-padded array). */
 int sbm_sign(int64_t n, const double* ds, double thr, double* sg);
 
-/* Text of the last CUDA error seen by this thread. */
+/* Text of the last error (CUDA failure or size rejection) seen by this thread. */
 const char* sbm_last_error(void);
 /* Version string of the compiled library. */
 const char* sbm_version(void);
