@@ -104,3 +104,46 @@ def potential_problem(psi: np.ndarray, k_solid: float = 1.0, k_elec: float = 0.1
     x[:, -1, :] = phi_hi
     rhs = np.zeros_like(coef, order="F")
     return dict(coef=coef, x=x, rhs=rhs, weight=np.asfortranarray(psi.copy()))
+
+
+def reference_tables(params):
+    """Fills the five 101-point property tables of the reference
+    (C_Li_X / M6 / Mb5 / J2 / O3, SBMES:210-242, not in its repository) with
+    smooth synthetic curves of plausible magnitude: chemical potential,
+    mobility (already scaled as SBMES:242 does), exchange current and
+    open-circuit voltage against the Li fraction on [0, 1]."""
+    x = np.arange(101) * 0.01
+    params.set_table("tbl_x", x)
+    params.set_table("tbl_mu", 0.05 * (2.0 * x - 1.0) + 0.02 * np.sin(6.0 * np.pi * x))
+    params.set_table("tbl_mb", 1.0e-9 * (1.0 + x))
+    params.set_table("tbl_i0", 1.0 + 0.5 * x * (1.0 - x))
+    params.set_table("tbl_ocv", 0.2 - 0.1 * x)
+    return params
+
+
+def step_schedule(xrf: float, dcrnt: float, trgi: float):
+    """dt and voltage-scan rate of one time step as the reference's time
+    loop chooses them (SBMES:360-383); all literals REAL(4) as there."""
+    f = lambda v: float(np.float32(v))
+    vsr0 = 1.0e-2 * 1.0e1 / f(3.25 ** 2) * f(2.5)
+    if dcrnt < f(0.07) * abs(trgi):
+        vsr = vsr0 * f(0.5)
+    elif dcrnt < f(0.20) * abs(trgi):
+        vsr = vsr0
+    elif dcrnt < f(0.40) * abs(trgi):
+        vsr = vsr0 * f(3.0)
+    elif dcrnt < f(0.75) * abs(trgi):
+        vsr = vsr0 * f(5.0)
+    else:
+        vsr = vsr0 * f(8.0)
+    base = np.float32(np.float32(1.05625e-02) * np.float32(0.125))
+    if xrf < f(0.12):
+        dt = float(np.float32(base * np.float32(0.75)))
+        vsr = vsr * 2
+    elif xrf < f(0.20):
+        dt = float(np.float32(base * np.float32(0.5)))
+        vsr = vsr * 10
+    else:
+        dt = float(np.float32(base * np.float32(0.5)))
+        vsr = vsr * 15
+    return dt, vsr

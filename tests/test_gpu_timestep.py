@@ -1,0 +1,109 @@
+"""GPU parity of whole electrochemical time steps (SBMES:357-840) against the
+oracle: set-up from two REAL(4) distance fields, then Cahn-Hilliard, the CnE
+solve with its flux condition and mean correction, the potentials with the
+Butler-Volmer Picard loop, and the voltage control -- for the reference's
+exponential Butler-Volmer and for the linearised form.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from elsim_gb300 import sbm, synth
+from oracle import sbm_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = [sbm.F_CNP, sbm.F_CNE, sbm.F_PHP, sbm.F_PHE, sbm.F_RXN]
+
+
+def _dist(shape, seed):
+    m = synth.microstructure(shape, seed=seed, reinit_steps=60, redist=orc.redist)
+    d = m["dist"][1:-1, 1:-1, 1:-1]
+    return d.astype(np.float32), (-d).astype(np.float32)
+
+
+def _params(tight, bv_mode):
+    p = synth.reference_tables(orc.params_reference())
+    p.bv_mode = bv_mode
+    if tight:
+        p.crt_cne = p.crt_php = p.crt_phe = 1e-11
+        p.crt_picard = 1e-11
+    return p
+
+
+def _run(shape, p, steps, seed=4, mean_every=None):
+    if mean_every:
+        p.cne_mean_every = mean_every
+    dp, de = _dist(shape, seed)
+    st = orc.State(*shape, p)
+    so = st.setup_domain(dp, de)
+    ctx = sbm.Context(*shape, params=p)
+    sg = ctx.setup_domain(dp, de)
+    for key in ("tPP", "tPE", "xrf", "trgI"):
+        assert abs(sg[key] - so[key]) <= 1e-12 * abs(so[key]), key
+    hist = []
+    for it in range(1, steps + 1):
+        dt, vsr = synth.step_schedule(so["xrf"], abs(so["trgI"] - so["scrnt"]), so["trgI"])
+        so = st.time_step(it, dt, vsr)
+        sg = ctx.time_step(it, dt, vsr)
+        hist.append((sg, so))
+    return ctx, st, hist
+
+
+@pytest.mark.parametrize("bv_mode", [sbm.BV_EXP, sbm.BV_LINEAR])
+def test_time_steps_match_oracle_tight(built, bv_mode):
+    shape = (20, 24, 16)
+    ctx, st, hist = _run(shape, _params(True, bv_mode), 3, mean_every=2)
+    sg, so = hist[-1]
+    for key in ("xrf", "scrnt", "bve", "infx"):
+        assert abs(sg[key] - so[key]) <= 1e-7 * max(abs(so[key]), 1e-12), (key, sg[key], so[key])
+    for f in FIELDS:
+        assert rel_l2(ctx.download(f), st.field(f)) < 1e-7, f
+    # the set-up fields are bit-for-bit functions of psi except for tanh
+    assert rel_l2(ctx.download(sbm.F_PSP), st.field(sbm.F_PSP)) < 1e-14
+    assert rel_l2(ctx.download(sbm.F_AVP), st.field(sbm.F_AVP)) < 1e-12
+    ctx.close()
+
+
+def test_time_steps_reference_tolerances(built):
+    """With the reference's own tolerances both sides stop on the same norms;
+    iteration counts agree to a couple of iterations, fields to the solver
+    tolerance."""
+    shape = (24, 20, 18)
+    ctx, st, hist = _run(shape, _params(False, sbm.BV_EXP), 3, seed=6)
+    for sg, so in hist:
+        for key in ("it_cne", "it_php", "it_phe", "n_picard"):
+            assert abs(sg[key] - so[key]) <= max(2, 0.02 * so[key]), (key, sg[key], so[key])
+    sg, so = hist[-1]
+    assert abs(sg["xrf"] - so["xrf"]) <= 1e-9 * abs(so["xrf"])
+    for f in (sbm.F_CNP, sbm.F_CNE):
+        assert rel_l2(ctx.download(f), st.field(f)) < 1e-7, f
+    ctx.close()
+
+
+def test_stage_calls_equal_full_step(built):
+    shape = (12, 16, 10)
+    p = _params(True, sbm.BV_EXP)
+    dp, de = _dist(shape, 8)
+    a = sbm.Context(*shape, params=p)
+    b = sbm.Context(*shape, params=p)
+    a.setup_domain(dp, de)
+    b.setup_domain(dp, de)
+    dt, vsr = 1e-3, 0.02
+    for it in (1, 2):
+        a.time_step(it, dt, vsr)
+        b.ch_step(dt)
+        b.cne_step(it, dt)
+        b.bv_update()
+        b.voltage_step(dt, vsr)
+    for f in FIELDS:
+        assert np.array_equal(a.download(f), b.download(f))
+    a.close()
+    b.close()
+
+
+def test_step_before_setup_is_a_state_error(built):
+    with sbm.Context(8, 8, 8) as ctx:
+        with pytest.raises(sbm.SbmError) as e:
+            ctx.time_step(1, 1e-3, 0.01)
+        assert e.value.code == sbm.ERR_STATE
