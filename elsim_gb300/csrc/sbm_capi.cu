@@ -210,19 +210,20 @@ int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p) {
   return SBM_OK;
 }
 
-int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double inner_tol,
-                       int inner_max) {
-  if (!ctx || zc64 < 0 || zc32 < 0 || chunk < 0 || zc64 > 64 || zc32 > 64 || chunk > 1024)
+int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta, int flags) {
+  if (!ctx || zc64 < 0 || zc32 < 0 || chunk < 0 || zc64 > 64 || zc32 > 64 || chunk > 1024 ||
+      !(delta >= 0.0 && delta < 1.0) || (flags & ~SBM_TUNE_NO_TMA))
     return SBM_ERR_ARG;
-  if (zc64 != ctx->zc64 || zc32 != ctx->zc32 || chunk != ctx->chunk) {
+  const int no_tma = (flags & SBM_TUNE_NO_TMA) ? 1 : 0;
+  if (zc64 != ctx->zc64 || zc32 != ctx->zc32 || chunk != ctx->chunk || no_tma != ctx->no_tma) {
     cudaStreamSynchronize(ctx->stream);
     release_graphs(ctx);
   }
   ctx->zc64 = zc64;
   ctx->zc32 = zc32;
   ctx->chunk = chunk;
-  ctx->inner_tol = inner_tol;
-  ctx->inner_max = inner_max;
+  ctx->inner_tol = delta;
+  ctx->no_tma = no_tma;
   return SBM_OK;
 }
 

@@ -212,6 +212,20 @@ struct OpArgs {
   int bcx0, bcx1; // SBM_BC_COPY / SBM_BC_ZERO for the search direction
 };
 
+// Face terms of S(p) = sum_f c_f (p_nb - p_c) in the reference's order
+// (y+, y-, x+, x-, z+, z-; SBMES:494-499), c_f = hk_nb + hk_c.
+template <typename T>
+__device__ __forceinline__ T face_sum(T kc, T pc, T kyp, T pyp, T kym, T pym, T kxp, T pxp,
+                                      T kxm, T pxm, T kzp, T pzp, T kzm, T pzm) {
+  T s = (kyp + kc) * (pyp - pc);
+  s = s - (kym + kc) * (pc - pym);
+  s = s + (kxp + kc) * (pxp - pc);
+  s = s - (kxm + kc) * (pc - pxm);
+  s = s + (kzp + kc) * (pzp - pc);
+  s = s - (kzm + kc) * (pc - pzm);
+  return s;
+}
+
 // ------------------------------------------------------- launchers
 // q = A x with x's ghosts read from memory (no reduction), FP64.  Used for
 // RHE = (1/dx^2) div(pce grad CnE), SBMES:591-596.
@@ -292,6 +306,7 @@ struct sbm_ctx {
   // arguments of the last mixed solve, replayed by sbm_bench_kernel
   sbm::OpArgs<float> last_op32{};
   int last_pc = -1;
+  int no_tma = 0;  // tuning flag: use the register-tiled FP32 stencil instead of TMA
   // learned preconditioner (opaque; owned by sbm_learned.cu)
   void* net = nullptr;
 };

@@ -40,20 +40,6 @@ int pick_zc(const Geo& g, int tuned) {
   return zc;
 }
 
-// Face terms of S(p) = sum_f c_f (p_nb - p_c) in the reference's order
-// (y+, y-, x+, x-, z+, z-; SBMES:494-499), c_f = hk_nb + hk_c.
-template <typename T>
-__device__ __forceinline__ T face_sum(T kc, T pc, T kyp, T pyp, T kym, T pym, T kxp, T pxp,
-                                      T kxm, T pxm, T kzp, T pzp, T kzm, T pzm) {
-  T s = (kyp + kc) * (pyp - pc);
-  s = s - (kym + kc) * (pc - pym);
-  s = s + (kxp + kc) * (pxp - pc);
-  s = s - (kxm + kc) * (pc - pxm);
-  s = s + (kzp + kc) * (pzp - pc);
-  s = s - (kzm + kc) * (pc - pzm);
-  return s;
-}
-
 // Per-thread z-march over interior column (i, j), planes k0..k1.  Body is
 // called with (c, k, pc, pzm, pzp_eff, kc, kzm, kzp) where p's z-neighbours
 // already carry the ghost rule (RULE) or the stored ghosts (!RULE).
@@ -435,6 +421,7 @@ int status_of(int done) {
     case 2: return SBM_ERR_MAXIT;
     case 3: return SBM_ERR_NONFINITE;
     case 4: return SBM_ERR_BREAKDOWN;
+    case 5: return SBM_ERR_TIMEOUT;
     default: return SBM_ERR_STATE;
   }
 }
@@ -890,6 +877,16 @@ int flat_blocks(int64_t items) {
 
 }  // namespace
 
+// sbm_tma.cu
+struct TmaPlan;
+bool tma_supported(const Geo& g32);
+int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, const float* hk,
+             const float* iv, const float* dg, int pc, int form, TmaPlan* plan);
+int tma_plan_size(void);
+int tma_init();
+void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
+                double* partials, CgState* st, cudaStream_t s);
+
 int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   if (sp.stop_rule != SBM_STOP_REL_RES) return SBM_ERR_ARG;
   int rc = ensure_fp32_work(ctx);
@@ -961,11 +958,23 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
     }
 #undef SBM_REL
   };
+  // TMA-staged stencil when the layout allows it (tensor maps of this solve)
+  const bool use_tma = (vec == 4) && !ctx->no_tma && tma_supported(g32);
+  std::vector<unsigned char> plan_buf(use_tma ? tma_plan_size() : 1);
+  TmaPlan* plan = reinterpret_cast<TmaPlan*>(plan_buf.data());
+  if (use_tma) {
+    if ((rc = tma_init())) return rc;
+    if ((rc = tma_plan(g32, ctx->r32, ctx->p32, ctx->rold32, ctx->hk32, ctx->z32, ctx->dg32,
+                       pc ? 1 : 0, sp.form, plan)))
+      return rc;
+  }
   // one iteration reading direction buffer `in` and writing `out`
   auto iter = [&](cudaStream_t s2, const float* in, float* out) {
 #define SBM_AD(F, P)                                                                           \
   do {                                                                                         \
-    if (vec == 4)                                                                              \
+    if (use_tma)                                                                               \
+      tma_launch(*plan, in == pbuf[0], op32, out, q32, ctx->partials, ctx->st, s2);            \
+    else if (vec == 4)                                                                         \
       k32v_apply_dir<F, P><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, r32, in, iv32, out, q32, \
                                                    ctx->partials, ctx->st);                    \
     else                                                                                       \
@@ -1001,8 +1010,8 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   const std::string key =
-      key_of("mixrel2", hk32, dg32, x32, r32, pbuf[0], pbuf[1], iv32, sp.scale, sp.form, sp.bcx0,
-             sp.bcx1, vec * 16 + zc32, pc, sh64.zc, chunk_len(ctx));
+      key_of(use_tma ? "mixrel2-tma" : "mixrel2", hk32, dg32, x32, r32, pbuf[0], pbuf[1], iv32,
+             sp.scale, sp.form, sp.bcx0, sp.bcx1, vec * 16 + zc32, pc, sh64.zc, chunk_len(ctx));
   cudaGraphExec_t ex = nullptr;
   int nodes = 0;
   rc = capture_graph(ctx, key, 6, body, &ex, &nodes);
@@ -1067,8 +1076,19 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
   float* q32 = ctx->q32 + kOff32;
   float* x32 = ctx->x32 + kOff32;
   float* iv = ctx->z32 + kOff32;
+  const bool use_tma = (vec == 4) && !ctx->no_tma && tma_supported(g32);
+  std::vector<unsigned char> plan_buf(use_tma ? tma_plan_size() : 1);
+  TmaPlan* plan = reinterpret_cast<TmaPlan*>(plan_buf.data());
+  if (use_tma && which == 0) {
+    int rc = tma_init();
+    if (!rc) rc = tma_plan(g32, ctx->r32, ctx->p32, ctx->rold32, ctx->hk32, ctx->z32, ctx->dg32,
+                           pc ? 1 : 0, op32.form, plan);
+    if (rc) return rc;
+  }
   auto launch = [&]() {
-    if (which == 0) {
+    if (which == 0 && use_tma) {
+      tma_launch(*plan, true, op32, pb, q32, ctx->partials, ctx->st32, s);
+    } else if (which == 0) {
       if (vec == 4) {
         if (op32.form == 0) {
           if (pc) k32v_apply_dir<0, true><<<vgrid, 256, 0, s>>>(op32, nchunk, zc32, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);

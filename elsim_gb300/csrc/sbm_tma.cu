@@ -1,0 +1,348 @@
+// sbm_tma.cu -- TMA-staged FP32 direction + stencil kernel of the mixed solver.
+//
+// One CTA owns a 64 (y) x 8 (x) tile of the FP32 layout and marches 16 z
+// planes.  For every plane it brings in, with cp.async.bulk.tensor (TMA),
+// a 72 x 10 box (tile + halo, x-start rounded down to a 16-byte boundary)
+// of each input array: r, p_old, hk and, when present, invd (Jacobi) and the
+// CnE diagonal.  Planes sit in a 6-stage shared-memory ring, each stage with
+// its mbarrier (expect_tx / complete_tx); the single producer thread keeps
+// three planes in flight ahead of the plane being computed.  p_new =
+// z + beta p_old is formed once per staged cell into a 3-plane ring, and the
+// 7-point SBM operator reads p_new and hk from shared memory.  Each thread
+// produces four y-consecutive voxels (float4 stores of p_new and q).
+//
+// Every mbarrier wait is bounded; on expiry the CTA records done = 5 in the
+// solver state (reported as SBM_ERR_TIMEOUT), waits (bounded) for its own
+// copies in flight and returns.  Loads use only this CTA's shared memory: no
+// cluster multicast.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+
+#include "sbm_internal.cuh"
+
+namespace sbm {
+
+namespace {
+
+constexpr int TX = 64;               // tile extent along y (voxels)
+constexpr int TY = 8;                // tile extent along x (rows)
+constexpr int NTH = TX / 4 * TY;     // 128 threads, one float4 each
+constexpr int BOXX = TX + 8;         // 72 floats: x-start rounded down to 4
+constexpr int BOXY = TY + 2;         // 10 rows
+constexpr int PLANE = BOXX * BOXY;   // 720 floats
+constexpr int PLANE_BYTES = PLANE * 4;
+constexpr int SLOT = 2944;           // bytes per array-plane, 128-byte multiple
+constexpr int NS = 6;                // stages in the ring
+constexpr int ZCT = 16;              // z planes per CTA
+constexpr unsigned kSpin = 1u << 20;  // try_wait attempts before giving up (about a second)
+
+struct TmaMaps {
+  CUtensorMap r, p, hk, iv, dg;
+};
+
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(saddr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity) {
+  for (unsigned n = 0; n < kSpin; ++n)
+    if (mbar_try_wait(b, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(saddr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(saddr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ float4 lds4(const float* p) {
+  return *reinterpret_cast<const float4*>(p);
+}
+
+template <int FORM, bool PC>
+__global__ void __launch_bounds__(NTH)
+    k32t_apply_dir(const __grid_constant__ TmaMaps maps, OpArgs<float> op, float* __restrict__ pnew,
+                   float* __restrict__ q, double* partials, CgState* st) {
+  constexpr int NA = 3 + (PC ? 1 : 0) + (FORM == 1 ? 1 : 0);
+  constexpr int A_IV = 3, A_DG = 3 + (PC ? 1 : 0);
+  extern __shared__ __align__(128) unsigned char smem[];
+  if (st->done) return;
+  const Geo g = op.g;
+  const float beta = (float)st->beta;
+  const int tid = threadIdx.x;
+  const int ntile_y = (g.ny + TX - 1) / TX;
+  const int tyb = blockIdx.x % ntile_y;
+  const int txb = blockIdx.x / ntile_y;
+  const int k0 = blockIdx.y * ZCT + 1;
+  const int k1 = min(k0 + ZCT - 1, g.nz);
+  const int nplanes = k1 - k0 + 3;  // planes k0-1 .. k1+1
+  const int x0 = TX * tyb;          // box start in buffer floats (= i0 - 1 + kOff32 - 3)
+  const int y0 = TY * txb;          // box start row (= j0 - 1)
+  const int row = tid / (TX / 4) + 1;
+  const int col = 4 + 4 * (tid % (TX / 4));
+  const int i0 = TX * tyb + (col - 4) + 1;
+  const int j = TY * txb + row;
+  const bool active = (i0 <= g.ny) && (j <= g.nx);
+  auto stage = [&](int s, int a) -> float* {
+    return reinterpret_cast<float*>(smem + (size_t)(s * NA + a) * SLOT);
+  };
+  float* const pring = reinterpret_cast<float*>(smem + (size_t)NS * NA * SLOT);
+  uint64_t* const bar = reinterpret_cast<uint64_t*>(smem + (size_t)(NS * NA + 3) * SLOT);
+  if (tid == 0) {
+    for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int m) {
+    const int s = m % NS;
+    const int z = k0 - 1 + m;
+    mbar_expect_tx(&bar[s], NA * PLANE_BYTES);
+    tma_load_3d(stage(s, 0), &maps.r, x0, y0, z, &bar[s]);
+    tma_load_3d(stage(s, 1), &maps.p, x0, y0, z, &bar[s]);
+    tma_load_3d(stage(s, 2), &maps.hk, x0, y0, z, &bar[s]);
+    if (PC) tma_load_3d(stage(s, A_IV), &maps.iv, x0, y0, z, &bar[s]);
+    if (FORM == 1) tma_load_3d(stage(s, A_DG), &maps.dg, x0, y0, z, &bar[s]);
+  };
+  int issued = 0;
+  if (tid == 0) {
+    for (; issued < NS && issued < nplanes; ++issued) issue(issued);
+  }
+  bool ok = true;
+  auto wait_plane = [&](int m) { return mbar_wait_bounded(&bar[m % NS], (unsigned)((m / NS) & 1)); };
+  // p_new of plane m for every staged cell (tile + halo) into ring slot m % 3
+  auto make_pn = [&](int m) {
+    const float4* R = reinterpret_cast<const float4*>(stage(m % NS, 0));
+    const float4* P = reinterpret_cast<const float4*>(stage(m % NS, 1));
+    const float4* IV = reinterpret_cast<const float4*>(stage(m % NS, PC ? A_IV : 0));
+    float4* D = reinterpret_cast<float4*>(pring + (m % 3) * (SLOT / 4));
+    for (int v = tid; v < PLANE / 4; v += NTH) {
+      const float4 rv = R[v], pv = P[v];
+      float4 z = rv;
+      if (PC) {
+        const float4 d = IV[v];
+        z = make_float4(d.x * rv.x, d.y * rv.y, d.z * rv.z, d.w * rv.w);
+      }
+      D[v] = make_float4(z.x + beta * pv.x, z.y + beta * pv.y, z.z + beta * pv.z,
+                         z.w + beta * pv.w);
+    }
+  };
+  ok = wait_plane(0);
+  if (ok) make_pn(0);
+  if (ok) ok = wait_plane(1);
+  if (ok) make_pn(1);
+  float acc = 0.f;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int o = row * BOXX + col;
+  for (int mk = 1; ok && mk <= nplanes - 2; ++mk) {
+    ok = wait_plane(mk + 1);
+    if (!ok) break;
+    make_pn(mk + 1);
+    __syncthreads();
+    const int k = k0 - 1 + mk;
+    if (active) {
+      const float* PM = pring + ((mk - 1) % 3) * (SLOT / 4);
+      const float* PCc = pring + (mk % 3) * (SLOT / 4);
+      const float* PP = pring + ((mk + 1) % 3) * (SLOT / 4);
+      const float* HM = stage((mk - 1) % NS, 2);
+      const float* HC = stage(mk % NS, 2);
+      const float* HP = stage((mk + 1) % NS, 2);
+      const float4 pc = lds4(PCc + o);
+      float4 pxm = lds4(PCc + o - BOXX), pxp = lds4(PCc + o + BOXX);
+      float4 pzm = lds4(PM + o), pzp = lds4(PP + o);
+      float pl = PCc[o - 1], pr = PCc[o + 4];
+      const float4 kc = lds4(HC + o), kxm = lds4(HC + o - BOXX), kxp = lds4(HC + o + BOXX);
+      const float4 kzm = lds4(HM + o), kzp = lds4(HP + o);
+      const float kl = HC[o - 1], kr = HC[o + 4];
+      if (i0 == 1) pl = pc.x;
+      if (i0 + 3 == g.ny) pr = pc.w;
+      if (j == 1) pxm = op.bcx0 ? zero4 : pc;
+      if (j == g.nx) pxp = op.bcx1 ? zero4 : pc;
+      if (k == 1) pzm = pc;
+      if (k == g.nz) pzp = pc;
+      const float pa[6] = {pl, pc.x, pc.y, pc.z, pc.w, pr};
+      const float ka[6] = {kl, kc.x, kc.y, kc.z, kc.w, kr};
+      const float pxa[4] = {pxm.x, pxm.y, pxm.z, pxm.w}, pxb[4] = {pxp.x, pxp.y, pxp.z, pxp.w};
+      const float kxa[4] = {kxm.x, kxm.y, kxm.z, kxm.w}, kxb[4] = {kxp.x, kxp.y, kxp.z, kxp.w};
+      const float pza[4] = {pzm.x, pzm.y, pzm.z, pzm.w}, pzb[4] = {pzp.x, pzp.y, pzp.z, pzp.w};
+      const float kza[4] = {kzm.x, kzm.y, kzm.z, kzm.w}, kzb[4] = {kzp.x, kzp.y, kzp.z, kzp.w};
+      float dg[4] = {0.f, 0.f, 0.f, 0.f};
+      if (FORM == 1) {
+        const float4 d4 = lds4(stage(mk % NS, A_DG) + o);
+        dg[0] = d4.x; dg[1] = d4.y; dg[2] = d4.z; dg[3] = d4.w;
+      }
+      float qa[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float s = face_sum<float>(ka[e + 1], pa[e + 1], ka[e + 2], pa[e + 2], ka[e], pa[e],
+                                        kxb[e], pxb[e], kxa[e], pxa[e], kzb[e], pzb[e], kza[e],
+                                        pza[e]);
+        qa[e] = (FORM == 0) ? op.scale * s : dg[e] * pa[e + 1] - op.scale * s;
+      }
+      const int64_t c = g.ix(i0, j, k);
+      *reinterpret_cast<float4*>(pnew + c) = pc;
+      *reinterpret_cast<float4*>(q + c) = make_float4(qa[0], qa[1], qa[2], qa[3]);
+      acc += (pa[1] * qa[0] + pa[2] * qa[1]) + (pa[3] * qa[2] + pa[4] * qa[3]);
+    }
+    __syncthreads();
+    if (tid == 0 && mk - 1 + NS < nplanes) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(mk - 1 + NS);
+      ++issued;
+    }
+  }
+  // Every thread must agree before the reduction: a CTA whose wait expired
+  // records the error and drains its own copies in flight.
+  const int failed = __syncthreads_or(ok ? 0 : 1);
+  if (failed) {
+    if (tid == 0) {
+      st->done = 5;
+      for (int s = 0; s < NS; ++s) {
+        // a stage is drained once its barrier has completed every phase
+        // that was armed; bounded in any case
+        for (unsigned n = 0; n < kSpin && !mbar_try_wait(&bar[s], 0) && !mbar_try_wait(&bar[s], 1);
+             ++n) {
+        }
+      }
+    }
+    __syncthreads();
+    acc = 0.f;
+  }
+  double v[1] = {(double)acc}, tot[1];
+  if (grid_reduce<1>(v, partials, &st->counter[0], tot)) {
+    if (threadIdx.x == 0) {
+      const double pq = tot[0];
+      st->pq = pq;
+      st->alpha = st->rho / pq;
+      if (st->done == 0) {
+        if (pq == 0.0) st->done = 4;
+        else if (!isfinite(pq)) st->done = 3;
+      }
+    }
+  }
+}
+
+size_t smem_bytes(int pc, int form) {
+  const int na = 3 + pc + form;
+  return (size_t)(NS * na + 3) * SLOT + NS * sizeof(uint64_t);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 3-D map over an FP32-layout buffer (base = allocation start, 16-byte aligned).
+bool make_map(CUtensorMap* m, const float* base, const Geo& g32) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)g32.sx, (cuuint64_t)(g32.nx + 2), (cuuint64_t)(g32.nz + 2)};
+  cuuint64_t strides[2] = {(cuuint64_t)g32.sx * 4, (cuuint64_t)g32.sz * 4};
+  cuuint32_t box[3] = {BOXX, BOXY, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims,
+                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// The TMA path needs rows of a multiple of 4 voxels (float4 output) and
+// 16-byte row strides (always true of the FP32 layout).
+bool tma_supported(const Geo& g32) { return (g32.ny % 4) == 0 && (g32.sx % 4) == 0 && encode_fn(); }
+
+struct TmaPlan {
+  TmaMaps fwd, bwd;  // fwd reads p buffer a, bwd reads buffer b
+  dim3 grid;
+  size_t smem;
+  int pc, form;
+};
+
+// Builds the tensor maps of one mixed solve.  Buffers are allocation bases
+// (the FP32 layout's element (i,j,k) sits at base + kOff32 + g32.ix(i,j,k)).
+int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, const float* hk,
+             const float* iv, const float* dg, int pc, int form, TmaPlan* plan) {
+  memset(plan, 0, sizeof(*plan));
+  if (!make_map(&plan->fwd.r, r, g32) || !make_map(&plan->fwd.p, pa, g32) ||
+      !make_map(&plan->fwd.hk, hk, g32) || (pc && !make_map(&plan->fwd.iv, iv, g32)) ||
+      (form && !make_map(&plan->fwd.dg, dg, g32)))
+    return SBM_ERR_STATE;
+  plan->bwd = plan->fwd;
+  if (!make_map(&plan->bwd.p, pb, g32)) return SBM_ERR_STATE;
+  const int ntile = ((g32.ny + TX - 1) / TX) * ((g32.nx + TY - 1) / TY);
+  plan->grid = dim3((unsigned)ntile, (unsigned)((g32.nz + ZCT - 1) / ZCT));
+  plan->pc = pc;
+  plan->form = form;
+  plan->smem = smem_bytes(pc, form);
+  return SBM_OK;
+}
+
+int tma_plan_size(void) { return (int)sizeof(TmaPlan); }
+
+// Sets the dynamic shared-memory limit of the four instantiations (once).
+int tma_init() {
+  static bool done = false;
+  if (done) return SBM_OK;
+  SBM_CUDA_TRY(cudaFuncSetAttribute(k32t_apply_dir<0, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(0, 0)));
+  SBM_CUDA_TRY(cudaFuncSetAttribute(k32t_apply_dir<0, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(1, 0)));
+  SBM_CUDA_TRY(cudaFuncSetAttribute(k32t_apply_dir<1, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(0, 1)));
+  SBM_CUDA_TRY(cudaFuncSetAttribute(k32t_apply_dir<1, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(1, 1)));
+  done = true;
+  return SBM_OK;
+}
+
+// One launch: reads p from buffer a (fwd) or b (!fwd), writes p_new to pnew.
+void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
+                double* partials, CgState* st, cudaStream_t s) {
+  const TmaMaps& m = fwd ? plan.fwd : plan.bwd;
+  if (plan.form == 0) {
+    if (plan.pc) k32t_apply_dir<0, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, pnew, q, partials, st);
+    else k32t_apply_dir<0, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, pnew, q, partials, st);
+  } else {
+    if (plan.pc) k32t_apply_dir<1, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, pnew, q, partials, st);
+    else k32t_apply_dir<1, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, pnew, q, partials, st);
+  }
+}
+
+}  // namespace sbm

@@ -30,8 +30,9 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libsbm_gb300.so"
 
 # status codes (include/sbm_capi.h)
-OK, ERR_ARG, ERR_CUDA, ERR_MAXIT, ERR_NONFINITE, ERR_BREAKDOWN, ERR_NOMEM, ERR_STATE = (
-    0, -1, -2, -3, -4, -5, -6, -7)
+OK, ERR_ARG, ERR_CUDA, ERR_MAXIT, ERR_NONFINITE, ERR_BREAKDOWN, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT = (
+    0, -1, -2, -3, -4, -5, -6, -7, -8)
+TUNE_NO_TMA = 1
 BC_COPY, BC_ZERO = 0, 1
 OP_CNE, OP_PHP, OP_PHE, OP_GENERIC = 0, 1, 2, 3
 STOP_REF_UPDATE, STOP_REF_RESID, STOP_REL_RES = 0, 1, 2
@@ -45,7 +46,8 @@ TBL_MAX = 128
 
 _ERRNAMES = {ERR_ARG: "bad argument", ERR_CUDA: "CUDA error", ERR_MAXIT: "iteration cap",
              ERR_NONFINITE: "non-finite value", ERR_BREAKDOWN: "CG breakdown",
-             ERR_NOMEM: "out of device memory", ERR_STATE: "invalid state"}
+             ERR_NOMEM: "out of device memory", ERR_STATE: "invalid state",
+             ERR_TIMEOUT: "device wait expired"}
 
 
 class SbmError(RuntimeError):
@@ -222,10 +224,11 @@ class Context:
         self.params = params
         _check(self.lib.sbm_ctx_set_params(self._h, C.byref(params)), "sbm_ctx_set_params")
 
-    def set_tuning(self, zc64=0, zc32=0, chunk=0, delta=0.0) -> None:
-        """Launch-shape knobs (0 = built-in) and the reliable-update factor."""
-        _check(self.lib.sbm_ctx_set_tuning(self._h, zc64, zc32, chunk, delta, 0),
-               "sbm_ctx_set_tuning")
+    def set_tuning(self, zc64=0, zc32=0, chunk=0, delta=0.0, no_tma=False) -> None:
+        """Launch-shape knobs (0 = built-in), the reliable-update factor and
+        the choice of the register-tiled instead of the TMA-staged stencil."""
+        _check(self.lib.sbm_ctx_set_tuning(self._h, zc64, zc32, chunk, delta,
+                                           TUNE_NO_TMA if no_tma else 0), "sbm_ctx_set_tuning")
 
     def bench_kernel(self, which: int, reps: int = 20) -> tuple[float, float]:
         """(ms per launch, algorithmic bytes per launch) of a solver kernel."""

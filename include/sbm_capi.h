@@ -38,6 +38,7 @@ extern "C" {
 #define SBM_ERR_BREAKDOWN     -5   /* p.Ap == 0 in CG                          */
 #define SBM_ERR_NOMEM         -6   /* device allocation failed                 */
 #define SBM_ERR_STATE         -7   /* call made in a state that forbids it     */
+#define SBM_ERR_TIMEOUT       -8   /* a bounded device-side wait expired       */
 
 /* ---------------------------------------------------------- enumerations */
 /* Ghost rule applied to the CG search direction at an x face
@@ -151,9 +152,10 @@ int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p);
  * per thread of the FP64 / FP32 stencil kernels, CG iterations per captured
  * graph chunk, and `delta` of the mixed solver (its FP64 residual is
  * recomputed whenever the FP32 residual norm has fallen by this factor;
- * default 0.1).  `reserved` must be 0.  No counterpart in the reference. */
-int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta,
-                       int reserved);
+ * default 0.1).  flags bit 0 (SBM_TUNE_NO_TMA): use the register-tiled FP32
+ * stencil instead of the TMA-staged one.  No counterpart in the reference. */
+#define SBM_TUNE_NO_TMA 1
+int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta, int flags);
 /* The context's CUDA stream as an opaque handle (cudaStream_t). */
 int sbm_ctx_stream(sbm_ctx* ctx, void** stream);
 int sbm_ctx_sync(sbm_ctx* ctx);
