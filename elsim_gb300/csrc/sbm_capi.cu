@@ -308,30 +308,11 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, doubl
   sp.max_it = max_it;
   sp.rhs = ctx->f[SBM_F_RHS];
   const double idx2 = 1.0 / (ctx->p.dx * ctx->p.dx);
+  (void)g;
   if (op == SBM_OP_GENERIC) {
-    SBM_CUDA_TRY(launch_half(g, ctx->f[SBM_F_COEF], ctx->hk_gen, ctx->stream));
-    sp.hk64 = ctx->hk_gen;
-    sp.form = 0;
-    sp.scale = scale;
-    sp.bcx0 = bc_x0;
-    sp.bcx1 = bc_x1;
-    sp.x = ctx->f[SBM_F_X];
-    sp.w = ctx->f[SBM_F_WEIGHT];
-    sp.wsum = 1.0;
-    if (stop_rule != SBM_STOP_REL_RES) {
-      // sum of the weight over the interior (host side, once per call)
-      const size_t n = (size_t)g.nh;
-      double* hw = (double*)malloc(sizeof(double) * n);
-      if (!hw) return SBM_ERR_NOMEM;
-      int rc = sbm_download(ctx, SBM_F_WEIGHT, hw, 1);
-      double ws = 0.0;
-      for (int k = 1; k <= g.nz; ++k)
-        for (int j = 1; j <= g.nx; ++j)
-          for (int i = 1; i <= g.ny; ++i) ws += hw[g.ix(i, j, k)];
-      free(hw);
-      if (rc) return rc;
-      sp.wsum = ws;
-    }
+    int rc = generic_spec(ctx, bc_x0, bc_x1, scale, tol, max_it, stop_rule, precision, precond,
+                          &sp);
+    if (rc) return rc;
   } else {
     if (!ctx->hk_kap) return SBM_ERR_STATE;
     if (op == SBM_OP_CNE) {
@@ -362,6 +343,52 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, doubl
   if (ms) *ms = r.ms;
   return r.status;
 }
+
+}  // extern "C"
+
+namespace sbm {
+// Solve spec of the GENERIC operator (coefficient, unknown, right-hand side
+// and weight from the context's public fields); also halves the coefficient.
+int generic_spec(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, double tol, int max_it,
+                 int stop_rule, int precision, int precond, SolveSpec* out) {
+  const Geo& g = ctx->g;
+  SolveSpec sp{};
+  sp.op = SBM_OP_GENERIC;
+  sp.precision = precision;
+  sp.precond = precond;
+  sp.stop_rule = stop_rule;
+  sp.tol = tol;
+  sp.max_it = max_it;
+  sp.rhs = ctx->f[SBM_F_RHS];
+  SBM_CUDA_TRY(launch_half(g, ctx->f[SBM_F_COEF], ctx->hk_gen, ctx->stream));
+  sp.hk64 = ctx->hk_gen;
+  sp.form = 0;
+  sp.scale = scale;
+  sp.bcx0 = bc_x0;
+  sp.bcx1 = bc_x1;
+  sp.x = ctx->f[SBM_F_X];
+  sp.w = ctx->f[SBM_F_WEIGHT];
+  sp.wsum = 1.0;
+  if (stop_rule != SBM_STOP_REL_RES) {
+    // sum of the weight over the interior (host side, once per call)
+    const size_t n = (size_t)g.nh;
+    double* hw = (double*)malloc(sizeof(double) * n);
+    if (!hw) return SBM_ERR_NOMEM;
+    int rc = sbm_download(ctx, SBM_F_WEIGHT, hw, 1);
+    double ws = 0.0;
+    for (int k = 1; k <= g.nz; ++k)
+      for (int j = 1; j <= g.nx; ++j)
+        for (int i = 1; i <= g.ny; ++i) ws += hw[g.ix(i, j, k)];
+    free(hw);
+    if (rc) return rc;
+    sp.wsum = ws;
+  }
+  *out = sp;
+  return SBM_OK;
+}
+}  // namespace sbm
+
+extern "C" {
 
 int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
                      double* bytes_per_launch) {

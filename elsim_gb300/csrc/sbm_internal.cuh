@@ -302,7 +302,12 @@ struct sbm_ctx {
   double inner_tol = 0.0;
   int inner_max = 0;
   // CUDA graphs of captured CG chunks, keyed by solve signature
-  std::map<std::string, std::pair<cudaGraphExec_t, int>> graphs;
+  struct GraphRec {
+    cudaGraphExec_t exec;
+    cudaGraph_t graph;
+    int nodes;
+  };
+  std::map<std::string, GraphRec> graphs;
   // arguments of the last mixed solve, replayed by sbm_bench_kernel
   sbm::OpArgs<float> last_op32{};
   int last_pc = -1;
@@ -313,6 +318,15 @@ struct sbm_ctx {
 
 namespace sbm {
 int solve(sbm_ctx* ctx, const SolveSpec& spec, SolveResult* out);
+// Phases of a mixed-precision solve, shared with the batched driver:
+// begin launches the set-up kernels on the context stream and returns the
+// captured iteration-chunk graph; end folds the correction into x.
+int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex, cudaGraph_t* graph,
+                int* nodes);
+int mixed_end(sbm_ctx* ctx, const SolveSpec& sp, const CgState& fin, SolveResult* out);
+int status_of_done(int done);
+int generic_spec(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, double tol, int max_it,
+                 int stop_rule, int precision, int precond, SolveSpec* sp);
 int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double* bytes_per_launch);
 int ensure_fp32_work(sbm_ctx* ctx);
 void release_graphs(sbm_ctx* ctx);

@@ -357,8 +357,8 @@ int capture_graph(sbm_ctx* ctx, const std::string& key, int nodes_per_iter, Body
                   cudaGraphExec_t* exec, int* nodes) {
   auto it = ctx->graphs.find(key);
   if (it != ctx->graphs.end()) {
-    *exec = it->second.first;
-    *nodes = it->second.second;
+    *exec = it->second.exec;
+    *nodes = it->second.nodes;
     return SBM_OK;
   }
   const int len = chunk_len(ctx);
@@ -378,12 +378,12 @@ int capture_graph(sbm_ctx* ctx, const std::string& key, int nodes_per_iter, Body
   }
   cudaGraphExec_t ex = nullptr;
   e = cudaGraphInstantiate(&ex, graph, 0);
-  cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
     set_error("cudaGraphInstantiate", e);
     return SBM_ERR_CUDA;
   }
-  ctx->graphs[key] = {ex, nodes_per_iter * len};
+  ctx->graphs[key] = {ex, graph, nodes_per_iter * len};
   *exec = ex;
   *nodes = nodes_per_iter * len;
   return SBM_OK;
@@ -881,13 +881,14 @@ int flat_blocks(int64_t items) {
 struct TmaPlan;
 bool tma_supported(const Geo& g32);
 int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, const float* hk,
-             const float* iv, const float* dg, int pc, int form, TmaPlan* plan);
+             const float* iv, const float* dg, int pc, int form, int zct, TmaPlan* plan);
 int tma_plan_size(void);
 int tma_init();
 void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
                 double* partials, CgState* st, cudaStream_t s);
 
-int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
+int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cudaGraph_t* graph_out,
+                int* nodes_out) {
   if (sp.stop_rule != SBM_STOP_REL_RES) return SBM_ERR_ARG;
   int rc = ensure_fp32_work(ctx);
   if (rc) return rc;
@@ -965,7 +966,7 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   if (use_tma) {
     if ((rc = tma_init())) return rc;
     if ((rc = tma_plan(g32, ctx->r32, ctx->p32, ctx->rold32, ctx->hk32, ctx->z32, ctx->dg32,
-                       pc ? 1 : 0, sp.form, plan)))
+                       pc ? 1 : 0, sp.form, ctx->zc32, plan)))
       return rc;
   }
   // one iteration reading direction buffer `in` and writing `out`
@@ -1018,9 +1019,18 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   if (rc) return rc;
   ctx->last_op32 = op32;
   ctx->last_pc = pc ? 1 : 0;
-  CgState fin;
-  rc = run_chunks(ctx, ex, nodes, ctx->st, ctx->h_st, &fin);
-  if (rc) return rc;
+  *ex_out = ex;
+  *nodes_out = nodes;
+  *graph_out = ctx->graphs[key].graph;
+  return SBM_OK;
+}
+
+int mixed_end(sbm_ctx* ctx, const SolveSpec& sp, const CgState& fin, SolveResult* out) {
+  const Geo& g = ctx->g;
+  const Geo& g32 = ctx->g32;
+  cudaStream_t s = ctx->stream;
+  const Shape sh64 = stencil_shape(g, pick_zc(g, ctx->zc64));
+  float* const x32 = ctx->x32 + kOff32;
   // x += d64 + x32 (interior): the ghosts of x keep their Dirichlet / flux data.
   k_finish<<<sh64.grid, sh64.block, 0, s>>>(g, g32, sh64.zc, sp.x, ctx->d64, x32);
   SBM_LAUNCHED(1);
@@ -1035,6 +1045,18 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   out->ms = ms;
   out->status = status_of(fin.done);
   return SBM_OK;
+}
+
+int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
+  cudaGraphExec_t ex = nullptr;
+  cudaGraph_t graph = nullptr;
+  int nodes = 0;
+  int rc = mixed_begin(ctx, sp, &ex, &graph, &nodes);
+  if (rc) return rc;
+  CgState fin;
+  rc = run_chunks(ctx, ex, nodes, ctx->st, ctx->h_st, &fin);
+  if (rc) return rc;
+  return mixed_end(ctx, sp, fin, out);
 }
 
 
@@ -1082,7 +1104,7 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
   if (use_tma && which == 0) {
     int rc = tma_init();
     if (!rc) rc = tma_plan(g32, ctx->r32, ctx->p32, ctx->rold32, ctx->hk32, ctx->z32, ctx->dg32,
-                           pc ? 1 : 0, op32.form, plan);
+                           pc ? 1 : 0, op32.form, ctx->zc32, plan);
     if (rc) return rc;
   }
   auto launch = [&]() {
@@ -1138,8 +1160,13 @@ int solve(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
 }
 
 void release_graphs(sbm_ctx* ctx) {
-  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second.first);
+  for (auto& kv : ctx->graphs) {
+    cudaGraphExecDestroy(kv.second.exec);
+    cudaGraphDestroy(kv.second.graph);
+  }
   ctx->graphs.clear();
 }
+
+int status_of_done(int done) { return status_of(done); }
 
 }  // namespace sbm

@@ -1,15 +1,16 @@
 // sbm_tma.cu -- TMA-staged FP32 direction + stencil kernel of the mixed solver.
 //
-// One CTA owns a 64 (y) x 8 (x) tile of the FP32 layout and marches 16 z
-// planes.  For every plane it brings in, with cp.async.bulk.tensor (TMA),
+// One CTA owns a 64 (y) x 8 (x) tile of the FP32 layout and marches a
+// tunable number of z planes (16 by default).  For every plane it brings in, with cp.async.bulk.tensor (TMA),
 // a 72 x 10 box (tile + halo, x-start rounded down to a 16-byte boundary)
 // of each input array: r, p_old, hk and, when present, invd (Jacobi) and the
 // CnE diagonal.  Planes sit in a 6-stage shared-memory ring, each stage with
 // its mbarrier (expect_tx / complete_tx); the single producer thread keeps
-// three planes in flight ahead of the plane being computed.  p_new =
-// z + beta p_old is formed once per staged cell into a 3-plane ring, and the
-// 7-point SBM operator reads p_new and hk from shared memory.  Each thread
-// produces four y-consecutive voxels (float4 stores of p_new and q).
+// two planes in flight ahead of the three being used.  p_new = z + beta p_old
+// is formed once per staged cell, in place over p_old, and the 7-point SBM
+// operator reads p_new and hk from shared memory (y-neighbours by warp
+// shuffle).  Each thread produces four y-consecutive voxels (float4 stores
+// of p_new and q).  One block barrier per plane.
 //
 // Every mbarrier wait is bounded; on expiry the CTA records done = 5 in the
 // solver state (reported as SBM_ERR_TIMEOUT), waits (bounded) for its own
@@ -88,33 +89,35 @@ __device__ __forceinline__ float4 lds4(const float* p) {
 
 template <int FORM, bool PC>
 __global__ void __launch_bounds__(NTH)
-    k32t_apply_dir(const __grid_constant__ TmaMaps maps, OpArgs<float> op, float* __restrict__ pnew,
-                   float* __restrict__ q, double* partials, CgState* st) {
+    k32t_apply_dir(const __grid_constant__ TmaMaps maps, OpArgs<float> op, int zct,
+                   float* __restrict__ pnew, float* __restrict__ q, double* partials,
+                   CgState* st) {
   constexpr int NA = 3 + (PC ? 1 : 0) + (FORM == 1 ? 1 : 0);
   constexpr int A_IV = 3, A_DG = 3 + (PC ? 1 : 0);
   extern __shared__ __align__(128) unsigned char smem[];
   if (st->done) return;
   const Geo g = op.g;
   const float beta = (float)st->beta;
+  const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x;
   const int ntile_y = (g.ny + TX - 1) / TX;
   const int tyb = blockIdx.x % ntile_y;
   const int txb = blockIdx.x / ntile_y;
-  const int k0 = blockIdx.y * ZCT + 1;
-  const int k1 = min(k0 + ZCT - 1, g.nz);
+  const int k0 = blockIdx.y * zct + 1;
+  const int k1 = min(k0 + zct - 1, g.nz);
   const int nplanes = k1 - k0 + 3;  // planes k0-1 .. k1+1
-  const int x0 = TX * tyb;          // box start in buffer floats (= i0 - 1 + kOff32 - 3)
+  const int x0 = TX * tyb;          // box start in buffer floats
   const int y0 = TY * txb;          // box start row (= j0 - 1)
+  const int q4 = tid % (TX / 4);    // float4 chunk within the row (16 per row)
   const int row = tid / (TX / 4) + 1;
-  const int col = 4 + 4 * (tid % (TX / 4));
-  const int i0 = TX * tyb + (col - 4) + 1;
+  const int col = 4 + 4 * q4;
+  const int i0 = TX * tyb + 4 * q4 + 1;
   const int j = TY * txb + row;
   const bool active = (i0 <= g.ny) && (j <= g.nx);
   auto stage = [&](int s, int a) -> float* {
     return reinterpret_cast<float*>(smem + (size_t)(s * NA + a) * SLOT);
   };
-  float* const pring = reinterpret_cast<float*>(smem + (size_t)NS * NA * SLOT);
-  uint64_t* const bar = reinterpret_cast<uint64_t*>(smem + (size_t)(NS * NA + 3) * SLOT);
+  uint64_t* const bar = reinterpret_cast<uint64_t*>(smem + (size_t)NS * NA * SLOT);
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -131,18 +134,16 @@ __global__ void __launch_bounds__(NTH)
     if (PC) tma_load_3d(stage(s, A_IV), &maps.iv, x0, y0, z, &bar[s]);
     if (FORM == 1) tma_load_3d(stage(s, A_DG), &maps.dg, x0, y0, z, &bar[s]);
   };
-  int issued = 0;
   if (tid == 0) {
-    for (; issued < NS && issued < nplanes; ++issued) issue(issued);
+    for (int m = 0; m < NS && m < nplanes; ++m) issue(m);
   }
-  bool ok = true;
   auto wait_plane = [&](int m) { return mbar_wait_bounded(&bar[m % NS], (unsigned)((m / NS) & 1)); };
-  // p_new of plane m for every staged cell (tile + halo) into ring slot m % 3
+  // p_new = z + beta p_old for every staged cell of plane m, written over
+  // p_old in place (stage array 1)
   auto make_pn = [&](int m) {
     const float4* R = reinterpret_cast<const float4*>(stage(m % NS, 0));
-    const float4* P = reinterpret_cast<const float4*>(stage(m % NS, 1));
+    float4* P = reinterpret_cast<float4*>(stage(m % NS, 1));
     const float4* IV = reinterpret_cast<const float4*>(stage(m % NS, PC ? A_IV : 0));
-    float4* D = reinterpret_cast<float4*>(pring + (m % 3) * (SLOT / 4));
     for (int v = tid; v < PLANE / 4; v += NTH) {
       const float4 rv = R[v], pv = P[v];
       float4 z = rv;
@@ -150,37 +151,57 @@ __global__ void __launch_bounds__(NTH)
         const float4 d = IV[v];
         z = make_float4(d.x * rv.x, d.y * rv.y, d.z * rv.z, d.w * rv.w);
       }
-      D[v] = make_float4(z.x + beta * pv.x, z.y + beta * pv.y, z.z + beta * pv.z,
+      P[v] = make_float4(z.x + beta * pv.x, z.y + beta * pv.y, z.z + beta * pv.z,
                          z.w + beta * pv.w);
     }
   };
-  ok = wait_plane(0);
+  bool ok = wait_plane(0);
   if (ok) make_pn(0);
   if (ok) ok = wait_plane(1);
   if (ok) make_pn(1);
   float acc = 0.f;
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   const int o = row * BOXX + col;
-  for (int mk = 1; ok && mk <= nplanes - 2; ++mk) {
-    ok = wait_plane(mk + 1);
-    if (!ok) break;
-    make_pn(mk + 1);
-    __syncthreads();
+  for (int mk = 1; mk <= nplanes - 2; ++mk) {
+    const bool w = ok && wait_plane(mk + 1);
+    if (w) make_pn(mk + 1);
+    // one barrier per plane: p_new of mk+1 is complete, and every thread has
+    // finished step mk-1, so the stage of plane mk-2 can be refilled.  The
+    // barrier also makes the give-up decision of the bounded waits uniform.
+    if (!__syncthreads_and(w)) {
+      ok = false;
+      break;
+    }
+    if (tid == 0 && mk >= 2 && mk - 2 + NS < nplanes) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(mk - 2 + NS);
+    }
     const int k = k0 - 1 + mk;
+    const float* PM = stage((mk - 1) % NS, 1);
+    const float* PCc = stage(mk % NS, 1);
+    const float* PP = stage((mk + 1) % NS, 1);
+    const float* HM = stage((mk - 1) % NS, 2);
+    const float* HC = stage(mk % NS, 2);
+    const float* HP = stage((mk + 1) % NS, 2);
+    const float4 pc = lds4(PCc + o);
+    const float4 kc = lds4(HC + o);
+    // y-neighbours from the adjacent chunk of the same row (lane +-1 within
+    // the 16 lanes of the row), scalar loads only at the row's ends
+    float pl = __shfl_up_sync(FULL, pc.w, 1), kl = __shfl_up_sync(FULL, kc.w, 1);
+    float pr = __shfl_down_sync(FULL, pc.x, 1), kr = __shfl_down_sync(FULL, kc.x, 1);
+    if (q4 == 0) {
+      pl = PCc[o - 1];
+      kl = HC[o - 1];
+    }
+    if (q4 == TX / 4 - 1) {
+      pr = PCc[o + 4];
+      kr = HC[o + 4];
+    }
     if (active) {
-      const float* PM = pring + ((mk - 1) % 3) * (SLOT / 4);
-      const float* PCc = pring + (mk % 3) * (SLOT / 4);
-      const float* PP = pring + ((mk + 1) % 3) * (SLOT / 4);
-      const float* HM = stage((mk - 1) % NS, 2);
-      const float* HC = stage(mk % NS, 2);
-      const float* HP = stage((mk + 1) % NS, 2);
-      const float4 pc = lds4(PCc + o);
       float4 pxm = lds4(PCc + o - BOXX), pxp = lds4(PCc + o + BOXX);
       float4 pzm = lds4(PM + o), pzp = lds4(PP + o);
-      float pl = PCc[o - 1], pr = PCc[o + 4];
-      const float4 kc = lds4(HC + o), kxm = lds4(HC + o - BOXX), kxp = lds4(HC + o + BOXX);
+      const float4 kxm = lds4(HC + o - BOXX), kxp = lds4(HC + o + BOXX);
       const float4 kzm = lds4(HM + o), kzp = lds4(HP + o);
-      const float kl = HC[o - 1], kr = HC[o + 4];
       if (i0 == 1) pl = pc.x;
       if (i0 + 3 == g.ny) pr = pc.w;
       if (j == 1) pxm = op.bcx0 ? zero4 : pc;
@@ -211,12 +232,6 @@ __global__ void __launch_bounds__(NTH)
       *reinterpret_cast<float4*>(q + c) = make_float4(qa[0], qa[1], qa[2], qa[3]);
       acc += (pa[1] * qa[0] + pa[2] * qa[1]) + (pa[3] * qa[2] + pa[4] * qa[3]);
     }
-    __syncthreads();
-    if (tid == 0 && mk - 1 + NS < nplanes) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(mk - 1 + NS);
-      ++issued;
-    }
   }
   // Every thread must agree before the reduction: a CTA whose wait expired
   // records the error and drains its own copies in flight.
@@ -225,8 +240,6 @@ __global__ void __launch_bounds__(NTH)
     if (tid == 0) {
       st->done = 5;
       for (int s = 0; s < NS; ++s) {
-        // a stage is drained once its barrier has completed every phase
-        // that was armed; bounded in any case
         for (unsigned n = 0; n < kSpin && !mbar_try_wait(&bar[s], 0) && !mbar_try_wait(&bar[s], 1);
              ++n) {
         }
@@ -251,7 +264,7 @@ __global__ void __launch_bounds__(NTH)
 
 size_t smem_bytes(int pc, int form) {
   const int na = 3 + pc + form;
-  return (size_t)(NS * na + 3) * SLOT + NS * sizeof(uint64_t);
+  return (size_t)NS * na * SLOT + NS * sizeof(uint64_t);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -292,13 +305,13 @@ struct TmaPlan {
   TmaMaps fwd, bwd;  // fwd reads p buffer a, bwd reads buffer b
   dim3 grid;
   size_t smem;
-  int pc, form;
+  int pc, form, zct;
 };
 
 // Builds the tensor maps of one mixed solve.  Buffers are allocation bases
 // (the FP32 layout's element (i,j,k) sits at base + kOff32 + g32.ix(i,j,k)).
 int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, const float* hk,
-             const float* iv, const float* dg, int pc, int form, TmaPlan* plan) {
+             const float* iv, const float* dg, int pc, int form, int zct, TmaPlan* plan) {
   memset(plan, 0, sizeof(*plan));
   if (!make_map(&plan->fwd.r, r, g32) || !make_map(&plan->fwd.p, pa, g32) ||
       !make_map(&plan->fwd.hk, hk, g32) || (pc && !make_map(&plan->fwd.iv, iv, g32)) ||
@@ -307,7 +320,9 @@ int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, c
   plan->bwd = plan->fwd;
   if (!make_map(&plan->bwd.p, pb, g32)) return SBM_ERR_STATE;
   const int ntile = ((g32.ny + TX - 1) / TX) * ((g32.nx + TY - 1) / TY);
-  plan->grid = dim3((unsigned)ntile, (unsigned)((g32.nz + ZCT - 1) / ZCT));
+  if (zct < 1) zct = ZCT;
+  plan->zct = zct;
+  plan->grid = dim3((unsigned)ntile, (unsigned)((g32.nz + zct - 1) / zct));
   plan->pc = pc;
   plan->form = form;
   plan->smem = smem_bytes(pc, form);
@@ -337,11 +352,11 @@ void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* p
                 double* partials, CgState* st, cudaStream_t s) {
   const TmaMaps& m = fwd ? plan.fwd : plan.bwd;
   if (plan.form == 0) {
-    if (plan.pc) k32t_apply_dir<0, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, pnew, q, partials, st);
-    else k32t_apply_dir<0, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, pnew, q, partials, st);
+    if (plan.pc) k32t_apply_dir<0, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
+    else k32t_apply_dir<0, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
   } else {
-    if (plan.pc) k32t_apply_dir<1, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, pnew, q, partials, st);
-    else k32t_apply_dir<1, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, pnew, q, partials, st);
+    if (plan.pc) k32t_apply_dir<1, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
+    else k32t_apply_dir<1, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
   }
 }
 

@@ -134,6 +134,8 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_cne_step": (C.c_int, [vp, C.c_int, C.c_double, C.c_int, C.POINTER(Scalars)]),
         "sbm_bv_update": (C.c_int, [vp, C.c_int, C.POINTER(Scalars)]),
         "sbm_voltage_step": (C.c_int, [vp, C.c_double, C.c_double, C.POINTER(Scalars)]),
+        "sbm_batch_solve": (C.c_int, [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_double,
+                                      C.c_double, C.c_int, C.c_int, ip, dp, ip, fp]),
         "sbm_table_lookup": (C.c_int, [i64, C.c_int, dp, dp, dp, dp]),
         "sbm_redist": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]),
         "sbm_accdiff": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, C.c_int]),
@@ -314,6 +316,22 @@ class Context:
         s = Scalars()
         _check(self.lib.sbm_voltage_step(self._h, dt, vsr, C.byref(s)), "sbm_voltage_step")
         return s.as_dict()
+
+
+def batch_solve(contexts, bc_x0=BC_ZERO, bc_x1=BC_ZERO, scale=1.0, tol=1e-8, max_it=100000,
+                precond=PC_JACOBI) -> dict:
+    """Mixed-precision GENERIC solves of many independent contexts advanced
+    together by one CUDA-graph launch per round (sbm_batch_solve)."""
+    lib = load_library()
+    n = len(contexts)
+    hs = (C.c_void_p * n)(*[c._h for c in contexts])
+    it = (C.c_int * n)()
+    res = (C.c_double * n)()
+    stt = (C.c_int * n)()
+    ms = C.c_float(0)
+    _check(lib.sbm_batch_solve(hs, n, bc_x0, bc_x1, scale, tol, max_it, precond, it, res, stt,
+                               C.byref(ms)), "sbm_batch_solve")
+    return dict(iters=list(it), final_res=list(res), status=list(stt), ms=ms.value)
 
 
 # ------------------------------------------------------- stateless routines

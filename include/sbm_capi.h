@@ -196,6 +196,16 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale,
 int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
                      double* bytes_per_launch);
 
+/* Batched solves (no counterpart in the reference): n independent
+ * contexts, each loaded with a GENERIC problem (COEF, X, RHS), solved by the
+ * mixed-precision CG to rel-res tol together -- their iteration chunks are
+ * child graphs of one parent CUDA graph, so one launch advances every
+ * unconverged volume.  Per-volume iterations, final rel-res and status go to
+ * the n-element arrays; ms_total is the device time of the whole batch. */
+int sbm_batch_solve(sbm_ctx** ctxs, int n, int bc_x0, int bc_x1, double scale, double tol,
+                    int max_it, int precond, int* iters, double* final_res, int* status,
+                    float* ms_total);
+
 /* One electrochemical time step, the body of the reference's time loop
  * (SBMES:397-840) for a given dt, voltage-scan rate vsr and step index
  * iter: Cahn-Hilliard, CnE implicit solve with the flux BC and mean
