@@ -18,6 +18,10 @@
 
 using namespace sbm;
 
+namespace sbm {
+int ghost_after_solve(sbm_ctx* ctx, double* f, int bcx0, int bcx1);  // sbm_fields.cu
+}
+
 namespace {
 
 struct BatchCache {
@@ -119,6 +123,9 @@ extern "C" int sbm_batch_solve(sbm_ctx** ctxs, int n, int bc_x0, int bc_x1, doub
       SolveResult res{};
       rc = mixed_end(c, specs[v], h[last * n + v], &res);
       if (rc) break;
+      // same post-condition as a single solve: Dirichlet faces keep their
+      // data, the other ghosts copy the edge
+      if ((rc = ghost_after_solve(c, specs[v].x, bc_x0, bc_x1))) break;
       if (iters) iters[v] = res.iters;
       if (final_res) final_res[v] = res.final_res;
       if (status) status[v] = res.status;
