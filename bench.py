@@ -56,8 +56,9 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N)
-    ap.add_argument("--workload", default="solve256", choices=["solve256", "batch96"],
-                    help="solve256: the headline 256^3 solve; batch96: 96 uneven sub-volumes")
+    ap.add_argument("--workload", default="solve256", choices=["solve256", "batch96", "profile"],
+                    help="solve256: the headline 256^3 solve; batch96: 96 uneven sub-volumes; "
+                         "profile: only the production solve, for ncu captures")
     return ap.parse_args()
 
 
@@ -412,12 +413,35 @@ def run_batch(args):
     return 0
 
 
+def run_profile(args):
+    """The production solve alone (no FP64 baseline, no CPU leg), `steps`
+    times after `warmup` solves: the command the ncu summaries profile."""
+    import __graft_entry__
+    __graft_entry__.build()
+    from elsim_gb300 import sbm, synth
+    n = args.size
+    m = synth.microstructure((n, n, n), seed=SEED, tunnel=True)
+    prob = synth.potential_problem(m["psi"])
+    with sbm.Context(n, n, n) as ctx:
+        for k in ("coef", "x", "rhs", "weight"):
+            ctx.upload(k, prob[k])
+        for _ in range(args.warmup + args.steps):
+            ctx.upload("x", prob["x"])
+            info = ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO,
+                                scale=1.0, tol=TOL, max_it=200000, stop_rule=sbm.STOP_REL_RES,
+                                precision=sbm.PREC_MIXED, precond=sbm.PC_JACOBI)
+        print(json.dumps({"workload": "profile", "n": n, **info}))
+    return 0
+
+
 def main():
     args = _args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch96":
         return run_batch(args)
+    if args.workload == "profile":
+        return run_profile(args)
     return run_ours(args)
 
 
