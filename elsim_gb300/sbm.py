@@ -137,6 +137,9 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_batch_solve": (C.c_int, [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_double,
                                       C.c_double, C.c_int, C.c_int, ip, dp, ip, fp]),
         "sbm_table_lookup": (C.c_int, [i64, C.c_int, dp, dp, dp, dp]),
+        "sbm_conv3d_bf16": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.POINTER(C.c_uint16), C.POINTER(C.c_uint16),
+                                      C.POINTER(C.c_float), C.c_int, C.c_int, C.c_int, fp]),
         "sbm_redist": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]),
         "sbm_accdiff": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, C.c_int]),
         "sbm_redist_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,

@@ -271,6 +271,18 @@ int sbm_sign(int64_t n, const double* ds, double thr, double* sg);
 
 /* Text of the last error (CUDA failure or size rejection) seen by this thread. */
 const char* sbm_last_error(void);
+/* One BF16 3x3x3 convolution (zero padding) of a channels-last grid, the
+ * building block of the learned preconditioner; no counterpart in the
+ * reference.  x: (ny*nx*nz) x cin BF16 bit patterns, voxel v = i + ny*(j +
+ * nx*k); w: cout x 27 x cin BF16 (tap t = (di+1) + 3(dj+1) + 9(dk+1));
+ * bias: cout FP32 (may be NULL); y: (ny*nx*nz) x cout FP32.  flip = 1 reads
+ * the neighbour at minus the tap offset (the transposed convolution of the
+ * backward pass).  use_tc = 1: tcgen05 tensor-core kernel; 0: CUDA-core
+ * kernel.  cin, cout multiples of 16, cout <= 256. */
+int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const uint16_t* x,
+                    const uint16_t* w, const float* bias, int relu, int flip, int use_tc,
+                    float* y);
+
 /* Version string of the compiled library. */
 const char* sbm_version(void);
 /* Number of kernel launches this process has issued through the library. */
