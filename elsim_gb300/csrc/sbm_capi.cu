@@ -10,6 +10,7 @@
 #include <new>
 
 #include "sbm_internal.cuh"
+#include "sbm_net.cuh"
 
 namespace sbm {
 
@@ -182,6 +183,7 @@ int sbm_ctx_destroy(sbm_ctx* ctx) {
   if (!ctx) return SBM_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   release_graphs(ctx);
+  net_pc_release(ctx);
   for (int f = 0; f < SBM_F_COUNT; ++f) cudaFree(ctx->f[f]);
   double* d[] = {ctx->hk_kap, ctx->hk_pce, ctx->hk_pcc, ctx->hk_gen, ctx->dab, ctx->dab1,
                  ctx->mu,     ctx->mb,     ctx->pmn,    ctx->rhe,    ctx->rxc, ctx->kfw,
@@ -295,7 +297,8 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, doubl
                  float* ms) {
   if (!ctx || max_it < 1 || !(tol >= 0.0)) return SBM_ERR_ARG;
   if (stop_rule < 0 || stop_rule > 2 || precision < 0 || precision > 1) return SBM_ERR_ARG;
-  if (precond != SBM_PC_NONE && precond != SBM_PC_JACOBI) return SBM_ERR_ARG;
+  if (precond != SBM_PC_NONE && precond != SBM_PC_JACOBI && precond != SBM_PC_LEARNED)
+    return SBM_ERR_ARG;
   if ((bc_x0 != SBM_BC_COPY && bc_x0 != SBM_BC_ZERO) || (bc_x1 != SBM_BC_COPY && bc_x1 != SBM_BC_ZERO))
     return SBM_ERR_ARG;
   const Geo& g = ctx->g;
@@ -342,6 +345,18 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, doubl
   if (final_res) *final_res = r.final_res;
   if (ms) *ms = r.ms;
   return r.status;
+}
+
+int sbm_ctx_last_precond(const sbm_ctx* ctx) { return ctx ? ctx->last_precond : SBM_ERR_ARG; }
+
+int sbm_learned_pc_apply(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, const double* r,
+                         double* z) {
+  if (!ctx || !r || !z) return SBM_ERR_ARG;
+  SolveSpec sp{};
+  int rc = generic_spec(ctx, bc_x0, bc_x1, scale, 1e-8, 1, SBM_STOP_REL_RES, SBM_PREC_MIXED,
+                        SBM_PC_LEARNED, &sp);
+  if (rc) return rc;
+  return learned_pc_apply(ctx, sp, r, z);
 }
 
 }  // extern "C"

@@ -1,24 +1,26 @@
 // sbm_conv.cu -- BF16 3x3x3 convolution on the 5th-generation tensor cores.
 //
-// Implicit GEMM: rows (M) = 128 consecutive voxels of a grid stored
-// channels-last (x[v*C + c], v = i + ny*(j + nx*k)), columns (N) = output
-// channels, reduction (K) = 27 taps x input channels, walked one tap and 16
-// input channels at a time (one tcgen05.mma of K = 16 per step).  For each
-// step the 128 threads gather the 128 x 16 activation slice (zero outside
-// the grid) and the N x 16 weight slice into shared memory in the canonical
-// no-swizzle K-major layout (8-row x 16-byte core matrices; K-adjacent core
-// matrices 128 bytes apart, row groups 256 bytes apart), one elected thread
-// issues the MMA with FP32 accumulation into tensor memory and commits it to
-// the stage's mbarrier, and a 4-stage ring lets the gather of the next steps
-// overlap the MMAs in flight.  The epilogue reads the accumulator with
-// tcgen05.ld (each warp its 32 lanes), adds the bias, optionally applies
-// ReLU and stores BF16 or FP32 into a channel slice of the output.
+// Forward / data-gradient kernel (k_conv3_tc): implicit GEMM with rows
+// (M) = 128 voxels of a grid stored channels-last (x[v*C + c],
+// v = i + ny*(j + nx*k)), columns (N) = up to 64 output channels per CTA,
+// reduction (K) = 27 taps x input channels.  The input tile with its halo is
+// staged once per 16-channel chunk and the 27 tap MMAs read it through
+// shifted UMMA descriptors (see the kernel).  One elected thread issues the
+// MMAs with FP32 accumulation in tensor memory and commits them to the
+// stage's mbarrier; the epilogue reads the accumulator with tcgen05.ld (each
+// warp its 32 lanes), adds the bias, optionally applies ReLU and stores BF16
+// or FP32 into a channel slice of the output.
+//
+// Weight-gradient kernel (k_wgrad_tc): GEMM with rows = (tap, input
+// channel) pairs, columns = output channels, reduction = voxels.
 //
 // Operands are BF16 x BF16 -> FP32 only.  Every mbarrier wait is bounded;
 // on expiry the CTA sets an error flag, frees its tensor memory and returns.
 #include <cuda_bf16.h>
 
-#include "sbm_internal.cuh"
+#include <algorithm>
+
+#include "sbm_conv.cuh"
 
 namespace sbm {
 
@@ -30,6 +32,14 @@ constexpr int KS = 16;           // K per MMA (BF16)
 constexpr int NSTG = 4;          // stages
 constexpr int A_BYTES = TM * KS * 2;   // 4096
 constexpr unsigned kSpinTc = 1u << 20;
+// halo-tiled forward kernel
+constexpr int TY = 8, TX = 16;                  // voxel tile (y, x), one z plane
+constexpr int HY = TY + 2, HX = TX + 2, HZ = 3;  // halo tile
+constexpr int HVOX = HY * HX * HZ;              // 540 voxels
+constexpr int A_HALF = HVOX * 16;               // one 8-channel half, bytes
+constexpr int A_STAGE = 2 * A_HALF;             // 17280
+constexpr int NT_MAX = 64;                      // output channels per CTA
+constexpr int NST = 2;                          // stages
 
 __device__ __forceinline__ uint32_t sa(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -110,39 +120,239 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
   for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
 }
 
-struct ConvArgs {
-  int ny, nx, nz;        // grid
-  int cin, cout;         // channels (multiples of 16)
-  int ldx, offx;         // input channel stride and offset (channel slices of concat buffers)
-  int ldy, offy;         // output channel stride and offset
-  const __nv_bfloat16* x;
-  const __nv_bfloat16* w;  // [cout][27][cin]
-  const float* bias;       // [cout] or null
-  __nv_bfloat16* y16;      // BF16 output or null
-  float* y32;              // FP32 output or null
-  int relu;
-  int flip;                // 1: tap t reads neighbour -offset (transposed convolution)
-  int* err;                // set to 1 if a wait expired
-};
+}  // namespace
 
+namespace {
+
+// Halo-tiled implicit GEMM.  A CTA owns a tile of TY x TX voxels in one z
+// plane (M = 128 rows, row m = voxel (y0 + m%8, x0 + m/8)) and NT output
+// channels.  For each 16-channel input chunk it stages the (TY+2) x (TX+2)
+// x 3 halo tile once in shared memory, in the canonical K-major layout
+// (8 consecutive y voxels x 16 bytes = one core matrix; x lines HY*16
+// bytes apart; the two 8-channel halves A_HALF bytes apart), together with
+// the chunk's weights for all 27 taps, and issues the 27 tap MMAs from
+// shifted descriptor start addresses: the tap offset (dy, dx, dz) moves the
+// start by (dy + HY*(dx + HX*dz)) * 16 bytes and the core-matrix strides stay
+// the same, so the input is read about 4x (halo) instead of 27x.  Two
+// stages let the gather of the next chunk overlap the MMAs in flight.
 __global__ void __launch_bounds__(NTHR) k_conv3_tc(ConvArgs a) {
+  if (a.skip && *a.skip) return;
   extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char* As = sm;                               // NSTG x 4096
-  unsigned char* Bs = sm + NSTG * A_BYTES;              // NSTG x N*32
+  const int n0 = blockIdx.y * NT_MAX;
+  const int nt = min(NT_MAX, a.cout - n0);
+  const int bbytes = 27 * nt * 32;
+  const int stage_bytes = A_STAGE + bbytes;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + NST * stage_bytes);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + NST + 1);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const int nty = (a.ny + TY - 1) / TY, ntx = (a.nx + TX - 1) / TX;
+  const int ty = blockIdx.x % nty;
+  const int tx = (blockIdx.x / nty) % ntx;
+  const int z0 = blockIdx.x / (nty * ntx);
+  const int y0 = ty * TY, x0 = tx * TX;
+  const int zl = z0 % a.nzs;  // plane index within its sample
+  const int ncols = nt <= 32 ? 32 : 64;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     sa(tslot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s <= NST; ++s) mb_init(&bar[s]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t id = idesc_bf16(nt);
+  const int nchunk = a.cin / KS;
+  const uint4 zero4 = make_uint4(0, 0, 0, 0);
+  bool ok = true;
+  for (int c = 0; c < nchunk; ++c) {
+    const int s = c % NST;
+    // the stage was last read by the MMAs of chunk c - NST
+    if (c >= NST) ok = ok && mb_wait(&bar[s], (unsigned)(((c - NST) / NST) & 1));
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    unsigned char* A = sm + s * stage_bytes;
+    unsigned char* B = A + A_STAGE;
+    // halo tile: item q -> voxel hv = q / 2 (hy fastest), channel half q % 2
+    for (int q0 = 0; q0 < HVOX * 2; q0 += NTHR * 4) {
+      uint4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int q = q0 + u * NTHR + tid;
+        v[u] = zero4;
+        if (q < HVOX * 2) {
+          const int hv = q >> 1, kh = q & 1;
+          const int hy = hv % HY, hx = (hv / HY) % HX, hz = hv / (HY * HX);
+          const int y = y0 + hy - 1, x = x0 + hx - 1, dz = hz - 1;
+          if (y >= 0 && y < a.ny && x >= 0 && x < a.nx && zl + dz >= 0 && zl + dz < a.nzs) {
+            const int64_t vox = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + dz));
+            v[u] = *reinterpret_cast<const uint4*>(a.x + vox * a.ldx + a.offx + c * KS + kh * 8);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int q = q0 + u * NTHR + tid;
+        if (q < HVOX * 2)
+          *reinterpret_cast<uint4*>(A + (q & 1) * A_HALF + (q >> 1) * 16) = v[u];
+      }
+    }
+    // weights of the chunk for all taps: item q -> tap, row n, half kh
+    const int nb2 = nt * 2;
+    for (int q0 = 0; q0 < 27 * nb2; q0 += NTHR * 4) {
+      uint4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int q = q0 + u * NTHR + tid;
+        v[u] = zero4;
+        if (q < 27 * nb2) {
+          const int t = q / nb2, n = (q % nb2) >> 1, kh = q & 1;
+          v[u] = *reinterpret_cast<const uint4*>(a.w + ((int64_t)(n0 + n) * 27 + t) * a.cin +
+                                                 c * KS + kh * 8);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int q = q0 + u * NTHR + tid;
+        if (q < 27 * nb2) {
+          const int t = q / nb2, n = (q % nb2) >> 1, kh = q & 1;
+          *reinterpret_cast<uint4*>(B + t * (nt * 32) + (n >> 3) * 256 + kh * 128 + (n & 7) * 16) =
+              v[u];
+        }
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int t = 0; t < 27; ++t) {
+        int dy = t % 3 - 1, dx = (t / 3) % 3 - 1, dz = t / 9 - 1;
+        if (a.flip) {
+          dy = -dy;
+          dx = -dx;
+          dz = -dz;
+        }
+        const uint32_t aoff = (uint32_t)(((1 + dz) * HX + (1 + dx)) * HY + (1 + dy)) * 16u;
+        const uint64_t ad = umma_desc(sa(A) + aoff, A_HALF, HY * 16);
+        const uint64_t bd = umma_desc(sa(B) + (uint32_t)(t * nt * 32), 128, 256);
+        tc_mma(tmem, ad, bd, id, (c > 0 || t > 0) ? 1u : 0u);
+      }
+      tc_commit(&bar[s]);
+    }
+  }
+  // all MMAs complete -> accumulator ready
+  if (ok && tid == 0) tc_commit(&bar[NST]);
+  ok = __syncthreads_and(ok) && mb_wait(&bar[NST], 0);
+  ok = __syncthreads_and(ok);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int y = y0 + (tid & 7), x = x0 + (tid >> 3);
+    const bool valid = y < a.ny && x < a.nx;
+    const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * z0);
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int c0 = 0; c0 < nt; c0 += 16) {
+      float acc[16];
+      tc_ld16(lane_base + (uint32_t)c0, acc);
+      if (valid) {
+        if (a.y16) {
+          __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            float val = acc[q] + (a.bias ? a.bias[n0 + c0 + q] : 0.f);
+            if (a.relu) val = fmaxf(val, 0.f);
+            o[q] = __float2bfloat16_rn(val);
+          }
+          uint4* dst = reinterpret_cast<uint4*>(a.y16 + v * a.ldy + a.offy + n0 + c0);
+          dst[0] = *reinterpret_cast<const uint4*>(&o[0]);
+          dst[1] = *reinterpret_cast<const uint4*>(&o[8]);
+        }
+        if (a.y32) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            float val = acc[q] + (a.bias ? a.bias[n0 + c0 + q] : 0.f);
+            if (a.relu) val = fmaxf(val, 0.f);
+            a.y32[v * a.ldy + a.offy + n0 + c0 + q] = val;
+          }
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(a.err, 1);
+    // bounded drain of MMAs still in flight before the memory is released
+    for (int s = 0; s < NST; ++s) {
+      for (unsigned n = 0; n < kSpinTc && !mb_try(&bar[s], 0) && !mb_try(&bar[s], 1); ++n) {
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols)
+                 : "memory");
+}
+
+// Reference 3x3x3 convolution on the CUDA cores (same data layout), FP32
+// accumulation of BF16 products: the check of the tensor-core kernel.
+__global__ void k_conv3_ref(ConvArgs a) {
+  if (a.skip && *a.skip) return;
+  const int64_t nvox = (int64_t)a.ny * a.nx * a.nz;
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nvox * a.cout) return;
+  const int co = (int)(idx % a.cout);
+  const int64_t v = idx / a.cout;
+  const int vi = (int)(v % a.ny);
+  const int64_t r = v / a.ny;
+  const int vj = (int)(r % a.nx), vk = (int)(r / a.nx);
+  float acc = a.bias ? a.bias[co] : 0.f;
+  for (int t = 0; t < 27; ++t) {
+    int di = t % 3 - 1, dj = (t / 3) % 3 - 1, dk = t / 9 - 1;
+    if (a.flip) {
+      di = -di;
+      dj = -dj;
+      dk = -dk;
+    }
+    const int ii = vi + di, jj = vj + dj, kk = vk + dk, kl = vk % a.nzs + dk;
+    if (ii < 0 || ii >= a.ny || jj < 0 || jj >= a.nx || kl < 0 || kl >= a.nzs) continue;
+    const int64_t nv = (int64_t)ii + (int64_t)a.ny * (jj + (int64_t)a.nx * kk);
+    for (int ci = 0; ci < a.cin; ++ci)
+      acc += __bfloat162float(a.x[nv * a.ldx + a.offx + ci]) *
+             __bfloat162float(a.w[((int64_t)co * 27 + t) * a.cin + ci]);
+  }
+  if (a.relu) acc = fmaxf(acc, 0.f);
+  if (a.y16) a.y16[v * a.ldy + a.offy + co] = __float2bfloat16_rn(acc);
+  if (a.y32) a.y32[v * a.ldy + a.offy + co] = acc;
+}
+
+// Weight gradient dW[co][t][ci] = sum_v dy[v][co] * x[nb(v,t)][ci] as a
+// tensor-core GEMM: rows (M) = 128 of the 27*cin (tap, channel) pairs,
+// columns (N) = cout, reduction (K) = the voxels of this CTA's slice, 16 per
+// MMA; both operands gathered into the same K-major core-matrix layout as
+// the forward kernel.  Each CTA adds its slice's partial sums atomically.
+__global__ void __launch_bounds__(NTHR) k_wgrad_tc(WgradArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* As = sm;
+  unsigned char* Bs = sm + NSTG * A_BYTES;
   const int bstride = a.cout * KS * 2;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + NSTG * bstride);  // NSTG barriers + 1
+  uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + NSTG * bstride);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + NSTG + 1);
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int64_t nvox = (int64_t)a.ny * a.nx * a.nz;
-  const int64_t v = (int64_t)blockIdx.x * TM + tid;
-  int vi = 0, vj = 0, vk = 0;
-  if (v < nvox) {
-    vi = (int)(v % a.ny);
-    const int64_t r = v / a.ny;
-    vj = (int)(r % a.nx);
-    vk = (int)(r / a.nx);
-  }
+  const int rows = 27 * a.cin;
+  const int m = blockIdx.x * TM + tid;  // (tap, channel) row of this thread
+  const int t = m / a.cin, ci = m % a.cin;
+  const int di = t % 3 - 1, dj = (t / 3) % 3 - 1, dk = t / 9 - 1;
+  const int64_t v0 = (int64_t)blockIdx.y * a.kv;
+  const int64_t v1 = min(v0 + a.kv, nvox);
   const int ncols = a.cout <= 32 ? 32 : (a.cout <= 64 ? 64 : (a.cout <= 128 ? 128 : 256));
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -160,78 +370,74 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(ConvArgs a) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
   const uint32_t id = idesc_bf16(a.cout);
-  const int csteps = a.cin / KS;
-  const int nsteps = 27 * csteps;
-  // A row of this thread: core matrix (group m/8, k-half) at g*256 + kk*128, row r at +r*16
+  const int nsteps = (int)((v1 - v0 + KS - 1) / KS);
   const int g = tid >> 3, rr = tid & 7;
   bool ok = true;
   for (int step = 0; step < nsteps; ++step) {
     const int s = step % NSTG;
-    // the stage was last used by step - NSTG: wait until its MMA has read it
     if (step >= NSTG) ok = ok && mb_wait(&bar[s], (unsigned)(((step - NSTG) / NSTG) & 1));
     if (!__syncthreads_and(ok)) {
       ok = false;
       break;
     }
-    const int t = step / csteps, cs = step % csteps;
-    const int di = t % 3 - 1, dj = (t / 3) % 3 - 1, dk = t / 9 - 1;
-    // gather 16 input channels of the tap's neighbour (zero outside the grid)
-    uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
-    if (v < nvox) {
-      const int si = a.flip ? -di : di, sj = a.flip ? -dj : dj, sk = a.flip ? -dk : dk;
-      const int ii = vi + si, jj = vj + sj, kk = vk + sk;
-      if (ii >= 0 && ii < a.ny && jj >= 0 && jj < a.nx && kk >= 0 && kk < a.nz) {
-        const int64_t nv = (int64_t)ii + (int64_t)a.ny * (jj + (int64_t)a.nx * kk);
-        const uint4* src =
-            reinterpret_cast<const uint4*>(a.x + nv * a.ldx + a.offx + cs * KS);
-        lo = src[0];
-        hi = src[1];
+    const int64_t vb = v0 + (int64_t)step * KS;
+    // A row m: x[nb(v, t)][ci] for the 16 voxels of this step
+    __align__(16) __nv_bfloat16 av[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      __nv_bfloat16 val = __float2bfloat16_rn(0.f);
+      const int64_t vv = vb + e;
+      if (m < rows && vv < v1) {
+        const int vi = (int)(vv % a.ny);
+        const int64_t r2 = vv / a.ny;
+        const int vj = (int)(r2 % a.nx), vk = (int)(r2 / a.nx);
+        const int ii = vi + di, jj = vj + dj, kk = vk + dk, kl = vk % a.nzs + dk;
+        if (ii >= 0 && ii < a.ny && jj >= 0 && jj < a.nx && kl >= 0 && kl < a.nzs)
+          val = a.x[((int64_t)ii + (int64_t)a.ny * (jj + (int64_t)a.nx * kk)) * a.ldx + a.offx + ci];
       }
+      av[e] = val;
     }
     unsigned char* A = As + s * A_BYTES;
-    *reinterpret_cast<uint4*>(A + g * 256 + rr * 16) = lo;
-    *reinterpret_cast<uint4*>(A + g * 256 + 128 + rr * 16) = hi;
-    // weights: row n = output channel, 16 input channels of this tap
+    *reinterpret_cast<uint4*>(A + g * 256 + rr * 16) = *reinterpret_cast<const uint4*>(&av[0]);
+    *reinterpret_cast<uint4*>(A + g * 256 + 128 + rr * 16) = *reinterpret_cast<const uint4*>(&av[8]);
+    // B row n: dy[v][n] for the 16 voxels
     unsigned char* B = Bs + s * bstride;
     for (int q = tid; q < a.cout * 2; q += NTHR) {
       const int n = q >> 1, kh = q & 1;
-      const uint4 wv = *reinterpret_cast<const uint4*>(a.w + ((int64_t)n * 27 + t) * a.cin +
-                                                       cs * KS + kh * 8);
-      *reinterpret_cast<uint4*>(B + (n >> 3) * 256 + kh * 128 + (n & 7) * 16) = wv;
+      __align__(16) __nv_bfloat16 bv[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int64_t vv = vb + kh * 8 + e;
+        bv[e] = (vv < v1) ? a.dy[vv * a.cout + n] : __float2bfloat16_rn(0.f);
+      }
+      *reinterpret_cast<uint4*>(B + (n >> 3) * 256 + kh * 128 + (n & 7) * 16) =
+          *reinterpret_cast<const uint4*>(bv);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint64_t ad = umma_desc(sa(A), 128, 256);
-      const uint64_t bd = umma_desc(sa(B), 128, 256);
-      tc_mma(tmem, ad, bd, id, step > 0 ? 1u : 0u);
+      tc_mma(tmem, umma_desc(sa(A), 128, 256), umma_desc(sa(B), 128, 256), id, step > 0 ? 1u : 0u);
       tc_commit(&bar[s]);
     }
   }
-  // all MMAs complete -> accumulator ready
-  if (ok && tid == 0) tc_commit(&bar[NSTG]);
-  ok = __syncthreads_and(ok) && mb_wait(&bar[NSTG], 0);
+  if (ok && tid == 0 && nsteps > 0) tc_commit(&bar[NSTG]);
+  ok = __syncthreads_and(ok) && (nsteps == 0 || mb_wait(&bar[NSTG], 0));
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok) {
+  if (ok && nsteps > 0) {
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     for (int c0 = 0; c0 < a.cout; c0 += 16) {
       float acc[16];
       tc_ld16(lane_base + (uint32_t)c0, acc);
-      if (v < nvox) {
+      if (m < rows) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          float val = acc[q] + (a.bias ? a.bias[c0 + q] : 0.f);
-          if (a.relu) val = fmaxf(val, 0.f);
-          if (a.y16) a.y16[v * a.ldy + a.offy + c0 + q] = __float2bfloat16_rn(val);
-          if (a.y32) a.y32[v * a.ldy + a.offy + c0 + q] = val;
-        }
+        for (int q = 0; q < 16; ++q)
+          atomicAdd(&a.dw[((int64_t)(c0 + q) * 27 + t) * a.cin + ci], acc[q]);
       }
     }
-  } else if (tid == 0) {
+  } else if (!ok && tid == 0) {
     atomicExch(a.err, 1);
-    // bounded drain of MMAs still in flight before the memory is released
     for (int s = 0; s < NSTG; ++s) {
       for (unsigned n = 0; n < kSpinTc && !mb_try(&bar[s], 0) && !mb_try(&bar[s], 1); ++n) {
       }
@@ -244,39 +450,12 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(ConvArgs a) {
                  : "memory");
 }
 
-// Reference 3x3x3 convolution on the CUDA cores (same data layout), FP32
-// accumulation of BF16 products: the check of the tensor-core kernel.
-__global__ void k_conv3_ref(ConvArgs a) {
-  const int64_t nvox = (int64_t)a.ny * a.nx * a.nz;
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= nvox * a.cout) return;
-  const int co = (int)(idx % a.cout);
-  const int64_t v = idx / a.cout;
-  const int vi = (int)(v % a.ny);
-  const int64_t r = v / a.ny;
-  const int vj = (int)(r % a.nx), vk = (int)(r / a.nx);
-  float acc = a.bias ? a.bias[co] : 0.f;
-  for (int t = 0; t < 27; ++t) {
-    int di = t % 3 - 1, dj = (t / 3) % 3 - 1, dk = t / 9 - 1;
-    if (a.flip) {
-      di = -di;
-      dj = -dj;
-      dk = -dk;
-    }
-    const int ii = vi + di, jj = vj + dj, kk = vk + dk;
-    if (ii < 0 || ii >= a.ny || jj < 0 || jj >= a.nx || kk < 0 || kk >= a.nz) continue;
-    const int64_t nv = (int64_t)ii + (int64_t)a.ny * (jj + (int64_t)a.nx * kk);
-    for (int ci = 0; ci < a.cin; ++ci)
-      acc += __bfloat162float(a.x[nv * a.ldx + a.offx + ci]) *
-             __bfloat162float(a.w[((int64_t)co * 27 + t) * a.cin + ci]);
-  }
-  if (a.relu) acc = fmaxf(acc, 0.f);
-  if (a.y16) a.y16[v * a.ldy + a.offy + co] = __float2bfloat16_rn(acc);
-  if (a.y32) a.y32[v * a.ldy + a.offy + co] = acc;
-}
-
 size_t conv_smem(int cout) {
   return (size_t)NSTG * A_BYTES + (size_t)NSTG * cout * KS * 2 + (NSTG + 1) * 8 + 16;
+}
+
+size_t conv_tile_smem(int nt) {
+  return (size_t)NST * (A_STAGE + 27 * nt * 32) + (NST + 1) * 8 + 16;
 }
 
 }  // namespace
@@ -285,12 +464,12 @@ bool conv_shape_ok(int cin, int cout) {
   return cin >= 16 && cin % 16 == 0 && cout >= 16 && cout % 16 == 0 && cout <= 256;
 }
 
-int conv3_launch(const ConvArgs* pa, int use_tc, cudaStream_t s);
-
 int conv3_init() {
   static bool done = false;
   if (done) return SBM_OK;
   SBM_CUDA_TRY(cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)conv_tile_smem(NT_MAX)));
+  SBM_CUDA_TRY(cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)conv_smem(256)));
   done = true;
   return SBM_OK;
@@ -331,7 +510,7 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
   if (bias) cudaMemcpyAsync(db, bias, cout * 4, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(de, 0, 4, s);
   ConvArgs a{};
-  a.ny = ny; a.nx = nx; a.nz = nz; a.cin = cin; a.cout = cout;
+  a.ny = ny; a.nx = nx; a.nz = nz; a.nzs = nz; a.cin = cin; a.cout = cout;
   a.ldx = cin; a.offx = 0; a.ldy = cout; a.offy = 0;
   a.x = (const __nv_bfloat16*)dx; a.w = (const __nv_bfloat16*)dw;
   a.bias = bias ? (const float*)db : nullptr;
@@ -347,12 +526,24 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
 }
 
 namespace sbm {
+int wgrad_launch(const WgradArgs* pa, cudaStream_t s) {
+  const WgradArgs& a = *pa;
+  const int64_t nv = (int64_t)a.ny * a.nx * a.nz;
+  const dim3 grid((unsigned)((27 * a.cin + TM - 1) / TM), (unsigned)((nv + a.kv - 1) / a.kv));
+  k_wgrad_tc<<<grid, NTHR, conv_smem(a.cout), s>>>(a);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
 int conv3_launch(const ConvArgs* pa, int use_tc, cudaStream_t s) {
   const ConvArgs& a = *pa;
   const int64_t nv = (int64_t)a.ny * a.nx * a.nz;
   if (use_tc) {
-    const unsigned blocks = (unsigned)((nv + TM - 1) / TM);
-    k_conv3_tc<<<blocks, NTHR, conv_smem(a.cout), s>>>(a);
+    const int64_t tiles = (int64_t)((a.ny + TY - 1) / TY) * ((a.nx + TX - 1) / TX) * a.nz;
+    const int ntn = (a.cout + NT_MAX - 1) / NT_MAX;
+    k_conv3_tc<<<dim3((unsigned)tiles, (unsigned)ntn), NTHR,
+                 conv_tile_smem(std::min(a.cout, NT_MAX)), s>>>(a);
   } else {
     const int64_t n = nv * a.cout;
     k_conv3_ref<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);

@@ -312,8 +312,10 @@ struct sbm_ctx {
   sbm::OpArgs<float> last_op32{};
   int last_pc = -1;
   int no_tma = 0;  // tuning flag: use the register-tiled FP32 stencil instead of TMA
-  // learned preconditioner (opaque; owned by sbm_learned.cu)
+  // learned preconditioner plan (opaque; owned by sbm_net.cu) and the
+  // preconditioner the last mixed solve actually used
   void* net = nullptr;
+  int last_precond = -1;
 };
 
 namespace sbm {
@@ -329,5 +331,6 @@ int generic_spec(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, double tol, i
                  int stop_rule, int precision, int precond, SolveSpec* sp);
 int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double* bytes_per_launch);
 int ensure_fp32_work(sbm_ctx* ctx);
+int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double* z);
 void release_graphs(sbm_ctx* ctx);
 }  // namespace sbm

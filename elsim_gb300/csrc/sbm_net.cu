@@ -1,0 +1,1031 @@
+// sbm_net.cu -- learned coarse-grid preconditioner for the flexible CG of
+// the mixed-precision solver (no counterpart in the reference, whose CG
+// loops are unpreconditioned).
+//
+//   z = D^-1 r + P e_c,     e_c = (s k_out / (scale c_ref)) N(f),
+//
+// R = average over 4x4x4 fine cells, P = cell-centred trilinear
+// interpolation (clamped at the faces), s = RMS of R r, c_ref = mean of
+// R K, N a 3D U-Net on the coarse grid whose input channels f are
+// [R r / s, R K / c_ref, 1, Dirichlet x0 face, Dirichlet x1 face, 0 ...].
+// N is trained (below, on the tensor cores) to map f to
+// R(A^-1 r) scale c_ref / (s k_out), so e_c approximates the restricted
+// error.  The result is not linear in r, hence the flexible CG.
+//
+// U-Net (channels, BF16 activations channels-last, FP32 accumulation):
+//   level 0 (coarse grid)   E0 16->16  ...........................  D0 48->16 -> 1x1 16->1
+//   level 1 (avg pool 2)    E1 16->32  .....................  D1 64->32
+//   level 2                 E2 32->32  ...............  D2 80->32
+//   level 3                 E3 32->48  .........  D3 112->48
+//   level 4                 E4 48->64 --(nearest upsampling)--^
+// 3x3x3 convolutions with bias and ReLU; each decoder level reads the
+// concatenation [upsampled lower output | encoder output] from one buffer.
+//
+// Training: loss = mean (N(f) - t)^2.  Backward uses the same tcgen05
+// convolution kernel with flipped taps and transposed weights for the data
+// gradient, a tcgen05 GEMM over voxels for the weight gradient, and Adam on
+// FP32 master weights with BF16 copies for the next forward pass.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "sbm_conv.cuh"
+#include "sbm_net.cuh"
+
+namespace sbm {
+namespace netd {
+
+typedef __nv_bfloat16 bf16;
+
+enum { E0, E1, E2, E3, E4, D3, D2, D1, D0, OUT, NLAYER };
+constexpr int kCi[NLAYER] = {16, 16, 32, 32, 48, 112, 80, 64, 48, 16};
+constexpr int kCo[NLAYER] = {16, 32, 32, 48, 64, 48, 32, 32, 16, 1};
+constexpr int kLev = 5;
+constexpr int kFeat = 16;
+constexpr int kCatW[4] = {48, 64, 80, 112};  // concat buffer width per level
+constexpr int kUpW[4] = {32, 32, 48, 64};    // [0, kUpW): upsampled; [kUpW, kCatW): encoder
+constexpr int kEnc[4] = {E0, E1, E2, E3};
+constexpr int kDec[4] = {D0, D1, D2, D3};
+
+struct Layout {
+  int64_t off[NLAYER];   // weights [co][taps][ci]
+  int64_t boff[NLAYER];  // biases [co]
+  int64_t total;
+};
+
+Layout make_layout() {
+  Layout L{};
+  int64_t o = 0;
+  for (int l = 0; l < NLAYER; ++l) {
+    const int taps = (l == OUT) ? 1 : 27;
+    L.off[l] = o;
+    o += (int64_t)kCo[l] * taps * kCi[l];
+    L.boff[l] = o;
+    o += kCo[l];
+  }
+  L.total = o;
+  return L;
+}
+const Layout kL = make_layout();
+
+struct Dims {
+  int ny, nx, nz, nzs;  // nz = stacked depth of all samples, nzs = one sample
+  __host__ __device__ int64_t v() const { return (int64_t)ny * nx * nz; }
+};
+
+inline Dims half(const Dims& d) { return Dims{d.ny / 2, d.nx / 2, d.nz / 2, d.nzs / 2}; }
+
+struct Work {
+  Dims d[kLev];
+  bool train = false;
+  bf16* in0 = nullptr;
+  bf16* cat[4] = {};
+  bf16* pin[kLev] = {};  // pooled encoder outputs, levels 1..4
+  bf16* a4 = nullptr;
+  bf16* dec[4] = {};
+  float* out = nullptr;
+  float* tgt = nullptr;
+  // backward
+  bf16* gdec[4] = {};  // gradients of the pre-activations
+  bf16* genc[4] = {};
+  bf16* ga4 = nullptr;
+  float* gcat[4] = {};  // data gradients of the decoder inputs
+  float* gpin[kLev] = {};
+  std::vector<void*> mem;
+  ~Work() {
+    for (void* p : mem) cudaFree(p);
+  }
+  template <typename T>
+  bool alloc(T** p, int64_t n) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, sizeof(T) * (size_t)(n > 0 ? n : 1)) != cudaSuccess) return false;
+    mem.push_back(q);
+    *p = static_cast<T*>(q);
+    return true;
+  }
+};
+
+// ------------------------------------------------------------- kernels
+
+__device__ __forceinline__ void vox(const Dims& d, int64_t v, int* i, int* j, int* k) {
+  *i = (int)(v % d.ny);
+  const int64_t r = v / d.ny;
+  *j = (int)(r % d.nx);
+  *k = (int)(r / d.nx);
+}
+
+__device__ __forceinline__ int64_t vid(const Dims& d, int i, int j, int k) {
+  return (int64_t)i + (int64_t)d.ny * (j + (int64_t)d.nx * k);
+}
+
+__device__ __forceinline__ int64_t child(const Dims& f, int i, int j, int k, int q) {
+  return vid(f, 2 * i + (q & 1), 2 * j + ((q >> 1) & 1), 2 * k + (q >> 2));
+}
+
+#define NET_LOOP(n)                                                                 \
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (n);         \
+       t += (int64_t)gridDim.x * blockDim.x)
+
+// y[vc][c] = mean of x[child][offx + c] over the 8 children (average pooling).
+__global__ void k_pool(Dims f, int C, const bf16* __restrict__ x, int ldx, int offx,
+                       bf16* __restrict__ y, const int* skip) {
+  if (skip && *skip) return;
+  const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
+  NET_LOOP(c.v() * C) {
+    const int ch = (int)(t % C);
+    const int64_t vc = t / C;
+    int i, j, k;
+    vox(c, vc, &i, &j, &k);
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += __bfloat162float(x[child(f, i, j, k, q) * ldx + offx + ch]);
+    y[vc * C + ch] = __float2bfloat16_rn(s * 0.125f);
+  }
+}
+
+// y[vf][offy + c] = x[parent(vf)][c] (nearest-neighbour upsampling).
+__global__ void k_up(Dims f, int C, const bf16* __restrict__ x, bf16* __restrict__ y, int ldy,
+                     int offy, const int* skip) {
+  if (skip && *skip) return;
+  const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
+  NET_LOOP(f.v() * C) {
+    const int ch = (int)(t % C);
+    const int64_t vf = t / C;
+    int i, j, k;
+    vox(f, vf, &i, &j, &k);
+    y[vf * ldy + offy + ch] = x[vid(c, i / 2, j / 2, k / 2) * C + ch];
+  }
+}
+
+// Backward of upsampling + ReLU: out[vc][c] = (act[vc][c] > 0) *
+// sum over the children of g[vf][offg + c].
+__global__ void k_bwd_up(Dims f, int C, const float* __restrict__ g, int ldg, int offg,
+                         const bf16* __restrict__ act, bf16* __restrict__ out) {
+  const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
+  NET_LOOP(c.v() * C) {
+    const int ch = (int)(t % C);
+    const int64_t vc = t / C;
+    int i, j, k;
+    vox(c, vc, &i, &j, &k);
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += g[child(f, i, j, k, q) * ldg + offg + ch];
+    out[vc * C + ch] = __float2bfloat16_rn(__bfloat162float(act[vc * C + ch]) > 0.f ? s : 0.f);
+  }
+}
+
+// Backward of an encoder output read by the skip connection and by the
+// pooling: out[vf][c] = (act > 0) * (g[vf][offg + c] + gp[parent][c] / 8).
+__global__ void k_bwd_skip(Dims f, int C, const float* __restrict__ g, int ldg, int offg,
+                           const float* __restrict__ gp, const bf16* __restrict__ act, int lda,
+                           int offa, bf16* __restrict__ out) {
+  const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
+  NET_LOOP(f.v() * C) {
+    const int ch = (int)(t % C);
+    const int64_t vf = t / C;
+    float s = g[vf * ldg + offg + ch];
+    if (gp) {
+      int i, j, k;
+      vox(f, vf, &i, &j, &k);
+      s += 0.125f * gp[vid(c, i / 2, j / 2, k / 2) * C + ch];
+    }
+    out[vf * C + ch] = __float2bfloat16_rn(__bfloat162float(act[vf * lda + offa + ch]) > 0.f ? s : 0.f);
+  }
+}
+
+// 1x1 output layer (FP32 weights): out[v] = b + sum_c w[c] d0[v][c]; with a
+// target, *loss += sum (out - tgt)^2.
+__global__ void k_out_fwd(int64_t V, const bf16* __restrict__ d0, const float* __restrict__ w,
+                          const float* __restrict__ b, float* __restrict__ out,
+                          const float* __restrict__ tgt, double* loss, const int* skip) {
+  if (skip && *skip) return;
+  __shared__ double sm[32];
+  double acc = 0.0;
+  NET_LOOP(V) {
+    const uint4* p = reinterpret_cast<const uint4*>(d0 + t * 16);
+    const uint4 lo = p[0], hi = p[1];
+    const bf16* a = reinterpret_cast<const bf16*>(&lo);
+    const bf16* h = reinterpret_cast<const bf16*>(&hi);
+    float s = b[0];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s += w[c] * __bfloat162float(a[c]);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s += w[8 + c] * __bfloat162float(h[c]);
+    out[t] = s;
+    if (tgt) {
+      const double e = (double)s - (double)tgt[t];
+      acc += e * e;
+    }
+  }
+  if (tgt) {
+    const double tot = block_sum(acc, sm);
+    if (threadIdx.x == 0) atomicAdd(loss, tot);
+  }
+}
+
+// Backward of the output layer and of D0's ReLU:
+// dout = 2 (out - tgt) / V_total; gd0[v][c] = (d0 > 0) dout w[c];
+// gw[c] += sum_v dout d0[v][c]; gb += sum_v dout.
+__global__ void k_out_bwd(int64_t V, float inv_v, const bf16* __restrict__ d0,
+                          const float* __restrict__ w, const float* __restrict__ out,
+                          const float* __restrict__ tgt, bf16* __restrict__ gd0,
+                          float* __restrict__ gw, float* __restrict__ gb) {
+  __shared__ float sm[17];
+  if (threadIdx.x < 17) sm[threadIdx.x] = 0.f;
+  __syncthreads();
+  float acc[17];
+#pragma unroll
+  for (int c = 0; c < 17; ++c) acc[c] = 0.f;
+  NET_LOOP(V) {
+    const float dout = 2.f * (out[t] - tgt[t]) * inv_v;
+    acc[16] += dout;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const float a = __bfloat162float(d0[t * 16 + c]);
+      acc[c] += dout * a;
+      gd0[t * 16 + c] = __float2bfloat16_rn(a > 0.f ? dout * w[c] : 0.f);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 17; ++c) {
+    float v = acc[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sm[c], v);
+  }
+  __syncthreads();
+  if (threadIdx.x < 16) atomicAdd(&gw[threadIdx.x], sm[threadIdx.x]);
+  if (threadIdx.x == 16) atomicAdd(gb, sm[16]);
+}
+
+// gb[c] += sum_v dy[v][c]   (C <= 64)
+__global__ void k_bias_grad(int64_t V, int C, const bf16* __restrict__ dy, float* __restrict__ gb) {
+  __shared__ float sm[64];
+  if (threadIdx.x < C) sm[threadIdx.x] = 0.f;
+  __syncthreads();
+  const int groups = blockDim.x / C;
+  const int c = threadIdx.x % C, grp = threadIdx.x / C;
+  float s = 0.f;
+  if (grp < groups)
+    for (int64_t v = (int64_t)blockIdx.x * groups + grp; v < V; v += (int64_t)gridDim.x * groups)
+      s += __bfloat162float(dy[v * C + c]);
+  if (grp < groups) atomicAdd(&sm[c], s);
+  __syncthreads();
+  if (threadIdx.x < C) atomicAdd(&gb[threadIdx.x], sm[threadIdx.x]);
+}
+
+struct LayerTab {
+  int64_t off[NLAYER];
+  int ci[NLAYER], co[NLAYER];
+};
+
+// Adam step on the FP32 master parameters (when `update`), then the BF16
+// copies of the convolution weights: w16 [co][27][ci] for the forward pass
+// and wt16 [ci][27][co] (same offsets) for the data gradient.
+__global__ void k_adam(int64_t P, int update, float* __restrict__ w, const float* __restrict__ g,
+                       float* __restrict__ m, float* __restrict__ v, float lr, float b1, float b2,
+                       float eps, float c1, float c2, LayerTab tab, bf16* __restrict__ w16,
+                       bf16* __restrict__ wt16) {
+  NET_LOOP(P) {
+    float wv = w[t];
+    if (update) {
+      const float gv = g[t];
+      const float mv = b1 * m[t] + (1.f - b1) * gv;
+      const float vv = b2 * v[t] + (1.f - b2) * gv * gv;
+      m[t] = mv;
+      v[t] = vv;
+      wv -= lr * (mv * c1) / (sqrtf(vv * c2) + eps);
+      w[t] = wv;
+    }
+    for (int l = 0; l < OUT; ++l) {
+      const int64_t n = (int64_t)tab.co[l] * 27 * tab.ci[l];
+      const int64_t rel = t - tab.off[l];
+      if (rel >= 0 && rel < n) {
+        const bf16 b = __float2bfloat16_rn(wv);
+        w16[t] = b;
+        const int ci = (int)(rel % tab.ci[l]);
+        const int tap = (int)((rel / tab.ci[l]) % 27);
+        const int co = (int)(rel / ((int64_t)27 * tab.ci[l]));
+        wt16[tab.off[l] + ((int64_t)ci * 27 + tap) * tab.co[l] + co] = b;
+      }
+    }
+  }
+}
+
+__global__ void k_loss_rec(double* loss, float inv_v, float* hist) {
+  *hist = (float)(*loss * (double)inv_v);
+  *loss = 0.0;
+}
+
+int grid_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+}  // namespace netd
+}  // namespace sbm
+
+using namespace sbm;
+using namespace sbm::netd;
+
+struct sbm_net {
+  float* w32 = nullptr;  // master parameters
+  float* m = nullptr;
+  float* v = nullptr;
+  float* grad = nullptr;
+  bf16* w16 = nullptr;
+  bf16* wt16 = nullptr;
+  int* err = nullptr;
+  double* loss = nullptr;
+  int64_t step = 0;
+  cudaStream_t stream = nullptr;
+  std::map<std::tuple<int, int, int, int, int>, Work*> works;
+};
+
+namespace sbm {
+namespace netd {
+
+LayerTab layer_tab() {
+  LayerTab t{};
+  for (int l = 0; l < NLAYER; ++l) {
+    t.off[l] = kL.off[l];
+    t.ci[l] = kCi[l];
+    t.co[l] = kCo[l];
+  }
+  return t;
+}
+
+int cast_weights(sbm_net* n, cudaStream_t s) {
+  k_adam<<<grid_for(kL.total), 256, 0, s>>>(kL.total, 0, n->w32, nullptr, nullptr, nullptr, 0.f,
+                                            0.f, 0.f, 0.f, 0.f, 0.f, layer_tab(), n->w16,
+                                            n->wt16);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
+bool dims_ok(int ny, int nx, int nz) {
+  return ny >= 16 && nx >= 16 && nz >= 16 && ny % 16 == 0 && nx % 16 == 0 && nz % 16 == 0;
+}
+
+Work* make_work(const Dims& d0, bool train) {
+  Work* w = new Work();
+  w->train = train;
+  w->d[0] = d0;
+  for (int l = 1; l < kLev; ++l) w->d[l] = half(w->d[l - 1]);
+  bool ok = w->alloc(&w->in0, w->d[0].v() * kFeat) && w->alloc(&w->out, w->d[0].v()) &&
+            w->alloc(&w->tgt, w->d[0].v()) && w->alloc(&w->a4, w->d[4].v() * kCo[E4]);
+  for (int l = 0; l < 4 && ok; ++l)
+    ok = w->alloc(&w->cat[l], w->d[l].v() * kCatW[l]) &&
+         w->alloc(&w->dec[l], w->d[l].v() * kCo[kDec[l]]) &&
+         w->alloc(&w->pin[l + 1], w->d[l + 1].v() * kCi[kEnc[0] + l + 1]);
+  if (ok && train) {
+    ok = w->alloc(&w->ga4, w->d[4].v() * kCo[E4]);
+    for (int l = 0; l < 4 && ok; ++l)
+      ok = w->alloc(&w->gdec[l], w->d[l].v() * kCo[kDec[l]]) &&
+           w->alloc(&w->genc[l], w->d[l].v() * kCo[kEnc[l]]) &&
+           w->alloc(&w->gcat[l], w->d[l].v() * kCatW[l]) &&
+           w->alloc(&w->gpin[l + 1], w->d[l + 1].v() * kCi[kEnc[0] + l + 1]);
+  }
+  if (!ok) {
+    delete w;
+    return nullptr;
+  }
+  // channels 1.. of the input stay zero unless a caller fills them
+  cudaMemset(w->in0, 0, sizeof(bf16) * w->d[0].v() * kFeat);
+  return w;
+}
+
+Work* work_for(sbm_net* n, int ny, int nx, int nzs, int nb, bool train) {
+  const auto key = std::make_tuple(ny, nx, nzs, nb, train ? 1 : 0);
+  auto it = n->works.find(key);
+  if (it != n->works.end()) return it->second;
+  Work* w = make_work(Dims{ny, nx, nzs * nb, nzs}, train);
+  if (!w) return nullptr;
+  n->works[key] = w;
+  return w;
+}
+
+int conv(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx, const bf16* wts,
+         bf16* y, int ldy, int offy, const int* skip, cudaStream_t s) {
+  ConvArgs a{};
+  const Dims& d = w.d[lev];
+  a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
+  a.cin = kCi[l]; a.cout = kCo[l];
+  a.ldx = ldx; a.offx = 0; a.ldy = ldy; a.offy = offy;
+  a.x = x; a.w = wts + kL.off[l]; a.bias = n->w32 + kL.boff[l];
+  a.y16 = y; a.y32 = nullptr; a.relu = 1; a.flip = 0; a.err = n->err; a.skip = skip;
+  return conv3_launch(&a, 1, s);
+}
+
+void pool(const Work& w, int lev, int C, const bf16* x, int ldx, int offx, bf16* y,
+          const int* skip, cudaStream_t s) {
+  const Dims& f = w.d[lev];
+  k_pool<<<grid_for(f.v() / 8 * C), 256, 0, s>>>(f, C, x, ldx, offx, y, skip);
+  SBM_LAUNCHED(1);
+}
+
+void up(const Work& w, int lev, int C, const bf16* x, bf16* y, int ldy, const int* skip,
+        cudaStream_t s) {
+  const Dims& f = w.d[lev];
+  k_up<<<grid_for(f.v() * C), 256, 0, s>>>(f, C, x, y, ldy, 0, skip);
+  SBM_LAUNCHED(1);
+}
+
+// Forward pass of the U-Net on w.in0 -> w.out (and the squared error
+// against w.tgt into n->loss when tgt).
+int forward(sbm_net* n, const Work& w, bool tgt, const int* skip, cudaStream_t s) {
+  int rc;
+  for (int lev = 0; lev < 4; ++lev) {
+    const int l = kEnc[lev];
+    const bf16* x = lev == 0 ? w.in0 : w.pin[lev];
+    if ((rc = conv(n, w, l, lev, x, kCi[l], n->w16, w.cat[lev], kCatW[lev], kUpW[lev], skip, s)))
+      return rc;
+    pool(w, lev, kCo[l], w.cat[lev], kCatW[lev], kUpW[lev], w.pin[lev + 1], skip, s);
+  }
+  if ((rc = conv(n, w, E4, 4, w.pin[4], kCi[E4], n->w16, w.a4, kCo[E4], 0, skip, s))) return rc;
+  for (int lev = 3; lev >= 0; --lev) {
+    const bf16* below = lev == 3 ? w.a4 : w.dec[lev + 1];
+    up(w, lev, kUpW[lev], below, w.cat[lev], kCatW[lev], skip, s);
+    const int l = kDec[lev];
+    if ((rc = conv(n, w, l, lev, w.cat[lev], kCatW[lev], n->w16, w.dec[lev], kCo[l], 0, skip, s)))
+      return rc;
+  }
+  const int64_t V = w.d[0].v();
+  k_out_fwd<<<grid_for(V), 256, 0, s>>>(V, w.dec[0], n->w32 + kL.off[OUT], n->w32 + kL.boff[OUT],
+                                        w.out, tgt ? w.tgt : nullptr, n->loss, skip);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
+int wgrad(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx, const bf16* gy,
+          cudaStream_t s) {
+  const Dims& d = w.d[lev];
+  WgradArgs a{};
+  a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
+  a.cin = kCi[l]; a.cout = kCo[l]; a.ldx = ldx; a.offx = 0;
+  a.x = x; a.dy = gy; a.dw = n->grad + kL.off[l]; a.err = n->err;
+  const int64_t V = d.v();
+  const int64_t gx = (27 * kCi[l] + 127) / 128;
+  int64_t kv = (V * gx + 1215) / 1216;
+  kv = (kv + 15) / 16 * 16;
+  if (kv < 64) kv = 64;
+  if (kv > 4096) kv = 4096;
+  a.kv = (int)kv;
+  int rc = wgrad_launch(&a, s);
+  if (rc) return rc;
+  const int C = kCo[l];
+  const int groups = 256 / C;
+  int64_t b = (V + groups * 8 - 1) / (groups * 8);
+  if (b > 152 * 8) b = 152 * 8;
+  if (b < 1) b = 1;
+  k_bias_grad<<<(unsigned)b, 256, 0, s>>>(V, C, gy, n->grad + kL.boff[l]);
+  SBM_LAUNCHED(1);
+  return SBM_OK;
+}
+
+int dgrad(sbm_net* n, const Work& w, int l, int lev, const bf16* gy, float* gx, cudaStream_t s) {
+  ConvArgs a{};
+  const Dims& d = w.d[lev];
+  a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
+  a.cin = kCo[l]; a.cout = kCi[l];
+  a.ldx = kCo[l]; a.offx = 0; a.ldy = kCi[l]; a.offy = 0;
+  a.x = gy; a.w = n->wt16 + kL.off[l]; a.bias = nullptr;
+  a.y16 = nullptr; a.y32 = gx; a.relu = 0; a.flip = 1; a.err = n->err; a.skip = nullptr;
+  return conv3_launch(&a, 1, s);
+}
+
+// Gradient of mean (out - tgt)^2 over all voxels of w into n->grad
+// (forward with the target must have run).
+int backward(sbm_net* n, const Work& w, cudaStream_t s) {
+  int rc;
+  SBM_CUDA_TRY(cudaMemsetAsync(n->grad, 0, sizeof(float) * kL.total, s));
+  const int64_t V = w.d[0].v();
+  k_out_bwd<<<grid_for(V), 256, 0, s>>>(V, 1.0f / (float)V, w.dec[0], n->w32 + kL.off[OUT], w.out,
+                                        w.tgt, w.gdec[0], n->grad + kL.off[OUT],
+                                        n->grad + kL.boff[OUT]);
+  SBM_LAUNCHED(1);
+  for (int lev = 0; lev < 4; ++lev) {
+    const int l = kDec[lev];
+    if ((rc = wgrad(n, w, l, lev, w.cat[lev], kCatW[lev], w.gdec[lev], s))) return rc;
+    if ((rc = dgrad(n, w, l, lev, w.gdec[lev], w.gcat[lev], s))) return rc;
+    const Dims& f = w.d[lev];
+    const bf16* act = lev == 3 ? w.a4 : w.dec[lev + 1];
+    bf16* out = lev == 3 ? w.ga4 : w.gdec[lev + 1];
+    k_bwd_up<<<grid_for(f.v() / 8 * kUpW[lev]), 256, 0, s>>>(f, kUpW[lev], w.gcat[lev],
+                                                             kCatW[lev], 0, act, out);
+    SBM_LAUNCHED(1);
+  }
+  if ((rc = wgrad(n, w, E4, 4, w.pin[4], kCi[E4], w.ga4, s))) return rc;
+  if ((rc = dgrad(n, w, E4, 4, w.ga4, w.gpin[4], s))) return rc;
+  for (int lev = 3; lev >= 0; --lev) {
+    const int l = kEnc[lev];
+    const Dims& f = w.d[lev];
+    const int C = kCo[l];
+    k_bwd_skip<<<grid_for(f.v() * C), 256, 0, s>>>(f, C, w.gcat[lev], kCatW[lev], kUpW[lev],
+                                                   w.gpin[lev + 1], w.cat[lev], kCatW[lev],
+                                                   kUpW[lev], w.genc[lev]);
+    SBM_LAUNCHED(1);
+    const bf16* x = lev == 0 ? w.in0 : w.pin[lev];
+    if ((rc = wgrad(n, w, l, lev, x, kCi[l], w.genc[lev], s))) return rc;
+    if (lev > 0 && (rc = dgrad(n, w, l, lev, w.genc[lev], w.gpin[lev], s))) return rc;
+  }
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
+int adam(sbm_net* n, float lr, cudaStream_t s) {
+  n->step += 1;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float c1 = 1.f / (1.f - powf(b1, (float)n->step));
+  const float c2 = 1.f / (1.f - powf(b2, (float)n->step));
+  k_adam<<<grid_for(kL.total), 256, 0, s>>>(kL.total, 1, n->w32, n->grad, n->m, n->v, lr, b1, b2,
+                                            eps, c1, c2, layer_tab(), n->w16, n->wt16);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
+uint16_t to_bf16_bits(float f) {
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+int upload_bf16(bf16* dst, const float* src, int64_t n, cudaStream_t s) {
+  std::vector<uint16_t> h((size_t)n);
+  for (int64_t i = 0; i < n; ++i) h[(size_t)i] = to_bf16_bits(src[i]);
+  SBM_CUDA_TRY(cudaMemcpyAsync(dst, h.data(), sizeof(uint16_t) * n, cudaMemcpyHostToDevice, s));
+  SBM_CUDA_TRY(cudaStreamSynchronize(s));
+  return SBM_OK;
+}
+
+uint64_t splitmix(uint64_t* x) {
+  uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+double unit(uint64_t* x) { return ((splitmix(x) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+int check_err(sbm_net* n) {
+  int h = 0;
+  SBM_CUDA_TRY(cudaMemcpyAsync(&h, n->err, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+  SBM_CUDA_TRY(cudaStreamSynchronize(n->stream));
+  if (h) {
+    set_error_msg("tensor-core convolution wait expired");
+    cudaMemsetAsync(n->err, 0, sizeof(int), n->stream);
+    return SBM_ERR_TIMEOUT;
+  }
+  return SBM_OK;
+}
+
+// ------------------------------------------------ solver-side plan
+
+// Coarse-cell means of the coefficient (2 hk) and their mean c_ref; the
+// last block stores c_ref and the output factor k_out / (scale c_ref).
+__global__ void k_pc_coef(Geo g, Dims c, const float* __restrict__ hk, float* __restrict__ coefc,
+                          double* partials, unsigned* counter, float* scal, double kout,
+                          double scale) {
+  double acc = 0.0;
+  NET_LOOP(c.v()) {
+    int i, j, k;
+    vox(c, t, &i, &j, &k);
+    float s = 0.f;
+    for (int kk = 0; kk < 4; ++kk)
+      for (int jj = 0; jj < 4; ++jj) {
+        const float* p = hk + g.ix(4 * i + 1, 4 * j + jj + 1, 4 * k + kk + 1);
+        const float4 v = *reinterpret_cast<const float4*>(p);
+        s += (v.x + v.y) + (v.z + v.w);
+      }
+    const float m = s * (2.f / 64.f);
+    coefc[t] = m;
+    acc += m;
+  }
+  double v[1] = {acc}, tot[1];
+  if (grid_reduce<1>(v, partials, counter, tot)) {
+    if (threadIdx.x == 0) {
+      const double cref = tot[0] / (double)c.v();
+      scal[3] = (float)cref;
+      scal[2] = (float)(kout / (scale * cref));
+    }
+  }
+}
+
+// Static input channels 1..15 of the coarse grid.
+__global__ void k_pc_feat(Dims c, const float* __restrict__ coefc, const float* scal, int bcx0,
+                          int bcx1, bf16* __restrict__ in0) {
+  NET_LOOP(c.v()) {
+    int i, j, k;
+    vox(c, t, &i, &j, &k);
+    float f[kFeat];
+#pragma unroll
+    for (int q = 0; q < kFeat; ++q) f[q] = 0.f;
+    f[1] = coefc[t] / scal[3];
+    f[2] = 1.f;
+    f[3] = (bcx0 == SBM_BC_ZERO && j == 0) ? 1.f : 0.f;
+    f[4] = (bcx1 == SBM_BC_ZERO && j == c.nx - 1) ? 1.f : 0.f;
+#pragma unroll
+    for (int q = 1; q < kFeat; ++q) in0[t * kFeat + q] = __float2bfloat16_rn(f[q]);
+  }
+}
+
+// rc = R r (4x4x4 means of the FP32 residual), s = RMS(rc).
+__global__ void k_pc_restrict(Geo g, Dims c, const float* __restrict__ r, float* __restrict__ rc,
+                              double* partials, float* scal, CgState* st) {
+  if (st->done) return;
+  double acc = 0.0;
+  NET_LOOP(c.v()) {
+    int i, j, k;
+    vox(c, t, &i, &j, &k);
+    float s = 0.f;
+    for (int kk = 0; kk < 4; ++kk)
+      for (int jj = 0; jj < 4; ++jj) {
+        const float4 v =
+            *reinterpret_cast<const float4*>(r + g.ix(4 * i + 1, 4 * j + jj + 1, 4 * k + kk + 1));
+        s += (v.x + v.y) + (v.z + v.w);
+      }
+    const float m = s * (1.f / 64.f);
+    rc[t] = m;
+    acc += (double)m * (double)m;
+  }
+  double v[1] = {acc}, tot[1];
+  if (grid_reduce<1>(v, partials, &st->counter[4], tot)) {
+    if (threadIdx.x == 0) {
+      const double s = sqrt(tot[0] / (double)c.v());
+      scal[0] = (float)s;
+      scal[1] = s > 0.0 ? (float)(1.0 / s) : 0.f;
+    }
+  }
+}
+
+__global__ void k_pc_pack(int64_t V, const float* __restrict__ rc, const float* scal,
+                          bf16* __restrict__ in0, const CgState* st) {
+  if (st->done) return;
+  const float inv = scal[1];
+  NET_LOOP(V) in0[t * kFeat] = __float2bfloat16_rn(rc[t] * inv);
+}
+
+// Interpolation weights of the 4 fine cells of one coarse cell along an
+// axis: fine cell e of coarse cell m lies at m - 3/8 + e/4 in coarse units.
+__device__ __forceinline__ void interp1(int fi, int n, int* lo, int* hi, float* wlo) {
+  const int m = fi >> 2, e = fi & 3;
+  const float wl[4] = {0.375f, 0.125f, 0.875f, 0.625f};
+  *lo = (e < 2) ? max(m - 1, 0) : m;
+  *hi = (e < 2) ? m : min(m + 1, n - 1);
+  *wlo = wl[e];
+}
+
+// z = invd*r + f * P(out) over the fine interior (4 y-consecutive cells per
+// item), f = s k_out / (scale c_ref); z.r and z.q_old reduced; the last
+// block sets rho, beta of the flexible CG.
+__global__ void __launch_bounds__(256)
+    k_pc_prolong(Geo g, Dims c, const float* __restrict__ out, const float* scal,
+                 const float* __restrict__ r, const float* __restrict__ iv,
+                 const float* __restrict__ q, float* __restrict__ z, const int* err,
+                 double* partials, CgState* st) {
+  if (st->done) return;
+  const float f = scal[0] * scal[2];
+  const int nchunk = g.ny / 4;
+  const int64_t n = (int64_t)nchunk * g.nx * g.nz;
+  float a_zr = 0.f, a_zq = 0.f;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(u % nchunk);
+    const int64_t rr = u / nchunk;
+    const int j = (int)(rr % g.nx) + 1;
+    const int k = (int)(rr / g.nx) + 1;
+    int x0, x1, z0, z1;
+    float wx, wz;
+    interp1(j - 1, c.nx, &x0, &x1, &wx);
+    interp1(k - 1, c.nz, &z0, &z1, &wz);
+    const int ym = max(m - 1, 0), yp = min(m + 1, c.ny - 1);
+    float col[3];  // y-neighbours (m-1, m, m+1) interpolated in x and z
+    const int ys[3] = {ym, m, yp};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float v00 = out[(int64_t)ys[a] + (int64_t)c.ny * (x0 + (int64_t)c.nx * z0)];
+      const float v10 = out[(int64_t)ys[a] + (int64_t)c.ny * (x1 + (int64_t)c.nx * z0)];
+      const float v01 = out[(int64_t)ys[a] + (int64_t)c.ny * (x0 + (int64_t)c.nx * z1)];
+      const float v11 = out[(int64_t)ys[a] + (int64_t)c.ny * (x1 + (int64_t)c.nx * z1)];
+      col[a] = wz * (wx * v00 + (1.f - wx) * v10) + (1.f - wz) * (wx * v01 + (1.f - wx) * v11);
+    }
+    const float e4[4] = {0.375f * col[0] + 0.625f * col[1], 0.125f * col[0] + 0.875f * col[1],
+                         0.875f * col[1] + 0.125f * col[2], 0.625f * col[1] + 0.375f * col[2]};
+    const int64_t idx = g.ix(4 * m + 1, j, k);
+    const float4 rv = *reinterpret_cast<const float4*>(r + idx);
+    const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
+    const float4 qv = *reinterpret_cast<const float4*>(q + idx);
+    float4 zv;
+    zv.x = dv.x * rv.x + f * e4[0];
+    zv.y = dv.y * rv.y + f * e4[1];
+    zv.z = dv.z * rv.z + f * e4[2];
+    zv.w = dv.w * rv.w + f * e4[3];
+    *reinterpret_cast<float4*>(z + idx) = zv;
+    a_zr += (zv.x * rv.x + zv.y * rv.y) + (zv.z * rv.z + zv.w * rv.w);
+    a_zq += (zv.x * qv.x + zv.y * qv.y) + (zv.z * qv.z + zv.w * qv.w);
+  }
+  double v[2] = {(double)a_zr, (double)a_zq}, tot[2];
+  if (grid_reduce<2>(v, partials, &st->counter[5], tot)) {
+    if (threadIdx.x == 0) {
+      const double zr = tot[0];
+      const double beta = st->initial ? 0.0 : -tot[1] / st->pq;
+      st->initial = 0;
+      st->rho = zr;
+      st->beta = beta;
+      if (*err) st->done = 5;
+      else if (!isfinite(zr) || !isfinite(beta)) st->done = 3;
+    }
+  }
+}
+
+struct NetPc {
+  sbm_net* net = nullptr;
+  double kout = 1.0;
+  Dims c{};
+  Work* w = nullptr;
+  float* rc = nullptr;
+  float* coefc = nullptr;
+  float* zf = nullptr;   // FP32 z (g32 layout)
+  float* scal = nullptr; // s, 1/s, k_out/(scale c_ref), c_ref
+  double* parts = nullptr;
+  unsigned* cnt = nullptr;
+  void release() {
+    delete w;
+    w = nullptr;
+    cudaFree(rc);
+    cudaFree(coefc);
+    cudaFree(zf);
+    cudaFree(scal);
+    cudaFree(parts);
+    cudaFree(cnt);
+    rc = coefc = zf = scal = nullptr;
+    parts = nullptr;
+    cnt = nullptr;
+  }
+};
+
+}  // namespace netd
+
+bool net_pc_usable(const sbm_ctx* ctx, int form) {
+  const netd::NetPc* pc = static_cast<const netd::NetPc*>(ctx->net);
+  const Geo& g = ctx->g;
+  return pc && pc->net && form == 0 && g.ny % 64 == 0 && g.nx % 64 == 0 && g.nz % 64 == 0;
+}
+
+int net_pc_begin(sbm_ctx* ctx, const float* hk32, double scale, int bcx0, int bcx1,
+                 cudaStream_t s) {
+  netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
+  int rc = conv3_init();
+  if (rc) return rc;
+  const Geo& g = ctx->g32;
+  const netd::Dims c{g.ny / 4, g.nx / 4, g.nz / 4, g.nz / 4};
+  if (!pc->w || pc->c.ny != c.ny || pc->c.nx != c.nx || pc->c.nz != c.nz) {
+    pc->release();
+    pc->c = c;
+    pc->w = netd::make_work(c, false);
+    if (!pc->w || cudaMalloc(&pc->rc, sizeof(float) * c.v()) ||
+        cudaMalloc(&pc->coefc, sizeof(float) * c.v()) ||
+        cudaMalloc(&pc->zf, sizeof(float) * g.nh) || cudaMalloc(&pc->scal, sizeof(float) * 8) ||
+        cudaMalloc(&pc->parts, sizeof(double) * 152 * 16) ||
+        cudaMalloc(&pc->cnt, sizeof(unsigned) * 4)) {
+      pc->release();
+      return SBM_ERR_NOMEM;
+    }
+    SBM_CUDA_TRY(cudaMemsetAsync(pc->zf, 0, sizeof(float) * g.nh, s));
+    SBM_CUDA_TRY(cudaMemsetAsync(pc->cnt, 0, sizeof(unsigned) * 4, s));
+    SBM_CUDA_TRY(cudaMemsetAsync(pc->scal, 0, sizeof(float) * 8, s));
+  }
+  netd::k_pc_coef<<<netd::grid_for(c.v()), 256, 0, s>>>(g, c, hk32, pc->coefc, pc->parts, pc->cnt,
+                                                         pc->scal, pc->kout, scale);
+  netd::k_pc_feat<<<netd::grid_for(c.v()), 256, 0, s>>>(c, pc->coefc, pc->scal, bcx0, bcx1,
+                                                         pc->w->in0);
+  SBM_LAUNCHED(2);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
+float* net_pc_zbuf(sbm_ctx* ctx) {
+  netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
+  return pc->zf + kOff32;
+}
+
+int net_pc_nodes() { return 3 + 9 + 4 + 4 + 1; }
+
+void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const float* q32,
+                   double* partials, CgState* st, cudaStream_t s) {
+  netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
+  const Geo& g = ctx->g32;
+  const netd::Dims& c = pc->c;
+  netd::k_pc_restrict<<<netd::grid_for(c.v()), 256, 0, s>>>(g, c, r32, pc->rc, partials, pc->scal,
+                                                             st);
+  netd::k_pc_pack<<<netd::grid_for(c.v()), 256, 0, s>>>(c.v(), pc->rc, pc->scal, pc->w->in0, st);
+  SBM_LAUNCHED(2);
+  netd::forward(pc->net, *pc->w, false, &st->done, s);
+  const int64_t items = (int64_t)(g.ny / 4) * g.nx * g.nz;
+  int64_t b = (items + 256 * 4 - 1) / (256 * 4);
+  if (b > 152 * 8) b = 152 * 8;
+  if (b < 1) b = 1;
+  netd::k_pc_prolong<<<(unsigned)b, 256, 0, s>>>(g, c, pc->w->out, pc->scal, r32, iv32, q32,
+                                                 pc->zf + kOff32, pc->net->err, partials, st);
+  SBM_LAUNCHED(1);
+}
+
+void net_pc_release(sbm_ctx* ctx) {
+  netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
+  if (!pc) return;
+  pc->release();
+  delete pc;
+  ctx->net = nullptr;
+}
+
+}  // namespace sbm
+
+// ------------------------------------------------------------- C-ABI
+
+extern "C" {
+
+int64_t sbm_net_param_count(void) { return kL.total; }
+
+int sbm_net_create(uint64_t seed, sbm_net** out) {
+  if (!out) return SBM_ERR_ARG;
+  *out = nullptr;
+  int rc = conv3_init();
+  if (rc) return rc;
+  sbm_net* n = new sbm_net();
+  const int64_t P = kL.total;
+  if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) ||
+      cudaMalloc(&n->w32, sizeof(float) * P) || cudaMalloc(&n->m, sizeof(float) * P) ||
+      cudaMalloc(&n->v, sizeof(float) * P) || cudaMalloc(&n->grad, sizeof(float) * P) ||
+      cudaMalloc(&n->w16, sizeof(bf16) * P) || cudaMalloc(&n->wt16, sizeof(bf16) * P) ||
+      cudaMalloc(&n->err, sizeof(int)) || cudaMalloc(&n->loss, sizeof(double))) {
+    sbm_net_destroy(n);
+    return SBM_ERR_NOMEM;
+  }
+  // He-normal initialisation of the convolutions, zero biases, small output layer
+  std::vector<float> h((size_t)P, 0.f);
+  uint64_t st = seed * 0x2545F4914F6CDD1Dull + 1;
+  for (int l = 0; l < NLAYER; ++l) {
+    const int taps = (l == OUT) ? 1 : 27;
+    const int64_t nw = (int64_t)kCo[l] * taps * kCi[l];
+    const double sd = (l == OUT) ? 0.1 : sqrt(2.0 / (taps * kCi[l]));
+    for (int64_t i = 0; i < nw; ++i) {
+      const double u1 = unit(&st), u2 = unit(&st);
+      h[(size_t)(kL.off[l] + i)] = (float)(sd * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+    }
+  }
+  rc = sbm_net_set_params(n, h.data(), P);
+  if (rc) {
+    sbm_net_destroy(n);
+    return rc;
+  }
+  *out = n;
+  return SBM_OK;
+}
+
+int sbm_net_destroy(sbm_net* n) {
+  if (!n) return SBM_ERR_ARG;
+  if (n->stream) cudaStreamSynchronize(n->stream);
+  for (auto& kv : n->works) delete kv.second;
+  void* p[] = {n->w32, n->m, n->v, n->grad, n->w16, n->wt16, n->err, n->loss};
+  for (void* q : p) cudaFree(q);
+  if (n->stream) cudaStreamDestroy(n->stream);
+  delete n;
+  return SBM_OK;
+}
+
+int sbm_net_get_params(const sbm_net* n, float* host, int64_t count) {
+  if (!n || !host || count != kL.total) return SBM_ERR_ARG;
+  SBM_CUDA_TRY(cudaMemcpyAsync(host, n->w32, sizeof(float) * count, cudaMemcpyDeviceToHost,
+                               n->stream));
+  SBM_CUDA_TRY(cudaStreamSynchronize(n->stream));
+  return SBM_OK;
+}
+
+int sbm_net_set_params(sbm_net* n, const float* host, int64_t count) {
+  if (!n || !host || count != kL.total) return SBM_ERR_ARG;
+  cudaStream_t s = n->stream;
+  SBM_CUDA_TRY(cudaMemcpyAsync(n->w32, host, sizeof(float) * count, cudaMemcpyHostToDevice, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(n->m, 0, sizeof(float) * count, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(n->v, 0, sizeof(float) * count, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(n->err, 0, sizeof(int), s));
+  SBM_CUDA_TRY(cudaMemsetAsync(n->loss, 0, sizeof(double), s));
+  n->step = 0;
+  int rc = cast_weights(n, s);
+  if (rc) return rc;
+  SBM_CUDA_TRY(cudaStreamSynchronize(s));
+  return SBM_OK;
+}
+
+int sbm_net_forward(sbm_net* n, int ny, int nx, int nz, int nb, const float* in, float* out) {
+  if (!n || !in || !out || nb < 1 || !dims_ok(ny, nx, nz)) return SBM_ERR_ARG;
+  Work* w = work_for(n, ny, nx, nz, nb, false);
+  if (!w) return SBM_ERR_NOMEM;
+  const int64_t V = w->d[0].v();
+  int rc = upload_bf16(w->in0, in, V * kFeat, n->stream);
+  if (rc) return rc;
+  if ((rc = forward(n, *w, false, nullptr, n->stream))) return rc;
+  SBM_CUDA_TRY(cudaMemcpyAsync(out, w->out, sizeof(float) * V, cudaMemcpyDeviceToHost, n->stream));
+  return check_err(n);
+}
+
+int sbm_net_loss_grad(sbm_net* n, int ny, int nx, int nz, int nb, const float* in,
+                      const float* target, double* loss, float* grad) {
+  if (!n || !in || !target || nb < 1 || !dims_ok(ny, nx, nz)) return SBM_ERR_ARG;
+  Work* w = work_for(n, ny, nx, nz, nb, true);
+  if (!w) return SBM_ERR_NOMEM;
+  cudaStream_t s = n->stream;
+  const int64_t V = w->d[0].v();
+  int rc = upload_bf16(w->in0, in, V * kFeat, s);
+  if (rc) return rc;
+  SBM_CUDA_TRY(cudaMemcpyAsync(w->tgt, target, sizeof(float) * V, cudaMemcpyHostToDevice, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(n->loss, 0, sizeof(double), s));
+  if ((rc = forward(n, *w, true, nullptr, s))) return rc;
+  if ((rc = backward(n, *w, s))) return rc;
+  double h = 0.0;
+  SBM_CUDA_TRY(cudaMemcpyAsync(&h, n->loss, sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (grad)
+    SBM_CUDA_TRY(cudaMemcpyAsync(grad, n->grad, sizeof(float) * kL.total, cudaMemcpyDeviceToHost, s));
+  if ((rc = check_err(n))) return rc;
+  if (loss) *loss = h / (double)V;
+  return SBM_OK;
+}
+
+int sbm_net_train(sbm_net* n, int ny, int nx, int nz, int nsamples, const float* in,
+                  const float* target, int steps, int batch, float lr, uint64_t seed,
+                  float* loss_hist) {
+  if (!n || !in || !target || nsamples < 1 || steps < 1 || batch < 1 || !(lr > 0.f) ||
+      !dims_ok(ny, nx, nz))
+    return SBM_ERR_ARG;
+  Work* w = work_for(n, ny, nx, nz, batch, true);
+  if (!w) return SBM_ERR_NOMEM;
+  cudaStream_t s = n->stream;
+  const int64_t Vs = (int64_t)ny * nx * nz;
+  bf16* din = nullptr;
+  float *dt = nullptr, *hist = nullptr;
+  auto fail = [&](int code) {
+    cudaStreamSynchronize(s);
+    cudaFree(din);
+    cudaFree(dt);
+    cudaFree(hist);
+    return code;
+  };
+  if (cudaMalloc(&din, sizeof(bf16) * Vs * kFeat * nsamples) ||
+      cudaMalloc(&dt, sizeof(float) * Vs * nsamples) || cudaMalloc(&hist, sizeof(float) * steps))
+    return fail(SBM_ERR_NOMEM);
+  int rc = upload_bf16(din, in, Vs * kFeat * nsamples, s);
+  if (rc) return fail(rc);
+  if (cudaMemcpyAsync(dt, target, sizeof(float) * Vs * nsamples, cudaMemcpyHostToDevice, s) ||
+      cudaMemsetAsync(n->loss, 0, sizeof(double), s))
+    return fail(SBM_ERR_CUDA);
+  uint64_t st = seed * 0x9E3779B97F4A7C15ull + 7;
+  const float inv_v = 1.0f / (float)(Vs * batch);
+  for (int it = 0; it < steps; ++it) {
+    for (int b = 0; b < batch; ++b) {
+      const int64_t q = (int64_t)(splitmix(&st) % (uint64_t)nsamples);
+      if (cudaMemcpyAsync(w->in0 + b * Vs * kFeat, din + q * Vs * kFeat, sizeof(bf16) * Vs * kFeat,
+                          cudaMemcpyDeviceToDevice, s) ||
+          cudaMemcpyAsync(w->tgt + b * Vs, dt + q * Vs, sizeof(float) * Vs,
+                          cudaMemcpyDeviceToDevice, s))
+        return fail(SBM_ERR_CUDA);
+    }
+    if ((rc = forward(n, *w, true, nullptr, s))) return fail(rc);
+    if ((rc = backward(n, *w, s))) return fail(rc);
+    if ((rc = adam(n, lr, s))) return fail(rc);
+    k_loss_rec<<<1, 1, 0, s>>>(n->loss, inv_v, hist + it);
+    SBM_LAUNCHED(1);
+  }
+  if (loss_hist &&
+      cudaMemcpyAsync(loss_hist, hist, sizeof(float) * steps, cudaMemcpyDeviceToHost, s))
+    return fail(SBM_ERR_CUDA);
+  if ((rc = check_err(n))) return fail(rc);
+  return fail(SBM_OK);
+}
+
+int sbm_ctx_set_net(sbm_ctx* ctx, sbm_net* n, double out_scale) {
+  if (!ctx || !(out_scale > 0.0)) return SBM_ERR_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  release_graphs(ctx);
+  if (!n) {
+    net_pc_release(ctx);
+    return SBM_OK;
+  }
+  NetPc* pc = static_cast<NetPc*>(ctx->net);
+  if (!pc) {
+    pc = new NetPc();
+    ctx->net = pc;
+  }
+  pc->net = n;
+  pc->kout = out_scale;
+  return SBM_OK;
+}
+
+}  // extern "C"

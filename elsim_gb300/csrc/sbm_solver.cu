@@ -23,8 +23,10 @@
 //         accumulated in FP64, without restarting the Krylov space.
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "sbm_internal.cuh"
+#include "sbm_net.cuh"
 
 namespace sbm {
 
@@ -702,7 +704,9 @@ __device__ __forceinline__ int64_t item_ix(const Geo& g, int nchunk, int64_t u, 
 // threads); decides whether the next step is a reliable update.  After a
 // reliable update the FP32 correction accumulated so far is first folded
 // into the FP64 one (d64 += x32, x32 = alpha p).
-template <bool PC, int VEC>
+// FLEX (flexible CG with the learned preconditioner): rho and beta are left
+// to the preconditioner kernel that follows.
+template <bool PC, int VEC, bool FLEX = false>
 __global__ void __launch_bounds__(256)
     k32_update(Geo g, Geo g64, int nchunk, float* __restrict__ x, const float* __restrict__ p,
                float* __restrict__ r, const float* __restrict__ q, const float* __restrict__ invd,
@@ -769,7 +773,7 @@ __global__ void __launch_bounds__(256)
                           (rr_new <= st->tol * st->tol * st->aux[0]) || (it >= st->max_it);
         if (trig) {
           st->reliable = 1;
-        } else {
+        } else if (!FLEX) {
           st->beta = rho_new / st->rho;
           st->rho = rho_new;
         }
@@ -783,7 +787,9 @@ __global__ void __launch_bounds__(256)
 // Reliable update: r = r0 - A_h (d64 + x32) in FP64 (ghost rules of the
 // search direction on the correction), r32 = (float) r, z = invd*r32;
 // convergence on the FP64 norm, new rho / beta.  No-op unless flagged.
-template <int FORM, bool PC>
+// FLEX: rho / beta and the first-residual flag are left to the flexible
+// preconditioner kernel that follows.
+template <int FORM, bool PC, bool FLEX = false>
 __global__ void __launch_bounds__(BX* BY)
     k_rel_resid(OpArgs<double> op, Geo g32, int zc, const double* __restrict__ d64,
                 const float* __restrict__ x32, const double* __restrict__ r0,
@@ -828,12 +834,14 @@ __global__ void __launch_bounds__(BX* BY)
       if (!isfinite(rms)) st->done = 3;
       else if (!(rms > st->tol)) st->done = 1;
       else if (st->iter >= st->max_it) st->done = 2;
-      st->beta = st->initial ? 0.0 : tot[2] / st->rho;
       if (st->initial) st->aux[0] = tot[1];
-      st->rho = tot[2];
+      if (!FLEX) {
+        st->beta = st->initial ? 0.0 : tot[2] / st->rho;
+        st->rho = tot[2];
+        st->initial = 0;
+      }
       st->rr = tot[1];
       st->maxrr = tot[1];
-      st->initial = 0;
       st->reliable = 0;
       st->accum_pending = 1;
     }
@@ -910,7 +918,10 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   OpArgs<double> op64{g, sp.hk64, sp.diag64, sp.scale, sp.form, sp.bcx0, sp.bcx1};
   OpArgs<float> op32{g32, hk32, sp.form ? dg32 : nullptr, (float)sp.scale, sp.form, sp.bcx0,
                      sp.bcx1};
-  const bool pc = sp.precond == SBM_PC_JACOBI;
+  // learned preconditioner when usable, else Jacobi (the documented fallback)
+  const bool learned = sp.precond == SBM_PC_LEARNED && net_pc_usable(ctx, sp.form) && vec == 4;
+  const bool pc = sp.precond == SBM_PC_JACOBI || (sp.precond == SBM_PC_LEARNED && !learned);
+  ctx->last_precond = learned ? SBM_PC_LEARNED : (pc ? SBM_PC_JACOBI : SBM_PC_NONE);
   const double delta = ctx->inner_tol > 0 ? ctx->inner_tol : 0.1;
   CgState* h = &ctx->h_st[2];
   memset(h, 0, sizeof(CgState));
@@ -929,10 +940,14 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
                                          dg32);
   SBM_LAUNCHED(1);
-  if (pc) {
+  if (pc || learned) {
     k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
     SBM_LAUNCHED(1);
   }
+  if (learned && (rc = net_pc_begin(ctx, hk32, sp.scale, sp.bcx0, sp.bcx1, s))) return rc;
+  // with the learned preconditioner the direction kernels read z from its buffer
+  float* const zl = learned ? net_pc_zbuf(ctx) : nullptr;
+  const float* const rdir = learned ? zl : r32;
   // r0 = b - A x0 with x0's stored ghosts (FP64); sets rr0.
   if (sp.form == 0)
     k_residual_mem<0, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x,
@@ -952,7 +967,10 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   k_rel_resid<F, P><<<sh64.grid, sh64.block, 0, s2>>>(op64, g32, sh64.zc, ctx->d64, x32,      \
                                                        ctx->r0, r32, iv32, ctx->partials,      \
                                                        ctx->st)
-    if (sp.form == 0) {
+    if (learned) {
+      k_rel_resid<0, false, true><<<sh64.grid, sh64.block, 0, s2>>>(
+          op64, g32, sh64.zc, ctx->d64, x32, ctx->r0, r32, iv32, ctx->partials, ctx->st);
+    } else if (sp.form == 0) {
       if (pc) SBM_REL(0, true); else SBM_REL(0, false);
     } else {
       if (pc) SBM_REL(1, true); else SBM_REL(1, false);
@@ -965,21 +983,22 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   TmaPlan* plan = reinterpret_cast<TmaPlan*>(plan_buf.data());
   if (use_tma) {
     if ((rc = tma_init())) return rc;
-    if ((rc = tma_plan(g32, ctx->r32, ctx->p32, ctx->rold32, ctx->hk32, ctx->z32, ctx->dg32,
-                       pc ? 1 : 0, sp.form, ctx->zc32, plan)))
+    if ((rc = tma_plan(g32, learned ? zl - kOff32 : ctx->r32, ctx->p32, ctx->rold32, ctx->hk32,
+                       ctx->z32, ctx->dg32, pc ? 1 : 0, sp.form, ctx->zc32, plan)))
       return rc;
   }
   // one iteration reading direction buffer `in` and writing `out`
   auto iter = [&](cudaStream_t s2, const float* in, float* out) {
+    if (learned) net_pc_launch(ctx, r32, iv32, q32, ctx->partials, ctx->st, s2);
 #define SBM_AD(F, P)                                                                           \
   do {                                                                                         \
     if (use_tma)                                                                               \
       tma_launch(*plan, in == pbuf[0], op32, out, q32, ctx->partials, ctx->st, s2);            \
     else if (vec == 4)                                                                         \
-      k32v_apply_dir<F, P><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, r32, in, iv32, out, q32, \
+      k32v_apply_dir<F, P><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, rdir, in, iv32, out, q32, \
                                                    ctx->partials, ctx->st);                    \
     else                                                                                       \
-      k32s_apply_dir<F, P><<<sh32.grid, sh32.block, 0, s2>>>(op32, sh32.zc, r32, in, iv32,     \
+      k32s_apply_dir<F, P><<<sh32.grid, sh32.block, 0, s2>>>(op32, sh32.zc, rdir, in, iv32,    \
                                                               out, q32, ctx->partials,         \
                                                               ctx->st);                        \
   } while (0)
@@ -992,7 +1011,10 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
 #define SBM_UP(P, V)                                                                         \
   k32_update<P, V><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, x32, out, r32, q32, iv32, ctx->d64, \
                                           ctx->partials, ctx->st)
-    if (vec == 4) {
+    if (learned) {
+      k32_update<false, 4, true><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, x32, out, r32, q32, iv32,
+                                                        ctx->d64, ctx->partials, ctx->st);
+    } else if (vec == 4) {
       if (pc) SBM_UP(true, 4); else SBM_UP(false, 4);
     } else {
       if (pc) SBM_UP(true, 1); else SBM_UP(false, 1);
@@ -1011,11 +1033,12 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   const std::string key =
-      key_of(use_tma ? "mixrel2-tma" : "mixrel2", hk32, dg32, x32, r32, pbuf[0], pbuf[1], iv32,
-             sp.scale, sp.form, sp.bcx0, sp.bcx1, vec * 16 + zc32, pc, sh64.zc, chunk_len(ctx));
+      key_of(learned ? (use_tma ? "mixfcg2-tma" : "mixfcg2") : (use_tma ? "mixrel2-tma" : "mixrel2"),
+             hk32, dg32, x32, r32, pbuf[0], pbuf[1], learned ? (const void*)zl : iv32, sp.scale,
+             sp.form, sp.bcx0, sp.bcx1, vec * 16 + zc32, pc, sh64.zc, chunk_len(ctx));
   cudaGraphExec_t ex = nullptr;
   int nodes = 0;
-  rc = capture_graph(ctx, key, 6, body, &ex, &nodes);
+  rc = capture_graph(ctx, key, learned ? 2 * (3 + net_pc_nodes()) : 6, body, &ex, &nodes);
   if (rc) return rc;
   ctx->last_op32 = op32;
   ctx->last_pc = pc ? 1 : 0;
@@ -1044,6 +1067,53 @@ int mixed_end(sbm_ctx* ctx, const SolveSpec& sp, const CgState& fin, SolveResult
   out->final_res = fin.rms;
   out->ms = ms;
   out->status = status_of(fin.done);
+  return SBM_OK;
+}
+
+// One application of the learned preconditioner to a host residual
+// (halo-padded FP64, interior used) on the solve spec's operator; z gets
+// the interior of M(r), ghosts zero.  For checking the preconditioner
+// against an independent restatement.
+int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double* z) {
+  if (!net_pc_usable(ctx, sp.form) || ctx->g.ny % 4) return SBM_ERR_STATE;
+  int rc = ensure_fp32_work(ctx);
+  if (rc) return rc;
+  const Geo& g = ctx->g;
+  const Geo& g32 = ctx->g32;
+  cudaStream_t s = ctx->stream;
+  float* const hk32 = ctx->hk32 + kOff32;
+  float* const iv32 = ctx->z32 + kOff32;
+  float* const r32 = ctx->r32 + kOff32;
+  float* const q32 = ctx->q32 + kOff32;
+  OpArgs<float> op32{g32, hk32, nullptr, (float)sp.scale, sp.form, sp.bcx0, sp.bcx1};
+  const Shape sh32 = stencil_shape(g32, pick_zc(g32, ctx->zc32));
+  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, nullptr, nullptr);
+  k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
+  SBM_LAUNCHED(2);
+  if ((rc = net_pc_begin(ctx, hk32, sp.scale, sp.bcx0, sp.bcx1, s))) return rc;
+  SBM_CUDA_TRY(cudaMemcpyAsync(ctx->r64, r, sizeof(double) * g.nh, cudaMemcpyHostToDevice, s));
+  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, ctx->r64, r32, nullptr, nullptr);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->q32, 0, sizeof(float) * g32.nh, s));
+  CgState* h = &ctx->h_st[2];
+  memset(h, 0, sizeof(CgState));
+  h->initial = 1;
+  SBM_CUDA_TRY(cudaMemcpyAsync(ctx->st32, h, sizeof(CgState), cudaMemcpyHostToDevice, s));
+  net_pc_launch(ctx, r32, iv32, q32, ctx->partials, ctx->st32, s);
+  SBM_CUDA_TRY(cudaGetLastError());
+  std::vector<float> hz((size_t)g32.nh);
+  SBM_CUDA_TRY(cudaMemcpyAsync(hz.data(), net_pc_zbuf(ctx) - kOff32, sizeof(float) * g32.nh,
+                               cudaMemcpyDeviceToHost, s));
+  SBM_CUDA_TRY(cudaMemcpyAsync(h, ctx->st32, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+  SBM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h->done == 5) {
+    set_error_msg("tensor-core convolution wait expired");
+    return SBM_ERR_TIMEOUT;
+  }
+  memset(z, 0, sizeof(double) * g.nh);
+  for (int k = 1; k <= g.nz; ++k)
+    for (int j = 1; j <= g.nx; ++j)
+      for (int i = 1; i <= g.ny; ++i) z[g.ix(i, j, k)] = hz[(size_t)(kOff32 + g32.ix(i, j, k))];
   return SBM_OK;
 }
 

@@ -1,0 +1,212 @@
+"""Learned coarse-grid preconditioner: training data, training recipe and the
+stored weights (no counterpart in the reference, whose CG loops are
+unpreconditioned).
+
+The network (``sbm.Net``, kernels in csrc/sbm_net.cu) maps the features of a
+residual r on the 4x-coarsened grid to the restricted error R(A^-1 r),
+normalised:
+
+    input  f = [R r / s, R K / c_ref, 1, x0 Dirichlet face, x1 Dirichlet face, 0...]
+    target t = R(A^-1 r) * scale * c_ref / (s * k_out)
+
+with s = RMS(R r), c_ref = mean(R K) and one constant k_out (stored with
+the weights) that brings the targets to unit RMS.  Pairs (r, A^-1 r) come
+from the library's own mixed-precision solver on seeded synthetic
+microstructures (``synth.microstructure``) and right-hand sides of several
+spectra; training runs on the GPU (``Net.train``).
+
+``python -m elsim_gb300.learned --out FILE`` reproduces the stored weights
+``elsim_gb300/weights/pc_unet.npz``.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import sbm, synth
+
+WEIGHTS = Path(__file__).resolve().parent / "weights" / "pc_unet.npz"
+NFEAT = 16
+
+
+# ------------------------------------------------------------- features
+
+def restrict(a: np.ndarray) -> np.ndarray:
+    """Means over 4x4x4 blocks of an interior array [i, j, k]."""
+    ny, nx, nz = a.shape
+    return a.reshape(ny // 4, 4, nx // 4, 4, nz // 4, 4).mean(axis=(1, 3, 5))
+
+
+def features(r_int: np.ndarray, coef_int: np.ndarray, bcx0: int, bcx1: int):
+    """(input [V][16] channels-last float32, s, c_ref) of one residual."""
+    rc = restrict(r_int)
+    cc = restrict(coef_int)
+    s = float(np.sqrt((rc ** 2).mean()))
+    cref = float(cc.mean())
+    f = np.zeros(rc.shape + (NFEAT,), dtype=np.float32)
+    f[..., 0] = rc / s if s > 0 else 0.0
+    f[..., 1] = cc / cref
+    f[..., 2] = 1.0
+    if bcx0 == sbm.BC_ZERO:
+        f[:, 0, :, 3] = 1.0
+    if bcx1 == sbm.BC_ZERO:
+        f[:, -1, :, 4] = 1.0
+    # [i, j, k, c] -> voxel v = i + ny*(j + nx*k)
+    return np.ascontiguousarray(np.transpose(f, (2, 1, 0, 3)).reshape(-1, NFEAT)), s, cref
+
+
+def target(e_int: np.ndarray, s: float, cref: float, scale: float, kout: float) -> np.ndarray:
+    t = restrict(e_int) * (scale * cref / (s * kout))
+    return np.ascontiguousarray(np.transpose(t, (2, 1, 0)).reshape(-1).astype(np.float32))
+
+
+# ------------------------------------------------------------- data
+
+def _smooth(a: np.ndarray, sigma: float) -> np.ndarray:
+    """Separable Gaussian blur (reflecting edges) of an interior field."""
+    if sigma <= 0:
+        return a
+    r = int(np.ceil(3 * sigma))
+    x = np.arange(-r, r + 1)
+    w = np.exp(-0.5 * (x / sigma) ** 2)
+    w /= w.sum()
+    out = a
+    for ax in range(3):
+        pad = [(0, 0)] * 3
+        pad[ax] = (r, r)
+        p = np.pad(out, pad, mode="reflect")
+        acc = np.zeros_like(out)
+        for q, wq in enumerate(w):
+            sl = [slice(None)] * 3
+            sl[ax] = slice(q, q + out.shape[ax])
+            acc += wq * p[tuple(sl)]
+        out = acc
+    return out
+
+
+def rhs_family(shape, rng, coef_h, scale=1.0):
+    """Right-hand sides of several spectra for one microstructure: white
+    noise, Gaussian-smoothed noise (sigma 1..8 cells), a face source like
+    the initial residual of the Dirichlet potential solve, and a mixture."""
+    ny, nx, nz = shape
+    out = []
+    out.append(rng.normal(size=shape))
+    for sig in (1.0, 2.5, 6.0):
+        out.append(_smooth(rng.normal(size=shape), sig))
+    face = np.zeros(shape)
+    hk = 0.5 * coef_h
+    lvl = rng.uniform(0.5, 1.5)
+    face[:, -1, :] = -scale * (hk[1:-1, -1, 1:-1] + hk[1:-1, -2, 1:-1]) * lvl
+    if rng.uniform() < 0.5:
+        face[:, 0, :] = -scale * (hk[1:-1, 0, 1:-1] + hk[1:-1, 1, 1:-1]) * rng.uniform(-1, 1)
+    out.append(face)
+    out.append(_smooth(rng.normal(size=shape), 3.0) + 0.2 * rng.normal(size=shape))
+    return out
+
+
+def make_pairs(n: int, seeds, tol: float = 1e-7, scale: float = 1.0, verbose: bool = False):
+    """(features, s, c_ref, coarse error) for every right-hand side of
+    rhs_family on the seeded n^3 microstructures; errors from the library's
+    mixed-precision Jacobi-CG (Dirichlet zero on both x faces)."""
+    feats, errs, meta = [], [], []
+    shape = (n, n, n)
+    for seed in seeds:
+        t0 = time.time()
+        rng = np.random.default_rng(1000 + seed)
+        frac = float(rng.uniform(0.45, 0.7))
+        ms = synth.microstructure(shape, seed=seed, solid_fraction=frac, tunnel=bool(seed % 2))
+        prob = synth.potential_problem(ms["psi"])
+        coef = prob["coef"]
+        with sbm.Context(n, n, n) as ctx:
+            ctx.upload("coef", coef)
+            ctx.upload("weight", prob["weight"])
+            for r in rhs_family(shape, rng, coef, scale):
+                rh = np.zeros(ctx.hshape, order="F")
+                rh[1:-1, 1:-1, 1:-1] = r
+                ctx.upload("rhs", rh)
+                ctx.upload("x", np.zeros(ctx.hshape, order="F"))
+                ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO,
+                             scale=scale, tol=tol, stop_rule=sbm.STOP_REL_RES,
+                             precision=sbm.PREC_MIXED, precond=sbm.PC_JACOBI)
+                e = ctx.download("x")[1:-1, 1:-1, 1:-1]
+                f, s, cref = features(r, coef[1:-1, 1:-1, 1:-1], sbm.BC_ZERO, sbm.BC_ZERO)
+                feats.append(f)
+                errs.append(restrict(e) * (scale * cref / s))
+                meta.append((seed, s, cref))
+        if verbose:
+            print(f"  seed {seed}: {time.time() - t0:.1f} s", flush=True)
+    return feats, errs, meta
+
+
+def to_targets(errs, kout: float) -> np.ndarray:
+    return np.concatenate([np.transpose(e, (2, 1, 0)).reshape(-1) / kout for e in errs]).astype(
+        np.float32)
+
+
+# ------------------------------------------------------------- weights
+
+def save(path, net: "sbm.Net", info: dict) -> None:
+    path = Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    np.savez_compressed(path, params=net.params(), out_scale=np.float64(net.out_scale),
+                        **{k: np.asarray(v) for k, v in info.items()})
+
+
+def load(path=None) -> "sbm.Net":
+    """The stored network (default: the weights shipped with the package)."""
+    z = np.load(Path(path) if path else WEIGHTS)
+    return sbm.Net(params=z["params"], out_scale=float(z["out_scale"]))
+
+
+# ------------------------------------------------------------- training
+
+def train(sizes=((64, 48), (128, 24)), steps=(1500, 800), batch=(8, 2), lr=(2e-3, 5e-4),
+          seed: int = 0, verbose: bool = True):
+    """Training recipe of the stored weights: for each (n, structures) stage
+    build pairs at n^3 (coarse n/4) and run Adam on the GPU; k_out from the
+    first stage's targets.  Returns (net, info)."""
+    net = sbm.Net(seed=seed)
+    kout = None
+    hist_all = []
+    for (n, nseeds), st, b, eta in zip(sizes, steps, batch, lr):
+        t0 = time.time()
+        seeds = range(seed * 1000 + n, seed * 1000 + n + nseeds)
+        feats, errs, _ = make_pairs(n, seeds, verbose=verbose)
+        if kout is None:
+            kout = float(np.sqrt(np.mean(np.concatenate([e.ravel() ** 2 for e in errs]))))
+            net.out_scale = kout
+        x = np.concatenate(feats)
+        t = to_targets(errs, kout)
+        dims = (n // 4, n // 4, n // 4)
+        if verbose:
+            print(f"stage n={n}: {len(feats)} pairs in {time.time() - t0:.1f} s", flush=True)
+        t1 = time.time()
+        # step-decayed learning rate within the stage
+        for part, f in ((0.6, 1.0), (0.3, 0.3), (0.1, 0.1)):
+            h = net.train(x, t, dims, steps=max(1, int(st * part)), batch=b, lr=eta * f,
+                          seed=seed + n + int(100 * f))
+            hist_all.append(h)
+        if verbose:
+            h = np.concatenate(hist_all)
+            print(f"  trained {st} steps in {time.time() - t1:.1f} s; loss {h[:20].mean():.4f}"
+                  f" -> {h[-20:].mean():.4f}", flush=True)
+    info = dict(sizes=np.array(sizes), steps=np.array(steps), batch=np.array(batch),
+                lr=np.array(lr), seed=seed, loss=np.concatenate(hist_all))
+    return net, info
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--out", default=str(WEIGHTS))
+    ap.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args(argv)
+    net, info = train(seed=a.seed)
+    save(a.out, net, info)
+    print("saved", a.out)
+
+
+if __name__ == "__main__":
+    main()

@@ -146,6 +146,18 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
         "sbm_rm_mask": (C.c_int, [i64, dp, dp, dp]),
         "sbm_sign": (C.c_int, [i64, dp, C.c_double, dp]),
+        "sbm_net_param_count": (i64, []),
+        "sbm_net_create": (C.c_int, [C.c_uint64, C.POINTER(vp)]),
+        "sbm_net_destroy": (C.c_int, [vp]),
+        "sbm_net_get_params": (C.c_int, [vp, fp, i64]),
+        "sbm_net_set_params": (C.c_int, [vp, fp, i64]),
+        "sbm_net_forward": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp]),
+        "sbm_net_loss_grad": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, dp, fp]),
+        "sbm_net_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int,
+                                    C.c_int, C.c_float, C.c_uint64, fp]),
+        "sbm_ctx_set_net": (C.c_int, [vp, vp, C.c_double]),
+        "sbm_ctx_last_precond": (C.c_int, [vp]),
+        "sbm_learned_pc_apply": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -294,6 +306,27 @@ class Context:
             _check(rc, "sbm_cg_solve")
         return dict(iters=it.value, final_res=res.value, ms=ms.value, status=rc)
 
+    def set_net(self, net: "Net | None", out_scale: float = 1.0) -> None:
+        """Attach the learned preconditioner (SBM_PC_LEARNED); None detaches.
+        The context keeps a reference so the network outlives it."""
+        self._net = net
+        _check(self.lib.sbm_ctx_set_net(self._h, net._h if net is not None else None,
+                                        out_scale if net is None else net.out_scale),
+               "sbm_ctx_set_net")
+
+    def last_precond(self) -> int:
+        """Preconditioner the last mixed-precision solve used (PC_*)."""
+        return int(self.lib.sbm_ctx_last_precond(self._h))
+
+    def learned_pc_apply(self, r, bc_x0=BC_ZERO, bc_x1=BC_ZERO, scale=1.0) -> np.ndarray:
+        """z = M(r) of the attached network for the GENERIC operator of the
+        uploaded coefficient (halo-padded arrays)."""
+        r = _f64(r, self.hshape)
+        z = np.zeros(self.hshape, dtype=np.float64, order="F")
+        _check(self.lib.sbm_learned_pc_apply(self._h, bc_x0, bc_x1, scale, _dptr(r), _dptr(z)),
+               "sbm_learned_pc_apply")
+        return z
+
     def time_step(self, it: int, dt: float, vsr: float, precision=PREC_FP64) -> dict:
         s = Scalars()
         _check(self.lib.sbm_time_step(self._h, it, dt, vsr, precision, C.byref(s)),
@@ -335,6 +368,76 @@ def batch_solve(contexts, bc_x0=BC_ZERO, bc_x1=BC_ZERO, scale=1.0, tol=1e-8, max
     _check(lib.sbm_batch_solve(hs, n, bc_x0, bc_x1, scale, tol, max_it, precond, it, res, stt,
                                C.byref(ms)), "sbm_batch_solve")
     return dict(iters=list(it), final_res=list(res), status=list(stt), ms=ms.value)
+
+
+class Net:
+    """The learned preconditioner's U-Net (sbm_net_*): parameters, forward
+    pass, loss gradient and on-GPU training.  Inputs are channels-last
+    (voxel v = i + ny*(j + nx*k), 16 channels), nb samples stacked along z."""
+
+    def __init__(self, seed: int = 0, params: np.ndarray | None = None, out_scale: float = 1.0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib.sbm_net_create(seed, C.byref(h)), "sbm_net_create")
+        self._h = h
+        self.out_scale = float(out_scale)
+        if params is not None:
+            self.set_params(params)
+
+    @staticmethod
+    def param_count() -> int:
+        return int(load_library().sbm_net_param_count())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.sbm_net_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.param_count(), dtype=np.float32)
+        _check(self.lib.sbm_net_get_params(self._h, _fptr(out), out.size), "sbm_net_get_params")
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(self.lib.sbm_net_set_params(self._h, _fptr(p), p.size), "sbm_net_set_params")
+
+    def forward(self, x, dims, nb: int = 1) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.empty(x.shape[0], dtype=np.float32)
+        _check(self.lib.sbm_net_forward(self._h, *dims, nb, _fptr(x), _fptr(out)),
+               "sbm_net_forward")
+        return out
+
+    def loss_grad(self, x, target, dims, nb: int = 1) -> tuple[float, np.ndarray]:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        g = np.empty(self.param_count(), dtype=np.float32)
+        loss = C.c_double(0)
+        _check(self.lib.sbm_net_loss_grad(self._h, *dims, nb, _fptr(x), _fptr(t), C.byref(loss),
+                                          _fptr(g)), "sbm_net_loss_grad")
+        return loss.value, g
+
+    def train(self, x, target, dims, steps: int, batch: int, lr: float, seed: int = 0) -> np.ndarray:
+        """x: (samples*V) x 16, target: samples*V; returns the loss per step."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        nv = int(np.prod(dims))
+        ns = t.size // nv
+        hist = np.empty(steps, dtype=np.float32)
+        _check(self.lib.sbm_net_train(self._h, *dims, ns, _fptr(x), _fptr(t), steps, batch, lr,
+                                      seed, _fptr(hist)), "sbm_net_train")
+        return hist
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
 # ------------------------------------------------------- stateless routines

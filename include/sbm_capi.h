@@ -283,6 +283,53 @@ int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const uint16_t* x
                     const uint16_t* w, const float* bias, int relu, int flip, int use_tc,
                     float* y);
 
+/* ---- Learned coarse-grid preconditioner (no counterpart in the reference).
+ *
+ * A 3D U-Net on the grid coarsened 4x per axis proposes the smooth part of
+ * the error: z = D^-1 r + P e_c with e_c = (s k_out / (scale c_ref)) N(f),
+ * R = 4x4x4 average, P = cell-centred trilinear interpolation, s = RMS(R r),
+ * c_ref = mean(R K); the input channels f (16 per coarse cell, voxel
+ * v = i + ny*(j + nx*k)) are [R r / s, R K / c_ref, 1, x0-face Dirichlet
+ * mask, x1-face Dirichlet mask, 0 x 11].  Because z is not linear in r the
+ * solver runs flexible CG (beta = -z.q_old / p_old.q_old).
+ * SBM_PC_LEARNED applies when a network is attached, the operator is the
+ * phP / phE / GENERIC form and ny, nx, nz are multiples of 64; otherwise the
+ * solve falls back to Jacobi (sbm_ctx_last_precond reports which ran).
+ * Only the mixed-precision solver takes it. */
+typedef struct sbm_net sbm_net;
+
+/* Number of FP32 parameters of the network. */
+int64_t sbm_net_param_count(void);
+/* New network, He-normal initialised from `seed`. */
+int sbm_net_create(uint64_t seed, sbm_net** out);
+int sbm_net_destroy(sbm_net* net);
+/* Master (FP32) parameters; set also resets the Adam state. */
+int sbm_net_get_params(const sbm_net* net, float* host, int64_t count);
+int sbm_net_set_params(sbm_net* net, const float* host, int64_t count);
+/* Forward pass on nb samples of ny x nx x nz coarse cells (multiples of 16)
+ * stacked along z: in (nb*ny*nx*nz) x 16 FP32 (rounded to BF16), out
+ * nb*ny*nx*nz FP32. */
+int sbm_net_forward(sbm_net* net, int ny, int nx, int nz, int nb, const float* in, float* out);
+/* loss = mean (out - target)^2 and its gradient with respect to every
+ * parameter (FP32, same order as the parameters; grad may be NULL). */
+int sbm_net_loss_grad(sbm_net* net, int ny, int nx, int nz, int nb, const float* in,
+                      const float* target, double* loss, float* grad);
+/* `steps` Adam steps (learning rate lr) on mini-batches of `batch` samples
+ * drawn (seeded) from nsamples input / target pairs; loss_hist[steps]
+ * receives each step's loss (may be NULL). */
+int sbm_net_train(sbm_net* net, int ny, int nx, int nz, int nsamples, const float* in,
+                  const float* target, int steps, int batch, float lr, uint64_t seed,
+                  float* loss_hist);
+/* Attach `net` (NULL detaches) to a context with output scale k_out.  The
+ * context does not own the network: keep it alive while attached. */
+int sbm_ctx_set_net(sbm_ctx* ctx, sbm_net* net, double out_scale);
+/* Preconditioner used by the last mixed-precision solve (SBM_PC_*). */
+int sbm_ctx_last_precond(const sbm_ctx* ctx);
+/* One application z = M(r) of the learned preconditioner for the GENERIC
+ * operator of the context's coefficient (halo-padded FP64 r and z). */
+int sbm_learned_pc_apply(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, const double* r,
+                         double* z);
+
 /* Version string of the compiled library. */
 const char* sbm_version(void);
 /* Number of kernel launches this process has issued through the library. */
