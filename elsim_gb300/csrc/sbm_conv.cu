@@ -36,8 +36,8 @@ constexpr unsigned kSpinTc = 1u << 20;
 constexpr int TY = 8, TX = 16;                  // voxel tile (y, x), one z plane
 constexpr int HY = TY + 2, HX = TX + 2, HZ = 3;  // halo tile
 constexpr int HVOX = HY * HX * HZ;              // 540 voxels
-constexpr int A_HALF = HVOX * 16;               // one 8-channel half, bytes
-constexpr int A_STAGE = 2 * A_HALF;             // 17280
+constexpr int A_BOX = HVOX * 16;                // bytes of one 8-channel half tile (8640)
+constexpr int A_HALF = (A_BOX + 127) / 128 * 128;  // its slot, 128-byte aligned (8704)
 constexpr int NT_MAX = 64;                      // output channels per CTA
 constexpr int NST = 2;                          // stages
 
@@ -124,26 +124,54 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 
 namespace {
 
-// Halo-tiled implicit GEMM.  A CTA owns a tile of TY x TX voxels in one z
-// plane (M = 128 rows, row m = voxel (y0 + m%8, x0 + m/8)) and NT output
-// channels.  For each 16-channel input chunk it stages the (TY+2) x (TX+2)
-// x 3 halo tile once in shared memory, in the canonical K-major layout
-// (8 consecutive y voxels x 16 bytes = one core matrix; x lines HY*16
-// bytes apart; the two 8-channel halves A_HALF bytes apart), together with
-// the chunk's weights for all 27 taps, and issues the 27 tap MMAs from
-// shifted descriptor start addresses: the tap offset (dy, dx, dz) moves the
-// start by (dy + HY*(dx + HX*dz)) * 16 bytes and the core-matrix strides stay
-// the same, so the input is read about 4x (halo) instead of 27x.  Two
-// stages let the gather of the next chunk overlap the MMAs in flight.
-__global__ void __launch_bounds__(NTHR) k_conv3_tc(ConvArgs a) {
+// Halo-tiled implicit GEMM fed by TMA.  A CTA owns a tile of TY x TX voxels
+// in one z plane (M = 128 rows, row m = voxel (y0 + m%8, x0 + m/8)) and
+// NT <= 64 output channels.  For each 16-channel input chunk two tensor-map
+// loads bring the (TY+2) x (TX+2) x 3 halo tile into shared memory (one
+// 8-channel half each, zero outside the grid and the sample), which is
+// exactly the canonical K-major operand layout: 8 consecutive y voxels x 16
+// bytes form a core matrix, x lines are HY*16 bytes apart, the halves
+// A_HALF bytes apart.  A bulk copy brings the chunk's weights for all 27
+// taps (pre-arranged image).  The 27 tap MMAs read the tile through
+// shifted descriptor start addresses: tap (dy, dx, dz) starts
+// (dy + HY*(dx + HX*dz)) * 16 bytes further, with the same strides, so the
+// input is read ~4x (halo) instead of 27x.  Thread 0 is producer and MMA
+// issuer over an NST-stage ring (full / consumed mbarriers).
+__device__ __forceinline__ void tma_load5(void* dst, const CUtensorMap* map, uint64_t* bar, int c0,
+                                          int c1, int c2, int c3, int c4) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(sa(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4),
+      "r"(sa(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes,
+                                          uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(sa(dst)),
+      "l"(src), "r"(bytes), "r"(sa(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(bar)), "r"(bytes)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvMap m, ConvArgs a) {
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(1024) unsigned char sm[];
   const int n0 = blockIdx.y * NT_MAX;
   const int nt = min(NT_MAX, a.cout - n0);
   const int bbytes = 27 * nt * 32;
-  const int stage_bytes = A_STAGE + bbytes;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + NST * stage_bytes);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + NST + 1);
+  const int stage_bytes = 2 * A_HALF + bbytes;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + NST * stage_bytes);
+  uint64_t* used = full + NST;
+  uint64_t* done = used + NST;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int nty = (a.ny + TY - 1) / TY, ntx = (a.nx + TX - 1) / TX;
@@ -151,7 +179,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(ConvArgs a) {
   const int tx = (blockIdx.x / nty) % ntx;
   const int z0 = blockIdx.x / (nty * ntx);
   const int y0 = ty * TY, x0 = tx * TX;
-  const int zl = z0 % a.nzs;  // plane index within its sample
+  const int zl = z0 % a.nzs, sample = z0 / a.nzs;
   const int ncols = nt <= 32 ? 32 : 64;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -161,79 +189,39 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(ConvArgs a) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    for (int s = 0; s <= NST; ++s) mb_init(&bar[s]);
+    for (int s = 0; s < 2 * NST + 1; ++s) mb_init(&full[s]);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  const uint32_t id = idesc_bf16(nt);
   const int nchunk = a.cin / KS;
-  const uint4 zero4 = make_uint4(0, 0, 0, 0);
   bool ok = true;
-  for (int c = 0; c < nchunk; ++c) {
-    const int s = c % NST;
-    // the stage was last read by the MMAs of chunk c - NST
-    if (c >= NST) ok = ok && mb_wait(&bar[s], (unsigned)(((c - NST) / NST) & 1));
-    if (!__syncthreads_and(ok)) {
-      ok = false;
-      break;
-    }
-    unsigned char* A = sm + s * stage_bytes;
-    unsigned char* B = A + A_STAGE;
-    // halo tile: item q -> voxel hv = q / 2 (hy fastest), channel half q % 2
-    for (int q0 = 0; q0 < HVOX * 2; q0 += NTHR * 4) {
-      uint4 v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int q = q0 + u * NTHR + tid;
-        v[u] = zero4;
-        if (q < HVOX * 2) {
-          const int hv = q >> 1, kh = q & 1;
-          const int hy = hv % HY, hx = (hv / HY) % HX, hz = hv / (HY * HX);
-          const int y = y0 + hy - 1, x = x0 + hx - 1, dz = hz - 1;
-          if (y >= 0 && y < a.ny && x >= 0 && x < a.nx && zl + dz >= 0 && zl + dz < a.nzs) {
-            const int64_t vox = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + dz));
-            v[u] = *reinterpret_cast<const uint4*>(a.x + vox * a.ldx + a.offx + c * KS + kh * 8);
-          }
-        }
+  if (tid == 0) {
+    const uint32_t id = idesc_bf16(nt);
+    const __nv_bfloat16* wsrc = a.wimg + (int64_t)64 * blockIdx.y * 27 * a.cin;
+    int issued[NST] = {}, landed[NST] = {}, committed[NST] = {}, freed[NST] = {};
+    auto load = [&](int c, int s) {
+      unsigned char* A = sm + s * stage_bytes;
+      expect_tx(&full[s], 2 * A_BOX + bbytes);
+      const int ch = a.offx + c * KS;
+      tma_load5(A, &m.x, &full[s], ch, y0 - 1, x0 - 1, zl - 1, sample);
+      tma_load5(A + A_HALF, &m.x, &full[s], ch + 8, y0 - 1, x0 - 1, zl - 1, sample);
+      bulk_load(A + 2 * A_HALF, wsrc + (int64_t)c * 27 * nt * 16, bbytes, &full[s]);
+      ++issued[s];
+    };
+    for (int c = 0; c < nchunk && c < NST; ++c) load(c, c);
+    for (int c = 0; c < nchunk; ++c) {
+      const int s = c % NST;
+      if (!mb_wait(&full[s], (unsigned)(landed[s] & 1))) {
+        ok = false;
+        break;
       }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int q = q0 + u * NTHR + tid;
-        if (q < HVOX * 2)
-          *reinterpret_cast<uint4*>(A + (q & 1) * A_HALF + (q >> 1) * 16) = v[u];
-      }
-    }
-    // weights of the chunk for all taps: item q -> tap, row n, half kh
-    const int nb2 = nt * 2;
-    for (int q0 = 0; q0 < 27 * nb2; q0 += NTHR * 4) {
-      uint4 v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int q = q0 + u * NTHR + tid;
-        v[u] = zero4;
-        if (q < 27 * nb2) {
-          const int t = q / nb2, n = (q % nb2) >> 1, kh = q & 1;
-          v[u] = *reinterpret_cast<const uint4*>(a.w + ((int64_t)(n0 + n) * 27 + t) * a.cin +
-                                                 c * KS + kh * 8);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int q = q0 + u * NTHR + tid;
-        if (q < 27 * nb2) {
-          const int t = q / nb2, n = (q % nb2) >> 1, kh = q & 1;
-          *reinterpret_cast<uint4*>(B + t * (nt * 32) + (n >> 3) * 256 + kh * 128 + (n & 7) * 16) =
-              v[u];
-        }
-      }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
+      ++landed[s];
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t A = sa(sm + s * stage_bytes);
+      const uint32_t B = A + 2 * A_HALF;
       for (int t = 0; t < 27; ++t) {
         int dy = t % 3 - 1, dx = (t / 3) % 3 - 1, dz = t / 9 - 1;
         if (a.flip) {
@@ -242,16 +230,33 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(ConvArgs a) {
           dz = -dz;
         }
         const uint32_t aoff = (uint32_t)(((1 + dz) * HX + (1 + dx)) * HY + (1 + dy)) * 16u;
-        const uint64_t ad = umma_desc(sa(A) + aoff, A_HALF, HY * 16);
-        const uint64_t bd = umma_desc(sa(B) + (uint32_t)(t * nt * 32), 128, 256);
-        tc_mma(tmem, ad, bd, id, (c > 0 || t > 0) ? 1u : 0u);
+        tc_mma(tmem, umma_desc(A + aoff, A_HALF, HY * 16),
+               umma_desc(B + (uint32_t)(t * nt * 32), 128, 256), id, (c > 0 || t > 0) ? 1u : 0u);
       }
-      tc_commit(&bar[s]);
+      tc_commit(&used[s]);
+      ++committed[s];
+      if (c + NST < nchunk) {
+        // the stage is reloaded once its MMAs have read it
+        if (!mb_wait(&used[s], (unsigned)(freed[s] & 1))) {
+          ok = false;
+          break;
+        }
+        ++freed[s];
+        load(c + NST, s);
+      }
+    }
+    if (ok) {
+      tc_commit(done);
+    } else {
+      // bounded drain of the copies and MMAs still in flight
+      for (int s = 0; s < NST; ++s) {
+        for (; landed[s] < issued[s]; ++landed[s]) mb_wait(&full[s], (unsigned)(landed[s] & 1));
+        for (; freed[s] < committed[s]; ++freed[s]) mb_wait(&used[s], (unsigned)(freed[s] & 1));
+      }
     }
   }
-  // all MMAs complete -> accumulator ready
-  if (ok && tid == 0) tc_commit(&bar[NST]);
-  ok = __syncthreads_and(ok) && mb_wait(&bar[NST], 0);
+  ok = __syncthreads_and(ok);
+  ok = ok && mb_wait(done, 0);
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
@@ -287,17 +292,27 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(ConvArgs a) {
     }
   } else if (tid == 0) {
     atomicExch(a.err, 1);
-    // bounded drain of MMAs still in flight before the memory is released
-    for (int s = 0; s < NST; ++s) {
-      for (unsigned n = 0; n < kSpinTc && !mb_try(&bar[s], 0) && !mb_try(&bar[s], 1); ++n) {
-      }
-    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols)
                  : "memory");
+}
+
+// Weight image: destination element (co, t, ci) of the (possibly
+// transposed) convolution from the source layout.
+__global__ void k_wimage(const __nv_bfloat16* __restrict__ w, int cout, int cin, int transpose,
+                         __nv_bfloat16* __restrict__ img) {
+  const int64_t n = (int64_t)cout * 27 * cin;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int ci = (int)(q % cin);
+    const int t = (int)((q / cin) % 27);
+    const int co = (int)(q / ((int64_t)27 * cin));
+    const int64_t src = transpose ? ((int64_t)ci * 27 + t) * cout + co : q;
+    img[wimage_index(co, t, ci, cout, cin)] = w[src];
+  }
 }
 
 // Reference 3x3x3 convolution on the CUDA cores (same data layout), FP32
@@ -455,7 +470,7 @@ size_t conv_smem(int cout) {
 }
 
 size_t conv_tile_smem(int nt) {
-  return (size_t)NST * (A_STAGE + 27 * nt * 32) + (NST + 1) * 8 + 16;
+  return (size_t)NST * (2 * A_HALF + 27 * nt * 32) + (2 * NST + 1) * 8 + 16;
 }
 
 }  // namespace
@@ -502,9 +517,13 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
     cudaStreamDestroy(s);
     return code;
   };
+  void* dimg = nullptr;
   if (cudaMalloc(&dx, nv * cin * 2) || cudaMalloc(&dw, (size_t)cout * 27 * cin * 2) ||
-      cudaMalloc(&db, cout * 4) || cudaMalloc(&dy, nv * cout * 4) || cudaMalloc(&de, 4))
+      cudaMalloc(&db, cout * 4) || cudaMalloc(&dy, nv * cout * 4) || cudaMalloc(&de, 4) ||
+      cudaMalloc(&dimg, (size_t)cout * 27 * cin * 2)) {
+    cudaFree(dimg);
     return fail(SBM_ERR_NOMEM);
+  }
   cudaMemcpyAsync(dx, x, nv * cin * 2, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(dw, w, (size_t)cout * 27 * cin * 2, cudaMemcpyHostToDevice, s);
   if (bias) cudaMemcpyAsync(db, bias, cout * 4, cudaMemcpyHostToDevice, s);
@@ -515,12 +534,20 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
   a.x = (const __nv_bfloat16*)dx; a.w = (const __nv_bfloat16*)dw;
   a.bias = bias ? (const float*)db : nullptr;
   a.y16 = nullptr; a.y32 = (float*)dy; a.relu = relu; a.flip = flip; a.err = (int*)de;
-  rc = conv3_launch(&a, use_tc, s);
-  if (rc) return fail(rc);
+  conv3_wimage(a.w, cout, cin, 0, (__nv_bfloat16*)dimg, s);
+  a.wimg = (const __nv_bfloat16*)dimg;
+  rc = conv3_launch(&a, nullptr, use_tc, s);
+  if (rc) {
+    cudaStreamSynchronize(s);
+    cudaFree(dimg);
+    return fail(rc);
+  }
   int herr = 0;
   cudaMemcpyAsync(y, dy, nv * cout * 4, cudaMemcpyDeviceToHost, s);
   cudaMemcpyAsync(&herr, de, 4, cudaMemcpyDeviceToHost, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) return fail(SBM_ERR_CUDA);
+  const cudaError_t e = cudaStreamSynchronize(s);
+  cudaFree(dimg);
+  if (e != cudaSuccess) return fail(SBM_ERR_CUDA);
   fail(0);
   return herr ? SBM_ERR_TIMEOUT : SBM_OK;
 }
@@ -536,14 +563,55 @@ int wgrad_launch(const WgradArgs* pa, cudaStream_t s) {
   return SBM_OK;
 }
 
-int conv3_launch(const ConvArgs* pa, int use_tc, cudaStream_t s) {
+int conv3_map(const ConvArgs* pa, ConvMap* m) {
+  const ConvArgs& a = *pa;
+  auto fn = tensor_map_encoder();
+  if (!fn) {
+    set_error_msg("cuTensorMapEncodeTiled unavailable");
+    return SBM_ERR_STATE;
+  }
+  const cuuint64_t ld = (cuuint64_t)a.ldx;
+  cuuint64_t dims[5] = {ld, (cuuint64_t)a.ny, (cuuint64_t)a.nx, (cuuint64_t)a.nzs,
+                        (cuuint64_t)(a.nz / a.nzs)};
+  cuuint64_t strides[4] = {ld * 2, ld * 2 * a.ny, ld * 2 * a.ny * a.nx,
+                           ld * 2 * a.ny * a.nx * a.nzs};
+  cuuint32_t box[5] = {8, HY, HX, HZ, 1};
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  const CUresult r = fn(&m->x, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5,
+                        const_cast<__nv_bfloat16*>(a.x), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error_msg("cuTensorMapEncodeTiled rejected a convolution input");
+    return SBM_ERR_STATE;
+  }
+  return SBM_OK;
+}
+
+void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, __nv_bfloat16* img,
+                  cudaStream_t s) {
+  const int64_t n = (int64_t)cout * 27 * cin;
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  k_wimage<<<(unsigned)b, 256, 0, s>>>(w, cout, cin, transpose, img);
+  SBM_LAUNCHED(1);
+}
+
+int conv3_launch(const ConvArgs* pa, const ConvMap* map, int use_tc, cudaStream_t s) {
   const ConvArgs& a = *pa;
   const int64_t nv = (int64_t)a.ny * a.nx * a.nz;
   if (use_tc) {
+    if ((a.ldx % 8) || (a.offx % 8) || (a.nz % a.nzs) || !a.wimg) return SBM_ERR_ARG;
+    ConvMap local;
+    if (!map) {
+      const int rc = conv3_map(pa, &local);
+      if (rc) return rc;
+      map = &local;
+    }
     const int64_t tiles = (int64_t)((a.ny + TY - 1) / TY) * ((a.nx + TX - 1) / TX) * a.nz;
     const int ntn = (a.cout + NT_MAX - 1) / NT_MAX;
     k_conv3_tc<<<dim3((unsigned)tiles, (unsigned)ntn), NTHR,
-                 conv_tile_smem(std::min(a.cout, NT_MAX)), s>>>(a);
+                 conv_tile_smem(std::min(a.cout, NT_MAX)), s>>>(*map, a);
   } else {
     const int64_t n = nv * a.cout;
     k_conv3_ref<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);

@@ -24,7 +24,7 @@
 // Training: loss = mean (N(f) - t)^2.  Backward uses the same tcgen05
 // convolution kernel with flipped taps and transposed weights for the data
 // gradient, a tcgen05 GEMM over voxels for the weight gradient, and Adam on
-// FP32 master weights with BF16 copies for the next forward pass.
+// FP32 master weights that rebuilds the BF16 weight images of both passes.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -96,6 +96,7 @@ struct Work {
   float* gcat[4] = {};  // data gradients of the decoder inputs
   float* gpin[kLev] = {};
   std::vector<void*> mem;
+  std::map<const void*, ConvMap> maps;  // tensor map of each convolution input
   ~Work() {
     for (void* p : mem) cudaFree(p);
   }
@@ -130,34 +131,47 @@ __device__ __forceinline__ int64_t child(const Dims& f, int i, int j, int k, int
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (n);         \
        t += (int64_t)gridDim.x * blockDim.x)
 
-// y[vc][c] = mean of x[child][offx + c] over the 8 children (average pooling).
+// y[vc][c] = mean of x[child][offx + c] over the 8 children (average
+// pooling); one thread per coarse voxel and 8 channels (16-byte accesses).
 __global__ void k_pool(Dims f, int C, const bf16* __restrict__ x, int ldx, int offx,
                        bf16* __restrict__ y, const int* skip) {
   if (skip && *skip) return;
   const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
-  NET_LOOP(c.v() * C) {
-    const int ch = (int)(t % C);
-    const int64_t vc = t / C;
+  const int G = C / 8;
+  NET_LOOP(c.v() * G) {
+    const int g8 = (int)(t % G) * 8;
+    const int64_t vc = t / G;
     int i, j, k;
     vox(c, vc, &i, &j, &k);
-    float s = 0.f;
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s += __bfloat162float(x[child(f, i, j, k, q) * ldx + offx + ch]);
-    y[vc * C + ch] = __float2bfloat16_rn(s * 0.125f);
+    for (int q = 0; q < 8; ++q) {
+      const uint4 u = *reinterpret_cast<const uint4*>(x + child(f, i, j, k, q) * ldx + offx + g8);
+      const bf16* h = reinterpret_cast<const bf16*>(&u);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) s[e] += __bfloat162float(h[e]);
+    }
+    __align__(16) bf16 o[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) o[e] = __float2bfloat16_rn(s[e] * 0.125f);
+    *reinterpret_cast<uint4*>(y + vc * C + g8) = *reinterpret_cast<const uint4*>(o);
   }
 }
 
-// y[vf][offy + c] = x[parent(vf)][c] (nearest-neighbour upsampling).
+// y[vf][offy + c] = x[parent(vf)][c] (nearest-neighbour upsampling); one
+// thread per fine voxel and 8 channels.
 __global__ void k_up(Dims f, int C, const bf16* __restrict__ x, bf16* __restrict__ y, int ldy,
                      int offy, const int* skip) {
   if (skip && *skip) return;
   const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
-  NET_LOOP(f.v() * C) {
-    const int ch = (int)(t % C);
-    const int64_t vf = t / C;
+  const int G = C / 8;
+  NET_LOOP(f.v() * G) {
+    const int g8 = (int)(t % G) * 8;
+    const int64_t vf = t / G;
     int i, j, k;
     vox(f, vf, &i, &j, &k);
-    y[vf * ldy + offy + ch] = x[vid(c, i / 2, j / 2, k / 2) * C + ch];
+    *reinterpret_cast<uint4*>(y + vf * ldy + offy + g8) =
+        *reinterpret_cast<const uint4*>(x + vid(c, i / 2, j / 2, k / 2) * C + g8);
   }
 }
 
@@ -283,12 +297,13 @@ struct LayerTab {
 };
 
 // Adam step on the FP32 master parameters (when `update`), then the BF16
-// copies of the convolution weights: w16 [co][27][ci] for the forward pass
-// and wt16 [ci][27][co] (same offsets) for the data gradient.
+// weight images of the tensor-core kernel: wimg for the forward pass and
+// wtimg for the data gradient (transposed convolution), at the layer's
+// parameter offset.
 __global__ void k_adam(int64_t P, int update, float* __restrict__ w, const float* __restrict__ g,
                        float* __restrict__ m, float* __restrict__ v, float lr, float b1, float b2,
-                       float eps, float c1, float c2, LayerTab tab, bf16* __restrict__ w16,
-                       bf16* __restrict__ wt16) {
+                       float eps, float c1, float c2, LayerTab tab, bf16* __restrict__ wimg,
+                       bf16* __restrict__ wtimg) {
   NET_LOOP(P) {
     float wv = w[t];
     if (update) {
@@ -305,11 +320,11 @@ __global__ void k_adam(int64_t P, int update, float* __restrict__ w, const float
       const int64_t rel = t - tab.off[l];
       if (rel >= 0 && rel < n) {
         const bf16 b = __float2bfloat16_rn(wv);
-        w16[t] = b;
         const int ci = (int)(rel % tab.ci[l]);
         const int tap = (int)((rel / tab.ci[l]) % 27);
         const int co = (int)(rel / ((int64_t)27 * tab.ci[l]));
-        wt16[tab.off[l] + ((int64_t)ci * 27 + tap) * tab.co[l] + co] = b;
+        wimg[tab.off[l] + wimage_index(co, tap, ci, tab.co[l], tab.ci[l])] = b;
+        wtimg[tab.off[l] + wimage_index(ci, tap, co, tab.ci[l], tab.co[l])] = b;
       }
     }
   }
@@ -338,8 +353,8 @@ struct sbm_net {
   float* m = nullptr;
   float* v = nullptr;
   float* grad = nullptr;
-  bf16* w16 = nullptr;
-  bf16* wt16 = nullptr;
+  bf16* wimg = nullptr;   // forward weight images
+  bf16* wtimg = nullptr;  // data-gradient weight images
   int* err = nullptr;
   double* loss = nullptr;
   int64_t step = 0;
@@ -362,8 +377,8 @@ LayerTab layer_tab() {
 
 int cast_weights(sbm_net* n, cudaStream_t s) {
   k_adam<<<grid_for(kL.total), 256, 0, s>>>(kL.total, 0, n->w32, nullptr, nullptr, nullptr, 0.f,
-                                            0.f, 0.f, 0.f, 0.f, 0.f, layer_tab(), n->w16,
-                                            n->wt16);
+                                            0.f, 0.f, 0.f, 0.f, 0.f, layer_tab(), n->wimg,
+                                            n->wtimg);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
@@ -411,49 +426,60 @@ Work* work_for(sbm_net* n, int ny, int nx, int nzs, int nb, bool train) {
   return w;
 }
 
-int conv(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx, const bf16* wts,
-         bf16* y, int ldy, int offy, const int* skip, cudaStream_t s) {
+// Tensor map of a convolution input (encoded once per buffer).
+const ConvMap* map_for(Work& w, const ConvArgs& a) {
+  auto it = w.maps.find(a.x);
+  if (it != w.maps.end()) return &it->second;
+  ConvMap m;
+  if (conv3_map(&a, &m)) return nullptr;
+  return &(w.maps[a.x] = m);
+}
+
+int conv(sbm_net* n, Work& w, int l, int lev, const bf16* x, int ldx, bf16* y, int ldy,
+         int offy, const int* skip, cudaStream_t s) {
   ConvArgs a{};
   const Dims& d = w.d[lev];
   a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
   a.cin = kCi[l]; a.cout = kCo[l];
   a.ldx = ldx; a.offx = 0; a.ldy = ldy; a.offy = offy;
-  a.x = x; a.w = wts + kL.off[l]; a.bias = n->w32 + kL.boff[l];
+  a.x = x; a.wimg = n->wimg + kL.off[l]; a.bias = n->w32 + kL.boff[l];
   a.y16 = y; a.y32 = nullptr; a.relu = 1; a.flip = 0; a.err = n->err; a.skip = skip;
-  return conv3_launch(&a, 1, s);
+  const ConvMap* m = map_for(w, a);
+  if (!m) return SBM_ERR_STATE;
+  return conv3_launch(&a, m, 1, s);
 }
 
 void pool(const Work& w, int lev, int C, const bf16* x, int ldx, int offx, bf16* y,
           const int* skip, cudaStream_t s) {
   const Dims& f = w.d[lev];
-  k_pool<<<grid_for(f.v() / 8 * C), 256, 0, s>>>(f, C, x, ldx, offx, y, skip);
+  k_pool<<<grid_for(f.v() / 8 * C / 8), 256, 0, s>>>(f, C, x, ldx, offx, y, skip);
   SBM_LAUNCHED(1);
 }
 
 void up(const Work& w, int lev, int C, const bf16* x, bf16* y, int ldy, const int* skip,
         cudaStream_t s) {
   const Dims& f = w.d[lev];
-  k_up<<<grid_for(f.v() * C), 256, 0, s>>>(f, C, x, y, ldy, 0, skip);
+  k_up<<<grid_for(f.v() * C / 8), 256, 0, s>>>(f, C, x, y, ldy, 0, skip);
   SBM_LAUNCHED(1);
 }
 
 // Forward pass of the U-Net on w.in0 -> w.out (and the squared error
 // against w.tgt into n->loss when tgt).
-int forward(sbm_net* n, const Work& w, bool tgt, const int* skip, cudaStream_t s) {
+int forward(sbm_net* n, Work& w, bool tgt, const int* skip, cudaStream_t s) {
   int rc;
   for (int lev = 0; lev < 4; ++lev) {
     const int l = kEnc[lev];
     const bf16* x = lev == 0 ? w.in0 : w.pin[lev];
-    if ((rc = conv(n, w, l, lev, x, kCi[l], n->w16, w.cat[lev], kCatW[lev], kUpW[lev], skip, s)))
+    if ((rc = conv(n, w, l, lev, x, kCi[l], w.cat[lev], kCatW[lev], kUpW[lev], skip, s)))
       return rc;
     pool(w, lev, kCo[l], w.cat[lev], kCatW[lev], kUpW[lev], w.pin[lev + 1], skip, s);
   }
-  if ((rc = conv(n, w, E4, 4, w.pin[4], kCi[E4], n->w16, w.a4, kCo[E4], 0, skip, s))) return rc;
+  if ((rc = conv(n, w, E4, 4, w.pin[4], kCi[E4], w.a4, kCo[E4], 0, skip, s))) return rc;
   for (int lev = 3; lev >= 0; --lev) {
     const bf16* below = lev == 3 ? w.a4 : w.dec[lev + 1];
     up(w, lev, kUpW[lev], below, w.cat[lev], kCatW[lev], skip, s);
     const int l = kDec[lev];
-    if ((rc = conv(n, w, l, lev, w.cat[lev], kCatW[lev], n->w16, w.dec[lev], kCo[l], 0, skip, s)))
+    if ((rc = conv(n, w, l, lev, w.cat[lev], kCatW[lev], w.dec[lev], kCo[l], 0, skip, s)))
       return rc;
   }
   const int64_t V = w.d[0].v();
@@ -490,20 +516,22 @@ int wgrad(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx, con
   return SBM_OK;
 }
 
-int dgrad(sbm_net* n, const Work& w, int l, int lev, const bf16* gy, float* gx, cudaStream_t s) {
+int dgrad(sbm_net* n, Work& w, int l, int lev, const bf16* gy, float* gx, cudaStream_t s) {
   ConvArgs a{};
   const Dims& d = w.d[lev];
   a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
   a.cin = kCo[l]; a.cout = kCi[l];
   a.ldx = kCo[l]; a.offx = 0; a.ldy = kCi[l]; a.offy = 0;
-  a.x = gy; a.w = n->wt16 + kL.off[l]; a.bias = nullptr;
+  a.x = gy; a.wimg = n->wtimg + kL.off[l]; a.bias = nullptr;
   a.y16 = nullptr; a.y32 = gx; a.relu = 0; a.flip = 1; a.err = n->err; a.skip = nullptr;
-  return conv3_launch(&a, 1, s);
+  const ConvMap* m = map_for(w, a);
+  if (!m) return SBM_ERR_STATE;
+  return conv3_launch(&a, m, 1, s);
 }
 
 // Gradient of mean (out - tgt)^2 over all voxels of w into n->grad
 // (forward with the target must have run).
-int backward(sbm_net* n, const Work& w, cudaStream_t s) {
+int backward(sbm_net* n, Work& w, cudaStream_t s) {
   int rc;
   SBM_CUDA_TRY(cudaMemsetAsync(n->grad, 0, sizeof(float) * kL.total, s));
   const int64_t V = w.d[0].v();
@@ -546,7 +574,7 @@ int adam(sbm_net* n, float lr, cudaStream_t s) {
   const float c1 = 1.f / (1.f - powf(b1, (float)n->step));
   const float c2 = 1.f / (1.f - powf(b2, (float)n->step));
   k_adam<<<grid_for(kL.total), 256, 0, s>>>(kL.total, 1, n->w32, n->grad, n->m, n->v, lr, b1, b2,
-                                            eps, c1, c2, layer_tab(), n->w16, n->wt16);
+                                            eps, c1, c2, layer_tab(), n->wimg, n->wtimg);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
@@ -865,7 +893,7 @@ int sbm_net_create(uint64_t seed, sbm_net** out) {
   if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) ||
       cudaMalloc(&n->w32, sizeof(float) * P) || cudaMalloc(&n->m, sizeof(float) * P) ||
       cudaMalloc(&n->v, sizeof(float) * P) || cudaMalloc(&n->grad, sizeof(float) * P) ||
-      cudaMalloc(&n->w16, sizeof(bf16) * P) || cudaMalloc(&n->wt16, sizeof(bf16) * P) ||
+      cudaMalloc(&n->wimg, sizeof(bf16) * P) || cudaMalloc(&n->wtimg, sizeof(bf16) * P) ||
       cudaMalloc(&n->err, sizeof(int)) || cudaMalloc(&n->loss, sizeof(double))) {
     sbm_net_destroy(n);
     return SBM_ERR_NOMEM;
@@ -895,7 +923,7 @@ int sbm_net_destroy(sbm_net* n) {
   if (!n) return SBM_ERR_ARG;
   if (n->stream) cudaStreamSynchronize(n->stream);
   for (auto& kv : n->works) delete kv.second;
-  void* p[] = {n->w32, n->m, n->v, n->grad, n->w16, n->wt16, n->err, n->loss};
+  void* p[] = {n->w32, n->m, n->v, n->grad, n->wimg, n->wtimg, n->err, n->loss};
   for (void* q : p) cudaFree(q);
   if (n->stream) cudaStreamDestroy(n->stream);
   delete n;

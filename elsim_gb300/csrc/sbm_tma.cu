@@ -24,6 +24,10 @@
 #include "sbm_internal.cuh"
 
 namespace sbm {
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
+}
+
+namespace sbm {
 
 namespace {
 
@@ -267,18 +271,7 @@ size_t smem_bytes(int pc, int form) {
   return (size_t)NS * na * SLOT + NS * sizeof(uint64_t);
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
-  return fn;
-}
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() { return tensor_map_encoder(); }
 
 // 3-D map over an FP32-layout buffer (base = allocation start, 16-byte aligned).
 bool make_map(CUtensorMap* m, const float* base, const Geo& g32) {
@@ -296,6 +289,20 @@ bool make_map(CUtensorMap* m, const float* base, const Geo& g32) {
 }
 
 }  // namespace
+
+// The driver's tensor-map encoder (runtime entry-point query, once).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
 
 // The TMA path needs rows of a multiple of 4 voxels (float4 output) and
 // 16-byte row strides (always true of the FP32 layout).
