@@ -19,6 +19,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "sbm_conv.cuh"
 
@@ -34,12 +35,14 @@ constexpr int A_BYTES = TM * KS * 2;   // 4096
 constexpr unsigned kSpinTc = 1u << 20;
 // halo-tiled forward kernel
 constexpr int TY = 8, TX = 16;                  // voxel tile (y, x), one z plane
-constexpr int HY = TY + 2, HX = TX + 2, HZ = 3;  // halo tile
-constexpr int HVOX = HY * HX * HZ;              // 540 voxels
-constexpr int A_BOX = HVOX * 16;                // bytes of one 8-channel half tile (8640)
-constexpr int A_HALF = (A_BOX + 127) / 128 * 128;  // its slot, 128-byte aligned (8704)
-constexpr int NT_MAX = 64;                      // output channels per CTA
-constexpr int NST = 2;                          // stages
+constexpr int HY = TY + 2, HX = TX + 2;        // halo tile in y, x (P + 2 planes in z)
+// slot of one 8-channel half of the halo tile of P planes, 128-byte aligned
+__host__ __device__ constexpr int a_half_bytes(int P) {
+  return (HY * HX * (P + 2) * 16 + 127) / 128 * 128;
+}
+constexpr int NT_MAX = 64;                      // output channels per CTA (wide tiles)
+constexpr int NST = 8;                          // most pipeline stages (<= 7 chunks used)
+constexpr int kSmemBudget = 200 * 1024;         // stage memory of a lone CTA
 
 __device__ __forceinline__ uint32_t sa(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -125,9 +128,10 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 namespace {
 
 // Halo-tiled implicit GEMM fed by TMA.  A CTA owns a tile of TY x TX voxels
-// in one z plane (M = 128 rows, row m = voxel (y0 + m%8, x0 + m/8)) and
-// NT <= 64 output channels.  For each 16-channel input chunk two tensor-map
-// loads bring the (TY+2) x (TX+2) x 3 halo tile into shared memory (one
+// in P = 1 or 2 z planes (per plane M = 128 rows, row m = voxel
+// (y0 + m%8, x0 + m/8), its own TMEM accumulator) and NT <= 64 output
+// channels.  For each 16-channel input chunk two tensor-map loads bring the
+// (TY+2) x (TX+2) x (P+2) halo tile into shared memory (one
 // 8-channel half each, zero outside the grid and the sample), which is
 // exactly the canonical K-major operand layout: 8 consecutive y voxels x 16
 // bytes form a core matrix, x lines are HY*16 bytes apart, the halves
@@ -135,8 +139,13 @@ namespace {
 // taps (pre-arranged image).  The 27 tap MMAs read the tile through
 // shifted descriptor start addresses: tap (dy, dx, dz) starts
 // (dy + HY*(dx + HX*dz)) * 16 bytes further, with the same strides, so the
-// input is read ~4x (halo) instead of 27x.  Thread 0 is producer and MMA
-// issuer over an NST-stage ring (full / consumed mbarriers).
+// input is read ~4x (halo) instead of 27x; the second plane's MMAs start
+// one plane (HX*HY*16 bytes) further.  Thread 0 is producer and MMA issuer
+// over an NST-stage ring (full / consumed mbarriers).  The epilogue can
+// also write the 2x2x2-pooled output (planes in registers, y / x pairs by
+// warp shuffle), the output copied to the 8 children of a 2x finer grid
+// (nearest upsampling into a decoder's concat buffer), and a fused 1x1
+// output layer.
 __device__ __forceinline__ void tma_load5(void* dst, const CUtensorMap* map, uint64_t* bar, int c0,
                                           int c1, int c2, int c3, int c4) {
   asm volatile(
@@ -161,14 +170,35 @@ __device__ __forceinline__ void expect_tx(uint64_t* bar, unsigned bytes) {
                : "memory");
 }
 
+// The 27 (x P) tap MMAs of one chunk.  Descriptors advance by constant
+// start-address offsets (the 14-bit start field holds address / 16).
+template <bool FLIP>
+__device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t bd, int nt, int P,
+                                           uint32_t id, bool acc) {
+#pragma unroll
+  for (int t = 0; t < 27; ++t) {
+    const int dy = FLIP ? 1 - t % 3 : t % 3 - 1;
+    const int dx = FLIP ? 1 - (t / 3) % 3 : (t / 3) % 3 - 1;
+    const int dz = FLIP ? 1 - t / 9 : t / 9 - 1;
+    const uint64_t b = bd + (uint64_t)(t * nt * 2);
+    const uint64_t a0 = ad + (uint64_t)((((1 + dz) * HX + (1 + dx)) * HY + (1 + dy)));
+    tc_mma(tmem, a0, b, id, (acc || t > 0) ? 1u : 0u);
+    if (P == 2) tc_mma(tmem + (uint32_t)nt, a0 + (uint64_t)(HX * HY), b, id, (acc || t > 0) ? 1u : 0u);
+  }
+}
+
 __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvMap m, ConvArgs a) {
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(1024) unsigned char sm[];
-  const int n0 = blockIdx.y * NT_MAX;
-  const int nt = min(NT_MAX, a.cout - n0);
+  const int P = a.planes;  // z planes per CTA (1 or 2), one accumulator each
+  const int ahalf = a_half_bytes(P);
+  const int n0 = blockIdx.y * a.tw;
+  const int nt = min(a.tw, a.cout - n0);
   const int bbytes = 27 * nt * 32;
-  const int stage_bytes = 2 * A_HALF + bbytes;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + NST * stage_bytes);
+  const int stage_bytes = 2 * ahalf + bbytes;
+  const int nchunk = a.cin / KS;
+  const int nst = a.nst;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);
   uint64_t* used = full + NST;
   uint64_t* done = used + NST;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
@@ -177,10 +207,10 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   const int nty = (a.ny + TY - 1) / TY, ntx = (a.nx + TX - 1) / TX;
   const int ty = blockIdx.x % nty;
   const int tx = (blockIdx.x / nty) % ntx;
-  const int z0 = blockIdx.x / (nty * ntx);
+  const int z0 = (blockIdx.x / (nty * ntx)) * P;
   const int y0 = ty * TY, x0 = tx * TX;
   const int zl = z0 % a.nzs, sample = z0 / a.nzs;
-  const int ncols = nt <= 32 ? 32 : 64;
+  const int ncols = P * nt <= 32 ? 32 : (P * nt <= 64 ? 64 : 128);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      sa(tslot)),
@@ -196,24 +226,25 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  const int nchunk = a.cin / KS;
   bool ok = true;
   if (tid == 0) {
     const uint32_t id = idesc_bf16(nt);
-    const __nv_bfloat16* wsrc = a.wimg + (int64_t)64 * blockIdx.y * 27 * a.cin;
+    const __nv_bfloat16* wsrc =
+        (a.tw == 16 ? a.wimg16 : a.wimg) + (int64_t)a.tw * blockIdx.y * 27 * a.cin;
+    const unsigned abox = (unsigned)(HY * HX * (P + 2) * 16);
     int issued[NST] = {}, landed[NST] = {}, committed[NST] = {}, freed[NST] = {};
     auto load = [&](int c, int s) {
       unsigned char* A = sm + s * stage_bytes;
-      expect_tx(&full[s], 2 * A_BOX + bbytes);
-      const int ch = a.offx + c * KS;
-      tma_load5(A, &m.x, &full[s], ch, y0 - 1, x0 - 1, zl - 1, sample);
-      tma_load5(A + A_HALF, &m.x, &full[s], ch + 8, y0 - 1, x0 - 1, zl - 1, sample);
-      bulk_load(A + 2 * A_HALF, wsrc + (int64_t)c * 27 * nt * 16, bbytes, &full[s]);
+      expect_tx(&full[s], 2 * abox + bbytes);
+      const int grp = (a.offx + c * KS) >> 3;
+      tma_load5(A, &m.x, &full[s], 8 * (y0 - 1), x0 - 1, zl - 1, sample, grp);
+      tma_load5(A + ahalf, &m.x, &full[s], 8 * (y0 - 1), x0 - 1, zl - 1, sample, grp + 1);
+      bulk_load(A + 2 * ahalf, wsrc + (int64_t)c * 27 * nt * 16, bbytes, &full[s]);
       ++issued[s];
     };
-    for (int c = 0; c < nchunk && c < NST; ++c) load(c, c);
+    for (int c = 0; c < nchunk && c < nst; ++c) load(c, c);
     for (int c = 0; c < nchunk; ++c) {
-      const int s = c % NST;
+      const int s = c % nst;
       if (!mb_wait(&full[s], (unsigned)(landed[s] & 1))) {
         ok = false;
         break;
@@ -221,35 +252,29 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
       ++landed[s];
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t A = sa(sm + s * stage_bytes);
-      const uint32_t B = A + 2 * A_HALF;
-      for (int t = 0; t < 27; ++t) {
-        int dy = t % 3 - 1, dx = (t / 3) % 3 - 1, dz = t / 9 - 1;
-        if (a.flip) {
-          dy = -dy;
-          dx = -dx;
-          dz = -dz;
-        }
-        const uint32_t aoff = (uint32_t)(((1 + dz) * HX + (1 + dx)) * HY + (1 + dy)) * 16u;
-        tc_mma(tmem, umma_desc(A + aoff, A_HALF, HY * 16),
-               umma_desc(B + (uint32_t)(t * nt * 32), 128, 256), id, (c > 0 || t > 0) ? 1u : 0u);
-      }
+      const uint64_t ad = umma_desc(A, ahalf, HY * 16);
+      const uint64_t bd = umma_desc(A + 2 * ahalf, 128, 256);
+      if (a.flip)
+        issue_taps<true>(tmem, ad, bd, nt, P, id, c > 0);
+      else
+        issue_taps<false>(tmem, ad, bd, nt, P, id, c > 0);
       tc_commit(&used[s]);
       ++committed[s];
-      if (c + NST < nchunk) {
+      if (c + nst < nchunk) {
         // the stage is reloaded once its MMAs have read it
         if (!mb_wait(&used[s], (unsigned)(freed[s] & 1))) {
           ok = false;
           break;
         }
         ++freed[s];
-        load(c + NST, s);
+        load(c + nst, s);
       }
     }
     if (ok) {
       tc_commit(done);
     } else {
       // bounded drain of the copies and MMAs still in flight
-      for (int s = 0; s < NST; ++s) {
+      for (int s = 0; s < nst; ++s) {
         for (; landed[s] < issued[s]; ++landed[s]) mb_wait(&full[s], (unsigned)(landed[s] & 1));
         for (; freed[s] < committed[s]; ++freed[s]) mb_wait(&used[s], (unsigned)(freed[s] & 1));
       }
@@ -260,34 +285,81 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
+    const unsigned FULL = 0xffffffffu;
+    const int64_t V = (int64_t)a.ny * a.nx * a.nz;
     const int y = y0 + (tid & 7), x = x0 + (tid >> 3);
     const bool valid = y < a.ny && x < a.nx;
-    const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * z0);
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    float head[2] = {0.f, 0.f};  // fused 1x1 output layer, per plane
     for (int c0 = 0; c0 < nt; c0 += 16) {
-      float acc[16];
-      tc_ld16(lane_base + (uint32_t)c0, acc);
-      if (valid) {
-        if (a.y16) {
-          __align__(16) __nv_bfloat16 o[16];
+      __align__(16) __nv_bfloat16 o[2][16];
+      for (int pl = 0; pl < P; ++pl) {
+        float acc[16];
+        tc_ld16(lane_base + (uint32_t)(pl * nt + c0), acc);
+        const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + pl));
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            float val = acc[q] + (a.bias ? a.bias[n0 + c0 + q] : 0.f);
-            if (a.relu) val = fmaxf(val, 0.f);
-            o[q] = __float2bfloat16_rn(val);
-          }
-          uint4* dst = reinterpret_cast<uint4*>(a.y16 + v * a.ldy + a.offy + n0 + c0);
-          dst[0] = *reinterpret_cast<const uint4*>(&o[0]);
-          dst[1] = *reinterpret_cast<const uint4*>(&o[8]);
+        for (int q = 0; q < 16; ++q) {
+          float val = acc[q] + (a.bias ? a.bias[n0 + c0 + q] : 0.f);
+          if (a.relu) val = fmaxf(val, 0.f);
+          o[pl][q] = __float2bfloat16_rn(val);
+          acc[q] = val;
+          if (a.w1x1) head[pl] += a.w1x1[n0 + c0 + q] * __bfloat162float(o[pl][q]);
+        }
+        if (!valid) continue;
+        const int ch = a.offy + n0 + c0;
+        if (a.y16) {
+          *reinterpret_cast<uint4*>(a.y16 + act_index(v, ch, V)) =
+              *reinterpret_cast<const uint4*>(&o[pl][0]);
+          *reinterpret_cast<uint4*>(a.y16 + act_index(v, ch + 8, V)) =
+              *reinterpret_cast<const uint4*>(&o[pl][8]);
         }
         if (a.y32) {
-#pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            float val = acc[q] + (a.bias ? a.bias[n0 + c0 + q] : 0.f);
-            if (a.relu) val = fmaxf(val, 0.f);
-            a.y32[v * a.ldy + a.offy + n0 + c0 + q] = val;
+          float4* d0 = reinterpret_cast<float4*>(a.y32 + act_index(v, ch, V));
+          float4* d1 = reinterpret_cast<float4*>(a.y32 + act_index(v, ch + 8, V));
+          d0[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+          d0[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+          d1[0] = make_float4(acc[8], acc[9], acc[10], acc[11]);
+          d1[1] = make_float4(acc[12], acc[13], acc[14], acc[15]);
+        }
+        if (a.up) {
+          // nearest upsampling: the 8 children in the finer grid
+          const int fy = 2 * a.ny, fx = 2 * a.nx;
+          for (int ch = 0; ch < 8; ++ch) {
+            const int64_t u = (int64_t)(2 * y + (ch & 1)) +
+                              (int64_t)fy * ((2 * x + ((ch >> 1) & 1)) +
+                                             (int64_t)fx * (2 * (z0 + pl) + (ch >> 2)));
+            const int cu = a.offu + n0 + c0;
+            *reinterpret_cast<uint4*>(a.up + act_index(u, cu, 8 * V)) =
+                *reinterpret_cast<const uint4*>(&o[pl][0]);
+            *reinterpret_cast<uint4*>(a.up + act_index(u, cu + 8, 8 * V)) =
+                *reinterpret_cast<const uint4*>(&o[pl][8]);
           }
         }
+      }
+      if (a.pool) {
+        // 2x2x2 average: planes in registers, y pairs lane^1, x pairs lane^8
+        __align__(16) __nv_bfloat16 pv[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          float sum = __bfloat162float(o[0][q]) + __bfloat162float(o[1][q]);
+          sum += __shfl_xor_sync(FULL, sum, 1);
+          sum += __shfl_xor_sync(FULL, sum, 8);
+          pv[q] = __float2bfloat16_rn(sum * 0.125f);
+        }
+        if (valid && (tid & 1) == 0 && ((tid >> 3) & 1) == 0) {
+          const int cy = a.ny / 2, cx = a.nx / 2;
+          const int64_t vc = (int64_t)(y / 2) + (int64_t)cy * ((x / 2) + (int64_t)cx * (z0 / 2));
+          *reinterpret_cast<uint4*>(a.pool + act_index(vc, n0 + c0, V / 8)) =
+              *reinterpret_cast<const uint4*>(&pv[0]);
+          *reinterpret_cast<uint4*>(a.pool + act_index(vc, n0 + c0 + 8, V / 8)) =
+              *reinterpret_cast<const uint4*>(&pv[8]);
+        }
+      }
+    }
+    if (a.w1x1 && valid) {
+      for (int pl = 0; pl < P; ++pl) {
+        const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + pl));
+        a.out1x1[v] = head[pl] + a.b1x1[0];
       }
     }
   } else if (tid == 0) {
@@ -303,7 +375,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
 // Weight image: destination element (co, t, ci) of the (possibly
 // transposed) convolution from the source layout.
 __global__ void k_wimage(const __nv_bfloat16* __restrict__ w, int cout, int cin, int transpose,
-                         __nv_bfloat16* __restrict__ img) {
+                         int tw, __nv_bfloat16* __restrict__ img) {
   const int64_t n = (int64_t)cout * 27 * cin;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
@@ -311,7 +383,7 @@ __global__ void k_wimage(const __nv_bfloat16* __restrict__ w, int cout, int cin,
     const int t = (int)((q / cin) % 27);
     const int co = (int)(q / ((int64_t)27 * cin));
     const int64_t src = transpose ? ((int64_t)ci * 27 + t) * cout + co : q;
-    img[wimage_index(co, t, ci, cout, cin)] = w[src];
+    img[wimage_index(co, t, ci, cout, cin, tw)] = w[src];
   }
 }
 
@@ -339,12 +411,12 @@ __global__ void k_conv3_ref(ConvArgs a) {
     if (ii < 0 || ii >= a.ny || jj < 0 || jj >= a.nx || kl < 0 || kl >= a.nzs) continue;
     const int64_t nv = (int64_t)ii + (int64_t)a.ny * (jj + (int64_t)a.nx * kk);
     for (int ci = 0; ci < a.cin; ++ci)
-      acc += __bfloat162float(a.x[nv * a.ldx + a.offx + ci]) *
+      acc += __bfloat162float(a.x[act_index(nv, a.offx + ci, nvox)]) *
              __bfloat162float(a.w[((int64_t)co * 27 + t) * a.cin + ci]);
   }
   if (a.relu) acc = fmaxf(acc, 0.f);
-  if (a.y16) a.y16[v * a.ldy + a.offy + co] = __float2bfloat16_rn(acc);
-  if (a.y32) a.y32[v * a.ldy + a.offy + co] = acc;
+  if (a.y16) a.y16[act_index(v, a.offy + co, nvox)] = __float2bfloat16_rn(acc);
+  if (a.y32) a.y32[act_index(v, a.offy + co, nvox)] = acc;
 }
 
 // Weight gradient dW[co][t][ci] = sum_v dy[v][co] * x[nb(v,t)][ci] as a
@@ -408,7 +480,8 @@ __global__ void __launch_bounds__(NTHR) k_wgrad_tc(WgradArgs a) {
         const int vj = (int)(r2 % a.nx), vk = (int)(r2 / a.nx);
         const int ii = vi + di, jj = vj + dj, kk = vk + dk, kl = vk % a.nzs + dk;
         if (ii >= 0 && ii < a.ny && jj >= 0 && jj < a.nx && kl >= 0 && kl < a.nzs)
-          val = a.x[((int64_t)ii + (int64_t)a.ny * (jj + (int64_t)a.nx * kk)) * a.ldx + a.offx + ci];
+          val = a.x[act_index((int64_t)ii + (int64_t)a.ny * (jj + (int64_t)a.nx * kk),
+                              a.offx + ci, nvox)];
       }
       av[e] = val;
     }
@@ -423,7 +496,7 @@ __global__ void __launch_bounds__(NTHR) k_wgrad_tc(WgradArgs a) {
 #pragma unroll
       for (int e = 0; e < 8; ++e) {
         const int64_t vv = vb + kh * 8 + e;
-        bv[e] = (vv < v1) ? a.dy[vv * a.cout + n] : __float2bfloat16_rn(0.f);
+        bv[e] = (vv < v1) ? a.dy[act_index(vv, n, nvox)] : __float2bfloat16_rn(0.f);
       }
       *reinterpret_cast<uint4*>(B + (n >> 3) * 256 + kh * 128 + (n & 7) * 16) =
           *reinterpret_cast<const uint4*>(bv);
@@ -469,8 +542,8 @@ size_t conv_smem(int cout) {
   return (size_t)NSTG * A_BYTES + (size_t)NSTG * cout * KS * 2 + (NSTG + 1) * 8 + 16;
 }
 
-size_t conv_tile_smem(int nt) {
-  return (size_t)NST * (2 * A_HALF + 27 * nt * 32) + (2 * NST + 1) * 8 + 16;
+size_t conv_tile_smem(int nt, int nst, int planes) {
+  return (size_t)nst * (2 * a_half_bytes(planes) + 27 * nt * 32) + (2 * NST + 1) * 8 + 16;
 }
 
 }  // namespace
@@ -483,7 +556,7 @@ int conv3_init() {
   static bool done = false;
   if (done) return SBM_OK;
   SBM_CUDA_TRY(cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)conv_tile_smem(NT_MAX)));
+                                    (int)(kSmemBudget + 1024)));
   SBM_CUDA_TRY(cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)conv_smem(256)));
   done = true;
@@ -524,17 +597,22 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
     cudaFree(dimg);
     return fail(SBM_ERR_NOMEM);
   }
-  cudaMemcpyAsync(dx, x, nv * cin * 2, cudaMemcpyHostToDevice, s);
+  // channels-last host arrays <-> channel-group planes on the device
+  std::vector<uint16_t> xp((size_t)(nv * cin));
+  for (int64_t v = 0; v < nv; ++v)
+    for (int c = 0; c < cin; ++c) xp[(size_t)act_index(v, c, nv)] = x[v * cin + c];
+  cudaMemcpyAsync(dx, xp.data(), nv * cin * 2, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(dw, w, (size_t)cout * 27 * cin * 2, cudaMemcpyHostToDevice, s);
   if (bias) cudaMemcpyAsync(db, bias, cout * 4, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(de, 0, 4, s);
   ConvArgs a{};
   a.ny = ny; a.nx = nx; a.nz = nz; a.nzs = nz; a.cin = cin; a.cout = cout;
-  a.ldx = cin; a.offx = 0; a.ldy = cout; a.offy = 0;
+  a.planes = (nz % 2 == 0) ? 2 : 1;
+  a.ldx = cin; a.offx = 0; a.offy = 0;
   a.x = (const __nv_bfloat16*)dx; a.w = (const __nv_bfloat16*)dw;
   a.bias = bias ? (const float*)db : nullptr;
   a.y16 = nullptr; a.y32 = (float*)dy; a.relu = relu; a.flip = flip; a.err = (int*)de;
-  conv3_wimage(a.w, cout, cin, 0, (__nv_bfloat16*)dimg, s);
+  conv3_wimage(a.w, cout, cin, 0, 64, (__nv_bfloat16*)dimg, s);
   a.wimg = (const __nv_bfloat16*)dimg;
   rc = conv3_launch(&a, nullptr, use_tc, s);
   if (rc) {
@@ -543,11 +621,14 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
     return fail(rc);
   }
   int herr = 0;
-  cudaMemcpyAsync(y, dy, nv * cout * 4, cudaMemcpyDeviceToHost, s);
+  std::vector<float> yp((size_t)(nv * cout));
+  cudaMemcpyAsync(yp.data(), dy, nv * cout * 4, cudaMemcpyDeviceToHost, s);
   cudaMemcpyAsync(&herr, de, 4, cudaMemcpyDeviceToHost, s);
   const cudaError_t e = cudaStreamSynchronize(s);
   cudaFree(dimg);
   if (e != cudaSuccess) return fail(SBM_ERR_CUDA);
+  for (int64_t v = 0; v < nv; ++v)
+    for (int c = 0; c < cout; ++c) y[v * cout + c] = yp[(size_t)act_index(v, c, nv)];
   fail(0);
   return herr ? SBM_ERR_TIMEOUT : SBM_OK;
 }
@@ -570,12 +651,12 @@ int conv3_map(const ConvArgs* pa, ConvMap* m) {
     set_error_msg("cuTensorMapEncodeTiled unavailable");
     return SBM_ERR_STATE;
   }
-  const cuuint64_t ld = (cuuint64_t)a.ldx;
-  cuuint64_t dims[5] = {ld, (cuuint64_t)a.ny, (cuuint64_t)a.nx, (cuuint64_t)a.nzs,
-                        (cuuint64_t)(a.nz / a.nzs)};
-  cuuint64_t strides[4] = {ld * 2, ld * 2 * a.ny, ld * 2 * a.ny * a.nx,
-                           ld * 2 * a.ny * a.nx * a.nzs};
-  cuuint32_t box[5] = {8, HY, HX, HZ, 1};
+  const cuuint64_t row = (cuuint64_t)8 * a.ny;  // 8 channels x y
+  const cuuint64_t V = (cuuint64_t)a.ny * a.nx * a.nz;
+  cuuint64_t dims[5] = {row, (cuuint64_t)a.nx, (cuuint64_t)a.nzs, (cuuint64_t)(a.nz / a.nzs),
+                        (cuuint64_t)(a.ldx / 8)};
+  cuuint64_t strides[4] = {row * 2, row * 2 * a.nx, row * 2 * a.nx * a.nzs, V * 8 * 2};
+  cuuint32_t box[5] = {8 * HY, HX, (cuuint32_t)(a.planes + 2), 1, 1};
   cuuint32_t es[5] = {1, 1, 1, 1, 1};
   const CUresult r = fn(&m->x, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5,
                         const_cast<__nv_bfloat16*>(a.x), dims, strides, box, es,
@@ -588,30 +669,46 @@ int conv3_map(const ConvArgs* pa, ConvMap* m) {
   return SBM_OK;
 }
 
-void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, __nv_bfloat16* img,
-                  cudaStream_t s) {
+void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, int tw,
+                  __nv_bfloat16* img, cudaStream_t s) {
   const int64_t n = (int64_t)cout * 27 * cin;
   int64_t b = (n + 255) / 256;
   if (b > 152 * 16) b = 152 * 16;
-  k_wimage<<<(unsigned)b, 256, 0, s>>>(w, cout, cin, transpose, img);
+  k_wimage<<<(unsigned)b, 256, 0, s>>>(w, cout, cin, transpose, tw, img);
   SBM_LAUNCHED(1);
 }
 
 int conv3_launch(const ConvArgs* pa, const ConvMap* map, int use_tc, cudaStream_t s) {
-  const ConvArgs& a = *pa;
+  ConvArgs a = *pa;
   const int64_t nv = (int64_t)a.ny * a.nx * a.nz;
   if (use_tc) {
     if ((a.ldx % 8) || (a.offx % 8) || (a.nz % a.nzs) || !a.wimg) return SBM_ERR_ARG;
+    if ((a.planes != 1 && a.planes != 2) || (a.planes == 2 && (a.nzs % 2)) ||
+        (a.pool && (a.planes != 2 || a.ny % 2 || a.nx % 2)) || (a.w1x1 && a.cout != 16) ||
+        (a.offu % 8) || (a.offy % 8))
+      return SBM_ERR_ARG;
     ConvMap local;
     if (!map) {
       const int rc = conv3_map(pa, &local);
       if (rc) return rc;
       map = &local;
     }
-    const int64_t tiles = (int64_t)((a.ny + TY - 1) / TY) * ((a.nx + TX - 1) / TX) * a.nz;
-    const int ntn = (a.cout + NT_MAX - 1) / NT_MAX;
-    k_conv3_tc<<<dim3((unsigned)tiles, (unsigned)ntn), NTHR,
-                 conv_tile_smem(std::min(a.cout, NT_MAX)), s>>>(*map, a);
+    const int64_t tiles =
+        (int64_t)((a.ny + TY - 1) / TY) * ((a.nx + TX - 1) / TX) * (a.nz / a.planes);
+    // narrow output tiles when the wide ones leave most SMs idle
+    a.tw = (a.wimg16 && tiles * ((a.cout + NT_MAX - 1) / NT_MAX) < 152) ? 16 : NT_MAX;
+    const int ntn = (a.cout + a.tw - 1) / a.tw;
+    const int nt = std::min(a.cout, a.tw);
+    const int nchunk = a.cin / KS;
+    // a lone wave keeps every chunk in flight; several waves keep two stages
+    // per CTA so that more CTAs share an SM
+    const size_t stage = conv_tile_smem(nt, 1, a.planes) - conv_tile_smem(nt, 0, a.planes);
+    int nst = std::min(2, nchunk);
+    if (tiles * ntn <= 152)
+      nst = std::max(nst, (int)std::min<size_t>(nchunk, kSmemBudget / stage));
+    a.nst = std::min(nst, NST);
+    k_conv3_tc<<<dim3((unsigned)tiles, (unsigned)ntn), NTHR, conv_tile_smem(nt, a.nst, a.planes),
+                 s>>>(*map, a);
   } else {
     const int64_t n = nv * a.cout;
     k_conv3_ref<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);

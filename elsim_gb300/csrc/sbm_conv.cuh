@@ -2,9 +2,14 @@
 // convolution kernels (sbm_conv.cu), shared with the learned
 // preconditioner (sbm_net.cu).
 //
-// Grids are channels-last, voxel v = i + ny*(j + nx*k).  A batch of
-// samples is stacked along z: nz = samples * nzs, and no tap reaches across
-// a sample boundary (zero padding at every sample's faces).
+// Activations are stored in channel-group planes: element (voxel v,
+// channel c) of a buffer of V voxels sits at act_index(v, c, V) =
+// ((c / 8) * V + v) * 8 + c % 8, voxel v = i + ny*(j + nx*k).  A run of 8
+// channels of consecutive y voxels is contiguous, so one tensor-map row of
+// the halo tile is 10 voxels x 16 bytes, and a channel slice starting at a
+// multiple of 8 is a set of whole planes (concatenation buffers).  A batch
+// of samples is stacked along z: nz = samples * nzs, and no tap reaches
+// across a sample boundary (zero padding at every sample's faces).
 #pragma once
 
 #include <cuda.h>
@@ -15,15 +20,20 @@
 
 namespace sbm {
 
+__host__ __device__ __forceinline__ int64_t act_index(int64_t v, int c, int64_t V) {
+  return (((int64_t)(c >> 3) * V + v) << 3) + (c & 7);
+}
+
 struct ConvArgs {
   int ny, nx, nz;          // grid (nz = stacked depth)
   int nzs;                 // depth of one sample
   int cin, cout;           // channels (multiples of 16)
-  int ldx, offx;           // input channel stride and offset (channel slices of concat buffers)
-  int ldy, offy;           // output channel stride and offset
+  int ldx, offx;           // channels of the input buffer and the slice's first channel
+  int offy;                // first output channel in the output buffer
   const __nv_bfloat16* x;
   const __nv_bfloat16* w;  // [cout][27][cin] (CUDA-core kernel)
-  const __nv_bfloat16* wimg;  // weight image of the tensor-core kernel (conv3_wimage)
+  const __nv_bfloat16* wimg;    // weight images of the tensor-core kernel (conv3_wimage)
+  const __nv_bfloat16* wimg16;  //   for 64- and 16-channel output tiles (wimg16 may be null)
   const float* bias;       // [cout] or null
   __nv_bfloat16* y16;      // BF16 output or null
   float* y32;              // FP32 output or null
@@ -31,12 +41,23 @@ struct ConvArgs {
   int flip;                // 1: tap t reads neighbour -offset (transposed convolution)
   int* err;                // set to 1 if a wait expired
   const int* skip;         // launch is a no-op while *skip != 0 (may be null)
+  // tensor-core kernel only:
+  int planes;              // z planes per CTA: 1, or 2 (nzs even)
+  __nv_bfloat16* pool;     // 2x2x2-averaged BF16 output [V/8][cout] (planes 2) or null
+  __nv_bfloat16* up;       // BF16 output copied to the 8 children in the 2x finer grid
+  int offu;                //   (first channel there) or null
+  const float* w1x1;       // fused 1x1 output layer (cout 16): out1x1[v] = b1x1 +
+  const float* b1x1;       //   sum_c w1x1[c] bf16(y[v][c]), or null
+  float* out1x1;
+  // set by conv3_launch
+  int tw;                  // output channels per CTA tile (64 or 16)
+  int nst;                 // pipeline stages
 };
 
 struct WgradArgs {
   int ny, nx, nz, nzs;
   int cin, cout;
-  int ldx, offx;                 // input activation channel stride / offset
+  int offx;                      // first channel of the layer input in its buffer
   const __nv_bfloat16* x;        // forward input of the layer
   const __nv_bfloat16* dy;       // gradient of the pre-activation [V][cout]
   float* dw;                     // [cout][27][cin], accumulated (atomic adds)
@@ -44,9 +65,9 @@ struct WgradArgs {
   int* err;
 };
 
-// Tensor map of a convolution input: 5-D (channel, y, x, z within the
-// sample, sample) over x with channel stride ldx; box = one 8-channel half
-// of the halo tile.
+// Tensor map of a convolution input: 5-D (8 channels x y merged, x, z
+// within the sample, sample, channel group); box = one 8-channel half of
+// the halo tile.
 struct ConvMap {
   CUtensorMap x;
 };
@@ -56,19 +77,21 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 bool conv_shape_ok(int cin, int cout);
 int conv3_init();
 int conv3_map(const ConvArgs* a, ConvMap* m);
-// Weight image of the tensor-core kernel from w [cout][27][cin] (transpose
-// = 0), or of the transposed convolution (data gradient) from the layer's
-// weights [cin][27][cout] (transpose = 1, cout/cin are those of the
-// transposed convolution).  img has cout*27*cin elements.
-void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, __nv_bfloat16* img,
-                  cudaStream_t s);
+// Weight image (output-channel tiles of width tw = 64 or 16) of the
+// tensor-core kernel from w [cout][27][cin] (transpose = 0), or of the
+// transposed convolution (data gradient) from the layer's weights
+// [cin][27][cout] (transpose = 1, cout/cin are those of the transposed
+// convolution).  img has cout*27*cin elements.
+void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, int tw,
+                  __nv_bfloat16* img, cudaStream_t s);
 // Index in the weight image of element (co, tap, ci) of a convolution with
-// cout x cin channels.
-__host__ __device__ inline int64_t wimage_index(int co, int t, int ci, int cout, int cin) {
-  const int j = co >> 6, n = co & 63;
-  const int nt = min(64, cout - 64 * j);
+// cout x cin channels: per output tile, per 16-channel input chunk, the
+// chunk's B operands of the 27 taps, each in the canonical K-major layout.
+__host__ __device__ inline int64_t wimage_index(int co, int t, int ci, int cout, int cin, int tw) {
+  const int j = co / tw, n = co % tw;
+  const int nt = min(tw, cout - tw * j);
   const int c = ci >> 4, kh = (ci >> 3) & 1, e = ci & 7;
-  const int64_t byte = (int64_t)64 * j * 27 * cin * 2 + (int64_t)c * 27 * nt * 32 +
+  const int64_t byte = (int64_t)tw * j * 27 * cin * 2 + (int64_t)c * 27 * nt * 32 +
                        (int64_t)t * nt * 32 + (n >> 3) * 256 + kh * 128 + (n & 7) * 16 + e * 2;
   return byte / 2;
 }

@@ -96,7 +96,7 @@ struct Work {
   float* gcat[4] = {};  // data gradients of the decoder inputs
   float* gpin[kLev] = {};
   std::vector<void*> mem;
-  std::map<const void*, ConvMap> maps;  // tensor map of each convolution input
+  std::map<std::pair<const void*, int>, ConvMap> maps;  // per convolution input and planes
   ~Work() {
     for (void* p : mem) cudaFree(p);
   }
@@ -131,114 +131,89 @@ __device__ __forceinline__ int64_t child(const Dims& f, int i, int j, int k, int
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (n);         \
        t += (int64_t)gridDim.x * blockDim.x)
 
-// y[vc][c] = mean of x[child][offx + c] over the 8 children (average
-// pooling); one thread per coarse voxel and 8 channels (16-byte accesses).
-__global__ void k_pool(Dims f, int C, const bf16* __restrict__ x, int ldx, int offx,
-                       bf16* __restrict__ y, const int* skip) {
-  if (skip && *skip) return;
-  const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
-  const int G = C / 8;
-  NET_LOOP(c.v() * G) {
-    const int g8 = (int)(t % G) * 8;
-    const int64_t vc = t / G;
-    int i, j, k;
-    vox(c, vc, &i, &j, &k);
-    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+// Loads / stores of one 8-channel group of a voxel (channel-group planes).
+__device__ __forceinline__ void ld8(const bf16* p, float (&v)[8]) {
+  const uint4 u = *reinterpret_cast<const uint4*>(p);
+  const bf16* h = reinterpret_cast<const bf16*>(&u);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const uint4 u = *reinterpret_cast<const uint4*>(x + child(f, i, j, k, q) * ldx + offx + g8);
-      const bf16* h = reinterpret_cast<const bf16*>(&u);
+  for (int e = 0; e < 8; ++e) v[e] = __bfloat162float(h[e]);
+}
+__device__ __forceinline__ void ld8(const float* p, float (&v)[8]) {
+  const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void st8(bf16* p, const float (&v)[8]) {
+  __align__(16) bf16 h[8];
 #pragma unroll
-      for (int e = 0; e < 8; ++e) s[e] += __bfloat162float(h[e]);
-    }
-    __align__(16) bf16 o[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) o[e] = __float2bfloat16_rn(s[e] * 0.125f);
-    *reinterpret_cast<uint4*>(y + vc * C + g8) = *reinterpret_cast<const uint4*>(o);
-  }
+  for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16_rn(v[e]);
+  *reinterpret_cast<uint4*>(p) = *reinterpret_cast<const uint4*>(h);
 }
 
-// y[vf][offy + c] = x[parent(vf)][c] (nearest-neighbour upsampling); one
-// thread per fine voxel and 8 channels.
-__global__ void k_up(Dims f, int C, const bf16* __restrict__ x, bf16* __restrict__ y, int ldy,
-                     int offy, const int* skip) {
-  if (skip && *skip) return;
-  const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
-  const int G = C / 8;
-  NET_LOOP(f.v() * G) {
-    const int g8 = (int)(t % G) * 8;
-    const int64_t vf = t / G;
-    int i, j, k;
-    vox(f, vf, &i, &j, &k);
-    *reinterpret_cast<uint4*>(y + vf * ldy + offy + g8) =
-        *reinterpret_cast<const uint4*>(x + vid(c, i / 2, j / 2, k / 2) * C + g8);
-  }
-}
-
-// Backward of upsampling + ReLU: out[vc][c] = (act[vc][c] > 0) *
-// sum over the children of g[vf][offg + c].
-__global__ void k_bwd_up(Dims f, int C, const float* __restrict__ g, int ldg, int offg,
+// Backward of upsampling + ReLU: out(vc, c) = (act(vc, c) > 0) * sum over
+// the children of g(vf, offg + c).  One thread per coarse voxel and group.
+__global__ void k_bwd_up(Dims f, int C, const float* __restrict__ g, int offg,
                          const bf16* __restrict__ act, bf16* __restrict__ out) {
   const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
-  NET_LOOP(c.v() * C) {
-    const int ch = (int)(t % C);
-    const int64_t vc = t / C;
+  const int64_t Vc = c.v(), Vf = f.v();
+  NET_LOOP(Vc * (C / 8)) {
+    const int64_t vc = t % Vc;
+    const int grp = (int)(t / Vc) * 8;
     int i, j, k;
     vox(c, vc, &i, &j, &k);
-    float s = 0.f;
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, a[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s += g[child(f, i, j, k, q) * ldg + offg + ch];
-    out[vc * C + ch] = __float2bfloat16_rn(__bfloat162float(act[vc * C + ch]) > 0.f ? s : 0.f);
+    for (int q = 0; q < 8; ++q) {
+      float v[8];
+      ld8(g + act_index(child(f, i, j, k, q), offg + grp, Vf), v);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) s[e] += v[e];
+    }
+    ld8(act + act_index(vc, grp, Vc), a);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) s[e] = a[e] > 0.f ? s[e] : 0.f;
+    st8(out + act_index(vc, grp, Vc), s);
   }
 }
 
 // Backward of an encoder output read by the skip connection and by the
-// pooling: out[vf][c] = (act > 0) * (g[vf][offg + c] + gp[parent][c] / 8).
-__global__ void k_bwd_skip(Dims f, int C, const float* __restrict__ g, int ldg, int offg,
-                           const float* __restrict__ gp, const bf16* __restrict__ act, int lda,
-                           int offa, bf16* __restrict__ out) {
+// pooling: out(vf, c) = (act(vf, offa + c) > 0) * (g(vf, offg + c) +
+// gp(parent, c) / 8).  One thread per fine voxel and group.
+__global__ void k_bwd_skip(Dims f, int C, const float* __restrict__ g, int offg,
+                           const float* __restrict__ gp, const bf16* __restrict__ act, int offa,
+                           bf16* __restrict__ out) {
   const Dims c = Dims{f.ny / 2, f.nx / 2, f.nz / 2, f.nzs / 2};
-  NET_LOOP(f.v() * C) {
-    const int ch = (int)(t % C);
-    const int64_t vf = t / C;
-    float s = g[vf * ldg + offg + ch];
+  const int64_t Vc = c.v(), Vf = f.v();
+  NET_LOOP(Vf * (C / 8)) {
+    const int64_t vf = t % Vf;
+    const int grp = (int)(t / Vf) * 8;
+    float s[8], a[8];
+    ld8(g + act_index(vf, offg + grp, Vf), s);
     if (gp) {
       int i, j, k;
       vox(f, vf, &i, &j, &k);
-      s += 0.125f * gp[vid(c, i / 2, j / 2, k / 2) * C + ch];
+      float p[8];
+      ld8(gp + act_index(vid(c, i / 2, j / 2, k / 2), grp, Vc), p);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) s[e] += 0.125f * p[e];
     }
-    out[vf * C + ch] = __float2bfloat16_rn(__bfloat162float(act[vf * lda + offa + ch]) > 0.f ? s : 0.f);
+    ld8(act + act_index(vf, offa + grp, Vf), a);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) s[e] = a[e] > 0.f ? s[e] : 0.f;
+    st8(out + act_index(vf, grp, Vf), s);
   }
 }
 
-// 1x1 output layer (FP32 weights): out[v] = b + sum_c w[c] d0[v][c]; with a
-// target, *loss += sum (out - tgt)^2.
-__global__ void k_out_fwd(int64_t V, const bf16* __restrict__ d0, const float* __restrict__ w,
-                          const float* __restrict__ b, float* __restrict__ out,
-                          const float* __restrict__ tgt, double* loss, const int* skip) {
-  if (skip && *skip) return;
+// *loss += sum_v (out[v] - tgt[v])^2
+__global__ void k_loss(int64_t V, const float* __restrict__ out, const float* __restrict__ tgt,
+                       double* loss) {
   __shared__ double sm[32];
   double acc = 0.0;
   NET_LOOP(V) {
-    const uint4* p = reinterpret_cast<const uint4*>(d0 + t * 16);
-    const uint4 lo = p[0], hi = p[1];
-    const bf16* a = reinterpret_cast<const bf16*>(&lo);
-    const bf16* h = reinterpret_cast<const bf16*>(&hi);
-    float s = b[0];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) s += w[c] * __bfloat162float(a[c]);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) s += w[8 + c] * __bfloat162float(h[c]);
-    out[t] = s;
-    if (tgt) {
-      const double e = (double)s - (double)tgt[t];
-      acc += e * e;
-    }
+    const double e = (double)out[t] - (double)tgt[t];
+    acc += e * e;
   }
-  if (tgt) {
-    const double tot = block_sum(acc, sm);
-    if (threadIdx.x == 0) atomicAdd(loss, tot);
-  }
+  const double tot = block_sum(acc, sm);
+  if (threadIdx.x == 0) atomicAdd(loss, tot);
 }
 
 // Backward of the output layer and of D0's ReLU:
@@ -258,10 +233,15 @@ __global__ void k_out_bwd(int64_t V, float inv_v, const bf16* __restrict__ d0,
     const float dout = 2.f * (out[t] - tgt[t]) * inv_v;
     acc[16] += dout;
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      const float a = __bfloat162float(d0[t * 16 + c]);
-      acc[c] += dout * a;
-      gd0[t * 16 + c] = __float2bfloat16_rn(a > 0.f ? dout * w[c] : 0.f);
+    for (int h = 0; h < 2; ++h) {
+      float a[8], gv[8];
+      ld8(d0 + act_index(t, 8 * h, V), a);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        acc[8 * h + e] += dout * a[e];
+        gv[e] = a[e] > 0.f ? dout * w[8 * h + e] : 0.f;
+      }
+      st8(gd0 + act_index(t, 8 * h, V), gv);
     }
   }
 #pragma unroll
@@ -285,7 +265,7 @@ __global__ void k_bias_grad(int64_t V, int C, const bf16* __restrict__ dy, float
   float s = 0.f;
   if (grp < groups)
     for (int64_t v = (int64_t)blockIdx.x * groups + grp; v < V; v += (int64_t)gridDim.x * groups)
-      s += __bfloat162float(dy[v * C + c]);
+      s += __bfloat162float(dy[act_index(v, c, V)]);
   if (grp < groups) atomicAdd(&sm[c], s);
   __syncthreads();
   if (threadIdx.x < C) atomicAdd(&gb[threadIdx.x], sm[threadIdx.x]);
@@ -303,7 +283,8 @@ struct LayerTab {
 __global__ void k_adam(int64_t P, int update, float* __restrict__ w, const float* __restrict__ g,
                        float* __restrict__ m, float* __restrict__ v, float lr, float b1, float b2,
                        float eps, float c1, float c2, LayerTab tab, bf16* __restrict__ wimg,
-                       bf16* __restrict__ wtimg) {
+                       bf16* __restrict__ wtimg, bf16* __restrict__ wimg16,
+                       bf16* __restrict__ wtimg16) {
   NET_LOOP(P) {
     float wv = w[t];
     if (update) {
@@ -323,8 +304,10 @@ __global__ void k_adam(int64_t P, int update, float* __restrict__ w, const float
         const int ci = (int)(rel % tab.ci[l]);
         const int tap = (int)((rel / tab.ci[l]) % 27);
         const int co = (int)(rel / ((int64_t)27 * tab.ci[l]));
-        wimg[tab.off[l] + wimage_index(co, tap, ci, tab.co[l], tab.ci[l])] = b;
-        wtimg[tab.off[l] + wimage_index(ci, tap, co, tab.ci[l], tab.co[l])] = b;
+        wimg[tab.off[l] + wimage_index(co, tap, ci, tab.co[l], tab.ci[l], 64)] = b;
+        wtimg[tab.off[l] + wimage_index(ci, tap, co, tab.ci[l], tab.co[l], 64)] = b;
+        wimg16[tab.off[l] + wimage_index(co, tap, ci, tab.co[l], tab.ci[l], 16)] = b;
+        wtimg16[tab.off[l] + wimage_index(ci, tap, co, tab.ci[l], tab.co[l], 16)] = b;
       }
     }
   }
@@ -353,8 +336,10 @@ struct sbm_net {
   float* m = nullptr;
   float* v = nullptr;
   float* grad = nullptr;
-  bf16* wimg = nullptr;   // forward weight images
+  bf16* wimg = nullptr;   // forward weight images (64-wide output tiles)
   bf16* wtimg = nullptr;  // data-gradient weight images
+  bf16* wimg16 = nullptr;   // the same for 16-wide output tiles
+  bf16* wtimg16 = nullptr;
   int* err = nullptr;
   double* loss = nullptr;
   int64_t step = 0;
@@ -378,7 +363,7 @@ LayerTab layer_tab() {
 int cast_weights(sbm_net* n, cudaStream_t s) {
   k_adam<<<grid_for(kL.total), 256, 0, s>>>(kL.total, 0, n->w32, nullptr, nullptr, nullptr, 0.f,
                                             0.f, 0.f, 0.f, 0.f, 0.f, layer_tab(), n->wimg,
-                                            n->wtimg);
+                                            n->wtimg, n->wimg16, n->wtimg16);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
@@ -426,66 +411,85 @@ Work* work_for(sbm_net* n, int ny, int nx, int nzs, int nb, bool train) {
   return w;
 }
 
-// Tensor map of a convolution input (encoded once per buffer).
+// Tensor map of a convolution input (encoded once per buffer and plane count).
 const ConvMap* map_for(Work& w, const ConvArgs& a) {
-  auto it = w.maps.find(a.x);
+  const auto key = std::make_pair((const void*)a.x, a.planes);
+  auto it = w.maps.find(key);
   if (it != w.maps.end()) return &it->second;
   ConvMap m;
   if (conv3_map(&a, &m)) return nullptr;
-  return &(w.maps[a.x] = m);
+  return &(w.maps[key] = m);
 }
 
-int conv(sbm_net* n, Work& w, int l, int lev, const bf16* x, int ldx, bf16* y, int ldy,
-         int offy, const int* skip, cudaStream_t s) {
+// Arguments of layer l at level lev reading x (a buffer of ldx channels),
+// with ReLU; outputs are filled in by the caller.
+// Two z planes per CTA where the epilogue pools (it needs both planes of a
+// 2x2x2 block) or the grid is large; one plane keeps more CTAs busy on the
+// small levels.
+int planes_for(const Dims& d, bool pool) {
+  if (d.nzs % 2) return 1;
+  return (pool || d.v() >= (int64_t)1 << 17) ? 2 : 1;
+}
+
+ConvArgs layer_args(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx,
+                    bool pool, const int* skip) {
   ConvArgs a{};
   const Dims& d = w.d[lev];
   a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
+  a.planes = planes_for(d, pool);
   a.cin = kCi[l]; a.cout = kCo[l];
-  a.ldx = ldx; a.offx = 0; a.ldy = ldy; a.offy = offy;
-  a.x = x; a.wimg = n->wimg + kL.off[l]; a.bias = n->w32 + kL.boff[l];
-  a.y16 = y; a.y32 = nullptr; a.relu = 1; a.flip = 0; a.err = n->err; a.skip = skip;
+  a.ldx = ldx; a.offx = 0;
+  a.x = x; a.wimg = n->wimg + kL.off[l]; a.wimg16 = n->wimg16 + kL.off[l];
+  a.bias = n->w32 + kL.boff[l];
+  a.relu = 1; a.flip = 0; a.err = n->err; a.skip = skip;
+  return a;
+}
+
+int launch(Work& w, const ConvArgs& a, cudaStream_t s) {
   const ConvMap* m = map_for(w, a);
   if (!m) return SBM_ERR_STATE;
   return conv3_launch(&a, m, 1, s);
 }
 
-void pool(const Work& w, int lev, int C, const bf16* x, int ldx, int offx, bf16* y,
-          const int* skip, cudaStream_t s) {
-  const Dims& f = w.d[lev];
-  k_pool<<<grid_for(f.v() / 8 * C / 8), 256, 0, s>>>(f, C, x, ldx, offx, y, skip);
-  SBM_LAUNCHED(1);
-}
-
-void up(const Work& w, int lev, int C, const bf16* x, bf16* y, int ldy, const int* skip,
-        cudaStream_t s) {
-  const Dims& f = w.d[lev];
-  k_up<<<grid_for(f.v() * C / 8), 256, 0, s>>>(f, C, x, y, ldy, 0, skip);
-  SBM_LAUNCHED(1);
-}
-
 // Forward pass of the U-Net on w.in0 -> w.out (and the squared error
-// against w.tgt into n->loss when tgt).
+// against w.tgt into n->loss when tgt).  Pooling, upsampling and the 1x1
+// output layer run in the convolution epilogues; activations that only the
+// backward pass reads (bottleneck and decoder outputs) are stored only
+// when training.
 int forward(sbm_net* n, Work& w, bool tgt, const int* skip, cudaStream_t s) {
   int rc;
   for (int lev = 0; lev < 4; ++lev) {
     const int l = kEnc[lev];
-    const bf16* x = lev == 0 ? w.in0 : w.pin[lev];
-    if ((rc = conv(n, w, l, lev, x, kCi[l], w.cat[lev], kCatW[lev], kUpW[lev], skip, s)))
-      return rc;
-    pool(w, lev, kCo[l], w.cat[lev], kCatW[lev], kUpW[lev], w.pin[lev + 1], skip, s);
+    ConvArgs a = layer_args(n, w, l, lev, lev == 0 ? w.in0 : w.pin[lev], kCi[l], true, skip);
+    a.y16 = w.cat[lev];
+    a.offy = kUpW[lev];
+    a.pool = w.pin[lev + 1];
+    if ((rc = launch(w, a, s))) return rc;
   }
-  if ((rc = conv(n, w, E4, 4, w.pin[4], kCi[E4], w.a4, kCo[E4], 0, skip, s))) return rc;
+  {
+    ConvArgs a = layer_args(n, w, E4, 4, w.pin[4], kCi[E4], false, skip);
+    a.y16 = w.train ? w.a4 : nullptr;
+    a.up = w.cat[3];
+    if ((rc = launch(w, a, s))) return rc;
+  }
   for (int lev = 3; lev >= 0; --lev) {
-    const bf16* below = lev == 3 ? w.a4 : w.dec[lev + 1];
-    up(w, lev, kUpW[lev], below, w.cat[lev], kCatW[lev], skip, s);
     const int l = kDec[lev];
-    if ((rc = conv(n, w, l, lev, w.cat[lev], kCatW[lev], w.dec[lev], kCo[l], 0, skip, s)))
-      return rc;
+    ConvArgs a = layer_args(n, w, l, lev, w.cat[lev], kCatW[lev], false, skip);
+    a.y16 = w.train ? w.dec[lev] : nullptr;
+    if (lev > 0) {
+      a.up = w.cat[lev - 1];
+    } else {
+      a.w1x1 = n->w32 + kL.off[OUT];
+      a.b1x1 = n->w32 + kL.boff[OUT];
+      a.out1x1 = w.out;
+    }
+    if ((rc = launch(w, a, s))) return rc;
   }
-  const int64_t V = w.d[0].v();
-  k_out_fwd<<<grid_for(V), 256, 0, s>>>(V, w.dec[0], n->w32 + kL.off[OUT], n->w32 + kL.boff[OUT],
-                                        w.out, tgt ? w.tgt : nullptr, n->loss, skip);
-  SBM_LAUNCHED(1);
+  if (tgt) {
+    const int64_t V = w.d[0].v();
+    k_loss<<<grid_for(V), 256, 0, s>>>(V, w.out, w.tgt, n->loss);
+    SBM_LAUNCHED(1);
+  }
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
 }
@@ -495,7 +499,7 @@ int wgrad(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx, con
   const Dims& d = w.d[lev];
   WgradArgs a{};
   a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
-  a.cin = kCi[l]; a.cout = kCo[l]; a.ldx = ldx; a.offx = 0;
+  a.cin = kCi[l]; a.cout = kCo[l]; a.offx = 0;
   a.x = x; a.dy = gy; a.dw = n->grad + kL.off[l]; a.err = n->err;
   const int64_t V = d.v();
   const int64_t gx = (27 * kCi[l] + 127) / 128;
@@ -520,13 +524,13 @@ int dgrad(sbm_net* n, Work& w, int l, int lev, const bf16* gy, float* gx, cudaSt
   ConvArgs a{};
   const Dims& d = w.d[lev];
   a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
+  a.planes = planes_for(d, false);
   a.cin = kCo[l]; a.cout = kCi[l];
-  a.ldx = kCo[l]; a.offx = 0; a.ldy = kCi[l]; a.offy = 0;
-  a.x = gy; a.wimg = n->wtimg + kL.off[l]; a.bias = nullptr;
+  a.ldx = kCo[l]; a.offx = 0; a.offy = 0;
+  a.x = gy; a.wimg = n->wtimg + kL.off[l]; a.wimg16 = n->wtimg16 + kL.off[l];
+  a.bias = nullptr;
   a.y16 = nullptr; a.y32 = gx; a.relu = 0; a.flip = 1; a.err = n->err; a.skip = nullptr;
-  const ConvMap* m = map_for(w, a);
-  if (!m) return SBM_ERR_STATE;
-  return conv3_launch(&a, m, 1, s);
+  return launch(w, a, s);
 }
 
 // Gradient of mean (out - tgt)^2 over all voxels of w into n->grad
@@ -546,8 +550,8 @@ int backward(sbm_net* n, Work& w, cudaStream_t s) {
     const Dims& f = w.d[lev];
     const bf16* act = lev == 3 ? w.a4 : w.dec[lev + 1];
     bf16* out = lev == 3 ? w.ga4 : w.gdec[lev + 1];
-    k_bwd_up<<<grid_for(f.v() / 8 * kUpW[lev]), 256, 0, s>>>(f, kUpW[lev], w.gcat[lev],
-                                                             kCatW[lev], 0, act, out);
+    k_bwd_up<<<grid_for(f.v() / 8 * kUpW[lev] / 8), 256, 0, s>>>(f, kUpW[lev], w.gcat[lev], 0,
+                                                                 act, out);
     SBM_LAUNCHED(1);
   }
   if ((rc = wgrad(n, w, E4, 4, w.pin[4], kCi[E4], w.ga4, s))) return rc;
@@ -556,9 +560,9 @@ int backward(sbm_net* n, Work& w, cudaStream_t s) {
     const int l = kEnc[lev];
     const Dims& f = w.d[lev];
     const int C = kCo[l];
-    k_bwd_skip<<<grid_for(f.v() * C), 256, 0, s>>>(f, C, w.gcat[lev], kCatW[lev], kUpW[lev],
-                                                   w.gpin[lev + 1], w.cat[lev], kCatW[lev],
-                                                   kUpW[lev], w.genc[lev]);
+    k_bwd_skip<<<grid_for(f.v() * C / 8), 256, 0, s>>>(f, C, w.gcat[lev], kUpW[lev],
+                                                       w.gpin[lev + 1], w.cat[lev], kUpW[lev],
+                                                       w.genc[lev]);
     SBM_LAUNCHED(1);
     const bf16* x = lev == 0 ? w.in0 : w.pin[lev];
     if ((rc = wgrad(n, w, l, lev, x, kCi[l], w.genc[lev], s))) return rc;
@@ -574,7 +578,8 @@ int adam(sbm_net* n, float lr, cudaStream_t s) {
   const float c1 = 1.f / (1.f - powf(b1, (float)n->step));
   const float c2 = 1.f / (1.f - powf(b2, (float)n->step));
   k_adam<<<grid_for(kL.total), 256, 0, s>>>(kL.total, 1, n->w32, n->grad, n->m, n->v, lr, b1, b2,
-                                            eps, c1, c2, layer_tab(), n->wimg, n->wtimg);
+                                            eps, c1, c2, layer_tab(), n->wimg, n->wtimg,
+                                            n->wimg16, n->wtimg16);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
@@ -587,9 +592,16 @@ uint16_t to_bf16_bits(float f) {
   return (uint16_t)(u >> 16);
 }
 
-int upload_bf16(bf16* dst, const float* src, int64_t n, cudaStream_t s) {
+// Channels-last FP32 input features (nblk blocks of V voxels x 16) ->
+// BF16 channel-group planes, each block planar over its own V.
+int upload_features(bf16* dst, const float* src, int64_t V, int64_t nblk, cudaStream_t s) {
+  const int64_t n = V * kFeat * nblk;
   std::vector<uint16_t> h((size_t)n);
-  for (int64_t i = 0; i < n; ++i) h[(size_t)i] = to_bf16_bits(src[i]);
+  for (int64_t b = 0; b < nblk; ++b)
+    for (int64_t v = 0; v < V; ++v)
+      for (int c = 0; c < kFeat; ++c)
+        h[(size_t)(b * V * kFeat + act_index(v, c, V))] =
+            to_bf16_bits(src[(b * V + v) * kFeat + c]);
   SBM_CUDA_TRY(cudaMemcpyAsync(dst, h.data(), sizeof(uint16_t) * n, cudaMemcpyHostToDevice, s));
   SBM_CUDA_TRY(cudaStreamSynchronize(s));
   return SBM_OK;
@@ -662,14 +674,15 @@ __global__ void k_pc_feat(Dims c, const float* __restrict__ coefc, const float* 
     f[3] = (bcx0 == SBM_BC_ZERO && j == 0) ? 1.f : 0.f;
     f[4] = (bcx1 == SBM_BC_ZERO && j == c.nx - 1) ? 1.f : 0.f;
 #pragma unroll
-    for (int q = 1; q < kFeat; ++q) in0[t * kFeat + q] = __float2bfloat16_rn(f[q]);
+    for (int q = 1; q < kFeat; ++q) in0[act_index(t, q, c.v())] = __float2bfloat16_rn(f[q]);
   }
 }
 
-// rc = R r (4x4x4 means of the FP32 residual), s = RMS(rc).
+// rc = R r (4x4x4 means of the FP32 residual), s = RMS(rc); only when the
+// update kernel has not produced them (first use, residual replacement).
 __global__ void k_pc_restrict(Geo g, Dims c, const float* __restrict__ r, float* __restrict__ rc,
                               double* partials, float* scal, CgState* st) {
-  if (st->done) return;
+  if (st->done || st->aux[1] != 0.0) return;
   double acc = 0.0;
   NET_LOOP(c.v()) {
     int i, j, k;
@@ -699,7 +712,7 @@ __global__ void k_pc_pack(int64_t V, const float* __restrict__ rc, const float* 
                           bf16* __restrict__ in0, const CgState* st) {
   if (st->done) return;
   const float inv = scal[1];
-  NET_LOOP(V) in0[t * kFeat] = __float2bfloat16_rn(rc[t] * inv);
+  NET_LOOP(V) in0[act_index(t, 0, V)] = __float2bfloat16_rn(rc[t] * inv);
 }
 
 // Interpolation weights of the 4 fine cells of one coarse cell along an
@@ -712,9 +725,11 @@ __device__ __forceinline__ void interp1(int fi, int n, int* lo, int* hi, float* 
   *wlo = wl[e];
 }
 
-// z = invd*r + f * P(out) over the fine interior (4 y-consecutive cells per
-// item), f = s k_out / (scale c_ref); z.r and z.q_old reduced; the last
-// block sets rho, beta of the flexible CG.
+// z = invd*r + f * P(out) over the fine interior, f = s k_out / (scale
+// c_ref); z.r and z.q_old reduced; the last block sets rho, beta of the
+// flexible CG.  One item = 4 y-consecutive fine cells (one coarse cell in
+// y) on one x row, marched over the 4 fine planes of one coarse z cell, so
+// the coarse values (3 y x 2 x x 3 z) are loaded once for 16 cells.
 __global__ void __launch_bounds__(256)
     k_pc_prolong(Geo g, Dims c, const float* __restrict__ out, const float* scal,
                  const float* __restrict__ r, const float* __restrict__ iv,
@@ -723,43 +738,50 @@ __global__ void __launch_bounds__(256)
   if (st->done) return;
   const float f = scal[0] * scal[2];
   const int nchunk = g.ny / 4;
-  const int64_t n = (int64_t)nchunk * g.nx * g.nz;
+  const int64_t n = (int64_t)nchunk * g.nx * (g.nz / 4);
+  const float wl[4] = {0.375f, 0.125f, 0.875f, 0.625f};
   float a_zr = 0.f, a_zq = 0.f;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
        u += (int64_t)gridDim.x * blockDim.x) {
     const int m = (int)(u % nchunk);
     const int64_t rr = u / nchunk;
     const int j = (int)(rr % g.nx) + 1;
-    const int k = (int)(rr / g.nx) + 1;
-    int x0, x1, z0, z1;
-    float wx, wz;
+    const int kc = (int)(rr / g.nx);
+    int x0, x1;
+    float wx;
     interp1(j - 1, c.nx, &x0, &x1, &wx);
-    interp1(k - 1, c.nz, &z0, &z1, &wz);
-    const int ym = max(m - 1, 0), yp = min(m + 1, c.ny - 1);
-    float col[3];  // y-neighbours (m-1, m, m+1) interpolated in x and z
-    const int ys[3] = {ym, m, yp};
+    const int ys[3] = {max(m - 1, 0), m, min(m + 1, c.ny - 1)};
+    const int zs[3] = {max(kc - 1, 0), kc, min(kc + 1, c.nz - 1)};
+    float cx[3][3];  // [y neighbour][z plane], interpolated in x
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float v00 = out[(int64_t)ys[a] + (int64_t)c.ny * (x0 + (int64_t)c.nx * z0)];
-      const float v10 = out[(int64_t)ys[a] + (int64_t)c.ny * (x1 + (int64_t)c.nx * z0)];
-      const float v01 = out[(int64_t)ys[a] + (int64_t)c.ny * (x0 + (int64_t)c.nx * z1)];
-      const float v11 = out[(int64_t)ys[a] + (int64_t)c.ny * (x1 + (int64_t)c.nx * z1)];
-      col[a] = wz * (wx * v00 + (1.f - wx) * v10) + (1.f - wz) * (wx * v01 + (1.f - wx) * v11);
+    for (int b = 0; b < 3; ++b) {
+      const int64_t r0 = (int64_t)c.ny * (x0 + (int64_t)c.nx * zs[b]);
+      const int64_t r1 = (int64_t)c.ny * (x1 + (int64_t)c.nx * zs[b]);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) cx[a][b] = wx * out[r0 + ys[a]] + (1.f - wx) * out[r1 + ys[a]];
     }
-    const float e4[4] = {0.375f * col[0] + 0.625f * col[1], 0.125f * col[0] + 0.875f * col[1],
-                         0.875f * col[1] + 0.125f * col[2], 0.625f * col[1] + 0.375f * col[2]};
-    const int64_t idx = g.ix(4 * m + 1, j, k);
-    const float4 rv = *reinterpret_cast<const float4*>(r + idx);
-    const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
-    const float4 qv = *reinterpret_cast<const float4*>(q + idx);
-    float4 zv;
-    zv.x = dv.x * rv.x + f * e4[0];
-    zv.y = dv.y * rv.y + f * e4[1];
-    zv.z = dv.z * rv.z + f * e4[2];
-    zv.w = dv.w * rv.w + f * e4[3];
-    *reinterpret_cast<float4*>(z + idx) = zv;
-    a_zr += (zv.x * rv.x + zv.y * rv.y) + (zv.z * rv.z + zv.w * rv.w);
-    a_zq += (zv.x * qv.x + zv.y * qv.y) + (zv.z * qv.z + zv.w * qv.w);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int lo = e < 2 ? 0 : 1;  // coarse planes (lo, lo + 1) of fine plane e
+      const float wz = wl[e];
+      float col[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) col[a] = wz * cx[a][lo] + (1.f - wz) * cx[a][lo + 1];
+      const float e4[4] = {0.375f * col[0] + 0.625f * col[1], 0.125f * col[0] + 0.875f * col[1],
+                           0.875f * col[1] + 0.125f * col[2], 0.625f * col[1] + 0.375f * col[2]};
+      const int64_t idx = g.ix(4 * m + 1, j, 4 * kc + 1 + e);
+      const float4 rv = *reinterpret_cast<const float4*>(r + idx);
+      const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
+      const float4 qv = *reinterpret_cast<const float4*>(q + idx);
+      float4 zv;
+      zv.x = dv.x * rv.x + f * e4[0];
+      zv.y = dv.y * rv.y + f * e4[1];
+      zv.z = dv.z * rv.z + f * e4[2];
+      zv.w = dv.w * rv.w + f * e4[3];
+      *reinterpret_cast<float4*>(z + idx) = zv;
+      a_zr += (zv.x * rv.x + zv.y * rv.y) + (zv.z * rv.z + zv.w * rv.w);
+      a_zq += (zv.x * qv.x + zv.y * qv.y) + (zv.z * qv.z + zv.w * qv.w);
+    }
   }
   double v[2] = {(double)a_zr, (double)a_zq}, tot[2];
   if (grid_reduce<2>(v, partials, &st->counter[5], tot)) {
@@ -846,7 +868,10 @@ float* net_pc_zbuf(sbm_ctx* ctx) {
   return pc->zf + kOff32;
 }
 
-int net_pc_nodes() { return 3 + 9 + 4 + 4 + 1; }
+float* net_pc_rc(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->rc; }
+float* net_pc_scal(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->scal; }
+
+int net_pc_nodes() { return 3 + 9; }
 
 void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const float* q32,
                    double* partials, CgState* st, cudaStream_t s) {
@@ -858,8 +883,8 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   netd::k_pc_pack<<<netd::grid_for(c.v()), 256, 0, s>>>(c.v(), pc->rc, pc->scal, pc->w->in0, st);
   SBM_LAUNCHED(2);
   netd::forward(pc->net, *pc->w, false, &st->done, s);
-  const int64_t items = (int64_t)(g.ny / 4) * g.nx * g.nz;
-  int64_t b = (items + 256 * 4 - 1) / (256 * 4);
+  const int64_t items = (int64_t)(g.ny / 4) * g.nx * (g.nz / 4);
+  int64_t b = (items + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;
   if (b < 1) b = 1;
   netd::k_pc_prolong<<<(unsigned)b, 256, 0, s>>>(g, c, pc->w->out, pc->scal, r32, iv32, q32,
@@ -894,6 +919,7 @@ int sbm_net_create(uint64_t seed, sbm_net** out) {
       cudaMalloc(&n->w32, sizeof(float) * P) || cudaMalloc(&n->m, sizeof(float) * P) ||
       cudaMalloc(&n->v, sizeof(float) * P) || cudaMalloc(&n->grad, sizeof(float) * P) ||
       cudaMalloc(&n->wimg, sizeof(bf16) * P) || cudaMalloc(&n->wtimg, sizeof(bf16) * P) ||
+      cudaMalloc(&n->wimg16, sizeof(bf16) * P) || cudaMalloc(&n->wtimg16, sizeof(bf16) * P) ||
       cudaMalloc(&n->err, sizeof(int)) || cudaMalloc(&n->loss, sizeof(double))) {
     sbm_net_destroy(n);
     return SBM_ERR_NOMEM;
@@ -923,7 +949,8 @@ int sbm_net_destroy(sbm_net* n) {
   if (!n) return SBM_ERR_ARG;
   if (n->stream) cudaStreamSynchronize(n->stream);
   for (auto& kv : n->works) delete kv.second;
-  void* p[] = {n->w32, n->m, n->v, n->grad, n->wimg, n->wtimg, n->err, n->loss};
+  void* p[] = {n->w32, n->m, n->v, n->grad, n->wimg, n->wtimg, n->wimg16, n->wtimg16,
+               n->err, n->loss};
   for (void* q : p) cudaFree(q);
   if (n->stream) cudaStreamDestroy(n->stream);
   delete n;
@@ -958,7 +985,7 @@ int sbm_net_forward(sbm_net* n, int ny, int nx, int nz, int nb, const float* in,
   Work* w = work_for(n, ny, nx, nz, nb, false);
   if (!w) return SBM_ERR_NOMEM;
   const int64_t V = w->d[0].v();
-  int rc = upload_bf16(w->in0, in, V * kFeat, n->stream);
+  int rc = upload_features(w->in0, in, V, 1, n->stream);
   if (rc) return rc;
   if ((rc = forward(n, *w, false, nullptr, n->stream))) return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(out, w->out, sizeof(float) * V, cudaMemcpyDeviceToHost, n->stream));
@@ -972,7 +999,7 @@ int sbm_net_loss_grad(sbm_net* n, int ny, int nx, int nz, int nb, const float* i
   if (!w) return SBM_ERR_NOMEM;
   cudaStream_t s = n->stream;
   const int64_t V = w->d[0].v();
-  int rc = upload_bf16(w->in0, in, V * kFeat, s);
+  int rc = upload_features(w->in0, in, V, 1, s);
   if (rc) return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(w->tgt, target, sizeof(float) * V, cudaMemcpyHostToDevice, s));
   SBM_CUDA_TRY(cudaMemsetAsync(n->loss, 0, sizeof(double), s));
@@ -1009,7 +1036,7 @@ int sbm_net_train(sbm_net* n, int ny, int nx, int nz, int nsamples, const float*
   if (cudaMalloc(&din, sizeof(bf16) * Vs * kFeat * nsamples) ||
       cudaMalloc(&dt, sizeof(float) * Vs * nsamples) || cudaMalloc(&hist, sizeof(float) * steps))
     return fail(SBM_ERR_NOMEM);
-  int rc = upload_bf16(din, in, Vs * kFeat * nsamples, s);
+  int rc = upload_features(din, in, Vs, nsamples, s);
   if (rc) return fail(rc);
   if (cudaMemcpyAsync(dt, target, sizeof(float) * Vs * nsamples, cudaMemcpyHostToDevice, s) ||
       cudaMemsetAsync(n->loss, 0, sizeof(double), s))
@@ -1019,8 +1046,11 @@ int sbm_net_train(sbm_net* n, int ny, int nx, int nz, int nsamples, const float*
   for (int it = 0; it < steps; ++it) {
     for (int b = 0; b < batch; ++b) {
       const int64_t q = (int64_t)(splitmix(&st) % (uint64_t)nsamples);
-      if (cudaMemcpyAsync(w->in0 + b * Vs * kFeat, din + q * Vs * kFeat, sizeof(bf16) * Vs * kFeat,
-                          cudaMemcpyDeviceToDevice, s) ||
+      const int64_t V = Vs * batch;
+      if (cudaMemcpyAsync(w->in0 + act_index(b * Vs, 0, V), din + q * Vs * kFeat,
+                          sizeof(bf16) * Vs * 8, cudaMemcpyDeviceToDevice, s) ||
+          cudaMemcpyAsync(w->in0 + act_index(b * Vs, 8, V), din + q * Vs * kFeat + Vs * 8,
+                          sizeof(bf16) * Vs * 8, cudaMemcpyDeviceToDevice, s) ||
           cudaMemcpyAsync(w->tgt + b * Vs, dt + q * Vs, sizeof(float) * Vs,
                           cudaMemcpyDeviceToDevice, s))
         return fail(SBM_ERR_CUDA);

@@ -24,6 +24,11 @@ int net_pc_begin(sbm_ctx* ctx, const float* hk32, double scale, int bcx0, int bc
 float* net_pc_zbuf(sbm_ctx* ctx);
 void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const float* q32,
                    double* partials, CgState* st, cudaStream_t s);
+// Coarse residual R r and the scalars (s, 1/s, ...) the preconditioner reads;
+// the flexible-CG update kernel fills them (and marks them valid in
+// CgState.aux[1]).
+float* net_pc_rc(sbm_ctx* ctx);
+float* net_pc_scal(sbm_ctx* ctx);
 // Kernel launches of one net_pc_launch.
 int net_pc_nodes();
 

@@ -21,6 +21,7 @@
 //         reduction) with FP64 iterative refinement by reliable updates: the
 //         residual is periodically recomputed in FP64 and the correction
 //         accumulated in FP64, without restarting the Krylov space.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -784,6 +785,84 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Update of the flexible CG with the learned preconditioner, walked by
+// 4x4x4 blocks: x32 += alpha p (folding into d64 after a reliable update),
+// r32 -= alpha q, r.r, and the block means rc = R r of the new residual with
+// their sum of squares, so the preconditioner needs no separate
+// restriction pass: the last block stores s = RMS(rc), 1/s and marks rc
+// valid (aux[1]; a residual replacement clears it).  Rows of the block are
+// float4 loads, consecutive threads take consecutive blocks along y.
+__global__ void __launch_bounds__(256)
+    k32_update_fcg(Geo g, Geo g64, float* __restrict__ x, const float* __restrict__ p,
+                   float* __restrict__ r, const float* __restrict__ q, double* __restrict__ d64,
+                   float* __restrict__ rc, float* __restrict__ scal, double* partials,
+                   CgState* st) {
+  if (st->done) return;
+  const bool fold = st->accum_pending != 0;
+  const float alpha = (float)st->alpha;
+  const int cny = g.ny / 4, cnx = g.nx / 4;
+  const int64_t ncell = (int64_t)cny * cnx * (g.nz / 4);
+  float a_rr = 0.f;
+  double a_rc = 0.0;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < ncell;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int ic = (int)(u % cny);
+    const int64_t rr = u / cny;
+    const int jc = (int)(rr % cnx), kc = (int)(rr / cnx);
+    const int i = 4 * ic + 1;
+    float sum = 0.f;
+#pragma unroll 4
+    for (int q16 = 0; q16 < 16; ++q16) {
+      const int j = 4 * jc + 1 + (q16 & 3), k = 4 * kc + 1 + (q16 >> 2);
+      const int64_t c = g.ix(i, j, k);
+      float4 xv = ld4(x + c);
+      const float4 pv = ld4(p + c), qv = ld4(q + c);
+      float4 rv = ld4(r + c);
+      if (fold) {
+        const int64_t c64 = g64.ix(i, j, k);
+        d64[c64] += (double)xv.x;
+        d64[c64 + 1] += (double)xv.y;
+        d64[c64 + 2] += (double)xv.z;
+        d64[c64 + 3] += (double)xv.w;
+        xv = make_float4(alpha * pv.x, alpha * pv.y, alpha * pv.z, alpha * pv.w);
+      } else {
+        xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+      }
+      rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
+      st4(x + c, xv);
+      st4(r + c, rv);
+      a_rr += (rv.x * rv.x + rv.y * rv.y) + (rv.z * rv.z + rv.w * rv.w);
+      sum += (rv.x + rv.y) + (rv.z + rv.w);
+    }
+    const float m = sum * (1.f / 64.f);
+    rc[u] = m;
+    a_rc += (double)m * (double)m;
+  }
+  double v[2] = {(double)a_rr, a_rc}, tot[2];
+  if (grid_reduce<2>(v, partials, &st->counter[1], tot)) {
+    if (threadIdx.x == 0) {
+      const double rr_new = tot[0];
+      const int it = st->iter + 1;
+      st->iter = it;
+      st->accum_pending = 0;
+      const double sc = sqrt(tot[1] / (double)ncell);
+      scal[0] = (float)sc;
+      scal[1] = sc > 0.0 ? (float)(1.0 / sc) : 0.f;
+      st->aux[1] = 1.0;
+      if (!isfinite(rr_new) || !isfinite(st->alpha)) {
+        st->done = 3;
+      } else {
+        const double maxrr = fmax(st->maxrr, rr_new);
+        if ((rr_new < st->delta2 * maxrr) || (rr_new <= st->tol * st->tol * st->aux[0]) ||
+            (it >= st->max_it))
+          st->reliable = 1;
+        st->rr = rr_new;
+        st->maxrr = maxrr;
+      }
+    }
+  }
+}
+
 // Reliable update: r = r0 - A_h (d64 + x32) in FP64 (ghost rules of the
 // search direction on the correction), r32 = (float) r, z = invd*r32;
 // convergence on the FP64 norm, new rho / beta.  No-op unless flagged.
@@ -835,6 +914,7 @@ __global__ void __launch_bounds__(BX* BY)
       else if (!(rms > st->tol)) st->done = 1;
       else if (st->iter >= st->max_it) st->done = 2;
       if (st->initial) st->aux[0] = tot[1];
+      st->aux[1] = 0.0;  // the coarse residual of the learned preconditioner is stale
       if (!FLEX) {
         st->beta = st->initial ? 0.0 : tot[2] / st->rho;
         st->rho = tot[2];
@@ -960,6 +1040,8 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   SBM_LAUNCHED(1);
   const int64_t items = (int64_t)nchunk * g.nx * g.nz;
   const dim3 fgrid(flat_blocks(items));
+  // the learned path's update: one thread per 4x4x4 block
+  const dim3 cgrid((unsigned)std::min<int64_t>(std::max<int64_t>(items / 16 / 256, 1), 152 * 8));
   const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
   float* const pbuf[2] = {p32, ctx->rold32 + kOff32};  // alternating direction buffers
   auto rel = [&](cudaStream_t s2) {
@@ -1012,8 +1094,9 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   k32_update<P, V><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, x32, out, r32, q32, iv32, ctx->d64, \
                                           ctx->partials, ctx->st)
     if (learned) {
-      k32_update<false, 4, true><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, x32, out, r32, q32, iv32,
-                                                        ctx->d64, ctx->partials, ctx->st);
+      k32_update_fcg<<<cgrid, 256, 0, s2>>>(g32, g, x32, out, r32, q32, ctx->d64,
+                                                             net_pc_rc(ctx), net_pc_scal(ctx),
+                                                             ctx->partials, ctx->st);
     } else if (vec == 4) {
       if (pc) SBM_UP(true, 4); else SBM_UP(false, 4);
     } else {

@@ -163,8 +163,8 @@ def load(path=None) -> "sbm.Net":
 
 # ------------------------------------------------------------- training
 
-def train(sizes=((64, 48), (128, 24)), steps=(1500, 800), batch=(8, 2), lr=(2e-3, 5e-4),
-          seed: int = 0, verbose: bool = True):
+def train(sizes=((64, 48), (128, 48), (256, 12)), steps=(1500, 3000, 1500), batch=(8, 4, 1),
+          lr=(2e-3, 1e-3, 5e-4), seed: int = 0, verbose: bool = True):
     """Training recipe of the stored weights: for each (n, structures) stage
     build pairs at n^3 (coarse n/4) and run Adam on the GPU; k_out from the
     first stage's targets.  Returns (net, info)."""

@@ -1,0 +1,81 @@
+"""CPU checks of the learned preconditioner's oracle and host logic: the
+NumPy backward pass against central finite differences (float64, no
+rounding), the product's feature computation against the oracle's, the
+prolongation's exactness on constant / linear fields, the parameter layout
+shared with the CUDA library, and the stored weights file."""
+import numpy as np
+import pytest
+
+from oracle import net_oracle as no
+from elsim_gb300 import learned
+
+
+def _params(seed, bias=0.1):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(no.NPARAM)
+    for l in range(10):
+        taps = 1 if l == no.OUT else 27
+        n = no.CO[l] * taps * no.CI[l]
+        p[no.OFF[l]:no.OFF[l] + n] = rng.normal(size=n) * np.sqrt(2.0 / (taps * no.CI[l]))
+        p[no.BOFF[l]:no.BOFF[l] + no.CO[l]] = rng.normal(size=no.CO[l]) * bias
+    return p
+
+
+def test_oracle_backward_matches_finite_differences():
+    rng = np.random.default_rng(3)
+    p = _params(1)
+    x = rng.normal(size=(1, 16, 16, 16, 16))
+    t = rng.normal(size=(1, 16, 16, 16))
+    _, g = no.loss_grad(p, x, t, rounding=False)
+    errs = []
+    for l in range(10):
+        for i in rng.integers(no.OFF[l], no.BOFF[l] + no.CO[l], size=2):
+            e = 1e-5 * max(1.0, abs(p[i]))
+            pp = p.copy()
+            pp[i] += e
+            lp = ((no.forward(pp, x, False)[0] - t) ** 2).mean()
+            pp[i] -= 2 * e
+            lm = ((no.forward(pp, x, False)[0] - t) ** 2).mean()
+            fd = (lp - lm) / (2 * e)
+            errs.append(abs(fd - g[i]) / max(abs(g[i]), 1e-6))
+    assert max(errs) < 1e-4
+
+
+def test_features_match_oracle():
+    rng = np.random.default_rng(4)
+    r = rng.normal(size=(32, 16, 24))
+    k = rng.uniform(0.1, 1.0, size=(32, 16, 24))
+    f1, s1, c1 = learned.features(r, k, 1, 0)
+    f2, s2, c2 = no.features(r, k, 1, 0)
+    assert f1.shape == (8 * 4 * 6, 16)
+    np.testing.assert_allclose(f1, f2.reshape(-1, 16), rtol=1e-6, atol=1e-6)
+    assert s1 == pytest.approx(s2) and c1 == pytest.approx(c2)
+    assert f1[:, 3].sum() == 8 * 6 and f1[:, 4].sum() == 0  # x0 face only
+
+
+def test_target_is_restricted_scaled_error():
+    rng = np.random.default_rng(5)
+    e = rng.normal(size=(16, 16, 16))
+    t = learned.target(e, s=2.0, cref=0.5, scale=3.0, kout=4.0)
+    ref = no.restrict(e) * 3.0 * 0.5 / (2.0 * 4.0)
+    np.testing.assert_allclose(t, np.transpose(ref, (2, 1, 0)).ravel(), rtol=1e-6)
+
+
+def test_prolongation_exact_on_constants_and_interior_linear():
+    assert np.abs(no.prolong(np.full((4, 5, 6), 2.5)) - 2.5).max() == 0.0
+    c = np.arange(8, dtype=float)[:, None, None] * np.ones((8, 3, 3))
+    f = no.prolong(c)
+    pos = (np.arange(32) + 0.5) / 4 - 0.5
+    np.testing.assert_allclose(f[2:-2, 1, 1], pos[2:-2], atol=1e-12)
+    assert f[0, 0, 0] == 0.0 and f[-1, 0, 0] == 7.0  # clamped at the faces
+
+
+def test_parameter_layout_matches_library(built):
+    from elsim_gb300 import sbm
+    assert sbm.Net.param_count() == no.NPARAM
+
+
+def test_stored_weights():
+    z = np.load(learned.WEIGHTS)
+    assert z["params"].dtype == np.float32 and z["params"].size == no.NPARAM
+    assert np.isfinite(z["params"]).all() and float(z["out_scale"]) > 0
