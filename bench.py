@@ -9,12 +9,15 @@ Node conductivity psi*1 + (1-psi)*0.1, Dirichlet phi = 0 / 1 on the two x
 ghost planes, Neumann elsewhere, zero right-hand side; solved until
 ||r||/||r0|| <= 1e-8 (r recomputed in FP64).
 
-Our arm (default): the production solver -- FP32 CG with Jacobi
-preconditioning and FP64 reliable-update refinement -- with fields resident
-in HBM; `value` is the mean device time of one solve (CUDA events on the
-solver stream), `e2e` the same solve through the C-ABI from pinned host
-buffers (coef/x/rhs uploaded, x downloaded) timed on the wall clock.  The
-plain FP64 CG (the drop-in) is timed beside it for the speed-up.
+Our arm (default): the production solver -- FP32 flexible CG with the
+learned coarse-grid preconditioner (a 3D U-Net on the 4x-coarsened grid,
+BF16 tcgen05 convolutions, weights elsim_gb300/weights/pc_unet.npz) and FP64
+reliable-update refinement -- with fields resident in HBM; `value` is the
+mean device time of one solve (CUDA events on the solver stream), `e2e` the
+same solve through the C-ABI from pinned host buffers (coef/x/rhs uploaded,
+x downloaded) timed on the wall clock.  The plain FP64 CG (the drop-in) and
+the FP32 Jacobi-PCG are timed beside it (`--pc jacobi` makes Jacobi-PCG the
+headline).
 
 --impl reference: the reference's algorithm (plain FP64 CG, its own
 restatement in C with OpenMP -- the Fortran reference has no compiler here)
@@ -46,6 +49,10 @@ TOL = 1e-8
 # FP64 CG in C) and the GPU FP64 CG both stop at 2038.
 FP64_ITERS = 2038
 METRIC = "sbm_potential_solve_time_256^3_relres_1e-8"
+# dram__bytes_read.sum + dram__bytes_write.sum of one k32t_apply_dir launch
+# at 256^3 (ncu): with the Jacobi read (Jacobi-PCG) and without it (flexible
+# CG with the learned preconditioner).
+APPLY_TRAFFIC = {1: 398.2e6, 2: None}
 UNIT = "s"
 
 
@@ -56,6 +63,8 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N)
+    ap.add_argument("--pc", default="learned", choices=["learned", "jacobi"],
+                    help="preconditioner of the headline solve")
     ap.add_argument("--workload", default="solve256", choices=["solve256", "batch96", "profile"],
                     help="solve256: the headline 256^3 solve; batch96: 96 uneven sub-volumes; "
                          "profile: only the production solve, for ncu captures")
@@ -232,13 +241,22 @@ def run_ours(args):
                             tol=TOL, max_it=200000, stop_rule=sbm.STOP_REL_RES, precision=prec,
                             precond=pc)
 
+    head_pc = sbm.PC_LEARNED if args.pc == "learned" else sbm.PC_JACOBI
+    if head_pc == sbm.PC_LEARNED:
+        from elsim_gb300 import learned
+        net = learned.load()
+        ctx.set_net(net)
     # the drop-in: plain FP64 CG (reference algorithm on the GPU)
     fp64 = solve(sbm.PREC_FP64, sbm.PC_NONE)
     x64 = ctx.download("x")[1:-1, 1:-1, 1:-1].copy()
     fp64_ms = ctx.bench_kernel(2, 10)
     plain = solve(sbm.PREC_MIXED, sbm.PC_NONE)
+    # Jacobi-PCG beside the headline (same timing protocol)
+    jac = [solve(sbm.PREC_MIXED, sbm.PC_JACOBI) for _ in range(max(1, args.warmup))]
+    jac = [solve(sbm.PREC_MIXED, sbm.PC_JACOBI) for _ in range(max(1, args.steps))]
+    jac_s = statistics.mean(r["ms"] for r in jac) / 1e3
     for _ in range(args.warmup):
-        solve(sbm.PREC_MIXED, sbm.PC_JACOBI)
+        solve(sbm.PREC_MIXED, head_pc)
     # timed region: K solves, each timed on the device with CUDA events on the
     # solver stream (x reset and L2 flush happen between solves, untimed)
     clocks = Clocks()
@@ -248,12 +266,13 @@ def run_ours(args):
     t0 = time.perf_counter()
     times = []
     for _ in range(args.steps):
-        info = solve(sbm.PREC_MIXED, sbm.PC_JACOBI)
+        info = solve(sbm.PREC_MIXED, head_pc)
         times.append(info["ms"] / 1e3)
     barrier()
     wall = time.perf_counter() - t0
     launches = sbm.launch_count() - l0
     clk = clocks.stop()
+    used_pc = ctx.last_precond()
     xm = ctx.download("x")[1:-1, 1:-1, 1:-1]
     rel_err = float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))
     t_local = max(times)
@@ -262,7 +281,8 @@ def run_ours(args):
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_local = float(tt.item())
     value = statistics.mean(times) if ws == 1 else t_local
-    # roofline of the dominant kernel (fused direction + stencil), timed live
+    # roofline of the dominant kernel (the fused direction + stencil kernel of
+    # the headline solve's inner loop), timed live on the solver stream
     ms_k, bytes_k = ctx.bench_kernel(0, 20)
     ms_u, bytes_u = ctx.bench_kernel(1, 20)
     peak, peak_kind = _peaks()
@@ -284,7 +304,7 @@ def run_ours(args):
             ctx.upload(k, pin[k][1])
         ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO, scale=1.0, tol=TOL,
                      max_it=200000, stop_rule=sbm.STOP_REL_RES, precision=sbm.PREC_MIXED,
-                     precond=sbm.PC_JACOBI)
+                     precond=head_pc)
         xo = np.ndarray(hshape, dtype=np.float64, buffer=xout_t.numpy(), order="F")
         lib = sbm.load_library()
         rc = lib.sbm_download(ctx._h, sbm.F_X, xo.ctypes.data_as(sbm.C.POINTER(sbm.C.c_double)), 1)
@@ -302,16 +322,23 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" + ("+bf16" if used_pc == sbm.PC_LEARNED else ""),
             "data": "synthetic (seeded spheres + tunnel; reference inputs are not public)",
             "config": _config(n, {
-                "method": "FP32 Jacobi-PCG, FP64 reliable-update refinement",
+                "method": ("FP32 flexible CG, learned U-Net coarse-grid preconditioner (BF16 "
+                           "tcgen05), FP64 reliable-update refinement"
+                           if used_pc == sbm.PC_LEARNED else
+                           "FP32 Jacobi-PCG, FP64 reliable-update refinement"),
+                "preconditioner": {0: "none", 1: "jacobi", 2: "learned"}.get(used_pc, "?"),
                 "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                 "iterations": info["iters"],
                 "relL2_vs_fp64_cg": rel_err,
                 "fp64_cg_s": fp64["ms"] / 1e3, "fp64_cg_iterations": fp64["iters"],
                 "mixed_no_pc_s": plain["ms"] / 1e3, "mixed_no_pc_iterations": plain["iters"],
+                "jacobi_pcg_s": jac_s, "jacobi_pcg_iterations": jac[-1]["iters"],
                 "speedup_vs_fp64_cg": fp64["ms"] / 1e3 / value,
+                "speedup_vs_jacobi_pcg": jac_s / value,
                 "voxel_updates_per_s": n ** 3 * info["iters"] / value,
                 "wall_s_timed_region": wall,
                 "update_kernel": {"ms": ms_u, "GB/s": bytes_u / (ms_u * 1e-3) / 1e9},
@@ -319,10 +346,12 @@ def run_ours(args):
                                         "GB/s": fp64_ms[1] / (fp64_ms[0] * 1e-3) / 1e9,
                                         "bound": "fp64 alu"},
             }),
-            "roofline": {"bound": "hbm", "kernel": "k32t_apply_dir (TMA-staged FP32 direction+stencil)",
+            "roofline": {"bound": "hbm", "kernel": "k32t_apply_dir (TMA-staged FP32 direction+stencil)"
+                                                    + (", no Jacobi read (flexible CG)" if used_pc == sbm.PC_LEARNED else ""),
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": 398.2e6,  # DRAM read+write of one launch (ncu)
+                         # DRAM read+write of one launch (ncu capture of the same variant)
+                         "traffic": APPLY_TRAFFIC.get(used_pc),
                          "algorithmic_bytes": bytes_k, "ms": ms_k},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": 3 * nh * 8,
@@ -422,14 +451,19 @@ def run_profile(args):
     n = args.size
     m = synth.microstructure((n, n, n), seed=SEED, tunnel=True)
     prob = synth.potential_problem(m["psi"])
+    pc = sbm.PC_LEARNED if args.pc == "learned" else sbm.PC_JACOBI
     with sbm.Context(n, n, n) as ctx:
         for k in ("coef", "x", "rhs", "weight"):
             ctx.upload(k, prob[k])
+        if pc == sbm.PC_LEARNED:
+            from elsim_gb300 import learned
+            net = learned.load()
+            ctx.set_net(net)
         for _ in range(args.warmup + args.steps):
             ctx.upload("x", prob["x"])
             info = ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO,
                                 scale=1.0, tol=TOL, max_it=200000, stop_rule=sbm.STOP_REL_RES,
-                                precision=sbm.PREC_MIXED, precond=sbm.PC_JACOBI)
+                                precision=sbm.PREC_MIXED, precond=pc)
         print(json.dumps({"workload": "profile", "n": n, **info}))
     return 0
 

@@ -28,6 +28,7 @@
 #include <cuda_bf16.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -1066,6 +1067,43 @@ int sbm_net_train(sbm_net* n, int ny, int nx, int nz, int nsamples, const float*
     return fail(SBM_ERR_CUDA);
   if ((rc = check_err(n))) return fail(rc);
   return fail(SBM_OK);
+}
+
+// Weights file: 8-byte magic "SBMNET01", int64 parameter count, float64
+// output scale k_out, then the FP32 parameters (little-endian).
+int sbm_net_load(const char* path, sbm_net** out, double* out_scale) {
+  if (!path || !out || !out_scale) return SBM_ERR_ARG;
+  *out = nullptr;
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    set_error_msg("cannot open the weights file");
+    return SBM_ERR_ARG;
+  }
+  char magic[8];
+  int64_t count = 0;
+  double scale = 0.0;
+  std::vector<float> h;
+  bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "SBMNET01", 8) == 0 &&
+            fread(&count, sizeof(count), 1, f) == 1 && count == kL.total &&
+            fread(&scale, sizeof(scale), 1, f) == 1 && scale > 0.0;
+  if (ok) {
+    h.resize((size_t)count);
+    ok = fread(h.data(), sizeof(float), (size_t)count, f) == (size_t)count;
+  }
+  fclose(f);
+  if (!ok) {
+    set_error_msg("not a weights file of this network");
+    return SBM_ERR_ARG;
+  }
+  int rc = sbm_net_create(0, out);
+  if (rc) return rc;
+  if ((rc = sbm_net_set_params(*out, h.data(), count))) {
+    sbm_net_destroy(*out);
+    *out = nullptr;
+    return rc;
+  }
+  *out_scale = scale;
+  return SBM_OK;
 }
 
 int sbm_ctx_set_net(sbm_ctx* ctx, sbm_net* n, double out_scale) {

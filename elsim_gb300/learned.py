@@ -15,8 +15,10 @@ from the library's own mixed-precision solver on seeded synthetic
 microstructures (``synth.microstructure``) and right-hand sides of several
 spectra; training runs on the GPU (``Net.train``).
 
-``python -m elsim_gb300.learned --out FILE`` reproduces the stored weights
-``elsim_gb300/weights/pc_unet.npz``.
+``python -m elsim_gb300.learned --out FILE`` reruns the recipe of the stored
+weights ``elsim_gb300/weights/pc_unet.bin`` (recorded in pc_unet.json; the
+reductions of the training kernels use atomics, so a rerun gives weights of
+the same quality, not the same bits).
 """
 from __future__ import annotations
 
@@ -28,7 +30,8 @@ import numpy as np
 
 from . import sbm, synth
 
-WEIGHTS = Path(__file__).resolve().parent / "weights" / "pc_unet.npz"
+WEIGHTS = Path(__file__).resolve().parent / "weights" / "pc_unet.bin"
+MAGIC = b"SBMNET01"
 NFEAT = 16
 
 
@@ -149,21 +152,44 @@ def to_targets(errs, kout: float) -> np.ndarray:
 # ------------------------------------------------------------- weights
 
 def save(path, net: "sbm.Net", info: dict) -> None:
+    """Weights file (the format sbm_net_load reads: magic, int64 count,
+    float64 k_out, FP32 parameters) and a JSON record of the recipe beside
+    it."""
+    import json
     path = Path(path)
     path.parent.mkdir(parents=True, exist_ok=True)
-    np.savez_compressed(path, params=net.params(), out_scale=np.float64(net.out_scale),
-                        **{k: np.asarray(v) for k, v in info.items()})
+    p = net.params().astype("<f4")
+    with open(path, "wb") as f:
+        f.write(MAGIC)
+        f.write(np.int64(p.size).astype("<i8").tobytes())
+        f.write(np.float64(net.out_scale).astype("<f8").tobytes())
+        f.write(p.tobytes())
+    rec = {k: (np.asarray(v).tolist()) for k, v in info.items() if k != "loss"}
+    loss = np.asarray(info.get("loss", []), dtype=float)
+    if loss.size:
+        rec["loss_first_last"] = [float(loss[:20].mean()), float(loss[-20:].mean())]
+    path.with_suffix(".json").write_text(json.dumps(rec, indent=1) + "\n")
+
+
+def read(path=None):
+    """(parameters, k_out) of a weights file."""
+    raw = Path(path or WEIGHTS).read_bytes()
+    if raw[:8] != MAGIC:
+        raise ValueError("not a weights file of the learned preconditioner")
+    n = int(np.frombuffer(raw[8:16], "<i8")[0])
+    kout = float(np.frombuffer(raw[16:24], "<f8")[0])
+    return np.frombuffer(raw[24:24 + 4 * n], "<f4").copy(), kout
 
 
 def load(path=None) -> "sbm.Net":
     """The stored network (default: the weights shipped with the package)."""
-    z = np.load(Path(path) if path else WEIGHTS)
-    return sbm.Net(params=z["params"], out_scale=float(z["out_scale"]))
+    p, kout = read(path)
+    return sbm.Net(params=p, out_scale=kout)
 
 
 # ------------------------------------------------------------- training
 
-def train(sizes=((64, 48), (128, 48), (256, 12)), steps=(1500, 3000, 1500), batch=(8, 4, 1),
+def train(sizes=((64, 48), (128, 96), (256, 32)), steps=(1500, 6000, 4000), batch=(8, 4, 2),
           lr=(2e-3, 1e-3, 5e-4), seed: int = 0, verbose: bool = True):
     """Training recipe of the stored weights: for each (n, structures) stage
     build pairs at n^3 (coarse n/4) and run Adam on the GPU; k_out from the

@@ -156,6 +156,7 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_net_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int,
                                     C.c_int, C.c_float, C.c_uint64, fp]),
         "sbm_ctx_set_net": (C.c_int, [vp, vp, C.c_double]),
+        "sbm_net_load": (C.c_int, [C.c_char_p, C.POINTER(vp), dp]),
         "sbm_ctx_last_precond": (C.c_int, [vp]),
         "sbm_learned_pc_apply": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp, dp]),
     }

@@ -14,7 +14,7 @@ MODULE sbm_capi
   INTEGER(C_INT), PARAMETER :: SBM_OP_CNE = 0, SBM_OP_PHP = 1, SBM_OP_PHE = 2, SBM_OP_GENERIC = 3
   INTEGER(C_INT), PARAMETER :: SBM_STOP_REF_UPDATE = 0, SBM_STOP_REF_RESID = 1, SBM_STOP_REL_RES = 2
   INTEGER(C_INT), PARAMETER :: SBM_PREC_FP64 = 0, SBM_PREC_MIXED = 1
-  INTEGER(C_INT), PARAMETER :: SBM_PC_NONE = 0, SBM_PC_JACOBI = 1
+  INTEGER(C_INT), PARAMETER :: SBM_PC_NONE = 0, SBM_PC_JACOBI = 1, SBM_PC_LEARNED = 2
   INTEGER(C_INT), PARAMETER :: SBM_F_PSP = 0, SBM_F_PSE = 1, SBM_F_AVP = 2, SBM_F_AVPX = 3, &
        SBM_F_CNP = 4, SBM_F_CNE = 5, SBM_F_PHP = 6, SBM_F_PHE = 7, SBM_F_RXN = 8, &
        SBM_F_COEF = 9, SBM_F_RHS = 10, SBM_F_X = 11, SBM_F_WEIGHT = 12
@@ -116,6 +116,26 @@ MODULE sbm_capi
       INTEGER(C_INT64_T), VALUE :: n
       REAL(C_DOUBLE), INTENT(IN) :: psA(*), cn(*)
       REAL(C_DOUBLE), INTENT(OUT) :: psB(*)
+    END FUNCTION
+    ! learned coarse-grid preconditioner (SBM_PC_LEARNED with SBM_PREC_MIXED)
+    INTEGER(C_INT) FUNCTION sbm_net_load(path, net, out_scale) BIND(C, NAME='sbm_net_load')
+      IMPORT :: C_INT, C_PTR, C_CHAR, C_DOUBLE
+      CHARACTER(KIND=C_CHAR), INTENT(IN) :: path(*)   ! NUL-terminated
+      TYPE(C_PTR), INTENT(OUT) :: net
+      REAL(C_DOUBLE), INTENT(OUT) :: out_scale
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_net_destroy(net) BIND(C, NAME='sbm_net_destroy')
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: net
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_ctx_set_net(ctx, net, out_scale) BIND(C, NAME='sbm_ctx_set_net')
+      IMPORT :: C_INT, C_PTR, C_DOUBLE
+      TYPE(C_PTR), VALUE :: ctx, net
+      REAL(C_DOUBLE), VALUE :: out_scale
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_ctx_last_precond(ctx) BIND(C, NAME='sbm_ctx_last_precond')
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: ctx
     END FUNCTION
   END INTERFACE
 END MODULE sbm_capi

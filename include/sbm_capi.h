@@ -320,6 +320,10 @@ int sbm_net_loss_grad(sbm_net* net, int ny, int nx, int nz, int nb, const float*
 int sbm_net_train(sbm_net* net, int ny, int nx, int nz, int nsamples, const float* in,
                   const float* target, int steps, int batch, float lr, uint64_t seed,
                   float* loss_hist);
+/* New network from a weights file (elsim_gb300/weights/pc_unet.bin: magic
+ * "SBMNET01", int64 parameter count, float64 k_out, FP32 parameters);
+ * *out_scale receives k_out for sbm_ctx_set_net. */
+int sbm_net_load(const char* path, sbm_net** out, double* out_scale);
 /* Attach `net` (NULL detaches) to a context with output scale k_out.  The
  * context does not own the network: keep it alive while attached. */
 int sbm_ctx_set_net(sbm_ctx* ctx, sbm_net* net, double out_scale);

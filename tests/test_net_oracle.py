@@ -76,6 +76,19 @@ def test_parameter_layout_matches_library(built):
 
 
 def test_stored_weights():
-    z = np.load(learned.WEIGHTS)
-    assert z["params"].dtype == np.float32 and z["params"].size == no.NPARAM
-    assert np.isfinite(z["params"]).all() and float(z["out_scale"]) > 0
+    p, kout = learned.read()
+    assert p.dtype == np.float32 and p.size == no.NPARAM
+    assert np.isfinite(p).all() and kout > 0
+
+
+def test_weights_file_round_trip(tmp_path):
+    class _Net:  # what save() reads from a network
+        out_scale = 2.5
+
+        def params(self):
+            return np.arange(no.NPARAM, dtype=np.float32)
+
+    learned.save(tmp_path / "w.bin", _Net(), {"sizes": [[64, 1]], "loss": np.ones(30)})
+    p, kout = learned.read(tmp_path / "w.bin")
+    assert kout == 2.5 and np.array_equal(p, np.arange(no.NPARAM, dtype=np.float32))
+    assert (tmp_path / "w.json").exists()
