@@ -170,20 +170,33 @@ __device__ __forceinline__ void expect_tx(uint64_t* bar, unsigned bytes) {
                : "memory");
 }
 
-// The 27 (x P) tap MMAs of one chunk.  Descriptors advance by constant
-// start-address offsets (the 14-bit start field holds address / 16).
-template <bool FLIP>
+// The tap MMAs of one chunk.  A descriptor = halo plane 0 at offset
+// (0, 0); B descriptor = the chunk's weight image.  Descriptors advance by
+// constant start-address offsets (the 14-bit start field holds address /
+// 16): halo plane h, in-plane offset (dy, dx) at ((h*HX + 1+dx)*HY + 1+dy)
+// units, B block q at 6 nt units and B row r at 2 r units.  One plane: 27
+// MMAs of N = nt.  Two planes (accumulators at columns 0 and nt): per
+// (dy, dx) four MMAs, halo planes 1 and 2 with N = 2 nt feeding both
+// accumulators (rows [W0 | W-1] and [W+1 | W0]), planes 0 and 3 with N = nt.
 __device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t bd, int nt, int P,
-                                           uint32_t id, bool acc) {
+                                           uint32_t id1, uint32_t id2, bool acc) {
 #pragma unroll
-  for (int t = 0; t < 27; ++t) {
-    const int dy = FLIP ? 1 - t % 3 : t % 3 - 1;
-    const int dx = FLIP ? 1 - (t / 3) % 3 : (t / 3) % 3 - 1;
-    const int dz = FLIP ? 1 - t / 9 : t / 9 - 1;
-    const uint64_t b = bd + (uint64_t)(t * nt * 2);
-    const uint64_t a0 = ad + (uint64_t)((((1 + dz) * HX + (1 + dx)) * HY + (1 + dy)));
-    tc_mma(tmem, a0, b, id, (acc || t > 0) ? 1u : 0u);
-    if (P == 2) tc_mma(tmem + (uint32_t)nt, a0 + (uint64_t)(HX * HY), b, id, (acc || t > 0) ? 1u : 0u);
+  for (int qq = 0; qq < 9; ++qq) {
+    const int dy = qq % 3 - 1, dx = qq / 3 - 1;
+    const uint64_t a0 = ad + (uint64_t)((1 + dx) * HY + (1 + dy));
+    const uint64_t b = bd + (uint64_t)(qq * 6 * nt);
+    const uint32_t first = (acc || qq > 0) ? 1u : 0u;
+    if (P == 1) {
+      // plane z0 + dz is halo plane 1 + dz; its weights are rows (1 - dz) nt
+      tc_mma(tmem, a0 + (uint64_t)(1 * HX * HY), b + (uint64_t)(2 * nt), id1, first);  // dz = 0
+      tc_mma(tmem, a0, b + (uint64_t)(4 * nt), id1, 1u);                               // dz = -1
+      tc_mma(tmem, a0 + (uint64_t)(2 * HX * HY), b, id1, 1u);                          // dz = +1
+    } else {
+      tc_mma(tmem, a0 + (uint64_t)(1 * HX * HY), b + (uint64_t)(2 * nt), id2, first);  // h = 1
+      tc_mma(tmem, a0, b + (uint64_t)(4 * nt), id1, 1u);                               // h = 0
+      tc_mma(tmem, a0 + (uint64_t)(2 * HX * HY), b, id2, 1u);                          // h = 2
+      tc_mma(tmem + (uint32_t)nt, a0 + (uint64_t)(3 * HX * HY), b, id1, 1u);           // h = 3
+    }
   }
 }
 
@@ -228,7 +241,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   const uint32_t tmem = *tslot;
   bool ok = true;
   if (tid == 0) {
-    const uint32_t id = idesc_bf16(nt);
+    const uint32_t id = idesc_bf16(nt), id2 = idesc_bf16(2 * nt);
     const __nv_bfloat16* wsrc =
         (a.tw == 16 ? a.wimg16 : a.wimg) + (int64_t)a.tw * blockIdx.y * 27 * a.cin;
     const unsigned abox = (unsigned)(HY * HX * (P + 2) * 16);
@@ -254,10 +267,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
       const uint32_t A = sa(sm + s * stage_bytes);
       const uint64_t ad = umma_desc(A, ahalf, HY * 16);
       const uint64_t bd = umma_desc(A + 2 * ahalf, 128, 256);
-      if (a.flip)
-        issue_taps<true>(tmem, ad, bd, nt, P, id, c > 0);
-      else
-        issue_taps<false>(tmem, ad, bd, nt, P, id, c > 0);
+      issue_taps(tmem, ad, bd, nt, P, id, id2, c > 0);
       tc_commit(&used[s]);
       ++committed[s];
       if (c + nst < nchunk) {
@@ -375,7 +385,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
 // Weight image: destination element (co, t, ci) of the (possibly
 // transposed) convolution from the source layout.
 __global__ void k_wimage(const __nv_bfloat16* __restrict__ w, int cout, int cin, int transpose,
-                         int tw, __nv_bfloat16* __restrict__ img) {
+                         int reverse, int tw, __nv_bfloat16* __restrict__ img) {
   const int64_t n = (int64_t)cout * 27 * cin;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
@@ -383,7 +393,7 @@ __global__ void k_wimage(const __nv_bfloat16* __restrict__ w, int cout, int cin,
     const int t = (int)((q / cin) % 27);
     const int co = (int)(q / ((int64_t)27 * cin));
     const int64_t src = transpose ? ((int64_t)ci * 27 + t) * cout + co : q;
-    img[wimage_index(co, t, ci, cout, cin, tw)] = w[src];
+    img[wimage_index(co, reverse ? 26 - t : t, ci, cout, cin, tw)] = w[src];
   }
 }
 
@@ -612,7 +622,7 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
   a.x = (const __nv_bfloat16*)dx; a.w = (const __nv_bfloat16*)dw;
   a.bias = bias ? (const float*)db : nullptr;
   a.y16 = nullptr; a.y32 = (float*)dy; a.relu = relu; a.flip = flip; a.err = (int*)de;
-  conv3_wimage(a.w, cout, cin, 0, 64, (__nv_bfloat16*)dimg, s);
+  conv3_wimage(a.w, cout, cin, 0, flip, 64, (__nv_bfloat16*)dimg, s);
   a.wimg = (const __nv_bfloat16*)dimg;
   rc = conv3_launch(&a, nullptr, use_tc, s);
   if (rc) {
@@ -669,12 +679,12 @@ int conv3_map(const ConvArgs* pa, ConvMap* m) {
   return SBM_OK;
 }
 
-void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, int tw,
+void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, int reverse, int tw,
                   __nv_bfloat16* img, cudaStream_t s) {
   const int64_t n = (int64_t)cout * 27 * cin;
   int64_t b = (n + 255) / 256;
   if (b > 152 * 16) b = 152 * 16;
-  k_wimage<<<(unsigned)b, 256, 0, s>>>(w, cout, cin, transpose, tw, img);
+  k_wimage<<<(unsigned)b, 256, 0, s>>>(w, cout, cin, transpose, reverse, tw, img);
   SBM_LAUNCHED(1);
 }
 

@@ -38,7 +38,8 @@ struct ConvArgs {
   __nv_bfloat16* y16;      // BF16 output or null
   float* y32;              // FP32 output or null
   int relu;
-  int flip;                // 1: tap t reads neighbour -offset (transposed convolution)
+  int flip;                // 1: tap t reads neighbour -offset (CUDA-core kernel; the
+                           //    tensor-core kernel takes it from a reversed weight image)
   int* err;                // set to 1 if a wait expired
   const int* skip;         // launch is a no-op while *skip != 0 (may be null)
   // tensor-core kernel only:
@@ -81,18 +82,26 @@ int conv3_map(const ConvArgs* a, ConvMap* m);
 // tensor-core kernel from w [cout][27][cin] (transpose = 0), or of the
 // transposed convolution (data gradient) from the layer's weights
 // [cin][27][cout] (transpose = 1, cout/cin are those of the transposed
-// convolution).  img has cout*27*cin elements.
-void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, int tw,
+// convolution); reverse = 1 stores tap t at 26 - t (the flipped taps of
+// the data gradient; the tensor-core kernel itself never flips).  img has
+// cout*27*cin elements.
+void conv3_wimage(const __nv_bfloat16* w, int cout, int cin, int transpose, int reverse, int tw,
                   __nv_bfloat16* img, cudaStream_t s);
 // Index in the weight image of element (co, tap, ci) of a convolution with
-// cout x cin channels: per output tile, per 16-channel input chunk, the
-// chunk's B operands of the 27 taps, each in the canonical K-major layout.
+// cout x cin channels.  Per output tile, per 16-channel input chunk, per
+// in-plane offset (dy, dx): one B operand of 3 nt rows in the canonical
+// K-major layout, rows [W(dz=+1) | W(dz=0) | W(dz=-1)], so that the two
+// middle halo planes of a two-plane tile each feed both accumulators with
+// one MMA of 2 nt columns.
 __host__ __device__ inline int64_t wimage_index(int co, int t, int ci, int cout, int cin, int tw) {
   const int j = co / tw, n = co % tw;
   const int nt = min(tw, cout - tw * j);
   const int c = ci >> 4, kh = (ci >> 3) & 1, e = ci & 7;
+  const int q = t % 9, dz = t / 9 - 1;  // (dy, dx) pair and z offset of tap t
+  const int r = (1 - dz) * nt + n;
   const int64_t byte = (int64_t)tw * j * 27 * cin * 2 + (int64_t)c * 27 * nt * 32 +
-                       (int64_t)t * nt * 32 + (n >> 3) * 256 + kh * 128 + (n & 7) * 16 + e * 2;
+                       (int64_t)q * 3 * nt * 32 + (r >> 3) * 256 + kh * 128 + (r & 7) * 16 +
+                       e * 2;
   return byte / 2;
 }
 // use_tc = 1: tcgen05 kernel (needs a.wimg and a map, encoded here when m

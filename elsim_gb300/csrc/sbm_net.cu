@@ -305,10 +305,11 @@ __global__ void k_adam(int64_t P, int update, float* __restrict__ w, const float
         const int ci = (int)(rel % tab.ci[l]);
         const int tap = (int)((rel / tab.ci[l]) % 27);
         const int co = (int)(rel / ((int64_t)27 * tab.ci[l]));
+        // data gradient: transposed channels and reversed taps
         wimg[tab.off[l] + wimage_index(co, tap, ci, tab.co[l], tab.ci[l], 64)] = b;
-        wtimg[tab.off[l] + wimage_index(ci, tap, co, tab.ci[l], tab.co[l], 64)] = b;
+        wtimg[tab.off[l] + wimage_index(ci, 26 - tap, co, tab.ci[l], tab.co[l], 64)] = b;
         wimg16[tab.off[l] + wimage_index(co, tap, ci, tab.co[l], tab.ci[l], 16)] = b;
-        wtimg16[tab.off[l] + wimage_index(ci, tap, co, tab.ci[l], tab.co[l], 16)] = b;
+        wtimg16[tab.off[l] + wimage_index(ci, 26 - tap, co, tab.ci[l], tab.co[l], 16)] = b;
       }
     }
   }
@@ -345,6 +346,10 @@ struct sbm_net {
   double* loss = nullptr;
   int64_t step = 0;
   cudaStream_t stream = nullptr;
+  // resident training set (sbm_net_set_data)
+  bf16* din = nullptr;     // per-sample channel-group planes
+  float* dt = nullptr;
+  int dny = 0, dnx = 0, dnz = 0, dns = 0;
   std::map<std::tuple<int, int, int, int, int>, Work*> works;
 };
 
@@ -951,7 +956,7 @@ int sbm_net_destroy(sbm_net* n) {
   if (n->stream) cudaStreamSynchronize(n->stream);
   for (auto& kv : n->works) delete kv.second;
   void* p[] = {n->w32, n->m, n->v, n->grad, n->wimg, n->wtimg, n->wimg16, n->wtimg16,
-               n->err, n->loss};
+               n->err, n->loss, n->din, n->dt};
   for (void* q : p) cudaFree(q);
   if (n->stream) cudaStreamDestroy(n->stream);
   delete n;
@@ -1015,44 +1020,61 @@ int sbm_net_loss_grad(sbm_net* n, int ny, int nx, int nz, int nb, const float* i
   return SBM_OK;
 }
 
-int sbm_net_train(sbm_net* n, int ny, int nx, int nz, int nsamples, const float* in,
-                  const float* target, int steps, int batch, float lr, uint64_t seed,
-                  float* loss_hist) {
-  if (!n || !in || !target || nsamples < 1 || steps < 1 || batch < 1 || !(lr > 0.f) ||
-      !dims_ok(ny, nx, nz))
-    return SBM_ERR_ARG;
+int sbm_net_set_data(sbm_net* n, int ny, int nx, int nz, int nsamples, const float* in,
+                     const float* target) {
+  if (!n || !in || !target || nsamples < 1 || !dims_ok(ny, nx, nz)) return SBM_ERR_ARG;
+  cudaStream_t s = n->stream;
+  cudaStreamSynchronize(s);
+  cudaFree(n->din);
+  cudaFree(n->dt);
+  n->din = nullptr;
+  n->dt = nullptr;
+  n->dns = 0;
+  const int64_t Vs = (int64_t)ny * nx * nz;
+  if (cudaMalloc(&n->din, sizeof(bf16) * Vs * kFeat * nsamples) ||
+      cudaMalloc(&n->dt, sizeof(float) * Vs * nsamples))
+    return SBM_ERR_NOMEM;
+  int rc = upload_features(n->din, in, Vs, nsamples, s);
+  if (rc) return rc;
+  SBM_CUDA_TRY(cudaMemcpyAsync(n->dt, target, sizeof(float) * Vs * nsamples,
+                               cudaMemcpyHostToDevice, s));
+  SBM_CUDA_TRY(cudaStreamSynchronize(s));
+  n->dny = ny;
+  n->dnx = nx;
+  n->dnz = nz;
+  n->dns = nsamples;
+  return SBM_OK;
+}
+
+int sbm_net_train_steps(sbm_net* n, int steps, int batch, float lr, uint64_t seed,
+                        float* loss_hist) {
+  if (!n || steps < 1 || batch < 1 || !(lr > 0.f)) return SBM_ERR_ARG;
+  if (!n->dns) return SBM_ERR_STATE;
+  const int ny = n->dny, nx = n->dnx, nz = n->dnz, nsamples = n->dns;
   Work* w = work_for(n, ny, nx, nz, batch, true);
   if (!w) return SBM_ERR_NOMEM;
   cudaStream_t s = n->stream;
   const int64_t Vs = (int64_t)ny * nx * nz;
-  bf16* din = nullptr;
-  float *dt = nullptr, *hist = nullptr;
+  float* hist = nullptr;
+  if (cudaMalloc(&hist, sizeof(float) * steps)) return SBM_ERR_NOMEM;
   auto fail = [&](int code) {
     cudaStreamSynchronize(s);
-    cudaFree(din);
-    cudaFree(dt);
     cudaFree(hist);
     return code;
   };
-  if (cudaMalloc(&din, sizeof(bf16) * Vs * kFeat * nsamples) ||
-      cudaMalloc(&dt, sizeof(float) * Vs * nsamples) || cudaMalloc(&hist, sizeof(float) * steps))
-    return fail(SBM_ERR_NOMEM);
-  int rc = upload_features(din, in, Vs, nsamples, s);
-  if (rc) return fail(rc);
-  if (cudaMemcpyAsync(dt, target, sizeof(float) * Vs * nsamples, cudaMemcpyHostToDevice, s) ||
-      cudaMemsetAsync(n->loss, 0, sizeof(double), s))
-    return fail(SBM_ERR_CUDA);
+  if (cudaMemsetAsync(n->loss, 0, sizeof(double), s)) return fail(SBM_ERR_CUDA);
   uint64_t st = seed * 0x9E3779B97F4A7C15ull + 7;
-  const float inv_v = 1.0f / (float)(Vs * batch);
+  const int64_t V = Vs * batch;
+  const float inv_v = 1.0f / (float)V;
+  int rc;
   for (int it = 0; it < steps; ++it) {
     for (int b = 0; b < batch; ++b) {
       const int64_t q = (int64_t)(splitmix(&st) % (uint64_t)nsamples);
-      const int64_t V = Vs * batch;
-      if (cudaMemcpyAsync(w->in0 + act_index(b * Vs, 0, V), din + q * Vs * kFeat,
+      if (cudaMemcpyAsync(w->in0 + act_index(b * Vs, 0, V), n->din + q * Vs * kFeat,
                           sizeof(bf16) * Vs * 8, cudaMemcpyDeviceToDevice, s) ||
-          cudaMemcpyAsync(w->in0 + act_index(b * Vs, 8, V), din + q * Vs * kFeat + Vs * 8,
+          cudaMemcpyAsync(w->in0 + act_index(b * Vs, 8, V), n->din + q * Vs * kFeat + Vs * 8,
                           sizeof(bf16) * Vs * 8, cudaMemcpyDeviceToDevice, s) ||
-          cudaMemcpyAsync(w->tgt + b * Vs, dt + q * Vs, sizeof(float) * Vs,
+          cudaMemcpyAsync(w->tgt + b * Vs, n->dt + q * Vs, sizeof(float) * Vs,
                           cudaMemcpyDeviceToDevice, s))
         return fail(SBM_ERR_CUDA);
     }
@@ -1067,6 +1089,15 @@ int sbm_net_train(sbm_net* n, int ny, int nx, int nz, int nsamples, const float*
     return fail(SBM_ERR_CUDA);
   if ((rc = check_err(n))) return fail(rc);
   return fail(SBM_OK);
+}
+
+int sbm_net_train(sbm_net* n, int ny, int nx, int nz, int nsamples, const float* in,
+                  const float* target, int steps, int batch, float lr, uint64_t seed,
+                  float* loss_hist) {
+  if (!n || steps < 1 || batch < 1 || !(lr > 0.f)) return SBM_ERR_ARG;
+  int rc = sbm_net_set_data(n, ny, nx, nz, nsamples, in, target);
+  if (rc) return rc;
+  return sbm_net_train_steps(n, steps, batch, lr, seed, loss_hist);
 }
 
 // Weights file: 8-byte magic "SBMNET01", int64 parameter count, float64

@@ -1224,8 +1224,10 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
 //   which 2: the FP64 stencil + dot kernel of the plain CG
 // and reports the algorithmic bytes one launch moves.
 int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double* bytes_per_launch) {
-  if (reps < 1 || which < 0 || which > 2) return SBM_ERR_ARG;
-  if (which < 2 && ctx->last_pc < 0) return SBM_ERR_STATE;
+  if (reps < 1 || which < 0 || which > 4) return SBM_ERR_ARG;
+  if (which != 2 && ctx->last_pc < 0) return SBM_ERR_STATE;
+  if (which >= 3 && (ctx->last_precond != SBM_PC_LEARNED || !net_pc_usable(ctx, 0)))
+    return SBM_ERR_STATE;
   const Geo& g = ctx->g;
   const Geo& g32 = ctx->g32;
   cudaStream_t s = ctx->stream;
@@ -1233,6 +1235,7 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
   CgState* h = &ctx->h_st[3];
   memset(h, 0, sizeof(CgState));
   h->rho = 1.0;
+  h->pq = 1.0;
   h->alpha = 1e-30;
   h->beta = 0.5;
   h->max_it = 1 << 30;
@@ -1280,6 +1283,13 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
         if (op32.form == 0) k32s_apply_dir<0, false><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);
         else k32s_apply_dir<1, false><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, r32, pa, iv, pb, q32, ctx->partials, ctx->st32);
       }
+    } else if (which == 3) {
+      net_pc_launch(ctx, r32, iv, q32, ctx->partials, ctx->st32, s);
+    } else if (which == 4) {
+      const dim3 cgrid((unsigned)std::min<int64_t>(
+          std::max<int64_t>((int64_t)nchunk * g.nx * g.nz / 16 / 256, 1), 152 * 8));
+      k32_update_fcg<<<cgrid, 256, 0, s>>>(g32, g, x32, pb, r32, q32, ctx->d64, net_pc_rc(ctx),
+                                          net_pc_scal(ctx), ctx->partials, ctx->st32);
     } else if (which == 1) {
       if (vec == 4) {
         if (pc) k32_update<true, 4><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);
@@ -1305,6 +1315,8 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
   double words;
   if (which == 0) words = 5.0 + (pc ? 1.0 : 0.0) + (op32.form ? 1.0 : 0.0);  // r,p_old,hk,[invd],[diag] -> p_new,q
   else if (which == 1) words = 6.0 + (pc ? 1.0 : 0.0);                       // x,p,r,q,[invd] -> x,r
+  else if (which == 3) words = 5.0;  // restriction r; prolongation r,invd,q -> z (coarse grid not counted)
+  else if (which == 4) words = 6.0;  // x,p,r,q -> x,r (+ the coarse means)
   else words = 3.0;                                                          // p,hk -> q (FP64)
   if (bytes_per_launch) *bytes_per_launch = words * (which == 2 ? 8.0 : 4.0) * n;
   return SBM_OK;

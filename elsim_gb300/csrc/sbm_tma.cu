@@ -19,6 +19,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "sbm_internal.cuh"
@@ -304,6 +305,36 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
+// z planes per CTA when not tuned: the launch should fill whole waves of
+// resident CTAs (a last, partly filled wave leaves SMs idle), and each CTA
+// also streams 2 halo planes, so minimise waves x (planes + 2) over 8..32.
+int auto_zct(int ntile, int nz, int pc, int form) {
+  int dev = 0, nsm = 152, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = smem_bytes(pc, form);
+  cudaError_t e;
+  if (form == 0)
+    e = pc ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<0, true>, NTH, smem)
+           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<0, false>, NTH, smem);
+  else
+    e = pc ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<1, true>, NTH, smem)
+           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<1, false>, NTH, smem);
+  if (e != cudaSuccess || per_sm < 1) return ZCT;
+  const int64_t cap = (int64_t)nsm * per_sm;
+  int best = ZCT;
+  int64_t best_cost = -1;
+  for (int z = 8; z <= 32; ++z) {
+    const int64_t ctas = (int64_t)ntile * ((nz + z - 1) / z);
+    const int64_t cost = ((ctas + cap - 1) / cap) * (int64_t)(std::min(z, nz) + 2);
+    if (best_cost < 0 || cost < best_cost || (cost == best_cost && z > best)) {
+      best = z;
+      best_cost = cost;
+    }
+  }
+  return best;
+}
+
 // The TMA path needs rows of a multiple of 4 voxels (float4 output) and
 // 16-byte row strides (always true of the FP32 layout).
 bool tma_supported(const Geo& g32) { return (g32.ny % 4) == 0 && (g32.sx % 4) == 0 && encode_fn(); }
@@ -327,7 +358,7 @@ int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, c
   plan->bwd = plan->fwd;
   if (!make_map(&plan->bwd.p, pb, g32)) return SBM_ERR_STATE;
   const int ntile = ((g32.ny + TX - 1) / TX) * ((g32.nx + TY - 1) / TY);
-  if (zct < 1) zct = ZCT;
+  if (zct < 1) zct = auto_zct(ntile, g32.nz, pc, form);
   plan->zct = zct;
   plan->grid = dim3((unsigned)ntile, (unsigned)((g32.nz + zct - 1) / zct));
   plan->pc = pc;

@@ -189,14 +189,55 @@ def load(path=None) -> "sbm.Net":
 
 # ------------------------------------------------------------- training
 
+# Validation structures (edge, seed): used by nothing else (training seeds
+# are seed*1000 + n + k, the tests and the benchmark use their own seeds).
+VALIDATION = ((128, 900001), (256, 900002))
+
+
+def validation_set(cases=VALIDATION):
+    """Contexts of the validation potential solves (tunnelled structures)."""
+    vals = []
+    for n, sd in cases:
+        ms = synth.microstructure((n, n, n), seed=sd, solid_fraction=0.6, tunnel=True)
+        prob = synth.potential_problem(ms["psi"])
+        ctx = sbm.Context(n, n, n)
+        for k in ("coef", "rhs", "weight"):
+            ctx.upload(k, prob[k])
+        vals.append((ctx, prob))
+    return vals
+
+
+def validate(net, vals, cap: int = 2000) -> int:
+    """Total flexible-CG iterations to rel-res 1e-8 over the validation
+    solves with `net` as preconditioner (cap per solve if it fails)."""
+    tot = 0
+    for ctx, prob in vals:
+        if getattr(ctx, "_net", None) is not net:
+            ctx.set_net(net)
+        ctx.upload("x", prob["x"])
+        r = ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO, scale=1.0,
+                         tol=1e-8, max_it=cap, stop_rule=sbm.STOP_REL_RES,
+                         precision=sbm.PREC_MIXED, precond=sbm.PC_LEARNED,
+                         raise_on_maxit=False)
+        tot += r["iters"] if r["status"] == sbm.OK else cap
+    return tot
+
+
 def train(sizes=((64, 48), (128, 96), (256, 32)), steps=(1500, 6000, 4000), batch=(8, 4, 2),
-          lr=(2e-3, 1e-3, 5e-4), seed: int = 0, verbose: bool = True):
+          lr=(2e-3, 1e-3, 5e-4), seed: int = 0, eval_every: int = 500, verbose: bool = True):
     """Training recipe of the stored weights: for each (n, structures) stage
-    build pairs at n^3 (coarse n/4) and run Adam on the GPU; k_out from the
-    first stage's targets.  Returns (net, info)."""
+    build pairs at n^3 (coarse n/4) and run Adam on the GPU (learning rate
+    decayed to 0.3x and 0.1x over the last 40 % and 10 % of the stage); k_out
+    from the first stage's targets.  Every `eval_every` steps the network is
+    scored by the flexible-CG iterations it needs on the validation solves,
+    and the best parameters seen are returned (the MSE of the coarse error is
+    only a proxy for the preconditioner's quality).  Returns (net, info)."""
     net = sbm.Net(seed=seed)
+    vals = validation_set()
     kout = None
-    hist_all = []
+    hist_all, val_hist = [], []
+    best, best_p = None, None
+    calls = 0
     for (n, nseeds), st, b, eta in zip(sizes, steps, batch, lr):
         t0 = time.time()
         seeds = range(seed * 1000 + n, seed * 1000 + n + nseeds)
@@ -204,23 +245,34 @@ def train(sizes=((64, 48), (128, 96), (256, 32)), steps=(1500, 6000, 4000), batc
         if kout is None:
             kout = float(np.sqrt(np.mean(np.concatenate([e.ravel() ** 2 for e in errs]))))
             net.out_scale = kout
-        x = np.concatenate(feats)
-        t = to_targets(errs, kout)
-        dims = (n // 4, n // 4, n // 4)
+        net.set_data(np.concatenate(feats), to_targets(errs, kout), (n // 4, n // 4, n // 4))
+        del feats, errs
         if verbose:
-            print(f"stage n={n}: {len(feats)} pairs in {time.time() - t0:.1f} s", flush=True)
+            print(f"stage n={n}: pairs in {time.time() - t0:.1f} s", flush=True)
         t1 = time.time()
-        # step-decayed learning rate within the stage
         for part, f in ((0.6, 1.0), (0.3, 0.3), (0.1, 0.1)):
-            h = net.train(x, t, dims, steps=max(1, int(st * part)), batch=b, lr=eta * f,
-                          seed=seed + n + int(100 * f))
-            hist_all.append(h)
+            todo = max(1, int(st * part))
+            while todo > 0:
+                k = min(eval_every, todo)
+                calls += 1
+                hist_all.append(net.train_steps(k, b, eta * f, seed=seed * 7919 + calls))
+                todo -= k
+                v = validate(net, vals)
+                val_hist.append(v)
+                if best is None or v < best:
+                    best, best_p = v, net.params().copy()
         if verbose:
             h = np.concatenate(hist_all)
             print(f"  trained {st} steps in {time.time() - t1:.1f} s; loss {h[:20].mean():.4f}"
-                  f" -> {h[-20:].mean():.4f}", flush=True)
+                  f" -> {h[-20:].mean():.4f}; validation iterations {val_hist[-1]}"
+                  f" (best {best})", flush=True)
+    net.set_params(best_p)
+    for ctx, _ in vals:
+        ctx.close()
     info = dict(sizes=np.array(sizes), steps=np.array(steps), batch=np.array(batch),
-                lr=np.array(lr), seed=seed, loss=np.concatenate(hist_all))
+                lr=np.array(lr), seed=seed, eval_every=eval_every,
+                validation=np.array(VALIDATION), validation_iterations=np.array(val_hist),
+                best_validation_iterations=best, loss=np.concatenate(hist_all))
     return net, info
 
 

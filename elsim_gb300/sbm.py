@@ -155,6 +155,8 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_net_loss_grad": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, dp, fp]),
         "sbm_net_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int,
                                     C.c_int, C.c_float, C.c_uint64, fp]),
+        "sbm_net_set_data": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp]),
+        "sbm_net_train_steps": (C.c_int, [vp, C.c_int, C.c_int, C.c_float, C.c_uint64, fp]),
         "sbm_ctx_set_net": (C.c_int, [vp, vp, C.c_double]),
         "sbm_net_load": (C.c_int, [C.c_char_p, C.POINTER(vp), dp]),
         "sbm_ctx_last_precond": (C.c_int, [vp]),
@@ -424,6 +426,22 @@ class Net:
         _check(self.lib.sbm_net_loss_grad(self._h, *dims, nb, _fptr(x), _fptr(t), C.byref(loss),
                                           _fptr(g)), "sbm_net_loss_grad")
         return loss.value, g
+
+    def set_data(self, x, target, dims) -> None:
+        """Keeps a training set (x: (samples*V) x 16, target: samples*V) on the
+        device for train_steps."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        ns = t.size // int(np.prod(dims))
+        _check(self.lib.sbm_net_set_data(self._h, *dims, ns, _fptr(x), _fptr(t)),
+               "sbm_net_set_data")
+
+    def train_steps(self, steps: int, batch: int, lr: float, seed: int = 0) -> np.ndarray:
+        """Adam steps on the resident training set; returns the loss per step."""
+        hist = np.empty(steps, dtype=np.float32)
+        _check(self.lib.sbm_net_train_steps(self._h, steps, batch, lr, seed, _fptr(hist)),
+               "sbm_net_train_steps")
+        return hist
 
     def train(self, x, target, dims, steps: int, batch: int, lr: float, seed: int = 0) -> np.ndarray:
         """x: (samples*V) x 16, target: samples*V; returns the loss per step."""

@@ -191,8 +191,11 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale,
 /* Benchmark hook (no counterpart in the reference): times `reps` launches
  * of one solver kernel on the context stream with CUDA events, replaying the
  * arguments of the last mixed-precision solve.  which 0: FP32 fused
- * direction + stencil kernel; 1: FP32 vector update; 2: FP64 stencil + dot.
- * Reports the mean launch time and the algorithmic bytes one launch moves. */
+ * direction + stencil kernel; 1: FP32 vector update; 2: FP64 stencil + dot;
+ * after a learned-preconditioner solve also 3: one application of the
+ * preconditioner (restriction, U-Net, prolongation: 12 launches) and 4:
+ * the flexible-CG update.  Reports the mean time and the algorithmic bytes
+ * one launch (one application) moves on the fine grid. */
 int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
                      double* bytes_per_launch);
 
@@ -314,9 +317,16 @@ int sbm_net_forward(sbm_net* net, int ny, int nx, int nz, int nb, const float* i
  * parameter (FP32, same order as the parameters; grad may be NULL). */
 int sbm_net_loss_grad(sbm_net* net, int ny, int nx, int nz, int nb, const float* in,
                       const float* target, double* loss, float* grad);
+/* Training set kept on the device until replaced or the network is
+ * destroyed: nsamples input / target pairs of ny x nx x nz coarse cells. */
+int sbm_net_set_data(sbm_net* net, int ny, int nx, int nz, int nsamples, const float* in,
+                     const float* target);
 /* `steps` Adam steps (learning rate lr) on mini-batches of `batch` samples
- * drawn (seeded) from nsamples input / target pairs; loss_hist[steps]
- * receives each step's loss (may be NULL). */
+ * drawn (seeded) from the resident training set; loss_hist[steps] receives
+ * each step's loss (may be NULL).  Adam's moments carry over between calls. */
+int sbm_net_train_steps(sbm_net* net, int steps, int batch, float lr, uint64_t seed,
+                        float* loss_hist);
+/* sbm_net_set_data followed by sbm_net_train_steps. */
 int sbm_net_train(sbm_net* net, int ny, int nx, int nz, int nsamples, const float* in,
                   const float* target, int steps, int batch, float lr, uint64_t seed,
                   float* loss_hist);
