@@ -201,6 +201,7 @@ __device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t 
 }
 
 __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvMap m, ConvArgs a) {
+  pdl_begin();
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(1024) unsigned char sm[];
   const int P = a.planes;  // z planes per CTA (1 or 2), one accumulator each
@@ -717,8 +718,12 @@ int conv3_launch(const ConvArgs* pa, const ConvMap* map, int use_tc, cudaStream_
     if (tiles * ntn <= 152)
       nst = std::max(nst, (int)std::min<size_t>(nchunk, kSmemBudget / stage));
     a.nst = std::min(nst, NST);
-    k_conv3_tc<<<dim3((unsigned)tiles, (unsigned)ntn), NTHR, conv_tile_smem(nt, a.nst, a.planes),
-                 s>>>(*map, a);
+    const cudaError_t e = launch_pdl(k_conv3_tc, dim3((unsigned)tiles, (unsigned)ntn), dim3(NTHR),
+                                     conv_tile_smem(nt, a.nst, a.planes), s, *map, a);
+    if (e != cudaSuccess) {
+      set_error("k_conv3_tc launch", e);
+      return SBM_ERR_CUDA;
+    }
   } else {
     const int64_t n = nv * a.cout;
     k_conv3_ref<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);

@@ -15,6 +15,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <utility>
 
 #include "../../include/sbm_capi.h"
 
@@ -133,6 +134,34 @@ const char* last_error();
   } while (0)
 
 #define SBM_LAUNCHED(n) ::sbm::g_launches.fetch_add((n), std::memory_order_relaxed)
+
+// ------------------------------------- programmatic dependent launch
+// Kernels of the captured CG loop start with pdl_begin(): they allow the
+// next kernel of the stream to be scheduled as soon as all their CTAs run,
+// then wait until the previous kernel has completed and its writes are
+// visible (a no-op when launched without the attribute).  Nothing is read
+// before the wait, so the overlap covers launch latency and CTA placement
+// only, and every wait ends (no kernel waits on a later one).
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // ---------------------------------------------------- device helpers
 __device__ __forceinline__ double warp_sum(double v) {

@@ -688,6 +688,7 @@ __global__ void k_pc_feat(Dims c, const float* __restrict__ coefc, const float* 
 // update kernel has not produced them (first use, residual replacement).
 __global__ void k_pc_restrict(Geo g, Dims c, const float* __restrict__ r, float* __restrict__ rc,
                               double* partials, float* scal, CgState* st) {
+  pdl_begin();
   if (st->done || st->aux[1] != 0.0) return;
   double acc = 0.0;
   NET_LOOP(c.v()) {
@@ -716,6 +717,7 @@ __global__ void k_pc_restrict(Geo g, Dims c, const float* __restrict__ r, float*
 
 __global__ void k_pc_pack(int64_t V, const float* __restrict__ rc, const float* scal,
                           bf16* __restrict__ in0, const CgState* st) {
+  pdl_begin();
   if (st->done) return;
   const float inv = scal[1];
   NET_LOOP(V) in0[act_index(t, 0, V)] = __float2bfloat16_rn(rc[t] * inv);
@@ -741,6 +743,7 @@ __global__ void __launch_bounds__(256)
                  const float* __restrict__ r, const float* __restrict__ iv,
                  const float* __restrict__ q, float* __restrict__ z, const int* err,
                  double* partials, CgState* st) {
+  pdl_begin();
   if (st->done) return;
   const float f = scal[0] * scal[2];
   const int nchunk = g.ny / 4;
@@ -884,17 +887,19 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   const Geo& g = ctx->g32;
   const netd::Dims& c = pc->c;
-  netd::k_pc_restrict<<<netd::grid_for(c.v()), 256, 0, s>>>(g, c, r32, pc->rc, partials, pc->scal,
-                                                             st);
-  netd::k_pc_pack<<<netd::grid_for(c.v()), 256, 0, s>>>(c.v(), pc->rc, pc->scal, pc->w->in0, st);
+  launch_pdl(netd::k_pc_restrict, dim3(netd::grid_for(c.v())), dim3(256), 0, s, g, c, r32, pc->rc,
+             partials, (float*)pc->scal, st);
+  launch_pdl(netd::k_pc_pack, dim3(netd::grid_for(c.v())), dim3(256), 0, s, c.v(),
+             (const float*)pc->rc, (const float*)pc->scal, pc->w->in0, (const CgState*)st);
   SBM_LAUNCHED(2);
   netd::forward(pc->net, *pc->w, false, &st->done, s);
   const int64_t items = (int64_t)(g.ny / 4) * g.nx * (g.nz / 4);
   int64_t b = (items + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;
   if (b < 1) b = 1;
-  netd::k_pc_prolong<<<(unsigned)b, 256, 0, s>>>(g, c, pc->w->out, pc->scal, r32, iv32, q32,
-                                                 pc->zf + kOff32, pc->net->err, partials, st);
+  launch_pdl(netd::k_pc_prolong, dim3((unsigned)b), dim3(256), 0, s, g, c,
+             (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->zf + kOff32,
+             (const int*)pc->net->err, partials, st);
   SBM_LAUNCHED(1);
 }
 

@@ -540,6 +540,7 @@ __global__ void __launch_bounds__(256, 4)
                    const float* __restrict__ pold, const float* __restrict__ invd,
                    float* __restrict__ pnew, float* __restrict__ q, double* partials,
                    CgState* st) {
+  pdl_begin();
   if (st->done) return;
   const Geo g = op.g;
   const float beta = (float)st->beta;
@@ -797,6 +798,7 @@ __global__ void __launch_bounds__(256)
                    float* __restrict__ r, const float* __restrict__ q, double* __restrict__ d64,
                    float* __restrict__ rc, float* __restrict__ scal, double* partials,
                    CgState* st) {
+  pdl_begin();
   if (st->done) return;
   const bool fold = st->accum_pending != 0;
   const float alpha = (float)st->alpha;
@@ -874,6 +876,7 @@ __global__ void __launch_bounds__(BX* BY)
                 const float* __restrict__ x32, const double* __restrict__ r0,
                 float* __restrict__ r32, const float* __restrict__ invd32, double* partials,
                 CgState* st) {
+  pdl_begin();
   if (!st->reliable || st->done) return;
   const Geo g = op.g;
   SBM_COLUMN_PROLOGUE(g, zc)
@@ -973,7 +976,7 @@ int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, c
 int tma_plan_size(void);
 int tma_init();
 void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
-                double* partials, CgState* st, cudaStream_t s);
+                double* partials, CgState* st, cudaStream_t s, bool pdl = false);
 
 int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cudaGraph_t* graph_out,
                 int* nodes_out) {
@@ -1054,8 +1057,9 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
                                                        ctx->r0, r32, iv32, ctx->partials,      \
                                                        ctx->st)
     if (learned) {
-      k_rel_resid<0, false, true><<<sh64.grid, sh64.block, 0, s2>>>(
-          op64, g32, sh64.zc, ctx->d64, x32, ctx->r0, r32, iv32, ctx->partials, ctx->st);
+      launch_pdl(k_rel_resid<0, false, true>, sh64.grid, sh64.block, 0, s2, op64, g32, sh64.zc,
+                 (const double*)ctx->d64, (const float*)x32, (const double*)ctx->r0, r32,
+                 (const float*)iv32, ctx->partials, ctx->st);
     } else if (sp.form == 0) {
       if (pc) SBM_REL(0, true); else SBM_REL(0, false);
     } else {
@@ -1079,7 +1083,7 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
 #define SBM_AD(F, P)                                                                           \
   do {                                                                                         \
     if (use_tma)                                                                               \
-      tma_launch(*plan, in == pbuf[0], op32, out, q32, ctx->partials, ctx->st, s2);            \
+      tma_launch(*plan, in == pbuf[0], op32, out, q32, ctx->partials, ctx->st, s2, learned);   \
     else if (vec == 4)                                                                         \
       k32v_apply_dir<F, P><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, rdir, in, iv32, out, q32, \
                                                    ctx->partials, ctx->st);                    \
@@ -1098,9 +1102,9 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   k32_update<P, V><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, x32, out, r32, q32, iv32, ctx->d64, \
                                           ctx->partials, ctx->st)
     if (learned) {
-      k32_update_fcg<<<cgrid, 256, 0, s2>>>(g32, g, x32, out, r32, q32, ctx->d64,
-                                                             net_pc_rc(ctx), net_pc_scal(ctx),
-                                                             ctx->partials, ctx->st);
+      launch_pdl(k32_update_fcg, cgrid, dim3(256), 0, s2, g32, g, x32, (const float*)out, r32,
+                 (const float*)q32, ctx->d64, net_pc_rc(ctx), net_pc_scal(ctx), ctx->partials,
+                 ctx->st);
     } else if (vec == 4) {
       if (pc) SBM_UP(true, 4); else SBM_UP(false, 4);
     } else {

@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(NTH)
     k32t_apply_dir(const __grid_constant__ TmaMaps maps, OpArgs<float> op, int zct,
                    float* __restrict__ pnew, float* __restrict__ q, double* partials,
                    CgState* st) {
+  pdl_begin();
   constexpr int NA = 3 + (PC ? 1 : 0) + (FORM == 1 ? 1 : 0);
   constexpr int A_IV = 3, A_DG = 3 + (PC ? 1 : 0);
   extern __shared__ __align__(128) unsigned char smem[];
@@ -387,8 +388,14 @@ int tma_init() {
 
 // One launch: reads p from buffer a (fwd) or b (!fwd), writes p_new to pnew.
 void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
-                double* partials, CgState* st, cudaStream_t s) {
+                double* partials, CgState* st, cudaStream_t s, bool pdl) {
   const TmaMaps& m = fwd ? plan.fwd : plan.bwd;
+  if (pdl && plan.form == 0 && !plan.pc) {
+    // the flexible-CG loop (learned preconditioner): programmatic launch
+    launch_pdl(k32t_apply_dir<0, false>, plan.grid, dim3(NTH), plan.smem, s, m, op, plan.zct,
+               pnew, q, partials, st);
+    return;
+  }
   if (plan.form == 0) {
     if (plan.pc) k32t_apply_dir<0, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
     else k32t_apply_dir<0, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);

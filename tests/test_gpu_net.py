@@ -80,6 +80,18 @@ def test_training_lowers_the_loss(built):
     assert h[-10:].mean() < 0.1 * h[:10].mean()
 
 
+def test_resident_training_set_continues_training(built):
+    n = sbm.Net(seed=8)
+    rng = np.random.default_rng(9)
+    x = rng.normal(size=(6, 16, 16, 16, 16)).astype(np.float32)
+    t = (0.3 * x[..., 0] - 0.2 * np.roll(x[..., 0], 2, axis=2)).astype(np.float32)
+    n.set_data(x.reshape(-1, 16), t.ravel(), (16, 16, 16))
+    h1 = n.train_steps(100, batch=3, lr=2e-3, seed=1)
+    h2 = n.train_steps(100, batch=3, lr=2e-3, seed=2)
+    assert np.isfinite(h1).all() and np.isfinite(h2).all()
+    assert h2[-10:].mean() < h1[-10:].mean() < h1[:10].mean()
+
+
 def _problem(n, seed):
     ms = synth.microstructure((n, n, n), seed=seed, solid_fraction=0.6)
     return synth.potential_problem(ms["psi"])
