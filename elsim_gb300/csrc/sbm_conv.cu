@@ -202,7 +202,7 @@ __device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t 
 
 __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvMap m, ConvArgs a) {
   pdl_begin();
-  if (a.skip && *a.skip) return;
+  if ((a.skip && *a.skip) || (a.skip2 && *a.skip2)) return;
   extern __shared__ __align__(1024) unsigned char sm[];
   const int P = a.planes;  // z planes per CTA (1 or 2), one accumulator each
   const int ahalf = a_half_bytes(P);

@@ -42,6 +42,7 @@ struct ConvArgs {
                            //    tensor-core kernel takes it from a reversed weight image)
   int* err;                // set to 1 if a wait expired
   const int* skip;         // launch is a no-op while *skip != 0 (may be null)
+  const int* skip2;        //   or while *skip2 != 0 (may be null)
   // tensor-core kernel only:
   int planes;              // z planes per CTA: 1, or 2 (nzs even)
   __nv_bfloat16* pool;     // 2x2x2-averaged BF16 output [V/8][cout] (planes 2) or null

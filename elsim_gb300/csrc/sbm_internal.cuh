@@ -115,6 +115,8 @@ struct CgState {
   int accum_pending;  // mixed: fold the FP32 correction into the FP64 one
   int initial;        // mixed: first residual of the solve (beta = 0)
   int n_reliable;     // mixed: number of FP64 residual replacements
+  int pc_off;         // learned preconditioner switched off (no progress): z = D^-1 r
+  int stall_iter;     // iteration of the last halving of the FP32 residual norm
   unsigned int counter[8];
 };
 

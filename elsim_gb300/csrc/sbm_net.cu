@@ -438,7 +438,7 @@ int planes_for(const Dims& d, bool pool) {
 }
 
 ConvArgs layer_args(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx,
-                    bool pool, const int* skip) {
+                    bool pool, const int* skip, const int* skip2) {
   ConvArgs a{};
   const Dims& d = w.d[lev];
   a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
@@ -447,7 +447,7 @@ ConvArgs layer_args(sbm_net* n, const Work& w, int l, int lev, const bf16* x, in
   a.ldx = ldx; a.offx = 0;
   a.x = x; a.wimg = n->wimg + kL.off[l]; a.wimg16 = n->wimg16 + kL.off[l];
   a.bias = n->w32 + kL.boff[l];
-  a.relu = 1; a.flip = 0; a.err = n->err; a.skip = skip;
+  a.relu = 1; a.flip = 0; a.err = n->err; a.skip = skip; a.skip2 = skip2;
   return a;
 }
 
@@ -462,25 +462,26 @@ int launch(Work& w, const ConvArgs& a, cudaStream_t s) {
 // output layer run in the convolution epilogues; activations that only the
 // backward pass reads (bottleneck and decoder outputs) are stored only
 // when training.
-int forward(sbm_net* n, Work& w, bool tgt, const int* skip, cudaStream_t s) {
+int forward(sbm_net* n, Work& w, bool tgt, const int* skip, const int* skip2, cudaStream_t s) {
   int rc;
   for (int lev = 0; lev < 4; ++lev) {
     const int l = kEnc[lev];
-    ConvArgs a = layer_args(n, w, l, lev, lev == 0 ? w.in0 : w.pin[lev], kCi[l], true, skip);
+    ConvArgs a =
+        layer_args(n, w, l, lev, lev == 0 ? w.in0 : w.pin[lev], kCi[l], true, skip, skip2);
     a.y16 = w.cat[lev];
     a.offy = kUpW[lev];
     a.pool = w.pin[lev + 1];
     if ((rc = launch(w, a, s))) return rc;
   }
   {
-    ConvArgs a = layer_args(n, w, E4, 4, w.pin[4], kCi[E4], false, skip);
+    ConvArgs a = layer_args(n, w, E4, 4, w.pin[4], kCi[E4], false, skip, skip2);
     a.y16 = w.train ? w.a4 : nullptr;
     a.up = w.cat[3];
     if ((rc = launch(w, a, s))) return rc;
   }
   for (int lev = 3; lev >= 0; --lev) {
     const int l = kDec[lev];
-    ConvArgs a = layer_args(n, w, l, lev, w.cat[lev], kCatW[lev], false, skip);
+    ConvArgs a = layer_args(n, w, l, lev, w.cat[lev], kCatW[lev], false, skip, skip2);
     a.y16 = w.train ? w.dec[lev] : nullptr;
     if (lev > 0) {
       a.up = w.cat[lev - 1];
@@ -689,7 +690,7 @@ __global__ void k_pc_feat(Dims c, const float* __restrict__ coefc, const float* 
 __global__ void k_pc_restrict(Geo g, Dims c, const float* __restrict__ r, float* __restrict__ rc,
                               double* partials, float* scal, CgState* st) {
   pdl_begin();
-  if (st->done || st->aux[1] != 0.0) return;
+  if (st->done || st->pc_off || st->aux[1] != 0.0) return;
   double acc = 0.0;
   NET_LOOP(c.v()) {
     int i, j, k;
@@ -718,7 +719,7 @@ __global__ void k_pc_restrict(Geo g, Dims c, const float* __restrict__ r, float*
 __global__ void k_pc_pack(int64_t V, const float* __restrict__ rc, const float* scal,
                           bf16* __restrict__ in0, const CgState* st) {
   pdl_begin();
-  if (st->done) return;
+  if (st->done || st->pc_off) return;
   const float inv = scal[1];
   NET_LOOP(V) in0[act_index(t, 0, V)] = __float2bfloat16_rn(rc[t] * inv);
 }
@@ -745,7 +746,8 @@ __global__ void __launch_bounds__(256)
                  double* partials, CgState* st) {
   pdl_begin();
   if (st->done) return;
-  const float f = scal[0] * scal[2];
+  const bool coarse = st->pc_off == 0;  // off: z = D^-1 r (Jacobi-PCG)
+  const float f = coarse ? scal[0] * scal[2] : 0.f;
   const int nchunk = g.ny / 4;
   const int64_t n = (int64_t)nchunk * g.nx * (g.nz / 4);
   const float wl[4] = {0.375f, 0.125f, 0.875f, 0.625f};
@@ -761,13 +763,15 @@ __global__ void __launch_bounds__(256)
     interp1(j - 1, c.nx, &x0, &x1, &wx);
     const int ys[3] = {max(m - 1, 0), m, min(m + 1, c.ny - 1)};
     const int zs[3] = {max(kc - 1, 0), kc, min(kc + 1, c.nz - 1)};
-    float cx[3][3];  // [y neighbour][z plane], interpolated in x
+    float cx[3][3] = {};  // [y neighbour][z plane], interpolated in x
+    if (coarse) {
 #pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      const int64_t r0 = (int64_t)c.ny * (x0 + (int64_t)c.nx * zs[b]);
-      const int64_t r1 = (int64_t)c.ny * (x1 + (int64_t)c.nx * zs[b]);
+      for (int b = 0; b < 3; ++b) {
+        const int64_t r0 = (int64_t)c.ny * (x0 + (int64_t)c.nx * zs[b]);
+        const int64_t r1 = (int64_t)c.ny * (x1 + (int64_t)c.nx * zs[b]);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) cx[a][b] = wx * out[r0 + ys[a]] + (1.f - wx) * out[r1 + ys[a]];
+        for (int a = 0; a < 3; ++a) cx[a][b] = wx * out[r0 + ys[a]] + (1.f - wx) * out[r1 + ys[a]];
+      }
     }
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -892,7 +896,7 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   launch_pdl(netd::k_pc_pack, dim3(netd::grid_for(c.v())), dim3(256), 0, s, c.v(),
              (const float*)pc->rc, (const float*)pc->scal, pc->w->in0, (const CgState*)st);
   SBM_LAUNCHED(2);
-  netd::forward(pc->net, *pc->w, false, &st->done, s);
+  netd::forward(pc->net, *pc->w, false, &st->done, &st->pc_off, s);
   const int64_t items = (int64_t)(g.ny / 4) * g.nx * (g.nz / 4);
   int64_t b = (items + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;
@@ -998,7 +1002,7 @@ int sbm_net_forward(sbm_net* n, int ny, int nx, int nz, int nb, const float* in,
   const int64_t V = w->d[0].v();
   int rc = upload_features(w->in0, in, V, 1, n->stream);
   if (rc) return rc;
-  if ((rc = forward(n, *w, false, nullptr, n->stream))) return rc;
+  if ((rc = forward(n, *w, false, nullptr, nullptr, n->stream))) return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(out, w->out, sizeof(float) * V, cudaMemcpyDeviceToHost, n->stream));
   return check_err(n);
 }
@@ -1014,7 +1018,7 @@ int sbm_net_loss_grad(sbm_net* n, int ny, int nx, int nz, int nb, const float* i
   if (rc) return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(w->tgt, target, sizeof(float) * V, cudaMemcpyHostToDevice, s));
   SBM_CUDA_TRY(cudaMemsetAsync(n->loss, 0, sizeof(double), s));
-  if ((rc = forward(n, *w, true, nullptr, s))) return rc;
+  if ((rc = forward(n, *w, true, nullptr, nullptr, s))) return rc;
   if ((rc = backward(n, *w, s))) return rc;
   double h = 0.0;
   SBM_CUDA_TRY(cudaMemcpyAsync(&h, n->loss, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1083,7 +1087,7 @@ int sbm_net_train_steps(sbm_net* n, int steps, int batch, float lr, uint64_t see
                           cudaMemcpyDeviceToDevice, s))
         return fail(SBM_ERR_CUDA);
     }
-    if ((rc = forward(n, *w, true, nullptr, s))) return fail(rc);
+    if ((rc = forward(n, *w, true, nullptr, nullptr, s))) return fail(rc);
     if ((rc = backward(n, *w, s))) return fail(rc);
     if ((rc = adam(n, lr, s))) return fail(rc);
     k_loss_rec<<<1, 1, 0, s>>>(n->loss, inv_v, hist + it);

@@ -357,14 +357,14 @@ int chunk_len(const sbm_ctx* ctx) {
 // issued by body(stream), and returns it with its kernel-node count.
 template <typename Body>
 int capture_graph(sbm_ctx* ctx, const std::string& key, int nodes_per_iter, Body&& body,
-                  cudaGraphExec_t* exec, int* nodes) {
+                  cudaGraphExec_t* exec, int* nodes, int len_override = 0) {
   auto it = ctx->graphs.find(key);
   if (it != ctx->graphs.end()) {
     *exec = it->second.exec;
     *nodes = it->second.nodes;
     return SBM_OK;
   }
-  const int len = chunk_len(ctx);
+  const int len = len_override > 0 ? len_override : chunk_len(ctx);
   cudaGraph_t graph = nullptr;
   SBM_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   for (int c = 0; c < len; ++c) body(ctx->stream);
@@ -851,6 +851,17 @@ __global__ void __launch_bounds__(256)
       scal[0] = (float)sc;
       scal[1] = sc > 0.0 ? (float)(1.0 / sc) : 0.f;
       st->aux[1] = 1.0;
+      // progress check of the learned preconditioner: the FP32 residual norm
+      // must halve within 50 iterations, else the solve continues as
+      // Jacobi-PCG (a network that does not fit the problem cannot stall it)
+      if (!st->pc_off) {
+        if (st->aux[3] <= 0.0 || rr_new < 0.25 * st->aux[3]) {
+          st->aux[3] = rr_new;
+          st->stall_iter = it;
+        } else if (it - st->stall_iter > 50) {
+          st->pc_off = 1;
+        }
+      }
       if (!isfinite(rr_new) || !isfinite(st->alpha)) {
         st->done = 3;
       } else {
@@ -1123,13 +1134,16 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   rel(s);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
+  // bodies of 2 iterations per captured chunk: the flexible CG converges in
+  // ~10x fewer iterations, so shorter chunks trim the no-op tail
+  const int clen = ctx->chunk > 0 ? ctx->chunk : (learned ? 4 : chunk_len(ctx));
   const std::string key =
       key_of(learned ? (use_tma ? "mixfcg2-tma" : "mixfcg2") : (use_tma ? "mixrel2-tma" : "mixrel2"),
              hk32, dg32, x32, r32, pbuf[0], pbuf[1], learned ? (const void*)zl : iv32, sp.scale,
-             sp.form, sp.bcx0, sp.bcx1, vec * 16 + zc32, pc, sh64.zc, chunk_len(ctx));
+             sp.form, sp.bcx0, sp.bcx1, vec * 16 + zc32, pc, sh64.zc, clen);
   cudaGraphExec_t ex = nullptr;
   int nodes = 0;
-  rc = capture_graph(ctx, key, learned ? 2 * (3 + net_pc_nodes()) : 6, body, &ex, &nodes);
+  rc = capture_graph(ctx, key, learned ? 2 * (3 + net_pc_nodes()) : 6, body, &ex, &nodes, clen);
   if (rc) return rc;
   ctx->last_op32 = op32;
   ctx->last_pc = pc ? 1 : 0;
@@ -1153,6 +1167,7 @@ int mixed_end(sbm_ctx* ctx, const SolveSpec& sp, const CgState& fin, SolveResult
   SBM_CUDA_TRY(cudaEventSynchronize(ctx->ev1));
   float ms = 0.f;
   SBM_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  if (fin.pc_off && ctx->last_precond == SBM_PC_LEARNED) ctx->last_precond = SBM_PC_JACOBI;
   out->iters = fin.iter;
   out->outer = fin.n_reliable;
   out->final_res = fin.rms;

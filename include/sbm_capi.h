@@ -337,7 +337,9 @@ int sbm_net_load(const char* path, sbm_net** out, double* out_scale);
 /* Attach `net` (NULL detaches) to a context with output scale k_out.  The
  * context does not own the network: keep it alive while attached. */
 int sbm_ctx_set_net(sbm_ctx* ctx, sbm_net* net, double out_scale);
-/* Preconditioner used by the last mixed-precision solve (SBM_PC_*). */
+/* Preconditioner used by the last mixed-precision solve (SBM_PC_*).  A
+ * learned-preconditioner solve whose FP32 residual norm stops halving
+ * within 50 iterations continues as Jacobi-PCG and reports SBM_PC_JACOBI. */
 int sbm_ctx_last_precond(const sbm_ctx* ctx);
 /* One application z = M(r) of the learned preconditioner for the GENERIC
  * operator of the context's coefficient (halo-padded FP64 r and z). */

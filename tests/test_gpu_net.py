@@ -162,3 +162,46 @@ def test_falls_back_to_jacobi(built):
     with _context(n, prob) as ctx:
         rl, _, used = _solve(ctx, prob, sbm.PC_LEARNED)
     assert used == sbm.PC_JACOBI and rl["status"] == sbm.OK
+
+
+def test_stalled_network_is_switched_off(built):
+    # random weights at a large output scale: the coarse correction is noise;
+    # the solve must still converge, continuing as Jacobi-PCG
+    n = 64
+    prob = _problem(n, 41)
+    bad = sbm.Net(seed=5)
+    bad.set_params(bad.params() * 3.0)
+    bad.out_scale = 1e3
+    with _context(n, prob) as ctx:
+        ctx.set_net(bad)
+        r, x, used = _solve(ctx, prob, sbm.PC_LEARNED)
+        rj, xj, _ = _solve(ctx, prob, sbm.PC_JACOBI)
+    assert r["status"] == sbm.OK and r["final_res"] <= 1e-8
+    assert used == sbm.PC_JACOBI
+    xi, ji = x[1:-1, 1:-1, 1:-1], xj[1:-1, 1:-1, 1:-1]
+    assert np.abs(xi - ji).max() <= 1e-6 * np.abs(ji).max()
+
+
+def test_learned_preconditioner_on_a_neumann_face(built):
+    # the network was trained with Dirichlet on both x faces; with a Neumann
+    # x0 face it still helps and the solve converges to the same solution
+    n = 64
+    prob = _problem(n, 42)
+    stored = learned.load()
+
+    def solve(ctx, pc):
+        ctx.upload("x", prob["x"])
+        r = ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_COPY, bc_x1=sbm.BC_ZERO, scale=1.0,
+                         tol=1e-8, max_it=20000, stop_rule=sbm.STOP_REL_RES,
+                         precision=sbm.PREC_MIXED, precond=pc)
+        return r, ctx.download("x")[1:-1, 1:-1, 1:-1]
+
+    with _context(n, prob) as ctx:
+        ctx.set_net(stored)
+        rl, xl = solve(ctx, sbm.PC_LEARNED)
+        used = ctx.last_precond()
+        rj, xj = solve(ctx, sbm.PC_JACOBI)
+    assert used == sbm.PC_LEARNED and rl["status"] == sbm.OK and rl["final_res"] <= 1e-8
+    assert rl["iters"] < 0.6 * rj["iters"]
+    assert np.abs(xl - xj).max() <= 1e-6 * np.abs(xj).max()
+
