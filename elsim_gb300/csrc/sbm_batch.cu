@@ -39,7 +39,7 @@ extern "C" int sbm_batch_solve(sbm_ctx** ctxs, int n, int bc_x0, int bc_x1, doub
                                int* status, float* ms_total) {
   if (!ctxs || n < 1 || max_it < 1 || !(tol >= 0.0)) return SBM_ERR_ARG;
   if ((bc_x0 != SBM_BC_COPY && bc_x0 != SBM_BC_ZERO) || (bc_x1 != SBM_BC_COPY && bc_x1 != SBM_BC_ZERO) ||
-      (precond != SBM_PC_NONE && precond != SBM_PC_JACOBI))
+      (precond != SBM_PC_NONE && precond != SBM_PC_JACOBI && precond != SBM_PC_LEARNED))
     return SBM_ERR_ARG;
   for (int v = 0; v < n; ++v)
     if (!ctxs[v]) return SBM_ERR_ARG;

@@ -15,8 +15,9 @@ from the library's own mixed-precision solver on seeded synthetic
 microstructures (``synth.microstructure``) and right-hand sides of several
 spectra; training runs on the GPU (``Net.train``).
 
-``python -m elsim_gb300.learned --out FILE`` reruns the recipe of the stored
-weights ``elsim_gb300/weights/pc_unet.bin`` (recorded in pc_unet.json; the
+``python -m elsim_gb300.learned --seed 1 --out FILE`` reruns the recipe of
+the stored weights ``elsim_gb300/weights/pc_unet.bin`` (recorded in
+pc_unet.json: seed 1, the best validation score of seeds 0-2; the
 reductions of the training kernels use atomics, so a rerun gives weights of
 the same quality, not the same bits).
 """

@@ -204,7 +204,9 @@ int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
  * mixed-precision CG to rel-res tol together -- their iteration chunks are
  * child graphs of one parent CUDA graph, so one launch advances every
  * unconverged volume.  Per-volume iterations, final rel-res and status go to
- * the n-element arrays; ms_total is the device time of the whole batch. */
+ * the n-element arrays; ms_total is the device time of the whole batch.
+ * precond SBM_PC_LEARNED applies per volume (its own attached network and
+ * grid permitting, else Jacobi; sbm_ctx_last_precond of each context). */
 int sbm_batch_solve(sbm_ctx** ctxs, int n, int bc_x0, int bc_x1, double scale, double tol,
                     int max_it, int precond, int* iters, double* final_res, int* status,
                     float* ms_total);

@@ -45,3 +45,33 @@ def test_batch_equals_individual_solves(built):
     assert again["iters"] == out["iters"]
     for c in ctxs:
         c.close()
+
+
+def test_batch_with_learned_preconditioner(built):
+    # 64^3 and 128^3 volumes take the learned preconditioner, the 48^3 one
+    # falls back to Jacobi; each equals its single solve
+    from elsim_gb300 import learned
+    net = learned.load()
+    sizes = [64, 48, 128, 64]
+    probs = [_vol(n, 300 + v, 0.55 + 0.03 * v) for v, n in enumerate(sizes)]
+    ctxs = [sbm.Context(n, n, n) for n in sizes]
+    for c, p in zip(ctxs, probs):
+        for k in ("coef", "x", "rhs", "weight"):
+            c.upload(k, p[k])
+        c.set_net(net)
+    out = sbm.batch_solve(ctxs, tol=1e-8, precond=sbm.PC_LEARNED)
+    assert out["status"] == [0] * len(sizes)
+    assert [c.last_precond() for c in ctxs] == [sbm.PC_LEARNED, sbm.PC_JACOBI, sbm.PC_LEARNED,
+                                                sbm.PC_LEARNED]
+    xs = [c.download("x") for c in ctxs]
+    for v, (c, p) in enumerate(zip(ctxs, probs)):
+        c.upload("x", p["x"])
+        info = c.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO, scale=1.0,
+                          tol=1e-8, max_it=100000, stop_rule=sbm.STOP_REL_RES,
+                          precision=sbm.PREC_MIXED, precond=sbm.PC_LEARNED)
+        assert info["iters"] == out["iters"][v]
+        assert np.array_equal(c.download("x"), xs[v])
+        assert out["final_res"][v] <= 1e-8
+    for c in ctxs:
+        c.close()
+
