@@ -300,7 +300,10 @@ int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const uint16_t* x
  * SBM_PC_LEARNED applies when a network is attached, the operator is the
  * phP / phE / GENERIC form and ny, nx, nz are multiples of 64; otherwise the
  * solve falls back to Jacobi (sbm_ctx_last_precond reports which ran).
- * Only the mixed-precision solver takes it. */
+ * Only the mixed-precision solver takes it.  Training / forward calls on
+ * one network come from one host thread at a time; any number of contexts
+ * may share a network as their preconditioner (they only read its
+ * weights). */
 typedef struct sbm_net sbm_net;
 
 /* Number of FP32 parameters of the network. */
