@@ -890,9 +890,23 @@ __global__ void __launch_bounds__(BX* BY)
   pdl_begin();
   if (!st->reliable || st->done) return;
   const Geo g = op.g;
+  // the first replacement of a solve sees a zero correction (d64 and x32
+  // were just cleared): the true residual is r0 itself, no stencil needed
+  const bool zero_corr = st->initial != 0;
   SBM_COLUMN_PROLOGUE(g, zc)
   double a_rr = 0.0, a_r32 = 0.0, a_rz = 0.0;
-  if (active && k0 <= k1) {
+  if (active && k0 <= k1 && zero_corr) {
+    for (int k = k0; k <= k1; ++k) {
+      const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
+      const double rv = r0[c];
+      const float rf = (float)rv;
+      r32[c3] = rf;
+      const float zf = PC ? invd32[c3] * rf : rf;
+      a_rr += rv * rv;
+      a_r32 += (double)rf * (double)rf;
+      a_rz += (double)rf * (double)zf;
+    }
+  } else if (active && k0 <= k1) {
     for (int k = k0; k <= k1; ++k) {
       const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
 #define V(o64, o32) (d64[c + (o64)] + (double)x32[c3 + (o32)])

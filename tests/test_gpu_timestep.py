@@ -145,3 +145,25 @@ def test_diverging_picard_loop_is_reported_not_hidden(built):
                 dt, vsr = synth.step_schedule(sg["xrf"], abs(sg["trgI"] - sg["scrnt"]), sg["trgI"])
                 sg = ctx.time_step(it, dt, vsr)
         assert e.value.code == sbm.ERR_NONFINITE
+
+
+def test_mixed_precision_time_steps_match_oracle(built):
+    """The whole step with the mixed-precision stage solves (FP32 Jacobi-PCG
+    inside FP64 refinement to rel-res 1e-10) against the FP64 oracle with
+    tightened CG tolerances: the same fields to 1e-6 in their phases."""
+    shape = (20, 24, 16)
+    p = _params(True, sbm.BV_EXP)
+    dp, de = _dist(shape, 4)
+    st = orc.State(*shape, p)
+    so = st.setup_domain(dp, de)
+    with sbm.Context(*shape, params=p) as ctx:
+        ctx.setup_domain(dp, de)
+        for it in (1, 2, 3):
+            dt, vsr = synth.step_schedule(so["xrf"], abs(so["trgI"] - so["scrnt"]), so["trgI"])
+            so = st.time_step(it, dt, vsr)
+            sg = ctx.time_step(it, dt, vsr, precision=sbm.PREC_MIXED)
+        for key in ("xrf", "scrnt", "bve"):
+            assert abs(sg[key] - so[key]) <= 1e-6 * max(abs(so[key]), 1e-12), (key, sg[key], so[key])
+        for f in FIELDS:
+            w = st.field(WEIGHT[f]) if WEIGHT[f] is not None else None
+            assert _werr(ctx.download(f), st.field(f), w) < 1e-6, f
