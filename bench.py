@@ -27,6 +27,7 @@ extrapolated to the 2038 iterations the FP64 CG needs on this workload.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import math
 import os
@@ -65,9 +66,11 @@ def _args():
     ap.add_argument("--size", type=int, default=N)
     ap.add_argument("--pc", default="learned", choices=["learned", "jacobi"],
                     help="preconditioner of the headline solve")
-    ap.add_argument("--workload", default="solve256", choices=["solve256", "batch96", "profile"],
+    ap.add_argument("--workload", default="solve256",
+                    choices=["solve256", "batch96", "profile", "frontend"],
                     help="solve256: the headline 256^3 solve; batch96: 96 uneven sub-volumes; "
-                         "profile: only the production solve, for ncu captures")
+                         "profile: only the production solve, for ncu captures; frontend: "
+                         "one frame of the LevelSet_3D geometry front end")
     return ap.parse_args()
 
 
@@ -492,6 +495,144 @@ def run_batch(args):
     return 0
 
 
+def run_frontend(args):
+    """One frame of the reference's geometry front end (LevelSet_3D.f90) at
+    its own sizes: TmpA 500x520x170 (seeded synthetic 0/1 voxels in place of
+    the scanned microstructure), grid 93 x 730 x 160, tunnel radius TuRd(8),
+    50 Allen-Cahn steps, sign, 175 reinitialisation steps.  `value` = device
+    time of a frame with the voxels resident; `e2e` = sbm_ls_frontend from
+    pinned host buffers (voxels up, distance down); the oracle runs the same
+    frame on the host cores and the two distances are compared bit for bit.
+    `config.production_frame_s`: the same frame on the time-stepping
+    program's 186 x 1460 x 320 grid (all lengths doubled)."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from elsim_gb300 import geometry, sbm
+    from oracle import sbm_oracle as orc
+    R = geometry.REFERENCE
+    yo, xo, zo, yg, zg, xoff, nth = (R[k] for k in ("yo", "xo", "zo", "yg", "zg", "xoff", "nthick"))
+    xg = xoff + nth * zo
+    n_fr = 8
+    tr = float(geometry.TUNNEL_RADII[n_fr])
+    ac, lit, dt = geometry.AC_ITERS, geometry.REDIST_ITERS, geometry.DT
+    vox = geometry.synthetic_voxels((yo, xo, zo), seed=SEED)
+    nv, nh = yo * xo * zo, (yg + 2) * (xg + 2) * (zg + 2)
+    lib = sbm.load_library()
+    dev = torch.device("cuda", 0)
+    vox_d = torch.from_numpy(vox.ravel(order="F")).to(dev)
+    ds, sg, tmp = (torch.empty(nh, dtype=torch.float64, device=dev) for _ in range(3))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def frame_dev(a=ac, n_lit=lit):
+        sbm._check(lib.sbm_ls_frontend_device(vox_d.data_ptr(), yo, xo, zo, yg, zg, xoff, nth, tr,
+                                              a, n_lit, dt, ds.data_ptr(), sg.data_ptr(),
+                                              tmp.data_ptr(), stream.cuda_stream),
+                   "sbm_ls_frontend_device")
+
+    def timed(fn, k):
+        out = []
+        for _ in range(k):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1) / 1e3)
+        return statistics.mean(out)
+
+    for _ in range(args.warmup):
+        frame_dev()
+    torch.cuda.synchronize()
+    clk = Clocks()
+    clk.start()
+    l0 = sbm.launch_count()
+    t_frame = timed(frame_dev, args.steps)
+    launches = (sbm.launch_count() - l0) // args.steps
+    clocks = clk.stop()
+    got = ds.cpu().numpy().reshape((yg + 2, xg + 2, zg + 2), order="F")
+    t_nolit = timed(lambda: frame_dev(n_lit=0), args.steps)
+    t_stack = timed(lambda: frame_dev(a=0, n_lit=0), args.steps)
+    t_redist = (t_frame - t_nolit) / lit
+    t_ac = (t_nolit - t_stack) / ac
+    # end to end through the C-ABI from pinned host memory
+    vox_h = torch.empty(nv, dtype=torch.float64, pin_memory=True)
+    vox_h.numpy()[:] = vox.ravel(order="F")
+    ds_h = torch.empty(nh, dtype=torch.float64, pin_memory=True)
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sbm._check(lib.sbm_ls_frontend(C.cast(vox_h.data_ptr(), C.POINTER(C.c_double)), yo, xo, zo,
+                                       yg, zg, xoff, nth, tr, ac, lit, dt,
+                                       C.cast(ds_h.data_ptr(), C.POINTER(C.c_double))),
+                   "sbm_ls_frontend")
+        if i >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    # the production grid of the time-stepping program, 186 x 1460 x 320
+    # (SBMES_3D_MPI_CH_Gr_CONJG_VD_T05_01_BQ_hx3.f90:73-75): the same frame
+    # with every length doubled (voxels upsampled 2x, 100 leading columns,
+    # tunnel radius 2 TuRd(8)); device time of one frame after one warm-up
+    del vox_d, ds, sg, tmp
+    v2 = np.asfortranarray(np.repeat(np.repeat(np.repeat(vox, 2, 0), 2, 1), 2, 2))
+    P = {"yo": 2 * yo, "xo": 2 * xo, "zo": 2 * zo, "yg": 2 * yg, "zg": 2 * zg, "xoff": 2 * xoff}
+    xg2 = P["xoff"] + nth * P["zo"]
+    nh2 = (P["yg"] + 2) * (xg2 + 2) * (P["zg"] + 2)
+    v2_d = torch.from_numpy(v2.ravel(order="F")).to(dev)
+    del v2
+    b2 = [torch.empty(nh2, dtype=torch.float64, device=dev) for _ in range(3)]
+
+    def frame_prod():
+        sbm._check(lib.sbm_ls_frontend_device(v2_d.data_ptr(), P["yo"], P["xo"], P["zo"], P["yg"],
+                                              P["zg"], P["xoff"], nth, 2 * tr, ac, lit, dt,
+                                              b2[0].data_ptr(), b2[1].data_ptr(),
+                                              b2[2].data_ptr(), stream.cuda_stream),
+                   "sbm_ls_frontend_device")
+
+    frame_prod()
+    t_prod = timed(frame_prod, 2)
+    del v2_d, b2
+    # the oracle: the same frame on the host cores
+    t0 = time.perf_counter()
+    want = orc.ls_frontend(vox, yg, zg, xoff, nth, tr, ac, lit, dt)
+    t_cpu = time.perf_counter() - t0
+    threads = orc.lib().orc_num_threads()
+    exact = bool(np.array_equal(got, want)) and bool(
+        np.array_equal(ds_h.numpy().reshape(got.shape, order="F"), want))
+    hbm, src = _peaks()
+    redist_bytes = 3 * 8 * nh  # sg and f read, nf written, every padded cell
+    ach = redist_bytes / t_redist / 1e9
+    line = {"metric": "ls_frontend_frame_time_93x730x160", "value": t_frame, "unit": "s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_frame * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded thresholded smoothed noise, 60% ones; the scanned "
+                    "microstructure is not public)",
+            "config": {"workload": f"LevelSet_3D frame: TmpA {yo}x{xo}x{zo}, grid {yg}x{xg}x{zg}, "
+                                   f"tunnel radius TuRd({n_fr}) = {tr:.4f}, {ac} Allen-Cahn + sign "
+                                   f"+ {lit} ReDist3D steps",
+                       "l2": "256 MB L2 flush between timed frames; working set 625 MB",
+                       "bit_exact_vs_oracle": exact,
+                       "ms_stack": t_stack * 1e3, "us_per_allen_cahn": t_ac * 1e6,
+                       "us_per_redist": t_redist * 1e6,
+                       "production_grid": f"{2 * yg}x{xg2}x{2 * zg} (lengths x2, voxels "
+                                          f"{2 * yo}x{2 * xo}x{2 * zo})",
+                       "production_frame_s": t_prod},
+            "roofline": {"kernel": "k_redist", "bound": "hbm", "achieved": ach, "peak": hbm,
+                         "unit": "GB/s", "frac": ach / hbm, "peak_source": src,
+                         "traffic": None,
+                         "note": "FP64-pipe-bound on GB300; algorithmic bytes 24 B x "
+                                 f"{nh} padded cells per launch"},
+            "cpu_baseline": {"value": t_cpu, "unit": "s", "cores": threads, "kind": "port",
+                             "sample": "the whole frame (oracle C restatement, OpenMP)"},
+            "e2e": {"value": statistics.mean(e2e), "unit": "s", "h2d_bytes_per_step": 8 * nv,
+                    "d2h_bytes_per_step": 8 * nh},
+            "clocks": clocks, "gpu_launches": launches}
+    print(json.dumps(line))
+    return 0
+
+
 def run_profile(args):
     """The production solve alone (no FP64 baseline, no CPU leg), `steps`
     times after `warmup` solves: the command the ncu summaries profile."""
@@ -526,6 +667,8 @@ def main():
         return run_batch(args)
     if args.workload == "profile":
         return run_profile(args)
+    if args.workload == "frontend":
+        return run_frontend(args)
     return run_ours(args)
 
 

@@ -38,6 +38,12 @@ int redist_dev(cudaStream_t s, const Geo& g, const double* sg, double* f, double
 int accdiff_dev(cudaStream_t s, const Geo& g, const double* psi, double* cn, double* tmp,
                 int term, int dirichlet_x);
 int rm_mask_dev(cudaStream_t s, int64_t n, const double* psA, const double* cn, double* psB);
+int allen_cahn_dev(cudaStream_t s, const Geo& g, double* f, double* tmp, int iters);
+int ls_geometry_dev(cudaStream_t s, const Geo& g, const double* vox, int yo, int xo, int zo,
+                    int xoff, double tr, double* ds);
+int ls_frontend_dev(cudaStream_t s, const Geo& g, const double* vox, int yo, int xo, int zo,
+                    int xoff, double tr, int ac_iters, int lit, double dt, double* ds, double* sg,
+                    double* tmp);
 int sign_dev(cudaStream_t s, int64_t n, const double* ds, double thr, double* sg);
 int ghost_after_solve(sbm_ctx* ctx, double* f, int bcx0, int bcx1);
 
@@ -284,6 +290,125 @@ int sbm_download(sbm_ctx* ctx, int field, double* h, int haloed) {
   return SBM_OK;
 }
 
+// ------------------------------------------------------------ snapshots
+//
+// A snapshot is a header followed by whole halo-padded FP64 fields: the 13
+// public fields and, once the electrochemical state exists, the 12 step
+// buffers (half coefficients of the kappa / pce / pcc operators, Dab, mu,
+// mobility, CnE right-hand side, reaction coefficients, forward / backward
+// rate constants and the previous phP / phE).  Everything a later time step
+// or solve reads from the context is in it, so a restored context continues
+// bit for bit; the CG work vectors are not, since every solve starts them
+// afresh.
+namespace {
+constexpr char kSnapMagic[8] = {'S', 'B', 'M', 'S', 'N', 'A', 'P', '1'};
+constexpr int kStepBufs = 12;
+
+struct SnapHeader {
+  char magic[8];
+  int32_t version;
+  int32_t ny, nx, nz;
+  int32_t nfields;    // field records after the header
+  int32_t step_work;  // 1 when the step buffers follow the public fields
+  int64_t nh;         // doubles per field record
+  sbm_params p;
+  sbm_scalars sc;
+};
+
+constexpr size_t kSnapHead = (sizeof(SnapHeader) + 63) / 64 * 64;
+
+int step_bufs(sbm_ctx* ctx, double** out) {
+  double* b[kStepBufs] = {ctx->hk_kap, ctx->hk_pce, ctx->hk_pcc, ctx->dab, ctx->mu,  ctx->mb,
+                          ctx->rhe,    ctx->rxc,    ctx->kfw,    ctx->kbw, ctx->ppo, ctx->peo};
+  for (int i = 0; i < kStepBufs; ++i) out[i] = b[i];
+  return ctx->hk_kap ? kStepBufs : 0;
+}
+}  // namespace
+
+int sbm_ctx_get_params(const sbm_ctx* ctx, sbm_params* p) {
+  if (!ctx || !p) return SBM_ERR_ARG;
+  *p = ctx->p;
+  return SBM_OK;
+}
+
+int sbm_ctx_get_scalars(const sbm_ctx* ctx, sbm_scalars* s) {
+  if (!ctx || !s) return SBM_ERR_ARG;
+  *s = ctx->sc;
+  return SBM_OK;
+}
+
+int sbm_ctx_snapshot_size(sbm_ctx* ctx, size_t* bytes) {
+  if (!ctx || !bytes) return SBM_ERR_ARG;
+  const int nf = SBM_F_COUNT + (ctx->hk_kap ? kStepBufs : 0);
+  *bytes = kSnapHead + (size_t)nf * sizeof(double) * (size_t)ctx->g.nh;
+  return SBM_OK;
+}
+
+int sbm_ctx_snapshot(sbm_ctx* ctx, void* buf, size_t bytes) {
+  size_t need = 0;
+  if (!ctx || !buf || sbm_ctx_snapshot_size(ctx, &need) || bytes < need) return SBM_ERR_ARG;
+  double* sb[kStepBufs];
+  const int ns = step_bufs(ctx, sb);
+  SnapHeader h;
+  memset(&h, 0, sizeof(h));
+  memcpy(h.magic, kSnapMagic, sizeof(h.magic));
+  h.version = 1;
+  h.ny = ctx->g.ny;
+  h.nx = ctx->g.nx;
+  h.nz = ctx->g.nz;
+  h.nfields = SBM_F_COUNT + ns;
+  h.step_work = ns ? 1 : 0;
+  h.nh = ctx->g.nh;
+  h.p = ctx->p;
+  h.sc = ctx->sc;
+  char* out = static_cast<char*>(buf);
+  memset(out, 0, kSnapHead);
+  memcpy(out, &h, sizeof(h));
+  const size_t fb = sizeof(double) * (size_t)ctx->g.nh;
+  for (int i = 0; i < h.nfields; ++i) {
+    const double* src = i < SBM_F_COUNT ? ctx->f[i] : sb[i - SBM_F_COUNT];
+    SBM_CUDA_TRY(cudaMemcpyAsync(out + kSnapHead + (size_t)i * fb, src, fb,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  SBM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SBM_OK;
+}
+
+int sbm_ctx_restore(sbm_ctx* ctx, const void* buf, size_t bytes) {
+  if (!ctx || !buf || bytes < kSnapHead) return SBM_ERR_ARG;
+  SnapHeader h;
+  memcpy(&h, buf, sizeof(h));
+  if (memcmp(h.magic, kSnapMagic, sizeof(h.magic)) != 0 || h.version != 1 ||
+      h.ny != ctx->g.ny || h.nx != ctx->g.nx || h.nz != ctx->g.nz || h.nh != ctx->g.nh ||
+      h.nfields != SBM_F_COUNT + (h.step_work ? kStepBufs : 0) || h.p.tbl_n < 2 ||
+      h.p.tbl_n > SBM_TBL_MAX)
+    return SBM_ERR_ARG;
+  const size_t fb = sizeof(double) * (size_t)ctx->g.nh;
+  if (bytes < kSnapHead + (size_t)h.nfields * fb) return SBM_ERR_ARG;
+  SBM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  release_graphs(ctx);
+  ctx->p = h.p;
+  ctx->sc = h.sc;
+  if (h.step_work) {
+    int rc = ensure_step_work(ctx);
+    if (rc) return rc;
+  }
+  double* sb[kStepBufs];
+  step_bufs(ctx, sb);
+  const char* in = static_cast<const char*>(buf);
+  for (int i = 0; i < h.nfields; ++i) {
+    double* dst = i < SBM_F_COUNT ? ctx->f[i] : sb[i - SBM_F_COUNT];
+    SBM_CUDA_TRY(cudaMemcpyAsync(dst, in + kSnapHead + (size_t)i * fb, fb,
+                                 cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (ctx->hk_kap) {
+    int rc = upload_tables(ctx);
+    if (rc) return rc;
+  }
+  SBM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SBM_OK;
+}
+
 int sbm_setup_domain(sbm_ctx* ctx, const float* dist_p, const float* dist_e, double zeta,
                      double cnp0, double cne0, double cr, sbm_scalars* s) {
   if (!ctx || !dist_p || !dist_e || !(zeta > 0.0) || !(cr != 0.0)) return SBM_ERR_ARG;
@@ -498,6 +623,67 @@ int sbm_table_lookup(int64_t n, int sz, const double* cord, const double* vals, 
   return SBM_OK;
 }
 
+namespace {
+// Arguments of the level-set geometry entry points; false when the stacked
+// grid or the tunnel loop would leave the reference's arrays.
+bool ls_args_ok(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff, int nthick,
+                double tr, const double* ds) {
+  if (!vox || !ds || yo < 1 || xo < 1 || zo < 1 || yg < 1 || zg < 1 || xoff < 0 || nthick < 1)
+    return false;
+  if (yg > yo || zg > xo || !(tr == tr)) return false;
+  const int64_t xg = xoff + (int64_t)nthick * zo;
+  if (xg > (1 << 24)) return false;
+  return (xg - 1) + (int64_t)zo * (zg - 1) < (int64_t)zo * xo;
+}
+}  // namespace
+
+int sbm_ls_geometry(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
+                    int nthick, double tr, double* ds) {
+  if (!ls_args_ok(vox, yo, xo, zo, yg, zg, xoff, nthick, tr, ds)) return SBM_ERR_ARG;
+  const Geo g = make_geo(yg, xoff + nthick * zo, zg);
+  const size_t nv = (size_t)yo * xo * zo;
+  DevBufs b;
+  Stream st;
+  double *dv = b.get<double>(nv), *dd = b.get<double>(g.nh);
+  if (!dv || !dd || !st.s) return SBM_ERR_NOMEM;
+  SBM_CUDA_TRY(cudaMemcpyAsync(dv, vox, sizeof(double) * nv, cudaMemcpyHostToDevice, st.s));
+  int rc = ls_geometry_dev(st.s, g, dv, yo, xo, zo, xoff, tr, dd);
+  if (rc) return rc;
+  SBM_CUDA_TRY(cudaMemcpyAsync(ds, dd, sizeof(double) * g.nh, cudaMemcpyDeviceToHost, st.s));
+  SBM_CUDA_TRY(cudaStreamSynchronize(st.s));
+  return SBM_OK;
+}
+
+int sbm_ls_frontend(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
+                    int nthick, double tr, int ac_iters, int lit, double dt, double* ds) {
+  if (!ls_args_ok(vox, yo, xo, zo, yg, zg, xoff, nthick, tr, ds) || ac_iters < 0 || lit < 0)
+    return SBM_ERR_ARG;
+  const Geo g = make_geo(yg, xoff + nthick * zo, zg);
+  const size_t nv = (size_t)yo * xo * zo;
+  DevBufs b;
+  Stream st;
+  double *dv = b.get<double>(nv), *dd = b.get<double>(g.nh), *dg = b.get<double>(g.nh),
+         *dt2 = b.get<double>(g.nh);
+  if (!dv || !dd || !dg || !dt2 || !st.s) return SBM_ERR_NOMEM;
+  SBM_CUDA_TRY(cudaMemcpyAsync(dv, vox, sizeof(double) * nv, cudaMemcpyHostToDevice, st.s));
+  int rc = ls_frontend_dev(st.s, g, dv, yo, xo, zo, xoff, tr, ac_iters, lit, dt, dd, dg, dt2);
+  if (rc) return rc;
+  SBM_CUDA_TRY(cudaMemcpyAsync(ds, dd, sizeof(double) * g.nh, cudaMemcpyDeviceToHost, st.s));
+  SBM_CUDA_TRY(cudaStreamSynchronize(st.s));
+  return SBM_OK;
+}
+
+int sbm_ls_frontend_device(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
+                           int nthick, double tr, int ac_iters, int lit, double dt, double* ds,
+                           double* sg, double* tmp, void* stream) {
+  if (!ls_args_ok(vox, yo, xo, zo, yg, zg, xoff, nthick, tr, ds) || !sg || !tmp ||
+      ac_iters < 0 || lit < 0)
+    return SBM_ERR_ARG;
+  const Geo g = make_geo(yg, xoff + nthick * zo, zg);
+  return ls_frontend_dev(static_cast<cudaStream_t>(stream), g, vox, yo, xo, zo, xoff, tr,
+                         ac_iters, lit, dt, ds, sg, tmp);
+}
+
 int sbm_redist(int lit, int py, int px, int pz, double dt, const double* sg, double* f) {
   if (lit < 0 || py < 1 || px < 1 || pz < 1 || !sg || !f) return SBM_ERR_ARG;
   const Geo g = make_geo(py, px, pz);
@@ -508,6 +694,21 @@ int sbm_redist(int lit, int py, int px, int pz, double dt, const double* sg, dou
   SBM_CUDA_TRY(cudaMemcpyAsync(ds, sg, sizeof(double) * g.nh, cudaMemcpyHostToDevice, st.s));
   SBM_CUDA_TRY(cudaMemcpyAsync(df, f, sizeof(double) * g.nh, cudaMemcpyHostToDevice, st.s));
   int rc = redist_dev(st.s, g, ds, df, dt2, lit, dt);
+  if (rc) return rc;
+  SBM_CUDA_TRY(cudaMemcpyAsync(f, df, sizeof(double) * g.nh, cudaMemcpyDeviceToHost, st.s));
+  SBM_CUDA_TRY(cudaStreamSynchronize(st.s));
+  return SBM_OK;
+}
+
+int sbm_allen_cahn(int iters, int py, int px, int pz, double* f) {
+  if (iters < 0 || py < 1 || px < 1 || pz < 1 || !f) return SBM_ERR_ARG;
+  const Geo g = make_geo(py, px, pz);
+  DevBufs b;
+  Stream st;
+  double *df = b.get<double>(g.nh), *dt2 = b.get<double>(g.nh);
+  if (!df || !dt2 || !st.s) return SBM_ERR_NOMEM;
+  SBM_CUDA_TRY(cudaMemcpyAsync(df, f, sizeof(double) * g.nh, cudaMemcpyHostToDevice, st.s));
+  int rc = allen_cahn_dev(st.s, g, df, dt2, iters);
   if (rc) return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(f, df, sizeof(double) * g.nh, cudaMemcpyDeviceToHost, st.s));
   SBM_CUDA_TRY(cudaStreamSynchronize(st.s));

@@ -6,6 +6,8 @@
 //   AccDiff sweep (solid / electrolyte)         AccDiff_3D.f90:111-169, :185-243
 //   disconnected-region mask                    RM_UCNCT_3D.f90:78-82, :127-130
 //   sign function                               LevelSet_3D.f90:140-144
+//   Allen-Cahn pre-smoothing                    LevelSet_3D.f90:116-136
+//   reorient / tunnels / stacking               LevelSet_3D.f90:80-122
 //
 // Bit-exactness: every operation is an explicit IEEE round-to-nearest
 // intrinsic (__dadd_rn, __dmul_rn, __ddiv_rn, __dsqrt_rn), so no multiply-add
@@ -14,9 +16,11 @@
 //
 // Both sweeps are Jacobi (the reference computes the whole new field from
 // the old one: nf/f in ReDist, the WHERE block in AccDiff), so each
-// iteration is one kernel reading buffer A and writing buffer B.  Each is
-// FP64-ALU-bound on GB300 (about 40 FP64 operations per voxel against 24
-// bytes of traffic).
+// iteration is one kernel reading buffer A and writing buffer B.  They are
+// bound by GB300's FP64 pipe, not by HBM (a ReDist step moves 24 bytes per
+// voxel), so comparisons and clamps run on integer bit patterns and only
+// the roundings the reference's result depends on stay FP64 (the identities
+// are stated above godunov()).
 #include "sbm_internal.cuh"
 
 namespace sbm {
@@ -24,30 +28,72 @@ namespace sbm {
 namespace {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
-__device__ __forceinline__ double dmax0(double a) { return a > 0.0 ? a : 0.0; }
-__device__ __forceinline__ double dmaxd(double a, double b) { return a > b ? a : b; }
+
+// GB300 issues FP64 arithmetic at a small fraction of its FP32 / integer
+// rate, and these sweeps are bound by that pipe, so the kernels below keep
+// only the FP64 operations whose rounding the reference's result depends
+// on; comparisons, clamps at zero and sign flips run as integer operations
+// on the bit patterns.  The results are unchanged for finite fields:
+//
+// * max(RN(fc - a), RN(fc - b)) = RN(fc - min(a, b)) and
+//   max(RN(a - fc), RN(b - fc)) = RN(max(a, b) - fc), since x -> RN(fc - x)
+//   and x -> RN(x - fc) are monotone (RN = round to nearest even);
+// * RN(-x) = -RN(x), so MAX(-bg, 0) with bg = f(i+1) - f(i) is
+//   MAX(RN(f(i) - f(i+1)), 0);
+// * max(RN(u*u), RN(v*v)) = RN(max(u, v)^2) for u, v >= 0.
+//
+// Hence each direction's MAX(MAX(.,0)**2, MAX(.,0)**2) of AbsGrd3DUW_XYZ is
+// one subtraction and one square.
+
+// Order-preserving integer key of a non-NaN double.
+__device__ __forceinline__ long long okey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double imin(double a, double b) { return okey(a) <= okey(b) ? a : b; }
+__device__ __forceinline__ double imax(double a, double b) { return okey(a) >= okey(b) ? a : b; }
+// MAX(x, 0.0d0) for non-NaN x (a zero result is +0; it is only squared).
+__device__ __forceinline__ double pos0(double x) { return __double_as_longlong(x) > 0 ? x : 0.0; }
 
 // AbsGrd3DUW_XYZ at interior cell c (LevelSet_3D.f90:294-317).
 __device__ __forceinline__ double godunov(const double* __restrict__ f, const Geo& g, int64_t c,
                                           double s) {
+  const long long sb = __double_as_longlong(s);
+  if ((sb << 1) == 0) return 0.0;  // sg == 0.0
   const double fc = f[c];
-  const double ag = __dsub_rn(fc, f[c - 1]);
-  const double bg = __dsub_rn(f[c + 1], fc);
-  const double cg = __dsub_rn(fc, f[c - g.sx]);
-  const double dg = __dsub_rn(f[c + g.sx], fc);
-  const double eg = __dsub_rn(fc, f[c - g.sz]);
-  const double fg = __dsub_rn(f[c + g.sz], fc);
-  if (s == 0.0) return 0.0;
-  double a, b, cc, d, e, ff;
-  if (s > 0.0) {
-    a = dmax0(ag); b = dmax0(-bg); cc = dmax0(cg); d = dmax0(-dg); e = dmax0(eg); ff = dmax0(-fg);
-  } else {
-    a = dmax0(-ag); b = dmax0(bg); cc = dmax0(-cg); d = dmax0(dg); e = dmax0(-eg); ff = dmax0(fg);
+  const double ym = f[c - 1], yp = f[c + 1], xm = f[c - g.sx], xp = f[c + g.sx];
+  const double zm = f[c - g.sz], zp = f[c + g.sz];
+  double a, b, e;
+  if (sb > 0) {  // MAX(ag,0), MAX(-bg,0) per direction
+    a = pos0(__dsub_rn(fc, imin(ym, yp)));
+    b = pos0(__dsub_rn(fc, imin(xm, xp)));
+    e = pos0(__dsub_rn(fc, imin(zm, zp)));
+  } else {       // MAX(-ag,0), MAX(bg,0) per direction
+    a = pos0(__dsub_rn(imax(ym, yp), fc));
+    b = pos0(__dsub_rn(imax(xm, xp), fc));
+    e = pos0(__dsub_rn(imax(zm, zp), fc));
   }
-  const double m1 = dmaxd(__dmul_rn(a, a), __dmul_rn(b, b));
-  const double m2 = dmaxd(__dmul_rn(cc, cc), __dmul_rn(d, d));
-  const double m3 = dmaxd(__dmul_rn(e, e), __dmul_rn(ff, ff));
-  return __dsqrt_rn(__dadd_rn(__dadd_rn(m1, m2), m3));
+  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(e, e)));
+}
+
+// RN(s*x) with the common s = +-1 as a sign flip.
+__device__ __forceinline__ double mul_sign(double s, double x) {
+  const long long sb = __double_as_longlong(s);
+  if (sb == 0x3ff0000000000000LL) return x;
+  if (sb == (long long)0xbff0000000000000ULL) return -x;
+  return __dmul_rn(s, x);
+}
+
+// (v*f > 0.0) of the reference: false for a zero factor or opposite signs;
+// for two normal factors with biased exponents summing to at least 972 the
+// product is at least 2^-1074 and rounds to a positive value; anything else
+// (possible underflow, Inf, NaN) takes the FP64 product.
+__device__ __forceinline__ bool prod_pos(double v, double f) {
+  const long long a = __double_as_longlong(v), b = __double_as_longlong(f);
+  if ((a << 1) == 0 || (b << 1) == 0 || (a ^ b) < 0) return false;
+  const int ea = (int)((a >> 52) & 0x7ff), eb = (int)((b >> 52) & 0x7ff);
+  if (ea != 0 && eb != 0 && ea != 0x7ff && eb != 0x7ff && ea + eb >= 972) return true;
+  return __dmul_rn(v, f) > 0.0;
 }
 
 // One ReDist3D_XYZ iteration over every cell of the padded array
@@ -66,9 +112,46 @@ __global__ void __launch_bounds__(256) k_redist(Geo g, const double* __restrict_
   const int64_t cc = g.ix(clampi(i, 1, g.ny), clampi(j, 1, g.nx), clampi(k, 1, g.nz));
   const double gf = godunov(f, g, cc, sg[cc]);
   const double fc = f[c], s = sg[c];
-  double v = __dadd_rn(fc, __dmul_rn(__dmul_rn(s, __dsub_rn(1.0, gf)), dt));
-  if (!(__dmul_rn(v, fc) > 0.0)) v = __dadd_rn(fc, __dmul_rn(small, s));
+  double v = __dadd_rn(fc, __dmul_rn(mul_sign(s, __dsub_rn(1.0, gf)), dt));
+  if (!prod_pos(v, fc)) v = __dadd_rn(fc, mul_sign(s, small));
   nf[c] = v;
+}
+
+// One Allen-Cahn pre-smoothing step (LevelSet_3D.f90:124-136) over every
+// cell of the padded array: the new value of the nearest interior cell, so
+// the ghosts leave as the NoGrdBc3D copies; neighbours are read at clamped
+// indices, which are exactly the zero-gradient ghosts the reference fills
+// before the loop and after every step.  step = 0 only fills the ghosts.
+//   sgF = 2*d*(1.0-d)*(1.0-2*d) - 0.64*(yp + ym + xp + xm + zp + zm - 6*d)
+//   d   = d - 0.05*sgF            (0.64, 0.05 REAL(4); no FMA contraction)
+__global__ void __launch_bounds__(256) k_allen_cahn(Geo g, const double* __restrict__ f,
+                                                    double* __restrict__ nf, int step) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > g.ny + 1 || j > g.nx + 1) return;
+  const int ci = clampi(i, 1, g.ny), cj = clampi(j, 1, g.nx), ck = clampi(k, 1, g.nz);
+  const double d = f[g.ix(ci, cj, ck)];
+  double v = d;
+  if (step) {
+    const double c064 = (double)0.64f, c005 = (double)0.05f;
+    double nb = __dadd_rn(f[g.ix(clampi(ci + 1, 1, g.ny), cj, ck)],
+                          f[g.ix(clampi(ci - 1, 1, g.ny), cj, ck)]);
+    nb = __dadd_rn(nb, f[g.ix(ci, clampi(cj + 1, 1, g.nx), ck)]);
+    nb = __dadd_rn(nb, f[g.ix(ci, clampi(cj - 1, 1, g.nx), ck)]);
+    nb = __dadd_rn(nb, f[g.ix(ci, cj, clampi(ck + 1, 1, g.nz))]);
+    nb = __dadd_rn(nb, f[g.ix(ci, cj, clampi(ck - 1, 1, g.nz))]);
+    nb = __dsub_rn(nb, __dmul_rn(6.0, d));
+    // 2*d exactly: one more in the exponent of a normal d below 2^1023
+    const long long db = __double_as_longlong(d);
+    const int de = (int)((db >> 52) & 0x7ff);
+    const double dd = (de != 0 && de < 0x7fe) ? __longlong_as_double(db + (1LL << 52))
+                                               : __dmul_rn(2.0, d);
+    const double w = __dmul_rn(__dmul_rn(dd, __dsub_rn(1.0, d)), __dsub_rn(1.0, dd));
+    const double sg = __dsub_rn(w, __dmul_rn(c064, nb));
+    v = __dsub_rn(d, __dmul_rn(c005, sg));
+  }
+  nf[g.ix(i, j, k)] = v;
 }
 
 struct AccArgs {
@@ -181,6 +264,128 @@ int redist_dev(cudaStream_t s, const Geo& g, const double* sg, double* f, double
   if (a != f) SBM_CUDA_TRY(cudaMemcpyAsync(f, a, sizeof(double) * g.nh, cudaMemcpyDeviceToDevice, s));
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
+}
+
+// `iters` Allen-Cahn steps on a device field (ghosts ignored on input,
+// zero-gradient on output); tmp scratch of the same size.
+int allen_cahn_dev(cudaStream_t s, const Geo& g, double* f, double* tmp, int iters) {
+  const dim3 blk(32, 8, 1);
+  const dim3 grd((g.ny + 2 + 31) / 32, (g.nx + 2 + 7) / 8, g.nz + 2);
+  double* a = f;
+  double* b = tmp;
+  for (int m = 0; m < (iters > 0 ? iters : 1); ++m) {
+    k_allen_cahn<<<grd, blk, 0, s>>>(g, a, b, iters > 0 ? 1 : 0);
+    double* t = a;
+    a = b;
+    b = t;
+  }
+  SBM_LAUNCHED(iters > 0 ? iters : 1);
+  if (a != f) SBM_CUDA_TRY(cudaMemcpyAsync(f, a, sizeof(double) * g.nh, cudaMemcpyDeviceToDevice, s));
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
+namespace {
+
+// The stacked voxel field dsF of LevelSet_3D.f90:80-122 as a gather, one
+// thread per cell of the halo-padded (yg+2)(xg+2)(zg+2) array (ghosts take
+// the nearest interior value: the NoGrdBc3D call of :122).
+//
+// The reference builds it in three passes over TmpB(yo,zo,xo):
+//   reorient   TmpB(i,kk,jj) = TmpA(i,jj,zo-kk+1)                   (:82-84)
+//   tunnels    TmpB(i,j,k) = 0 for j = 1..xg, k = 1..zg where
+//              |(i,k)-(1,zg)| < tr or |(i,k)-(yg,1)| < tr             (:87-106)
+//   stack      dsF(:,xoff+t*zo+r,:) = TmpB(:, r or zo+1-r, 1:zg) for
+//              thickness t (even t straight, odd t mirrored)          (:109-119)
+// The tunnel loop runs j up to xg while TmpB's second extent is zo, so with
+// Fortran's column-major storage its write to (i,j,k) lands on element
+// (i, MOD(j-1+zo*(k-1), zo)+1, (j-1+zo*(k-1))/zo+1): a TmpB element with
+// column index J = (b2-1) + zo*(b3-1) is zeroed when some loop point
+// (j,k) has j-1 + zo*(k-1) = J and meets the tunnel test for its own k.
+// The gather tests exactly those k (at most ceil(xg/zo)+1 of them).
+struct StackArgs {
+  const double* vox;     // TmpA(yo,xo,zo), Fortran order
+  int yo, xo, zo;
+  int xoff, xg;          // leading zero columns; xg = xoff + nthick*zo
+  double tr;             // tunnel radius
+};
+
+__device__ __forceinline__ bool in_tunnel(int i, int k, int yg, int zg, double tr) {
+  const double a = __dsub_rn((double)i, 1.0), b = __dsub_rn((double)k, (double)zg);
+  if (__dsqrt_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b))) < tr) return true;
+  const double c = __dsub_rn((double)i, (double)yg), d = __dsub_rn((double)k, 1.0);
+  return __dsqrt_rn(__dadd_rn(__dmul_rn(c, c), __dmul_rn(d, d))) < tr;
+}
+
+__global__ void __launch_bounds__(256) k_ls_stack(Geo g, StackArgs a, double* __restrict__ ds) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > g.ny + 1 || j > g.nx + 1) return;
+  const int ci = clampi(i, 1, g.ny), cj = clampi(j, 1, g.nx), ck = clampi(k, 1, g.nz);
+  double v = 0.0;
+  if (cj > a.xoff) {
+    const int t = (cj - a.xoff - 1) / a.zo, r = (cj - a.xoff - 1) - t * a.zo;
+    const int b2 = (t & 1) ? a.zo - r : r + 1;  // TmpB second index
+    const int b3 = ck;                           // TmpB third index
+    const int64_t J = (int64_t)(b2 - 1) + (int64_t)a.zo * (b3 - 1);
+    int64_t mlo = J - (a.xg - 1);
+    mlo = mlo <= 0 ? 0 : (mlo + a.zo - 1) / a.zo;
+    int64_t mhi = J / a.zo;
+    if (mhi > g.nz - 1) mhi = g.nz - 1;
+    bool zero = false;
+    for (int64_t m = mlo; m <= mhi && !zero; ++m) zero = in_tunnel(ci, (int)m + 1, g.ny, g.nz, a.tr);
+    if (!zero)
+      v = a.vox[(int64_t)(ci - 1) + (int64_t)a.yo * ((int64_t)(b3 - 1) + (int64_t)a.xo * (a.zo - b2))];
+  }
+  ds[g.ix(i, j, k)] = v;
+}
+
+// Sign function of the pre-smoothed field (LevelSet_3D.f90:140-144) over
+// every cell, and the zero start of the reinitialisation (:147).
+__global__ void k_ls_sign(int64_t n, double* __restrict__ d, double* __restrict__ sg) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    sg[c] = d[c] > 0.5 ? 1.0 : -1.0;
+    d[c] = 0.0;
+  }
+}
+
+}  // namespace
+
+// dsF of LevelSet_3D.f90:80-122 from device voxels; g is the (yg, xg, zg)
+// grid, xg = xoff + nthick*zo.
+int ls_geometry_dev(cudaStream_t s, const Geo& g, const double* vox, int yo, int xo, int zo,
+                    int xoff, double tr, double* ds) {
+  StackArgs a;
+  a.vox = vox;
+  a.yo = yo;
+  a.xo = xo;
+  a.zo = zo;
+  a.xoff = xoff;
+  a.xg = g.nx;
+  a.tr = tr;
+  const dim3 blk(32, 8, 1);
+  const dim3 grd((g.ny + 2 + 31) / 32, (g.nx + 2 + 7) / 8, g.nz + 2);
+  k_ls_stack<<<grd, blk, 0, s>>>(g, a, ds);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
+// One frame of LevelSet_3D.f90:80-150: stacked field, `ac_iters` Allen-Cahn
+// steps, sign, `lit` reinitialisation steps from zero.  The distance lands
+// in ds; sg and tmp are scratch of the same size.
+int ls_frontend_dev(cudaStream_t s, const Geo& g, const double* vox, int yo, int xo, int zo,
+                    int xoff, double tr, int ac_iters, int lit, double dt, double* ds, double* sg,
+                    double* tmp) {
+  int rc = ls_geometry_dev(s, g, vox, yo, xo, zo, xoff, tr, ds);
+  if (!rc && ac_iters > 0) rc = allen_cahn_dev(s, g, ds, tmp, ac_iters);
+  if (rc) return rc;
+  k_ls_sign<<<4 * 152, 256, 0, s>>>(g.nh, ds, sg);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return redist_dev(s, g, sg, ds, tmp, lit, dt);
 }
 
 // AccDiff iterations 2..term on device buffers; cn in/out (ghosts included),

@@ -21,6 +21,7 @@ is missing the import of a ``Context`` fails.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 from pathlib import Path
 
@@ -120,6 +121,11 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_ctx_set_tuning": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]),
         "sbm_ctx_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "sbm_ctx_sync": (C.c_int, [vp]),
+        "sbm_ctx_get_params": (C.c_int, [vp, C.POINTER(Params)]),
+        "sbm_ctx_get_scalars": (C.c_int, [vp, C.POINTER(Scalars)]),
+        "sbm_ctx_snapshot_size": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
+        "sbm_ctx_snapshot": (C.c_int, [vp, vp, C.c_size_t]),
+        "sbm_ctx_restore": (C.c_int, [vp, vp, C.c_size_t]),
         "sbm_upload": (C.c_int, [vp, C.c_int, dp, C.c_int]),
         "sbm_download": (C.c_int, [vp, C.c_int, dp, C.c_int]),
         "sbm_field_ptr": (C.c_int, [vp, C.c_int, C.POINTER(dp)]),
@@ -142,6 +148,13 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
                                       C.POINTER(C.c_float), C.c_int, C.c_int, C.c_int, fp]),
         "sbm_redist": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]),
         "sbm_accdiff": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, C.c_int]),
+        "sbm_allen_cahn": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, dp]),
+        "sbm_ls_geometry": (C.c_int, [dp] + [C.c_int] * 7 + [C.c_double, dp]),
+        "sbm_ls_frontend": (C.c_int, [dp] + [C.c_int] * 7 + [C.c_double, C.c_int, C.c_int,
+                                                              C.c_double, dp]),
+        "sbm_ls_frontend_device": (C.c_int, [C.c_void_p] + [C.c_int] * 7 +
+                                   [C.c_double, C.c_int, C.c_int, C.c_double] +
+                                   [C.c_void_p] * 4),
         "sbm_redist_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
         "sbm_rm_mask": (C.c_int, [i64, dp, dp, dp]),
@@ -208,6 +221,38 @@ def launch_count() -> int:
     return int(load_library().sbm_launch_count())
 
 
+CKPT_MAGIC = b"SBMCKPT1"
+
+
+def write_checkpoint(path, blob, meta: dict) -> Path:
+    """Checkpoint file: 8-byte magic, u64 length of the JSON meta, the meta,
+    zero padding to a multiple of 64 bytes, the snapshot bytes.  Written to a
+    temporary name and renamed, so a crash leaves the previous file whole."""
+    path = Path(path)
+    js = json.dumps(meta, sort_keys=True).encode()
+    head = CKPT_MAGIC + np.uint64(len(js)).astype("<u8").tobytes() + js
+    head += b"\0" * (-len(head) % 64)
+    tmp = path.with_name(path.name + ".tmp")
+    with open(tmp, "wb") as f:
+        f.write(head)
+        f.write(memoryview(np.ascontiguousarray(blob, dtype=np.uint8)))
+    os.replace(tmp, path)
+    return path
+
+
+def read_checkpoint(path) -> tuple[dict, np.ndarray]:
+    """(meta, snapshot bytes) of a checkpoint file."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    if raw.size < 16 or raw[:8].tobytes() != CKPT_MAGIC:
+        raise ValueError(f"{path}: not a checkpoint file")
+    n = int(raw[8:16].view("<u8")[0])
+    if 16 + n > raw.size:
+        raise ValueError(f"{path}: truncated checkpoint")
+    meta = json.loads(raw[16:16 + n].tobytes())
+    start = 16 + n + (-(16 + n) % 64)
+    return meta, raw[start:]
+
+
 class Context:
     """One device-resident SBM domain of ny x nx x nz interior voxels."""
 
@@ -265,6 +310,40 @@ class Context:
 
     def sync(self) -> None:
         _check(self.lib.sbm_ctx_sync(self._h), "sbm_ctx_sync")
+
+    def scalars(self) -> dict:
+        s = Scalars()
+        _check(self.lib.sbm_ctx_get_scalars(self._h, C.byref(s)), "sbm_ctx_get_scalars")
+        return s.as_dict()
+
+    # -- checkpoint / resume
+    def snapshot(self) -> np.ndarray:
+        """The context's state (parameters, scalars, every FP64 field a later
+        step reads) as a host byte array; see sbm_ctx_snapshot."""
+        n = C.c_size_t(0)
+        _check(self.lib.sbm_ctx_snapshot_size(self._h, C.byref(n)), "sbm_ctx_snapshot_size")
+        buf = np.empty(n.value, dtype=np.uint8)
+        _check(self.lib.sbm_ctx_snapshot(self._h, buf.ctypes.data, n.value), "sbm_ctx_snapshot")
+        return buf
+
+    def restore(self, buf) -> None:
+        """Loads a snapshot of a context with the same grid."""
+        buf = np.ascontiguousarray(np.frombuffer(buf, dtype=np.uint8))
+        _check(self.lib.sbm_ctx_restore(self._h, buf.ctypes.data, buf.size), "sbm_ctx_restore")
+        p = Params()
+        _check(self.lib.sbm_ctx_get_params(self._h, C.byref(p)), "sbm_ctx_get_params")
+        self.params = p
+
+    def save(self, path, **meta) -> Path:
+        """Writes a checkpoint file: the snapshot plus the caller's run
+        counters (``meta``, e.g. iteration, time, frame) as JSON."""
+        return write_checkpoint(path, self.snapshot(), meta)
+
+    def load(self, path) -> dict:
+        """Restores a checkpoint file written by ``save``; returns its meta."""
+        meta, blob = read_checkpoint(path)
+        self.restore(blob)
+        return meta
 
     # -- fields
     def upload(self, field, a, haloed: bool = True) -> None:
@@ -485,6 +564,42 @@ def redist3d_xyz(lit: int, sg, f, dt: float = 1.0e-1) -> np.ndarray:
     py, px, pz = (s - 2 for s in sg.shape)
     _check(lib.sbm_redist(lit, py, px, pz, dt, _dptr(sg), _dptr(f)), "sbm_redist")
     return f
+
+
+def allen_cahn(iters: int, f) -> np.ndarray:
+    """Allen-Cahn pre-smoothing (LevelSet_3D.f90:116-136) on the GPU;
+    returns the new halo-padded field (ghosts zero-gradient)."""
+    lib = load_library()
+    f = _f64(f).copy(order="F")
+    py, px, pz = (s - 2 for s in f.shape)
+    _check(lib.sbm_allen_cahn(iters, py, px, pz, _dptr(f)), "sbm_allen_cahn")
+    return f
+
+
+def ls_geometry(vox, yg: int, zg: int, xoff: int, nthick: int, tr: float) -> np.ndarray:
+    """Stacked voxel field of LevelSet_3D.f90:80-122 on the GPU from
+    TmpA = vox (yo, xo, zo); returns the halo-padded (yg+2, xg+2, zg+2)
+    field, xg = xoff + nthick*zo."""
+    lib = load_library()
+    vox = _f64(vox)
+    yo, xo, zo = vox.shape
+    ds = np.zeros((yg + 2, xoff + nthick * zo + 2, zg + 2), order="F")
+    _check(lib.sbm_ls_geometry(_dptr(vox), yo, xo, zo, yg, zg, xoff, nthick, float(tr),
+                               _dptr(ds)), "sbm_ls_geometry")
+    return ds
+
+
+def ls_frontend(vox, yg: int, zg: int, xoff: int, nthick: int, tr: float, ac_iters: int = 50,
+                lit: int = 175, dt: float = 1.0e-1) -> np.ndarray:
+    """One frame of the LevelSet_3D front end (LevelSet_3D.f90:80-150) on the
+    GPU; returns the halo-padded distance."""
+    lib = load_library()
+    vox = _f64(vox)
+    yo, xo, zo = vox.shape
+    ds = np.zeros((yg + 2, xoff + nthick * zo + 2, zg + 2), order="F")
+    _check(lib.sbm_ls_frontend(_dptr(vox), yo, xo, zo, yg, zg, xoff, nthick, float(tr),
+                               ac_iters, lit, float(dt), _dptr(ds)), "sbm_ls_frontend")
+    return ds
 
 
 def accdiff(psi, cn, term: int = 1501, dirichlet_x: int = 1) -> np.ndarray:

@@ -51,6 +51,21 @@ MODULE sbm_capi
       IMPORT :: C_INT, C_PTR
       TYPE(C_PTR), VALUE :: ctx
     END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_ctx_snapshot_size(ctx, bytes) BIND(C, NAME='sbm_ctx_snapshot_size')
+      IMPORT :: C_INT, C_PTR, C_SIZE_T
+      TYPE(C_PTR), VALUE :: ctx
+      INTEGER(C_SIZE_T), INTENT(OUT) :: bytes
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_ctx_snapshot(ctx, buf, bytes) BIND(C, NAME='sbm_ctx_snapshot')
+      IMPORT :: C_INT, C_PTR, C_SIZE_T
+      TYPE(C_PTR), VALUE :: ctx, buf
+      INTEGER(C_SIZE_T), VALUE :: bytes
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_ctx_restore(ctx, buf, bytes) BIND(C, NAME='sbm_ctx_restore')
+      IMPORT :: C_INT, C_PTR, C_SIZE_T
+      TYPE(C_PTR), VALUE :: ctx, buf
+      INTEGER(C_SIZE_T), VALUE :: bytes
+    END FUNCTION
     INTEGER(C_INT) FUNCTION sbm_upload(ctx, field, h, haloed) BIND(C, NAME='sbm_upload')
       IMPORT :: C_INT, C_PTR, C_DOUBLE
       TYPE(C_PTR), VALUE :: ctx
@@ -103,6 +118,34 @@ MODULE sbm_capi
       REAL(C_DOUBLE), VALUE :: dt
       REAL(C_DOUBLE), INTENT(IN) :: sg(*)
       REAL(C_DOUBLE), INTENT(INOUT) :: f(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_allen_cahn(iters, py, px, pz, f) BIND(C, NAME='sbm_allen_cahn')
+      IMPORT :: C_INT, C_DOUBLE
+      INTEGER(C_INT), VALUE :: iters, py, px, pz
+      REAL(C_DOUBLE), INTENT(INOUT) :: f(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_ls_geometry(vox, yo, xo, zo, yg, zg, xoff, nthick, tr, ds) &
+        BIND(C, NAME='sbm_ls_geometry')
+      IMPORT :: C_INT, C_DOUBLE
+      REAL(C_DOUBLE), INTENT(IN) :: vox(*)
+      INTEGER(C_INT), VALUE :: yo, xo, zo, yg, zg, xoff, nthick
+      REAL(C_DOUBLE), VALUE :: tr
+      REAL(C_DOUBLE), INTENT(OUT) :: ds(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_ls_frontend(vox, yo, xo, zo, yg, zg, xoff, nthick, tr, &
+        ac_iters, lit, dt, ds) BIND(C, NAME='sbm_ls_frontend')
+      IMPORT :: C_INT, C_DOUBLE
+      REAL(C_DOUBLE), INTENT(IN) :: vox(*)
+      INTEGER(C_INT), VALUE :: yo, xo, zo, yg, zg, xoff, nthick, ac_iters, lit
+      REAL(C_DOUBLE), VALUE :: tr, dt
+      REAL(C_DOUBLE), INTENT(OUT) :: ds(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_ls_frontend_device(vox, yo, xo, zo, yg, zg, xoff, nthick, tr, &
+        ac_iters, lit, dt, ds, sg, tmp, stream) BIND(C, NAME='sbm_ls_frontend_device')
+      IMPORT :: C_INT, C_DOUBLE, C_PTR
+      TYPE(C_PTR), VALUE :: vox, ds, sg, tmp, stream
+      INTEGER(C_INT), VALUE :: yo, xo, zo, yg, zg, xoff, nthick, ac_iters, lit
+      REAL(C_DOUBLE), VALUE :: tr, dt
     END FUNCTION
     INTEGER(C_INT) FUNCTION sbm_accdiff(py, px, pz, psi, cn, term, dirichlet_x) &
          BIND(C, NAME='sbm_accdiff')

@@ -159,6 +159,24 @@ int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta
 /* The context's CUDA stream as an opaque handle (cudaStream_t). */
 int sbm_ctx_stream(sbm_ctx* ctx, void** stream);
 int sbm_ctx_sync(sbm_ctx* ctx);
+/* The context's parameters and electrochemical scalars (host copies). */
+int sbm_ctx_get_params(const sbm_ctx* ctx, sbm_params* p);
+int sbm_ctx_get_scalars(const sbm_ctx* ctx, sbm_scalars* s);
+
+/* Checkpoint / resume (no counterpart in the reference, whose periodic
+ * REAL(4) dumps are outputs only).  A snapshot holds the parameters, the
+ * electrochemical scalars and every halo-padded FP64 field a later solve or
+ * time step reads: the 13 public fields and, after sbm_setup_domain, the 12
+ * step buffers (operator half coefficients, Dab, mu, mobility, reaction
+ * coefficients, rate constants, previous phP / phE).  A context restored
+ * from it continues bit for bit like the one it was taken from.  The buffer
+ * is host memory of sbm_ctx_snapshot_size bytes (pinned memory copies
+ * fastest); restore requires the same grid and rejects any other buffer
+ * with SBM_ERR_ARG.  The run's own counters (iteration, time, frame) are the
+ * caller's to keep beside it. */
+int sbm_ctx_snapshot_size(sbm_ctx* ctx, size_t* bytes);
+int sbm_ctx_snapshot(sbm_ctx* ctx, void* buf, size_t bytes);
+int sbm_ctx_restore(sbm_ctx* ctx, const void* buf, size_t bytes);
 
 /* Host <-> device copies of a field.  `haloed` = 1: h has the halo-padded
  * shape (ny+2)(nx+2)(nz+2); 0: interior shape ny*nx*nz (ghosts untouched). */
@@ -241,6 +259,45 @@ int sbm_table_lookup(int64_t n, int sz, const double* cord, const double* vals,
  * halo-padded.  Bit-exact with the reference arithmetic. */
 int sbm_redist(int lit, int py, int px, int pz, double dt,
                const double* sg, double* f);
+
+/* Allen-Cahn pre-smoothing of the stacked voxel field before the sign and
+ * the reinitialisation, LevelSet_3D.f90:116-136: NoGrdBc3D, then `iters`
+ * steps (the reference runs 50) of
+ *   sgF = 2 f (1 - f)(1 - 2 f) - 0.64 (sum of the 6 neighbours - 6 f),
+ *   f = f - 0.05 sgF   (0.64, 0.05 REAL(4)), NoGrdBc3D,
+ * in place on the halo-padded (py+2)(px+2)(pz+2) array; bit-exact. */
+int sbm_allen_cahn(int iters, int py, int px, int pz, double* f);
+
+/* The stacked voxel field of LevelSet_3D.f90:80-122 for one tunnel radius:
+ * vox = TmpA(yo,xo,zo) (Fortran order) is reoriented (TmpB(i,k,j) =
+ * TmpA(i,j,zo-k+1)), cylindrical tunnels of radius tr about (i,k) = (1,zg)
+ * and (yg,1) are zeroed by the reference's loop over j = 1..xg (its writes
+ * past TmpB's second extent zo land where column-major storage puts them,
+ * :87-106), and nthick thicknesses of zo columns (even ones straight, odd
+ * ones mirrored) are stacked after xoff zero columns (:109-119; the
+ * reference: yo,xo,zo = 500,520,170, yg = 93, zg = 160, xoff = 50,
+ * nthick = 4, tr = TuRd(3..13)).  ds: the halo-padded
+ * (yg+2)(xg+2)(zg+2) field, xg = xoff + nthick*zo, ghosts zero-gradient
+ * (:122).  Requires yg <= yo, zg <= xo and (xg-1) + zo*(zg-1) < zo*xo (the
+ * tunnel loop stays inside TmpB).  Bit-exact. */
+int sbm_ls_geometry(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
+                    int nthick, double tr, double* ds);
+
+/* One frame of the LevelSet_3D front end on the GPU (:80-150): the stacked
+ * field above, ac_iters Allen-Cahn steps (50), sign (> 0.5 -> +1, else -1,
+ * ghosts included), lit reinitialisation steps (175) of time step dt (0.1)
+ * from zero.  ds: the halo-padded distance (OutPut3D writes its interior).
+ * Bit-exact with the reference arithmetic. */
+int sbm_ls_frontend(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
+                    int nthick, double tr, int ac_iters, int lit, double dt, double* ds);
+
+/* sbm_ls_frontend on caller-owned DEVICE buffers: vox (yo*xo*zo doubles),
+ * ds, sg, tmp (each (yg+2)(xg+2)(zg+2) doubles; ds receives the distance,
+ * sg the sign field, tmp is scratch).  Enqueued on `stream` (cudaStream_t,
+ * NULL = the default stream); returns without waiting. */
+int sbm_ls_frontend_device(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
+                           int nthick, double tr, int ac_iters, int lit, double dt, double* ds,
+                           double* sg, double* tmp, void* stream);
 
 /* One phase of the AccDiff_3D connectivity sweep, AccDiff_3D.f90:111-169
  * (solid, dirichlet_x = 1: Dirichlet 1 at x = px+1) and :185-243

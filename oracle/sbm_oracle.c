@@ -183,6 +183,93 @@ void orc_absgrd(int py, int px, int pz, const double* sg, const double* f, doubl
       }
 }
 
+/* Allen-Cahn pre-smoothing of the stacked voxel field, LS:116-136:
+ * NoGrdBc3D, then `iters` times
+ *   sgF = 2*dsF*(1.0-dsF)*(1.0-2*dsF) - 0.64*(six neighbours - 6*dsF)
+ *   dsF = dsF - 0.05*sgF                       (interior, array semantics)
+ *   NoGrdBc3D
+ * with the REAL(4) literals 0.64 and 0.05 promoted to REAL(8) and the
+ * Fortran left-to-right evaluation order. */
+void orc_allen_cahn(int iters, int py, int px, int pz, double* f) {
+  const int ny = py, nx = px, nz = pz;
+  const size_t n = (size_t)(ny + 2) * (nx + 2) * (nz + 2);
+  const double c064 = (double)0.64f, c005 = (double)0.05f;
+  double* s = (double*)malloc(n * sizeof(double));
+  if (!s) return;
+  orc_nogrdbc(py, px, pz, f);
+  for (int it = 0; it < iters; ++it) {
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= nx; ++j)
+        for (int i = 1; i <= ny; ++i) {
+          const double d = f[IX(i, j, k)];
+          const double lap = f[IX(i + 1, j, k)] + f[IX(i - 1, j, k)] + f[IX(i, j + 1, k)] +
+                             f[IX(i, j - 1, k)] + f[IX(i, j, k + 1)] + f[IX(i, j, k - 1)] -
+                             6 * d;
+          s[IX(i, j, k)] = 2 * d * (1.0 - d) * (1.0 - 2 * d) - c064 * lap;
+        }
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= nx; ++j)
+        for (int i = 1; i <= ny; ++i) f[IX(i, j, k)] = f[IX(i, j, k)] - c005 * s[IX(i, j, k)];
+    orc_nogrdbc(py, px, pz, f);
+  }
+  free(s);
+}
+
+/* The stacked voxel field, LS:80-122, literally: TmpB(yo,zo,xo) from the
+ * reorientation loop (:82-84), the tunnel loop over k = 1..zg, j = 1..xg,
+ * i = 1..yg writing TmpB(i,j,k) through its column-major address
+ * (i-1) + yo*((j-1) + zo*(k-1)) even where j exceeds zo (:87-106), the
+ * stacking of nthick thicknesses after xoff zero columns (:109-119: the
+ * reference's 4 = straight, mirrored, copy of the first, copy of the second),
+ * then NoGrdBc3D (:122).  ds is the halo-padded (yg+2)(xg+2)(zg+2) array,
+ * xg = xoff + nthick*zo.  Returns 0, or -1 when an argument is out of range
+ * or the tunnel loop would leave TmpB. */
+int orc_ls_geometry(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
+                    int nthick, double tr, double* ds) {
+  const long xg = xoff + (long)nthick * zo;
+  if (yo < 1 || xo < 1 || zo < 1 || yg < 1 || zg < 1 || xoff < 0 || nthick < 1 || yg > yo ||
+      zg > xo || (xg - 1) + (long)zo * (zg - 1) >= (long)zo * xo)
+    return -1;
+  const size_t nb = (size_t)yo * zo * xo;
+  double* tb = (double*)malloc(nb * sizeof(double));
+  if (!tb) return -1;
+  /* TmpB(1:yo,k,1:xo) = TmpA(1:yo,1:xo,zo-k+1) */
+  for (long k = 1; k <= zo; ++k)
+    for (long j = 1; j <= xo; ++j)
+      for (long i = 1; i <= yo; ++i)
+        tb[(i - 1) + yo * ((k - 1) + zo * (j - 1))] = vox[(i - 1) + yo * ((j - 1) + xo * (zo - k))];
+  for (long k = 1; k <= zg; ++k)
+    for (long j = 1; j <= xg; ++j)
+      for (long i = 1; i <= yg; ++i) {
+        const size_t at = (size_t)((i - 1) + yo * ((j - 1) + zo * (k - 1)));
+        double rad = sqrt(((double)i - 1.0) * ((double)i - 1.0) +
+                          ((double)k - (double)zg) * ((double)k - (double)zg));
+        if (rad < tr) tb[at] = 0.0;
+        rad = sqrt(((double)i - (double)yg) * ((double)i - (double)yg) +
+                   ((double)k - 1.0) * ((double)k - 1.0));
+        if (rad < tr) tb[at] = 0.0;
+      }
+  const int ny = yg, nx = (int)xg, nz = zg;
+  for (long k = 1; k <= zg; ++k)
+    for (long j = 1; j <= xg; ++j)
+      for (long i = 1; i <= yg; ++i) {
+        double v = 0.0;
+        if (j > xoff) {
+          const long t = (j - xoff - 1) / zo, r = (j - xoff - 1) % zo;
+          /* thickness 1: TmpB(:,1:zo,:); thickness 2: TmpB(:, j-((j-221)*2+51), :)
+           * = column zo..1; later ones repeat the first two */
+          const long c = (t % 2 == 0) ? r + 1 : zo - r;
+          v = tb[(i - 1) + yo * ((c - 1) + zo * (k - 1))];
+        }
+        ds[IX(i, j, k)] = v;
+      }
+  free(tb);
+  orc_nogrdbc(yg, (int)xg, zg, ds);
+  return 0;
+}
+
 /* ReDist3D_XYZ, LS:194-261 (dt = 1.0d-1) and RM:209-276 (dt = 1.0e-1
  * REAL(4)): f_t = sg (1 - |grad f|) on every cell including the ghosts,
  * with the sign-change guard of LS:245-249. */

@@ -48,6 +48,9 @@ void orc_connectivity(int py, int px, int pz, const double* dist, double width,
                       int term, double* cn_solid, double* cn_elec);
 void orc_rm_mask(int64_t n, const double* psA, const double* cn, double* psB);
 void orc_sign(int64_t n, const double* ds, double thr, double* sg);
+void orc_allen_cahn(int iters, int py, int px, int pz, double* f);
+int orc_ls_geometry(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
+                    int nthick, double tr, double* ds);
 
 /* fields */
 void orc_psi_from_dist(int ny, int nx, int nz, const float* d, double zeta, double* psi);

@@ -40,6 +40,8 @@ def lib() -> C.CDLL:
         "orc_connectivity": (None, [i, i, i, dp, d, i, dp, dp]),
         "orc_rm_mask": (None, [i64, dp, dp, dp]),
         "orc_sign": (None, [i64, dp, d, dp]),
+        "orc_allen_cahn": (None, [i, i, i, i, dp]),
+        "orc_ls_geometry": (i, [dp, i, i, i, i, i, i, i, d, dp]),
         "orc_psi_from_dist": (None, [i, i, i, fp, d, dp]),
         "orc_avp": (None, [i, i, i, dp, dp, d, d, dp, dp]),
         "orc_table": (None, [i64, i, dp, dp, dp, dp]),
@@ -83,6 +85,33 @@ def nogrdbc(f):
     f = _F(f).copy(order="F")
     lib().orc_nogrdbc(*hdims(f), _p(f))
     return f
+
+
+def allen_cahn(iters, f):
+    """LevelSet_3D.f90:116-136 on a halo-padded field (returns a new array)."""
+    f = _F(f).copy(order="F")
+    lib().orc_allen_cahn(iters, *hdims(f), _p(f))
+    return f
+
+
+def ls_geometry(vox, yg, zg, xoff, nthick, tr):
+    """LevelSet_3D.f90:80-122 (reorient, tunnels, stacking, NoGrdBc3D) on
+    TmpA = vox (yo, xo, zo); returns the halo-padded stacked field."""
+    vox = _F(vox)
+    yo, xo, zo = vox.shape
+    ds = np.zeros((yg + 2, xoff + nthick * zo + 2, zg + 2), order="F")
+    rc = lib().orc_ls_geometry(_p(vox), yo, xo, zo, yg, zg, xoff, nthick, float(tr), _p(ds))
+    if rc:
+        raise ValueError("geometry arguments out of range")
+    return ds
+
+
+def ls_frontend(vox, yg, zg, xoff, nthick, tr, ac_iters=50, lit=175, dt=1.0e-1):
+    """One frame of LevelSet_3D.f90:80-150: stacked field, Allen-Cahn,
+    sign, reinitialisation from zero; returns the halo-padded distance."""
+    ds = allen_cahn(ac_iters, ls_geometry(vox, yg, zg, xoff, nthick, tr))
+    sg = np.asfortranarray(sign(ds.ravel(order="F")).reshape(ds.shape, order="F"))
+    return redist(lit, sg, np.zeros_like(ds, order="F"), dt)
 
 
 def redist(lit, sg, f, dt=1.0e-1):

@@ -37,6 +37,21 @@ def nogrdbc(f):
     return f
 
 
+def allen_cahn(d, iters):
+    """LevelSet_3D.f90:116-136 in array syntax: NoGrdBc3D, then per step
+    sgF = 2*d*(1.0-d)*(1.0-2*d) - 0.64*(neighbours - 6*d), d = d - 0.05*sgF,
+    NoGrdBc3D (0.64, 0.05 REAL(4))."""
+    d = nogrdbc(d.copy())
+    I = slice(1, -1)
+    for _ in range(iters):
+        c = d[I, I, I]
+        nb = d[2:, I, I] + d[:-2, I, I] + d[I, 2:, I] + d[I, :-2, I] + d[I, I, 2:] + d[I, I, :-2] - 6 * c
+        sg = 2 * c * (1.0 - c) * (1.0 - 2 * c) - f4(0.64) * nb
+        d[I, I, I] = c - f4(0.05) * sg
+        nogrdbc(d)
+    return d
+
+
 def absgrd(sg, f):
     """AbsGrd3DUW_XYZ, LevelSet_3D.f90:289-320, interior result."""
     c = f[1:-1, 1:-1, 1:-1]
@@ -246,6 +261,11 @@ def main():
     ch = ch_update(cnp, psP, mb_t, mu_t, cord, rxn, avpx, dt, dx, 6.76e-10, f4(0.0312))
     out.update(ch_cnp=cnp, ch_psP=psP, ch_mu_t=mu_t, ch_mb_t=mb_t, ch_rxn=rxn, ch_avpx=avpx,
                ch_out=ch)
+    # Allen-Cahn pre-smoothing of a noisy 0/1 voxel field (ghosts arbitrary)
+    vox = (rng.uniform(size=(ny + 2, nx + 2, nz + 2)) < 0.55).astype(np.float64)
+    vox += rng.normal(size=vox.shape) * 0.05
+    out["ac_in"] = vox
+    out["ac_out"] = allen_cahn(vox, 17)
     np.savez_compressed(HERE / "golden_v1.npz", **out)
     print("wrote", HERE / "golden_v1.npz", sorted(out))
 

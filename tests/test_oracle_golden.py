@@ -2,7 +2,8 @@
 restatement (tests/golden/make_golden.py).  CPU only.
 
 Bit-exact where the arithmetic has no transcendental call and no reduction
-(level set, AccDiff, tables, operators, interface measure, Cahn-Hilliard).
+(level set, Allen-Cahn pre-smoothing, AccDiff, tables, operators, interface
+measure, Cahn-Hilliard).
 """
 from pathlib import Path
 
@@ -19,6 +20,10 @@ def test_redist_matches_golden():
     assert np.array_equal(orc.redist(9, sg, np.zeros_like(sg), 1.0e-1), G["redist_out_d"])
     assert np.array_equal(orc.redist(9, sg, np.zeros_like(sg), float(np.float32(0.1))),
                           G["redist_out_f"])
+
+
+def test_allen_cahn_matches_golden():
+    assert np.array_equal(orc.allen_cahn(17, G["ac_in"]), G["ac_out"])
 
 
 def test_accdiff_matches_golden():

@@ -128,3 +128,21 @@ def test_table_of_linear_function_is_exact():
     assert np.allclose(orc.table(cord, vals, c), 2.0 * c + 0.5, rtol=0, atol=1e-13)
     # clamps: below 0 -> 1e-6, above 1 -> 1
     assert np.allclose(orc.table(cord, vals, np.array([-5.0, 7.0])), [0.5 + 2e-6, 2.5])
+
+
+def test_allen_cahn_fixed_points_and_direction():
+    """LevelSet_3D.f90:116-136: 0, 1/2 and 1 are fixed points of the double
+    well (constant fields do not move, the Laplacian of a constant is 0);
+    values below 1/2 move toward 0, above toward 1; the ghosts end as
+    zero-gradient copies."""
+    for v in (0.0, 0.5, 1.0):
+        f = np.full((6, 7, 5), v)
+        assert np.array_equal(orc.allen_cahn(30, f), f)
+    f = np.full((6, 7, 22), 0.4)
+    f[:, :, 11:] = 0.6  # two thick slabs: each relaxes toward its well
+    g = orc.allen_cahn(40, f)
+    assert g[3, 3, 1] < 0.1 and g[3, 3, -2] > 0.9
+    assert np.all(np.diff(g[3, 3, 1:-1]) >= 0)  # a monotone interface between them
+    assert np.array_equal(g[0], g[1]) and np.array_equal(g[:, -1], g[:, -2])
+    assert np.array_equal(g[:, :, 0], g[:, :, 1])
+
