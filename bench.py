@@ -67,10 +67,11 @@ def _args():
     ap.add_argument("--pc", default="learned", choices=["learned", "jacobi"],
                     help="preconditioner of the headline solve")
     ap.add_argument("--workload", default="solve256",
-                    choices=["solve256", "batch96", "profile", "frontend"],
+                    choices=["solve256", "batch96", "profile", "frontend", "step128"],
                     help="solve256: the headline 256^3 solve; batch96: 96 uneven sub-volumes; "
                          "profile: only the production solve, for ncu captures; frontend: "
-                         "one frame of the LevelSet_3D geometry front end")
+                         "one frame of the LevelSet_3D geometry front end; step128: the "
+                         "full electrochemical time step at 128^3")
     return ap.parse_args()
 
 
@@ -633,6 +634,99 @@ def run_frontend(args):
     return 0
 
 
+def run_step128(args):
+    """The full electrochemical step at 128^3 (double-well Cahn-Hilliard,
+    linearised Butler-Volmer with i0 = 1e-3, 20 reinitialisation steps,
+    c0 = 0.5 +- 0.01, dt = 1e-3): `steps` x 100 time steps on the GPU after
+    `warmup` x 10; `value` = device time per time step (CUDA events on the
+    context stream).  The oracle runs the first two steps of the same run on
+    the host cores (CPU baseline per step), and the GPU's fields after them
+    are compared with the oracle's."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from elsim_gb300 import sbm, synth
+    from oracle import sbm_oracle as orc
+    n = 128
+    shape = (n, n, n)
+    p = synth.full_step_params(orc.params_reference())
+    m = synth.microstructure(shape, seed=SEED, reinit_steps=20)
+    d = m["dist"][1:-1, 1:-1, 1:-1]
+    dp, de = d.astype(np.float32), (-d).astype(np.float32)
+    c0 = synth.full_step_concentration(shape, SEED)
+    dt = synth.FULL_STEP_DT
+    ctx = sbm.Context(*shape, params=p)
+    s0 = ctx.setup_domain(dp, de)
+    ctx.upload(sbm.F_CNP, c0)
+    init = ctx.snapshot()
+    vsr = synth.step_schedule(s0["xrf"], 0.0, s0["trgI"])[1]
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    nsteps = 100
+
+    def run(k):
+        hist = []
+        for it in range(1, k + 1):
+            hist.append(ctx.time_step(it, dt, vsr))
+        return hist
+
+    for _ in range(args.warmup):
+        ctx.restore(init)
+        run(10)
+    times, iters = [], []
+    clk = Clocks()
+    clk.start()
+    l0 = sbm.launch_count()
+    for _ in range(args.steps):
+        ctx.restore(init)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        hist = run(nsteps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3 / nsteps)
+        iters.append(sum(h["it_cne"] + h["it_php"] + h["it_phe"] for h in hist))
+    launches = (sbm.launch_count() - l0) // args.steps
+    clocks = clk.stop()
+    # the oracle: the first two steps of the same run, then the GPU's fields
+    ctx.restore(init)
+    g2 = run(2)
+    st = orc.State(*shape, p)
+    so = st.setup_domain(dp, de)
+    st.set_field(sbm.F_CNP, c0)
+    t0 = time.perf_counter()
+    for it in (1, 2):
+        so = st.time_step(it, dt, vsr)
+    t_cpu = (time.perf_counter() - t0) / 2
+    werr = {}
+    for name, f, w in (("CnP", sbm.F_CNP, sbm.F_PSP), ("CnE", sbm.F_CNE, sbm.F_PSE),
+                       ("phP", sbm.F_PHP, sbm.F_PSP), ("phE", sbm.F_PHE, sbm.F_PSE)):
+        a, b, ww = ctx.download(f)[1:-1, 1:-1, 1:-1], st.field(f)[1:-1, 1:-1, 1:-1], \
+            st.field(w)[1:-1, 1:-1, 1:-1]
+        werr[name] = float(np.sqrt((ww * (a - b) ** 2).sum() / max((ww * b * b).sum(), 1e-300)))
+    threads = orc.lib().orc_num_threads()
+    t = statistics.mean(times)
+    line = {"metric": "sbm_full_step_time_128^3", "value": t, "unit": "s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded spheres, 20 reinitialisation steps)",
+            "config": {"workload": "full electrochemical time step 128^3: double-well CH (W=1, "
+                                   "kappa=1 voxel^2, M=1), linearised BV i0=1e-3, dt=1e-3, "
+                                   "c0=0.5+-0.01; one step = CH, CnE solve, BV Picard with phP "
+                                   "/ phE solves, voltage control",
+                       "time_steps_per_run": nsteps, "cg_iterations_per_run": iters[-1],
+                       "xrf_after": hist[-1]["xrf"],
+                       "weighted_rel_err_vs_oracle_after_2_steps": werr,
+                       "xrf_after_2_steps": {"gpu": g2[-1]["xrf"], "oracle": so["xrf"]}},
+            "cpu_baseline": {"value": t_cpu, "unit": "s", "cores": threads, "kind": "port",
+                             "sample": "time steps 1-2 of the same run (oracle C restatement, "
+                                       "OpenMP)"},
+            "clocks": clocks, "gpu_launches": launches}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def run_profile(args):
     """The production solve alone (no FP64 baseline, no CPU leg), `steps`
     times after `warmup` solves: the command the ncu summaries profile."""
@@ -669,6 +763,8 @@ def main():
         return run_profile(args)
     if args.workload == "frontend":
         return run_frontend(args)
+    if args.workload == "step128":
+        return run_step128(args)
     return run_ours(args)
 
 

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <vector>
 
 #include "sbm_internal.cuh"
 #include "sbm_net.cuh"
@@ -128,6 +129,8 @@ int sbm_params_reference(sbm_params* p) {
   p->crt_phe = 1.0e-6;                                   // :98
   p->crt_picard = 1.0e-8;                                // :627
   p->max_it_cne = 50001;                                 // :551 (EXIT after itlp > 50000)
+  p->ch_mode = SBM_CH_TABLE;
+  p->ch_w = 1.0;
   p->max_it_php = 30001;                                 // :710
   p->max_it_phe = 100001;                                // :791
   p->max_picard = 1000;
@@ -670,6 +673,91 @@ int sbm_ls_frontend(const double* vox, int yo, int xo, int zo, int yg, int zg, i
   if (rc) return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(ds, dd, sizeof(double) * g.nh, cudaMemcpyDeviceToHost, st.s));
   SBM_CUDA_TRY(cudaStreamSynchronize(st.s));
+  return SBM_OK;
+}
+
+namespace {
+// Interior (py*px*pz, Fortran order) host array into the interior of a
+// halo-padded device array, one 2-D copy per z plane.
+int upload_interior(const Geo& g, const double* h, double* d, cudaStream_t s) {
+  for (int k = 1; k <= g.nz; ++k)
+    SBM_CUDA_TRY(cudaMemcpy2DAsync(d + g.ix(1, 1, k), sizeof(double) * g.sx,
+                                   h + (size_t)g.ny * g.nx * (k - 1), sizeof(double) * g.ny,
+                                   sizeof(double) * g.ny, g.nx, cudaMemcpyHostToDevice, s));
+  return SBM_OK;
+}
+
+// 0.5*(1.0 + TANH(d/width)) on the host with the C library's tanh (the
+// oracle's), so the thresholds the sweeps test see the same psi.
+std::vector<double> psi_host(const double* dist, size_t n, double width) {
+  std::vector<double> v(n);
+  for (size_t c = 0; c < n; ++c) v[c] = 0.5 * (1.0 + std::tanh(dist[c] / width));
+  return v;
+}
+}  // namespace
+
+int sbm_connectivity(int py, int px, int pz, const double* dist, double width, int term,
+                     double* cn_solid, double* cn_elec) {
+  if (py < 1 || px < 1 || pz < 1 || !dist || !cn_solid || !cn_elec || term < 1 ||
+      !(width != 0.0))
+    return SBM_ERR_ARG;
+  const Geo g = make_geo(py, px, pz);
+  const size_t n = (size_t)py * px * pz;
+  std::vector<double> psi = psi_host(dist, n, width);
+  DevBufs b;
+  Stream st;
+  double *dp = b.get<double>(g.nh), *dc = b.get<double>(g.nh), *dt2 = b.get<double>(g.nh);
+  if (!dp || !dc || !dt2 || !st.s) return SBM_ERR_NOMEM;
+  int rc = upload_interior(g, psi.data(), dp, st.s);
+  if (!rc) rc = allen_cahn_dev(st.s, g, dp, dt2, 0);  // NoGrdBc3D fill, AD:88-97
+  if (rc) return rc;
+  for (int phase = 0; phase < 2; ++phase) {
+    if (phase == 1) {  // AD:175: interior 1 - psi, ghosts keep the solid values
+      for (double& v : psi) v = 1.0e0 - v;
+      if ((rc = upload_interior(g, psi.data(), dp, st.s))) return rc;
+    }
+    SBM_CUDA_TRY(cudaMemsetAsync(dc, 0, sizeof(double) * g.nh, st.s));
+    if ((rc = accdiff_dev(st.s, g, dp, dc, dt2, term, phase == 0 ? 1 : 0))) return rc;
+    SBM_CUDA_TRY(cudaMemcpyAsync(phase == 0 ? cn_solid : cn_elec, dc, sizeof(double) * g.nh,
+                                 cudaMemcpyDeviceToHost, st.s));
+    SBM_CUDA_TRY(cudaStreamSynchronize(st.s));
+  }
+  return SBM_OK;
+}
+
+int sbm_rm_ucnct(int py, int px, int pz, const double* dist, const double* cn_solid,
+                 const double* cn_elec, int lit, double* d_solid, double* d_elec) {
+  if (py < 1 || px < 1 || pz < 1 || !dist || !cn_solid || !cn_elec || !d_solid || !d_elec ||
+      lit < 0)
+    return SBM_ERR_ARG;
+  const Geo g = make_geo(py, px, pz);
+  const size_t n = (size_t)py * px * pz;
+  std::vector<double> psa = psi_host(dist, n, 1.0);  // RM:70
+  DevBufs b;
+  Stream st;
+  double *da = b.get<double>(g.nh), *dc = b.get<double>(g.nh), *dd = b.get<double>(g.nh),
+         *dg = b.get<double>(g.nh), *dt2 = b.get<double>(g.nh);
+  if (!da || !dc || !dd || !dg || !dt2 || !st.s) return SBM_ERR_NOMEM;
+  SBM_CUDA_TRY(cudaMemsetAsync(da, 0, sizeof(double) * g.nh, st.s));
+  SBM_CUDA_TRY(cudaMemsetAsync(dc, 0, sizeof(double) * g.nh, st.s));
+  const double dt = (double)1.0e-1f;  // RM:236, dt = 1.0e-1 REAL(4)
+  int rc;
+  for (int phase = 0; phase < 2; ++phase) {
+    if (phase == 1)
+      for (double& v : psa) v = 1.0e0 - v;  // RM:114
+    if ((rc = upload_interior(g, psa.data(), da, st.s))) return rc;
+    if ((rc = upload_interior(g, phase == 0 ? cn_solid : cn_elec, dc, st.s))) return rc;
+    // RM:79-82 / :127-130 mask, :86-88 dsF = psB with NoGrdBc3D, :91-96 sign,
+    // :99-100 reinitialisation from zero
+    if ((rc = rm_mask_dev(st.s, g.nh, da, dc, dd))) return rc;
+    if ((rc = allen_cahn_dev(st.s, g, dd, dt2, 0))) return rc;
+    if ((rc = sign_dev(st.s, g.nh, dd, 0.5, dg))) return rc;
+    SBM_CUDA_TRY(cudaMemsetAsync(dd, 0, sizeof(double) * g.nh, st.s));
+    if ((rc = redist_dev(st.s, g, dg, dd, dt2, lit, dt))) return rc;
+    SBM_CUDA_TRY(cudaMemcpyAsync(phase == 0 ? d_solid : d_elec, dd, sizeof(double) * g.nh,
+                                 cudaMemcpyDeviceToHost, st.s));
+    SBM_CUDA_TRY(cudaStreamSynchronize(st.s));
+  }
   return SBM_OK;
 }
 

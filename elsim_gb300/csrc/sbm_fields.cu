@@ -223,10 +223,13 @@ struct ChArgs {
   double* mb;
   double dx2, eps;
   Tbl tmu, tmb;
+  int double_well;  // SBM_CH_DOUBLE_WELL: mu from the analytic well of height w
+  double w;
 };
 
 // SBMES:398-405, :411: Lap in the reference's term order (x, y, z),
-// mu = Tbl(c) - eps*Lap, Mb = DTbl(c).
+// mu = Tbl(c) - eps*Lap, Mb = DTbl(c); with the double well
+// mu = w*2*c*(1-c)*(1-2*c) - eps*Lap (left to right).
 __global__ void k_ch_mu(ChArgs a) {
   __shared__ double sx[SBM_TBL_MAX], smu[SBM_TBL_MAX], smb[SBM_TBL_MAX];
   for (int q = threadIdx.x; q < a.tmu.n; q += blockDim.x) {
@@ -249,7 +252,9 @@ __global__ void k_ch_mu(ChArgs a) {
     l = l - 2.0 * u;
     l = l + a.cnp[c + g.sz];
     l = l / a.dx2;
-    a.mu[c] = table_at(u, a.tmu.n, sx, smu, ditv) - a.eps * l;
+    const double f0 = a.double_well ? (((a.w * 2.0) * u) * (1.0 - u)) * (1.0 - 2.0 * u)
+                                     : table_at(u, a.tmu.n, sx, smu, ditv);
+    a.mu[c] = f0 - a.eps * l;
     a.mb[c] = table_at(u, a.tmb.n, sx, smb, ditv);
   }
 }
@@ -499,7 +504,8 @@ int step_ch(sbm_ctx* ctx, double dt, sbm_scalars* out) {
   cudaStream_t s = ctx->stream;
   const sbm_params& p = ctx->p;
   const double dx2 = p.dx * p.dx;
-  ChArgs a{g, ctx->f[SBM_F_CNP], ctx->mu, ctx->mb, dx2, p.eps, tbl_dev(ctx, 0), tbl_dev(ctx, 1)};
+  ChArgs a{g,      ctx->f[SBM_F_CNP], ctx->mu, ctx->mb, dx2, p.eps, tbl_dev(ctx, 0), tbl_dev(ctx, 1),
+           p.ch_mode == SBM_CH_DOUBLE_WELL, p.ch_w};
   k_ch_mu<<<flat(g.ninterior()), 256, 0, s>>>(a);
   SBM_LAUNCHED(1);
   int rc;

@@ -88,6 +88,18 @@ def frame(vox: np.ndarray, n: int, yg: int = REFERENCE["yg"], zg: int = REFERENC
     return ds[1:-1, 1:-1, 1:-1]
 
 
+def connected(dist: np.ndarray, term: int = 1501, lit: int = REDIST_ITERS):
+    """The AccDiff_3D and RM_UCNCT_3D programs for one interior distance
+    field (a frame's output) on the GPU: connectivity of each phase, then the
+    solid and electrolyte distances with their disconnected regions removed
+    (the GRP_LS / POR_LS fields the cell model reads).  Returns
+    (d_solid, d_elec, cn_solid, cn_elec), all interior."""
+    cs, ce = sbm.connectivity(dist, 0.75, term)
+    i = (slice(1, -1),) * 3
+    ds, de = sbm.rm_ucnct(dist, cs[i], ce[i], lit)
+    return ds[i], de[i], cs[i], ce[i]
+
+
 def run(vox: np.ndarray, frames=FRAMES, prefix: str = PREFIX, directory=".",
         **kw) -> list[Path]:
     """The reference's frame loop (LevelSet_3D.f90:72-152): one REAL(8)

@@ -40,6 +40,7 @@ STOP_REF_UPDATE, STOP_REF_RESID, STOP_REL_RES = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 PC_NONE, PC_JACOBI, PC_LEARNED = 0, 1, 2
 BV_EXP, BV_LINEAR = 0, 1
+CH_TABLE, CH_DOUBLE_WELL = 0, 1
 F_PSP, F_PSE, F_AVP, F_AVPX, F_CNP, F_CNE, F_PHP, F_PHE, F_RXN, F_COEF, F_RHS, F_X, F_WEIGHT = range(13)
 FIELDS = dict(psP=F_PSP, psE=F_PSE, AvP=F_AVP, AvPx=F_AVPX, CnP=F_CNP, CnE=F_CNE, phP=F_PHP,
               phE=F_PHE, Rxn=F_RXN, coef=F_COEF, rhs=F_RHS, x=F_X, weight=F_WEIGHT)
@@ -67,8 +68,9 @@ class Params(C.Structure):
         "dab_c3", "cne_ref", "cst1", "frd", "bvp", "bve", "kap_scale", "avp_mask", "i0_scale",
         "kfw_c", "crt_cne", "crt_php", "crt_phe", "crt_picard")] + [
         (n, C.c_int) for n in ("max_it_cne", "max_it_php", "max_it_phe", "max_picard",
-                               "cne_mean_every", "bv_mode", "tbl_n", "pad_")] + [
-        (n, C.c_double * TBL_MAX) for n in ("tbl_x", "tbl_mu", "tbl_mb", "tbl_i0", "tbl_ocv")]
+                               "cne_mean_every", "bv_mode", "tbl_n", "ch_mode")] + [
+        (n, C.c_double * TBL_MAX) for n in ("tbl_x", "tbl_mu", "tbl_mb", "tbl_i0", "tbl_ocv")] + [
+        ("ch_w", C.c_double)]
 
     def set_table(self, name: str, values) -> None:
         v = np.asarray(values, dtype=np.float64)
@@ -150,6 +152,8 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_accdiff": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, C.c_int]),
         "sbm_allen_cahn": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, dp]),
         "sbm_ls_geometry": (C.c_int, [dp] + [C.c_int] * 7 + [C.c_double, dp]),
+        "sbm_connectivity": (C.c_int, [C.c_int] * 3 + [dp, C.c_double, C.c_int, dp, dp]),
+        "sbm_rm_ucnct": (C.c_int, [C.c_int] * 3 + [dp, dp, dp, C.c_int, dp, dp]),
         "sbm_ls_frontend": (C.c_int, [dp] + [C.c_int] * 7 + [C.c_double, C.c_int, C.c_int,
                                                               C.c_double, dp]),
         "sbm_ls_frontend_device": (C.c_int, [C.c_void_p] + [C.c_int] * 7 +
@@ -600,6 +604,33 @@ def ls_frontend(vox, yg: int, zg: int, xoff: int, nthick: int, tr: float, ac_ite
     _check(lib.sbm_ls_frontend(_dptr(vox), yo, xo, zo, yg, zg, xoff, nthick, float(tr),
                                ac_iters, lit, float(dt), _dptr(ds)), "sbm_ls_frontend")
     return ds
+
+
+def connectivity(dist, width: float = 0.75, term: int = 1501) -> tuple[np.ndarray, np.ndarray]:
+    """AccDiff_3D program body for one interior distance field on the GPU:
+    halo-padded Cn of the solid and of the electrolyte."""
+    lib = load_library()
+    d = _f64(dist)
+    py, px, pz = d.shape
+    cs = np.zeros((py + 2, px + 2, pz + 2), order="F")
+    ce = np.zeros_like(cs)
+    _check(lib.sbm_connectivity(py, px, pz, _dptr(d), width, term, _dptr(cs), _dptr(ce)),
+           "sbm_connectivity")
+    return cs, ce
+
+
+def rm_ucnct(dist, cn_solid, cn_elec, lit: int = 175) -> tuple[np.ndarray, np.ndarray]:
+    """RM_UCNCT_3D program body on the GPU: halo-padded (solid, electrolyte)
+    distances with the disconnected regions removed; all inputs interior."""
+    lib = load_library()
+    d = _f64(dist)
+    cs, ce = _f64(cn_solid, d.shape), _f64(cn_elec, d.shape)
+    py, px, pz = d.shape
+    ds = np.zeros((py + 2, px + 2, pz + 2), order="F")
+    de = np.zeros_like(ds)
+    _check(lib.sbm_rm_ucnct(py, px, pz, _dptr(d), _dptr(cs), _dptr(ce), lit, _dptr(ds),
+                            _dptr(de)), "sbm_rm_ucnct")
+    return ds, de
 
 
 def accdiff(psi, cn, term: int = 1501, dirichlet_x: int = 1) -> np.ndarray:

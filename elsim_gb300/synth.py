@@ -121,6 +121,43 @@ def reference_tables(params):
     return params
 
 
+def full_step_params(params):
+    """The 128^3 full-electrochemical-step workload: Cahn-Hilliard with the
+    analytic double well of height W = 1, gradient coefficient kappa = 1
+    voxel^2 and mobility M = 1 voxel^2 per unit time -- in the reference's
+    physical grid spacing dx that is eps = dx^2 and a mobility table of dx^2,
+    so the update equals the voxel-unit one -- and Butler-Volmer linearised
+    in the potential jump with a uniform exchange current i0 = i0_scale =
+    1e-3 (a table of ones) and zero open-circuit voltage; everything else
+    (dx, the potentials, CnE) as the reference."""
+    from .sbm import BV_LINEAR, CH_DOUBLE_WELL
+
+    x = np.arange(101) * 0.01
+    dx2 = params.dx * params.dx
+    params.eps = dx2
+    params.ch_mode = CH_DOUBLE_WELL
+    params.ch_w = 1.0
+    params.bv_mode = BV_LINEAR
+    params.i0_scale = 1.0e-3
+    params.set_table("tbl_x", x)
+    params.set_table("tbl_mu", np.zeros(101))
+    params.set_table("tbl_mb", np.full(101, dx2))
+    params.set_table("tbl_i0", np.ones(101))
+    params.set_table("tbl_ocv", np.zeros(101))
+    return params
+
+
+def full_step_concentration(shape, seed: int) -> np.ndarray:
+    """Halo-padded initial particle concentration 0.5 + U(-0.01, 0.01),
+    ghosts copied from the nearest interior cell."""
+    rng = np.random.default_rng(seed + 104729)
+    c = 0.5 + rng.uniform(-0.01, 0.01, size=shape)
+    return np.asfortranarray(np.pad(c, 1, mode="edge"))
+
+
+FULL_STEP_DT = 1.0e-3
+
+
 def step_schedule(xrf: float, dcrnt: float, trgi: float):
     """dt and voltage-scan rate of one time step as the reference's time
     loop chooses them (SBMES:360-383); all literals REAL(4) as there."""

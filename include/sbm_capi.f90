@@ -15,6 +15,8 @@ MODULE sbm_capi
   INTEGER(C_INT), PARAMETER :: SBM_STOP_REF_UPDATE = 0, SBM_STOP_REF_RESID = 1, SBM_STOP_REL_RES = 2
   INTEGER(C_INT), PARAMETER :: SBM_PREC_FP64 = 0, SBM_PREC_MIXED = 1
   INTEGER(C_INT), PARAMETER :: SBM_PC_NONE = 0, SBM_PC_JACOBI = 1, SBM_PC_LEARNED = 2
+  INTEGER(C_INT), PARAMETER :: SBM_BV_EXP = 0, SBM_BV_LINEAR = 1
+  INTEGER(C_INT), PARAMETER :: SBM_CH_TABLE = 0, SBM_CH_DOUBLE_WELL = 1
   INTEGER(C_INT), PARAMETER :: SBM_F_PSP = 0, SBM_F_PSE = 1, SBM_F_AVP = 2, SBM_F_AVPX = 3, &
        SBM_F_CNP = 4, SBM_F_CNE = 5, SBM_F_PHP = 6, SBM_F_PHE = 7, SBM_F_RXN = 8, &
        SBM_F_COEF = 9, SBM_F_RHS = 10, SBM_F_X = 11, SBM_F_WEIGHT = 12
@@ -26,9 +28,10 @@ MODULE sbm_capi
     REAL(C_DOUBLE) :: kap_scale, avp_mask, i0_scale, kfw_c
     REAL(C_DOUBLE) :: crt_cne, crt_php, crt_phe, crt_picard
     INTEGER(C_INT) :: max_it_cne, max_it_php, max_it_phe, max_picard
-    INTEGER(C_INT) :: cne_mean_every, bv_mode, tbl_n, pad_
+    INTEGER(C_INT) :: cne_mean_every, bv_mode, tbl_n, ch_mode
     REAL(C_DOUBLE) :: tbl_x(SBM_TBL_MAX), tbl_mu(SBM_TBL_MAX), tbl_mb(SBM_TBL_MAX)
     REAL(C_DOUBLE) :: tbl_i0(SBM_TBL_MAX), tbl_ocv(SBM_TBL_MAX)
+    REAL(C_DOUBLE) :: ch_w
   END TYPE sbm_params
 
   TYPE, BIND(C) :: sbm_scalars
@@ -146,6 +149,21 @@ MODULE sbm_capi
       TYPE(C_PTR), VALUE :: vox, ds, sg, tmp, stream
       INTEGER(C_INT), VALUE :: yo, xo, zo, yg, zg, xoff, nthick, ac_iters, lit
       REAL(C_DOUBLE), VALUE :: tr, dt
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_connectivity(py, px, pz, dist, width, term, cn_solid, cn_elec) &
+        BIND(C, NAME='sbm_connectivity')
+      IMPORT :: C_INT, C_DOUBLE
+      INTEGER(C_INT), VALUE :: py, px, pz, term
+      REAL(C_DOUBLE), VALUE :: width
+      REAL(C_DOUBLE), INTENT(IN) :: dist(*)
+      REAL(C_DOUBLE), INTENT(OUT) :: cn_solid(*), cn_elec(*)
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION sbm_rm_ucnct(py, px, pz, dist, cn_solid, cn_elec, lit, d_solid, &
+        d_elec) BIND(C, NAME='sbm_rm_ucnct')
+      IMPORT :: C_INT, C_DOUBLE
+      INTEGER(C_INT), VALUE :: py, px, pz, lit
+      REAL(C_DOUBLE), INTENT(IN) :: dist(*), cn_solid(*), cn_elec(*)
+      REAL(C_DOUBLE), INTENT(OUT) :: d_solid(*), d_elec(*)
     END FUNCTION
     INTEGER(C_INT) FUNCTION sbm_accdiff(py, px, pz, psi, cn, term, dirichlet_x) &
          BIND(C, NAME='sbm_accdiff')

@@ -75,6 +75,12 @@ extern "C" {
 #define SBM_BV_EXP      0   /* reference exponential form        */
 #define SBM_BV_LINEAR   1   /* first-order expansion in dPh      */
 
+/* Cahn-Hilliard chemical potential (sbm_params.ch_mode) */
+#define SBM_CH_TABLE        0   /* reference: mu = Tbl(c) - eps Lap c, SBMES:403-411 */
+#define SBM_CH_DOUBLE_WELL  1   /* mu = ch_w 2c(1-c)(1-2c) - eps Lap c (the analytic
+                                   double well of the 128^3 full-step workload);
+                                   mobility still from tbl_mb (all ones: M = 1) */
+
 /* Device-resident fields of a context.  All are halo-padded FP64. */
 enum sbm_field {
   SBM_F_PSP = 0,   /* psP  particle domain parameter      SBMES:143 */
@@ -117,12 +123,13 @@ typedef struct sbm_params {
   int    cne_mean_every;  /* 100, SBMES:562 */
   int    bv_mode;         /* SBM_BV_EXP or SBM_BV_LINEAR */
   int    tbl_n;           /* table length (101), SBMES:210-242 */
-  int    pad_;
+  int    ch_mode;         /* SBM_CH_TABLE or SBM_CH_DOUBLE_WELL */
   double tbl_x[SBM_TBL_MAX];    /* Tbl(1,:)  coordinates   */
   double tbl_mu[SBM_TBL_MAX];   /* Tbl(2,:)  chemical potential, C_Li_M6 */
   double tbl_mb[SBM_TBL_MAX];   /* DTbl(2,:) mobility, C_Li_Mb5 (already scaled) */
   double tbl_i0[SBM_TBL_MAX];   /* iTbl(2,:) exchange current, C_Li_J2 */
   double tbl_ocv[SBM_TBL_MAX];  /* OTbl(2,:) open-circuit voltage, C_Li_O3 */
+  double ch_w;                  /* double-well height W (SBM_CH_DOUBLE_WELL) */
 } sbm_params;
 
 /* Scalars of the electrochemical state that the reference keeps in
@@ -290,6 +297,27 @@ int sbm_ls_geometry(const double* vox, int yo, int xo, int zo, int yg, int zg, i
  * Bit-exact with the reference arithmetic. */
 int sbm_ls_frontend(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
                     int nthick, double tr, int ac_iters, int lit, double dt, double* ds);
+
+/* The per-frame body of the AccDiff_3D program (AccDiff_3D.f90:76-243):
+ * psi = 0.5*(1.0+TANH(dist/width)) (width 0.75; computed on the host with
+ * the C library's tanh) with zero-gradient ghosts, then `term` (1501)
+ * connectivity sweeps of the solid (Cn = 1 on the x = px+1 face) and of the
+ * electrolyte (interior psi -> 1 - psi, the ghosts keeping the solid values
+ * as in the reference; Cn = 1 on the x = 0 face), each from Cn = 0.
+ * dist: interior py*px*pz; cn_solid / cn_elec: halo-padded outputs.
+ * Bit-exact with the reference arithmetic. */
+int sbm_connectivity(int py, int px, int pz, const double* dist, double width, int term,
+                     double* cn_solid, double* cn_elec);
+
+/* The per-frame body of the RM_UCNCT_3D program (RM_UCNCT_3D.f90:68-141):
+ * for the solid (psA = 0.5*(1.0+TANH(dist/1.0))) and the electrolyte
+ * (1 - psA), zero psA where the phase's Cn < 1.0e-4, sign (> 0.5) with
+ * zero-gradient ghosts and `lit` (175) reinitialisation steps from zero with
+ * dt = 1.0e-1 REAL(4): the distance of each phase with its disconnected
+ * regions removed.  dist, cn_solid, cn_elec: interior py*px*pz;
+ * d_solid / d_elec: halo-padded outputs.  Bit-exact. */
+int sbm_rm_ucnct(int py, int px, int pz, const double* dist, const double* cn_solid,
+                 const double* cn_elec, int lit, double* d_solid, double* d_elec);
 
 /* sbm_ls_frontend on caller-owned DEVICE buffers: vox (yo*xo*zo doubles),
  * ds, sg, tmp (each (yg+2)(xg+2)(zg+2) doubles; ds receives the distance,

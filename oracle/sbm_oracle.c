@@ -391,6 +391,40 @@ void orc_connectivity(int py, int px, int pz, const double* dist, double width,
   free(psi);
 }
 
+/* The per-frame body of the RM_UCNCT_3D program, RM:68-141 (both phases):
+ * psA = 0.5*(1.0+TANH(d/1.0)) (electrolyte: 1 - psA), psB = psA with 0
+ * where the phase's Cn < 1.0e-4 (REAL(4)), dsF = psB with NoGrdBc3D
+ * ghosts, sign (> 0.5), reinitialisation from zero for `lit` steps with
+ * dt = 1.0e-1 REAL(4).  cn_* and dist are interior arrays; d_* halo-padded. */
+void orc_rm_ucnct(int py, int px, int pz, const double* dist, const double* cn_solid,
+                  const double* cn_elec, int lit, double* d_solid, double* d_elec) {
+  const int ny = py, nx = px, nz = pz;
+  const size_t n = (size_t)ny * nx * nz;
+  const double thr = (double)1.0e-4f;
+  double* psa = (double*)malloc(n * sizeof(double));
+  double* sg = (double*)malloc(NH * sizeof(double));
+  for (size_t c = 0; c < n; ++c) psa[c] = 0.5 * (1.0 + tanh(dist[c] / 1.0));
+  for (int phase = 0; phase < 2; ++phase) {
+    const double* cn = phase == 0 ? cn_solid : cn_elec;
+    double* ds = phase == 0 ? d_solid : d_elec;
+    if (phase == 1)
+      for (size_t c = 0; c < n; ++c) psa[c] = 1.0e0 - psa[c];
+    memset(ds, 0, NH * sizeof(double));
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= nx; ++j)
+        for (int i = 1; i <= ny; ++i) {
+          const size_t q = (size_t)(i - 1) + (size_t)ny * ((size_t)(j - 1) + (size_t)nx * (k - 1));
+          ds[IX(i, j, k)] = (cn[q] < thr) ? 0.0 : psa[q];
+        }
+    orc_nogrdbc(py, px, pz, ds);
+    orc_sign((int64_t)NH, ds, 0.5, sg);
+    memset(ds, 0, NH * sizeof(double));
+    orc_redist(lit, (double)1.0e-1f, py, px, pz, sg, ds);
+  }
+  free(psa);
+  free(sg);
+}
+
 /* RM:79-82 and RM:119,128-130. */
 void orc_rm_mask(int64_t n, const double* psA, const double* cn, double* psB) {
   const double thr = (double)1.0e-4f;
@@ -626,6 +660,8 @@ int orc_params_reference(sbm_params* p) {
   p->max_picard = 1000;
   p->cne_mean_every = 100;                              /* :562 */
   p->bv_mode = SBM_BV_EXP;
+  p->ch_mode = SBM_CH_TABLE;
+  p->ch_w = 1.0;
   p->tbl_n = 101;
   for (int t = 0; t < 101; ++t) {
     p->tbl_x[t] = t * 0.01;
@@ -756,6 +792,11 @@ int orc_ch_step(orc_state* s, double dt, sbm_scalars* sc) {
       const size_t c0 = IX(1, j, k);
       orc_table(ny, p->tbl_n, p->tbl_x, p->tbl_mu, cnp + c0, s->mu + c0);
       orc_table(ny, p->tbl_n, p->tbl_x, p->tbl_mb, cnp + c0, s->mb + c0);
+      if (p->ch_mode == SBM_CH_DOUBLE_WELL)
+        for (int i = 1; i <= ny; ++i) { /* mu = W*2*c*(1-c)*(1-2*c), left to right */
+          const double u = cnp[c0 + i - 1];
+          s->mu[c0 + i - 1] = (((p->ch_w * 2.0) * u) * (1.0 - u)) * (1.0 - 2.0 * u);
+        }
     }
   bc_copy_all(ny, nx, nz, s->mb);                             /* :407-409 */
 #pragma omp parallel for schedule(static)

@@ -49,6 +49,8 @@ void orc_connectivity(int py, int px, int pz, const double* dist, double width,
 void orc_rm_mask(int64_t n, const double* psA, const double* cn, double* psB);
 void orc_sign(int64_t n, const double* ds, double thr, double* sg);
 void orc_allen_cahn(int iters, int py, int px, int pz, double* f);
+void orc_rm_ucnct(int py, int px, int pz, const double* dist, const double* cn_solid,
+                  const double* cn_elec, int lit, double* d_solid, double* d_elec);
 int orc_ls_geometry(const double* vox, int yo, int xo, int zo, int yg, int zg, int xoff,
                     int nthick, double tr, double* ds);
 

@@ -42,6 +42,7 @@ def lib() -> C.CDLL:
         "orc_sign": (None, [i64, dp, d, dp]),
         "orc_allen_cahn": (None, [i, i, i, i, dp]),
         "orc_ls_geometry": (i, [dp, i, i, i, i, i, i, i, d, dp]),
+        "orc_rm_ucnct": (None, [i, i, i, dp, dp, dp, i, dp, dp]),
         "orc_psi_from_dist": (None, [i, i, i, fp, d, dp]),
         "orc_avp": (None, [i, i, i, dp, dp, d, d, dp, dp]),
         "orc_table": (None, [i64, i, dp, dp, dp, dp]),
@@ -140,6 +141,18 @@ def connectivity(dist_interior, width=0.75, term=1501):
     ce = np.zeros_like(cs)
     lib().orc_connectivity(ny, nx, nz, _p(d), width, term, _p(cs), _p(ce))
     return cs, ce
+
+
+def rm_ucnct(dist_interior, cn_solid, cn_elec, lit=175):
+    """RM_UCNCT_3D.f90:68-141 for one frame: (solid, electrolyte) distance,
+    halo-padded, from the interior distance and the phases' interior Cn."""
+    d = _F(dist_interior)
+    ny, nx, nz = d.shape
+    cs, ce = _F(cn_solid), _F(cn_elec)
+    out_s = np.zeros((ny + 2, nx + 2, nz + 2), order="F")
+    out_e = np.zeros_like(out_s)
+    lib().orc_rm_ucnct(ny, nx, nz, _p(d), _p(cs), _p(ce), lit, _p(out_s), _p(out_e))
+    return out_s, out_e
 
 
 def rm_mask(psA, cn):

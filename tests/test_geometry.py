@@ -122,3 +122,29 @@ def test_frontend_oracle_signs():
     d = orc.ls_frontend(vox, tr=2.0, ac_iters=5, lit=20, **SMALL)
     sm = orc.allen_cahn(5, orc.ls_geometry(vox, tr=2.0, **SMALL))
     assert np.array_equal(d > 0, sm > 0.5)
+
+
+def _slab_and_ball(shape=(20, 28, 16)):
+    """Interior distance-like field: +2 in a solid slab touching the x = px+1
+    face and in an isolated ball, -2 elsewhere."""
+    ny, nx, nz = shape
+    i, j, k = np.meshgrid(np.arange(ny), np.arange(nx), np.arange(nz), indexing="ij")
+    slab = j >= nx - 6
+    ball = (i - ny / 2) ** 2 + (j - nx / 3) ** 2 + (k - nz / 2) ** 2 <= 16
+    return np.asfortranarray(np.where(slab | ball, 2.0, -2.0)), slab, ball
+
+
+def test_connectivity_removes_isolated_solid():
+    # AccDiff_3D + RM_UCNCT_3D: the ball has no path to the solid's Dirichlet
+    # face, so its Cn stays 0 and the solid distance drops it; the slab keeps
+    # Cn = 1 and stays solid; the electrolyte (Dirichlet face x = 0) is one
+    # connected region and keeps its sign
+    d, slab, ball = _slab_and_ball()
+    cs, ce = orc.connectivity(d, 0.75, 1501)
+    i = (slice(1, -1),) * 3
+    assert cs[i][ball].max() < 1e-4 and cs[i][slab].min() == 1.0
+    elec = ~(slab | ball)
+    assert ce[i][elec].min() > 1e-4
+    ds, de = orc.rm_ucnct(d, cs[i], ce[i], lit=40)
+    assert (ds[i][ball] < 0).all() and (ds[i][slab] > 0).all()
+    assert np.array_equal(de[i] > 0, elec)

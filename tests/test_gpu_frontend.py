@@ -75,3 +75,44 @@ def test_frame_file(sbm, tmp_path):
     d = fortran_io.read_array(path, np.float64, (21, 4 + 4 * 12, 33))
     want = orc.ls_frontend(vox, 21, 33, 4, 4, geometry.TUNNEL_RADII[5], 10, 30)
     assert np.array_equal(d, want[1:-1, 1:-1, 1:-1])
+
+
+def _frame_distance(shape=(40, 52, 14), seed=11):
+    from elsim_gb300 import geometry
+
+    vox = geometry.synthetic_voxels(shape, seed=seed, blob=1.5)
+    ds = orc.ls_frontend(vox, 23, 37, 4, 4, float(geometry.TUNNEL_RADII[3]), 20, 60)
+    return np.asfortranarray(ds[1:-1, 1:-1, 1:-1])
+
+
+def test_connectivity_program(sbm):
+    d = _frame_distance()
+    got = sbm.connectivity(d, 0.75, 1501)
+    want = orc.connectivity(d, 0.75, 1501)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+def test_rm_ucnct_program(sbm):
+    d = _frame_distance(seed=12)
+    cs, ce = orc.connectivity(d, 0.75, 1501)
+    i = (slice(1, -1),) * 3
+    # the structure has disconnected pieces in at least one phase
+    psa = 0.5 * (1.0 + np.tanh(d))
+    assert ((cs[i] < 1e-4) & (psa > 0.5)).any() or ((ce[i] < 1e-4) & (psa < 0.5)).any()
+    got = sbm.rm_ucnct(d, cs[i], ce[i], 175)
+    want = orc.rm_ucnct(d, cs[i], ce[i], 175)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+def test_geometry_chain(sbm):
+    from elsim_gb300 import geometry
+
+    d = _frame_distance(seed=13)
+    ds, de, cs, ce = geometry.connected(d, term=301, lit=50)
+    wcs, wce = orc.connectivity(d, 0.75, 301)
+    i = (slice(1, -1),) * 3
+    wds, wde = orc.rm_ucnct(d, wcs[i], wce[i], 50)
+    assert np.array_equal(cs, wcs[i]) and np.array_equal(ce, wce[i])
+    assert np.array_equal(ds, wds[i]) and np.array_equal(de, wde[i])

@@ -167,3 +167,61 @@ def test_mixed_precision_time_steps_match_oracle(built):
         for f in FIELDS:
             w = st.field(WEIGHT[f]) if WEIGHT[f] is not None else None
             assert _werr(ctx.download(f), st.field(f), w) < 1e-6, f
+
+
+def _full_step_setup(shape, seed, tight):
+    """The full-step workload (double-well Cahn-Hilliard, linearised
+    Butler-Volmer, i0 = 1e-3, 20 reinitialisation steps, c0 = 0.5 +- 0.01)."""
+    p = synth.full_step_params(orc.params_reference())
+    if tight:
+        p.crt_cne = p.crt_php = p.crt_phe = 1e-11
+    m = synth.microstructure(shape, seed=seed, reinit_steps=20, redist=orc.redist)
+    d = m["dist"][1:-1, 1:-1, 1:-1]
+    return p, d.astype(np.float32), (-d).astype(np.float32), synth.full_step_concentration(shape, seed)
+
+
+def test_full_step_workload_matches_oracle(built):
+    shape = (20, 24, 16)
+    p, dp, de, c0 = _full_step_setup(shape, 4, True)
+    st = orc.State(*shape, p)
+    so = st.setup_domain(dp, de)
+    st.set_field(sbm.F_CNP, c0)
+    with sbm.Context(*shape, params=p) as ctx:
+        ctx.setup_domain(dp, de)
+        ctx.upload(sbm.F_CNP, c0)
+        vsr = synth.step_schedule(so["xrf"], 0.0, so["trgI"])[1]
+        for it in range(1, 6):
+            so = st.time_step(it, synth.FULL_STEP_DT, vsr)
+            sg = ctx.time_step(it, synth.FULL_STEP_DT, vsr)
+        for key in ("xrf", "scrnt", "bve"):
+            assert abs(sg[key] - so[key]) <= 1e-7 * max(abs(so[key]), 1e-12), (key, sg[key], so[key])
+        for f in FIELDS:
+            w = st.field(WEIGHT[f]) if WEIGHT[f] is not None else None
+            assert _werr(ctx.download(f), st.field(f), w) < 1e-7, f
+
+
+def test_full_step_workload_128(built):
+    """128^3, 100 steps of the full-step workload on the GPU: every solve
+    converges, the concentration stays finite and inside [0, 1], the mean
+    moves only by the reaction, and a second run from the same state is
+    bit-identical (deterministic reductions)."""
+    shape = (128, 128, 128)
+    p, dp, de, c0 = _full_step_setup(shape, 1, False)
+    with sbm.Context(*shape, params=p) as ctx:
+        s0 = ctx.setup_domain(dp, de)
+        ctx.upload(sbm.F_CNP, c0)
+        vsr = synth.step_schedule(s0["xrf"], 0.0, s0["trgI"])[1]
+        snap = None
+        hist = []
+        for it in range(1, 101):
+            if it == 91:
+                snap = ctx.snapshot()
+            hist.append(ctx.time_step(it, synth.FULL_STEP_DT, vsr))
+        c = ctx.download(sbm.F_CNP)[1:-1, 1:-1, 1:-1]
+        assert np.isfinite(c).all() and c.min() >= 0.0 and c.max() <= 1.0
+        assert all(h["it_cne"] < p.max_it_cne - 1 and h["n_picard"] < p.max_picard for h in hist)
+        assert abs(hist[-1]["xrf"] - 0.5) < 0.05
+        ctx.restore(snap)
+        again = [ctx.time_step(it, synth.FULL_STEP_DT, vsr) for it in range(91, 101)]
+        assert again == hist[90:]
+        assert np.array_equal(ctx.download(sbm.F_CNP)[1:-1, 1:-1, 1:-1], c)

@@ -146,3 +146,44 @@ def test_allen_cahn_fixed_points_and_direction():
     assert np.array_equal(g[0], g[1]) and np.array_equal(g[:, -1], g[:, -2])
     assert np.array_equal(g[:, :, 0], g[:, :, 1])
 
+
+
+def test_double_well_cahn_hilliard_pin():
+    """The double-well chemical potential of the full-step workload:
+    mu = W*2c(1-c)(1-2c) - eps*Lap c, restated in NumPy, against the oracle's
+    Cahn-Hilliard update on a random field with psP = 1 and no reaction."""
+    from elsim_gb300 import sbm, synth
+    from oracle import sbm_oracle as orc
+    shape = (9, 7, 6)
+    p = synth.full_step_params(orc.params_reference())
+    p.ch_w = 1.7
+    st = orc.State(*shape, p)
+    rng = np.random.default_rng(3)
+    dist = rng.uniform(2.0, 3.0, size=shape).astype(np.float32)
+    st.setup_domain(dist, -dist)
+    c = np.pad(rng.uniform(0.3, 0.7, size=shape), 1, mode="edge")
+    st.set_field(sbm.F_CNP, np.asfortranarray(c))
+    psp = st.field(sbm.F_PSP)
+    st.set_field(sbm.F_RXN, np.zeros_like(c, order="F"))
+    dt = 1e-3
+    st.ch_step(dt)
+    got = st.field(sbm.F_CNP)[1:-1, 1:-1, 1:-1]
+    dx2 = p.dx * p.dx
+
+    def lap(u):
+        return ((u[2:, 1:-1, 1:-1] + u[:-2, 1:-1, 1:-1] + u[1:-1, 2:, 1:-1] + u[1:-1, :-2, 1:-1]
+                 + u[1:-1, 1:-1, 2:] + u[1:-1, 1:-1, :-2] - 6 * u[1:-1, 1:-1, 1:-1]) / dx2)
+
+    ci = c[1:-1, 1:-1, 1:-1]
+    mu = np.pad(1.7 * 2 * ci * (1 - ci) * (1 - 2 * ci) - p.eps * lap(c), 1, mode="edge")
+    pm = np.pad(psp[1:-1, 1:-1, 1:-1] * dx2, 1, mode="edge")
+    m0 = mu[1:-1, 1:-1, 1:-1]
+    p0 = pm[1:-1, 1:-1, 1:-1]
+    dvc = np.zeros_like(ci)
+    for sl in ((slice(2, None), slice(1, -1), slice(1, -1)), (slice(None, -2), slice(1, -1), slice(1, -1)),
+               (slice(1, -1), slice(2, None), slice(1, -1)), (slice(1, -1), slice(None, -2), slice(1, -1)),
+               (slice(1, -1), slice(1, -1), slice(2, None)), (slice(1, -1), slice(1, -1), slice(None, -2))):
+        dvc += 0.5 * (pm[sl] + p0) * (mu[sl] - m0)
+    want = ci + dt * (dvc / dx2) / psp[1:-1, 1:-1, 1:-1]
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-14)
+    assert not np.allclose(got, ci, rtol=0, atol=1e-9)  # the step did move c
