@@ -223,10 +223,12 @@ int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p) {
 
 int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta, int flags) {
   if (!ctx || zc64 < 0 || zc32 < 0 || chunk < 0 || zc64 > 64 || zc32 > 64 || chunk > 1024 ||
-      !(delta >= 0.0 && delta < 1.0) || (flags & ~SBM_TUNE_NO_TMA))
+      !(delta >= 0.0 && delta < 1.0) || (flags & ~(SBM_TUNE_NO_TMA | SBM_TUNE_PC_ADDITIVE)))
     return SBM_ERR_ARG;
   const int no_tma = (flags & SBM_TUNE_NO_TMA) ? 1 : 0;
-  if (zc64 != ctx->zc64 || zc32 != ctx->zc32 || chunk != ctx->chunk || no_tma != ctx->no_tma) {
+  const int pc_add = (flags & SBM_TUNE_PC_ADDITIVE) ? 1 : 0;
+  if (zc64 != ctx->zc64 || zc32 != ctx->zc32 || chunk != ctx->chunk || no_tma != ctx->no_tma ||
+      pc_add != ctx->pc_additive) {
     cudaStreamSynchronize(ctx->stream);
     release_graphs(ctx);
   }
@@ -235,6 +237,7 @@ int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta
   ctx->chunk = chunk;
   ctx->inner_tol = delta;
   ctx->no_tma = no_tma;
+  ctx->pc_additive = pc_add;
   return SBM_OK;
 }
 

@@ -343,6 +343,7 @@ struct sbm_ctx {
   sbm::OpArgs<float> last_op32{};
   int last_pc = -1;
   int no_tma = 0;  // tuning flag: use the register-tiled FP32 stencil instead of TMA
+  int pc_additive = 0;  // tuning flag: additive learned preconditioner (no smoothing step)
   // learned preconditioner plan (opaque; owned by sbm_net.cu) and the
   // preconditioner the last mixed solve actually used
   void* net = nullptr;

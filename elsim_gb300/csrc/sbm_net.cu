@@ -734,66 +734,187 @@ __device__ __forceinline__ void interp1(int fi, int n, int* lo, int* hi, float* 
   *wlo = wl[e];
 }
 
-// z = invd*r + f * P(out) over the fine interior, f = s k_out / (scale
-// c_ref); z.r and z.q_old reduced; the last block sets rho, beta of the
+// x-interpolated coarse window of fine column jj for the coarse y cells
+// m-1..m+1 and z cells kc-1..kc+1 (clamped), w[y][z].
+__device__ __forceinline__ void xwin(const float* __restrict__ out, const Dims& c, int jj, int m,
+                                     int kc, float w[3][3]) {
+  int x0, x1;
+  float wx;
+  interp1(jj - 1, c.nx, &x0, &x1, &wx);
+  const int ys[3] = {max(m - 1, 0), m, min(m + 1, c.ny - 1)};
+  const int zs[3] = {max(kc - 1, 0), kc, min(kc + 1, c.nz - 1)};
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    const int64_t r0 = (int64_t)c.ny * (x0 + (int64_t)c.nx * zs[b]);
+    const int64_t r1 = (int64_t)c.ny * (x1 + (int64_t)c.nx * zs[b]);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) w[a][b] = wx * out[r0 + ys[a]] + (1.f - wx) * out[r1 + ys[a]];
+  }
+}
+
+// Weights of the cell-centred linear interpolation for the fine offsets
+// -1..4 of one coarse cell: value = w * C[lo] + (1 - w) * C[lo + 1] over
+// the window C[0..2] = coarse cells (m-1, m, m+1).
+__device__ __forceinline__ constexpr float win6(int t) {
+  return t == 0 ? 0.625f : t == 1 ? 0.375f : t == 2 ? 0.125f : t == 3 ? 0.875f
+       : t == 4 ? 0.625f : 0.375f;
+}
+__device__ __forceinline__ constexpr int lo6(int t) { return t < 3 ? 0 : 1; }
+
+// The coarse correction and its smoothing.  f = s k_out / (scale c_ref).
+//   additive (MULT = false):        z = invd*r + z1,  z1 = f P(out)
+//   multiplicative (MULT = true):   z = z1 + omega*invd*(r - A z1)
+// The multiplicative form evaluates A z1 (the FP32 operator with the
+// search-direction ghost rules) without storing z1: every thread rebuilds
+// z1 on its cells' 7-point neighbourhood from the coarse values (the x-1,
+// x, x+1 columns), so the only extra traffic is the half coefficient.
+// z.r and z.q_old are reduced; the last block sets rho, beta of the
 // flexible CG.  One item = 4 y-consecutive fine cells (one coarse cell in
-// y) on one x row, marched over the 4 fine planes of one coarse z cell, so
-// the coarse values (3 y x 2 x x 3 z) are loaded once for 16 cells.
+// y) on one x row, marched over the 4 fine planes of one coarse z cell.
+// With the coarse part switched off (pc_off) both forms are z = invd*r.
+template <bool MULT>
 __global__ void __launch_bounds__(256)
     k_pc_prolong(Geo g, Dims c, const float* __restrict__ out, const float* scal,
                  const float* __restrict__ r, const float* __restrict__ iv,
-                 const float* __restrict__ q, float* __restrict__ z, const int* err,
+                 const float* __restrict__ q, const float* __restrict__ hk, float scale,
+                 int bcx0, int bcx1, float omega, float* __restrict__ z, const int* err,
                  double* partials, CgState* st) {
   pdl_begin();
   if (st->done) return;
   const bool coarse = st->pc_off == 0;  // off: z = D^-1 r (Jacobi-PCG)
   const float f = coarse ? scal[0] * scal[2] : 0.f;
-  const int nchunk = g.ny / 4;
-  const int64_t n = (int64_t)nchunk * g.nx * (g.nz / 4);
-  const float wl[4] = {0.375f, 0.125f, 0.875f, 0.625f};
   float a_zr = 0.f, a_zq = 0.f;
-  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
-       u += (int64_t)gridDim.x * blockDim.x) {
-    const int m = (int)(u % nchunk);
-    const int64_t rr = u / nchunk;
-    const int j = (int)(rr % g.nx) + 1;
-    const int kc = (int)(rr / g.nx);
-    int x0, x1;
-    float wx;
-    interp1(j - 1, c.nx, &x0, &x1, &wx);
-    const int ys[3] = {max(m - 1, 0), m, min(m + 1, c.ny - 1)};
-    const int zs[3] = {max(kc - 1, 0), kc, min(kc + 1, c.nz - 1)};
-    float cx[3][3] = {};  // [y neighbour][z plane], interpolated in x
-    if (coarse) {
+  if (!MULT || !coarse) {
+    const int nchunk = g.ny / 4;
+    const int64_t n = (int64_t)nchunk * g.nx * (g.nz / 4);
+    const float wl[4] = {0.375f, 0.125f, 0.875f, 0.625f};
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+         u += (int64_t)gridDim.x * blockDim.x) {
+      const int m = (int)(u % nchunk);
+      const int64_t rr = u / nchunk;
+      const int j = (int)(rr % g.nx) + 1;
+      const int kc = (int)(rr / g.nx);
+      int x0, x1;
+      float wx;
+      interp1(j - 1, c.nx, &x0, &x1, &wx);
+      const int ys[3] = {max(m - 1, 0), m, min(m + 1, c.ny - 1)};
+      const int zs[3] = {max(kc - 1, 0), kc, min(kc + 1, c.nz - 1)};
+      float cx[3][3] = {};  // [y neighbour][z plane], interpolated in x
+      if (coarse) {
 #pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        const int64_t r0 = (int64_t)c.ny * (x0 + (int64_t)c.nx * zs[b]);
-        const int64_t r1 = (int64_t)c.ny * (x1 + (int64_t)c.nx * zs[b]);
+        for (int b = 0; b < 3; ++b) {
+          const int64_t r0 = (int64_t)c.ny * (x0 + (int64_t)c.nx * zs[b]);
+          const int64_t r1 = (int64_t)c.ny * (x1 + (int64_t)c.nx * zs[b]);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) cx[a][b] = wx * out[r0 + ys[a]] + (1.f - wx) * out[r1 + ys[a]];
+          for (int a = 0; a < 3; ++a) cx[a][b] = wx * out[r0 + ys[a]] + (1.f - wx) * out[r1 + ys[a]];
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int lo = e < 2 ? 0 : 1;  // coarse planes (lo, lo + 1) of fine plane e
+        const float wz = wl[e];
+        float col[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) col[a] = wz * cx[a][lo] + (1.f - wz) * cx[a][lo + 1];
+        const float e4[4] = {0.375f * col[0] + 0.625f * col[1], 0.125f * col[0] + 0.875f * col[1],
+                             0.875f * col[1] + 0.125f * col[2], 0.625f * col[1] + 0.375f * col[2]};
+        const int64_t idx = g.ix(4 * m + 1, j, 4 * kc + 1 + e);
+        const float4 rv = *reinterpret_cast<const float4*>(r + idx);
+        const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
+        const float4 qv = *reinterpret_cast<const float4*>(q + idx);
+        float4 zv;
+        zv.x = dv.x * rv.x + f * e4[0];
+        zv.y = dv.y * rv.y + f * e4[1];
+        zv.z = dv.z * rv.z + f * e4[2];
+        zv.w = dv.w * rv.w + f * e4[3];
+        *reinterpret_cast<float4*>(z + idx) = zv;
+        a_zr += (zv.x * rv.x + zv.y * rv.y) + (zv.z * rv.z + zv.w * rv.w);
+        a_zq += (zv.x * qv.x + zv.y * qv.y) + (zv.z * qv.z + zv.w * qv.w);
       }
     }
+  } else {
+    const int nchunk = g.ny / 4;
+    const int64_t n = (int64_t)nchunk * g.nx * (g.nz / 4);
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+         u += (int64_t)gridDim.x * blockDim.x) {
+      const int m = (int)(u % nchunk);
+      const int64_t rr = u / nchunk;
+      const int j = (int)(rr % g.nx) + 1;
+      const int kc = (int)(rr / g.nx);
+      // z1 of the centre column on fine planes -1..4 x fine y offsets -1..4
+      float zc[6][6], zm[4][4], zp[4][4];
+      {
+        float w[3][3];
+        xwin(out, c, j, m, kc, w);
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int lo = e < 2 ? 0 : 1;  // coarse planes (lo, lo + 1) of fine plane e
-      const float wz = wl[e];
-      float col[3];
+        for (int t = 0; t < 6; ++t) {
+          float col[3];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) col[a] = wz * cx[a][lo] + (1.f - wz) * cx[a][lo + 1];
-      const float e4[4] = {0.375f * col[0] + 0.625f * col[1], 0.125f * col[0] + 0.875f * col[1],
-                           0.875f * col[1] + 0.125f * col[2], 0.625f * col[1] + 0.375f * col[2]};
-      const int64_t idx = g.ix(4 * m + 1, j, 4 * kc + 1 + e);
-      const float4 rv = *reinterpret_cast<const float4*>(r + idx);
-      const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
-      const float4 qv = *reinterpret_cast<const float4*>(q + idx);
-      float4 zv;
-      zv.x = dv.x * rv.x + f * e4[0];
-      zv.y = dv.y * rv.y + f * e4[1];
-      zv.z = dv.z * rv.z + f * e4[2];
-      zv.w = dv.w * rv.w + f * e4[3];
-      *reinterpret_cast<float4*>(z + idx) = zv;
-      a_zr += (zv.x * rv.x + zv.y * rv.y) + (zv.z * rv.z + zv.w * rv.w);
-      a_zq += (zv.x * qv.x + zv.y * qv.y) + (zv.z * qv.z + zv.w * qv.w);
+          for (int a = 0; a < 3; ++a)
+            col[a] = win6(t) * w[a][lo6(t)] + (1.f - win6(t)) * w[a][lo6(t) + 1];
+#pragma unroll
+          for (int y = 0; y < 6; ++y)
+            zc[t][y] = f * (win6(y) * col[lo6(y)] + (1.f - win6(y)) * col[lo6(y) + 1]);
+        }
+      }
+      // z1 of the x-1 and x+1 columns on planes 0..3, y offsets 0..3
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        const int jj = side == 0 ? max(j - 1, 1) : min(j + 1, g.nx);
+        float w[3][3];
+        xwin(out, c, jj, m, kc, w);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          float col[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+            col[a] = win6(e + 1) * w[a][lo6(e + 1)] + (1.f - win6(e + 1)) * w[a][lo6(e + 1) + 1];
+#pragma unroll
+          for (int y = 0; y < 4; ++y) {
+            const float v = f * (win6(y + 1) * col[lo6(y + 1)] +
+                                 (1.f - win6(y + 1)) * col[lo6(y + 1) + 1]);
+            if (side == 0) zm[e][y] = v;
+            else zp[e][y] = v;
+          }
+        }
+      }
+      const int i0 = 4 * m + 1;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int k = 4 * kc + 1 + e;
+        const int64_t idx = g.ix(i0, j, k);
+        const float4 rv = *reinterpret_cast<const float4*>(r + idx);
+        const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
+        const float4 qv = *reinterpret_cast<const float4*>(q + idx);
+        const float4 k4 = *reinterpret_cast<const float4*>(hk + idx);
+        const float4 kx0 = *reinterpret_cast<const float4*>(hk + idx - g.sx);
+        const float4 kx1 = *reinterpret_cast<const float4*>(hk + idx + g.sx);
+        const float4 kz0 = *reinterpret_cast<const float4*>(hk + idx - g.sz);
+        const float4 kz1 = *reinterpret_cast<const float4*>(hk + idx + g.sz);
+        const float ky[6] = {hk[idx - 1], k4.x, k4.y, k4.z, k4.w, hk[idx + 4]};
+        const float kxa[4] = {kx0.x, kx0.y, kx0.z, kx0.w}, kxb[4] = {kx1.x, kx1.y, kx1.z, kx1.w};
+        const float kza[4] = {kz0.x, kz0.y, kz0.z, kz0.w}, kzb[4] = {kz1.x, kz1.y, kz1.z, kz1.w};
+        const float ra[4] = {rv.x, rv.y, rv.z, rv.w}, da[4] = {dv.x, dv.y, dv.z, dv.w};
+        const float qa[4] = {qv.x, qv.y, qv.z, qv.w};
+        float za[4];
+#pragma unroll
+        for (int y = 0; y < 4; ++y) {
+          const int i = i0 + y;
+          const float pc = zc[e + 1][y + 1];
+          const float pym = (i == 1) ? pc : zc[e + 1][y];
+          const float pyp = (i == g.ny) ? pc : zc[e + 1][y + 2];
+          const float pxm = (j == 1) ? (bcx0 ? 0.f : pc) : zm[e][y];
+          const float pxp = (j == g.nx) ? (bcx1 ? 0.f : pc) : zp[e][y];
+          const float pzm = (k == 1) ? pc : zc[e][y + 1];
+          const float pzp = (k == g.nz) ? pc : zc[e + 2][y + 1];
+          const float s = face_sum<float>(ky[y + 1], pc, ky[y + 2], pyp, ky[y], pym, kxb[y], pxp,
+                                          kxa[y], pxm, kzb[y], pzp, kza[y], pzm);
+          za[y] = pc + omega * (da[y] * (ra[y] - scale * s));
+          a_zr += za[y] * ra[y];
+          a_zq += za[y] * qa[y];
+        }
+        *reinterpret_cast<float4*>(z + idx) = make_float4(za[0], za[1], za[2], za[3]);
+      }
     }
   }
   double v[2] = {(double)a_zr, (double)a_zq}, tot[2];
@@ -821,6 +942,10 @@ struct NetPc {
   float* scal = nullptr; // s, 1/s, k_out/(scale c_ref), c_ref
   double* parts = nullptr;
   unsigned* cnt = nullptr;
+  // operator of the current solve, for the multiplicative smoothing step
+  const float* hk32 = nullptr;
+  float scale = 1.f;
+  int bcx0 = 0, bcx1 = 0;
   void release() {
     delete w;
     w = nullptr;
@@ -867,6 +992,10 @@ int net_pc_begin(sbm_ctx* ctx, const float* hk32, double scale, int bcx0, int bc
     SBM_CUDA_TRY(cudaMemsetAsync(pc->cnt, 0, sizeof(unsigned) * 4, s));
     SBM_CUDA_TRY(cudaMemsetAsync(pc->scal, 0, sizeof(float) * 8, s));
   }
+  pc->hk32 = hk32;
+  pc->scale = (float)scale;
+  pc->bcx0 = bcx0;
+  pc->bcx1 = bcx1;
   netd::k_pc_coef<<<netd::grid_for(c.v()), 256, 0, s>>>(g, c, hk32, pc->coefc, pc->parts, pc->cnt,
                                                          pc->scal, pc->kout, scale);
   netd::k_pc_feat<<<netd::grid_for(c.v()), 256, 0, s>>>(c, pc->coefc, pc->scal, bcx0, bcx1,
@@ -901,9 +1030,19 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   int64_t b = (items + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;
   if (b < 1) b = 1;
-  launch_pdl(netd::k_pc_prolong, dim3((unsigned)b), dim3(256), 0, s, g, c,
-             (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->zf + kOff32,
-             (const int*)pc->net->err, partials, st);
+  // the multiplicative form with an over-relaxed Jacobi step (omega = 1.5:
+  // flexible-CG iterations of the 128^3 validation solve fall from 92 with
+  // the additive form to 54; 53-55 for omega in 1.5..1.9)
+  if (ctx->pc_additive)
+    launch_pdl(netd::k_pc_prolong<false>, dim3((unsigned)b), dim3(256), 0, s, g, c,
+               (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->hk32,
+               pc->scale, pc->bcx0, pc->bcx1, 1.f, pc->zf + kOff32, (const int*)pc->net->err,
+               partials, st);
+  else
+    launch_pdl(netd::k_pc_prolong<true>, dim3((unsigned)b), dim3(256), 0, s, g, c,
+               (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->hk32,
+               pc->scale, pc->bcx0, pc->bcx1, 1.5f, pc->zf + kOff32, (const int*)pc->net->err,
+               partials, st);
   SBM_LAUNCHED(1);
 }
 

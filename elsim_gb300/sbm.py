@@ -34,6 +34,7 @@ LIB_PATH = _PKG / "libsbm_gb300.so"
 OK, ERR_ARG, ERR_CUDA, ERR_MAXIT, ERR_NONFINITE, ERR_BREAKDOWN, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT = (
     0, -1, -2, -3, -4, -5, -6, -7, -8)
 TUNE_NO_TMA = 1
+TUNE_PC_ADDITIVE = 2
 BC_COPY, BC_ZERO = 0, 1
 OP_CNE, OP_PHP, OP_PHE, OP_GENERIC = 0, 1, 2, 3
 STOP_REF_UPDATE, STOP_REF_RESID, STOP_REL_RES = 0, 1, 2
@@ -293,11 +294,14 @@ class Context:
         self.params = params
         _check(self.lib.sbm_ctx_set_params(self._h, C.byref(params)), "sbm_ctx_set_params")
 
-    def set_tuning(self, zc64=0, zc32=0, chunk=0, delta=0.0, no_tma=False) -> None:
-        """Launch-shape knobs (0 = built-in), the reliable-update factor and
-        the choice of the register-tiled instead of the TMA-staged stencil."""
-        _check(self.lib.sbm_ctx_set_tuning(self._h, zc64, zc32, chunk, delta,
-                                           TUNE_NO_TMA if no_tma else 0), "sbm_ctx_set_tuning")
+    def set_tuning(self, zc64=0, zc32=0, chunk=0, delta=0.0, no_tma=False,
+                   pc_additive=False) -> None:
+        """Launch-shape knobs (0 = built-in), the reliable-update factor, the
+        choice of the register-tiled instead of the TMA-staged stencil and of
+        the additive instead of the multiplicative learned preconditioner."""
+        flags = (TUNE_NO_TMA if no_tma else 0) | (TUNE_PC_ADDITIVE if pc_additive else 0)
+        _check(self.lib.sbm_ctx_set_tuning(self._h, zc64, zc32, chunk, delta, flags),
+               "sbm_ctx_set_tuning")
 
     def bench_kernel(self, which: int, reps: int = 20) -> tuple[float, float]:
         """(ms per launch, algorithmic bytes per launch) of a solver kernel."""

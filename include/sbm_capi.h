@@ -159,9 +159,14 @@ int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p);
  * per thread of the FP64 / FP32 stencil kernels, CG iterations per captured
  * graph chunk, and `delta` of the mixed solver (its FP64 residual is
  * recomputed whenever the FP32 residual norm has fallen by this factor;
- * default 0.1).  flags bit 0 (SBM_TUNE_NO_TMA): use the register-tiled FP32
- * stencil instead of the TMA-staged one.  No counterpart in the reference. */
+ * default 1e-2, 1e-3 with the learned preconditioner).  flags bit 0
+ * (SBM_TUNE_NO_TMA): use the register-tiled FP32 stencil instead of the
+ * TMA-staged one; bit 1 (SBM_TUNE_PC_ADDITIVE): apply the learned
+ * preconditioner in its additive form z = D^-1 r + P e_c instead of the
+ * default multiplicative one z = z1 + 1.5 D^-1 (r - A z1), z1 = P e_c.
+ * No counterpart in the reference. */
 #define SBM_TUNE_NO_TMA 1
+#define SBM_TUNE_PC_ADDITIVE 2
 int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta, int flags);
 /* The context's CUDA stream as an opaque handle (cudaStream_t). */
 int sbm_ctx_stream(sbm_ctx* ctx, void** stream);

@@ -268,13 +268,45 @@ def inv_diag(coef_h, scale, bcx0, bcx1):
     return np.where(d != 0, 1.0 / np.where(d != 0, d, 1.0), 0.0)
 
 
-def pc_apply(p, kout, coef_h, r_h, scale=1.0, bcx0=1, bcx1=1, rounding=True):
-    """z = D^-1 r + P e_c on the interior (halo-padded in and out)."""
+def apply_dir(coef_h, p_int, scale, bcx0, bcx1):
+    """scale * S(p) on the interior with the search-direction ghost rules
+    (y and z faces copy the edge cell, an x face is 0 when Dirichlet, else a
+    copy); faces hk_nb + hk_c, hk = K/2, in the order y+, y-, x+, x-, z+, z-."""
+    hk = 0.5 * np.asarray(coef_h, dtype=np.float64)
+    p = np.pad(np.asarray(p_int, dtype=np.float64), 1, mode="edge")
+    if bcx0:
+        p[:, 0, :] = 0.0
+    if bcx1:
+        p[:, -1, :] = 0.0
+    I = slice(1, -1)
+    kc, pc = hk[I, I, I], p[I, I, I]
+    s = (hk[2:, I, I] + kc) * (p[2:, I, I] - pc)
+    s = s - (kc + hk[:-2, I, I]) * (pc - p[:-2, I, I])
+    s = s + (hk[I, 2:, I] + kc) * (p[I, 2:, I] - pc)
+    s = s - (kc + hk[I, :-2, I]) * (pc - p[I, :-2, I])
+    s = s + (hk[I, I, 2:] + kc) * (p[I, I, 2:] - pc)
+    s = s - (kc + hk[I, I, :-2]) * (pc - p[I, I, :-2])
+    return scale * s
+
+
+OMEGA = 1.5  # weight of the Jacobi step of the multiplicative form
+
+
+def pc_apply(p, kout, coef_h, r_h, scale=1.0, bcx0=1, bcx1=1, rounding=True,
+             multiplicative=True, omega=OMEGA):
+    """The learned preconditioner on the interior (halo-padded in and out):
+    z1 = P e_c, then z = z1 + omega D^-1 (r - A z1) (multiplicative, the
+    default) or z = D^-1 r + z1 (additive)."""
     r = r_h[1:-1, 1:-1, 1:-1]
     coef = coef_h[1:-1, 1:-1, 1:-1]
     f, s, cref = features(r, coef, bcx0, bcx1)
     out, _ = forward(p, f, rounding)
     ec = from_cl(out) * s * kout / (scale * cref)
+    z1 = prolong(ec)
+    invd = inv_diag(coef_h, scale, bcx0, bcx1)
     z = np.zeros_like(r_h)
-    z[1:-1, 1:-1, 1:-1] = inv_diag(coef_h, scale, bcx0, bcx1) * r + prolong(ec)
+    if multiplicative:
+        z[1:-1, 1:-1, 1:-1] = z1 + omega * (invd * (r - apply_dir(coef_h, z1, scale, bcx0, bcx1)))
+    else:
+        z[1:-1, 1:-1, 1:-1] = invd * r + z1
     return z
