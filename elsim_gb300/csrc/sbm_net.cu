@@ -734,57 +734,23 @@ __device__ __forceinline__ void interp1(int fi, int n, int* lo, int* hi, float* 
   *wlo = wl[e];
 }
 
-// x-interpolated coarse window of fine column jj for the coarse y cells
-// m-1..m+1 and z cells kc-1..kc+1 (clamped), w[y][z].
-__device__ __forceinline__ void xwin(const float* __restrict__ out, const Dims& c, int jj, int m,
-                                     int kc, float w[3][3]) {
-  int x0, x1;
-  float wx;
-  interp1(jj - 1, c.nx, &x0, &x1, &wx);
-  const int ys[3] = {max(m - 1, 0), m, min(m + 1, c.ny - 1)};
-  const int zs[3] = {max(kc - 1, 0), kc, min(kc + 1, c.nz - 1)};
-#pragma unroll
-  for (int b = 0; b < 3; ++b) {
-    const int64_t r0 = (int64_t)c.ny * (x0 + (int64_t)c.nx * zs[b]);
-    const int64_t r1 = (int64_t)c.ny * (x1 + (int64_t)c.nx * zs[b]);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) w[a][b] = wx * out[r0 + ys[a]] + (1.f - wx) * out[r1 + ys[a]];
-  }
-}
-
-// Weights of the cell-centred linear interpolation for the fine offsets
-// -1..4 of one coarse cell: value = w * C[lo] + (1 - w) * C[lo + 1] over
-// the window C[0..2] = coarse cells (m-1, m, m+1).
-__device__ __forceinline__ constexpr float win6(int t) {
-  return t == 0 ? 0.625f : t == 1 ? 0.375f : t == 2 ? 0.125f : t == 3 ? 0.875f
-       : t == 4 ? 0.625f : 0.375f;
-}
-__device__ __forceinline__ constexpr int lo6(int t) { return t < 3 ? 0 : 1; }
-
-// The coarse correction and its smoothing.  f = s k_out / (scale c_ref).
-//   additive (MULT = false):        z = invd*r + z1,  z1 = f P(out)
-//   multiplicative (MULT = true):   z = z1 + omega*invd*(r - A z1)
-// The multiplicative form evaluates A z1 (the FP32 operator with the
-// search-direction ghost rules) without storing z1: every thread rebuilds
-// z1 on its cells' 7-point neighbourhood from the coarse values (the x-1,
-// x, x+1 columns), so the only extra traffic is the half coefficient.
-// z.r and z.q_old are reduced; the last block sets rho, beta of the
-// flexible CG.  One item = 4 y-consecutive fine cells (one coarse cell in
-// y) on one x row, marched over the 4 fine planes of one coarse z cell.
-// With the coarse part switched off (pc_off) both forms are z = invd*r.
-template <bool MULT>
+// z = invd*r + f * P(out) over the fine interior (the additive form), f =
+// s k_out / (scale c_ref); z.r and z.q_old reduced; the last block sets rho,
+// beta of the flexible CG.  One item = 4 y-consecutive fine cells (one
+// coarse cell in y) on one x row, marched over the 4 fine planes of one
+// coarse z cell, so the coarse values (3 y x 2 x x 3 z) are loaded once for
+// 16 cells.  With the coarse part switched off (pc_off): z = invd*r.
 __global__ void __launch_bounds__(256)
     k_pc_prolong(Geo g, Dims c, const float* __restrict__ out, const float* scal,
                  const float* __restrict__ r, const float* __restrict__ iv,
-                 const float* __restrict__ q, const float* __restrict__ hk, float scale,
-                 int bcx0, int bcx1, float omega, float* __restrict__ z, const int* err,
+                 const float* __restrict__ q, float* __restrict__ z, const int* err,
                  double* partials, CgState* st) {
   pdl_begin();
   if (st->done) return;
   const bool coarse = st->pc_off == 0;  // off: z = D^-1 r (Jacobi-PCG)
   const float f = coarse ? scal[0] * scal[2] : 0.f;
   float a_zr = 0.f, a_zq = 0.f;
-  if (!MULT || !coarse) {
+  {
     const int nchunk = g.ny / 4;
     const int64_t n = (int64_t)nchunk * g.nx * (g.nz / 4);
     const float wl[4] = {0.375f, 0.125f, 0.875f, 0.625f};
@@ -832,60 +798,130 @@ __global__ void __launch_bounds__(256)
         a_zq += (zv.x * qv.x + zv.y * qv.y) + (zv.z * qv.z + zv.w * qv.w);
       }
     }
-  } else {
-    const int nchunk = g.ny / 4;
-    const int64_t n = (int64_t)nchunk * g.nx * (g.nz / 4);
-    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
-         u += (int64_t)gridDim.x * blockDim.x) {
-      const int m = (int)(u % nchunk);
-      const int64_t rr = u / nchunk;
-      const int j = (int)(rr % g.nx) + 1;
-      const int kc = (int)(rr / g.nx);
-      // z1 of the centre column on fine planes -1..4 x fine y offsets -1..4
-      float zc[6][6], zm[4][4], zp[4][4];
-      {
-        float w[3][3];
-        xwin(out, c, j, m, kc, w);
+  }
+  double v[2] = {(double)a_zr, (double)a_zq}, tot[2];
+  if (grid_reduce<2>(v, partials, &st->counter[5], tot)) {
+    if (threadIdx.x == 0) {
+      const double zr = tot[0];
+      const double beta = st->initial ? 0.0 : -tot[1] / st->pq;
+      st->initial = 0;
+      st->rho = zr;
+      st->beta = beta;
+      if (*err) st->done = 5;
+      else if (!isfinite(zr) || !isfinite(beta)) st->done = 3;
+    }
+  }
+}
+
+// The multiplicative form z = z1 + omega*invd*(r - A z1), z1 = f P(out), by
+// tiles of 64 (y) x 8 (x) x 4 (z) fine cells.  The block interpolates the
+// coarse window (18 y x 4 x x 3 z cells, clamped) in x and then in z onto
+// the tile's fine x / z positions with their one-cell halo, in shared
+// memory (the order of k_pc_prolong); each thread then takes 4
+// y-consecutive cells (one coarse y cell), interpolates z1 in y for them
+// and their 6 neighbours from three coarse values per row, and applies the
+// FP32 operator with the search-direction ghost rules.  Global traffic per
+// cell: r, invd, q_old and hk read, z written (20 B); the coarse values come
+// from L2.  z.r and z.q_old are reduced as in k_pc_prolong.  Tiles are
+// walked grid-stride (every block the same count: the barriers are uniform).
+constexpr int kMTY = 64, kMTX = 8, kMTZ = 4;
+constexpr int kWY = kMTY / 4 + 2;  // coarse y window
+__global__ void __launch_bounds__(256, 3)
+    k_pc_mult_tiled(Geo g, Dims c, const float* __restrict__ out, const float* scal,
+                    const float* __restrict__ r, const float* __restrict__ iv,
+                    const float* __restrict__ q, const float* __restrict__ hk, float scale,
+                    int bcx0, int bcx1, float omega, float* __restrict__ z, const int* err,
+                    double* partials, CgState* st) {
+  __shared__ float sA[3][kMTX / 4 + 2][kWY];
+  __shared__ float sB[3][kMTX + 2][kWY];
+  __shared__ float sC[kMTZ + 2][kMTX + 2][kWY];
+  pdl_begin();
+  if (st->done) return;
+  const bool coarse = st->pc_off == 0;  // off: z = D^-1 r (Jacobi-PCG)
+  const float f = coarse ? scal[0] * scal[2] : 0.f;
+  const int tid = threadIdx.x;
+  const int nty = g.ny / kMTY, ntx = g.nx / kMTX;
+  const int64_t ntiles = (int64_t)nty * ntx * (g.nz / kMTZ);
+  // per-thread roles of the staging loops: (x, y) column of the windows
+  const int col_y = tid % kWY, col_x = tid / kWY;  // col_x < kMTX + 2 for tid < 180
+  float a_zr = 0.f, a_zq = 0.f;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int by = (int)(tile % nty);
+    const int bx = (int)((tile / nty) % ntx);
+    const int bz = (int)(tile / ((int64_t)nty * ntx));
+    const int y0 = kMTY * by + 1, x0 = kMTX * bx + 1, z0 = kMTZ * bz + 1;
+    // coarse index of window entry 0 in y, x, z
+    const int cy0 = (kMTY / 4) * by - 1, cx0 = (kMTX / 4) * bx - 1, cz0 = bz - 1;
+    if (coarse) {
+      __syncthreads();  // the previous tile's readers are done
+      if (col_x < kMTX / 4 + 2) {
+        const int cy = min(max(cy0 + col_y, 0), c.ny - 1);
+        const int cx = min(max(cx0 + col_x, 0), c.nx - 1);
 #pragma unroll
-        for (int t = 0; t < 6; ++t) {
-          float col[3];
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-            col[a] = win6(t) * w[a][lo6(t)] + (1.f - win6(t)) * w[a][lo6(t) + 1];
-#pragma unroll
-          for (int y = 0; y < 6; ++y)
-            zc[t][y] = f * (win6(y) * col[lo6(y)] + (1.f - win6(y)) * col[lo6(y) + 1]);
+        for (int zz = 0; zz < 3; ++zz) {
+          const int cz = min(max(cz0 + zz, 0), c.nz - 1);
+          sA[zz][col_x][col_y] = out[cy + (int64_t)c.ny * (cx + (int64_t)c.nx * cz)];
         }
       }
-      // z1 of the x-1 and x+1 columns on planes 0..3, y offsets 0..3
+      __syncthreads();
+      if (col_x < kMTX + 2) {  // x interpolation to the fine x positions x0-1 .. x0+kMTX
+        int lo, hi;
+        float w;
+        interp1(x0 - 2 + col_x, c.nx, &lo, &hi, &w);
 #pragma unroll
-      for (int side = 0; side < 2; ++side) {
-        const int jj = side == 0 ? max(j - 1, 1) : min(j + 1, g.nx);
-        float w[3][3];
-        xwin(out, c, jj, m, kc, w);
+        for (int zz = 0; zz < 3; ++zz)
+          sB[zz][col_x][col_y] = w * sA[zz][lo - cx0][col_y] + (1.f - w) * sA[zz][hi - cx0][col_y];
+      }
+      __syncthreads();
+      if (col_x < kMTX + 2) {  // z interpolation to the fine planes z0-1 .. z0+kMTZ
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          float col[3];
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-            col[a] = win6(e + 1) * w[a][lo6(e + 1)] + (1.f - win6(e + 1)) * w[a][lo6(e + 1) + 1];
-#pragma unroll
-          for (int y = 0; y < 4; ++y) {
-            const float v = f * (win6(y + 1) * col[lo6(y + 1)] +
-                                 (1.f - win6(y + 1)) * col[lo6(y + 1) + 1]);
-            if (side == 0) zm[e][y] = v;
-            else zp[e][y] = v;
-          }
+        for (int zf = 0; zf < kMTZ + 2; ++zf) {
+          int lo, hi;
+          float w;
+          interp1(z0 - 2 + zf, c.nz, &lo, &hi, &w);
+          sC[zf][col_x][col_y] =
+              f * (w * sB[lo - cz0][col_x][col_y] + (1.f - w) * sB[hi - cz0][col_x][col_y]);
         }
       }
-      const int i0 = 4 * m + 1;
+      __syncthreads();
+    }
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      const int u = tid + 256 * h;
+      const int mq = u % (kMTY / 4), xl = (u / (kMTY / 4)) % kMTX, zl = u / ((kMTY / 4) * kMTX);
+      const int i0 = y0 + 4 * mq, j = x0 + xl, k = z0 + zl;
+      const int64_t idx = g.ix(i0, j, k);
+      const float4 rv = *reinterpret_cast<const float4*>(r + idx);
+      const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
+      const float4 qv = *reinterpret_cast<const float4*>(q + idx);
+      const float ra[4] = {rv.x, rv.y, rv.z, rv.w}, da[4] = {dv.x, dv.y, dv.z, dv.w};
+      const float qa[4] = {qv.x, qv.y, qv.z, qv.w};
+      float za[4];
+      if (coarse) {
+        const int xf = 1 + xl, zf = 1 + zl;
+        // y interpolation: coarse cells (m-1, m, m+1) are window entries
+        // mq, mq+1, mq+2; fine offsets -1..4 of this coarse cell
+        float cen[6], ym[4], yp[4], zm4[4], zp4[4];
+        {
+          const float a0 = sC[zf][xf][mq], a1 = sC[zf][xf][mq + 1], a2 = sC[zf][xf][mq + 2];
+          cen[0] = 0.625f * a0 + 0.375f * a1;
+          cen[1] = 0.375f * a0 + 0.625f * a1;
+          cen[2] = 0.125f * a0 + 0.875f * a1;
+          cen[3] = 0.875f * a1 + 0.125f * a2;
+          cen[4] = 0.625f * a1 + 0.375f * a2;
+          cen[5] = 0.375f * a1 + 0.625f * a2;
+        }
+        const float* rows[4] = {&sC[zf][xf - 1][0], &sC[zf][xf + 1][0], &sC[zf - 1][xf][0],
+                                &sC[zf + 1][xf][0]};
+        float* dst[4] = {ym, yp, zm4, zp4};
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int k = 4 * kc + 1 + e;
-        const int64_t idx = g.ix(i0, j, k);
-        const float4 rv = *reinterpret_cast<const float4*>(r + idx);
-        const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
-        const float4 qv = *reinterpret_cast<const float4*>(q + idx);
+        for (int t = 0; t < 4; ++t) {
+          const float a0 = rows[t][mq], a1 = rows[t][mq + 1], a2 = rows[t][mq + 2];
+          dst[t][0] = 0.375f * a0 + 0.625f * a1;
+          dst[t][1] = 0.125f * a0 + 0.875f * a1;
+          dst[t][2] = 0.875f * a1 + 0.125f * a2;
+          dst[t][3] = 0.625f * a1 + 0.375f * a2;
+        }
         const float4 k4 = *reinterpret_cast<const float4*>(hk + idx);
         const float4 kx0 = *reinterpret_cast<const float4*>(hk + idx - g.sx);
         const float4 kx1 = *reinterpret_cast<const float4*>(hk + idx + g.sx);
@@ -894,27 +930,37 @@ __global__ void __launch_bounds__(256)
         const float ky[6] = {hk[idx - 1], k4.x, k4.y, k4.z, k4.w, hk[idx + 4]};
         const float kxa[4] = {kx0.x, kx0.y, kx0.z, kx0.w}, kxb[4] = {kx1.x, kx1.y, kx1.z, kx1.w};
         const float kza[4] = {kz0.x, kz0.y, kz0.z, kz0.w}, kzb[4] = {kz1.x, kz1.y, kz1.z, kz1.w};
-        const float ra[4] = {rv.x, rv.y, rv.z, rv.w}, da[4] = {dv.x, dv.y, dv.z, dv.w};
-        const float qa[4] = {qv.x, qv.y, qv.z, qv.w};
-        float za[4];
+        // ghost rules only for the cells on a domain face
+        if (i0 == 1 || i0 + 3 == g.ny || j == 1 || j == g.nx || k == 1 || k == g.nz) {
+          if (i0 == 1) cen[0] = cen[1];
+          if (i0 + 3 == g.ny) cen[5] = cen[4];
+#pragma unroll
+          for (int y = 0; y < 4; ++y) {
+            const float pc = cen[y + 1];
+            if (j == 1) ym[y] = bcx0 ? 0.f : pc;
+            if (j == g.nx) yp[y] = bcx1 ? 0.f : pc;
+            if (k == 1) zm4[y] = pc;
+            if (k == g.nz) zp4[y] = pc;
+          }
+        }
 #pragma unroll
         for (int y = 0; y < 4; ++y) {
-          const int i = i0 + y;
-          const float pc = zc[e + 1][y + 1];
-          const float pym = (i == 1) ? pc : zc[e + 1][y];
-          const float pyp = (i == g.ny) ? pc : zc[e + 1][y + 2];
-          const float pxm = (j == 1) ? (bcx0 ? 0.f : pc) : zm[e][y];
-          const float pxp = (j == g.nx) ? (bcx1 ? 0.f : pc) : zp[e][y];
-          const float pzm = (k == 1) ? pc : zc[e][y + 1];
-          const float pzp = (k == g.nz) ? pc : zc[e + 2][y + 1];
-          const float s = face_sum<float>(ky[y + 1], pc, ky[y + 2], pyp, ky[y], pym, kxb[y], pxp,
-                                          kxa[y], pxm, kzb[y], pzp, kza[y], pzm);
-          za[y] = pc + omega * (da[y] * (ra[y] - scale * s));
-          a_zr += za[y] * ra[y];
-          a_zq += za[y] * qa[y];
+          const float pc = cen[y + 1];
+          const float sv = face_sum<float>(ky[y + 1], pc, ky[y + 2], cen[y + 2], ky[y], cen[y],
+                                           kxb[y], yp[y], kxa[y], ym[y], kzb[y], zp4[y], kza[y],
+                                           zm4[y]);
+          za[y] = pc + omega * (da[y] * (ra[y] - scale * sv));
         }
-        *reinterpret_cast<float4*>(z + idx) = make_float4(za[0], za[1], za[2], za[3]);
+      } else {
+#pragma unroll
+        for (int y = 0; y < 4; ++y) za[y] = da[y] * ra[y];
       }
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        a_zr += za[y] * ra[y];
+        a_zq += za[y] * qa[y];
+      }
+      *reinterpret_cast<float4*>(z + idx) = make_float4(za[0], za[1], za[2], za[3]);
     }
   }
   double v[2] = {(double)a_zr, (double)a_zq}, tot[2];
@@ -1033,16 +1079,19 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   // the multiplicative form with an over-relaxed Jacobi step (omega = 1.5:
   // flexible-CG iterations of the 128^3 validation solve fall from 92 with
   // the additive form to 54; 53-55 for omega in 1.5..1.9)
-  if (ctx->pc_additive)
-    launch_pdl(netd::k_pc_prolong<false>, dim3((unsigned)b), dim3(256), 0, s, g, c,
-               (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->hk32,
-               pc->scale, pc->bcx0, pc->bcx1, 1.f, pc->zf + kOff32, (const int*)pc->net->err,
-               partials, st);
-  else
-    launch_pdl(netd::k_pc_prolong<true>, dim3((unsigned)b), dim3(256), 0, s, g, c,
-               (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->hk32,
-               pc->scale, pc->bcx0, pc->bcx1, 1.5f, pc->zf + kOff32, (const int*)pc->net->err,
-               partials, st);
+  if (ctx->pc_additive) {
+    launch_pdl(netd::k_pc_prolong, dim3((unsigned)b), dim3(256), 0, s, g, c,
+               (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->zf + kOff32,
+               (const int*)pc->net->err, partials, st);
+  } else {
+    const int64_t tiles =
+        (int64_t)(g.ny / netd::kMTY) * (g.nx / netd::kMTX) * (g.nz / netd::kMTZ);
+    // one wave of resident blocks (3 per SM at 80 registers), grid-stride
+    const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
+    launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, c, (const float*)pc->w->out,
+               (const float*)pc->scal, r32, iv32, q32, pc->hk32, pc->scale, pc->bcx0, pc->bcx1,
+               1.5f, pc->zf + kOff32, (const int*)pc->net->err, partials, st);
+  }
   SBM_LAUNCHED(1);
 }
 
