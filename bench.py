@@ -11,12 +11,14 @@ ghost planes, Neumann elsewhere, zero right-hand side; solved until
 
 Our arm (default): the production solver -- FP32 flexible CG with the
 learned coarse-grid preconditioner (a 3D U-Net on the 4x-coarsened grid,
-BF16 tcgen05 convolutions, weights elsim_gb300/weights/pc_unet.npz) and FP64
-reliable-update refinement -- with fields resident in HBM; `value` is the
-mean device time of one solve (CUDA events on the solver stream), `e2e` the
-same solve through the C-ABI from pinned host buffers (coef/x/rhs uploaded,
-x downloaded) timed on the wall clock.  The plain FP64 CG (the drop-in) and
-the FP32 Jacobi-PCG are timed beside it (`--pc jacobi` makes Jacobi-PCG the
+BF16 tcgen05 convolutions, weights elsim_gb300/weights/pc_unet.bin) applied
+multiplicatively (coarse correction, then one Jacobi step with omega 1.5)
+and FP64 reliable-update refinement -- with fields resident in HBM; `value`
+is the mean device time of one solve (CUDA events on the solver stream),
+`e2e` the same solve through the C-ABI from pinned host buffers
+(coef/x/rhs uploaded, x downloaded) timed on the wall clock.  The plain FP64
+CG (the drop-in), the FP32 Jacobi-PCG and the additive form of the learned
+preconditioner are timed beside it (`--pc jacobi` makes Jacobi-PCG the
 headline).
 
 --impl reference: the reference's algorithm (plain FP64 CG, its own
