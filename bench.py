@@ -56,6 +56,9 @@ METRIC = "sbm_potential_solve_time_256^3_relres_1e-8"
 # at 256^3 (ncu): with the Jacobi read (Jacobi-PCG) and without it (flexible
 # CG with the learned preconditioner).
 APPLY_TRAFFIC = {1: 398.2e6, 2: 326.2e6}
+# dram__bytes_read.sum + dram__bytes_write.sum of the 9 k_conv3_tc launches
+# of one preconditioner application at 256^3 (ncu); None until captured
+CONV_TRAFFIC = None
 UNIT = "s"
 
 
@@ -316,13 +319,18 @@ def run_ours(args):
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_local = float(tt.item())
     value = statistics.mean(times) if ws == 1 else t_local
-    # roofline of the dominant kernel (the fused direction + stencil kernel of
-    # the headline solve's inner loop), timed live on the solver stream
+    # kernel timings live on the solver stream: the fused direction + stencil
+    # kernel (HBM roofline; the headline roofline for Jacobi-PCG) and, with
+    # the learned preconditioner, its parts (the U-Net convolutions are the
+    # dominant kernel of that solve: tensor roofline)
     ms_k, bytes_k = ctx.bench_kernel(0, 20)
     extra = {}
+    roofline = None
     if used_pc == sbm.PC_LEARNED:
         ms_pc, bytes_pc = ctx.bench_kernel(3, 20)
         ms_u, bytes_u = ctx.bench_kernel(4, 20)
+        ms_cv, _ = ctx.bench_kernel(5, 20)
+        ms_m, bytes_m = ctx.bench_kernel(6, 20)
         fl = unet_flops(n)
         tpk, tkind = _bf16_peak()
         extra["preconditioner_application"] = {
@@ -332,10 +340,28 @@ def run_ours(args):
             "bf16_peak_tflops": tpk, "bf16_peak_kind": tkind,
             "note": "the convolutions are latency / shared-memory bound (small N, few CTAs on "
                     "the coarse levels), far from the tensor peak"}
+        extra["multiplicative_step_kernel"] = {
+            "kernel": "k_pc_mult_tiled", "ms": ms_m,
+            "GB/s": bytes_m / (ms_m * 1e-3) / 1e9, "bound": "hbm"}
+        # the dominant kernel of the solve (32 % of its time over 9 launches
+        # per iteration): the U-Net convolutions on the tensor cores
+        ach = fl / (ms_cv * 1e-3) / 1e12
+        roofline = {"bound": "tensor", "kernel": "k_conv3_tc (the 9 U-Net convolutions of one "
+                                                    "preconditioner application, BF16 tcgen05)",
+                    "achieved": ach, "peak": tpk, "unit": "TFLOP/s", "frac": ach / tpk,
+                    "peak_kind": tkind, "traffic": CONV_TRAFFIC, "algorithmic_flops": fl,
+                    "ms": ms_cv}
     else:
         ms_u, bytes_u = ctx.bench_kernel(1, 20)
     peak, peak_kind = _peaks()
     achieved = bytes_k / (ms_k * 1e-3) / 1e9
+    apply_roofline = {"bound": "hbm", "kernel": "k32t_apply_dir (TMA-staged FP32 direction+stencil)"
+                      + (", no Jacobi read (flexible CG)" if used_pc == sbm.PC_LEARNED else ""),
+                      "achieved": achieved, "peak": peak, "unit": "GB/s",
+                      "frac": achieved / peak, "peak_kind": peak_kind,
+                      # DRAM read+write of one launch (ncu capture of the same variant)
+                      "traffic": APPLY_TRAFFIC.get(used_pc),
+                      "algorithmic_bytes": bytes_k, "ms": ms_k}
     # e2e through the C-ABI with pinned host buffers
     pin = {}
     for k in ("coef", "x", "rhs"):
@@ -394,17 +420,12 @@ def run_ours(args):
                 "wall_s_timed_region": wall,
                 "update_kernel": {"ms": ms_u, "GB/s": bytes_u / (ms_u * 1e-3) / 1e9},
                 **extra,
+                "direction_stencil_kernel": apply_roofline,
                 "fp64_stencil_kernel": {"ms": fp64_ms[0],
                                         "GB/s": fp64_ms[1] / (fp64_ms[0] * 1e-3) / 1e9,
                                         "bound": "fp64 alu"},
             }),
-            "roofline": {"bound": "hbm", "kernel": "k32t_apply_dir (TMA-staged FP32 direction+stencil)"
-                                                    + (", no Jacobi read (flexible CG)" if used_pc == sbm.PC_LEARNED else ""),
-                         "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind,
-                         # DRAM read+write of one launch (ncu capture of the same variant)
-                         "traffic": APPLY_TRAFFIC.get(used_pc),
-                         "algorithmic_bytes": bytes_k, "ms": ms_k},
+            "roofline": roofline or apply_roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": 3 * nh * 8,
                     "d2h_bytes_per_step": nh * 8},

@@ -1095,6 +1095,23 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   SBM_LAUNCHED(1);
 }
 
+void net_pc_launch_part(sbm_ctx* ctx, int part, const float* r32, const float* iv32,
+                        const float* q32, double* partials, CgState* st, cudaStream_t s) {
+  netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
+  const Geo& g = ctx->g32;
+  const netd::Dims& c = pc->c;
+  if (part == 0) {
+    netd::forward(pc->net, *pc->w, false, &st->done, &st->pc_off, s);
+    return;
+  }
+  const int64_t tiles = (int64_t)(g.ny / netd::kMTY) * (g.nx / netd::kMTX) * (g.nz / netd::kMTZ);
+  const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
+  launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, c, (const float*)pc->w->out,
+             (const float*)pc->scal, r32, iv32, q32, pc->hk32, pc->scale, pc->bcx0, pc->bcx1,
+             1.5f, pc->zf + kOff32, (const int*)pc->net->err, partials, st);
+  SBM_LAUNCHED(1);
+}
+
 void net_pc_release(sbm_ctx* ctx) {
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   if (!pc) return;

@@ -31,6 +31,10 @@ float* net_pc_rc(sbm_ctx* ctx);
 float* net_pc_scal(sbm_ctx* ctx);
 // Kernel launches of one net_pc_launch.
 int net_pc_nodes();
+// One part of net_pc_launch for timing: 0 = the 9 U-Net convolutions on the
+// current input, 1 = the multiplicative prolongation / Jacobi step.
+void net_pc_launch_part(sbm_ctx* ctx, int part, const float* r32, const float* iv32,
+                        const float* q32, double* partials, CgState* st, cudaStream_t s);
 
 void net_pc_release(sbm_ctx* ctx);
 

@@ -1257,7 +1257,7 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
 //   which 2: the FP64 stencil + dot kernel of the plain CG
 // and reports the algorithmic bytes one launch moves.
 int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double* bytes_per_launch) {
-  if (reps < 1 || which < 0 || which > 4) return SBM_ERR_ARG;
+  if (reps < 1 || which < 0 || which > 6) return SBM_ERR_ARG;
   if (which != 2 && ctx->last_pc < 0) return SBM_ERR_STATE;
   if (which >= 3 && (ctx->last_precond != SBM_PC_LEARNED || !net_pc_usable(ctx, 0)))
     return SBM_ERR_STATE;
@@ -1318,6 +1318,8 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
       }
     } else if (which == 3) {
       net_pc_launch(ctx, r32, iv, q32, ctx->partials, ctx->st32, s);
+    } else if (which == 5 || which == 6) {
+      net_pc_launch_part(ctx, which - 5, r32, iv, q32, ctx->partials, ctx->st32, s);
     } else if (which == 4) {
       const dim3 cgrid((unsigned)std::min<int64_t>(
           std::max<int64_t>((int64_t)nchunk * g.nx * g.nz / 16 / 256, 1), 152 * 8));
@@ -1348,8 +1350,11 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
   double words;
   if (which == 0) words = 5.0 + (pc ? 1.0 : 0.0) + (op32.form ? 1.0 : 0.0);  // r,p_old,hk,[invd],[diag] -> p_new,q
   else if (which == 1) words = 6.0 + (pc ? 1.0 : 0.0);                       // x,p,r,q,[invd] -> x,r
-  else if (which == 3) words = 5.0;  // restriction r; prolongation r,invd,q -> z (coarse grid not counted)
+  // restriction r; prolongation r,invd,q,[hk] -> z (coarse grid not counted)
+  else if (which == 3) words = ctx->pc_additive ? 5.0 : 6.0;
   else if (which == 4) words = 6.0;  // x,p,r,q -> x,r (+ the coarse means)
+  else if (which == 5) words = 0.0;  // convolutions: coarse grid only (flops, not fine bytes)
+  else if (which == 6) words = 5.0;  // r,invd,q,hk -> z
   else words = 3.0;                                                          // p,hk -> q (FP64)
   if (bytes_per_launch) *bytes_per_launch = words * (which == 2 ? 8.0 : 4.0) * n;
   return SBM_OK;
