@@ -182,8 +182,13 @@ __device__ __forceinline__ void expect_tx(uint64_t* bar, unsigned bytes) {
 // MMAs of N = nt.  Two planes (accumulators at columns 0 and nt): per
 // (dy, dx) four MMAs, halo planes 1 and 2 with N = 2 nt feeding both
 // accumulators (rows [W0 | W-1] and [W+1 | W0]), planes 0 and 3 with N = nt.
+// Four planes (accumulators at 0, nt, 2nt, 3nt): halo plane h feeds the
+// outputs h-2 .. h with dz = +1, 0, -1, so planes 2 and 3 are one MMA of
+// N = 3 nt over rows [W+1 | W0 | W-1] each; planes 1 and 4 (N = 2 nt) come
+// first, as each of them starts two accumulators that no earlier MMA of the
+// chunk touched.
 __device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t bd, int nt, int P,
-                                           uint32_t id1, uint32_t id2, bool acc) {
+                                           uint32_t id1, uint32_t id2, uint32_t id3, bool acc) {
 #pragma unroll
   for (int qq = 0; qq < 9; ++qq) {
     const int dy = qq % 3 - 1, dx = qq / 3 - 1;
@@ -195,11 +200,19 @@ __device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t 
       tc_mma(tmem, a0 + (uint64_t)(1 * HX * HY), b + (uint64_t)(2 * nt), id1, first);  // dz = 0
       tc_mma(tmem, a0, b + (uint64_t)(4 * nt), id1, 1u);                               // dz = -1
       tc_mma(tmem, a0 + (uint64_t)(2 * HX * HY), b, id1, 1u);                          // dz = +1
-    } else {
+    } else if (P == 2) {
       tc_mma(tmem, a0 + (uint64_t)(1 * HX * HY), b + (uint64_t)(2 * nt), id2, first);  // h = 1
       tc_mma(tmem, a0, b + (uint64_t)(4 * nt), id1, 1u);                               // h = 0
       tc_mma(tmem, a0 + (uint64_t)(2 * HX * HY), b, id2, 1u);                          // h = 2
       tc_mma(tmem + (uint32_t)nt, a0 + (uint64_t)(3 * HX * HY), b, id1, 1u);           // h = 3
+    } else {
+      const uint32_t hs = (uint32_t)(HX * HY);
+      tc_mma(tmem, a0 + 1 * hs, b + (uint64_t)(2 * nt), id2, first);           // h = 1: o0, o1
+      tc_mma(tmem + (uint32_t)(2 * nt), a0 + 4 * hs, b, id2, first);           // h = 4: o2, o3
+      tc_mma(tmem, a0, b + (uint64_t)(4 * nt), id1, 1u);                       // h = 0: o0
+      tc_mma(tmem, a0 + 2 * hs, b, id3, 1u);                                   // h = 2: o0..o2
+      tc_mma(tmem + (uint32_t)nt, a0 + 3 * hs, b, id3, 1u);                    // h = 3: o1..o3
+      tc_mma(tmem + (uint32_t)(3 * nt), a0 + 5 * hs, b, id1, 1u);              // h = 5: o3
     }
   }
 }
@@ -208,7 +221,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   pdl_begin();
   if ((a.skip && *a.skip) || (a.skip2 && *a.skip2)) return;
   extern __shared__ __align__(1024) unsigned char sm[];
-  const int P = a.planes;  // z planes per CTA (1 or 2), one accumulator each
+  const int P = a.planes;  // z planes per CTA (1, 2 or 4), one accumulator each
   const int ahalf = a_half_bytes(P);
   const int n0 = blockIdx.y * a.tw;
   const int nt = min(a.tw, a.cout - n0);
@@ -228,7 +241,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   const int z0 = (blockIdx.x / (nty * ntx)) * P;
   const int y0 = ty * TY, x0 = tx * TX;
   const int zl = z0 % a.nzs, sample = z0 / a.nzs;
-  const int ncols = P * nt <= 32 ? 32 : (P * nt <= 64 ? 64 : 128);
+  const int ncols = P * nt <= 32 ? 32 : (P * nt <= 64 ? 64 : (P * nt <= 128 ? 128 : 256));
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      sa(tslot)),
@@ -246,7 +259,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   const uint32_t tmem = *tslot;
   bool ok = true;
   if (tid == 0) {
-    const uint32_t id = idesc_bf16(nt), id2 = idesc_bf16(2 * nt);
+    const uint32_t id = idesc_bf16(nt), id2 = idesc_bf16(2 * nt), id3 = idesc_bf16(3 * nt);
     const __nv_bfloat16* wsrc =
         (a.tw == 16 ? a.wimg16 : a.wimg) + (int64_t)a.tw * blockIdx.y * 27 * a.cin;
     const unsigned abox = (unsigned)(HY * HX * (P + 2) * 16);
@@ -272,7 +285,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
       const uint32_t A = sa(sm + s * stage_bytes);
       const uint64_t ad = umma_desc(A, ahalf, HY * 16);
       const uint64_t bd = umma_desc(A + 2 * ahalf, 128, 256);
-      issue_taps(tmem, ad, bd, nt, P, id, id2, c > 0);
+      issue_taps(tmem, ad, bd, nt, P, id, id2, id3, c > 0);
       tc_commit(&used[s]);
       ++committed[s];
       if (c + nst < nchunk) {
@@ -305,9 +318,9 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
     const int y = y0 + (tid & 7), x = x0 + (tid >> 3);
     const bool valid = y < a.ny && x < a.nx;
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    float head[2] = {0.f, 0.f};  // fused 1x1 output layer, per plane
+    float head[4] = {0.f, 0.f, 0.f, 0.f};  // fused 1x1 output layer, per plane
     for (int c0 = 0; c0 < nt; c0 += 16) {
-      __align__(16) __nv_bfloat16 o[2][16];
+      __align__(16) __nv_bfloat16 o[4][16];
       for (int pl = 0; pl < P; ++pl) {
         float acc[16];
         tc_ld16(lane_base + (uint32_t)(pl * nt + c0), acc);
@@ -351,19 +364,20 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
           }
         }
       }
-      if (a.pool) {
-        // 2x2x2 average: planes in registers, y pairs lane^1, x pairs lane^8
+      // 2x2x2 average: plane pairs in registers, y pairs lane^1, x pairs lane^8
+      for (int pp = 0; a.pool && pp < P; pp += 2) {
         __align__(16) __nv_bfloat16 pv[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          float sum = __bfloat162float(o[0][q]) + __bfloat162float(o[1][q]);
+          float sum = __bfloat162float(o[pp][q]) + __bfloat162float(o[pp + 1][q]);
           sum += __shfl_xor_sync(FULL, sum, 1);
           sum += __shfl_xor_sync(FULL, sum, 8);
           pv[q] = __float2bfloat16_rn(sum * 0.125f);
         }
         if (valid && (tid & 1) == 0 && ((tid >> 3) & 1) == 0) {
           const int cy = a.ny / 2, cx = a.nx / 2;
-          const int64_t vc = (int64_t)(y / 2) + (int64_t)cy * ((x / 2) + (int64_t)cx * (z0 / 2));
+          const int64_t vc =
+              (int64_t)(y / 2) + (int64_t)cy * ((x / 2) + (int64_t)cx * ((z0 + pp) / 2));
           *reinterpret_cast<uint4*>(a.pool + act_index(vc, n0 + c0, V / 8)) =
               *reinterpret_cast<const uint4*>(&pv[0]);
           *reinterpret_cast<uint4*>(a.pool + act_index(vc, n0 + c0 + 8, V / 8)) =
@@ -622,7 +636,7 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
   cudaMemsetAsync(de, 0, 4, s);
   ConvArgs a{};
   a.ny = ny; a.nx = nx; a.nz = nz; a.nzs = nz; a.cin = cin; a.cout = cout;
-  a.planes = (nz % 2 == 0) ? 2 : 1;
+  a.planes = (nz % 4 == 0 && cout <= 32) ? 4 : ((nz % 2 == 0) ? 2 : 1);
   a.ldx = cin; a.offx = 0; a.offy = 0;
   a.x = (const __nv_bfloat16*)dx; a.w = (const __nv_bfloat16*)dw;
   a.bias = bias ? (const float*)db : nullptr;
@@ -698,8 +712,8 @@ int conv3_launch(const ConvArgs* pa, const ConvMap* map, int use_tc, cudaStream_
   const int64_t nv = (int64_t)a.ny * a.nx * a.nz;
   if (use_tc) {
     if ((a.ldx % 8) || (a.offx % 8) || (a.nz % a.nzs) || !a.wimg) return SBM_ERR_ARG;
-    if ((a.planes != 1 && a.planes != 2) || (a.planes == 2 && (a.nzs % 2)) ||
-        (a.pool && (a.planes != 2 || a.ny % 2 || a.nx % 2)) || (a.w1x1 && a.cout != 16) ||
+    if ((a.planes != 1 && a.planes != 2 && a.planes != 4) || (a.nzs % a.planes) ||
+        (a.pool && (a.planes == 1 || a.ny % 2 || a.nx % 2)) || (a.w1x1 && a.cout != 16) ||
         (a.offu % 8) || (a.offy % 8))
       return SBM_ERR_ARG;
     ConvMap local;

@@ -432,8 +432,13 @@ const ConvMap* map_for(Work& w, const ConvArgs& a) {
 // Two z planes per CTA where the epilogue pools (it needs both planes of a
 // 2x2x2 block) or the grid is large; one plane keeps more CTAs busy on the
 // small levels.
-int planes_for(const Dims& d, bool pool) {
+// z planes per CTA of a convolution at level d: four on the large levels
+// with at most 32 output channels (half the CTAs of two planes, so the 64^3
+// layers of a 256^3 solve fit in one wave), two when pooling or on other
+// large levels, else one.
+int planes_for(const Dims& d, bool pool, int cout) {
   if (d.nzs % 2) return 1;
+  if (d.nzs % 4 == 0 && cout <= 32 && d.v() >= (int64_t)1 << 17) return 4;
   return (pool || d.v() >= (int64_t)1 << 17) ? 2 : 1;
 }
 
@@ -442,7 +447,7 @@ ConvArgs layer_args(sbm_net* n, const Work& w, int l, int lev, const bf16* x, in
   ConvArgs a{};
   const Dims& d = w.d[lev];
   a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
-  a.planes = planes_for(d, pool);
+  a.planes = planes_for(d, pool, kCo[l]);
   a.cin = kCi[l]; a.cout = kCo[l];
   a.ldx = ldx; a.offx = 0;
   a.x = x; a.wimg = n->wimg + kL.off[l]; a.wimg16 = n->wimg16 + kL.off[l];
@@ -531,7 +536,7 @@ int dgrad(sbm_net* n, Work& w, int l, int lev, const bf16* gy, float* gx, cudaSt
   ConvArgs a{};
   const Dims& d = w.d[lev];
   a.ny = d.ny; a.nx = d.nx; a.nz = d.nz; a.nzs = d.nzs;
-  a.planes = planes_for(d, false);
+  a.planes = planes_for(d, false, kCi[l]);
   a.cin = kCo[l]; a.cout = kCi[l];
   a.ldx = kCo[l]; a.offx = 0; a.offy = 0;
   a.x = gy; a.wimg = n->wtimg + kL.off[l]; a.wimg16 = n->wtimg16 + kL.off[l];

@@ -63,6 +63,23 @@ def test_gradient_matches_oracle(net):
     assert float(g @ gr / (np.linalg.norm(g) * np.linalg.norm(gr))) >= 0.9999
 
 
+def test_forward_and_gradient_at_64(net):
+    """At 64^3 the finest level has 2^18 voxels: its convolutions take four z
+    planes per CTA (E0 with the fused pooling, D0 with the fused 1x1 head,
+    E0's data gradient)."""
+    x, t = _batch(5, nb=1, n=64)
+    p = net.params().astype(np.float64)
+    out = net.forward(x.reshape(-1, 16), (64, 64, 64), nb=1)
+    ref, _ = no.forward(p, x.astype(np.float64), rounding=True)
+    assert _rel(out, ref.ravel()) <= 5e-3
+    loss, g = net.loss_grad(x.reshape(-1, 16), t.ravel(), (64, 64, 64), nb=1)
+    lr, gr = no.loss_grad(p, x.astype(np.float64), t.astype(np.float64), rounding=True)
+    assert loss == pytest.approx(lr, rel=1e-4)
+    for l in range(10):
+        a, b = no.OFF[l], no.BOFF[l] + no.CO[l]
+        assert _rel(g[a:b], gr[a:b]) <= 2e-2, l
+
+
 def test_samples_in_a_batch_do_not_interact(net):
     x, _ = _batch(3)
     both = net.forward(x.reshape(-1, 16), (16, 16, 16), nb=2)
