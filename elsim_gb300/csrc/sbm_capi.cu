@@ -298,7 +298,7 @@ int sbm_download(sbm_ctx* ctx, int field, double* h, int haloed) {
 
 // ------------------------------------------------------------ snapshots
 //
-// A snapshot is a header followed by whole halo-padded FP64 fields: the 13
+// A snapshot is a header followed by whole halo-padded FP64 fields: the 14
 // public fields and, once the electrochemical state exists, the 12 step
 // buffers (half coefficients of the kappa / pce / pcc operators, Dab, mu,
 // mobility, CnE right-hand side, reaction coefficients, forward / backward
@@ -358,7 +358,7 @@ int sbm_ctx_snapshot(sbm_ctx* ctx, void* buf, size_t bytes) {
   SnapHeader h;
   memset(&h, 0, sizeof(h));
   memcpy(h.magic, kSnapMagic, sizeof(h.magic));
-  h.version = 1;
+  h.version = 2;
   h.ny = ctx->g.ny;
   h.nx = ctx->g.nx;
   h.nz = ctx->g.nz;
@@ -384,7 +384,7 @@ int sbm_ctx_restore(sbm_ctx* ctx, const void* buf, size_t bytes) {
   if (!ctx || !buf || bytes < kSnapHead) return SBM_ERR_ARG;
   SnapHeader h;
   memcpy(&h, buf, sizeof(h));
-  if (memcmp(h.magic, kSnapMagic, sizeof(h.magic)) != 0 || h.version != 1 ||
+  if (memcmp(h.magic, kSnapMagic, sizeof(h.magic)) != 0 || h.version != 2 ||
       h.ny != ctx->g.ny || h.nx != ctx->g.nx || h.nz != ctx->g.nz || h.nh != ctx->g.nh ||
       h.nfields != SBM_F_COUNT + (h.step_work ? kStepBufs : 0) || h.p.tbl_n < 2 ||
       h.p.tbl_n > SBM_TBL_MAX)
@@ -443,8 +443,8 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, doubl
   sp.rhs = ctx->f[SBM_F_RHS];
   const double idx2 = 1.0 / (ctx->p.dx * ctx->p.dx);
   (void)g;
-  if (op == SBM_OP_GENERIC) {
-    int rc = generic_spec(ctx, bc_x0, bc_x1, scale, tol, max_it, stop_rule, precision, precond,
+  if (op == SBM_OP_GENERIC || op == SBM_OP_GENERIC_DIAG) {
+    int rc = generic_spec(ctx, op, bc_x0, bc_x1, scale, tol, max_it, stop_rule, precision, precond,
                           &sp);
     if (rc) return rc;
   } else {
@@ -468,7 +468,7 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, doubl
   SolveResult r{};
   int rc = solve(ctx, sp, &r);
   if (rc) return rc;
-  if (op == SBM_OP_GENERIC) {
+  if (op == SBM_OP_GENERIC || op == SBM_OP_GENERIC_DIAG) {
     if ((rc = ghost_after_solve(ctx, sp.x, sp.bcx0, sp.bcx1))) return rc;
     SBM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   }
@@ -484,7 +484,8 @@ int sbm_learned_pc_apply(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, const
                          double* z) {
   if (!ctx || !r || !z) return SBM_ERR_ARG;
   SolveSpec sp{};
-  int rc = generic_spec(ctx, bc_x0, bc_x1, scale, 1e-8, 1, SBM_STOP_REL_RES, SBM_PREC_MIXED,
+  int rc = generic_spec(ctx, SBM_OP_GENERIC, bc_x0, bc_x1, scale, 1e-8, 1, SBM_STOP_REL_RES,
+                        SBM_PREC_MIXED,
                         SBM_PC_LEARNED, &sp);
   if (rc) return rc;
   return learned_pc_apply(ctx, sp, r, z);
@@ -493,13 +494,15 @@ int sbm_learned_pc_apply(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, const
 }  // extern "C"
 
 namespace sbm {
-// Solve spec of the GENERIC operator (coefficient, unknown, right-hand side
-// and weight from the context's public fields); also halves the coefficient.
-int generic_spec(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, double tol, int max_it,
+// Solve spec of the GENERIC / GENERIC_DIAG operator (coefficient, diagonal,
+// unknown, right-hand side and weight from the context's public fields);
+// also halves the coefficient.
+int generic_spec(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, double tol, int max_it,
                  int stop_rule, int precision, int precond, SolveSpec* out) {
   const Geo& g = ctx->g;
+  if (op != SBM_OP_GENERIC && op != SBM_OP_GENERIC_DIAG) return SBM_ERR_ARG;
   SolveSpec sp{};
-  sp.op = SBM_OP_GENERIC;
+  sp.op = op;
   sp.precision = precision;
   sp.precond = precond;
   sp.stop_rule = stop_rule;
@@ -508,7 +511,8 @@ int generic_spec(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, double tol, i
   sp.rhs = ctx->f[SBM_F_RHS];
   SBM_CUDA_TRY(launch_half(g, ctx->f[SBM_F_COEF], ctx->hk_gen, ctx->stream));
   sp.hk64 = ctx->hk_gen;
-  sp.form = 0;
+  sp.form = op == SBM_OP_GENERIC_DIAG ? 1 : 0;
+  sp.diag64 = op == SBM_OP_GENERIC_DIAG ? ctx->f[SBM_F_DIAG] : nullptr;
   sp.scale = scale;
   sp.bcx0 = bc_x0;
   sp.bcx1 = bc_x1;

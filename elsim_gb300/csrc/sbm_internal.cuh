@@ -359,7 +359,7 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex, cudaGrap
                 int* nodes);
 int mixed_end(sbm_ctx* ctx, const SolveSpec& sp, const CgState& fin, SolveResult* out);
 int status_of_done(int done);
-int generic_spec(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, double tol, int max_it,
+int generic_spec(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale, double tol, int max_it,
                  int stop_rule, int precision, int precond, SolveSpec* sp);
 int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double* bytes_per_launch);
 int ensure_fp32_work(sbm_ctx* ctx);

@@ -36,15 +36,16 @@ OK, ERR_ARG, ERR_CUDA, ERR_MAXIT, ERR_NONFINITE, ERR_BREAKDOWN, ERR_NOMEM, ERR_S
 TUNE_NO_TMA = 1
 TUNE_PC_ADDITIVE = 2
 BC_COPY, BC_ZERO = 0, 1
-OP_CNE, OP_PHP, OP_PHE, OP_GENERIC = 0, 1, 2, 3
+OP_CNE, OP_PHP, OP_PHE, OP_GENERIC, OP_GENERIC_DIAG = 0, 1, 2, 3, 4
 STOP_REF_UPDATE, STOP_REF_RESID, STOP_REL_RES = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 PC_NONE, PC_JACOBI, PC_LEARNED = 0, 1, 2
 BV_EXP, BV_LINEAR = 0, 1
 CH_TABLE, CH_DOUBLE_WELL = 0, 1
-F_PSP, F_PSE, F_AVP, F_AVPX, F_CNP, F_CNE, F_PHP, F_PHE, F_RXN, F_COEF, F_RHS, F_X, F_WEIGHT = range(13)
+(F_PSP, F_PSE, F_AVP, F_AVPX, F_CNP, F_CNE, F_PHP, F_PHE, F_RXN, F_COEF, F_RHS, F_X, F_WEIGHT,
+ F_DIAG) = range(14)
 FIELDS = dict(psP=F_PSP, psE=F_PSE, AvP=F_AVP, AvPx=F_AVPX, CnP=F_CNP, CnE=F_CNE, phP=F_PHP,
-              phE=F_PHE, Rxn=F_RXN, coef=F_COEF, rhs=F_RHS, x=F_X, weight=F_WEIGHT)
+              phE=F_PHE, Rxn=F_RXN, coef=F_COEF, rhs=F_RHS, x=F_X, weight=F_WEIGHT, diag=F_DIAG)
 TBL_MAX = 128
 
 _ERRNAMES = {ERR_ARG: "bad argument", ERR_CUDA: "CUDA error", ERR_MAXIT: "iteration cap",
@@ -145,6 +146,8 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_voltage_step": (C.c_int, [vp, C.c_double, C.c_double, C.POINTER(Scalars)]),
         "sbm_batch_solve": (C.c_int, [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_double,
                                       C.c_double, C.c_int, C.c_int, ip, dp, ip, fp]),
+        "sbm_batch_solve_ops": (C.c_int, [C.POINTER(vp), ip, ip, ip, dp, C.c_int, C.c_double,
+                                          C.c_int, C.c_int, ip, dp, ip, fp]),
         "sbm_table_lookup": (C.c_int, [i64, C.c_int, dp, dp, dp, dp]),
         "sbm_conv3d_bf16": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.POINTER(C.c_uint16), C.POINTER(C.c_uint16),
@@ -457,6 +460,27 @@ def batch_solve(contexts, bc_x0=BC_ZERO, bc_x1=BC_ZERO, scale=1.0, tol=1e-8, max
     ms = C.c_float(0)
     _check(lib.sbm_batch_solve(hs, n, bc_x0, bc_x1, scale, tol, max_it, precond, it, res, stt,
                                C.byref(ms)), "sbm_batch_solve")
+    return dict(iters=list(it), final_res=list(res), status=list(stt), ms=ms.value)
+
+
+def batch_solve_ops(contexts, ops, bc_x0, bc_x1, scales, tol=1e-8, max_it=100000,
+                    precond=PC_JACOBI) -> dict:
+    """As batch_solve with one system per context of either GENERIC form
+    (OP_GENERIC or OP_GENERIC_DIAG) and its own x-face rules and scale
+    (sbm_batch_solve_ops)."""
+    lib = load_library()
+    n = len(contexts)
+    if not (len(ops) == len(bc_x0) == len(bc_x1) == len(scales) == n):
+        raise ValueError("one op, x-face rule pair and scale per context")
+    hs = (C.c_void_p * n)(*[c._h for c in contexts])
+    it = (C.c_int * n)()
+    res = (C.c_double * n)()
+    stt = (C.c_int * n)()
+    ms = C.c_float(0)
+    arr = lambda t, v: (t * n)(*v)
+    _check(lib.sbm_batch_solve_ops(hs, arr(C.c_int, ops), arr(C.c_int, bc_x0),
+                                   arr(C.c_int, bc_x1), arr(C.c_double, scales), n, tol, max_it,
+                                   precond, it, res, stt, C.byref(ms)), "sbm_batch_solve_ops")
     return dict(iters=list(it), final_res=list(res), status=list(stt), ms=ms.value)
 
 

@@ -106,6 +106,25 @@ def potential_problem(psi: np.ndarray, k_solid: float = 1.0, k_elec: float = 0.1
     return dict(coef=coef, x=x, rhs=rhs, weight=np.asfortranarray(psi.copy()))
 
 
+CONC_SCALE = 0.1  # dt D / dx^2 of the synthetic concentration solve
+
+
+def concentration_problem(psi: np.ndarray, seed: int = 0) -> dict:
+    """An implicit concentration step in the CnE form of the reference
+    (SBMES:515-521): psE c - s div(psE grad c) = psE c_old, psE = 1 - psi +
+    1e-6 (its floor, SBMES:258), face coefficients from psE, s = CONC_SCALE,
+    Neumann on every face; c_old = 1 + 0.1 x smoothed noise, also the
+    initial guess.  Fields for OP_GENERIC_DIAG: coef, diag, rhs, x, weight."""
+    from scipy.ndimage import gaussian_filter
+
+    pse = np.asfortranarray(1.0 - psi + 1.0e-6)
+    rng = np.random.default_rng(seed + 7)
+    c0 = 1.0 + 0.1 * gaussian_filter(rng.standard_normal(psi.shape), 2.0, mode="nearest")
+    c0 = np.asfortranarray(c0)
+    return dict(coef=pse.copy(order="F"), diag=pse, rhs=np.asfortranarray(pse * c0), x=c0,
+                weight=pse.copy(order="F"), scale=CONC_SCALE)
+
+
 def reference_tables(params):
     """Fills the five 101-point property tables of the reference
     (C_Li_X / M6 / Mb5 / J2 / O3, SBMES:210-242, not in its repository) with

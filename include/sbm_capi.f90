@@ -12,6 +12,7 @@ MODULE sbm_capi
   INTEGER(C_INT), PARAMETER :: SBM_OK = 0, SBM_ERR_MAXIT = -3
   INTEGER(C_INT), PARAMETER :: SBM_BC_COPY = 0, SBM_BC_ZERO = 1
   INTEGER(C_INT), PARAMETER :: SBM_OP_CNE = 0, SBM_OP_PHP = 1, SBM_OP_PHE = 2, SBM_OP_GENERIC = 3
+  INTEGER(C_INT), PARAMETER :: SBM_OP_GENERIC_DIAG = 4
   INTEGER(C_INT), PARAMETER :: SBM_STOP_REF_UPDATE = 0, SBM_STOP_REF_RESID = 1, SBM_STOP_REL_RES = 2
   INTEGER(C_INT), PARAMETER :: SBM_PREC_FP64 = 0, SBM_PREC_MIXED = 1
   INTEGER(C_INT), PARAMETER :: SBM_PC_NONE = 0, SBM_PC_JACOBI = 1, SBM_PC_LEARNED = 2
@@ -19,7 +20,7 @@ MODULE sbm_capi
   INTEGER(C_INT), PARAMETER :: SBM_CH_TABLE = 0, SBM_CH_DOUBLE_WELL = 1
   INTEGER(C_INT), PARAMETER :: SBM_F_PSP = 0, SBM_F_PSE = 1, SBM_F_AVP = 2, SBM_F_AVPX = 3, &
        SBM_F_CNP = 4, SBM_F_CNE = 5, SBM_F_PHP = 6, SBM_F_PHE = 7, SBM_F_RXN = 8, &
-       SBM_F_COEF = 9, SBM_F_RHS = 10, SBM_F_X = 11, SBM_F_WEIGHT = 12
+       SBM_F_COEF = 9, SBM_F_RHS = 10, SBM_F_X = 11, SBM_F_WEIGHT = 12, SBM_F_DIAG = 13
   INTEGER, PARAMETER :: SBM_TBL_MAX = 128
 
   TYPE, BIND(C) :: sbm_params

@@ -49,11 +49,14 @@ extern "C" {
 
 /* Operator families (SBMES:515-521 CnE, :670-676 phP, :751-757 phE).
  * GENERIC is the phP form on the context's COEF field with the x-face ghost
- * rules taken from the solve call (used for the plain potential solve). */
+ * rules taken from the solve call (used for the plain potential solve);
+ * GENERIC_DIAG the CnE form on the context's fields, q = DIAG p - scale
+ * S(p) with faces from COEF (a concentration solve with its mass term). */
 #define SBM_OP_CNE      0
 #define SBM_OP_PHP      1
 #define SBM_OP_PHE      2
 #define SBM_OP_GENERIC  3
+#define SBM_OP_GENERIC_DIAG 4
 
 /* Stopping rules.  REF_UPDATE: sqrt(sum(w*dx^2)/sum(w)) < tol, the
  * potential loops (SBMES:699-705, :780-786).  REF_RESID:
@@ -96,6 +99,7 @@ enum sbm_field {
   SBM_F_RHS,       /* right-hand side of a GENERIC solve       */
   SBM_F_X,         /* unknown of a GENERIC solve (ghosts = Dirichlet data) */
   SBM_F_WEIGHT,    /* psi weight of the GENERIC stopping norm  */
+  SBM_F_DIAG,      /* diagonal (mass) term of GENERIC_DIAG     */
   SBM_F_COUNT
 };
 
@@ -178,7 +182,7 @@ int sbm_ctx_get_scalars(const sbm_ctx* ctx, sbm_scalars* s);
 /* Checkpoint / resume (no counterpart in the reference, whose periodic
  * REAL(4) dumps are outputs only).  A snapshot holds the parameters, the
  * electrochemical scalars and every halo-padded FP64 field a later solve or
- * time step reads: the 13 public fields and, after sbm_setup_domain, the 12
+ * time step reads: the 14 public fields and, after sbm_setup_domain, the 12
  * step buffers (operator half coefficients, Dab, mu, mobility, reaction
  * coefficients, rate constants, previous phP / phE).  A context restored
  * from it continues bit for bit like the one it was taken from.  The buffer
@@ -233,15 +237,28 @@ int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
 
 /* Batched solves (no counterpart in the reference): n independent
  * contexts, each loaded with a GENERIC problem (COEF, X, RHS), solved by the
- * mixed-precision CG to rel-res tol together -- their iteration chunks are
- * child graphs of one parent CUDA graph, so one launch advances every
- * unconverged volume.  Per-volume iterations, final rel-res and status go to
- * the n-element arrays; ms_total is the device time of the whole batch.
- * precond SBM_PC_LEARNED applies per volume (its own attached network and
- * grid permitting, else Jacobi; sbm_ctx_last_precond of each context). */
+ * mixed-precision CG to rel-res tol together in ONE graph launch: a parent
+ * CUDA graph holds per volume a WHILE conditional node whose body is the
+ * volume's captured iteration chunk, re-armed on the device while the
+ * volume is not done (at most max_it + 2 rounds), so converged volumes stop
+ * launching work and the host waits once.  Per-volume iterations, final
+ * rel-res and status go to the n-element arrays; ms_total is the device
+ * time of the whole batch.  precond SBM_PC_LEARNED applies per volume (its
+ * own attached network and grid permitting, else Jacobi;
+ * sbm_ctx_last_precond of each context). */
 int sbm_batch_solve(sbm_ctx** ctxs, int n, int bc_x0, int bc_x1, double scale, double tol,
                     int max_it, int precond, int* iters, double* final_res, int* status,
                     float* ms_total);
+
+/* The same with one system per context of either GENERIC operator: ops[v]
+ * is SBM_OP_GENERIC (potential form) or SBM_OP_GENERIC_DIAG (concentration
+ * form, diagonal from the context's DIAG field), with its own x-face rules
+ * and scale, so potential and concentration systems of many sub-volumes
+ * advance in the same graph launches.  The learned preconditioner applies
+ * to GENERIC systems only (GENERIC_DIAG ones use Jacobi). */
+int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bc_x0, const int* bc_x1,
+                        const double* scale, int n, double tol, int max_it, int precond,
+                        int* iters, double* final_res, int* status, float* ms_total);
 
 /* One electrochemical time step, the body of the reference's time loop
  * (SBMES:397-840) for a given dt, voltage-scan rate vsr and step index

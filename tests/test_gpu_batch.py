@@ -75,3 +75,68 @@ def test_batch_with_learned_preconditioner(built):
     for c in ctxs:
         c.close()
 
+
+
+def _conc(n, seed, frac):
+    m = synth.microstructure((n, n, n), seed=seed, solid_fraction=frac, reinit_steps=60,
+                             redist=orc.redist)
+    return synth.concentration_problem(m["psi"], seed)
+
+
+def _load(ctx, prob, keys=("coef", "x", "rhs", "weight", "diag")):
+    for k in keys:
+        if k in prob:
+            ctx.upload(k, prob[k])
+
+
+def test_concentration_form_matches_oracle(built):
+    """OP_GENERIC_DIAG (q = diag p - scale S(p), the CnE form) in FP64 against
+    the oracle's CG with the same diagonal, and in mixed precision."""
+    n = 24
+    p = _conc(n, 21, 0.6)
+    with sbm.Context(n, n, n) as c:
+        _load(c, p)
+        info = c.cg_solve(op=sbm.OP_GENERIC_DIAG, bc_x0=sbm.BC_COPY, bc_x1=sbm.BC_COPY,
+                          scale=p["scale"], tol=1e-10, max_it=10000, stop_rule=sbm.STOP_REL_RES)
+        x64 = c.download("x")
+        xo, io = orc.cg(p["coef"], p["rhs"], p["x"], p["scale"], sbm.BC_COPY, sbm.BC_COPY,
+                        sbm.STOP_REL_RES, 1e-10, 10000, diag=p["diag"])
+        assert abs(info["iters"] - io["iters"]) <= 3, (info, io)
+        assert rel_l2(x64, xo) < 1e-9
+        c.upload("x", p["x"])
+        info = c.cg_solve(op=sbm.OP_GENERIC_DIAG, bc_x0=sbm.BC_COPY, bc_x1=sbm.BC_COPY,
+                          scale=p["scale"], tol=1e-8, max_it=10000, stop_rule=sbm.STOP_REL_RES,
+                          precision=sbm.PREC_MIXED, precond=sbm.PC_LEARNED)
+        assert c.last_precond() == sbm.PC_JACOBI  # no network on the diagonal form
+        assert rel_l2(c.download("x"), xo) < 1e-6
+
+
+def test_batch_of_potential_and_concentration_systems(built):
+    """Potential (GENERIC, Dirichlet x faces) and concentration (GENERIC_DIAG,
+    Neumann) systems of several sub-volumes in one batch: each equals its
+    single solve bit for bit."""
+    sizes = [24, 16, 32, 20]
+    ctxs, probs, ops, b0, b1, sc = [], [], [], [], [], []
+    for v, n in enumerate(sizes):
+        for kind in ("pot", "conc"):
+            p = _vol(n, 700 + v, 0.55) if kind == "pot" else _conc(n, 700 + v, 0.55)
+            c = sbm.Context(n, n, n)
+            _load(c, p)
+            ctxs.append(c)
+            probs.append(p)
+            ops.append(sbm.OP_GENERIC if kind == "pot" else sbm.OP_GENERIC_DIAG)
+            b0.append(sbm.BC_ZERO if kind == "pot" else sbm.BC_COPY)
+            b1.append(sbm.BC_ZERO if kind == "pot" else sbm.BC_COPY)
+            sc.append(1.0 if kind == "pot" else p["scale"])
+    out = sbm.batch_solve_ops(ctxs, ops, b0, b1, sc, tol=1e-8, precond=sbm.PC_JACOBI)
+    assert out["status"] == [0] * len(ctxs)
+    xs = [c.download("x") for c in ctxs]
+    for v, (c, p) in enumerate(zip(ctxs, probs)):
+        c.upload("x", p["x"])
+        info = c.cg_solve(op=ops[v], bc_x0=b0[v], bc_x1=b1[v], scale=sc[v], tol=1e-8,
+                          max_it=100000, stop_rule=sbm.STOP_REL_RES, precision=sbm.PREC_MIXED,
+                          precond=sbm.PC_JACOBI)
+        assert info["iters"] == out["iters"][v]
+        assert np.array_equal(c.download("x"), xs[v])
+    for c in ctxs:
+        c.close()
