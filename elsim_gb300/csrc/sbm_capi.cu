@@ -197,7 +197,8 @@ int sbm_ctx_destroy(sbm_ctx* ctx) {
   double* d[] = {ctx->hk_kap, ctx->hk_pce, ctx->hk_pcc, ctx->hk_gen, ctx->dab, ctx->dab1,
                  ctx->mu,     ctx->mb,     ctx->pmn,    ctx->rhe,    ctx->rxc, ctx->kfw,
                  ctx->kbw,    ctx->ppo,    ctx->peo,    ctx->tmp,    ctx->r64, ctx->p64,
-                 ctx->q64,    ctx->d64,    ctx->r0,     ctx->partials, ctx->d_scal};
+                 ctx->q64,    ctx->d64,    ctx->r0,     ctx->partials, ctx->d_scal,
+                 ctx->fc64};
   for (double* q : d) cudaFree(q);
   float* fl[] = {ctx->hk32, ctx->dg32, ctx->r32, ctx->p32, ctx->q32, ctx->x32, ctx->z32, ctx->rold32};
   for (float* q : fl) cudaFree(q);

@@ -241,7 +241,28 @@ struct OpArgs {
   T scale;
   int form;       // 0 or 1
   int bcx0, bcx1; // SBM_BC_COPY / SBM_BC_ZERO for the search direction
+  // optional stored face coefficients (FP64 path): y, x and z faces of every
+  // padded cell, fc[c] = hk[c+1] + hk[c], fc[nh + c] = hk[c+sx] + hk[c],
+  // fc[2 nh + c] = hk[c+sz] + hk[c] -- the values face_sum forms, read
+  // instead of recomputed (the FP64 stencil is bound by GB300's FP64 rate)
+  const T* fc = nullptr;
 };
+
+// face_sum with stored faces: the same operands and order, so the same bits.
+template <typename T>
+__device__ __forceinline__ T face_sum_stored(const Geo& g, const T* __restrict__ fc, int64_t c,
+                                             T pc, T pyp, T pym, T pxp, T pxm, T pzp, T pzm) {
+  const T* fy = fc;
+  const T* fx = fc + g.nh;
+  const T* fz = fc + 2 * g.nh;
+  T s = fy[c] * (pyp - pc);
+  s = s - fy[c - 1] * (pc - pym);
+  s = s + fx[c] * (pxp - pc);
+  s = s - fx[c - g.sx] * (pc - pxm);
+  s = s + fz[c] * (pzp - pc);
+  s = s - fz[c - g.sz] * (pc - pzm);
+  return s;
+}
 
 // Face terms of S(p) = sum_f c_f (p_nb - p_c) in the reference's order
 // (y+, y-, x+, x-, z+, z-; SBMES:494-499), c_f = hk_nb + hk_c.
@@ -316,6 +337,8 @@ struct sbm_ctx {
   double *ppo = nullptr, *peo = nullptr, *tmp = nullptr;
   // FP64 CG work: residual, direction, A*direction, IR correction, IR r0
   double *r64 = nullptr, *p64 = nullptr, *q64 = nullptr, *d64 = nullptr, *r0 = nullptr;
+  // stored y / x / z face coefficients of the current FP64 operator (3 nh)
+  double* fc64 = nullptr;
   // FP32 work: half coefficient, diagonal, residual, direction, A*direction, correction, z
   float *hk32 = nullptr, *dg32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr,
         *x32 = nullptr, *z32 = nullptr, *rold32 = nullptr;

@@ -58,16 +58,18 @@ int pick_zc(const Geo& g, int tuned) {
 // copy (SBM_BC_COPY) or read zero (SBM_BC_ZERO).
 template <typename T, bool RULE>
 __device__ __forceinline__ T stencil_at(const Geo& g, const T* __restrict__ hk,
-                                        const T* __restrict__ p, int64_t c, int i, int j, T pc,
-                                        T kc, T pzm, T pzp, T kzm, T kzp, int bcx0, int bcx1) {
+                                        const T* __restrict__ fc, const T* __restrict__ p,
+                                        int64_t c, int i, int j, T pc, T kc, T pzm, T pzp, T kzm,
+                                        T kzp, int bcx0, int bcx1) {
   T pym = p[c - 1], pyp = p[c + 1], pxm = p[c - g.sx], pxp = p[c + g.sx];
-  const T kym = hk[c - 1], kyp = hk[c + 1], kxm = hk[c - g.sx], kxp = hk[c + g.sx];
   if (RULE) {
     if (i == 1) pym = pc;
     if (i == g.ny) pyp = pc;
     if (j == 1) pxm = bcx0 ? T(0) : pc;
     if (j == g.nx) pxp = bcx1 ? T(0) : pc;
   }
+  if (fc) return face_sum_stored<T>(g, fc, c, pc, pyp, pym, pxp, pxm, pzp, pzm);
+  const T kym = hk[c - 1], kyp = hk[c + 1], kxm = hk[c - g.sx], kxp = hk[c + g.sx];
   return face_sum<T>(kc, pc, kyp, pyp, kym, pym, kxp, pxp, kxm, pxm, kzp, pzp, kzm, pzm);
 }
 
@@ -83,16 +85,17 @@ __global__ void __launch_bounds__(BX* BY) k_apply(OpArgs<T> op, int zc, const T*
   SBM_COLUMN_PROLOGUE(g, zc)
   T acc = T(0);
   if (active && k0 <= k1) {
+    const bool sf = op.fc != nullptr;  // stored faces: no half coefficient reads
     int64_t c = g.ix(i, j, k0);
-    T pc = p[c], kc = op.hk[c];
-    T pzm = p[c - g.sz], kzm = op.hk[c - g.sz];
+    T pc = p[c], kc = sf ? T(0) : op.hk[c];
+    T pzm = p[c - g.sz], kzm = sf ? T(0) : op.hk[c - g.sz];
     if (RULE && k0 == 1) pzm = pc;
     for (int k = k0; k <= k1; ++k) {
       const T pzp_raw = p[c + g.sz];
-      const T kzp = op.hk[c + g.sz];
+      const T kzp = sf ? T(0) : op.hk[c + g.sz];
       const T pzp = (RULE && k == g.nz) ? pc : pzp_raw;
-      const T s = stencil_at<T, RULE>(g, op.hk, p, c, i, j, pc, kc, pzm, pzp, kzm, kzp, op.bcx0,
-                                      op.bcx1);
+      const T s = stencil_at<T, RULE>(g, op.hk, op.fc, p, c, i, j, pc, kc, pzm, pzp, kzm, kzp,
+                                      op.bcx0, op.bcx1);
       T qv;
       if (FORM == 0)
         qv = op.scale * s;
@@ -134,13 +137,14 @@ __global__ void __launch_bounds__(BX* BY)
   SBM_COLUMN_PROLOGUE(g, zc)
   double a_rr = 0.0, a_rz = 0.0;
   if (active && k0 <= k1) {
+    const bool sf = op.fc != nullptr;
     int64_t c = g.ix(i, j, k0);
-    double pc = x[c], kc = op.hk[c];
-    double pzm = x[c - g.sz], kzm = op.hk[c - g.sz];
+    double pc = x[c], kc = sf ? 0.0 : op.hk[c];
+    double pzm = x[c - g.sz], kzm = sf ? 0.0 : op.hk[c - g.sz];
     for (int k = k0; k <= k1; ++k) {
-      const double pzp = x[c + g.sz], kzp = op.hk[c + g.sz];
-      const double s = stencil_at<double, false>(g, op.hk, x, c, i, j, pc, kc, pzm, pzp, kzm,
-                                                 kzp, 0, 0);
+      const double pzp = x[c + g.sz], kzp = sf ? 0.0 : op.hk[c + g.sz];
+      const double s = stencil_at<double, false>(g, op.hk, op.fc, x, c, i, j, pc, kc, pzm, pzp,
+                                                 kzm, kzp, 0, 0);
       const double ax = (FORM == 0) ? op.scale * s : op.diag[c] * pc - op.scale * s;
       const double rv = b[c] - ax;
       r[c] = rv;
@@ -438,11 +442,41 @@ std::string key_of(const char* tag, const void* a, const void* b, const void* c,
   return std::string(buf);
 }
 
+__global__ void k_faces(Geo g, const double* __restrict__ hk, double* __restrict__ fc) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.nh;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const double kc = hk[c];
+    fc[c] = c + 1 < g.nh ? hk[c + 1] + kc : 0.0;
+    fc[g.nh + c] = c + g.sx < g.nh ? hk[c + g.sx] + kc : 0.0;
+    fc[2 * g.nh + c] = c + g.sz < g.nh ? hk[c + g.sz] + kc : 0.0;
+  }
+}
+
+// Stored faces of hk (OpArgs::fc) into ctx->fc64, allocated on first use.
+int compute_faces(sbm_ctx* ctx, const double* hk, cudaStream_t s) {
+  const Geo& g = ctx->g;
+  if (!ctx->fc64) {
+    const cudaError_t e = cudaMalloc(&ctx->fc64, sizeof(double) * 3 * (size_t)g.nh);
+    if (e != cudaSuccess) {
+      ctx->fc64 = nullptr;
+      set_error("cudaMalloc faces", e);
+      return SBM_ERR_NOMEM;
+    }
+  }
+  k_faces<<<flat_grid(g.nh), 256, 0, s>>>(g, hk, ctx->fc64);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}
+
 int solve_fp64(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   const Geo& g = ctx->g;
   cudaStream_t s = ctx->stream;
   const Shape sh = stencil_shape(g, pick_zc(g, ctx->zc64));
   OpArgs<double> op{g, sp.hk64, sp.diag64, sp.scale, sp.form, sp.bcx0, sp.bcx1};
+  int frc = compute_faces(ctx, sp.hk64, s);
+  if (frc) return frc;
+  op.fc = ctx->fc64;
   const bool pc = sp.precond == SBM_PC_JACOBI;
   CgState* h = &ctx->h_st[2];
   memset(h, 0, sizeof(CgState));
@@ -919,9 +953,10 @@ __global__ void __launch_bounds__(BX* BY)
       const double pzp = (k == g.nz) ? pc : V(g.sz, g32.sz);
 #undef V
       const double* hk = op.hk;
-      const double s = face_sum<double>(hk[c], pc, hk[c + 1], pyp, hk[c - 1], pym, hk[c + g.sx],
-                                        pxp, hk[c - g.sx], pxm, hk[c + g.sz], pzp, hk[c - g.sz],
-                                        pzm);
+      const double s =
+          op.fc ? face_sum_stored<double>(g, op.fc, c, pc, pyp, pym, pxp, pxm, pzp, pzm)
+                : face_sum<double>(hk[c], pc, hk[c + 1], pyp, hk[c - 1], pym, hk[c + g.sx], pxp,
+                                   hk[c - g.sx], pxm, hk[c + g.sz], pzp, hk[c - g.sz], pzm);
       const double ad = (FORM == 0) ? op.scale * s : op.diag[c] * pc - op.scale * s;
       const double rv = r0[c] - ad;
       const float rf = (float)rv;
@@ -1024,6 +1059,8 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   float* const x32 = ctx->x32 + kOff32;
   float* const iv32 = ctx->z32 + kOff32;
   OpArgs<double> op64{g, sp.hk64, sp.diag64, sp.scale, sp.form, sp.bcx0, sp.bcx1};
+  if ((rc = compute_faces(ctx, sp.hk64, s))) return rc;
+  op64.fc = ctx->fc64;
   OpArgs<float> op32{g32, hk32, sp.form ? dg32 : nullptr, (float)sp.scale, sp.form, sp.bcx0,
                      sp.bcx1};
   // learned preconditioner when usable, else Jacobi (the documented fallback)
@@ -1300,6 +1337,10 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
                            pc ? 1 : 0, op32.form, ctx->zc32, plan);
     if (rc) return rc;
   }
+  if (which == 2) {
+    int rc = compute_faces(ctx, ctx->hk_gen, s);
+    if (rc) return rc;
+  }
   auto launch = [&]() {
     if (which == 0 && use_tma) {
       tma_launch(*plan, true, op32, pb, q32, ctx->partials, ctx->st32, s);
@@ -1334,6 +1375,7 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
       }
     } else {
       OpArgs<double> op{g, ctx->hk_gen, nullptr, 1.0, 0, SBM_BC_ZERO, SBM_BC_ZERO};
+      op.fc = ctx->fc64;  // stored faces of the GENERIC operator (computed above)
       k_apply<double, 0, true, true><<<sh64.grid, sh64.block, 0, s>>>(op, sh64.zc, ctx->p64, ctx->q64, ctx->partials, ctx->st32);
     }
   };
