@@ -657,6 +657,13 @@ def run_frontend(args):
     frame_prod()
     t_prod = timed(frame_prod, 2)
     del v2_d, b2
+    # the AccDiff_3D program (1501 connectivity sweeps of each phase) on the
+    # frame's distance, through the C-ABI (host psi, transfers included)
+    dist = np.asfortranarray(got[1:-1, 1:-1, 1:-1])
+    sbm.connectivity(dist, 0.75, 11)
+    t0 = time.perf_counter()
+    sbm.connectivity(dist, 0.75, 1501)
+    t_conn = time.perf_counter() - t0
     # the oracle: the same frame on the host cores
     t0 = time.perf_counter()
     want = orc.ls_frontend(vox, yg, zg, xoff, nth, tr, ac, lit, dt)
@@ -681,7 +688,8 @@ def run_frontend(args):
                        "us_per_redist": t_redist * 1e6,
                        "production_grid": f"{2 * yg}x{xg2}x{2 * zg} (lengths x2, voxels "
                                           f"{2 * yo}x{2 * xo}x{2 * zo})",
-                       "production_frame_s": t_prod},
+                       "production_frame_s": t_prod,
+                       "connectivity_program_s": t_conn},
             "roofline": {"kernel": "k_redist", "bound": "hbm", "achieved": ach, "peak": hbm,
                          "unit": "GB/s", "frac": ach / hbm, "peak_source": src,
                          "traffic": None,

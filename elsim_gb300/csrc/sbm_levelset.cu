@@ -163,7 +163,26 @@ struct AccArgs {
   int dirichlet_x;  // 1: Cn = 1 at x = nx+1 (solid); 0: at x = 0 (electrolyte)
   int stored;       // 1: read Cn's ghosts from memory (first iteration)
   int accel;        // MOD(iter,5) == 1
+  // psi is the same in every iteration, so its face sums and the factor
+  // 0.5*idh2/psi are formed once per call (the same operations, so the
+  // same bits): fs[c] = psi(i+1)+psi(i), fs[nh+c] = psi(j+1)+psi(j),
+  // fs[2nh+c] = psi(k+1)+psi(k); qd[c] = (0.5*idh2)/psi where psi >= 0.4
+  const double* fs;
+  const double* qd;
 };
+
+// The per-call constants of the AccDiff sweep (see AccArgs::fs, qd).
+__global__ void k_acc_pre(Geo g, const double* __restrict__ psi, double half_idh2, double thr,
+                          double* __restrict__ fs, double* __restrict__ qd) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.nh;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const double p = psi[c];
+    fs[c] = c + 1 < g.nh ? __dadd_rn(psi[c + 1], p) : 0.0;
+    fs[g.nh + c] = c + g.sx < g.nh ? __dadd_rn(psi[c + g.sx], p) : 0.0;
+    fs[2 * g.nh + c] = c + g.sz < g.nh ? __dadd_rn(psi[c + g.sz], p) : 0.0;
+    qd[c] = p >= thr ? __ddiv_rn(half_idh2, p) : 0.0;
+  }
+}
 
 // One AccDiff iteration on the interior (AccDiff_3D.f90:118-134): Jacobi
 // masked diffusion, then the acceleration step.  After the first iteration
@@ -192,14 +211,18 @@ __global__ void __launch_bounds__(256) k_accdiff(AccArgs a) {
       if (k == g.nz) zp = u;
       if (k == 1) zm = u;
     }
-    const double* ps = a.psi;
-    double s = __dmul_rn(__dadd_rn(ps[c + 1], p), __dsub_rn(yp, u));
-    s = __dsub_rn(s, __dmul_rn(__dadd_rn(p, ps[c - 1]), __dsub_rn(u, ym)));
-    s = __dadd_rn(s, __dmul_rn(__dadd_rn(ps[c + g.sx], p), __dsub_rn(xp, u)));
-    s = __dsub_rn(s, __dmul_rn(__dadd_rn(p, ps[c - g.sx]), __dsub_rn(u, xm)));
-    s = __dadd_rn(s, __dmul_rn(__dadd_rn(ps[c + g.sz], p), __dsub_rn(zp, u)));
-    s = __dsub_rn(s, __dmul_rn(__dadd_rn(p, ps[c - g.sz]), __dsub_rn(u, zm)));
-    const double div = __dmul_rn(__ddiv_rn(a.half_idh2, p), s);
+    // psi(i+1)+psi(i), psi(i)+psi(i-1), ... in the reference's term order;
+    // psi(i)+psi(i-1) is the stored psi(i-1)+psi(i) (addition commutes)
+    const double* fy = a.fs;
+    const double* fx = a.fs + g.nh;
+    const double* fz = a.fs + 2 * g.nh;
+    double s = __dmul_rn(fy[c], __dsub_rn(yp, u));
+    s = __dsub_rn(s, __dmul_rn(fy[c - 1], __dsub_rn(u, ym)));
+    s = __dadd_rn(s, __dmul_rn(fx[c], __dsub_rn(xp, u)));
+    s = __dsub_rn(s, __dmul_rn(fx[c - g.sx], __dsub_rn(u, xm)));
+    s = __dadd_rn(s, __dmul_rn(fz[c], __dsub_rn(zp, u)));
+    s = __dsub_rn(s, __dmul_rn(fz[c - g.sz], __dsub_rn(u, zm)));
+    const double div = __dmul_rn(a.qd[c], s);
     un = __dadd_rn(u, __dmul_rn(a.dt, div));
   }
   if (a.accel && un > a.cmin && p > a.thr) un = 1.0;
@@ -402,6 +425,12 @@ int accdiff_dev(cudaStream_t s, const Geo& g, const double* psi, double* cn, dou
   a.thr = (double)4.0e-1f;            // :118, :133
   a.cmin = (double)1.0e-4f;           // :133
   a.dirichlet_x = dirichlet_x;
+  double* fs = nullptr;
+  SBM_CUDA_TRY(cudaMallocAsync(&fs, sizeof(double) * 4 * (size_t)g.nh, s));
+  k_acc_pre<<<flat(g.nh), 256, 0, s>>>(g, psi, a.half_idh2, a.thr, fs, fs + 3 * g.nh);
+  SBM_LAUNCHED(1);
+  a.fs = fs;
+  a.qd = fs + 3 * g.nh;
   double* src = cn;
   double* dst = tmp;
   // the interior of tmp must carry the ghosts too once we read it with
@@ -425,6 +454,7 @@ int accdiff_dev(cudaStream_t s, const Geo& g, const double* psi, double* cn, dou
     k_acc_ghost<<<gg, blk, 0, s>>>(g, cn, dirichlet_x);
     SBM_LAUNCHED(1);
   }
+  SBM_CUDA_TRY(cudaFreeAsync(fs, s));
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
 }
