@@ -829,6 +829,10 @@ __global__ void __launch_bounds__(256)
 // cell: r, invd, q_old and hk read, z written (20 B); the coarse values come
 // from L2.  z.r and z.q_old are reduced as in k_pc_prolong.  Tiles are
 // walked grid-stride (every block the same count: the barriers are uniform).
+// Weight of the Jacobi step of the multiplicative form: flexible-CG
+// iterations of the 128^3 validation solve are 53-55 for 1.5..1.9, 61-88
+// for weights <= 1 (NumPy prototype with the stored network).
+constexpr float kPcOmega = 1.5f;
 constexpr int kMTY = 64, kMTX = 8, kMTZ = 4;
 constexpr int kWY = kMTY / 4 + 2;  // coarse y window
 __global__ void __launch_bounds__(256, 3)
@@ -1081,9 +1085,9 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   int64_t b = (items + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;
   if (b < 1) b = 1;
-  // the multiplicative form with an over-relaxed Jacobi step (omega = 1.5:
+  // the multiplicative form with an over-relaxed Jacobi step (kPcOmega;
   // flexible-CG iterations of the 128^3 validation solve fall from 92 with
-  // the additive form to 54; 53-55 for omega in 1.5..1.9)
+  // the additive form to 54)
   if (ctx->pc_additive) {
     launch_pdl(netd::k_pc_prolong, dim3((unsigned)b), dim3(256), 0, s, g, c,
                (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->zf + kOff32,
@@ -1095,7 +1099,7 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
     const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
     launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, c, (const float*)pc->w->out,
                (const float*)pc->scal, r32, iv32, q32, pc->hk32, pc->scale, pc->bcx0, pc->bcx1,
-               1.5f, pc->zf + kOff32, (const int*)pc->net->err, partials, st);
+               netd::kPcOmega, pc->zf + kOff32, (const int*)pc->net->err, partials, st);
   }
   SBM_LAUNCHED(1);
 }
@@ -1113,7 +1117,7 @@ void net_pc_launch_part(sbm_ctx* ctx, int part, const float* r32, const float* i
   const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
   launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, c, (const float*)pc->w->out,
              (const float*)pc->scal, r32, iv32, q32, pc->hk32, pc->scale, pc->bcx0, pc->bcx1,
-             1.5f, pc->zf + kOff32, (const int*)pc->net->err, partials, st);
+             netd::kPcOmega, pc->zf + kOff32, (const int*)pc->net->err, partials, st);
   SBM_LAUNCHED(1);
 }
 

@@ -245,7 +245,9 @@ int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
  * rel-res and status go to the n-element arrays; ms_total is the device
  * time of the whole batch.  precond SBM_PC_LEARNED applies per volume (its
  * own attached network and grid permitting, else Jacobi;
- * sbm_ctx_last_precond of each context). */
+ * sbm_ctx_last_precond of each context).  The library caches the parent
+ * graph of the last batch (rebuilt when the set of volumes changes), so
+ * batch calls must not overlap: one host thread at a time. */
 int sbm_batch_solve(sbm_ctx** ctxs, int n, int bc_x0, int bc_x1, double scale, double tol,
                     int max_it, int precond, int* iters, double* final_res, int* status,
                     float* ms_total);
