@@ -371,7 +371,8 @@ def run_ours(args):
         pin[k] = (t, a)
     xout_t = torch.empty(nh, dtype=torch.float64, pin_memory=True)
     e2e = []
-    for step in range(max(1, args.steps)):
+    # W untimed warm-up round trips, then K timed ones
+    for step in range(args.warmup + max(1, args.steps)):
         flush.zero_()
         barrier()
         t1 = time.perf_counter()
@@ -384,7 +385,8 @@ def run_ours(args):
         lib = sbm.load_library()
         rc = lib.sbm_download(ctx._h, sbm.F_X, xo.ctypes.data_as(sbm.C.POINTER(sbm.C.c_double)), 1)
         assert rc == 0
-        e2e.append(time.perf_counter() - t1)
+        if step >= args.warmup:
+            e2e.append(time.perf_counter() - t1)
     e2e_v = statistics.mean(e2e)
     cpu = None
     if rank == 0 and ws == 1:
