@@ -80,7 +80,19 @@ extern "C" int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bc
   std::vector<cudaGraph_t> graphs(n);
   std::vector<int> vnodes((size_t)n, 0);
   cudaStream_t bs = ctxs[0]->stream;  // the batch runs on the first volume's stream
-  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  // events and the pinned state copies, released on every return path
+  struct Scratch {
+    cudaEvent_t t0 = nullptr, t1 = nullptr, ev = nullptr;
+    CgState* h = nullptr;
+    ~Scratch() {
+      if (t0) cudaEventDestroy(t0);
+      if (t1) cudaEventDestroy(t1);
+      if (ev) cudaEventDestroy(ev);
+      if (h) cudaFreeHost(h);
+    }
+  } sc;
+  cudaEvent_t& t0 = sc.t0;
+  cudaEvent_t& t1 = sc.t1;
   SBM_CUDA_TRY(cudaEventCreate(&t0));
   SBM_CUDA_TRY(cudaEventCreate(&t1));
   SBM_CUDA_TRY(cudaEventRecord(t0, bs));
@@ -144,10 +156,10 @@ extern "C" int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bc
   }
   // one launch runs every volume to convergence; then all states and round
   // counts come back in one go
-  CgState* h = nullptr;
+  CgState*& h = sc.h;
   SBM_CUDA_TRY(cudaMallocHost(&h, sizeof(CgState) * n));
   std::vector<int> rounds((size_t)n, 0);
-  cudaEvent_t ev;
+  cudaEvent_t& ev = sc.ev;
   SBM_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   int rc = SBM_OK;
   SBM_CUDA_TRY(cudaGraphLaunch(g_batch.exec, bs));
@@ -185,10 +197,6 @@ extern "C" int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bc
   float ms = 0.f;
   cudaEventElapsedTime(&ms, t0, t1);
   if (ms_total) *ms_total = ms;
-  cudaEventDestroy(ev);
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
-  cudaFreeHost(h);
   return rc;
 }
 

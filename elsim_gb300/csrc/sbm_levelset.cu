@@ -425,8 +425,16 @@ int accdiff_dev(cudaStream_t s, const Geo& g, const double* psi, double* cn, dou
   a.thr = (double)4.0e-1f;            // :118, :133
   a.cmin = (double)1.0e-4f;           // :133
   a.dirichlet_x = dirichlet_x;
-  double* fs = nullptr;
-  SBM_CUDA_TRY(cudaMallocAsync(&fs, sizeof(double) * 4 * (size_t)g.nh, s));
+  // per-call constants, stream-ordered scratch released on every return path
+  struct Scratch {
+    double* p = nullptr;
+    cudaStream_t s;
+    ~Scratch() {
+      if (p) cudaFreeAsync(p, s);
+    }
+  } scr{nullptr, s};
+  SBM_CUDA_TRY(cudaMallocAsync(&scr.p, sizeof(double) * 4 * (size_t)g.nh, s));
+  double* fs = scr.p;
   k_acc_pre<<<flat(g.nh), 256, 0, s>>>(g, psi, a.half_idh2, a.thr, fs, fs + 3 * g.nh);
   SBM_LAUNCHED(1);
   a.fs = fs;
@@ -454,7 +462,6 @@ int accdiff_dev(cudaStream_t s, const Geo& g, const double* psi, double* cn, dou
     k_acc_ghost<<<gg, blk, 0, s>>>(g, cn, dirichlet_x);
     SBM_LAUNCHED(1);
   }
-  SBM_CUDA_TRY(cudaFreeAsync(fs, s));
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
 }
