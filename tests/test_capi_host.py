@@ -87,3 +87,42 @@ def test_missing_library_fails_loudly(tmp_path):
             "    print('loud', 'no CPU fallback' in str(e))\n") % (str(ROOT), str(tmp_path / "x.so"))
     out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True).stdout
     assert "loud True" in out
+
+
+def test_entry_points_reject_bad_arguments_before_any_device_work(built):
+    """The geometry, connectivity, batch and checkpoint entry points check
+    their arguments on the host and return SBM_ERR_ARG (-1) without touching
+    the GPU: out-of-range stacking geometries, negative iteration counts,
+    unknown operators, null buffers."""
+    from elsim_gb300 import sbm
+    lib = sbm.load_library()
+    dp = C.POINTER(C.c_double)
+    vox = np.zeros(12 * 14 * 5)
+    out = np.zeros(100000)
+    v, o = vox.ctypes.data_as(dp), out.ctypes.data_as(dp)
+    # yg > yo; zg > xo; the tunnel loop would leave TmpB; negative offset
+    assert lib.sbm_ls_geometry(v, 12, 14, 5, 13, 9, 3, 4, 1.0, o) == sbm.ERR_ARG
+    assert lib.sbm_ls_geometry(v, 12, 14, 5, 7, 15, 3, 4, 1.0, o) == sbm.ERR_ARG
+    assert lib.sbm_ls_geometry(v, 12, 14, 5, 7, 9, 3, 30, 1.0, o) == sbm.ERR_ARG
+    assert lib.sbm_ls_geometry(v, 12, 14, 5, 7, 9, -1, 4, 1.0, o) == sbm.ERR_ARG
+    assert lib.sbm_ls_geometry(v, 12, 14, 5, 7, 9, 3, 4, float("nan"), o) == sbm.ERR_ARG
+    assert lib.sbm_ls_frontend(v, 12, 14, 5, 7, 9, 3, 4, 1.0, -1, 10, 0.1, o) == sbm.ERR_ARG
+    assert lib.sbm_ls_frontend(v, 12, 14, 5, 7, 9, 3, 4, 1.0, 5, -2, 0.1, o) == sbm.ERR_ARG
+    assert lib.sbm_allen_cahn(-1, 4, 4, 4, o) == sbm.ERR_ARG
+    assert lib.sbm_allen_cahn(3, 0, 4, 4, o) == sbm.ERR_ARG
+    assert lib.sbm_connectivity(0, 4, 4, o, 0.75, 10, o, o) == sbm.ERR_ARG
+    assert lib.sbm_connectivity(4, 4, 4, o, 0.0, 10, o, o) == sbm.ERR_ARG
+    assert lib.sbm_rm_ucnct(4, 4, 4, o, o, o, -1, o, o) == sbm.ERR_ARG
+    # batches: null contexts, an unknown operator
+    ops = (C.c_int * 1)(7)
+    bc = (C.c_int * 1)(0)
+    sc = (C.c_double * 1)(1.0)
+    hs = (C.c_void_p * 1)(None)
+    assert lib.sbm_batch_solve_ops(hs, ops, bc, bc, sc, 1, 1e-8, 100, 1, None, None, None,
+                                   None) == sbm.ERR_ARG
+    assert lib.sbm_batch_solve(None, 1, 0, 0, 1.0, 1e-8, 100, 1, None, None, None,
+                               None) == sbm.ERR_ARG
+    # checkpoints: no context
+    n = C.c_size_t(0)
+    assert lib.sbm_ctx_snapshot_size(None, C.byref(n)) == sbm.ERR_ARG
+    assert lib.sbm_ctx_restore(None, None, 0) == sbm.ERR_ARG
