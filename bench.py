@@ -57,8 +57,8 @@ METRIC = "sbm_potential_solve_time_256^3_relres_1e-8"
 # CG with the learned preconditioner).
 APPLY_TRAFFIC = {1: 398.2e6, 2: 326.2e6}
 # dram__bytes_read.sum + dram__bytes_write.sum of the 9 k_conv3_tc launches
-# of one preconditioner application at 256^3 (ncu); None until captured
-CONV_TRAFFIC = None
+# of one preconditioner application at 256^3 (ncu)
+CONV_TRAFFIC = 41.56e6
 UNIT = "s"
 
 
