@@ -187,3 +187,28 @@ def test_double_well_cahn_hilliard_pin():
     want = ci + dt * (dvc / dx2) / psp[1:-1, 1:-1, 1:-1]
     assert np.allclose(got, want, rtol=1e-12, atol=1e-14)
     assert not np.allclose(got, ci, rtol=0, atol=1e-9)  # the step did move c
+
+
+def test_cg_error_energy_decreases_monotonically():
+    """CG on a small SPD system (the CnE form, diagonal + scaled diffusion,
+    Neumann faces): the energy norm of the error, e.A e, must fall with every
+    further iteration -- the defining property of CG."""
+    rng = np.random.default_rng(7)
+    shp = (6, 5, 4)
+    K = np.asfortranarray(rng.uniform(0.2, 2.0, tuple(s + 2 for s in shp)))
+    dg = np.asfortranarray(rng.uniform(0.5, 1.5, K.shape))
+    rhs = np.asfortranarray(rng.normal(size=K.shape))
+    x0 = _pad(shp)
+    i = (slice(1, -1),) * 3
+    xs, _ = orc.cg(K, rhs, x0, 0.3, sbm.BC_COPY, sbm.BC_COPY, sbm.STOP_REL_RES, 1e-15, 5000,
+                   diag=dg)
+    energies = []
+    for m in range(1, 16):
+        xm, _ = orc.cg(K, rhs, x0, 0.3, sbm.BC_COPY, sbm.BC_COPY, sbm.STOP_REL_RES, 0.0, m,
+                       diag=dg)
+        e = _pad(shp)
+        e[i] = xm[i] - xs[i]
+        e = _homog(e, 0, 0)
+        energies.append(float((orc.apply(K, e, 0.3, diag=dg)[i] * e[i]).sum()))
+    assert all(a > 0 for a in energies)
+    assert all(b < a for a, b in zip(energies, energies[1:])), energies
