@@ -12,7 +12,7 @@ ghost planes, Neumann elsewhere, zero right-hand side; solved until
 Our arm (default): the production solver -- FP32 flexible CG with the
 learned coarse-grid preconditioner (a 3D U-Net on the 4x-coarsened grid,
 BF16 tcgen05 convolutions, weights elsim_gb300/weights/pc_unet.bin) applied
-multiplicatively (coarse correction, then one Jacobi step with omega 1.5)
+multiplicatively (coarse correction, then one Jacobi step with omega 2.3)
 and FP64 reliable-update refinement -- with fields resident in HBM; `value`
 is the mean device time of one solve (CUDA events on the solver stream),
 `e2e` the same solve through the C-ABI from pinned host buffers
@@ -404,7 +404,7 @@ def run_ours(args):
             "data": "synthetic (seeded spheres + tunnel; reference inputs are not public)",
             "config": _config(n, {
                 "method": ("FP32 flexible CG, learned U-Net coarse-grid correction (BF16 "
-                           "tcgen05) followed by one Jacobi step (omega 1.5) on the remaining "
+                           "tcgen05) followed by one Jacobi step (omega 2.3) on the remaining "
                            "residual, FP64 reliable-update refinement"
                            if used_pc == sbm.PC_LEARNED else
                            "FP32 Jacobi-PCG, FP64 reliable-update refinement"),

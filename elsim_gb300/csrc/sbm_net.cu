@@ -829,10 +829,15 @@ __global__ void __launch_bounds__(256)
 // cell: r, invd, q_old and hk read, z written (20 B); the coarse values come
 // from L2.  z.r and z.q_old are reduced as in k_pc_prolong.  Tiles are
 // walked grid-stride (every block the same count: the barriers are uniform).
-// Weight of the Jacobi step of the multiplicative form: flexible-CG
-// iterations of the 128^3 validation solve are 53-55 for 1.5..1.9, 61-88
-// for weights <= 1 (NumPy prototype with the stored network).
-constexpr float kPcOmega = 1.5f;
+// Weight of the Jacobi step of the multiplicative form.  Flexible-CG
+// iterations on the GPU (256^3 headline / 128^3 and 256^3 held-out / 64^3 /
+// 128^3 structures): omega 1.5: 86/56/82/54/67, 1.9: 72/47/71/51/53,
+// 2.1: 63/46/66/52/50, 2.3: 61/49/63/55/50, 2.6: 61/55/63/60/56; small
+// grids hardly depend on it, large ones gain most near 2.1-2.3.
+#ifndef SBM_PC_OMEGA
+#define SBM_PC_OMEGA 2.3f
+#endif
+constexpr float kPcOmega = SBM_PC_OMEGA;
 constexpr int kMTY = 64, kMTX = 8, kMTZ = 4;
 constexpr int kWY = kMTY / 4 + 2;  // coarse y window
 __global__ void __launch_bounds__(256, 3)
@@ -1086,8 +1091,8 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   if (b > 152 * 8) b = 152 * 8;
   if (b < 1) b = 1;
   // the multiplicative form with an over-relaxed Jacobi step (kPcOmega;
-  // flexible-CG iterations of the 128^3 validation solve fall from 92 with
-  // the additive form to 54)
+  // flexible-CG iterations of the 256^3 headline solve fall from 123-128
+  // with the additive form to 61)
   if (ctx->pc_additive) {
     launch_pdl(netd::k_pc_prolong, dim3((unsigned)b), dim3(256), 0, s, g, c,
                (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->zf + kOff32,

@@ -167,7 +167,7 @@ int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p);
  * (SBM_TUNE_NO_TMA): use the register-tiled FP32 stencil instead of the
  * TMA-staged one; bit 1 (SBM_TUNE_PC_ADDITIVE): apply the learned
  * preconditioner in its additive form z = D^-1 r + P e_c instead of the
- * default multiplicative one z = z1 + 1.5 D^-1 (r - A z1), z1 = P e_c.
+ * default multiplicative one z = z1 + 2.3 D^-1 (r - A z1), z1 = P e_c.
  * No counterpart in the reference. */
 #define SBM_TUNE_NO_TMA 1
 #define SBM_TUNE_PC_ADDITIVE 2

@@ -289,7 +289,7 @@ def apply_dir(coef_h, p_int, scale, bcx0, bcx1):
     return scale * s
 
 
-OMEGA = 1.5  # weight of the Jacobi step of the multiplicative form
+OMEGA = 2.3  # weight of the Jacobi step of the multiplicative form (the GPU's)
 
 
 def pc_apply(p, kout, coef_h, r_h, scale=1.0, bcx0=1, bcx1=1, rounding=True,

@@ -114,7 +114,7 @@ def test_apply_dir_matches_c_oracle():
 def test_multiplicative_form_cuts_iterations():
     """Flexible CG (FP64, NumPy) on a 64^3 tunnelled structure with the
     stored network: the multiplicative form (coarse correction, then one
-    Jacobi step with omega = 1.5 on the remaining residual) needs clearly
+    Jacobi step with the GPU's omega on the remaining residual) needs clearly
     fewer iterations than the additive form."""
     from elsim_gb300 import learned, synth
     from oracle import sbm_oracle as orc
