@@ -174,6 +174,18 @@ __device__ __forceinline__ void expect_tx(uint64_t* bar, unsigned bytes) {
                : "memory");
 }
 
+// Adds to the transaction count of the current phase without arriving (the
+// arrival follows with the stage's remaining copies).
+__device__ __forceinline__ void expect_tx_only(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(sa(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mb_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sa(bar)) : "memory");
+}
+
 // The tap MMAs of one chunk.  A descriptor = halo plane 0 at offset
 // (0, 0); B descriptor = the chunk's weight image.  Descriptors advance by
 // constant start-address offsets (the 14-bit start field holds address /
@@ -218,8 +230,6 @@ __device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t 
 }
 
 __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvMap m, ConvArgs a) {
-  pdl_begin();
-  if ((a.skip && *a.skip) || (a.skip2 && *a.skip2)) return;
   extern __shared__ __align__(1024) unsigned char sm[];
   const int P = a.planes;  // z planes per CTA (1, 2 or 4), one accumulator each
   const int ahalf = a_half_bytes(P);
@@ -242,16 +252,44 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   const int y0 = ty * TY, x0 = tx * TX;
   const int zl = z0 % a.nzs, sample = z0 / a.nzs;
   const int ncols = P * nt <= 32 ? 32 : (P * nt <= 64 ? 64 : (P * nt <= 128 ? 128 : 256));
+  // Set-up that reads nothing the preceding kernels write runs before
+  // griddepcontrol.wait, overlapping their tail: the barriers, the
+  // tensor-map prefetch and, when the weights are frozen (a.wpre), the
+  // weight copies of the first stages.  Tensor memory is allocated only
+  // after the wait: a CTA waiting on an earlier grid holds none, so it can
+  // never keep a CTA of that grid from allocating.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  const __nv_bfloat16* wsrc =
+      (a.tw == 16 ? a.wimg16 : a.wimg) + (int64_t)a.tw * blockIdx.y * 27 * a.cin;
+  const int npre = a.wpre ? min(nchunk, nst) : 0;  // chunks whose weights are already on the way
+  if (tid == 0) {
+    for (int s = 0; s < 2 * NST + 1; ++s) mb_init(&full[s]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&m.x)) : "memory");
+    for (int c = 0; c < npre; ++c) {
+      expect_tx_only(&full[c], bbytes);
+      bulk_load(sm + c * stage_bytes + 2 * ahalf, wsrc + (int64_t)c * 27 * nt * 16, bbytes,
+                &full[c]);
+    }
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if ((a.skip && *a.skip) || (a.skip2 && *a.skip2)) {
+    // the flag is the same for every thread; the copies in flight land
+    // before the CTA exits
+    if (tid == 0) {
+      for (int c = 0; c < npre; ++c) {
+        mb_arrive(&full[c]);
+        mb_wait(&full[c], 0);
+      }
+    }
+    return;
+  }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      sa(tslot)),
                  "r"(ncols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  if (tid == 0) {
-    for (int s = 0; s < 2 * NST + 1; ++s) mb_init(&full[s]);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -260,17 +298,16 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   bool ok = true;
   if (tid == 0) {
     const uint32_t id = idesc_bf16(nt), id2 = idesc_bf16(2 * nt), id3 = idesc_bf16(3 * nt);
-    const __nv_bfloat16* wsrc =
-        (a.tw == 16 ? a.wimg16 : a.wimg) + (int64_t)a.tw * blockIdx.y * 27 * a.cin;
     const unsigned abox = (unsigned)(HY * HX * (P + 2) * 16);
     int issued[NST] = {}, landed[NST] = {}, committed[NST] = {}, freed[NST] = {};
     auto load = [&](int c, int s) {
       unsigned char* A = sm + s * stage_bytes;
-      expect_tx(&full[s], 2 * abox + bbytes);
+      const bool pre = c < npre;  // weights issued before the wait
+      expect_tx(&full[s], 2 * abox + (pre ? 0u : (unsigned)bbytes));
       const int grp = (a.offx + c * KS) >> 3;
       tma_load5(A, &m.x, &full[s], 8 * (y0 - 1), x0 - 1, zl - 1, sample, grp);
       tma_load5(A + ahalf, &m.x, &full[s], 8 * (y0 - 1), x0 - 1, zl - 1, sample, grp + 1);
-      bulk_load(A + 2 * ahalf, wsrc + (int64_t)c * 27 * nt * 16, bbytes, &full[s]);
+      if (!pre) bulk_load(A + 2 * ahalf, wsrc + (int64_t)c * 27 * nt * 16, bbytes, &full[s]);
       ++issued[s];
     };
     for (int c = 0; c < nchunk && c < nst; ++c) load(c, c);
@@ -643,6 +680,13 @@ extern "C" int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const 
   a.y16 = nullptr; a.y32 = (float*)dy; a.relu = relu; a.flip = flip; a.err = (int*)de;
   conv3_wimage(a.w, cout, cin, 0, flip, 64, (__nv_bfloat16*)dimg, s);
   a.wimg = (const __nv_bfloat16*)dimg;
+  // the uploads and the weight image are complete before the launch, so
+  // the kernel may copy the weights before its dependency wait
+  if (cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaFree(dimg);
+    return fail(SBM_ERR_CUDA);
+  }
+  a.wpre = 1;
   rc = conv3_launch(&a, nullptr, use_tc, s);
   if (rc) {
     cudaStreamSynchronize(s);

@@ -43,6 +43,9 @@ struct ConvArgs {
   int* err;                // set to 1 if a wait expired
   const int* skip;         // launch is a no-op while *skip != 0 (may be null)
   const int* skip2;        //   or while *skip2 != 0 (may be null)
+  int wpre;                // 1: no kernel of the launch's dependency chain writes the
+                           //    weight images, so the tensor-core kernel copies them
+                           //    before waiting on the preceding kernel
   // tensor-core kernel only:
   int planes;              // z planes per CTA: 1, or 2 (nzs even)
   __nv_bfloat16* pool;     // 2x2x2-averaged BF16 output [V/8][cout] (planes 2) or null

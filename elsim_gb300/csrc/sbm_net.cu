@@ -453,6 +453,9 @@ ConvArgs layer_args(sbm_net* n, const Work& w, int l, int lev, const bf16* x, in
   a.x = x; a.wimg = n->wimg + kL.off[l]; a.wimg16 = n->wimg16 + kL.off[l];
   a.bias = n->w32 + kL.boff[l];
   a.relu = 1; a.flip = 0; a.err = n->err; a.skip = skip; a.skip2 = skip2;
+  // the preconditioner's passes (the only ones with skip flags) run on
+  // frozen weights; training rewrites them between passes
+  a.wpre = skip != nullptr;
   return a;
 }
 
