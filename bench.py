@@ -371,8 +371,10 @@ def run_ours(args):
         pin[k] = (t, a)
     xout_t = torch.empty(nh, dtype=torch.float64, pin_memory=True)
     e2e = []
-    # W untimed warm-up round trips, then K timed ones
-    for step in range(args.warmup + max(1, args.steps)):
+    # W untimed warm-up round trips, then max(K, 10) timed ones: the host
+    # side (a shared machine) varies by a few ms between round trips
+    n_e2e = max(10, args.steps)
+    for step in range(args.warmup + n_e2e):
         flush.zero_()
         barrier()
         t1 = time.perf_counter()
@@ -430,7 +432,9 @@ def run_ours(args):
             "roofline": roofline or apply_roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": 3 * nh * 8,
-                    "d2h_bytes_per_step": nh * 8},
+                    "d2h_bytes_per_step": nh * 8, "round_trips": len(e2e),
+                    "min": min(e2e), "median": statistics.median(e2e),
+                    "max": max(e2e)},
             "gpu_launches": launches,
             "clocks": clk,
         }
