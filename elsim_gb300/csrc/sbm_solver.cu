@@ -1229,8 +1229,10 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   // bodies of 2 iterations per captured chunk: the flexible CG converges in
-  // ~10x fewer iterations, so shorter chunks trim the no-op tail
-  const int clen = ctx->chunk > 0 ? ctx->chunk : (learned ? 4 : chunk_len(ctx));
+  // ~10x fewer iterations, so shorter chunks trim the no-op tail (256^3,
+  // 61 iterations: 28.51 / 28.26 / 28.19 / 28.21 ms with 8 / 4 / 2 / 1
+  // bodies per chunk)
+  const int clen = ctx->chunk > 0 ? ctx->chunk : (learned ? 2 : chunk_len(ctx));
   const std::string key =
       key_of(learned ? (use_tma ? "mixfcg2-tma" : "mixfcg2") : (use_tma ? "mixrel2-tma" : "mixrel2"),
              hk32, dg32, x32, r32, pbuf[0], pbuf[1], learned ? (const void*)zl : iv32, sp.scale,
