@@ -915,6 +915,9 @@ __global__ void __launch_bounds__(256)
 // convergence on the FP64 norm, new rho / beta.  No-op unless flagged.
 // FLEX: rho / beta and the first-residual flag are left to the flexible
 // preconditioner kernel that follows.
+// Tiles of BX x BY columns x zc planes are walked grid-stride by a grid of
+// a few blocks per SM (rel_grid): the launch is a no-op in most iterations,
+// and a small grid keeps that no-op cheap.
 template <int FORM, bool PC, bool FLEX = false>
 __global__ void __launch_bounds__(BX* BY)
     k_rel_resid(OpArgs<double> op, Geo g32, int zc, const double* __restrict__ d64,
@@ -927,87 +930,95 @@ __global__ void __launch_bounds__(BX* BY)
   // the first replacement of a solve sees a zero correction (d64 and x32
   // were just cleared): the true residual is r0 itself, no stencil needed
   const bool zero_corr = st->initial != 0;
-  SBM_COLUMN_PROLOGUE(g, zc)
+  const int nty = (g.ny + BX - 1) / BX, ntx = (g.nx + BY - 1) / BY;
+  const int ntiles = nty * ntx * ((g.nz + zc - 1) / zc);
   double a_rr = 0.0, a_r32 = 0.0, a_rz = 0.0;
-  if (active && k0 <= k1 && zero_corr) {
-    for (int k = k0; k <= k1; ++k) {
-      const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
-      const double rv = r0[c];
-      const float rf = (float)rv;
-      r32[c3] = rf;
-      const float zf = PC ? invd32[c3] * rf : rf;
-      a_rr += rv * rv;
-      a_r32 += (double)rf * (double)rf;
-      a_rz += (double)rf * (double)zf;
-    }
-  } else if (!zero_corr && k0 <= k1) {
-    // The correction V = d64 + (double)x32 of each cell is formed once: the
-    // thread's own column rolls along z (vm, vc, vp) and every plane is
-    // shared, with its in-plane halo, through shared memory, so the lateral
-    // neighbours are read instead of formed again (the same operations on
-    // the same operands: the same bits).  This cuts the FP64 instructions
-    // per cell from about 34 to about 20; the kernel is FP64-pipe bound.
-    // All threads of the block march the same planes k0..k1 (uniform
-    // barriers); 80 of them also form the halo cells of each plane.
-    __shared__ double sv[BY + 2][BX + 2];
-    const int tx = threadIdx.x, ty = threadIdx.y, tf = ty * BX + tx;
-    const int ib = blockIdx.x * BX, jb = blockIdx.y * BY;  // cell (ib + col, jb + row)
-    int hrow = -1, hcol = -1;
-    if (tf < 2 * BX) {  // rows 0 and BY + 1 (x halo)
-      hcol = tf % BX + 1;
-      hrow = tf < BX ? 0 : BY + 1;
-    } else if (tf < 2 * BX + 2 * BY) {  // columns 0 and BX + 1 (y halo)
-      const int u = tf - 2 * BX;
-      hrow = u % BY + 1;
-      hcol = u < BY ? 0 : BX + 1;
-    }
-    const int hi = ib + hcol, hj = jb + hrow;
-    // only interior halo cells are ever read (the ghost rules replace the rest)
-    const bool hact = hrow >= 0 && hi >= 1 && hi <= g.ny && hj >= 1 && hj <= g.nx;
-    auto corr = [&](int ii, int jj, int kk) {
-      return d64[g.ix(ii, jj, kk)] + (double)x32[g32.ix(ii, jj, kk)];
-    };
-    double vc = 0.0, vm = 0.0;
-    if (active) {
-      vc = corr(i, j, k0);
-      vm = (k0 == 1) ? vc : corr(i, j, k0 - 1);
-    }
-    for (int k = k0; k <= k1; ++k) {
-      double vp = 0.0, hv = 0.0;
-      if (active) vp = (k == g.nz) ? vc : corr(i, j, k + 1);
-      if (hact) hv = corr(hi, hj, k);
-      __syncthreads();  // the previous plane's readers are done
-      sv[ty + 1][tx + 1] = vc;
-      if (hrow >= 0) sv[hrow][hcol] = hv;
-      __syncthreads();
-      if (active) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int ib = (t % nty) * BX, jb = ((t / nty) % ntx) * BY;  // cell (ib + col, jb + row)
+    const int i = ib + threadIdx.x + 1, j = jb + threadIdx.y + 1;
+    const int k0 = (t / (nty * ntx)) * zc + 1;
+    const int k1 = min(k0 + zc - 1, g.nz);
+    const bool active = (i <= g.ny) && (j <= g.nx);
+    if (active && zero_corr) {
+      for (int k = k0; k <= k1; ++k) {
         const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
-        const double pc = vc;
-        const double pym = (i == 1) ? pc : sv[ty + 1][tx];
-        const double pyp = (i == g.ny) ? pc : sv[ty + 1][tx + 2];
-        const double pxm = (j == 1) ? (op.bcx0 ? 0.0 : pc) : sv[ty][tx + 1];
-        const double pxp = (j == g.nx) ? (op.bcx1 ? 0.0 : pc) : sv[ty + 2][tx + 1];
-        const double pzm = vm;
-        const double pzp = vp;
-        const double* hk = op.hk;
-        const double s =
-            op.fc ? face_sum_stored<double>(g, op.fc, c, pc, pyp, pym, pxp, pxm, pzp, pzm)
-                  : face_sum<double>(hk[c], pc, hk[c + 1], pyp, hk[c - 1], pym, hk[c + g.sx],
-                                     pxp, hk[c - g.sx], pxm, hk[c + g.sz], pzp, hk[c - g.sz],
-                                     pzm);
-        const double ad = (FORM == 0) ? op.scale * s : op.diag[c] * pc - op.scale * s;
-        const double rv = r0[c] - ad;
+        const double rv = r0[c];
         const float rf = (float)rv;
         r32[c3] = rf;
+        const float zf = PC ? invd32[c3] * rf : rf;
         a_rr += rv * rv;
         a_r32 += (double)rf * (double)rf;
-        if (!FLEX) {  // the flexible solver takes rho from its preconditioner kernel
-          const float zf = PC ? invd32[c3] * rf : rf;
-          a_rz += (double)rf * (double)zf;
-        }
+        a_rz += (double)rf * (double)zf;
       }
-      vm = vc;
-      vc = vp;
+    } else if (!zero_corr) {
+      // The correction V = d64 + (double)x32 of each cell is formed once: the
+      // thread's own column rolls along z (vm, vc, vp) and every plane is
+      // shared, with its in-plane halo, through shared memory, so the lateral
+      // neighbours are read instead of formed again (the same operations on
+      // the same operands: the same bits).  This cuts the FP64 instructions
+      // per cell from about 34 to about 20; the kernel is FP64-pipe bound.
+      // All threads of the block march the same planes k0..k1 (uniform
+      // barriers); 80 of them also form the halo cells of each plane.
+      __shared__ double sv[BY + 2][BX + 2];
+      const int tx = threadIdx.x, ty = threadIdx.y, tf = ty * BX + tx;
+      int hrow = -1, hcol = -1;
+      if (tf < 2 * BX) {  // rows 0 and BY + 1 (x halo)
+        hcol = tf % BX + 1;
+        hrow = tf < BX ? 0 : BY + 1;
+      } else if (tf < 2 * BX + 2 * BY) {  // columns 0 and BX + 1 (y halo)
+        const int u = tf - 2 * BX;
+        hrow = u % BY + 1;
+        hcol = u < BY ? 0 : BX + 1;
+      }
+      const int hi = ib + hcol, hj = jb + hrow;
+      // only interior halo cells are ever read (the ghost rules replace the rest)
+      const bool hact = hrow >= 0 && hi >= 1 && hi <= g.ny && hj >= 1 && hj <= g.nx;
+      auto corr = [&](int ii, int jj, int kk) {
+        return d64[g.ix(ii, jj, kk)] + (double)x32[g32.ix(ii, jj, kk)];
+      };
+      double vc = 0.0, vm = 0.0;
+      if (active) {
+        vc = corr(i, j, k0);
+        vm = (k0 == 1) ? vc : corr(i, j, k0 - 1);
+      }
+      for (int k = k0; k <= k1; ++k) {
+        double vp = 0.0, hv = 0.0;
+        if (active) vp = (k == g.nz) ? vc : corr(i, j, k + 1);
+        if (hact) hv = corr(hi, hj, k);
+        __syncthreads();  // the previous plane's readers are done
+        sv[ty + 1][tx + 1] = vc;
+        if (hrow >= 0) sv[hrow][hcol] = hv;
+        __syncthreads();
+        if (active) {
+          const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
+          const double pc = vc;
+          const double pym = (i == 1) ? pc : sv[ty + 1][tx];
+          const double pyp = (i == g.ny) ? pc : sv[ty + 1][tx + 2];
+          const double pxm = (j == 1) ? (op.bcx0 ? 0.0 : pc) : sv[ty][tx + 1];
+          const double pxp = (j == g.nx) ? (op.bcx1 ? 0.0 : pc) : sv[ty + 2][tx + 1];
+          const double pzm = vm;
+          const double pzp = vp;
+          const double* hk = op.hk;
+          const double s =
+              op.fc ? face_sum_stored<double>(g, op.fc, c, pc, pyp, pym, pxp, pxm, pzp, pzm)
+                    : face_sum<double>(hk[c], pc, hk[c + 1], pyp, hk[c - 1], pym, hk[c + g.sx],
+                                       pxp, hk[c - g.sx], pxm, hk[c + g.sz], pzp, hk[c - g.sz],
+                                       pzm);
+          const double ad = (FORM == 0) ? op.scale * s : op.diag[c] * pc - op.scale * s;
+          const double rv = r0[c] - ad;
+          const float rf = (float)rv;
+          r32[c3] = rf;
+          a_rr += rv * rv;
+          a_r32 += (double)rf * (double)rf;
+          if (!FLEX) {  // the flexible solver takes rho from its preconditioner kernel
+            const float zf = PC ? invd32[c3] * rf : rf;
+            a_rz += (double)rf * (double)zf;
+          }
+        }
+        vm = vc;
+        vc = vp;
+      }
+      __syncthreads();  // the next tile reuses the plane tile
     }
   }
   double v[3] = {a_rr, a_r32, a_rz}, tot[3];
@@ -1156,13 +1167,17 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   const dim3 cgrid((unsigned)std::min<int64_t>(std::max<int64_t>(items / 16 / 256, 1), 152 * 8));
   const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
   float* const pbuf[2] = {p32, ctx->rold32 + kOff32};  // alternating direction buffers
+  // the replacement kernel walks its tiles grid-stride with four blocks per
+  // SM (four fit at its 56 registers), so its usual no-op launch is cheap
+  const int64_t rel_tiles = (int64_t)sh64.grid.x * sh64.grid.y * sh64.grid.z;
+  const dim3 rgrid((unsigned)std::min<int64_t>(rel_tiles, 152 * 4));
   auto rel = [&](cudaStream_t s2) {
 #define SBM_REL(F, P)                                                                          \
-  k_rel_resid<F, P><<<sh64.grid, sh64.block, 0, s2>>>(op64, g32, sh64.zc, ctx->d64, x32,      \
-                                                       ctx->r0, r32, iv32, ctx->partials,      \
-                                                       ctx->st)
+  k_rel_resid<F, P><<<rgrid, sh64.block, 0, s2>>>(op64, g32, sh64.zc, ctx->d64, x32,          \
+                                                   ctx->r0, r32, iv32, ctx->partials,          \
+                                                   ctx->st)
     if (learned) {
-      launch_pdl(k_rel_resid<0, false, true>, sh64.grid, sh64.block, 0, s2, op64, g32, sh64.zc,
+      launch_pdl(k_rel_resid<0, false, true>, rgrid, sh64.block, 0, s2, op64, g32, sh64.zc,
                  (const double*)ctx->d64, (const float*)x32, (const double*)ctx->r0, r32,
                  (const float*)iv32, ctx->partials, ctx->st);
     } else if (sp.form == 0) {
