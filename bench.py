@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import gc
 import json
 import math
 import os
@@ -298,6 +299,10 @@ def run_ours(args):
     # timed region: K solves, each timed on the device with CUDA events on the
     # solver stream (x reset and L2 flush happen between solves, untimed)
     clocks = Clocks()
+    # a collection of the interpreter's garbage inside a timed solve stalls
+    # the host that feeds the captured chunks (tens of ms with torch loaded)
+    gc.collect()
+    gc.disable()
     barrier()
     clocks.start()
     l0 = sbm.launch_count()
@@ -307,6 +312,7 @@ def run_ours(args):
         info = solve(sbm.PREC_MIXED, head_pc)
         times.append(info["ms"] / 1e3)
     barrier()
+    gc.enable()
     wall = time.perf_counter() - t0
     launches = sbm.launch_count() - l0
     clk = clocks.stop()
@@ -374,6 +380,8 @@ def run_ours(args):
     # W untimed warm-up round trips, then max(K, 10) timed ones: the host
     # side (a shared machine) varies by a few ms between round trips
     n_e2e = max(10, args.steps)
+    gc.collect()
+    gc.disable()
     for step in range(args.warmup + n_e2e):
         flush.zero_()
         barrier()
@@ -389,6 +397,7 @@ def run_ours(args):
         assert rc == 0
         if step >= args.warmup:
             e2e.append(time.perf_counter() - t1)
+    gc.enable()
     e2e_v = statistics.mean(e2e)
     cpu = None
     if rank == 0 and ws == 1:
