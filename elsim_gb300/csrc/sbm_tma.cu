@@ -292,7 +292,7 @@ bool make_map(CUtensorMap* m, const float* base, const Geo& g32) {
 
 }  // namespace
 
-// The driver's tensor-map encoder (runtime entry-point query, once).
+// The CUDA driver API's tensor-map encoder (runtime entry-point query, once).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
