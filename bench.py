@@ -16,7 +16,8 @@ multiplicatively (coarse correction, then one Jacobi step with omega 2.3)
 and FP64 reliable-update refinement -- with fields resident in HBM; `value`
 is the mean device time of one solve (CUDA events on the solver stream),
 `e2e` the same solve through the C-ABI from pinned host buffers
-(coef/x/rhs uploaded, x downloaded) timed on the wall clock.  The plain FP64
+(coef/x/rhs uploaded, x downloaded) timed on the wall clock, the median of
+at least 10 round trips (mean, extremes and samples beside it).  The plain FP64
 CG (the drop-in), the FP32 Jacobi-PCG and the additive form of the learned
 preconditioner are timed beside it (`--pc jacobi` makes Jacobi-PCG the
 headline).
@@ -398,7 +399,10 @@ def run_ours(args):
         if step >= args.warmup:
             e2e.append(time.perf_counter() - t1)
     gc.enable()
-    e2e_v = statistics.mean(e2e)
+    # the median: about one round trip in ten on the shared host stalls for
+    # 15-19 ms on the host side (seen with the collector off too); the mean
+    # and every sample stay in the line
+    e2e_v = statistics.median(e2e)
     cpu = None
     if rank == 0 and ws == 1:
         cv, ci = cpu_sample(prob, 12.0)
@@ -441,9 +445,10 @@ def run_ours(args):
             "roofline": roofline or apply_roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": 3 * nh * 8,
-                    "d2h_bytes_per_step": nh * 8, "round_trips": len(e2e),
-                    "min": min(e2e), "median": statistics.median(e2e),
-                    "max": max(e2e)},
+                    "d2h_bytes_per_step": nh * 8, "statistic": "median",
+                    "round_trips": len(e2e), "mean": statistics.mean(e2e),
+                    "min": min(e2e), "max": max(e2e),
+                    "samples": [round(t, 6) for t in e2e]},
             "gpu_launches": launches,
             "clocks": clk,
         }
