@@ -1,0 +1,82 @@
+"""Host side of bench.py without a GPU: the reference arm's JSON line (the
+reference's CG restated by the oracle, on the host cores) on a small grid,
+the clock / throttle-reason parser of the sampled nvidia-smi log, and the
+U-Net FLOP count behind the tensor roofline."""
+import json
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+sys.path.insert(0, str(ROOT))
+import bench  # noqa: E402
+
+
+def test_reference_arm_line(built):
+    out = subprocess.run(
+        [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--size", "32",
+         "--steps", "1", "--warmup", "0"],
+        cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+                "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference"
+    assert line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["higher_is_better"] is False
+    assert line["value"] > 0 and line["steps"] == 1 and line["warmup"] == 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    assert line["config"]["grid"] == [32, 32, 32]
+
+
+class _Done:
+    """Stands in for the nvidia-smi process the sampler stops."""
+
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+    def kill(self):
+        pass
+
+
+def _clocks(lines):
+    c = bench.Clocks()
+    c.f.write("".join(ln + "\n" for ln in lines))
+    c.f.flush()
+    c.p = _Done()
+    return c.stop()
+
+
+def test_clock_parser_median_and_reasons():
+    ok = "0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active"
+    capped = "0, 1980, 2070, 1390.5, 0x4, Not Active, Not Active, Not Active, Active"
+    slow = "0, 1500, 2070, 700.0, 0x8, Active, Not Active, Not Active, Not Active"
+    r = _clocks([ok, ok, capped])
+    assert r["sm_mhz"] == 2070.0 and r["sm_max_mhz"] == 2070.0 and r["samples"] == 3
+    assert r["reasons"] == ["sw_power_cap"]
+    r = _clocks([ok, slow, "garbage line", "0, n/a, 2070"])
+    assert r["samples"] == 2 and r["reasons"] == ["hw_slowdown"]
+    assert r["sm_mhz"] == pytest.approx((2070.0 + 1500.0) / 2)
+
+
+def test_clock_parser_without_samples():
+    r = _clocks([])
+    assert r["sm_mhz"] is None and r["samples"] == 0 and r["reasons"] == []
+
+
+def test_unet_flops():
+    # 2 * cin * cout * 27 * voxels over the nine 3x3x3 layers at 64^3 coarse
+    want = sum(2 * ci * co * 27 * (64 >> lev) ** 3 for ci, co, lev in bench.UNET)
+    assert bench.unet_flops(256) == want == 20_019_806_208
+    assert bench.unet_flops(128) * 8 == bench.unet_flops(256)
