@@ -9,10 +9,12 @@ import re
 
 import pytest
 
+from capi_header import c_constants as _c_constants
+from capi_header import c_functions as _c_functions
+from capi_header import c_struct as _c_struct
 from conftest import ROOT
 
 F90 = (ROOT / "include" / "sbm_capi.f90").read_text()
-HDR = (ROOT / "include" / "sbm_capi.h").read_text()
 
 # Fortran kind -> C base type
 KIND = {"INTEGER(C_INT)": "int", "REAL(C_DOUBLE)": "double", "REAL(C_FLOAT)": "float",
@@ -65,63 +67,6 @@ def _decl(line):
         m = re.match(r"(\w+)\s*(\((.*)\))?$", item.strip())
         names.append((m.group(1).lower(), m.group(3)))
     return attrs[0].replace(" ", ""), attrs[1:], names
-
-
-def _c_text():
-    return re.sub(r"/\*.*?\*/", "", HDR, flags=re.S)
-
-
-def _c_constants():
-    text = _c_text()
-    vals = {m.group(1): int(m.group(2))
-            for m in re.finditer(r"#define\s+(SBM_\w+)\s+(-?\d+)\b", text)}
-    body = re.search(r"enum\s+sbm_field\s*\{(.*?)\}", text, re.S).group(1)
-    n = 0
-    for item in _split_top(body):
-        m = re.match(r"(\w+)\s*(=\s*(-?\d+))?$", item.strip())
-        if not m:
-            continue
-        if m.group(3) is not None:
-            n = int(m.group(3))
-        vals[m.group(1)] = n
-        n += 1
-    return vals
-
-
-def _c_param(p):
-    p = re.sub(r"\bconst\b|\bstruct\b", " ", p)
-    stars = p.count("*")
-    toks = p.replace("*", " ").split()
-    return toks[0], stars, toks[-1]
-
-
-def _c_functions():
-    text = " ".join(re.sub(r"^\s*#.*$", "", _c_text(), flags=re.M).split())
-    funcs = {}
-    for stmt in re.split(r"[;{}]", text):
-        m = re.match(r"\s*[\w\s\*]*?\b(sbm_\w+)\s*\(([^()]*)\)\s*$", stmt)
-        if not m:
-            continue
-        params = [] if m.group(2).strip() in ("", "void") else [
-            _c_param(p) for p in m.group(2).split(",")]
-        funcs[m.group(1)] = params
-    return funcs
-
-
-def _c_struct(name):
-    text = _c_text()
-    body = re.search(r"typedef\s+struct\s+%s\s*\{(.*?)\}\s*%s\s*;" % (name, name), text,
-                     re.S).group(1)
-    fields = []
-    for stmt in body.split(";"):
-        stmt = stmt.strip()
-        if not stmt:
-            continue
-        ctype, rest = stmt.split(None, 1)
-        for item in rest.split(","):
-            m = re.match(r"(\w+)\s*(\[(\w+)\])?$", item.strip())
-            fields.append((m.group(1).lower(), ctype, m.group(3)))
-    return fields
 
 
 def _f90_types():
