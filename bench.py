@@ -88,6 +88,18 @@ def _dist():
     return ws, rank
 
 
+def _max_over_ranks(x: float, ws: int, device) -> float:
+    """The largest of every rank's x (a job of replicas takes as long as
+    its slowest one); x itself on one process."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _config(n, extra=None):
     cfg = {"workload": f"SBM potential solve {n}^3, spheres r~U[4,10] + tunnel r=6, "
                        f"solid 0.6, k=psi+0.1(1-psi), Dirichlet 0/1 on x faces, rel-res 1e-8",
@@ -320,11 +332,7 @@ def run_ours(args):
     used_pc = ctx.last_precond()
     xm = ctx.download("x")[1:-1, 1:-1, 1:-1]
     rel_err = float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))
-    t_local = max(times)
-    if ws > 1:
-        tt = torch.tensor([t_local], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_local = float(tt.item())
+    t_local = _max_over_ranks(max(times), ws, dev)
     value = statistics.mean(times) if ws == 1 else t_local
     # kernel timings live on the solver stream: the fused direction + stencil
     # kernel (HBM roofline; the headline roofline for Jacobi-PCG) and, with
@@ -402,7 +410,7 @@ def run_ours(args):
     # the median: about one round trip in ten on the shared host stalls for
     # 15-19 ms on the host side (seen with the collector off too); the mean
     # and every sample stay in the line
-    e2e_v = statistics.median(e2e)
+    e2e_v = _max_over_ranks(statistics.median(e2e), ws, dev)
     cpu = None
     if rank == 0 and ws == 1:
         cv, ci = cpu_sample(prob, 12.0)

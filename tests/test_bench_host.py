@@ -80,3 +80,50 @@ def test_unet_flops():
     want = sum(2 * ci * co * 27 * (64 >> lev) ** 3 for ci, co, lev in bench.UNET)
     assert bench.unet_flops(256) == want == 20_019_806_208
     assert bench.unet_flops(128) * 8 == bench.unet_flops(256)
+
+
+def _max_worker(rank, port, q):
+    import torch
+    import torch.distributed as dist
+
+    sys.path.insert(0, str(ROOT))
+    import bench as b
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=2)
+    try:
+        q.put((rank, b._max_over_ranks(1.5 + 2.0 * rank, 2, torch.device("cpu"))))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_max_over_ranks_with_two_gloo_ranks():
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_max_worker, args=(r, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert got == {0: 3.5, 1: 3.5}
+    assert bench._max_over_ranks(2.25, 1, None) == 2.25
+
+
+def test_reference_arm_on_a_non_zero_rank_is_silent(built):
+    import os
+
+    env = dict(os.environ, WORLD_SIZE="2", RANK="1", LOCAL_RANK="1")
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                          "--size", "32", "--steps", "1", "--warmup", "0"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=300, env=env)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip() == ""
