@@ -142,6 +142,8 @@ static double sum_dsq_w(int ny, int nx, int nz, const double* a, const double* b
   return t;
 }
 
+/* Global interior sum of a*b: the reference's local sum + MPI_ALLGATHER +
+ * SUM over ranks (e.g. the CG norms of SBMES:524-540), on one domain. */
 double orc_dot(int ny, int nx, int nz, const double* a, const double* b) {
   return sum_prod(ny, nx, nz, a, b);
 }
@@ -625,6 +627,8 @@ int orc_cg(int ny, int nx, int nz, const double* K, const double* diag, double s
 
 /* ------------------------------------------------------- reference params */
 
+/* The reference's parameters and literal values (SBMES:90-136), REAL(4)
+ * literals promoted as Fortran does. */
 int orc_params_reference(sbm_params* p) {
   if (!p) return SBM_ERR_ARG;
   memset(p, 0, sizeof(*p));
@@ -1032,6 +1036,9 @@ int orc_voltage_step(orc_state* s, double dt, double vsr, sbm_scalars* sc) {
   return SBM_OK;
 }
 
+/* One pass of the reference's time loop body, DO WHILE (Xrf < 0.971)
+ * (SBMES:357-877): Cahn-Hilliard, the CnE solve, the Butler-Volmer Picard
+ * loop with the phP / phE solves, and the voltage control. */
 int orc_time_step(orc_state* s, int iter, double dt, double vsr, sbm_scalars* sc) {
   sbm_scalars tmp;
   memset(&tmp, 0, sizeof(tmp));
