@@ -172,10 +172,14 @@ int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p);
 #define SBM_TUNE_NO_TMA 1
 #define SBM_TUNE_PC_ADDITIVE 2
 int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta, int flags);
-/* The context's CUDA stream as an opaque handle (cudaStream_t). */
+/* The context's CUDA stream as an opaque handle (cudaStream_t), and a wait
+ * for everything enqueued on it (no counterpart in the reference: its work
+ * is synchronous). */
 int sbm_ctx_stream(sbm_ctx* ctx, void** stream);
 int sbm_ctx_sync(sbm_ctx* ctx);
-/* The context's parameters and electrochemical scalars (host copies). */
+/* The context's parameters (the reference's parameter block, SBMES:90-136)
+ * and electrochemical scalars (tPP, tPE, Xrf, the current and the boundary
+ * potential of the reference's time loop, SBMES:357-877), host copies. */
 int sbm_ctx_get_params(const sbm_ctx* ctx, sbm_params* p);
 int sbm_ctx_get_scalars(const sbm_ctx* ctx, sbm_scalars* s);
 
@@ -402,8 +406,11 @@ int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const uint16_t* x
 /* ---- Learned coarse-grid preconditioner (no counterpart in the reference).
  *
  * A 3D U-Net on the grid coarsened 4x per axis proposes the smooth part of
- * the error: z = D^-1 r + P e_c with e_c = (s k_out / (scale c_ref)) N(f),
- * R = 4x4x4 average, P = cell-centred trilinear interpolation, s = RMS(R r),
+ * the error, z1 = P e_c with e_c = (s k_out / (scale c_ref)) N(f), followed
+ * by one over-relaxed Jacobi step on the residual it leaves:
+ * z = z1 + 2.3 D^-1 (r - A z1) (the default; z = D^-1 r + z1 with
+ * SBM_TUNE_PC_ADDITIVE), R = 4x4x4 average, P = cell-centred trilinear
+ * interpolation, s = RMS(R r),
  * c_ref = mean(R K); the input channels f (16 per coarse cell, voxel
  * v = i + ny*(j + nx*k)) are [R r / s, R K / c_ref, 1, x0-face Dirichlet
  * mask, x1-face Dirichlet mask, 0 x 11].  Because z is not linear in r the
