@@ -50,9 +50,6 @@ sys.path.insert(0, str(ROOT))
 N = 256
 SEED = 1
 TOL = 1e-8
-# FP64 CG iterations to rel-res 1e-8 on this workload: the oracle (plain
-# FP64 CG in C) and the GPU FP64 CG both stop at 2038.
-FP64_ITERS = 2038
 METRIC = "sbm_potential_solve_time_256^3_relres_1e-8"
 # dram__bytes_read.sum + dram__bytes_write.sum of one k32t_apply_dir launch
 # at 256^3 (ncu): with the Jacobi read (Jacobi-PCG) and without it (flexible
@@ -190,23 +187,53 @@ def unet_flops(n):
 
 # --------------------------------------------------------------- CPU side
 
-def cpu_sample(prob, budget_s: float):
-    """Oracle FP64 CG on the host cores for a bounded number of iterations,
-    extrapolated to the FP64 iteration count; returns (seconds, info)."""
+def _orc_threads(n):
+    from oracle import sbm_oracle as orc
+    orc.lib().orc_set_num_threads(n)
+    return orc.lib().orc_num_threads()
+
+
+def oracle_solve(prob, threads=0, tol=TOL, max_it=200000):
+    """The reference's plain FP64 CG (the oracle's C restatement) run to
+    convergence on `threads` host threads (0: all); returns (seconds, x,
+    info).  Concentration problems carry their diagonal and scale."""
     from oracle import sbm_oracle as orc
     from elsim_gb300 import sbm
-    threads = orc.lib().orc_num_threads()
-    t = time.perf_counter()
-    orc.cg(prob["coef"], prob["rhs"], prob["x"], 1.0, sbm.BC_ZERO, sbm.BC_ZERO, sbm.STOP_REL_RES,
-           TOL, 5)
-    per = (time.perf_counter() - t) / 5
-    iters = int(max(5, min(FP64_ITERS, budget_s / max(per, 1e-6))))
-    t = time.perf_counter()
-    _, info = orc.cg(prob["coef"], prob["rhs"], prob["x"], 1.0, sbm.BC_ZERO, sbm.BC_ZERO,
-                     sbm.STOP_REL_RES, TOL, iters)
-    el = time.perf_counter() - t
-    return el / info["iters"] * FP64_ITERS, {"iters": info["iters"], "seconds": el,
-                                              "threads": threads}
+    used = _orc_threads(threads)
+    try:
+        bc = sbm.BC_COPY if "diag" in prob else sbm.BC_ZERO
+        t = time.perf_counter()
+        x, info = orc.cg(prob["coef"], prob["rhs"], prob["x"], prob.get("scale", 1.0), bc, bc,
+                         sbm.STOP_REL_RES, tol, max_it, diag=prob.get("diag"))
+        el = time.perf_counter() - t
+    finally:
+        _orc_threads(0)
+    info["threads"] = used
+    return el, x, info
+
+
+def oracle_rate(prob, budget_s: float, full_iters: int, threads=0):
+    """Oracle FP64 CG on `threads` host threads (0: all) for a bounded number
+    of iterations (about budget_s seconds), scaled to `full_iters`, the
+    iteration count a full solve of the same problem took (measured, not
+    assumed); returns (seconds for the full solve, info)."""
+    from oracle import sbm_oracle as orc
+    from elsim_gb300 import sbm
+    used = _orc_threads(threads)
+    try:
+        t = time.perf_counter()
+        orc.cg(prob["coef"], prob["rhs"], prob["x"], 1.0, sbm.BC_ZERO, sbm.BC_ZERO,
+               sbm.STOP_REL_RES, 0.0, 3)
+        per = (time.perf_counter() - t) / 3
+        iters = int(max(3, min(full_iters, budget_s / max(per, 1e-6))))
+        t = time.perf_counter()
+        _, info = orc.cg(prob["coef"], prob["rhs"], prob["x"], 1.0, sbm.BC_ZERO, sbm.BC_ZERO,
+                         sbm.STOP_REL_RES, 0.0, iters)
+        el = time.perf_counter() - t
+    finally:
+        _orc_threads(0)
+    return el / info["iters"] * full_iters, {"iters": info["iters"], "seconds": el,
+                                              "threads": used, "full_iters": full_iters}
 
 
 def run_reference(args):
@@ -218,26 +245,32 @@ def run_reference(args):
     n = args.size
     m = synth.microstructure((n, n, n), seed=SEED, tunnel=True, redist=orc.redist)
     prob = synth.potential_problem(m["psi"])
-    budget = 8.0
+    # one full solve first: it fixes the iteration count each bounded step
+    # is scaled to, and its own time is reported beside the steps
+    t_full, _, full = oracle_solve(prob)
+    budget = 4.0
     for _ in range(args.warmup):
-        cpu_sample(prob, budget / 4)
+        oracle_rate(prob, budget / 4, full["iters"])
     vals, infos = [], []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, info = cpu_sample(prob, budget)
+        v, info = oracle_rate(prob, budget, full["iters"])
         vals.append(v)
         infos.append(info)
     wall = time.perf_counter() - t0
     value = statistics.mean(vals)
     threads = infos[0]["threads"]
     sample = (f"{infos[0]['iters']} FP64 CG iterations of the {n}^3 solve per step on {threads} "
-              f"OpenMP threads (oracle port of the reference CG), extrapolated x{FP64_ITERS}/"
-              f"{infos[0]['iters']} to the full solve")
+              f"OpenMP threads (oracle port of the reference CG), scaled to the {full['iters']} "
+              f"iterations of a full oracle solve of the same problem measured in this run "
+              f"({t_full:.2f} s)")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded spheres + tunnel; reference inputs are not public)",
             "impl": "reference", "config": _config(n),
+            "full_solve": {"s": t_full, "iterations": full["iters"], "threads": threads,
+                           "final_rel_res": full["final_res"]},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -247,6 +280,152 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------- GPU side
+
+def concentration_solves(ctx, conc, pc, flush, reps=3):
+    """The CnE-form concentration system (psE c - s div(psE grad c) = psE
+    c_old, Neumann) of the headline microstructure on the same context:
+    mixed-precision solves to rel-res TOL after one warm-up; returns (info,
+    interior solution)."""
+    import torch
+    from elsim_gb300 import sbm
+    for k in ("coef", "x", "rhs", "weight", "diag"):
+        ctx.upload(k, conc[k])
+
+    def solve():
+        ctx.upload("x", conc["x"])
+        flush.zero_()
+        torch.cuda.synchronize()
+        return ctx.cg_solve(op=sbm.OP_GENERIC_DIAG, bc_x0=sbm.BC_COPY, bc_x1=sbm.BC_COPY,
+                            scale=conc["scale"], tol=TOL, max_it=200000,
+                            stop_rule=sbm.STOP_REL_RES, precision=sbm.PREC_MIXED, precond=pc)
+
+    solve()
+    runs = [solve() for _ in range(reps)]
+    x = ctx.download("x")[1:-1, 1:-1, 1:-1].copy()
+    info = {"s": statistics.mean(r["ms"] for r in runs) / 1e3, "iterations": runs[-1]["iters"],
+            "preconditioner": {0: "none", 1: "jacobi", 2: "learned"}.get(ctx.last_precond(), "?")}
+    return info, x
+
+
+def side_c1(net=None):
+    """The plain 64^3 potential solve (spheres r ~ U[4,10], solid 0.6, 175
+    reinitialisation steps, Dirichlet 0/1 on the x faces): GPU FP64 CG and
+    the production mixed solve against the oracle's FP64 CG on all host
+    threads and on one."""
+    from elsim_gb300 import sbm, synth
+    n1 = 64
+    m1 = synth.microstructure((n1, n1, n1), seed=SEED)
+    p1 = synth.potential_problem(m1["psi"])
+    out = {"grid": [n1, n1, n1], "seed": SEED}
+    with sbm.Context(n1, n1, n1) as c:
+        for k in ("coef", "x", "rhs", "weight"):
+            c.upload(k, p1[k])
+
+        def sv(prec, pc):
+            c.upload("x", p1["x"])
+            return c.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO,
+                              scale=1.0, tol=TOL, max_it=200000, stop_rule=sbm.STOP_REL_RES,
+                              precision=prec, precond=pc)
+
+        sv(sbm.PREC_FP64, sbm.PC_NONE)
+        g64 = [sv(sbm.PREC_FP64, sbm.PC_NONE) for _ in range(3)]
+        x_g = c.download("x")[1:-1, 1:-1, 1:-1].copy()
+        x_l = None
+        if net is not None:
+            c.set_net(net)
+            sv(sbm.PREC_MIXED, sbm.PC_LEARNED)
+            gl = [sv(sbm.PREC_MIXED, sbm.PC_LEARNED) for _ in range(3)]
+            x_l = c.download("x")[1:-1, 1:-1, 1:-1].copy()
+            out["gpu_mixed_learned_s"] = statistics.mean(r["ms"] for r in gl) / 1e3
+            out["gpu_mixed_learned_iterations"] = gl[-1]["iters"]
+            out["gpu_mixed_learned_preconditioner"] = c.last_precond()
+    t_all, xo, io = oracle_solve(p1)
+    t_one, _, io1 = oracle_solve(p1, threads=1)
+    xo = xo[1:-1, 1:-1, 1:-1]
+    out.update({"gpu_fp64_cg_s": statistics.mean(r["ms"] for r in g64) / 1e3,
+                "gpu_fp64_cg_iterations": g64[-1]["iters"],
+                "cpu_fp64_cg_s": t_all, "cpu_threads": io["threads"],
+                "cpu_fp64_cg_single_thread_s": t_one,
+                "oracle_iterations": io["iters"],
+                "relL2_fp64_cg_vs_oracle": float(np.linalg.norm(x_g - xo) / np.linalg.norm(xo))})
+    if x_l is not None:
+        out["relL2_mixed_learned_vs_oracle"] = float(np.linalg.norm(x_l - xo) / np.linalg.norm(xo))
+    return out
+
+
+def side_c2():
+    """One full electrochemical time step at 128^3 (double-well
+    Cahn-Hilliard, linearised Butler-Volmer, 20 reinitialisation steps): the
+    GPU's device time for steps 2 and 3 of a run (step 1 skips the CnE
+    solve) against the oracle's step 2 on all host threads and step 3 on one,
+    and the GPU's fields after two steps against the oracle's."""
+    import torch
+    from elsim_gb300 import sbm, synth
+    from oracle import sbm_oracle as orc
+    shape = (128, 128, 128)
+    p = synth.full_step_params(orc.params_reference())
+    m2 = synth.microstructure(shape, seed=SEED, reinit_steps=20)
+    d = m2["dist"][1:-1, 1:-1, 1:-1]
+    dp, de = d.astype(np.float32), (-d).astype(np.float32)
+    c0 = synth.full_step_concentration(shape, SEED)
+    dt = synth.FULL_STEP_DT
+    out = {"grid": list(shape), "seed": SEED}
+    with sbm.Context(*shape, params=p) as ctx:
+        s0 = ctx.setup_domain(dp, de)
+        ctx.upload(sbm.F_CNP, c0)
+        init = ctx.snapshot()
+        vsr = synth.step_schedule(s0["xrf"], 0.0, s0["trgI"])[1]
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        t2, t3 = [], []
+        for rep in range(3):
+            ctx.restore(init)
+            ctx.time_step(1, dt, vsr)
+            for it, acc in ((2, t2), (3, t3)):
+                if it == 3 and rep == 2:
+                    fields = {f: ctx.download(f) for f in (sbm.F_CNP, sbm.F_CNE, sbm.F_PHP,
+                                                           sbm.F_PHE)}
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                sc = ctx.time_step(it, dt, vsr)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                acc.append(e0.elapsed_time(e1) / 1e3)
+                if it == 2:
+                    s2 = sc
+    st = orc.State(*shape, p)
+    st.setup_domain(dp, de)
+    st.set_field(sbm.F_CNP, c0)
+    t = time.perf_counter()
+    st.time_step(1, dt, vsr)
+    t_o1 = time.perf_counter() - t
+    t = time.perf_counter()
+    so2 = st.time_step(2, dt, vsr)
+    t_o2 = time.perf_counter() - t
+    werr = {}
+    for name, f, w in (("CnP", sbm.F_CNP, sbm.F_PSP), ("CnE", sbm.F_CNE, sbm.F_PSE),
+                       ("phP", sbm.F_PHP, sbm.F_PSP), ("phE", sbm.F_PHE, sbm.F_PSE)):
+        a, b = fields[f][1:-1, 1:-1, 1:-1], st.field(f)[1:-1, 1:-1, 1:-1]
+        ww = st.field(w)[1:-1, 1:-1, 1:-1]
+        werr[name] = float(np.sqrt((ww * (a - b) ** 2).sum() / max((ww * b * b).sum(), 1e-300)))
+    threads = _orc_threads(1)
+    try:
+        t = time.perf_counter()
+        st.time_step(3, dt, vsr)
+        t_o3 = time.perf_counter() - t
+    finally:
+        _orc_threads(0)
+    st.close()
+    out.update({"gpu_step2_s": statistics.mean(t2), "gpu_step3_s": statistics.mean(t3),
+                "cpu_step1_s": t_o1, "cpu_step2_s": t_o2,
+                "cpu_threads": orc.lib().orc_num_threads(),
+                "cpu_step3_single_thread_s": t_o3, "single_thread_check": threads,
+                "weighted_rel_err_vs_oracle_after_2_steps": werr,
+                "xrf_after_2_steps": {"gpu": s2["xrf"], "oracle": so2["xrf"]},
+                "cg_iterations_step2": {"gpu": s2["it_cne"] + s2["it_php"] + s2["it_phe"],
+                                        "oracle": so2["it_cne"] + so2["it_php"] + so2["it_phe"]}})
+    return out
+
 
 def run_ours(args):
     import torch
@@ -286,6 +465,7 @@ def run_ours(args):
                             precond=pc)
 
     head_pc = sbm.PC_LEARNED if args.pc == "learned" else sbm.PC_JACOBI
+    net = None
     if head_pc == sbm.PC_LEARNED:
         from elsim_gb300 import learned
         net = learned.load()
@@ -412,12 +592,45 @@ def run_ours(args):
     # and every sample stay in the line
     e2e_v = _max_over_ranks(statistics.median(e2e), ws, dev)
     cpu = None
+    parity = {}
+    side = {}
     if rank == 0 and ws == 1:
-        cv, ci = cpu_sample(prob, 12.0)
-        cpu = {"value": cv, "unit": UNIT, "cores": ci["threads"], "kind": "port",
-               "sample": f"{ci['iters']} oracle FP64 CG iterations of the same {n}^3 solve "
-                         f"({ci['seconds']:.1f} s on {ci['threads']} threads), extrapolated "
-                         f"x{FP64_ITERS}/{ci['iters']}"}
+        # the concentration system of the same microstructure (CnE form)
+        conc = synth.concentration_problem(m["psi"], SEED)
+        cinfo, xc = concentration_solves(ctx, conc, head_pc, flush)
+        # CPU legs: the reference's plain FP64 CG (oracle restatement) run to
+        # convergence on all host threads -- its time is the like-for-like
+        # baseline and its solution the parity reference -- and a bounded
+        # single-thread sample scaled to the iteration count it measured
+        t_full, xo, io = oracle_solve(prob)
+        t_one, i_one = oracle_rate(prob, 10.0, io["iters"], threads=1)
+        cpu = {"value": t_full, "unit": UNIT, "cores": io["threads"], "kind": "port",
+               "sample": f"the whole {n}^3 solve: oracle FP64 CG (the reference's "
+                         f"algorithm) to rel-res {TOL:g}, {io['iters']} iterations on "
+                         f"{io['threads']} OpenMP threads",
+               "iterations": io["iters"],
+               "single_thread": {"value": t_one, "unit": UNIT, "cores": 1,
+                                 "sample": f"{i_one['iters']} iterations on 1 thread "
+                                           f"({i_one['seconds']:.1f} s), scaled to the "
+                                           f"{io['iters']} iterations of the full solve"}}
+        xo_i = xo[1:-1, 1:-1, 1:-1]
+        t_oc, xoc, ioc = oracle_solve(conc)
+        xoc_i = xoc[1:-1, 1:-1, 1:-1]
+        parity = {
+            "relL2_phi_vs_oracle": float(np.linalg.norm(xm - xo_i) / np.linalg.norm(xo_i)),
+            "relL2_fp64_cg_vs_oracle": float(np.linalg.norm(x64 - xo_i) / np.linalg.norm(xo_i)),
+            "oracle_iterations": io["iters"],
+            "relL2_c_vs_oracle": float(np.linalg.norm(xc - xoc_i) / np.linalg.norm(xoc_i)),
+            "concentration": {**cinfo, "oracle_s": t_oc, "oracle_iterations": ioc["iters"]},
+            "like_for_like": {
+                "what": "plain FP64 CG on the GPU (the drop-in) vs the same algorithm on the "
+                        "host cores (oracle, all threads)",
+                "gpu_fp64_cg_s": fp64["ms"] / 1e3, "cpu_fp64_cg_s": t_full,
+                "speedup": t_full / (fp64["ms"] / 1e3)},
+            "headline_vs_cpu_fp64_cg": t_full / value,
+        }
+        side = {"c1_plain_cg_64": side_c1(net if head_pc == sbm.PC_LEARNED else None),
+                "c2_full_step_128": side_c2()}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -449,6 +662,8 @@ def run_ours(args):
                 "fp64_stencil_kernel": {"ms": fp64_ms[0],
                                         "GB/s": fp64_ms[1] / (fp64_ms[0] * 1e-3) / 1e9,
                                         "bound": "fp64 alu"},
+                **parity,
+                **side,
             }),
             "roofline": roofline or apply_roofline,
             "cpu_baseline": cpu,

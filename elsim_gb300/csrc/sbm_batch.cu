@@ -12,6 +12,7 @@
 // least one iteration) the volume is marked as having hit the iteration cap.
 // No counterpart in the reference, which solves one domain per MPI job.
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -34,6 +35,9 @@ struct BatchCache {
   int nvol = 0;
 };
 BatchCache g_batch;
+// Batch calls from several host threads take turns: the cached parent graph
+// and its round counters are shared by every call.
+std::mutex g_batch_mu;
 
 // Sets the WHILE condition of one volume: another round while the solve is
 // not done and fewer than `cap` rounds ran (init: before the first round).
@@ -76,6 +80,7 @@ extern "C" int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bc
         (bcx0[v] != SBM_BC_COPY && bcx0[v] != SBM_BC_ZERO) ||
         (bcx1[v] != SBM_BC_COPY && bcx1[v] != SBM_BC_ZERO))
       return SBM_ERR_ARG;
+  std::lock_guard<std::mutex> batch_lock(g_batch_mu);
   std::vector<SolveSpec> specs(n);
   std::vector<cudaGraph_t> graphs(n);
   std::vector<int> vnodes((size_t)n, 0);

@@ -526,6 +526,8 @@ __global__ void __launch_bounds__(NTHR) k_wgrad_tc(WgradArgs a) {
   const int nsteps = (int)((v1 - v0 + KS - 1) / KS);
   const int g = tid >> 3, rr = tid & 7;
   bool ok = true;
+  int ncommitted = 0;      // steps whose MMAs thread 0 committed to bar[step % NSTG]
+  bool done_commit = false;  // the final commit to bar[NSTG] was issued
   for (int step = 0; step < nsteps; ++step) {
     const int s = step % NSTG;
     if (step >= NSTG) ok = ok && mb_wait(&bar[s], (unsigned)(((step - NSTG) / NSTG) & 1));
@@ -573,9 +575,13 @@ __global__ void __launch_bounds__(NTHR) k_wgrad_tc(WgradArgs a) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       tc_mma(tmem, umma_desc(sa(A), 128, 256), umma_desc(sa(B), 128, 256), id, step > 0 ? 1u : 0u);
       tc_commit(&bar[s]);
+      ncommitted = step + 1;
     }
   }
-  if (ok && tid == 0 && nsteps > 0) tc_commit(&bar[NSTG]);
+  if (ok && tid == 0 && nsteps > 0) {
+    tc_commit(&bar[NSTG]);
+    done_commit = true;
+  }
   ok = __syncthreads_and(ok) && (nsteps == 0 || mb_wait(&bar[NSTG], 0));
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -592,10 +598,15 @@ __global__ void __launch_bounds__(NTHR) k_wgrad_tc(WgradArgs a) {
     }
   } else if (!ok && tid == 0) {
     atomicExch(a.err, 1);
-    for (int s = 0; s < NSTG; ++s) {
-      for (unsigned n = 0; n < kSpinTc && !mb_try(&bar[s], 0) && !mb_try(&bar[s], 1); ++n) {
-      }
+    // Bounded drain before the tensor memory is freed: a stage's commits
+    // complete in order, and the loop waited for every commit but the last
+    // of each stage, so wait for that last phase of each stage, then for the
+    // final commit if it was issued.
+    for (int s = 0; s < NSTG && s < ncommitted; ++s) {
+      const int last = s + ((ncommitted - 1 - s) / NSTG) * NSTG;
+      mb_wait(&bar[s], (unsigned)((last / NSTG) & 1));
     }
+    if (done_commit) mb_wait(&bar[NSTG], 0);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();

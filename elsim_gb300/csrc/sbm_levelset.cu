@@ -284,8 +284,10 @@ int redist_dev(cudaStream_t s, const Geo& g, const double* sg, double* f, double
     b = t;
   }
   SBM_LAUNCHED(lit);
-  if (a != f) SBM_CUDA_TRY(cudaMemcpyAsync(f, a, sizeof(double) * g.nh, cudaMemcpyDeviceToDevice, s));
+  // a launch that failed leaves the ping-pong buffer stale: report it before
+  // anything is copied back into f
   SBM_CUDA_TRY(cudaGetLastError());
+  if (a != f) SBM_CUDA_TRY(cudaMemcpyAsync(f, a, sizeof(double) * g.nh, cudaMemcpyDeviceToDevice, s));
   return SBM_OK;
 }
 
@@ -303,8 +305,8 @@ int allen_cahn_dev(cudaStream_t s, const Geo& g, double* f, double* tmp, int ite
     b = t;
   }
   SBM_LAUNCHED(iters > 0 ? iters : 1);
-  if (a != f) SBM_CUDA_TRY(cudaMemcpyAsync(f, a, sizeof(double) * g.nh, cudaMemcpyDeviceToDevice, s));
   SBM_CUDA_TRY(cudaGetLastError());
+  if (a != f) SBM_CUDA_TRY(cudaMemcpyAsync(f, a, sizeof(double) * g.nh, cudaMemcpyDeviceToDevice, s));
   return SBM_OK;
 }
 
@@ -489,7 +491,8 @@ int sign_dev(cudaStream_t s, int64_t n, const double* ds, double thr, double* sg
 // ping-pong field of the Jacobi sweep -- is the fixed array below: every GPU
 // that loads this library holds it (SBM_NOALLOC_REDIST_MAX_CELLS doubles,
 // 8 MiB) until the process exits.  All calls share it: two calls whose work
-// overlaps on the GPU (different streams or host threads) race on it.  The
+// overlaps on the GPU (different streams or host threads) race on it.  A call
+// waits for its stream to finish the iterations before it returns.  The
 // sweep writes every cell of the scratch before reading it, so the contents
 // a previous call left behind never matter and nothing is cleared.
 
@@ -531,13 +534,18 @@ int redist_scratch(double** out) {
 extern "C" int sbm_redist_noalloc(int lit, int py, int px, int pz, double dt, const double* sg,
                                   double* f, void* stream) {
   if (lit < 0 || py < 1 || px < 1 || pz < 1 || !sg || !f) return SBM_ERR_ARG;
-  const int64_t cells = (int64_t)(py + 2) * (px + 2) * (pz + 2);
+  const int64_t cells = ((int64_t)py + 2) * ((int64_t)px + 2) * ((int64_t)pz + 2);
   if (cells > SBM_NOALLOC_REDIST_MAX_CELLS) {
     char msg[160];
     snprintf(msg, sizeof(msg),
              "sbm_redist_noalloc: %lld padded cells exceed the %d-cell built-in scratch",
              (long long)cells, SBM_NOALLOC_REDIST_MAX_CELLS);
     sbm::set_error_msg(msg);
+    return SBM_ERR_ARG;
+  }
+  // one grid plane of CTAs per padded z plane: the grid's z extent is 65535
+  if ((int64_t)pz + 2 > 65535) {
+    sbm::set_error_msg("sbm_redist_noalloc: pz + 2 exceeds 65535 z planes");
     return SBM_ERR_ARG;
   }
   double* scratch = nullptr;

@@ -44,6 +44,13 @@ constexpr int NS = 6;                // stages in the ring
 constexpr int ZCT = 16;              // z planes per CTA
 constexpr unsigned kSpin = 1u << 20;  // try_wait attempts before giving up (about a second)
 
+// Attempts of the consumer-side waits (the planes the CTA computes on).  The
+// default is kSpin; sbm_set_wait_limit lowers it so that a test can make the
+// waits run out without any fault: with 0 every consumer wait gives up at
+// once.  The drain of an expired CTA always keeps the full kSpin bound, so
+// no copy is still landing in shared memory when the CTA exits.
+__device__ unsigned g_wait_tries = kSpin;
+
 struct TmaMaps {
   CUtensorMap r, p, hk, iv, dg;
 };
@@ -73,8 +80,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
   return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity) {
-  for (unsigned n = 0; n < kSpin; ++n)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity, unsigned tries) {
+  for (unsigned n = 0; n < tries; ++n)
     if (mbar_try_wait(b, parity)) return true;
   return false;
 }
@@ -130,8 +137,10 @@ __global__ void __launch_bounds__(NTH)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
+  int n_issued = 0;  // planes 0 .. n_issued-1 have been issued (thread 0)
   auto issue = [&](int m) {
     const int s = m % NS;
+    n_issued = m + 1;
     const int z = k0 - 1 + m;
     mbar_expect_tx(&bar[s], NA * PLANE_BYTES);
     tma_load_3d(stage(s, 0), &maps.r, x0, y0, z, &bar[s]);
@@ -143,7 +152,10 @@ __global__ void __launch_bounds__(NTH)
   if (tid == 0) {
     for (int m = 0; m < NS && m < nplanes; ++m) issue(m);
   }
-  auto wait_plane = [&](int m) { return mbar_wait_bounded(&bar[m % NS], (unsigned)((m / NS) & 1)); };
+  const unsigned tries = g_wait_tries;
+  auto wait_plane = [&](int m) {
+    return mbar_wait_bounded(&bar[m % NS], (unsigned)((m / NS) & 1), tries);
+  };
   // p_new = z + beta p_old for every staged cell of plane m, written over
   // p_old in place (stage array 1)
   auto make_pn = [&](int m) {
@@ -245,10 +257,12 @@ __global__ void __launch_bounds__(NTH)
   if (failed) {
     if (tid == 0) {
       st->done = 5;
-      for (int s = 0; s < NS; ++s) {
-        for (unsigned n = 0; n < kSpin && !mbar_try_wait(&bar[s], 0) && !mbar_try_wait(&bar[s], 1);
-             ++n) {
-        }
+      // Planes land in issue order per stage, and a stage is refilled only
+      // after every thread waited for its previous plane, so each stage has
+      // at most its last issued plane outstanding: wait for that phase.
+      for (int s = 0; s < NS && s < n_issued; ++s) {
+        const int last = s + ((n_issued - 1 - s) / NS) * NS;
+        mbar_wait_bounded(&bar[s], (unsigned)((last / NS) & 1), kSpin);
       }
     }
     __syncthreads();
@@ -406,3 +420,14 @@ void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* p
 }
 
 }  // namespace sbm
+
+// Test hook of the bounded waits (no counterpart in the reference): sets how
+// many times the consumer-side mbarrier waits of the TMA-staged stencil
+// kernel try before giving up, on the current device; tries < 0 restores the
+// built-in bound.  With 0 every launch of the kernel records SBM_ERR_TIMEOUT
+// without touching its outputs; its CTAs still wait out their own copies.
+extern "C" int sbm_set_wait_limit(int tries) {
+  const unsigned v = tries < 0 ? sbm::kSpin : (unsigned)tries;
+  SBM_CUDA_TRY(cudaMemcpyToSymbol(sbm::g_wait_tries, &v, sizeof(v)));
+  return SBM_OK;
+}

@@ -165,6 +165,7 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
                                    [C.c_void_p] * 4),
         "sbm_redist_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
+        "sbm_set_wait_limit": (C.c_int, [C.c_int]),
         "sbm_rm_mask": (C.c_int, [i64, dp, dp, dp]),
         "sbm_sign": (C.c_int, [i64, dp, C.c_double, dp]),
         "sbm_net_param_count": (i64, []),
@@ -235,7 +236,9 @@ CKPT_MAGIC = b"SBMCKPT1"
 def write_checkpoint(path, blob, meta: dict) -> Path:
     """Checkpoint file: 8-byte magic, u64 length of the JSON meta, the meta,
     zero padding to a multiple of 64 bytes, the snapshot bytes.  Written to a
-    temporary name and renamed, so a crash leaves the previous file whole."""
+    temporary name, flushed to stable storage (fsync of the file, then of its
+    directory after the rename), so a process crash or a power loss leaves
+    either the previous file or the new one whole."""
     path = Path(path)
     js = json.dumps(meta, sort_keys=True).encode()
     head = CKPT_MAGIC + np.uint64(len(js)).astype("<u8").tobytes() + js
@@ -244,7 +247,19 @@ def write_checkpoint(path, blob, meta: dict) -> Path:
     with open(tmp, "wb") as f:
         f.write(head)
         f.write(memoryview(np.ascontiguousarray(blob, dtype=np.uint8)))
+        f.flush()
+        os.fsync(f.fileno())
     os.replace(tmp, path)
+    try:
+        dfd = os.open(path.parent if str(path.parent) else ".", os.O_RDONLY)
+    except OSError:
+        return path  # a directory that cannot be opened for reading
+    try:
+        os.fsync(dfd)
+    except OSError:
+        pass  # file systems that do not sync directories
+    finally:
+        os.close(dfd)
     return path
 
 

@@ -250,8 +250,10 @@ int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
  * time of the whole batch.  precond SBM_PC_LEARNED applies per volume (its
  * own attached network and grid permitting, else Jacobi;
  * sbm_ctx_last_precond of each context).  The library caches the parent
- * graph of the last batch (rebuilt when the set of volumes changes), so
- * batch calls must not overlap: one host thread at a time. */
+ * graph of the last batch (rebuilt when the set of volumes changes); batch
+ * calls from several host threads are serialised by a lock around that
+ * cache, and a context must not be used by another call while its batch
+ * runs. */
 int sbm_batch_solve(sbm_ctx** ctxs, int n, int bc_x0, int bc_x1, double scale, double tol,
                     int max_it, int precond, int* iters, double* final_res, int* status,
                     float* ms_total);
@@ -369,11 +371,13 @@ int sbm_accdiff(int py, int px, int pz, const double* psi, double* cn,
  * whose GPU memory is all owned by another allocator or framework, or one
  * that runs under a fixed memory budget set at start-up.  This variant takes
  * DEVICE pointers sg and f (halo-padded, f in/out), enqueues the lit
- * iterations on `stream` (a cudaStream_t; NULL = the default stream), waits
- * for them, and uses as scratch a fixed array built into the library
- * (SBM_NOALLOC_REDIST_MAX_CELLS doubles, 8 MiB, held on every GPU that loads
- * the library until exit); grids of more padded cells are rejected with
- * SBM_ERR_ARG and a message in sbm_last_error().  It calls no cudaMalloc or cudaFree.  The first call on a
+ * iterations on `stream` (a cudaStream_t; NULL = the default stream) and
+ * blocks the calling thread until that stream has finished them
+ * (cudaStreamSynchronize).  Its scratch is a fixed array built into the
+ * library (SBM_NOALLOC_REDIST_MAX_CELLS doubles, 8 MiB, held on every GPU
+ * that loads the library until exit); grids of more padded cells, or with
+ * pz + 2 > 65535, are rejected with SBM_ERR_ARG and a message in
+ * sbm_last_error().  It calls no cudaMalloc or cudaFree.  The first call on a
  * device looks up the scratch address on that device, so make that first
  * call before any stream capture.  All calls share the scratch: calls that
  * overlap on the GPU race.  Results are bit-identical to sbm_redist. */
@@ -468,6 +472,16 @@ int sbm_ctx_last_precond(const sbm_ctx* ctx);
  * operator of the context's coefficient (halo-padded FP64 r and z). */
 int sbm_learned_pc_apply(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, const double* r,
                          double* z);
+
+/* Test hook of the device-side bounded waits (no counterpart in the
+ * reference): the number of attempts each consumer-side mbarrier wait of
+ * the TMA-staged FP32 stencil kernel makes before the CTA gives up, records
+ * the expiry (the solve returns SBM_ERR_TIMEOUT) and returns after waiting
+ * out its own copies in flight with the full built-in bound.  tries < 0
+ * restores the default (2^20 attempts, about a second); 0 makes every wait
+ * give up at once.  Applies to the current device, for every context; call
+ * it only while no solve runs. */
+int sbm_set_wait_limit(int tries);
 
 /* Version string of the compiled library. */
 const char* sbm_version(void);

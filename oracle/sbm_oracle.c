@@ -32,6 +32,19 @@ int orc_num_threads(void) {
 #endif
 }
 
+/* Threads of the following parallel regions of the calling host thread
+ * (the CPU baseline times one thread and all of them); n <= 0 restores the
+ * count the library started with.  Results do not depend on it. */
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+  static int initial = 0;
+  if (!initial) initial = omp_get_max_threads();
+  omp_set_num_threads(n > 0 ? n : initial);
+#else
+  (void)n;
+#endif
+}
+
 /* --------------------------------------------------------------- ghosts */
 
 /* NoGrdBc3D, LS:164-190 (same as RM:180-205). */

@@ -87,6 +87,7 @@ int  orc_time_step(orc_state* s, int iter, double dt, double vsr, sbm_scalars* s
 
 int  orc_params_reference(sbm_params* p);
 int  orc_num_threads(void);
+void orc_set_num_threads(int n);
 
 #ifdef __cplusplus
 }

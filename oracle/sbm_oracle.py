@@ -61,6 +61,7 @@ def lib() -> C.CDLL:
         "orc_time_step": (i, [vp, i, d, d, C.POINTER(Scalars)]),
         "orc_params_reference": (i, [C.POINTER(Params)]),
         "orc_num_threads": (i, []),
+        "orc_set_num_threads": (None, [i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

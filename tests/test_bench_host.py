@@ -35,6 +35,32 @@ def test_reference_arm_line(built):
     assert e2e["value"] == line["value"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert line["config"]["grid"] == [32, 32, 32]
+    # the iteration count each bounded step is scaled to comes from a full
+    # oracle solve of the same problem in the same run
+    fs = line["full_solve"]
+    assert fs["iterations"] > 0 and fs["s"] > 0 and fs["final_rel_res"] <= 1e-8
+    assert f"{fs['iterations']} iterations of a full oracle solve" in cb["sample"]
+
+
+def test_oracle_thread_count_is_settable_and_restored(built):
+    from oracle import sbm_oracle as orc
+    lib = orc.lib()
+    n0 = lib.orc_num_threads()
+    assert bench._orc_threads(1) == 1
+    assert bench._orc_threads(0) == n0
+
+
+def test_oracle_rate_scales_a_sample_to_the_measured_count(built):
+    from elsim_gb300 import synth
+    from oracle import sbm_oracle as orc
+    m = synth.microstructure((24, 24, 24), seed=3, reinit_steps=20, redist=orc.redist)
+    prob = synth.potential_problem(m["psi"])
+    t_full, x, info = bench.oracle_solve(prob)
+    assert info["status"] == 0 and info["iters"] > 10
+    est, s = bench.oracle_rate(prob, 1e-9, info["iters"], threads=1)
+    # the smallest sample (3 iterations), scaled to the full count
+    assert s["iters"] == 3 and s["full_iters"] == info["iters"] and s["threads"] == 1
+    assert est == pytest.approx(s["seconds"] / 3 * info["iters"])
 
 
 class _Done:

@@ -167,3 +167,30 @@ def test_zero_rhs_zero_boundary_converges_immediately(built):
                             tol=1e-8, max_it=100, stop_rule=sbm.STOP_REL_RES)
         assert info["iters"] == 0 and info["status"] == 0
         assert not ctx.download("x").any()
+
+
+def test_expired_device_wait_reports_timeout_and_the_context_recovers(built):
+    """The TMA-staged stencil kernel's bounded waits: with the consumer-side
+    limit at 0 every wait gives up at once (no fault, no hang: each CTA still
+    waits out its own copies), the solve reports SBM_ERR_TIMEOUT, and after
+    the limit is restored the same context solves normally."""
+    shape = (64, 40, 24)  # ny a multiple of 4: the TMA-staged kernel runs
+    m, prob = _problem(shape, 21)
+    lib = sbm.load_library()
+    kw = dict(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO, scale=1.0, tol=1e-8,
+              max_it=20000, stop_rule=sbm.STOP_REL_RES, precision=sbm.PREC_MIXED,
+              precond=sbm.PC_JACOBI)
+    with sbm.Context(*shape) as ctx:
+        _load(ctx, prob)
+        assert lib.sbm_set_wait_limit(0) == sbm.OK
+        try:
+            with pytest.raises(sbm.SbmError) as exc:
+                ctx.cg_solve(**kw)
+        finally:
+            assert lib.sbm_set_wait_limit(-1) == sbm.OK
+        assert exc.value.code == sbm.ERR_TIMEOUT
+        ctx.upload("x", prob["x"])
+        info = ctx.cg_solve(**kw)
+        x = ctx.download("x")
+    assert info["status"] == 0
+    assert _true_relres(prob, x) <= 1.05e-8

@@ -43,6 +43,18 @@ def test_noalloc_redist_equals_allocating_entry_point_twice(built):
     assert np.array_equal(got2, sbm.redist3d_xyz(20, sg2, f2, dt))
 
 
+def test_noalloc_fills_the_whole_scratch(built):
+    # (126+2)(126+2)(62+2) = 2^20 padded cells: exactly the scratch's size; an
+    # odd iteration count leaves the result in the scratch before the copy back
+    shape = (126, 126, 62)
+    assert (shape[0] + 2) * (shape[1] + 2) * (shape[2] + 2) == 1 << 20
+    sg = synth.sign_field(synth.spheres(shape, seed=4, solid_fraction=0.5, rmin=3, rmax=8))
+    f0 = np.zeros_like(sg)
+    for _ in range(2):
+        got = _noalloc(7, sg, f0, 1.0e-1)
+        assert np.array_equal(got, sbm.redist3d_xyz(7, sg, f0, 1.0e-1))
+
+
 def test_noalloc_rejects_grid_beyond_scratch(built):
     import torch
     lib = sbm.load_library()
@@ -52,4 +64,12 @@ def test_noalloc_rejects_grid_beyond_scratch(built):
     rc = lib.sbm_redist_noalloc(1, n, n, n, 0.1, buf.data_ptr(), buf.data_ptr(), None)
     assert rc == sbm.ERR_ARG
     assert b"scratch" in lib.sbm_last_error()
+    # a thin grid within the cell limit whose z extent the launch grid cannot hold
+    rc = lib.sbm_redist_noalloc(1, 1, 1, 70000, 0.1, buf.data_ptr(), buf.data_ptr(), None)
+    assert rc == sbm.ERR_ARG
+    assert b"65535" in lib.sbm_last_error()
+    # extents whose padded sizes overflow 32-bit arithmetic
+    big = 2 ** 31 - 2
+    rc = lib.sbm_redist_noalloc(1, big, big, big, 0.1, buf.data_ptr(), buf.data_ptr(), None)
+    assert rc == sbm.ERR_ARG
     assert not buf.cpu().numpy().any()
