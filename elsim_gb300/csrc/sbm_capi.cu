@@ -483,10 +483,14 @@ int sbm_ctx_last_precond(const sbm_ctx* ctx) { return ctx ? ctx->last_precond : 
 
 int sbm_learned_pc_apply(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, const double* r,
                          double* z) {
-  if (!ctx || !r || !z) return SBM_ERR_ARG;
+  return sbm_learned_pc_apply_op(ctx, SBM_OP_GENERIC, bc_x0, bc_x1, scale, r, z);
+}
+
+int sbm_learned_pc_apply_op(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale,
+                            const double* r, double* z) {
+  if (!ctx || !r || !z || (op != SBM_OP_GENERIC && op != SBM_OP_GENERIC_DIAG)) return SBM_ERR_ARG;
   SolveSpec sp{};
-  int rc = generic_spec(ctx, SBM_OP_GENERIC, bc_x0, bc_x1, scale, 1e-8, 1, SBM_STOP_REL_RES,
-                        SBM_PREC_MIXED,
+  int rc = generic_spec(ctx, op, bc_x0, bc_x1, scale, 1e-8, 1, SBM_STOP_REL_RES, SBM_PREC_MIXED,
                         SBM_PC_LEARNED, &sp);
   if (rc) return rc;
   return learned_pc_apply(ctx, sp, r, z);

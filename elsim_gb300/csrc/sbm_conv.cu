@@ -362,10 +362,15 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
         float acc[16];
         tc_ld16(lane_base + (uint32_t)(pl * nt + c0), acc);
         const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + pl));
+        // voxels in the zero padding of a padded grid keep zero outputs, as
+        // the zero fill beyond a grid face would present them
+        const bool live =
+            a.vny == 0 || (y < a.vny && x < a.vnx && (zl + pl) < a.vnz);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           float val = acc[q] + (a.bias ? a.bias[n0 + c0 + q] : 0.f);
           if (a.relu) val = fmaxf(val, 0.f);
+          if (!live) val = 0.f;
           o[pl][q] = __float2bfloat16_rn(val);
           acc[q] = val;
           if (a.w1x1) head[pl] += a.w1x1[n0 + c0 + q] * __bfloat162float(o[pl][q]);
@@ -390,14 +395,17 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
           // nearest upsampling: the 8 children in the finer grid
           const int fy = 2 * a.ny, fx = 2 * a.nx;
           for (int ch = 0; ch < 8; ++ch) {
-            const int64_t u = (int64_t)(2 * y + (ch & 1)) +
-                              (int64_t)fy * ((2 * x + ((ch >> 1) & 1)) +
-                                             (int64_t)fx * (2 * (z0 + pl) + (ch >> 2)));
+            const int cy = 2 * y + (ch & 1), cxx = 2 * x + ((ch >> 1) & 1);
+            const int czl = 2 * (zl + pl) + (ch >> 2);
+            const int64_t u = (int64_t)cy +
+                              (int64_t)fy * (cxx + (int64_t)fx * (2 * (z0 + pl) + (ch >> 2)));
             const int cu = a.offu + n0 + c0;
+            const bool ulive = a.uvny == 0 || (cy < a.uvny && cxx < a.uvnx && czl < a.uvnz);
+            const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
             *reinterpret_cast<uint4*>(a.up + act_index(u, cu, 8 * V)) =
-                *reinterpret_cast<const uint4*>(&o[pl][0]);
+                ulive ? *reinterpret_cast<const uint4*>(&o[pl][0]) : zero4;
             *reinterpret_cast<uint4*>(a.up + act_index(u, cu + 8, 8 * V)) =
-                *reinterpret_cast<const uint4*>(&o[pl][8]);
+                ulive ? *reinterpret_cast<const uint4*>(&o[pl][8]) : zero4;
           }
         }
       }

@@ -48,6 +48,10 @@ struct ConvArgs {
                            //    before waiting on the preceding kernel
   // tensor-core kernel only:
   int planes;              // z planes per CTA: 1, or 2 (nzs even)
+  int vny, vnx, vnz;       // valid extents of a zero-padded grid (vnz per sample): outputs
+                           //   of voxels beyond them are stored as 0; vny = 0: all valid
+  int uvny, uvnx, uvnz;    // the same of the 2x finer grid `up` writes (children beyond
+                           //   them receive 0)
   __nv_bfloat16* pool;     // 2x2x2-averaged BF16 output [V/8][cout] (planes 2) or null
   __nv_bfloat16* up;       // BF16 output copied to the 8 children in the 2x finer grid
   int offu;                //   (first channel there) or null

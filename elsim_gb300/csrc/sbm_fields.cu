@@ -555,7 +555,10 @@ static int step_solve(sbm_ctx* ctx, int op, int precision, double cne_scale, int
   if (precision == SBM_PREC_MIXED) {
     sp.stop_rule = SBM_STOP_REL_RES;
     sp.tol = kMixedStepTol;
-    sp.precond = SBM_PC_JACOBI;  // the FP64 path keeps the reference's plain CG
+    // the learned preconditioner where a network is attached and suits the
+    // grid and the operator, else Jacobi (the FP64 path keeps the
+    // reference's plain CG)
+    sp.precond = SBM_PC_LEARNED;
   }
   SolveResult r{};
   int rc = solve(ctx, sp, &r);

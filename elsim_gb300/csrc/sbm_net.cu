@@ -82,6 +82,10 @@ inline Dims half(const Dims& d) { return Dims{d.ny / 2, d.nx / 2, d.nz / 2, d.nz
 
 struct Work {
   Dims d[kLev];
+  // a zero-padded grid: the valid extents per level (voxels beyond them
+  // keep zero activations); vd == d when not padded
+  Dims vd[kLev];
+  bool padded = false;
   bool train = false;
   bf16* in0 = nullptr;
   bf16* cat[4] = {};
@@ -345,6 +349,7 @@ struct sbm_net {
   int* err = nullptr;
   double* loss = nullptr;
   int64_t step = 0;
+  int mass = 0;  // trained with input channel 5 (the CnE form's mass term)
   cudaStream_t stream = nullptr;
   // resident training set (sbm_net_set_data)
   bf16* din = nullptr;     // per-sample channel-group planes
@@ -379,11 +384,17 @@ bool dims_ok(int ny, int nx, int nz) {
   return ny >= 16 && nx >= 16 && nz >= 16 && ny % 16 == 0 && nx % 16 == 0 && nz % 16 == 0;
 }
 
-Work* make_work(const Dims& d0, bool train) {
+Work* make_work(const Dims& d0, bool train, const Dims* valid = nullptr) {
   Work* w = new Work();
   w->train = train;
   w->d[0] = d0;
   for (int l = 1; l < kLev; ++l) w->d[l] = half(w->d[l - 1]);
+  w->padded = valid != nullptr;
+  w->vd[0] = valid ? *valid : d0;
+  for (int l = 1; l < kLev; ++l) {
+    const Dims& u = w->vd[l - 1];
+    w->vd[l] = Dims{(u.ny + 1) / 2, (u.nx + 1) / 2, (u.nz + 1) / 2, (u.nzs + 1) / 2};
+  }
   bool ok = w->alloc(&w->in0, w->d[0].v() * kFeat) && w->alloc(&w->out, w->d[0].v()) &&
             w->alloc(&w->tgt, w->d[0].v()) && w->alloc(&w->a4, w->d[4].v() * kCo[E4]);
   for (int l = 0; l < 4 && ok; ++l)
@@ -456,6 +467,12 @@ ConvArgs layer_args(sbm_net* n, const Work& w, int l, int lev, const bf16* x, in
   // the preconditioner's passes (the only ones with skip flags) run on
   // frozen weights; training rewrites them between passes
   a.wpre = skip != nullptr;
+  if (w.padded) {
+    a.vny = w.vd[lev].ny; a.vnx = w.vd[lev].nx; a.vnz = w.vd[lev].nzs;
+    if (lev > 0) {
+      a.uvny = w.vd[lev - 1].ny; a.uvnx = w.vd[lev - 1].nx; a.uvnz = w.vd[lev - 1].nzs;
+    }
+  }
   return a;
 }
 
@@ -645,49 +662,80 @@ int check_err(sbm_net* n) {
 
 // ------------------------------------------------ solver-side plan
 
-// Coarse-cell means of the coefficient (2 hk) and their mean c_ref; the
-// last block stores c_ref and the output factor k_out / (scale c_ref).
-__global__ void k_pc_coef(Geo g, Dims c, const float* __restrict__ hk, float* __restrict__ coefc,
-                          double* partials, unsigned* counter, float* scal, double kout,
-                          double scale) {
-  double acc = 0.0;
-  NET_LOOP(c.v()) {
+// The coarse grid of a solve: cv = the fine interior / 4 per axis (the
+// valid cells), c = cv rounded up to a multiple of 16 per axis (the grid the
+// U-Net runs on; its extra cells are zero padding).  Coarse arrays use c's
+// strides.
+
+// Coarse-cell means of the coefficient (2 hk) and, for the CnE form, of the
+// diagonal; the last block stores c_ref = mean of the former over the valid
+// cells and the output factor sgn k_out / (scale c_ref).  sgn = -1 for the
+// CnE form, whose operator diag - scale S has the opposite sign of the
+// potential form's scale S, so that the network sees both in one convention.
+__global__ void k_pc_coef(Geo g, Dims c, Dims cv, const float* __restrict__ hk,
+                          const float* __restrict__ dg, float* __restrict__ coefc,
+                          float* __restrict__ massc, double* partials, unsigned* counter,
+                          float* scal, double kout, double scale, double sgn) {
+  double acc = 0.0, accm = 0.0;
+  NET_LOOP(cv.v()) {
     int i, j, k;
-    vox(c, t, &i, &j, &k);
-    float s = 0.f;
+    vox(cv, t, &i, &j, &k);
+    float s = 0.f, sm = 0.f;
     for (int kk = 0; kk < 4; ++kk)
       for (int jj = 0; jj < 4; ++jj) {
-        const float* p = hk + g.ix(4 * i + 1, 4 * j + jj + 1, 4 * k + kk + 1);
-        const float4 v = *reinterpret_cast<const float4*>(p);
+        const int64_t o = g.ix(4 * i + 1, 4 * j + jj + 1, 4 * k + kk + 1);
+        const float4 v = *reinterpret_cast<const float4*>(hk + o);
         s += (v.x + v.y) + (v.z + v.w);
+        if (dg) {
+          const float4 d = *reinterpret_cast<const float4*>(dg + o);
+          sm += (d.x + d.y) + (d.z + d.w);
+        }
       }
     const float m = s * (2.f / 64.f);
-    coefc[t] = m;
+    const int64_t tp = vid(c, i, j, k);
+    coefc[tp] = m;
     acc += m;
+    if (dg) {
+      massc[tp] = sm * (1.f / 64.f);
+      accm += sm * (1.f / 64.f);
+    }
   }
-  double v[1] = {acc}, tot[1];
-  if (grid_reduce<1>(v, partials, counter, tot)) {
+  double v[2] = {acc, accm}, tot[2];
+  if (grid_reduce<2>(v, partials, counter, tot)) {
     if (threadIdx.x == 0) {
-      const double cref = tot[0] / (double)c.v();
+      const double cref = tot[0] / (double)cv.v();
       scal[3] = (float)cref;
-      scal[2] = (float)(kout / (scale * cref));
+      scal[2] = (float)(sgn * kout / (scale * cref));
+      scal[4] = (float)(scale * cref);
+      scal[5] = (float)(tot[1] / (double)cv.v());
     }
   }
 }
 
-// Static input channels 1..15 of the coarse grid.
-__global__ void k_pc_feat(Dims c, const float* __restrict__ coefc, const float* scal, int bcx0,
-                          int bcx1, bf16* __restrict__ in0) {
+// Static input channels 1..15 of the coarse grid: R K / c_ref, 1, the two
+// Dirichlet x-face masks and, for the CnE form (mass), x / (1 + x) with
+// x = R diag / (scale c_ref), the weight of the mass term against the
+// diffusion; zero in the padding.
+__global__ void k_pc_feat(Dims c, Dims cv, const float* __restrict__ coefc,
+                          const float* __restrict__ massc, const float* scal, int bcx0,
+                          int bcx1, int mass, bf16* __restrict__ in0) {
   NET_LOOP(c.v()) {
     int i, j, k;
     vox(c, t, &i, &j, &k);
+    const bool live = i < cv.ny && j < cv.nx && k < cv.nz;
     float f[kFeat];
 #pragma unroll
     for (int q = 0; q < kFeat; ++q) f[q] = 0.f;
-    f[1] = coefc[t] / scal[3];
-    f[2] = 1.f;
-    f[3] = (bcx0 == SBM_BC_ZERO && j == 0) ? 1.f : 0.f;
-    f[4] = (bcx1 == SBM_BC_ZERO && j == c.nx - 1) ? 1.f : 0.f;
+    if (live) {
+      f[1] = coefc[t] / scal[3];
+      f[2] = 1.f;
+      f[3] = (bcx0 == SBM_BC_ZERO && j == 0) ? 1.f : 0.f;
+      f[4] = (bcx1 == SBM_BC_ZERO && j == cv.nx - 1) ? 1.f : 0.f;
+      if (mass) {
+        const float x = massc[t] / scal[4];
+        f[5] = x / (1.f + x);
+      }
+    }
 #pragma unroll
     for (int q = 1; q < kFeat; ++q) in0[act_index(t, q, c.v())] = __float2bfloat16_rn(f[q]);
   }
@@ -695,14 +743,14 @@ __global__ void k_pc_feat(Dims c, const float* __restrict__ coefc, const float* 
 
 // rc = R r (4x4x4 means of the FP32 residual), s = RMS(rc); only when the
 // update kernel has not produced them (first use, residual replacement).
-__global__ void k_pc_restrict(Geo g, Dims c, const float* __restrict__ r, float* __restrict__ rc,
-                              double* partials, float* scal, CgState* st) {
+__global__ void k_pc_restrict(Geo g, Dims c, Dims cv, const float* __restrict__ r,
+                              float* __restrict__ rc, double* partials, float* scal, CgState* st) {
   pdl_begin();
   if (st->done || st->pc_off || st->aux[1] != 0.0) return;
   double acc = 0.0;
-  NET_LOOP(c.v()) {
+  NET_LOOP(cv.v()) {
     int i, j, k;
-    vox(c, t, &i, &j, &k);
+    vox(cv, t, &i, &j, &k);
     float s = 0.f;
     for (int kk = 0; kk < 4; ++kk)
       for (int jj = 0; jj < 4; ++jj) {
@@ -711,13 +759,13 @@ __global__ void k_pc_restrict(Geo g, Dims c, const float* __restrict__ r, float*
         s += (v.x + v.y) + (v.z + v.w);
       }
     const float m = s * (1.f / 64.f);
-    rc[t] = m;
+    rc[vid(c, i, j, k)] = m;
     acc += (double)m * (double)m;
   }
   double v[1] = {acc}, tot[1];
   if (grid_reduce<1>(v, partials, &st->counter[4], tot)) {
     if (threadIdx.x == 0) {
-      const double s = sqrt(tot[0] / (double)c.v());
+      const double s = sqrt(tot[0] / (double)cv.v());
       scal[0] = (float)s;
       scal[1] = s > 0.0 ? (float)(1.0 / s) : 0.f;
     }
@@ -749,7 +797,7 @@ __device__ __forceinline__ void interp1(int fi, int n, int* lo, int* hi, float* 
 // coarse z cell, so the coarse values (3 y x 2 x x 3 z) are loaded once for
 // 16 cells.  With the coarse part switched off (pc_off): z = invd*r.
 __global__ void __launch_bounds__(256)
-    k_pc_prolong(Geo g, Dims c, const float* __restrict__ out, const float* scal,
+    k_pc_prolong(Geo g, Dims c, Dims cv, const float* __restrict__ out, const float* scal,
                  const float* __restrict__ r, const float* __restrict__ iv,
                  const float* __restrict__ q, float* __restrict__ z, const int* err,
                  double* partials, CgState* st) {
@@ -770,9 +818,9 @@ __global__ void __launch_bounds__(256)
       const int kc = (int)(rr / g.nx);
       int x0, x1;
       float wx;
-      interp1(j - 1, c.nx, &x0, &x1, &wx);
-      const int ys[3] = {max(m - 1, 0), m, min(m + 1, c.ny - 1)};
-      const int zs[3] = {max(kc - 1, 0), kc, min(kc + 1, c.nz - 1)};
+      interp1(j - 1, cv.nx, &x0, &x1, &wx);
+      const int ys[3] = {max(m - 1, 0), m, min(m + 1, cv.ny - 1)};
+      const int zs[3] = {max(kc - 1, 0), kc, min(kc + 1, cv.nz - 1)};
       float cx[3][3] = {};  // [y neighbour][z plane], interpolated in x
       if (coarse) {
 #pragma unroll
@@ -844,11 +892,11 @@ constexpr float kPcOmega = SBM_PC_OMEGA;
 constexpr int kMTY = 64, kMTX = 8, kMTZ = 4;
 constexpr int kWY = kMTY / 4 + 2;  // coarse y window
 __global__ void __launch_bounds__(256, 3)
-    k_pc_mult_tiled(Geo g, Dims c, const float* __restrict__ out, const float* scal,
+    k_pc_mult_tiled(Geo g, Dims c, Dims cv, const float* __restrict__ out, const float* scal,
                     const float* __restrict__ r, const float* __restrict__ iv,
-                    const float* __restrict__ q, const float* __restrict__ hk, float scale,
-                    int bcx0, int bcx1, float omega, float* __restrict__ z, const int* err,
-                    double* partials, CgState* st) {
+                    const float* __restrict__ q, const float* __restrict__ hk,
+                    const float* __restrict__ dg, float scale, int bcx0, int bcx1, float omega,
+                    float* __restrict__ z, const int* err, double* partials, CgState* st) {
   __shared__ float sA[3][kMTX / 4 + 2][kWY];
   __shared__ float sB[3][kMTX + 2][kWY];
   __shared__ float sC[kMTZ + 2][kMTX + 2][kWY];
@@ -857,7 +905,7 @@ __global__ void __launch_bounds__(256, 3)
   const bool coarse = st->pc_off == 0;  // off: z = D^-1 r (Jacobi-PCG)
   const float f = coarse ? scal[0] * scal[2] : 0.f;
   const int tid = threadIdx.x;
-  const int nty = g.ny / kMTY, ntx = g.nx / kMTX;
+  const int nty = (g.ny + kMTY - 1) / kMTY, ntx = g.nx / kMTX;  // the last y tile may be partial
   const int64_t ntiles = (int64_t)nty * ntx * (g.nz / kMTZ);
   // per-thread roles of the staging loops: (x, y) column of the windows
   const int col_y = tid % kWY, col_x = tid / kWY;  // col_x < kMTX + 2 for tid < 180
@@ -872,11 +920,11 @@ __global__ void __launch_bounds__(256, 3)
     if (coarse) {
       __syncthreads();  // the previous tile's readers are done
       if (col_x < kMTX / 4 + 2) {
-        const int cy = min(max(cy0 + col_y, 0), c.ny - 1);
-        const int cx = min(max(cx0 + col_x, 0), c.nx - 1);
+        const int cy = min(max(cy0 + col_y, 0), cv.ny - 1);
+        const int cx = min(max(cx0 + col_x, 0), cv.nx - 1);
 #pragma unroll
         for (int zz = 0; zz < 3; ++zz) {
-          const int cz = min(max(cz0 + zz, 0), c.nz - 1);
+          const int cz = min(max(cz0 + zz, 0), cv.nz - 1);
           sA[zz][col_x][col_y] = out[cy + (int64_t)c.ny * (cx + (int64_t)c.nx * cz)];
         }
       }
@@ -884,7 +932,7 @@ __global__ void __launch_bounds__(256, 3)
       if (col_x < kMTX + 2) {  // x interpolation to the fine x positions x0-1 .. x0+kMTX
         int lo, hi;
         float w;
-        interp1(x0 - 2 + col_x, c.nx, &lo, &hi, &w);
+        interp1(x0 - 2 + col_x, cv.nx, &lo, &hi, &w);
 #pragma unroll
         for (int zz = 0; zz < 3; ++zz)
           sB[zz][col_x][col_y] = w * sA[zz][lo - cx0][col_y] + (1.f - w) * sA[zz][hi - cx0][col_y];
@@ -895,7 +943,7 @@ __global__ void __launch_bounds__(256, 3)
         for (int zf = 0; zf < kMTZ + 2; ++zf) {
           int lo, hi;
           float w;
-          interp1(z0 - 2 + zf, c.nz, &lo, &hi, &w);
+          interp1(z0 - 2 + zf, cv.nz, &lo, &hi, &w);
           sC[zf][col_x][col_y] =
               f * (w * sB[lo - cz0][col_x][col_y] + (1.f - w) * sB[hi - cz0][col_x][col_y]);
         }
@@ -907,6 +955,7 @@ __global__ void __launch_bounds__(256, 3)
       const int u = tid + 256 * h;
       const int mq = u % (kMTY / 4), xl = (u / (kMTY / 4)) % kMTX, zl = u / ((kMTY / 4) * kMTX);
       const int i0 = y0 + 4 * mq, j = x0 + xl, k = z0 + zl;
+      if (i0 > g.ny) continue;  // beyond a partial tile (ny is a multiple of 4)
       const int64_t idx = g.ix(i0, j, k);
       const float4 rv = *reinterpret_cast<const float4*>(r + idx);
       const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
@@ -960,13 +1009,19 @@ __global__ void __launch_bounds__(256, 3)
             if (k == g.nz) zp4[y] = pc;
           }
         }
+        float dga[4] = {0.f, 0.f, 0.f, 0.f};
+        if (dg) {  // the CnE form: A p = diag p - scale S(p)
+          const float4 d4 = *reinterpret_cast<const float4*>(dg + idx);
+          dga[0] = d4.x; dga[1] = d4.y; dga[2] = d4.z; dga[3] = d4.w;
+        }
 #pragma unroll
         for (int y = 0; y < 4; ++y) {
           const float pc = cen[y + 1];
           const float sv = face_sum<float>(ky[y + 1], pc, ky[y + 2], cen[y + 2], ky[y], cen[y],
                                            kxb[y], yp[y], kxa[y], ym[y], kzb[y], zp4[y], kza[y],
                                            zm4[y]);
-          za[y] = pc + omega * (da[y] * (ra[y] - scale * sv));
+          const float az = dg ? dga[y] * pc - scale * sv : scale * sv;
+          za[y] = pc + omega * (da[y] * (ra[y] - az));
         }
       } else {
 #pragma unroll
@@ -997,16 +1052,19 @@ __global__ void __launch_bounds__(256, 3)
 struct NetPc {
   sbm_net* net = nullptr;
   double kout = 1.0;
-  Dims c{};
+  Dims c{};   // the U-Net's grid: cv rounded up to multiples of 16 (zero padding)
+  Dims cv{};  // the coarse cells of the solve's grid (fine interior / 4)
   Work* w = nullptr;
   float* rc = nullptr;
   float* coefc = nullptr;
+  float* massc = nullptr;  // coarse means of the CnE diagonal
   float* zf = nullptr;   // FP32 z (g32 layout)
   float* scal = nullptr; // s, 1/s, k_out/(scale c_ref), c_ref
   double* parts = nullptr;
   unsigned* cnt = nullptr;
   // operator of the current solve, for the multiplicative smoothing step
   const float* hk32 = nullptr;
+  const float* dg32 = nullptr;  // the CnE form's diagonal (null: potential form)
   float scale = 1.f;
   int bcx0 = 0, bcx1 = 0;
   void release() {
@@ -1014,11 +1072,12 @@ struct NetPc {
     w = nullptr;
     cudaFree(rc);
     cudaFree(coefc);
+    cudaFree(massc);
     cudaFree(zf);
     cudaFree(scal);
     cudaFree(parts);
     cudaFree(cnt);
-    rc = coefc = zf = scal = nullptr;
+    rc = coefc = massc = zf = scal = nullptr;
     parts = nullptr;
     cnt = nullptr;
   }
@@ -1026,43 +1085,58 @@ struct NetPc {
 
 }  // namespace netd
 
+// The learned preconditioner applies to grids whose extents are multiples
+// of 16 (coarse grids of whole 4^3 blocks, zero-padded to multiples of 16
+// for the U-Net's four poolings), to the potential form, and to the CnE
+// form (diag - scale S) when the network was trained with the mass channel.
 bool net_pc_usable(const sbm_ctx* ctx, int form) {
   const netd::NetPc* pc = static_cast<const netd::NetPc*>(ctx->net);
   const Geo& g = ctx->g;
-  return pc && pc->net && form == 0 && g.ny % 64 == 0 && g.nx % 64 == 0 && g.nz % 64 == 0;
+  return pc && pc->net && (form == 0 || pc->net->mass) && g.ny % 16 == 0 && g.nx % 16 == 0 &&
+         g.nz % 16 == 0;
 }
 
-int net_pc_begin(sbm_ctx* ctx, const float* hk32, double scale, int bcx0, int bcx1,
-                 cudaStream_t s) {
+int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, double scale, int bcx0,
+                 int bcx1, cudaStream_t s) {
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   int rc = conv3_init();
   if (rc) return rc;
   const Geo& g = ctx->g32;
-  const netd::Dims c{g.ny / 4, g.nx / 4, g.nz / 4, g.nz / 4};
-  if (!pc->w || pc->c.ny != c.ny || pc->c.nx != c.nx || pc->c.nz != c.nz) {
+  const netd::Dims cv{g.ny / 4, g.nx / 4, g.nz / 4, g.nz / 4};
+  auto r16 = [](int n) { return (n + 15) / 16 * 16; };
+  const netd::Dims c{r16(cv.ny), r16(cv.nx), r16(cv.nz), r16(cv.nz)};
+  if (!pc->w || pc->cv.ny != cv.ny || pc->cv.nx != cv.nx || pc->cv.nz != cv.nz) {
     pc->release();
     pc->c = c;
-    pc->w = netd::make_work(c, false);
+    pc->cv = cv;
+    pc->w = netd::make_work(c, false, &cv);
     if (!pc->w || cudaMalloc(&pc->rc, sizeof(float) * c.v()) ||
         cudaMalloc(&pc->coefc, sizeof(float) * c.v()) ||
+        cudaMalloc(&pc->massc, sizeof(float) * c.v()) ||
         cudaMalloc(&pc->zf, sizeof(float) * g.nh) || cudaMalloc(&pc->scal, sizeof(float) * 8) ||
-        cudaMalloc(&pc->parts, sizeof(double) * 152 * 16) ||
+        cudaMalloc(&pc->parts, sizeof(double) * 152 * 16 * 2) ||
         cudaMalloc(&pc->cnt, sizeof(unsigned) * 4)) {
       pc->release();
       return SBM_ERR_NOMEM;
     }
+    // the padding cells of the coarse arrays stay zero
+    SBM_CUDA_TRY(cudaMemsetAsync(pc->rc, 0, sizeof(float) * c.v(), s));
+    SBM_CUDA_TRY(cudaMemsetAsync(pc->coefc, 0, sizeof(float) * c.v(), s));
+    SBM_CUDA_TRY(cudaMemsetAsync(pc->massc, 0, sizeof(float) * c.v(), s));
     SBM_CUDA_TRY(cudaMemsetAsync(pc->zf, 0, sizeof(float) * g.nh, s));
     SBM_CUDA_TRY(cudaMemsetAsync(pc->cnt, 0, sizeof(unsigned) * 4, s));
     SBM_CUDA_TRY(cudaMemsetAsync(pc->scal, 0, sizeof(float) * 8, s));
   }
   pc->hk32 = hk32;
+  pc->dg32 = dg32;
   pc->scale = (float)scale;
   pc->bcx0 = bcx0;
   pc->bcx1 = bcx1;
-  netd::k_pc_coef<<<netd::grid_for(c.v()), 256, 0, s>>>(g, c, hk32, pc->coefc, pc->parts, pc->cnt,
-                                                         pc->scal, pc->kout, scale);
-  netd::k_pc_feat<<<netd::grid_for(c.v()), 256, 0, s>>>(c, pc->coefc, pc->scal, bcx0, bcx1,
-                                                         pc->w->in0);
+  netd::k_pc_coef<<<netd::grid_for(cv.v()), 256, 0, s>>>(g, c, cv, hk32, dg32, pc->coefc,
+                                                          pc->massc, pc->parts, pc->cnt, pc->scal,
+                                                          pc->kout, scale, dg32 ? -1.0 : 1.0);
+  netd::k_pc_feat<<<netd::grid_for(c.v()), 256, 0, s>>>(c, cv, pc->coefc, pc->massc, pc->scal,
+                                                         bcx0, bcx1, dg32 ? 1 : 0, pc->w->in0);
   SBM_LAUNCHED(2);
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
@@ -1074,17 +1148,37 @@ float* net_pc_zbuf(sbm_ctx* ctx) {
 }
 
 float* net_pc_rc(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->rc; }
+// y and x strides of the coarse arrays (the padded grid's extents)
+void net_pc_rc_strides(sbm_ctx* ctx, int* sy, int* sx) {
+  const netd::NetPc* pc = static_cast<const netd::NetPc*>(ctx->net);
+  *sy = pc->c.ny;
+  *sx = pc->c.nx;
+}
 float* net_pc_scal(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->scal; }
 
 int net_pc_nodes() { return 3 + 9; }
+
+// The multiplicative step: tiles of 64 x 8 x 4 fine cells (the last y tile
+// may be partial), one wave of resident blocks (3 per SM at 80 registers)
+// walking them grid-stride.
+static void launch_mult(netd::NetPc* pc, const Geo& g, const float* r32, const float* iv32,
+                        const float* q32, double* partials, CgState* st, cudaStream_t s) {
+  const int64_t tiles = (int64_t)((g.ny + netd::kMTY - 1) / netd::kMTY) * (g.nx / netd::kMTX) *
+                        (g.nz / netd::kMTZ);
+  const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
+  launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, pc->c, pc->cv,
+             (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->hk32,
+             pc->dg32, pc->scale, pc->bcx0, pc->bcx1, netd::kPcOmega, pc->zf + kOff32,
+             (const int*)pc->net->err, partials, st);
+}
 
 void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const float* q32,
                    double* partials, CgState* st, cudaStream_t s) {
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   const Geo& g = ctx->g32;
   const netd::Dims& c = pc->c;
-  launch_pdl(netd::k_pc_restrict, dim3(netd::grid_for(c.v())), dim3(256), 0, s, g, c, r32, pc->rc,
-             partials, (float*)pc->scal, st);
+  launch_pdl(netd::k_pc_restrict, dim3(netd::grid_for(pc->cv.v())), dim3(256), 0, s, g, c, pc->cv,
+             r32, pc->rc, partials, (float*)pc->scal, st);
   launch_pdl(netd::k_pc_pack, dim3(netd::grid_for(c.v())), dim3(256), 0, s, c.v(),
              (const float*)pc->rc, (const float*)pc->scal, pc->w->in0, (const CgState*)st);
   SBM_LAUNCHED(2);
@@ -1097,17 +1191,11 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
   // flexible-CG iterations of the 256^3 headline solve fall from 123-128
   // with the additive form to 61)
   if (ctx->pc_additive) {
-    launch_pdl(netd::k_pc_prolong, dim3((unsigned)b), dim3(256), 0, s, g, c,
+    launch_pdl(netd::k_pc_prolong, dim3((unsigned)b), dim3(256), 0, s, g, c, pc->cv,
                (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->zf + kOff32,
                (const int*)pc->net->err, partials, st);
   } else {
-    const int64_t tiles =
-        (int64_t)(g.ny / netd::kMTY) * (g.nx / netd::kMTX) * (g.nz / netd::kMTZ);
-    // one wave of resident blocks (3 per SM at 80 registers), grid-stride
-    const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
-    launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, c, (const float*)pc->w->out,
-               (const float*)pc->scal, r32, iv32, q32, pc->hk32, pc->scale, pc->bcx0, pc->bcx1,
-               netd::kPcOmega, pc->zf + kOff32, (const int*)pc->net->err, partials, st);
+    launch_mult(pc, g, r32, iv32, q32, partials, st, s);
   }
   SBM_LAUNCHED(1);
 }
@@ -1121,11 +1209,8 @@ void net_pc_launch_part(sbm_ctx* ctx, int part, const float* r32, const float* i
     netd::forward(pc->net, *pc->w, false, &st->done, &st->pc_off, s);
     return;
   }
-  const int64_t tiles = (int64_t)(g.ny / netd::kMTY) * (g.nx / netd::kMTX) * (g.nz / netd::kMTZ);
-  const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
-  launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, c, (const float*)pc->w->out,
-             (const float*)pc->scal, r32, iv32, q32, pc->hk32, pc->scale, pc->bcx0, pc->bcx1,
-             netd::kPcOmega, pc->zf + kOff32, (const int*)pc->net->err, partials, st);
+  (void)c;
+  launch_mult(pc, g, r32, iv32, q32, partials, st, s);
   SBM_LAUNCHED(1);
 }
 
@@ -1331,8 +1416,10 @@ int sbm_net_train(sbm_net* n, int ny, int nx, int nz, int nsamples, const float*
   return sbm_net_train_steps(n, steps, batch, lr, seed, loss_hist);
 }
 
-// Weights file: 8-byte magic "SBMNET01", int64 parameter count, float64
-// output scale k_out, then the FP32 parameters (little-endian).
+// Weights file: 8-byte magic "SBMNET01" (a network trained on the potential
+// form only) or "SBMNET02" (also trained on the CnE form, reading input
+// channel 5), int64 parameter count, float64 output scale k_out, then the
+// FP32 parameters (little-endian).
 int sbm_net_load(const char* path, sbm_net** out, double* out_scale) {
   if (!path || !out || !out_scale) return SBM_ERR_ARG;
   *out = nullptr;
@@ -1345,7 +1432,8 @@ int sbm_net_load(const char* path, sbm_net** out, double* out_scale) {
   int64_t count = 0;
   double scale = 0.0;
   std::vector<float> h;
-  bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "SBMNET01", 8) == 0 &&
+  bool ok = fread(magic, 1, 8, f) == 8 &&
+            (memcmp(magic, "SBMNET01", 8) == 0 || memcmp(magic, "SBMNET02", 8) == 0) &&
             fread(&count, sizeof(count), 1, f) == 1 && count == kL.total &&
             fread(&scale, sizeof(scale), 1, f) == 1 && scale > 0.0;
   if (ok) {
@@ -1364,9 +1452,18 @@ int sbm_net_load(const char* path, sbm_net** out, double* out_scale) {
     *out = nullptr;
     return rc;
   }
+  (*out)->mass = memcmp(magic, "SBMNET02", 8) == 0 ? 1 : 0;
   *out_scale = scale;
   return SBM_OK;
 }
+
+int sbm_net_set_mass_channel(sbm_net* n, int on) {
+  if (!n || (on != 0 && on != 1)) return SBM_ERR_ARG;
+  n->mass = on;
+  return SBM_OK;
+}
+
+int sbm_net_get_mass_channel(const sbm_net* n) { return n ? n->mass : SBM_ERR_ARG; }
 
 int sbm_ctx_set_net(sbm_ctx* ctx, sbm_net* n, double out_scale) {
   if (!ctx || !(out_scale > 0.0)) return SBM_ERR_ARG;

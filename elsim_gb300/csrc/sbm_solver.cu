@@ -830,8 +830,8 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     k32_update_fcg(Geo g, Geo g64, float* __restrict__ x, const float* __restrict__ p,
                    float* __restrict__ r, const float* __restrict__ q, double* __restrict__ d64,
-                   float* __restrict__ rc, float* __restrict__ scal, double* partials,
-                   CgState* st) {
+                   float* __restrict__ rc, int rcy, int rcx, float* __restrict__ scal,
+                   double* partials, CgState* st) {
   pdl_begin();
   if (st->done) return;
   const bool fold = st->accum_pending != 0;
@@ -871,7 +871,7 @@ __global__ void __launch_bounds__(256)
       sum += (rv.x + rv.y) + (rv.z + rv.w);
     }
     const float m = sum * (1.f / 64.f);
-    rc[u] = m;
+    rc[ic + (int64_t)rcy * (jc + (int64_t)rcx * kc)] = m;  // strides of the padded coarse grid
     a_rc += (double)m * (double)m;
   }
   double v[2] = {(double)a_rr, a_rc}, tot[2];
@@ -1148,7 +1148,11 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
     k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
     SBM_LAUNCHED(1);
   }
-  if (learned && (rc = net_pc_begin(ctx, hk32, sp.scale, sp.bcx0, sp.bcx1, s))) return rc;
+  if (learned &&
+      (rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, sp.scale, sp.bcx0, sp.bcx1, s)))
+    return rc;
+  int rcy = 0, rcx = 0;
+  if (learned) net_pc_rc_strides(ctx, &rcy, &rcx);
   // with the learned preconditioner the direction kernels read z from its buffer
   float* const zl = learned ? net_pc_zbuf(ctx) : nullptr;
   const float* const rdir = learned ? zl : r32;
@@ -1178,9 +1182,10 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
                                                    ctx->r0, r32, iv32, ctx->partials,          \
                                                    ctx->st)
     if (learned) {
-      launch_pdl(k_rel_resid<0, false, true>, rgrid, sh64.block, 0, s2, op64, g32, sh64.zc,
-                 (const double*)ctx->d64, (const float*)x32, (const double*)ctx->r0, r32,
-                 (const float*)iv32, ctx->partials, ctx->st);
+      launch_pdl(sp.form ? k_rel_resid<1, false, true> : k_rel_resid<0, false, true>, rgrid,
+                 sh64.block, 0, s2, op64, g32, sh64.zc, (const double*)ctx->d64,
+                 (const float*)x32, (const double*)ctx->r0, r32, (const float*)iv32,
+                 ctx->partials, ctx->st);
     } else if (sp.form == 0) {
       if (pc) SBM_REL(0, true); else SBM_REL(0, false);
     } else {
@@ -1224,8 +1229,8 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
                                           ctx->partials, ctx->st)
     if (learned) {
       launch_pdl(k32_update_fcg, cgrid, dim3(256), 0, s2, g32, g, x32, (const float*)out, r32,
-                 (const float*)q32, ctx->d64, net_pc_rc(ctx), net_pc_scal(ctx), ctx->partials,
-                 ctx->st);
+                 (const float*)q32, ctx->d64, net_pc_rc(ctx), rcy, rcx, net_pc_scal(ctx),
+                 ctx->partials, ctx->st);
     } else if (vec == 4) {
       if (pc) SBM_UP(true, 4); else SBM_UP(false, 4);
     } else {
@@ -1300,15 +1305,19 @@ int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double*
   const Geo& g32 = ctx->g32;
   cudaStream_t s = ctx->stream;
   float* const hk32 = ctx->hk32 + kOff32;
+  float* const dg32 = ctx->dg32 + kOff32;
   float* const iv32 = ctx->z32 + kOff32;
   float* const r32 = ctx->r32 + kOff32;
   float* const q32 = ctx->q32 + kOff32;
-  OpArgs<float> op32{g32, hk32, nullptr, (float)sp.scale, sp.form, sp.bcx0, sp.bcx1};
+  OpArgs<float> op32{g32, hk32, sp.form ? dg32 : nullptr, (float)sp.scale, sp.form, sp.bcx0,
+                     sp.bcx1};
   const Shape sh32 = stencil_shape(g32, pick_zc(g32, ctx->zc32));
-  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, nullptr, nullptr);
+  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
+                                         dg32);
   k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
   SBM_LAUNCHED(2);
-  if ((rc = net_pc_begin(ctx, hk32, sp.scale, sp.bcx0, sp.bcx1, s))) return rc;
+  if ((rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, sp.scale, sp.bcx0, sp.bcx1, s)))
+    return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(ctx->r64, r, sizeof(double) * g.nh, cudaMemcpyHostToDevice, s));
   k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, ctx->r64, r32, nullptr, nullptr);
   SBM_LAUNCHED(1);
@@ -1425,8 +1434,10 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
     } else if (which == 4) {
       const dim3 cgrid((unsigned)std::min<int64_t>(
           std::max<int64_t>((int64_t)nchunk * g.nx * g.nz / 16 / 256, 1), 152 * 8));
+      int rcy = 0, rcx = 0;
+      net_pc_rc_strides(ctx, &rcy, &rcx);
       k32_update_fcg<<<cgrid, 256, 0, s>>>(g32, g, x32, pb, r32, q32, ctx->d64, net_pc_rc(ctx),
-                                          net_pc_scal(ctx), ctx->partials, ctx->st32);
+                                          rcy, rcx, net_pc_scal(ctx), ctx->partials, ctx->st32);
     } else if (which == 1) {
       if (vec == 4) {
         if (pc) k32_update<true, 4><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);

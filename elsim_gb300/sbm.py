@@ -183,6 +183,10 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_net_load": (C.c_int, [C.c_char_p, C.POINTER(vp), dp]),
         "sbm_ctx_last_precond": (C.c_int, [vp]),
         "sbm_learned_pc_apply": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp, dp]),
+        "sbm_learned_pc_apply_op": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_double, dp,
+                                              dp]),
+        "sbm_net_set_mass_channel": (C.c_int, [vp, C.c_int]),
+        "sbm_net_get_mass_channel": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -426,13 +430,15 @@ class Context:
         """Preconditioner the last mixed-precision solve used (PC_*)."""
         return int(self.lib.sbm_ctx_last_precond(self._h))
 
-    def learned_pc_apply(self, r, bc_x0=BC_ZERO, bc_x1=BC_ZERO, scale=1.0) -> np.ndarray:
-        """z = M(r) of the attached network for the GENERIC operator of the
-        uploaded coefficient (halo-padded arrays)."""
+    def learned_pc_apply(self, r, bc_x0=BC_ZERO, bc_x1=BC_ZERO, scale=1.0,
+                         op=OP_GENERIC) -> np.ndarray:
+        """z = M(r) of the attached network for the GENERIC (or, with
+        op=OP_GENERIC_DIAG, the diagonal CnE-form) operator of the uploaded
+        coefficient (halo-padded arrays)."""
         r = _f64(r, self.hshape)
         z = np.zeros(self.hshape, dtype=np.float64, order="F")
-        _check(self.lib.sbm_learned_pc_apply(self._h, bc_x0, bc_x1, scale, _dptr(r), _dptr(z)),
-               "sbm_learned_pc_apply")
+        _check(self.lib.sbm_learned_pc_apply_op(self._h, op, bc_x0, bc_x1, scale, _dptr(r),
+                                                _dptr(z)), "sbm_learned_pc_apply_op")
         return z
 
     def time_step(self, it: int, dt: float, vsr: float, precision=PREC_FP64) -> dict:
@@ -504,7 +510,8 @@ class Net:
     pass, loss gradient and on-GPU training.  Inputs are channels-last
     (voxel v = i + ny*(j + nx*k), 16 channels), nb samples stacked along z."""
 
-    def __init__(self, seed: int = 0, params: np.ndarray | None = None, out_scale: float = 1.0):
+    def __init__(self, seed: int = 0, params: np.ndarray | None = None, out_scale: float = 1.0,
+                 mass: bool = False):
         self.lib = load_library()
         h = C.c_void_p()
         _check(self.lib.sbm_net_create(seed, C.byref(h)), "sbm_net_create")
@@ -512,6 +519,18 @@ class Net:
         self.out_scale = float(out_scale)
         if params is not None:
             self.set_params(params)
+        self.mass = mass
+
+    @property
+    def mass(self) -> bool:
+        """True when the network reads input channel 5, the mass term of the
+        CnE form (it then also preconditions GENERIC_DIAG / CnE solves)."""
+        return bool(self.lib.sbm_net_get_mass_channel(self._h))
+
+    @mass.setter
+    def mass(self, on: bool) -> None:
+        _check(self.lib.sbm_net_set_mass_channel(self._h, 1 if on else 0),
+               "sbm_net_set_mass_channel")
 
     @staticmethod
     def param_count() -> int:

@@ -272,7 +272,11 @@ int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bc_x0, const 
  * (SBMES:397-840) for a given dt, voltage-scan rate vsr and step index
  * iter: Cahn-Hilliard, CnE implicit solve with the flux BC and mean
  * correction, Dab/pce/pcN, tables, Butler-Volmer Picard loop with the phP
- * and phE solves, current sum and voltage control. */
+ * and phE solves, current sum and voltage control.  precision
+ * SBM_PREC_FP64 runs the reference's plain CG with its stopping norms;
+ * SBM_PREC_MIXED solves each system to rel-res 1e-10 with the mixed solver,
+ * preconditioned by the attached network where it applies (see
+ * SBM_PC_LEARNED below), else by Jacobi. */
 int sbm_time_step(sbm_ctx* ctx, int iter, double dt, double vsr,
                   int precision, sbm_scalars* s);
 
@@ -419,9 +423,14 @@ int sbm_conv3d_bf16(int ny, int nx, int nz, int cin, int cout, const uint16_t* x
  * v = i + ny*(j + nx*k)) are [R r / s, R K / c_ref, 1, x0-face Dirichlet
  * mask, x1-face Dirichlet mask, 0 x 11].  Because z is not linear in r the
  * solver runs flexible CG (beta = -z.q_old / p_old.q_old).
- * SBM_PC_LEARNED applies when a network is attached, the operator is the
- * phP / phE / GENERIC form and ny, nx, nz are multiples of 64; otherwise the
- * solve falls back to Jacobi (sbm_ctx_last_precond reports which ran).
+ * SBM_PC_LEARNED applies when a network is attached and ny, nx, nz are
+ * multiples of 16 (the coarse grid, ny/4 x nx/4 x nz/4 cells, is padded with
+ * zero cells to multiples of 16 for the U-Net, whose activations stay zero
+ * there), to the phP / phE / GENERIC form, and to the CnE / GENERIC_DIAG
+ * form q = diag p - scale S(p) when the network was trained with the mass
+ * channel (input channel 5 = x / (1 + x), x = R diag / (scale c_ref); the
+ * output's sign follows the operator's); otherwise the solve falls back to
+ * Jacobi (sbm_ctx_last_precond reports which ran).
  * Only the mixed-precision solver takes it.  Training / forward calls on
  * one network come from one host thread at a time; any number of contexts
  * may share a network as their preconditioner (they only read its
@@ -458,9 +467,15 @@ int sbm_net_train(sbm_net* net, int ny, int nx, int nz, int nsamples, const floa
                   const float* target, int steps, int batch, float lr, uint64_t seed,
                   float* loss_hist);
 /* New network from a weights file (elsim_gb300/weights/pc_unet.bin: magic
- * "SBMNET01", int64 parameter count, float64 k_out, FP32 parameters);
- * *out_scale receives k_out for sbm_ctx_set_net. */
+ * "SBMNET01", or "SBMNET02" for a network trained with the mass channel,
+ * int64 parameter count, float64 k_out, FP32 parameters); *out_scale
+ * receives k_out for sbm_ctx_set_net. */
 int sbm_net_load(const char* path, sbm_net** out, double* out_scale);
+/* Whether the network reads input channel 5 (the CnE form's mass term): a
+ * network trained on such systems sets it (1) before it is attached; the
+ * getter returns 0 or 1. */
+int sbm_net_set_mass_channel(sbm_net* net, int on);
+int sbm_net_get_mass_channel(const sbm_net* net);
 /* Attach `net` (NULL detaches) to a context with output scale k_out.  The
  * context does not own the network: keep it alive while attached. */
 int sbm_ctx_set_net(sbm_ctx* ctx, sbm_net* net, double out_scale);
@@ -472,6 +487,10 @@ int sbm_ctx_last_precond(const sbm_ctx* ctx);
  * operator of the context's coefficient (halo-padded FP64 r and z). */
 int sbm_learned_pc_apply(sbm_ctx* ctx, int bc_x0, int bc_x1, double scale, const double* r,
                          double* z);
+/* The same for op = SBM_OP_GENERIC or SBM_OP_GENERIC_DIAG (diagonal from
+ * the context's DIAG field). */
+int sbm_learned_pc_apply_op(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale,
+                            const double* r, double* z);
 
 /* Test hook of the device-side bounded waits (no counterpart in the
  * reference): the number of attempts each consumer-side mbarrier wait of

@@ -113,29 +113,53 @@ def up_bwd(g):
     return g.reshape(nb, nz // 2, 2, nx // 2, 2, ny // 2, 2, c).sum(axis=(2, 4, 6))
 
 
-def forward(p, x, rounding=True):
+def level_valid(valid):
+    """Valid extents (y, x, z) per level of a zero-padded grid: each level
+    halves the previous one's, rounding up."""
+    out = [tuple(valid)]
+    for _ in range(4):
+        out.append(tuple((v + 1) // 2 for v in out[-1]))
+    return out
+
+
+def mask(a, v):
+    """Zero the cells of a [nb, nz, nx, ny, C] array beyond valid extents
+    v = (y, x, z) (the padding of a padded grid); None: nothing."""
+    if v is None:
+        return a
+    a = a.copy()
+    a[:, v[2]:] = 0.0
+    a[:, :, v[1]:] = 0.0
+    a[:, :, :, v[0]:] = 0.0
+    return a
+
+
+def forward(p, x, rounding=True, valid=None):
     """U-Net forward on x [nb, nz, nx, ny, 16]; returns (out [nb, nz, nx, ny],
-    cache of the stored activations)."""
+    cache of the stored activations).  valid = (y, x, z) extents of a grid
+    zero-padded beyond them: every layer's outputs (and upsampled copies)
+    stay zero in the padding."""
     R = bf16 if rounding else (lambda a: a)
     x = R(x)
     w16 = {l: (R(weights(p, l)[0]) if l != OUT else weights(p, l)[0], weights(p, l)[1])
            for l in range(10)}
+    lv = level_valid(valid) if valid is not None else [None] * 5
     cat = [None] * 4
     pin = [None] * 5
     dec = [None] * 4
     h = x
     for lev in range(4):
         l = ENC[lev]
-        e = R(np.maximum(conv(h, *w16[l]), 0.0))
+        e = mask(R(np.maximum(conv(h, *w16[l]), 0.0)), lv[lev])
         cat[lev] = np.concatenate([np.zeros(e.shape[:4] + (UPW[lev],)), e], axis=4)
         pin[lev + 1] = R(pool(e))
         h = pin[lev + 1]
-    a4 = R(np.maximum(conv(pin[4], *w16[E4]), 0.0))
+    a4 = mask(R(np.maximum(conv(pin[4], *w16[E4]), 0.0)), lv[4])
     below = a4
     for lev in (3, 2, 1, 0):
-        cat[lev][..., :UPW[lev]] = up(below)
+        cat[lev][..., :UPW[lev]] = mask(up(below), lv[lev])
         l = DEC[lev]
-        dec[lev] = R(np.maximum(conv(cat[lev], *w16[l]), 0.0))
+        dec[lev] = mask(R(np.maximum(conv(cat[lev], *w16[l]), 0.0)), lv[lev])
         below = dec[lev]
     wo, bo = w16[OUT]
     out = dec[0] @ wo[0, 0, :] + bo[0]
@@ -199,9 +223,12 @@ def from_cl(a):
     return np.transpose(a[0], (2, 1, 0))
 
 
-def features(r_int, coef_int, bcx0, bcx1):
-    """Input channels [nb=1, nz, nx, ny, 16], s and c_ref from the interior
-    residual and coefficient (fine interior arrays [i, j, k])."""
+def features(r_int, coef_int, bcx0, bcx1, diag_int=None, scale=1.0, pad=16):
+    """Input channels [nb=1, nz, nx, ny, 16], s, c_ref and the valid coarse
+    extents (y, x, z) from the interior residual and coefficient (fine
+    interior arrays [i, j, k]); the coarse grid is zero-padded to multiples
+    of `pad`.  With the CnE form's diagonal, channel 5 = x / (1 + x), x =
+    R diag / (scale c_ref)."""
     rc = restrict(r_int)
     cc = restrict(coef_int)
     s = float(np.sqrt((rc ** 2).mean()))
@@ -215,7 +242,13 @@ def features(r_int, coef_int, bcx0, bcx1):
         f[:, 0, :, 3] = 1.0
     if bcx1 == 1:
         f[:, -1, :, 4] = 1.0
-    return np.transpose(f, (2, 1, 0, 3))[None], s, cref
+    if diag_int is not None:
+        x = restrict(diag_int) / (scale * cref)
+        f[..., 5] = x / (1.0 + x)
+    up16 = lambda n: -(-n // pad) * pad
+    fp = np.zeros((up16(nyc), up16(nxc), up16(nzc), NFEAT))
+    fp[:nyc, :nxc, :nzc] = f
+    return np.transpose(fp, (2, 1, 0, 3))[None], s, cref, (nyc, nxc, nzc)
 
 
 def _interp_axis(n_fine):
@@ -243,10 +276,11 @@ def prolong(ec):
     return out
 
 
-def inv_diag(coef_h, scale, bcx0, bcx1):
-    """1 / diagonal of q = scale * S(p) (halo-padded coefficient K, hk = K/2,
-    face coefficient hk_nb + hk_c; y and z faces Neumann, an x face adds its
-    term when it is Dirichlet)."""
+def inv_diag(coef_h, scale, bcx0, bcx1, diag_h=None):
+    """1 / diagonal of q = scale * S(p), or of q = diag p - scale * S(p) when
+    diag_h is given (halo-padded coefficient K, hk = K/2, face coefficient
+    hk_nb + hk_c; y and z faces Neumann, an x face adds its term when it is
+    Dirichlet)."""
     hk = 0.5 * np.asarray(coef_h, dtype=np.float64)
     ny, nx, nz = (n - 2 for n in hk.shape)
     I = slice(1, -1)
@@ -265,6 +299,8 @@ def inv_diag(coef_h, scale, bcx0, bcx1):
     s[:, :, 1:] += hk[I, I, 1:nz] + kc[:, :, 1:]
     s[:, :, :-1] += hk[I, I, 2:nz + 1] + kc[:, :, :-1]
     d = -scale * s
+    if diag_h is not None:
+        d = np.asarray(diag_h, dtype=np.float64)[I, I, I] + scale * s
     return np.where(d != 0, 1.0 / np.where(d != 0, d, 1.0), 0.0)
 
 
@@ -293,20 +329,28 @@ OMEGA = 2.3  # weight of the Jacobi step of the multiplicative form (the GPU's)
 
 
 def pc_apply(p, kout, coef_h, r_h, scale=1.0, bcx0=1, bcx1=1, rounding=True,
-             multiplicative=True, omega=OMEGA):
+             multiplicative=True, omega=OMEGA, diag_h=None):
     """The learned preconditioner on the interior (halo-padded in and out):
     z1 = P e_c, then z = z1 + omega D^-1 (r - A z1) (multiplicative, the
-    default) or z = D^-1 r + z1 (additive)."""
+    default) or z = D^-1 r + z1 (additive).  A = scale S (the potential
+    form) or, with diag_h, A = diag - scale S (the CnE form: mass channel
+    fed, e_c's sign flipped).  Coarse grids are zero-padded to multiples of
+    16 for the network."""
     r = r_h[1:-1, 1:-1, 1:-1]
     coef = coef_h[1:-1, 1:-1, 1:-1]
-    f, s, cref = features(r, coef, bcx0, bcx1)
-    out, _ = forward(p, f, rounding)
-    ec = from_cl(out) * s * kout / (scale * cref)
+    dg = None if diag_h is None else np.asarray(diag_h, dtype=np.float64)[1:-1, 1:-1, 1:-1]
+    f, s, cref, v = features(r, coef, bcx0, bcx1, dg, scale)
+    out, _ = forward(p, f, rounding, valid=v)
+    sgn = -1.0 if dg is not None else 1.0
+    ec = from_cl(out)[:v[0], :v[1], :v[2]] * (sgn * s * kout / (scale * cref))
     z1 = prolong(ec)
-    invd = inv_diag(coef_h, scale, bcx0, bcx1)
+    invd = inv_diag(coef_h, scale, bcx0, bcx1, diag_h)
     z = np.zeros_like(r_h)
     if multiplicative:
-        z[1:-1, 1:-1, 1:-1] = z1 + omega * (invd * (r - apply_dir(coef_h, z1, scale, bcx0, bcx1)))
+        az1 = apply_dir(coef_h, z1, scale, bcx0, bcx1)
+        if dg is not None:
+            az1 = dg * z1 - az1
+        z[1:-1, 1:-1, 1:-1] = z1 + omega * (invd * (r - az1))
     else:
         z[1:-1, 1:-1, 1:-1] = invd * r + z1
     return z

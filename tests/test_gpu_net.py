@@ -163,7 +163,7 @@ def test_learned_preconditioner_cuts_iterations(built):
 
 def test_falls_back_to_jacobi(built):
     stored = learned.load()
-    # extents that are not multiples of 64
+    # extents that are not multiples of 16
     n = 60
     prob = _problem(n, 31)
     with _context(n, prob) as ctx:
@@ -222,3 +222,86 @@ def test_learned_preconditioner_on_a_neumann_face(built):
     assert rl["iters"] < 0.6 * rj["iters"]
     assert np.abs(xl - xj).max() <= 1e-6 * np.abs(xj).max()
 
+
+
+def _shape_problem(shape, seed, tunnel=False):
+    ms = synth.microstructure(shape, seed=seed, solid_fraction=0.6, tunnel=tunnel)
+    return ms, synth.potential_problem(ms["psi"])
+
+
+@pytest.mark.parametrize("shape", [(48, 48, 48), (48, 32, 80)])
+def test_preconditioner_on_a_padded_coarse_grid_matches_oracle(built, shape):
+    """Extents that are multiples of 16 but not of 64: the coarse grid (12 x
+    12 x 12, 12 x 8 x 20) is zero-padded to multiples of 16 for the U-Net,
+    whose activations stay zero in the padding; the y tiles of the
+    multiplicative step are partial.  GPU against the NumPy oracle."""
+    _, prob = _shape_problem(shape, 51)
+    stored = learned.load()
+    with sbm.Context(*shape) as ctx:
+        for f in ("coef", "rhs", "weight", "x"):
+            ctx.upload(f, prob[f])
+        ctx.set_net(stored)
+        rng = np.random.default_rng(52)
+        r = np.zeros(ctx.hshape, order="F")
+        r[1:-1, 1:-1, 1:-1] = rng.normal(size=shape)
+        z = ctx.learned_pc_apply(r)
+    zr = no.pc_apply(stored.params().astype(np.float64), stored.out_scale, prob["coef"], r)
+    assert _rel(z[1:-1, 1:-1, 1:-1], zr[1:-1, 1:-1, 1:-1]) <= 1e-3
+
+
+@pytest.mark.parametrize("n", [48, 96])
+def test_learned_solve_on_grids_of_48_and_96(built, n):
+    """The batched workload's 48^3 and 96^3 volumes run the learned
+    preconditioner (padded coarse grids), converge to the same FP64 true
+    residual and need fewer iterations than Jacobi-PCG."""
+    from oracle import sbm_oracle as orc
+    _, prob = _shape_problem((n, n, n), 60 + n, tunnel=True)
+    stored = learned.load()
+    with _context(n, prob) as ctx:
+        ctx.set_net(stored)
+        rl, xl, used = _solve(ctx, prob, sbm.PC_LEARNED)
+        rj, xj, _ = _solve(ctx, prob, sbm.PC_JACOBI)
+    assert used == sbm.PC_LEARNED and rl["status"] == sbm.OK
+    assert rl["iters"] < 0.6 * rj["iters"], (rl["iters"], rj["iters"])
+    xo, io = orc.cg(prob["coef"], prob["rhs"], prob["x"], 1.0, sbm.BC_ZERO, sbm.BC_ZERO,
+                    sbm.STOP_REL_RES, 1e-8, 50000)
+    assert _rel(xl[1:-1, 1:-1, 1:-1], xo[1:-1, 1:-1, 1:-1]) <= 1e-6
+
+
+def test_cne_form_preconditioner_matches_oracle(built):
+    """The CnE form q = diag p - scale S(p) (a network flagged as reading the
+    mass channel; random weights suffice for parity): coarse features with
+    channel 5, the output's sign flipped, and the diagonal in the Jacobi
+    step, GPU against the NumPy oracle on a padded 48 x 64 x 32 grid."""
+    shape = (48, 64, 32)
+    ms = synth.microstructure(shape, seed=71, solid_fraction=0.6)
+    prob = learned.cne_problem(ms["psi"], np.random.default_rng(72))
+    prob["scale"] = 5.0
+    net = sbm.Net(seed=73, mass=True)
+    net.out_scale = 0.5
+    with sbm.Context(*shape) as ctx:
+        for f in ("coef", "weight", "diag"):
+            ctx.upload(f, prob[f])
+        ctx.set_net(net)
+        rng = np.random.default_rng(74)
+        r = np.zeros(ctx.hshape, order="F")
+        r[1:-1, 1:-1, 1:-1] = rng.normal(size=shape)
+        z = ctx.learned_pc_apply(r, bc_x0=sbm.BC_COPY, bc_x1=sbm.BC_COPY, scale=5.0,
+                                 op=sbm.OP_GENERIC_DIAG)
+    zr = no.pc_apply(net.params().astype(np.float64), 0.5, prob["coef"], r, scale=5.0, bcx0=0,
+                     bcx1=0, diag_h=prob["diag"])
+    assert _rel(z[1:-1, 1:-1, 1:-1], zr[1:-1, 1:-1, 1:-1]) <= 1e-3
+    # without the flag the CnE form is not the network's: the solve falls back
+    net.mass = False
+    with sbm.Context(*shape) as ctx:
+        for f in ("coef", "weight", "diag"):
+            ctx.upload(f, prob[f])
+        rhs = np.zeros(ctx.hshape, order="F")
+        rhs[1:-1, 1:-1, 1:-1] = r[1:-1, 1:-1, 1:-1]
+        ctx.upload("rhs", rhs)
+        ctx.upload("x", np.zeros(ctx.hshape, order="F"))
+        ctx.set_net(net)
+        info = ctx.cg_solve(op=sbm.OP_GENERIC_DIAG, bc_x0=sbm.BC_COPY, bc_x1=sbm.BC_COPY,
+                            scale=5.0, tol=1e-8, max_it=20000, stop_rule=sbm.STOP_REL_RES,
+                            precision=sbm.PREC_MIXED, precond=sbm.PC_LEARNED)
+        assert info["status"] == sbm.OK and ctx.last_precond() == sbm.PC_JACOBI

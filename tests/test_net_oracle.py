@@ -41,16 +41,41 @@ def test_oracle_backward_matches_finite_differences():
     assert max(errs) < 1e-4
 
 
-def test_features_match_oracle():
+@pytest.mark.parametrize("cne", [False, True])
+def test_features_match_oracle(cne):
     rng = np.random.default_rng(4)
     r = rng.normal(size=(32, 16, 24))
     k = rng.uniform(0.1, 1.0, size=(32, 16, 24))
-    f1, s1, c1 = learned.features(r, k, 1, 0)
-    f2, s2, c2 = no.features(r, k, 1, 0)
-    assert f1.shape == (8 * 4 * 6, 16)
-    np.testing.assert_allclose(f1, f2.reshape(-1, 16), rtol=1e-6, atol=1e-6)
+    d = rng.uniform(0.0, 1.0, size=(32, 16, 24)) if cne else None
+    f1, s1, c1 = learned.features(r, k, 1, 0, d, 0.3)
+    f2, s2, c2, v = no.features(r, k, 1, 0, d, 0.3)
+    assert f1.shape == (8 * 4 * 6, 16) and v == (8, 4, 6)
+    # the oracle pads the coarse grid with zero cells to multiples of 16
+    assert f2.shape == (1, 16, 16, 16, 16)
+    assert not f2[0, 6:].any() and not f2[0, :, 4:].any() and not f2[0, :, :, 8:].any()
+    np.testing.assert_allclose(f1, f2[0, :6, :4, :8].reshape(-1, 16), rtol=1e-6, atol=1e-6)
     assert s1 == pytest.approx(s2) and c1 == pytest.approx(c2)
     assert f1[:, 3].sum() == 8 * 6 and f1[:, 4].sum() == 0  # x0 face only
+    if cne:
+        x = no.restrict(d) / (0.3 * c2)
+        np.testing.assert_allclose(f2[0, :6, :4, :8, 5], np.transpose(x / (1 + x), (2, 1, 0)),
+                                   rtol=1e-12)
+    else:
+        assert not f1[:, 5].any()
+
+
+def test_padded_forward_equals_unpadded_where_the_grid_is_whole():
+    """A 16^3 grid zero-padded to 32^3 with the padding masked runs the
+    network exactly as the 16^3 grid itself: the zero padding stands for the
+    convolutions' zero fill beyond the faces."""
+    rng = np.random.default_rng(8)
+    p = _params(2)
+    x = rng.normal(size=(1, 16, 16, 16, 16))
+    want, _ = no.forward(p, x, rounding=False)
+    xp = np.zeros((1, 32, 32, 32, 16))
+    xp[:, :16, :16, :16] = x
+    got, _ = no.forward(p, xp, rounding=False, valid=(16, 16, 16))
+    np.testing.assert_allclose(got[:, :16, :16, :16], want, rtol=1e-12, atol=1e-12)
 
 
 def test_target_is_restricted_scaled_error():
