@@ -48,11 +48,12 @@ def test_batch_equals_individual_solves(built):
 
 
 def test_batch_with_learned_preconditioner(built):
-    # 64^3 and 128^3 volumes take the learned preconditioner, the 48^3 one
-    # falls back to Jacobi; each equals its single solve
+    # 64^3, 48^3 (zero-padded coarse grid) and 128^3 volumes take the learned
+    # preconditioner, the 60^3 one (not a multiple of 16) falls back to
+    # Jacobi; each equals its single solve
     from elsim_gb300 import learned
     net = learned.load()
-    sizes = [64, 48, 128, 64]
+    sizes = [64, 48, 128, 60]
     probs = [_vol(n, 300 + v, 0.55 + 0.03 * v) for v, n in enumerate(sizes)]
     ctxs = [sbm.Context(n, n, n) for n in sizes]
     for c, p in zip(ctxs, probs):
@@ -61,8 +62,8 @@ def test_batch_with_learned_preconditioner(built):
         c.set_net(net)
     out = sbm.batch_solve(ctxs, tol=1e-8, precond=sbm.PC_LEARNED)
     assert out["status"] == [0] * len(sizes)
-    assert [c.last_precond() for c in ctxs] == [sbm.PC_LEARNED, sbm.PC_JACOBI, sbm.PC_LEARNED,
-                                                sbm.PC_LEARNED]
+    assert [c.last_precond() for c in ctxs] == [sbm.PC_LEARNED, sbm.PC_LEARNED, sbm.PC_LEARNED,
+                                                sbm.PC_JACOBI]
     xs = [c.download("x") for c in ctxs]
     for v, (c, p) in enumerate(zip(ctxs, probs)):
         c.upload("x", p["x"])
