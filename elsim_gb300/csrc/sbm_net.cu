@@ -489,33 +489,52 @@ int launch(Work& w, const ConvArgs& a, cudaStream_t s) {
 // when training.
 int forward(sbm_net* n, Work& w, bool tgt, const int* skip, const int* skip2, cudaStream_t s) {
   int rc;
+  // the nine convolutions in launch order: E0..E3 (pooling), E4, D3..D0
+  ConvArgs a[9];
   for (int lev = 0; lev < 4; ++lev) {
     const int l = kEnc[lev];
-    ConvArgs a =
-        layer_args(n, w, l, lev, lev == 0 ? w.in0 : w.pin[lev], kCi[l], true, skip, skip2);
-    a.y16 = w.cat[lev];
-    a.offy = kUpW[lev];
-    a.pool = w.pin[lev + 1];
-    if ((rc = launch(w, a, s))) return rc;
+    a[lev] = layer_args(n, w, l, lev, lev == 0 ? w.in0 : w.pin[lev], kCi[l], true, skip, skip2);
+    a[lev].y16 = w.cat[lev];
+    a[lev].offy = kUpW[lev];
+    a[lev].pool = w.pin[lev + 1];
   }
-  {
-    ConvArgs a = layer_args(n, w, E4, 4, w.pin[4], kCi[E4], false, skip, skip2);
-    a.y16 = w.train ? w.a4 : nullptr;
-    a.up = w.cat[3];
-    if ((rc = launch(w, a, s))) return rc;
-  }
+  a[4] = layer_args(n, w, E4, 4, w.pin[4], kCi[E4], false, skip, skip2);
+  a[4].y16 = w.train ? w.a4 : nullptr;
+  a[4].up = w.cat[3];
   for (int lev = 3; lev >= 0; --lev) {
     const int l = kDec[lev];
-    ConvArgs a = layer_args(n, w, l, lev, w.cat[lev], kCatW[lev], false, skip, skip2);
-    a.y16 = w.train ? w.dec[lev] : nullptr;
+    ConvArgs& d = a[8 - lev];
+    d = layer_args(n, w, l, lev, w.cat[lev], kCatW[lev], false, skip, skip2);
+    d.y16 = w.train ? w.dec[lev] : nullptr;
     if (lev > 0) {
-      a.up = w.cat[lev - 1];
+      d.up = w.cat[lev - 1];
     } else {
-      a.w1x1 = n->w32 + kL.off[OUT];
-      a.b1x1 = n->w32 + kL.boff[OUT];
-      a.out1x1 = w.out;
+      d.w1x1 = n->w32 + kL.off[OUT];
+      d.b1x1 = n->w32 + kL.boff[OUT];
+      d.out1x1 = w.out;
     }
-    if ((rc = launch(w, a, s))) return rc;
+  }
+  // The deep levels E2, E3, E4, D3, D2 (few CTAs per layer) run as one
+  // chain launch of one thread-block cluster when it fits: two planes where
+  // the epilogue pools (and on D2, whose level has as many tiles as E2's),
+  // one elsewhere.
+  ConvArgs ch[5] = {a[2], a[3], a[4], a[5], a[6]};
+  const int chain_planes[5] = {2, 2, 1, 1, 2};
+  for (int q = 0; q < 5; ++q)
+    ch[q].planes = (ch[q].nzs % chain_planes[q] == 0) ? chain_planes[q] : 1;
+  const bool chain = conv3_chain_usable(ch, 5);
+  for (int q = 0; q < 9; ++q) {
+    if (chain && q >= 2 && q <= 6) {
+      if (q > 2) continue;
+      const ConvMap* maps[5];
+      for (int c = 0; c < 5; ++c) {
+        maps[c] = map_for(w, ch[c]);
+        if (!maps[c]) return SBM_ERR_STATE;
+      }
+      if ((rc = conv3_chain_launch(ch, maps, 5, s))) return rc;
+      continue;
+    }
+    if ((rc = launch(w, a[q], s))) return rc;
   }
   if (tgt) {
     const int64_t V = w.d[0].v();
@@ -524,6 +543,19 @@ int forward(sbm_net* n, Work& w, bool tgt, const int* skip, const int* skip2, cu
   }
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
+}
+
+// Kernel launches of one forward pass of w (the deep levels' chain counts one).
+int forward_launches(const sbm_net* n, const Work& w, const int* skip, const int* skip2) {
+  ConvArgs ch[5];
+  const int chain_planes[5] = {2, 2, 1, 1, 2};
+  const int lev[5] = {2, 3, 4, 3, 2};
+  const int lay[5] = {E2, E3, E4, D3, D2};
+  for (int q = 0; q < 5; ++q) {
+    ch[q] = layer_args(const_cast<sbm_net*>(n), w, lay[q], lev[q], w.in0, 16, q < 2, skip, skip2);
+    ch[q].planes = (ch[q].nzs % chain_planes[q] == 0) ? chain_planes[q] : 1;
+  }
+  return conv3_chain_usable(ch, 5) ? 5 : 9;
 }
 
 int wgrad(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx, const bf16* gy,
@@ -1156,7 +1188,10 @@ void net_pc_rc_strides(sbm_ctx* ctx, int* sy, int* sx) {
 }
 float* net_pc_scal(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->scal; }
 
-int net_pc_nodes() { return 3 + 9; }
+int net_pc_nodes(sbm_ctx* ctx) {
+  const netd::NetPc* pc = static_cast<const netd::NetPc*>(ctx->net);
+  return 3 + netd::forward_launches(pc->net, *pc->w, nullptr, nullptr);
+}
 
 // The multiplicative step: tiles of 64 x 8 x 4 fine cells (the last y tile
 // may be partial), one wave of resident blocks (3 per SM at 80 registers)
