@@ -71,11 +71,13 @@ def _args():
     ap.add_argument("--pc", default="learned", choices=["learned", "jacobi"],
                     help="preconditioner of the headline solve")
     ap.add_argument("--workload", default="solve256",
-                    choices=["solve256", "batch96", "profile", "frontend", "step128"],
+                    choices=["solve256", "batch96", "profile", "frontend", "step128", "unet64"],
                     help="solve256: the headline 256^3 solve; batch96: 96 uneven sub-volumes; "
                          "profile: only the production solve, for ncu captures; frontend: "
                          "one frame of the LevelSet_3D geometry front end; step128: the "
-                         "full electrochemical time step at 128^3")
+                         "full electrochemical time step at 128^3; unet64: forward passes "
+                         "of the preconditioner's U-Net on the 64^3 coarse grid of a 256^3 "
+                         "solve (the size its ncu captures use)")
     return ap.parse_args()
 
 
@@ -1069,6 +1071,32 @@ def run_profile(args):
     return 0
 
 
+def run_unet64(args):
+    """Forward passes of the learned preconditioner's U-Net (stored weights)
+    on the 64^3 coarse grid of a 256^3 solve, through sbm_net_forward (host
+    input, uploaded once per call): `steps` calls after `warmup`; `value` =
+    wall time per call, the tensor roofline of the convolutions from the
+    same FLOP count as the headline line."""
+    import __graft_entry__
+    __graft_entry__.build()
+    from elsim_gb300 import learned
+    net = learned.load()
+    rng = np.random.default_rng(SEED)
+    c = 64
+    x = rng.normal(size=(c ** 3, 16)).astype(np.float32)
+    x[:, 5:] = 0.0
+    x[:, 2] = 1.0
+    for _ in range(args.warmup):
+        net.forward(x, (c, c, c))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = net.forward(x, (c, c, c))
+    t = (time.perf_counter() - t0) / args.steps
+    print(json.dumps({"workload": "unet64", "coarse_grid": [c, c, c], "s_per_call": t,
+                      "unet_gflop": unet_flops(4 * c) / 1e9, "out_rms": float(np.sqrt((out ** 2).mean()))}))
+    return 0
+
+
 def main():
     args = _args()
     if args.impl == "reference":
@@ -1081,6 +1109,8 @@ def main():
         return run_frontend(args)
     if args.workload == "step128":
         return run_step128(args)
+    if args.workload == "unet64":
+        return run_unet64(args)
     return run_ours(args)
 
 

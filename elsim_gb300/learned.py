@@ -121,6 +121,23 @@ def rhs_family(shape, rng, coef_h, scale=1.0):
     return out
 
 
+def rhs_bv(shape, rng, psi_h, count=10):
+    """Right-hand sides like the Butler-Volmer source of the potential
+    systems (SBMES:631-641: RHS = -F R AvPx, the reaction rate times the
+    interface measure): the interface measure |grad psi| (central
+    differences) times a random smooth rate field (Gaussian-smoothed noise,
+    sigma 1-6 cells, random offset and sign), `count` of them."""
+    g = np.gradient(psi_h, axis=(0, 1, 2))
+    avp = np.sqrt(g[0] ** 2 + g[1] ** 2 + g[2] ** 2)[1:-1, 1:-1, 1:-1]
+    avp = np.where(avp < 1e-2, 0.0, avp)
+    out = []
+    for _ in range(count):
+        rate = _smooth(rng.normal(size=shape), float(rng.uniform(1.0, 6.0)))
+        rate = rate / max(np.abs(rate).max(), 1e-30) + rng.uniform(-0.5, 0.5)
+        out.append(avp * rate * rng.choice([-1.0, 1.0]))
+    return out
+
+
 def cne_problem(psi_h: np.ndarray, rng) -> dict:
     """A CnE-form system q = diag p - scale S(p) like the concentration solve
     of either phase (SBMES:515-521): diag = psE = 1 - psi + 1e-6 (electrolyte)
@@ -136,7 +153,7 @@ def cne_problem(psi_h: np.ndarray, rng) -> dict:
 
 
 def make_pairs(n: int, seeds, tol: float = 1e-7, scale: float = 1.0, verbose: bool = False,
-               form: int = 0):
+               form: int = 0, rhs: str = "family"):
     """(features, s, c_ref, coarse error) for every right-hand side of
     rhs_family on the seeded n^3 microstructures; errors from the library's
     mixed-precision Jacobi-CG.  form 0: the potential operator scale S
@@ -162,9 +179,12 @@ def make_pairs(n: int, seeds, tol: float = 1e-7, scale: float = 1.0, verbose: bo
             ctx.upload("weight", prob["weight"])
             if diag is not None:
                 ctx.upload("diag", diag)
-            rhss = rhs_family(shape, rng, coef, sc)
-            if form:
-                rhss = rhss[:4] + rhss[5:]  # no Dirichlet face source
+            if rhs == "bv":
+                rhss = rhs_bv(shape, rng, ms["psi"])
+            else:
+                rhss = rhs_family(shape, rng, coef, sc)
+                if form:
+                    rhss = rhss[:4] + rhss[5:]  # no Dirichlet face source
             for r in rhss:
                 rh = np.zeros(ctx.hshape, order="F")
                 rh[1:-1, 1:-1, 1:-1] = r
@@ -292,7 +312,8 @@ def validate(net, vals, cap: int = 2000) -> int:
 
 
 def train(sizes=((64, 48), (128, 96)), steps=(1500, 12000), batch=(8, 4), lr=(2e-3, 1e-3),
-          seed: int = 0, eval_every: int = 500, verbose: bool = True, cne: bool = False):
+          seed: int = 0, eval_every: int = 500, verbose: bool = True, cne: bool = False,
+          rhs: str = "family"):
     """Training recipe of the stored weights: for each (n, structures) stage
     build pairs at n^3 (coarse n/4) and run Adam on the GPU (learning rate
     decayed to 0.3x and 0.1x over the last 40 % and 10 % of the stage); k_out
@@ -312,7 +333,7 @@ def train(sizes=((64, 48), (128, 96)), steps=(1500, 12000), batch=(8, 4), lr=(2e
     for (n, nseeds), st, b, eta in zip(sizes, steps, batch, lr):
         t0 = time.time()
         seeds = range(seed * 1000 + n, seed * 1000 + n + nseeds)
-        feats, errs, _ = make_pairs(n, seeds, verbose=verbose)
+        feats, errs, _ = make_pairs(n, seeds, verbose=verbose, rhs=rhs)
         if cne:
             f1, e1, _ = make_pairs(n, range(seed * 1000 + 500 + n, seed * 1000 + 500 + n + nseeds),
                                    verbose=verbose, form=1)
@@ -347,7 +368,7 @@ def train(sizes=((64, 48), (128, 96)), steps=(1500, 12000), batch=(8, 4), lr=(2e
     for ctx, *_ in vals:
         ctx.close()
     info = dict(sizes=np.array(sizes), steps=np.array(steps), batch=np.array(batch),
-                lr=np.array(lr), seed=seed, eval_every=eval_every, cne=cne,
+                lr=np.array(lr), seed=seed, eval_every=eval_every, cne=cne, rhs=rhs,
                 validation=np.array(VALIDATION),
                 validation_cne=np.array(VALIDATION_CNE if cne else []),
                 validation_iterations=np.array(val_hist),
@@ -361,8 +382,16 @@ def main(argv=None) -> None:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cne", action="store_true",
                     help="train on CnE-form systems too (the network then reads the mass channel)")
+    ap.add_argument("--recipe", default="shipped", choices=["shipped", "bv64"],
+                    help="shipped: the recipe of the stored weights (64^3 and 128^3 stages, "
+                         "right-hand sides of several spectra); bv64: 2,000 pairs from 200 "
+                         "structures of 64^3 with Butler-Volmer-like interface sources")
     a = ap.parse_args(argv)
-    net, info = train(seed=a.seed, cne=a.cne)
+    if a.recipe == "bv64":
+        net, info = train(sizes=((64, 200),), steps=(13500,), batch=(8,), lr=(1.5e-3,),
+                          seed=a.seed, cne=a.cne, rhs="bv")
+    else:
+        net, info = train(seed=a.seed, cne=a.cne)
     save(a.out, net, info)
     print("saved", a.out)
 
