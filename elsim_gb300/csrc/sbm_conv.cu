@@ -45,6 +45,12 @@ constexpr int NST = 8;                          // most pipeline stages (<= 7 ch
 constexpr int kChainMax = 5;                    // layers of one chain launch (sbm_conv.cuh)
 constexpr int kChainCtas = 16;                  // CTAs of the chain's one cluster
 constexpr int kChainBudget = 200 * 1024;        // stage memory of a chain CTA
+#ifndef SBM_CHAIN_TW
+#define SBM_CHAIN_TW 16
+#endif
+// output channels per item of a chain layer (16: more items, each CTA
+// copies a quarter of a 64-channel layer's weights; 64: fewer items)
+constexpr int kChainTw = SBM_CHAIN_TW;
 constexpr int kSmemBudget = 200 * 1024;         // stage memory of a lone CTA
 #ifndef SBM_CONV_WAVE_STAGES
 #define SBM_CONV_WAVE_STAGES 1
@@ -616,7 +622,9 @@ __global__ void __launch_bounds__(NTHR) k_conv3_chain(const __grid_constant__ Ch
       }
     }
     // the layer's outputs (generic-proxy stores) before the next layer's
-    // tensor-map (async-proxy) loads of them, in any CTA of the cluster
+    // tensor-map (async-proxy) loads of them, in any CTA of the cluster; the
+    // block barrier first reconverges thread 0 (the preload) with its warp
+    __syncthreads();
     asm volatile("fence.proxy.async.global;" ::: "memory");
     cluster_sync_all();
     asm volatile("fence.proxy.async.global;" ::: "memory");
@@ -866,12 +874,16 @@ int conv3_init() {
   return SBM_OK;
 }
 
-// Items (voxel tiles x output tiles of 64 channels), stages and stage bytes
-// of one chain layer.
+// Output channels per item of a chain layer.
+static int chain_tw(const ConvArgs& a) { return (a.wimg16 && kChainTw == 16) ? 16 : NT_MAX; }
+
+// Items (voxel tiles x output-channel tiles), stages and stage bytes of one
+// chain layer.
 static void chain_layer(const ConvArgs& a, int* tiles, int* items, int* nst, int* bytes) {
-  const int nt = std::min(a.cout, NT_MAX);
+  const int tw = chain_tw(a);
+  const int nt = std::min(a.cout, tw);
   *tiles = ((a.ny + TY - 1) / TY) * ((a.nx + TX - 1) / TX) * (a.nz / a.planes);
-  *items = *tiles * ((a.cout + NT_MAX - 1) / NT_MAX);
+  *items = *tiles * ((a.cout + tw - 1) / tw);
   const int stage = 2 * a_half_bytes(a.planes) + 27 * nt * 32;
   *nst = std::min(std::min(a.cin / KS, kChainBudget / stage), NST);
   *bytes = *nst * stage;
@@ -886,7 +898,8 @@ bool conv3_chain_usable(const ConvArgs* a, int n) {
         (a[L].offy % 8) || (a[L].offu % 8) || !a[L].wimg)
       return false;
     chain_layer(a[L], &tiles, &items, &nst, &bytes);
-    if (items > 2 * kChainCtas || nst < 1 || a[L].planes * std::min(a[L].cout, NT_MAX) > 128 ||
+    if (items > 2 * kChainCtas || nst < 1 ||
+        a[L].planes * std::min(a[L].cout, chain_tw(a[L])) > 128 ||
         a[L].skip != a[0].skip || a[L].skip2 != a[0].skip2)
       return false;
   }
@@ -900,7 +913,7 @@ int conv3_chain_launch(const ConvArgs* in, const ConvMap* const* maps, int n, cu
   for (int L = 0; L < n; ++L) {
     ConvArgs a = in[L];
     int bytes;
-    a.tw = NT_MAX;
+    a.tw = chain_tw(a);
     chain_layer(a, &c.tiles[L], &c.items[L], &a.nst, &bytes);
     bar = std::max(bar, bytes);
     c.a[L] = a;

@@ -487,6 +487,28 @@ int launch(Work& w, const ConvArgs& a, cudaStream_t s) {
 // output layer run in the convolution epilogues; activations that only the
 // backward pass reads (bottleneck and decoder outputs) are stored only
 // when training.
+// Layers of the forward pass (launch order E0..E4, D3..D0) that run as one
+// chain launch: kChainLen layers from kChainFirst (0 layers: none).
+#ifndef SBM_CHAIN_FIRST
+#define SBM_CHAIN_FIRST 3
+#endif
+#ifndef SBM_CHAIN_LEN
+#define SBM_CHAIN_LEN 3
+#endif
+constexpr int kChainFirst = SBM_CHAIN_FIRST, kChainLen = SBM_CHAIN_LEN;
+
+// The chain layers' arguments (planes: 2 where the epilogue pools and on
+// the 16-tile levels, 1 elsewhere); returns their number.
+int chain_args(const ConvArgs* a, ConvArgs* ch) {
+  for (int q = 0; q < kChainLen; ++q) {
+    const int l = kChainFirst + q;
+    ch[q] = a[l];
+    const int want = (a[l].pool || l == 2 || l == 6) ? 2 : 1;
+    ch[q].planes = (ch[q].nzs % want == 0) ? want : 1;
+  }
+  return kChainLen;
+}
+
 int forward(sbm_net* n, Work& w, bool tgt, const int* skip, const int* skip2, cudaStream_t s) {
   int rc;
   // the nine convolutions in launch order: E0..E3 (pooling), E4, D3..D0
@@ -514,24 +536,22 @@ int forward(sbm_net* n, Work& w, bool tgt, const int* skip, const int* skip2, cu
       d.out1x1 = w.out;
     }
   }
-  // The deep levels E2, E3, E4, D3, D2 (few CTAs per layer) run as one
-  // chain launch of one thread-block cluster when it fits: two planes where
-  // the epilogue pools (and on D2, whose level has as many tiles as E2's),
+  // The deep levels (few CTAs per layer) run as one chain launch of one
+  // thread-block cluster when it fits: layers [kChainFirst, kChainFirst +
+  // kChainLen) of the launch order, two planes where the epilogue pools,
   // one elsewhere.
-  ConvArgs ch[5] = {a[2], a[3], a[4], a[5], a[6]};
-  const int chain_planes[5] = {2, 2, 1, 1, 2};
-  for (int q = 0; q < 5; ++q)
-    ch[q].planes = (ch[q].nzs % chain_planes[q] == 0) ? chain_planes[q] : 1;
-  const bool chain = conv3_chain_usable(ch, 5);
+  ConvArgs ch[5];
+  const int nch = chain_args(a, ch);
+  const bool chain = nch > 0 && conv3_chain_usable(ch, nch);
   for (int q = 0; q < 9; ++q) {
-    if (chain && q >= 2 && q <= 6) {
-      if (q > 2) continue;
+    if (chain && q >= kChainFirst && q < kChainFirst + nch) {
+      if (q > kChainFirst) continue;
       const ConvMap* maps[5];
-      for (int c = 0; c < 5; ++c) {
+      for (int c = 0; c < nch; ++c) {
         maps[c] = map_for(w, ch[c]);
         if (!maps[c]) return SBM_ERR_STATE;
       }
-      if ((rc = conv3_chain_launch(ch, maps, 5, s))) return rc;
+      if ((rc = conv3_chain_launch(ch, maps, nch, s))) return rc;
       continue;
     }
     if ((rc = launch(w, a[q], s))) return rc;
@@ -545,17 +565,18 @@ int forward(sbm_net* n, Work& w, bool tgt, const int* skip, const int* skip2, cu
   return SBM_OK;
 }
 
-// Kernel launches of one forward pass of w (the deep levels' chain counts one).
+// Kernel launches of one forward pass of w (a chain counts one).
 int forward_launches(const sbm_net* n, const Work& w, const int* skip, const int* skip2) {
-  ConvArgs ch[5];
-  const int chain_planes[5] = {2, 2, 1, 1, 2};
-  const int lev[5] = {2, 3, 4, 3, 2};
-  const int lay[5] = {E2, E3, E4, D3, D2};
-  for (int q = 0; q < 5; ++q) {
-    ch[q] = layer_args(const_cast<sbm_net*>(n), w, lay[q], lev[q], w.in0, 16, q < 2, skip, skip2);
-    ch[q].planes = (ch[q].nzs % chain_planes[q] == 0) ? chain_planes[q] : 1;
+  ConvArgs a[9];
+  const int lev[9] = {0, 1, 2, 3, 4, 3, 2, 1, 0};
+  const int lay[9] = {E0, E1, E2, E3, E4, D3, D2, D1, D0};
+  for (int q = 0; q < 9; ++q) {
+    a[q] = layer_args(const_cast<sbm_net*>(n), w, lay[q], lev[q], w.in0, 16, q < 4, skip, skip2);
+    if (q < 4) a[q].pool = w.pin[lev[q] + 1];
   }
-  return conv3_chain_usable(ch, 5) ? 5 : 9;
+  ConvArgs ch[5];
+  const int nch = chain_args(a, ch);
+  return (nch > 0 && conv3_chain_usable(ch, nch)) ? 9 - nch + 1 : 9;
 }
 
 int wgrad(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx, const bf16* gy,
