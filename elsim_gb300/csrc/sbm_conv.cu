@@ -42,15 +42,6 @@ __host__ __device__ constexpr int a_half_bytes(int P) {
 }
 constexpr int NT_MAX = 64;                      // output channels per CTA (wide tiles)
 constexpr int NST = 8;                          // most pipeline stages (<= 7 chunks used)
-constexpr int kChainMax = 5;                    // layers of one chain launch (sbm_conv.cuh)
-constexpr int kChainCtas = 16;                  // CTAs of the chain's one cluster
-constexpr int kChainBudget = 200 * 1024;        // stage memory of a chain CTA
-#ifndef SBM_CHAIN_TW
-#define SBM_CHAIN_TW 16
-#endif
-// output channels per item of a chain layer (16: more items, each CTA
-// copies a quarter of a 64-channel layer's weights; 64: fewer items)
-constexpr int kChainTw = SBM_CHAIN_TW;
 constexpr int kSmemBudget = 200 * 1024;         // stage memory of a lone CTA
 #ifndef SBM_CONV_WAVE_STAGES
 #define SBM_CONV_WAVE_STAGES 1
@@ -238,125 +229,126 @@ __device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t 
   }
 }
 
-// Running phase counters of one CTA's stage barriers (thread 0's copy).
-// They persist across the items a CTA runs within one launch: stage s's
-// barriers have completed issued[s] / committed[s] phases once every load
-// landed and every commit arrived.
-struct StagePhases {
-  int issued[NST], landed[NST], committed[NST], freed[NST];
-};
-
-// Weight image of output tile jn of a convolution, and the bytes of one
-// chunk of it.
-__device__ __forceinline__ const __nv_bfloat16* conv_wsrc(const ConvArgs& a, int jn) {
-  return (a.tw == 16 ? a.wimg16 : a.wimg) + (int64_t)a.tw * jn * 27 * a.cin;
-}
-
-// Thread 0: the weight copies of the first `npre` chunks of item (., jn)
-// into the stage B slots (frozen weights), before the item's activation
-// loads arm the stages.
-__device__ __forceinline__ void conv_preload(const ConvArgs& a, int jn, unsigned char* sm,
-                                             uint64_t* full, int npre) {
-  const int P = a.planes;
-  const int ahalf = a_half_bytes(P);
-  const int nt = min(a.tw, a.cout - jn * a.tw);
-  const int bbytes = 27 * nt * 32;
-  const int stage_bytes = 2 * ahalf + bbytes;
-  const __nv_bfloat16* wsrc = conv_wsrc(a, jn);
-  for (int c = 0; c < npre; ++c) {
-    expect_tx_only(&full[c], bbytes);
-    bulk_load(sm + c * stage_bytes + 2 * ahalf, wsrc + (int64_t)c * 27 * nt * 16, bbytes,
-              &full[c]);
-  }
-}
-
-// One item of a convolution: output-channel tile jn of voxel tile `tile`
-// (TY x TX voxels in P planes).  Thread 0 loads (TMA) and issues the tap
-// MMAs over the NST-stage ring; every thread then waits for the item's
-// commit (`done`, phase done_phase) and runs the epilogue from the TMEM
-// accumulators.  `npre` chunks' weights were issued by conv_preload.
-// Returns false (the same in every thread) when a bounded wait expired;
-// the item's copies and MMAs still in flight are waited out (bounded) first.
-__device__ bool conv_item(const CUtensorMap* mx, const ConvArgs& a, int tile, int jn,
-                          unsigned char* sm, uint64_t* full, uint64_t* used, uint64_t* done,
-                          uint32_t tmem, int npre, StagePhases& ph, int done_phase) {
+__global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvMap m, ConvArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
   const int P = a.planes;  // z planes per CTA (1, 2 or 4), one accumulator each
   const int ahalf = a_half_bytes(P);
-  const int n0 = jn * a.tw;
+  const int n0 = blockIdx.y * a.tw;
   const int nt = min(a.tw, a.cout - n0);
   const int bbytes = 27 * nt * 32;
   const int stage_bytes = 2 * ahalf + bbytes;
   const int nchunk = a.cin / KS;
   const int nst = a.nst;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);
+  uint64_t* used = full + NST;
+  uint64_t* done = used + NST;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int nty = (a.ny + TY - 1) / TY, ntx = (a.nx + TX - 1) / TX;
-  const int ty = tile % nty;
-  const int tx = (tile / nty) % ntx;
-  const int z0 = (tile / (nty * ntx)) * P;
+  const int ty = blockIdx.x % nty;
+  const int tx = (blockIdx.x / nty) % ntx;
+  const int z0 = (blockIdx.x / (nty * ntx)) * P;
   const int y0 = ty * TY, x0 = tx * TX;
   const int zl = z0 % a.nzs, sample = z0 / a.nzs;
-  const __nv_bfloat16* wsrc = conv_wsrc(a, jn);
+  const int ncols = P * nt <= 32 ? 32 : (P * nt <= 64 ? 64 : (P * nt <= 128 ? 128 : 256));
+  // Set-up that reads nothing the preceding kernels write runs before
+  // griddepcontrol.wait, overlapping their tail: the barriers, the
+  // tensor-map prefetch and, when the weights are frozen (a.wpre), the
+  // weight copies of the first stages.  Tensor memory is allocated only
+  // after the wait: a CTA waiting on an earlier grid holds none, so it can
+  // never keep a CTA of that grid from allocating.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  const __nv_bfloat16* wsrc =
+      (a.tw == 16 ? a.wimg16 : a.wimg) + (int64_t)a.tw * blockIdx.y * 27 * a.cin;
+  const int npre = a.wpre ? min(nchunk, nst) : 0;  // chunks whose weights are already on the way
+  if (tid == 0) {
+    for (int s = 0; s < 2 * NST + 1; ++s) mb_init(&full[s]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&m.x)) : "memory");
+    for (int c = 0; c < npre; ++c) {
+      expect_tx_only(&full[c], bbytes);
+      bulk_load(sm + c * stage_bytes + 2 * ahalf, wsrc + (int64_t)c * 27 * nt * 16, bbytes,
+                &full[c]);
+    }
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if ((a.skip && *a.skip) || (a.skip2 && *a.skip2)) {
+    // the flag is the same for every thread; the copies in flight land
+    // before the CTA exits
+    if (tid == 0) {
+      for (int c = 0; c < npre; ++c) {
+        mb_arrive(&full[c]);
+        mb_wait(&full[c], 0);
+      }
+    }
+    return;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     sa(tslot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
   bool ok = true;
   if (tid == 0) {
     const uint32_t id = idesc_bf16(nt), id2 = idesc_bf16(2 * nt), id3 = idesc_bf16(3 * nt);
     const unsigned abox = (unsigned)(HY * HX * (P + 2) * 16);
+    int issued[NST] = {}, landed[NST] = {}, committed[NST] = {}, freed[NST] = {};
     auto load = [&](int c, int s) {
       unsigned char* A = sm + s * stage_bytes;
-      const bool pre = c < npre;  // weights already issued
+      const bool pre = c < npre;  // weights issued before the wait
       expect_tx(&full[s], 2 * abox + (pre ? 0u : (unsigned)bbytes));
       const int grp = (a.offx + c * KS) >> 3;
-      tma_load5(A, mx, &full[s], 8 * (y0 - 1), x0 - 1, zl - 1, sample, grp);
-      tma_load5(A + ahalf, mx, &full[s], 8 * (y0 - 1), x0 - 1, zl - 1, sample, grp + 1);
+      tma_load5(A, &m.x, &full[s], 8 * (y0 - 1), x0 - 1, zl - 1, sample, grp);
+      tma_load5(A + ahalf, &m.x, &full[s], 8 * (y0 - 1), x0 - 1, zl - 1, sample, grp + 1);
       if (!pre) bulk_load(A + 2 * ahalf, wsrc + (int64_t)c * 27 * nt * 16, bbytes, &full[s]);
-      ++ph.issued[s];
+      ++issued[s];
     };
     for (int c = 0; c < nchunk && c < nst; ++c) load(c, c);
     for (int c = 0; c < nchunk; ++c) {
       const int s = c % nst;
-      if (!mb_wait(&full[s], (unsigned)(ph.landed[s] & 1))) {
+      if (!mb_wait(&full[s], (unsigned)(landed[s] & 1))) {
         ok = false;
         break;
       }
-      ++ph.landed[s];
+      ++landed[s];
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t A = sa(sm + s * stage_bytes);
       const uint64_t ad = umma_desc(A, ahalf, HY * 16);
       const uint64_t bd = umma_desc(A + 2 * ahalf, 128, 256);
       issue_taps(tmem, ad, bd, nt, P, id, id2, id3, c > 0);
       tc_commit(&used[s]);
-      ++ph.committed[s];
+      ++committed[s];
       if (c + nst < nchunk) {
         // the stage is reloaded once its MMAs have read it
-        if (!mb_wait(&used[s], (unsigned)(ph.freed[s] & 1))) {
+        if (!mb_wait(&used[s], (unsigned)(freed[s] & 1))) {
           ok = false;
           break;
         }
-        ++ph.freed[s];
+        ++freed[s];
         load(c + nst, s);
       }
     }
-    if (ok) tc_commit(done);
-    // Every load of the item lands and every commit of its stages arrives
-    // before the stages are used again (bounded waits; after an expired wait
-    // this is the drain of the copies and MMAs still in flight).
-    for (int s = 0; s < nst; ++s) {
-      for (; ph.landed[s] < ph.issued[s]; ++ph.landed[s])
-        mb_wait(&full[s], (unsigned)(ph.landed[s] & 1));
-      if (ok) continue;  // the used phases are waited after the done commit
-      for (; ph.freed[s] < ph.committed[s]; ++ph.freed[s])
-        mb_wait(&used[s], (unsigned)(ph.freed[s] & 1));
+    if (ok) {
+      tc_commit(done);
+    } else {
+      // bounded drain of the copies and MMAs still in flight
+      for (int s = 0; s < nst; ++s) {
+        for (; landed[s] < issued[s]; ++landed[s]) mb_wait(&full[s], (unsigned)(landed[s] & 1));
+        for (; freed[s] < committed[s]; ++freed[s]) mb_wait(&used[s], (unsigned)(freed[s] & 1));
+      }
     }
   }
   ok = __syncthreads_and(ok);
-  ok = ok && mb_wait(done, (unsigned)(done_phase & 1));
+  ok = ok && mb_wait(done, 0);
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (tid == 0 && ok) {
-    for (int s = 0; s < nst; ++s)
-      for (; ph.freed[s] < ph.committed[s]; ++ph.freed[s])
-        mb_wait(&used[s], (unsigned)(ph.freed[s] & 1));
-  }
   if (ok) {
     const unsigned FULL = 0xffffffffu;
     const int64_t V = (int64_t)a.ny * a.nx * a.nz;
@@ -447,199 +439,10 @@ __device__ bool conv_item(const CUtensorMap* mx, const ConvArgs& a, int tile, in
   } else if (tid == 0) {
     atomicExch(a.err, 1);
   }
-  return ok;
-}
-
-__global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvMap m, ConvArgs a) {
-  extern __shared__ __align__(1024) unsigned char sm[];
-  const int P = a.planes;
-  const int ahalf = a_half_bytes(P);
-  const int jn = blockIdx.y;
-  const int nt = min(a.tw, a.cout - jn * a.tw);
-  const int stage_bytes = 2 * ahalf + 27 * nt * 32;
-  const int nchunk = a.cin / KS;
-  const int nst = a.nst;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + nst * stage_bytes);
-  uint64_t* used = full + NST;
-  uint64_t* done = used + NST;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5;
-  const int ncols = P * nt <= 32 ? 32 : (P * nt <= 64 ? 64 : (P * nt <= 128 ? 128 : 256));
-  // Set-up that reads nothing the preceding kernels write runs before
-  // griddepcontrol.wait, overlapping their tail: the barriers, the
-  // tensor-map prefetch and, when the weights are frozen (a.wpre), the
-  // weight copies of the first stages.  Tensor memory is allocated only
-  // after the wait: a CTA waiting on an earlier grid holds none, so it can
-  // never keep a CTA of that grid from allocating.
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  const int npre = a.wpre ? min(nchunk, nst) : 0;  // chunks whose weights are already on the way
-  if (tid == 0) {
-    for (int s = 0; s < 2 * NST + 1; ++s) mb_init(&full[s]);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&m.x)) : "memory");
-    conv_preload(a, jn, sm, full, npre);
-  }
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  if ((a.skip && *a.skip) || (a.skip2 && *a.skip2)) {
-    // the flag is the same for every thread; the copies in flight land
-    // before the CTA exits
-    if (tid == 0) {
-      for (int c = 0; c < npre; ++c) {
-        mb_arrive(&full[c]);
-        mb_wait(&full[c], 0);
-      }
-    }
-    return;
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     sa(tslot)),
-                 "r"(ncols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tslot;
-  StagePhases ph = {};
-  conv_item(&m.x, a, blockIdx.x, jn, sm, full, used, done, tmem, npre, ph, 0);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols)
-                 : "memory");
-}
-
-// A chain of small convolutions (the U-Net's deep levels) in ONE launch of
-// one thread-block cluster: layer after layer, each CTA of the cluster
-// runs the items (voxel tile x output-channel tile) rank, rank + CTAs, ...
-// of the layer, then the cluster barrier (release / acquire) makes the
-// layer's outputs visible to the next layer's tensor-map loads.  The
-// cluster's CTAs are scheduled together, so the barrier never waits on a
-// CTA that is not resident.  Tensor memory is allocated once; the stage
-// barriers' phases run on across items, and each item's first weight
-// chunks are copied while the previous layer finishes (frozen weights).
-struct ChainArgs {
-  ConvMap map[kChainMax];
-  ConvArgs a[kChainMax];
-  int items[kChainMax];  // voxel tiles x output-channel tiles of each layer
-  int tiles[kChainMax];  // voxel tiles of each layer
-  int nlayer;
-  int bar_off;           // byte offset of the barriers in dynamic shared memory
-};
-
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-__global__ void __launch_bounds__(NTHR) k_conv3_chain(const __grid_constant__ ChainArgs c) {
-  extern __shared__ __align__(1024) unsigned char sm[];
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + c.bar_off);
-  uint64_t* used = full + NST;
-  uint64_t* done = used + NST;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5;
-  const int rank = blockIdx.x, ncta = gridDim.x;  // the grid is one cluster
-  constexpr int kCols = 128;                      // P * nt <= 128 for every chain layer
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  // the first item of this CTA and its preloaded weight chunks
-  auto first_npre = [&](int L) { return c.a[L].wpre ? min(c.a[L].cin / KS, c.a[L].nst) : 0; };
-  int npre = 0;
-  if (tid == 0) {
-    for (int s = 0; s < 2 * NST + 1; ++s) mb_init(&full[s]);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    for (int L = 0; L < c.nlayer; ++L)
-      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&c.map[L].x))
-                   : "memory");
-    if (rank < c.items[0]) {
-      npre = first_npre(0);
-      conv_preload(c.a[0], rank / c.tiles[0], sm, full, npre);
-    }
-  }
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  const ConvArgs& a0 = c.a[0];
-  if ((a0.skip && *a0.skip) || (a0.skip2 && *a0.skip2)) {
-    // every CTA of the cluster sees the same flag and leaves here
-    if (tid == 0) {
-      for (int q = 0; q < npre; ++q) {
-        mb_arrive(&full[q]);
-        mb_wait(&full[q], 0);
-      }
-    }
-    return;
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     sa(tslot)),
-                 "r"(kCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tslot;
-  StagePhases ph = {};
-  int done_phase = 0;
-  bool ok = true;
-  for (int L = 0; L < c.nlayer; ++L) {
-    const ConvArgs& a = c.a[L];
-    for (int it = rank; it < c.items[L]; it += ncta) {
-      if (ok) {
-        ok = conv_item(&c.map[L].x, a, it % c.tiles[L], it / c.tiles[L], sm, full, used, done,
-                       tmem, npre, ph, done_phase);
-        ++done_phase;
-      }
-      npre = 0;
-      // the next item of this CTA (this layer or a later one) gets its first
-      // weight chunks now: the stages are idle
-      if (ok && tid == 0) {
-        int nL = L, nit = it + ncta;
-        while (nL < c.nlayer && nit >= c.items[nL]) {
-          ++nL;
-          nit = rank;
-        }
-        if (nL < c.nlayer) {
-          npre = first_npre(nL);
-          conv_preload(c.a[nL], nit / c.tiles[nL], sm, full, npre);
-        }
-      }
-    }
-    if (tid == 0 && c.items[L] <= rank) {
-      // no item of this layer here: the preload for a later layer is issued
-      // by the loop above only after an item, so issue it now
-      if (ok && npre == 0) {
-        int nL = L + 1;
-        while (nL < c.nlayer && c.items[nL] <= rank) ++nL;
-        if (nL < c.nlayer && nL == L + 1) {
-          npre = first_npre(nL);
-          conv_preload(c.a[nL], rank / c.tiles[nL], sm, full, npre);
-        }
-      }
-    }
-    // the layer's outputs (generic-proxy stores) before the next layer's
-    // tensor-map (async-proxy) loads of them, in any CTA of the cluster; the
-    // block barrier first reconverges thread 0 (the preload) with its warp
-    __syncthreads();
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-    cluster_sync_all();
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-  }
-  if (tid == 0 && npre > 0) {
-    // a preload whose item never ran (an expired wait stopped the chain)
-    for (int q = 0; q < npre; ++q) {
-      mb_arrive(&full[q]);
-      mb_wait(&full[q], (unsigned)(ph.landed[q] & 1));
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols)
                  : "memory");
 }
 
@@ -834,11 +637,6 @@ bool conv_shape_ok(int cin, int cout) {
   return cin >= 16 && cin % 16 == 0 && cout >= 16 && cout % 16 == 0 && cout <= 256;
 }
 
-namespace {
-int g_chain_ok = -1;  // the one-cluster chain kernel fits this device (checked once)
-size_t chain_smem() { return (size_t)kChainBudget + (2 * NST + 1) * 8 + 16 + 128; }
-}  // namespace
-
 int conv3_init() {
   static bool done = false;
   if (done) return SBM_OK;
@@ -846,101 +644,7 @@ int conv3_init() {
                                     (int)(kSmemBudget + 1024)));
   SBM_CUDA_TRY(cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)conv_smem(256)));
-  // the chain kernel: one cluster of kChainCtas CTAs (a non-portable size on
-  // some parts); used only when the device can hold such a cluster
-  g_chain_ok = 0;
-  if (cudaFuncSetAttribute(k_conv3_chain, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)chain_smem()) == cudaSuccess &&
-      cudaFuncSetAttribute(k_conv3_chain, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
-          cudaSuccess) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kChainCtas);
-    cfg.blockDim = dim3(NTHR);
-    cfg.dynamicSmemBytes = chain_smem();
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kChainCtas;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, k_conv3_chain, &cfg) == cudaSuccess &&
-        nclusters >= 1)
-      g_chain_ok = 1;
-  }
-  cudaGetLastError();  // a refused attribute is not an error of the library
   done = true;
-  return SBM_OK;
-}
-
-// Output channels per item of a chain layer.
-static int chain_tw(const ConvArgs& a) { return (a.wimg16 && kChainTw == 16) ? 16 : NT_MAX; }
-
-// Items (voxel tiles x output-channel tiles), stages and stage bytes of one
-// chain layer.
-static void chain_layer(const ConvArgs& a, int* tiles, int* items, int* nst, int* bytes) {
-  const int tw = chain_tw(a);
-  const int nt = std::min(a.cout, tw);
-  *tiles = ((a.ny + TY - 1) / TY) * ((a.nx + TX - 1) / TX) * (a.nz / a.planes);
-  *items = *tiles * ((a.cout + tw - 1) / tw);
-  const int stage = 2 * a_half_bytes(a.planes) + 27 * nt * 32;
-  *nst = std::min(std::min(a.cin / KS, kChainBudget / stage), NST);
-  *bytes = *nst * stage;
-}
-
-bool conv3_chain_usable(const ConvArgs* a, int n) {
-  if (g_chain_ok != 1 || n < 1 || n > kChainMax) return false;
-  for (int L = 0; L < n; ++L) {
-    int tiles, items, nst, bytes;
-    if ((a[L].planes != 1 && a[L].planes != 2) || (a[L].nzs % a[L].planes) ||
-        (a[L].pool && a[L].planes != 2) || a[L].w1x1 || (a[L].ldx % 8) || (a[L].offx % 8) ||
-        (a[L].offy % 8) || (a[L].offu % 8) || !a[L].wimg)
-      return false;
-    chain_layer(a[L], &tiles, &items, &nst, &bytes);
-    if (items > 2 * kChainCtas || nst < 1 ||
-        a[L].planes * std::min(a[L].cout, chain_tw(a[L])) > 128 ||
-        a[L].skip != a[0].skip || a[L].skip2 != a[0].skip2)
-      return false;
-  }
-  return true;
-}
-
-int conv3_chain_launch(const ConvArgs* in, const ConvMap* const* maps, int n, cudaStream_t s) {
-  if (!conv3_chain_usable(in, n)) return SBM_ERR_STATE;
-  ChainArgs c{};
-  int bar = 0;
-  for (int L = 0; L < n; ++L) {
-    ConvArgs a = in[L];
-    int bytes;
-    a.tw = chain_tw(a);
-    chain_layer(a, &c.tiles[L], &c.items[L], &a.nst, &bytes);
-    bar = std::max(bar, bytes);
-    c.a[L] = a;
-    c.map[L] = *maps[L];
-  }
-  c.nlayer = n;
-  c.bar_off = (bar + 127) / 128 * 128;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kChainCtas);
-  cfg.blockDim = dim3(NTHR);
-  cfg.dynamicSmemBytes = (size_t)c.bar_off + (2 * NST + 1) * 8 + 16;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[2];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kChainCtas;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[1].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 2;
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, k_conv3_chain, c);
-  if (e != cudaSuccess) {
-    set_error("k_conv3_chain launch", e);
-    return SBM_ERR_CUDA;
-  }
-  SBM_LAUNCHED(1);
   return SBM_OK;
 }
 

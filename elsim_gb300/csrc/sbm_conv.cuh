@@ -115,16 +115,6 @@ __host__ __device__ inline int64_t wimage_index(int co, int t, int ci, int cout,
 // use_tc = 1: tcgen05 kernel (needs a.wimg and a map, encoded here when m
 // is null); 0: CUDA-core reference kernel (a.w).
 int conv3_launch(const ConvArgs* a, const ConvMap* m, int use_tc, cudaStream_t s);
-// n <= 5 convolutions, each reading the previous ones' outputs, in one
-// launch of one thread-block cluster of 16 CTAs (layer by layer, a cluster
-// barrier between them): the U-Net's deep levels, whose few CTAs per layer
-// leave the separate launches latency-bound.  Usable when the device holds
-// such a cluster, every layer has at most 32 items (voxel tiles x 64-channel
-// output tiles), planes 1 or 2 (2 where the epilogue pools), no fused 1x1
-// head, and every layer has the same skip flags; maps[L] = the tensor map
-// of layer L's input with its plane count.
-bool conv3_chain_usable(const ConvArgs* a, int n);
-int conv3_chain_launch(const ConvArgs* a, const ConvMap* const* maps, int n, cudaStream_t s);
 int wgrad_launch(const WgradArgs* a, cudaStream_t s);
 
 }  // namespace sbm

@@ -487,74 +487,35 @@ int launch(Work& w, const ConvArgs& a, cudaStream_t s) {
 // output layer run in the convolution epilogues; activations that only the
 // backward pass reads (bottleneck and decoder outputs) are stored only
 // when training.
-// Layers of the forward pass (launch order E0..E4, D3..D0) that run as one
-// chain launch: kChainLen layers from kChainFirst (0 layers: none).
-#ifndef SBM_CHAIN_FIRST
-#define SBM_CHAIN_FIRST 3
-#endif
-#ifndef SBM_CHAIN_LEN
-#define SBM_CHAIN_LEN 3
-#endif
-constexpr int kChainFirst = SBM_CHAIN_FIRST, kChainLen = SBM_CHAIN_LEN;
-
-// The chain layers' arguments (planes: 2 where the epilogue pools and on
-// the 16-tile levels, 1 elsewhere); returns their number.
-int chain_args(const ConvArgs* a, ConvArgs* ch) {
-  for (int q = 0; q < kChainLen; ++q) {
-    const int l = kChainFirst + q;
-    ch[q] = a[l];
-    const int want = (a[l].pool || l == 2 || l == 6) ? 2 : 1;
-    ch[q].planes = (ch[q].nzs % want == 0) ? want : 1;
-  }
-  return kChainLen;
-}
-
 int forward(sbm_net* n, Work& w, bool tgt, const int* skip, const int* skip2, cudaStream_t s) {
   int rc;
-  // the nine convolutions in launch order: E0..E3 (pooling), E4, D3..D0
-  ConvArgs a[9];
   for (int lev = 0; lev < 4; ++lev) {
     const int l = kEnc[lev];
-    a[lev] = layer_args(n, w, l, lev, lev == 0 ? w.in0 : w.pin[lev], kCi[l], true, skip, skip2);
-    a[lev].y16 = w.cat[lev];
-    a[lev].offy = kUpW[lev];
-    a[lev].pool = w.pin[lev + 1];
+    ConvArgs a =
+        layer_args(n, w, l, lev, lev == 0 ? w.in0 : w.pin[lev], kCi[l], true, skip, skip2);
+    a.y16 = w.cat[lev];
+    a.offy = kUpW[lev];
+    a.pool = w.pin[lev + 1];
+    if ((rc = launch(w, a, s))) return rc;
   }
-  a[4] = layer_args(n, w, E4, 4, w.pin[4], kCi[E4], false, skip, skip2);
-  a[4].y16 = w.train ? w.a4 : nullptr;
-  a[4].up = w.cat[3];
+  {
+    ConvArgs a = layer_args(n, w, E4, 4, w.pin[4], kCi[E4], false, skip, skip2);
+    a.y16 = w.train ? w.a4 : nullptr;
+    a.up = w.cat[3];
+    if ((rc = launch(w, a, s))) return rc;
+  }
   for (int lev = 3; lev >= 0; --lev) {
     const int l = kDec[lev];
-    ConvArgs& d = a[8 - lev];
-    d = layer_args(n, w, l, lev, w.cat[lev], kCatW[lev], false, skip, skip2);
-    d.y16 = w.train ? w.dec[lev] : nullptr;
+    ConvArgs a = layer_args(n, w, l, lev, w.cat[lev], kCatW[lev], false, skip, skip2);
+    a.y16 = w.train ? w.dec[lev] : nullptr;
     if (lev > 0) {
-      d.up = w.cat[lev - 1];
+      a.up = w.cat[lev - 1];
     } else {
-      d.w1x1 = n->w32 + kL.off[OUT];
-      d.b1x1 = n->w32 + kL.boff[OUT];
-      d.out1x1 = w.out;
+      a.w1x1 = n->w32 + kL.off[OUT];
+      a.b1x1 = n->w32 + kL.boff[OUT];
+      a.out1x1 = w.out;
     }
-  }
-  // The deep levels (few CTAs per layer) run as one chain launch of one
-  // thread-block cluster when it fits: layers [kChainFirst, kChainFirst +
-  // kChainLen) of the launch order, two planes where the epilogue pools,
-  // one elsewhere.
-  ConvArgs ch[5];
-  const int nch = chain_args(a, ch);
-  const bool chain = nch > 0 && conv3_chain_usable(ch, nch);
-  for (int q = 0; q < 9; ++q) {
-    if (chain && q >= kChainFirst && q < kChainFirst + nch) {
-      if (q > kChainFirst) continue;
-      const ConvMap* maps[5];
-      for (int c = 0; c < nch; ++c) {
-        maps[c] = map_for(w, ch[c]);
-        if (!maps[c]) return SBM_ERR_STATE;
-      }
-      if ((rc = conv3_chain_launch(ch, maps, nch, s))) return rc;
-      continue;
-    }
-    if ((rc = launch(w, a[q], s))) return rc;
+    if ((rc = launch(w, a, s))) return rc;
   }
   if (tgt) {
     const int64_t V = w.d[0].v();
@@ -563,20 +524,6 @@ int forward(sbm_net* n, Work& w, bool tgt, const int* skip, const int* skip2, cu
   }
   SBM_CUDA_TRY(cudaGetLastError());
   return SBM_OK;
-}
-
-// Kernel launches of one forward pass of w (a chain counts one).
-int forward_launches(const sbm_net* n, const Work& w, const int* skip, const int* skip2) {
-  ConvArgs a[9];
-  const int lev[9] = {0, 1, 2, 3, 4, 3, 2, 1, 0};
-  const int lay[9] = {E0, E1, E2, E3, E4, D3, D2, D1, D0};
-  for (int q = 0; q < 9; ++q) {
-    a[q] = layer_args(const_cast<sbm_net*>(n), w, lay[q], lev[q], w.in0, 16, q < 4, skip, skip2);
-    if (q < 4) a[q].pool = w.pin[lev[q] + 1];
-  }
-  ConvArgs ch[5];
-  const int nch = chain_args(a, ch);
-  return (nch > 0 && conv3_chain_usable(ch, nch)) ? 9 - nch + 1 : 9;
 }
 
 int wgrad(sbm_net* n, const Work& w, int l, int lev, const bf16* x, int ldx, const bf16* gy,
@@ -1209,10 +1156,7 @@ void net_pc_rc_strides(sbm_ctx* ctx, int* sy, int* sx) {
 }
 float* net_pc_scal(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->scal; }
 
-int net_pc_nodes(sbm_ctx* ctx) {
-  const netd::NetPc* pc = static_cast<const netd::NetPc*>(ctx->net);
-  return 3 + netd::forward_launches(pc->net, *pc->w, nullptr, nullptr);
-}
+int net_pc_nodes() { return 3 + 9; }
 
 // The multiplicative step: tiles of 64 x 8 x 4 fine cells (the last y tile
 // may be partial), one wave of resident blocks (3 per SM at 80 registers)

@@ -33,8 +33,8 @@ float* net_pc_rc(sbm_ctx* ctx);
 // y and x strides of the coarse arrays (R r is stored with them)
 void net_pc_rc_strides(sbm_ctx* ctx, int* sy, int* sx);
 float* net_pc_scal(sbm_ctx* ctx);
-// Kernel launches of one net_pc_launch (after net_pc_begin).
-int net_pc_nodes(sbm_ctx* ctx);
+// Kernel launches of one net_pc_launch.
+int net_pc_nodes();
 // One part of net_pc_launch for timing: 0 = the 9 U-Net convolutions on the
 // current input, 1 = the multiplicative prolongation / Jacobi step.
 void net_pc_launch_part(sbm_ctx* ctx, int part, const float* r32, const float* iv32,

@@ -1288,7 +1288,7 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
              sp.form, sp.bcx0, sp.bcx1, vec * 16 + zc32, pc, sh64.zc, clen);
   cudaGraphExec_t ex = nullptr;
   int nodes = 0;
-  rc = capture_graph(ctx, key, learned ? 2 * (3 + net_pc_nodes(ctx)) : 6, body, &ex, &nodes, clen);
+  rc = capture_graph(ctx, key, learned ? 2 * (3 + net_pc_nodes()) : 6, body, &ex, &nodes, clen);
   if (rc) return rc;
   ctx->last_op32 = op32;
   ctx->last_pc = pc ? 1 : 0;
