@@ -52,9 +52,9 @@ SEED = 1
 TOL = 1e-8
 METRIC = "sbm_potential_solve_time_256^3_relres_1e-8"
 # dram__bytes_read.sum + dram__bytes_write.sum of one k32t_apply_dir launch
-# at 256^3 (ncu): with the Jacobi read (Jacobi-PCG) and without it (flexible
-# CG with the learned preconditioner).
-APPLY_TRAFFIC = {1: 398.2e6, 2: 326.2e6}
+# at 256^3 (ncu): with the Jacobi read (Jacobi-PCG); the flexible-CG variant
+# (learned preconditioner) is not captured yet.
+APPLY_TRAFFIC = {1: 398.2e6}
 # dram__bytes_read.sum + dram__bytes_write.sum of the 9 k_conv3_tc launches
 # of one preconditioner application at 256^3 (ncu)
 CONV_TRAFFIC = 41.56e6
@@ -521,11 +521,11 @@ def run_ours(args):
     # the learned preconditioner, its parts (the U-Net convolutions are the
     # dominant kernel of that solve: tensor roofline)
     ms_k, bytes_k = ctx.bench_kernel(0, 20)
+    peak, peak_kind = _peaks()
     extra = {}
     roofline = None
     if used_pc == sbm.PC_LEARNED:
         ms_pc, bytes_pc = ctx.bench_kernel(3, 20)
-        ms_u, bytes_u = ctx.bench_kernel(4, 20)
         ms_cv, _ = ctx.bench_kernel(5, 20)
         ms_m, bytes_m = ctx.bench_kernel(6, 20)
         fl = unet_flops(n)
@@ -538,8 +538,10 @@ def run_ours(args):
             "note": "the convolutions are latency / shared-memory bound (small N, few CTAs on "
                     "the coarse levels), far from the tensor peak"}
         extra["multiplicative_step_kernel"] = {
-            "kernel": "k_pc_mult_tiled", "ms": ms_m,
-            "GB/s": bytes_m / (ms_m * 1e-3) / 1e9, "bound": "hbm"}
+            "kernel": "k_pc_mult_tiled (r -= alpha q, z = z1 + omega D^-1 (r - A z1), z.r, "
+                      "z.q_old, r.r)", "ms": ms_m,
+            "GB/s": bytes_m / (ms_m * 1e-3) / 1e9, "frac": bytes_m / (ms_m * 1e-3) / 1e9 / peak,
+            "bound": "hbm"}
         # the dominant kernel of the solve (32 % of its time over 9 launches
         # per iteration): the U-Net convolutions on the tensor cores
         ach = fl / (ms_cv * 1e-3) / 1e12
@@ -550,10 +552,11 @@ def run_ours(args):
                     "ms": ms_cv}
     else:
         ms_u, bytes_u = ctx.bench_kernel(1, 20)
-    peak, peak_kind = _peaks()
+        extra["update_kernel"] = {"ms": ms_u, "GB/s": bytes_u / (ms_u * 1e-3) / 1e9}
     achieved = bytes_k / (ms_k * 1e-3) / 1e9
     apply_roofline = {"bound": "hbm", "kernel": "k32t_apply_dir (TMA-staged FP32 direction+stencil)"
-                      + (", no Jacobi read (flexible CG)" if used_pc == sbm.PC_LEARNED else ""),
+                      + (", flexible-CG variant: no Jacobi read, the deferred x32 += alpha p_old "
+                         "and R q in the same pass" if used_pc == sbm.PC_LEARNED else ""),
                       "achieved": achieved, "peak": peak, "unit": "GB/s",
                       "frac": achieved / peak, "peak_kind": peak_kind,
                       # DRAM read+write of one launch (ncu capture of the same variant)
@@ -658,7 +661,6 @@ def run_ours(args):
                 "speedup_vs_jacobi_pcg": jac_s / value,
                 "voxel_updates_per_s": n ** 3 * info["iters"] / value,
                 "wall_s_timed_region": wall,
-                "update_kernel": {"ms": ms_u, "GB/s": bytes_u / (ms_u * 1e-3) / 1e9},
                 **extra,
                 "direction_stencil_kernel": apply_roofline,
                 "fp64_stencil_kernel": {"ms": fp64_ms[0],

@@ -248,6 +248,23 @@ struct OpArgs {
   const T* fc = nullptr;
 };
 
+// Extra operands of the flexible-CG direction kernel (learned
+// preconditioner).  That kernel also applies the previous iteration's
+// deferred x32 += alpha p_old (or, after a residual replacement, folds x32
+// into d64 first) and restricts q = A p_new to the coarse grid (rq = 4x4x4
+// means, strides rcy / rcx of the coarse arrays), so that neither x nor the
+// restriction of the residual needs a pass of its own.
+struct FcgDirArgs {
+  float* x32 = nullptr;       // FP32 correction (g32 layout)
+  double* d64 = nullptr;      // FP64 correction (g64 layout)
+  Geo g64{};
+  const float* rc = nullptr;  // R r of the current residual (coarse)
+  float* rq = nullptr;        // R q of the new direction (coarse, written)
+  float* scal = nullptr;      // s = RMS(R r_next), 1/s (written by the last block)
+  int rcy = 0, rcx = 0;       // y and x strides of the coarse arrays
+  int64_t ncell = 0;          // valid coarse cells
+};
+
 // face_sum with stored faces: the same operands and order, so the same bits.
 template <typename T>
 __device__ __forceinline__ T face_sum_stored(const Geo& g, const T* __restrict__ fc, int64_t c,

@@ -741,12 +741,15 @@ __global__ void k_pc_feat(Dims c, Dims cv, const float* __restrict__ coefc,
   }
 }
 
-// rc = R r (4x4x4 means of the FP32 residual), s = RMS(rc); only when the
-// update kernel has not produced them (first use, residual replacement).
+// rc = R r (4x4x4 means of the FP32 residual) when it is stale (first use,
+// residual replacement); s = RMS(rc - alpha rq), the scale of the next U-Net
+// input (the pack kernel that follows applies the pending alpha rq).
 __global__ void k_pc_restrict(Geo g, Dims c, Dims cv, const float* __restrict__ r,
-                              float* __restrict__ rc, double* partials, float* scal, CgState* st) {
+                              float* __restrict__ rc, const float* __restrict__ rq,
+                              double* partials, float* scal, CgState* st) {
   pdl_begin();
   if (st->done || st->pc_off || st->aux[1] != 0.0) return;
+  const float alpha = (float)st->alpha;
   double acc = 0.0;
   NET_LOOP(cv.v()) {
     int i, j, k;
@@ -759,8 +762,10 @@ __global__ void k_pc_restrict(Geo g, Dims c, Dims cv, const float* __restrict__ 
         s += (v.x + v.y) + (v.z + v.w);
       }
     const float m = s * (1.f / 64.f);
-    rc[vid(c, i, j, k)] = m;
-    acc += (double)m * (double)m;
+    const int64_t tc = vid(c, i, j, k);
+    rc[tc] = m;
+    const float mn = m - alpha * rq[tc];
+    acc += (double)mn * (double)mn;
   }
   double v[1] = {acc}, tot[1];
   if (grid_reduce<1>(v, partials, &st->counter[4], tot)) {
@@ -768,16 +773,73 @@ __global__ void k_pc_restrict(Geo g, Dims c, Dims cv, const float* __restrict__ 
       const double s = sqrt(tot[0] / (double)cv.v());
       scal[0] = (float)s;
       scal[1] = s > 0.0 ? (float)(1.0 / s) : 0.f;
+      st->aux[1] = 1.0;  // rc holds R r of the current residual
     }
   }
 }
 
-__global__ void k_pc_pack(int64_t V, const float* __restrict__ rc, const float* scal,
-                          bf16* __restrict__ in0, const CgState* st) {
+// rc -= alpha rq (R r of the updated residual, alpha the step the
+// preconditioner kernel that follows applies to r), the U-Net's residual
+// channel rc / s, and |rc|^2 (aux[2]) for the next scale.
+__global__ void k_pc_pack(int64_t V, float* __restrict__ rc, const float* __restrict__ rq,
+                          const float* scal, bf16* __restrict__ in0, double* partials,
+                          CgState* st) {
   pdl_begin();
   if (st->done || st->pc_off) return;
   const float inv = scal[1];
-  NET_LOOP(V) in0[act_index(t, 0, V)] = __float2bfloat16_rn(rc[t] * inv);
+  const float alpha = (float)st->alpha;
+  double acc = 0.0;
+  NET_LOOP(V) {
+    const float m = rc[t] - alpha * rq[t];
+    rc[t] = m;
+    acc += (double)m * (double)m;
+    in0[act_index(t, 0, V)] = __float2bfloat16_rn(m * inv);
+  }
+  double v[1] = {acc}, tot[1];
+  if (grid_reduce<1>(v, partials, &st->counter[1], tot))
+    if (threadIdx.x == 0) st->aux[2] = tot[0];
+}
+
+// Last block of the flexible CG's preconditioner kernel, which also applies
+// the pending r -= alpha q (rupd; not on the first residual): rho = z.r,
+// beta = -z.q_old / p.q_old (0 on the first residual), and what an update
+// of r decides -- the iteration count, the learned preconditioner's
+// progress check (the FP32 residual norm must halve within 50 iterations,
+// else the solve continues as Jacobi-PCG, so a network that does not fit
+// the problem cannot stall it) and the reliable-update trigger.
+__device__ void fcg_close(CgState* st, double zr, double zq, double rr, bool rupd, int err) {
+  const double beta = st->initial ? 0.0 : -zq / st->pq;
+  st->initial = 0;
+  st->rho = zr;
+  st->beta = beta;
+  if (err) {
+    st->done = 5;
+    return;
+  }
+  if (!isfinite(zr) || !isfinite(beta)) {
+    st->done = 3;
+    return;
+  }
+  if (!rupd) return;
+  const int it = st->iter + 1;
+  st->iter = it;
+  if (!st->pc_off) {
+    if (st->aux[3] <= 0.0 || rr < 0.25 * st->aux[3]) {
+      st->aux[3] = rr;
+      st->stall_iter = it;
+    } else if (it - st->stall_iter > 50) {
+      st->pc_off = 1;
+    }
+  }
+  if (!isfinite(rr) || !isfinite(st->alpha)) {
+    st->done = 3;
+    return;
+  }
+  const double maxrr = fmax(st->maxrr, rr);
+  if ((rr < st->delta2 * maxrr) || (rr <= st->tol * st->tol * st->aux[0]) || (it >= st->max_it))
+    st->reliable = 1;
+  st->rr = rr;
+  st->maxrr = maxrr;
 }
 
 // Interpolation weights of the 4 fine cells of one coarse cell along an
@@ -790,22 +852,25 @@ __device__ __forceinline__ void interp1(int fi, int n, int* lo, int* hi, float* 
   *wlo = wl[e];
 }
 
-// z = invd*r + f * P(out) over the fine interior (the additive form), f =
-// s k_out / (scale c_ref); z.r and z.q_old reduced; the last block sets rho,
-// beta of the flexible CG.  One item = 4 y-consecutive fine cells (one
+// The additive form: r -= alpha q (the pending update of the flexible CG,
+// not on the first residual), then z = invd*r + f * P(out) over the fine
+// interior, f = s k_out / (scale c_ref); z.r, z.q_old and r.r reduced; the
+// last block runs fcg_close.  One item = 4 y-consecutive fine cells (one
 // coarse cell in y) on one x row, marched over the 4 fine planes of one
 // coarse z cell, so the coarse values (3 y x 2 x x 3 z) are loaded once for
 // 16 cells.  With the coarse part switched off (pc_off): z = invd*r.
 __global__ void __launch_bounds__(256)
     k_pc_prolong(Geo g, Dims c, Dims cv, const float* __restrict__ out, const float* scal,
-                 const float* __restrict__ r, const float* __restrict__ iv,
+                 float* __restrict__ r, const float* __restrict__ iv,
                  const float* __restrict__ q, float* __restrict__ z, const int* err,
                  double* partials, CgState* st) {
   pdl_begin();
   if (st->done) return;
   const bool coarse = st->pc_off == 0;  // off: z = D^-1 r (Jacobi-PCG)
   const float f = coarse ? scal[0] * scal[2] : 0.f;
-  float a_zr = 0.f, a_zq = 0.f;
+  const bool rupd = st->initial == 0;
+  const float alpha = (float)st->alpha;
+  float a_zr = 0.f, a_zq = 0.f, a_rr = 0.f;
   {
     const int nchunk = g.ny / 4;
     const int64_t n = (int64_t)nchunk * g.nx * (g.nz / 4);
@@ -841,9 +906,13 @@ __global__ void __launch_bounds__(256)
         const float e4[4] = {0.375f * col[0] + 0.625f * col[1], 0.125f * col[0] + 0.875f * col[1],
                              0.875f * col[1] + 0.125f * col[2], 0.625f * col[1] + 0.375f * col[2]};
         const int64_t idx = g.ix(4 * m + 1, j, 4 * kc + 1 + e);
-        const float4 rv = *reinterpret_cast<const float4*>(r + idx);
+        float4 rv = *reinterpret_cast<const float4*>(r + idx);
         const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
         const float4 qv = *reinterpret_cast<const float4*>(q + idx);
+        if (rupd) {
+          rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
+          *reinterpret_cast<float4*>(r + idx) = rv;
+        }
         float4 zv;
         zv.x = dv.x * rv.x + f * e4[0];
         zv.y = dv.y * rv.y + f * e4[1];
@@ -852,34 +921,30 @@ __global__ void __launch_bounds__(256)
         *reinterpret_cast<float4*>(z + idx) = zv;
         a_zr += (zv.x * rv.x + zv.y * rv.y) + (zv.z * rv.z + zv.w * rv.w);
         a_zq += (zv.x * qv.x + zv.y * qv.y) + (zv.z * qv.z + zv.w * qv.w);
+        a_rr += (rv.x * rv.x + rv.y * rv.y) + (rv.z * rv.z + rv.w * rv.w);
       }
     }
   }
-  double v[2] = {(double)a_zr, (double)a_zq}, tot[2];
-  if (grid_reduce<2>(v, partials, &st->counter[5], tot)) {
-    if (threadIdx.x == 0) {
-      const double zr = tot[0];
-      const double beta = st->initial ? 0.0 : -tot[1] / st->pq;
-      st->initial = 0;
-      st->rho = zr;
-      st->beta = beta;
-      if (*err) st->done = 5;
-      else if (!isfinite(zr) || !isfinite(beta)) st->done = 3;
-    }
-  }
+  double v[3] = {(double)a_zr, (double)a_zq, (double)a_rr}, tot[3];
+  if (grid_reduce<3>(v, partials, &st->counter[5], tot))
+    if (threadIdx.x == 0) fcg_close(st, tot[0], tot[1], tot[2], rupd, *err);
 }
 
 // The multiplicative form z = z1 + omega*invd*(r - A z1), z1 = f P(out), by
-// tiles of 64 (y) x 8 (x) x 4 (z) fine cells.  The block interpolates the
-// coarse window (18 y x 4 x x 3 z cells, clamped) in x and then in z onto
-// the tile's fine x / z positions with their one-cell halo, in shared
-// memory (the order of k_pc_prolong); each thread then takes 4
+// tiles of 64 (y) x 8 (x) x 4 (z) fine cells, after the pending update
+// r -= alpha q of the flexible CG (not on the first residual).  The block
+// interpolates the coarse window (18 y x 4 x x 3 z cells, clamped) in x and
+// then in z onto the tile's fine x / z positions with their one-cell halo,
+// in shared memory (the order of k_pc_prolong); each thread then takes 4
 // y-consecutive cells (one coarse y cell), interpolates z1 in y for them
 // and their 6 neighbours from three coarse values per row, and applies the
-// FP32 operator with the search-direction ghost rules.  Global traffic per
-// cell: r, invd, q_old and hk read, z written (20 B); the coarse values come
-// from L2.  z.r and z.q_old are reduced as in k_pc_prolong.  Tiles are
-// walked grid-stride (every block the same count: the barriers are uniform).
+// FP32 operator with the search-direction ghost rules.  The Jacobi weight
+// invd is formed from the same half coefficients (the operations of
+// k_invdiag), so it is not read.  Global traffic per cell: r, q_old and hk
+// read, r and z written (20 B); the coarse values and the neighbours' hk
+// come from L2.  z.r, z.q_old and r.r are reduced and the last block runs
+// fcg_close.  Tiles are walked grid-stride (every block the same count: the
+// barriers are uniform).
 // Weight of the Jacobi step of the multiplicative form.  Flexible-CG
 // iterations on the GPU (256^3 headline / 128^3 and 256^3 held-out / 64^3 /
 // 128^3 structures): omega 1.5: 86/56/82/54/67, 1.9: 72/47/71/51/53,
@@ -893,10 +958,10 @@ constexpr int kMTY = 64, kMTX = 8, kMTZ = 4;
 constexpr int kWY = kMTY / 4 + 2;  // coarse y window
 __global__ void __launch_bounds__(256, 3)
     k_pc_mult_tiled(Geo g, Dims c, Dims cv, const float* __restrict__ out, const float* scal,
-                    const float* __restrict__ r, const float* __restrict__ iv,
-                    const float* __restrict__ q, const float* __restrict__ hk,
-                    const float* __restrict__ dg, float scale, int bcx0, int bcx1, float omega,
-                    float* __restrict__ z, const int* err, double* partials, CgState* st) {
+                    float* __restrict__ r, const float* __restrict__ q,
+                    const float* __restrict__ hk, const float* __restrict__ dg, float scale,
+                    int bcx0, int bcx1, float omega, float* __restrict__ z, const int* err,
+                    double* partials, CgState* st) {
   __shared__ float sA[3][kMTX / 4 + 2][kWY];
   __shared__ float sB[3][kMTX + 2][kWY];
   __shared__ float sC[kMTZ + 2][kMTX + 2][kWY];
@@ -904,12 +969,14 @@ __global__ void __launch_bounds__(256, 3)
   if (st->done) return;
   const bool coarse = st->pc_off == 0;  // off: z = D^-1 r (Jacobi-PCG)
   const float f = coarse ? scal[0] * scal[2] : 0.f;
+  const bool rupd = st->initial == 0;
+  const float alpha = (float)st->alpha;
   const int tid = threadIdx.x;
   const int nty = (g.ny + kMTY - 1) / kMTY, ntx = g.nx / kMTX;  // the last y tile may be partial
   const int64_t ntiles = (int64_t)nty * ntx * (g.nz / kMTZ);
   // per-thread roles of the staging loops: (x, y) column of the windows
   const int col_y = tid % kWY, col_x = tid / kWY;  // col_x < kMTX + 2 for tid < 180
-  float a_zr = 0.f, a_zq = 0.f;
+  float a_zr = 0.f, a_zq = 0.f, a_rr = 0.f;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int by = (int)(tile % nty);
     const int bx = (int)((tile / nty) % ntx);
@@ -957,11 +1024,42 @@ __global__ void __launch_bounds__(256, 3)
       const int i0 = y0 + 4 * mq, j = x0 + xl, k = z0 + zl;
       if (i0 > g.ny) continue;  // beyond a partial tile (ny is a multiple of 4)
       const int64_t idx = g.ix(i0, j, k);
-      const float4 rv = *reinterpret_cast<const float4*>(r + idx);
-      const float4 dv = *reinterpret_cast<const float4*>(iv + idx);
+      float4 rv = *reinterpret_cast<const float4*>(r + idx);
       const float4 qv = *reinterpret_cast<const float4*>(q + idx);
-      const float ra[4] = {rv.x, rv.y, rv.z, rv.w}, da[4] = {dv.x, dv.y, dv.z, dv.w};
+      if (rupd) {
+        rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
+        *reinterpret_cast<float4*>(r + idx) = rv;
+      }
+      const float ra[4] = {rv.x, rv.y, rv.z, rv.w};
       const float qa[4] = {qv.x, qv.y, qv.z, qv.w};
+      const float4 k4 = *reinterpret_cast<const float4*>(hk + idx);
+      const float4 kx0 = *reinterpret_cast<const float4*>(hk + idx - g.sx);
+      const float4 kx1 = *reinterpret_cast<const float4*>(hk + idx + g.sx);
+      const float4 kz0 = *reinterpret_cast<const float4*>(hk + idx - g.sz);
+      const float4 kz1 = *reinterpret_cast<const float4*>(hk + idx + g.sz);
+      const float ky[6] = {hk[idx - 1], k4.x, k4.y, k4.z, k4.w, hk[idx + 4]};
+      const float kxa[4] = {kx0.x, kx0.y, kx0.z, kx0.w}, kxb[4] = {kx1.x, kx1.y, kx1.z, kx1.w};
+      const float kza[4] = {kz0.x, kz0.y, kz0.z, kz0.w}, kzb[4] = {kz1.x, kz1.y, kz1.z, kz1.w};
+      float dga[4] = {0.f, 0.f, 0.f, 0.f};
+      if (dg) {  // the CnE form: A p = diag p - scale S(p)
+        const float4 d4 = *reinterpret_cast<const float4*>(dg + idx);
+        dga[0] = d4.x; dga[1] = d4.y; dga[2] = d4.z; dga[3] = d4.w;
+      }
+      // the Jacobi weight 1 / A_cc, faces summed in k_invdiag's order
+      float da[4];
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        const float kc = ky[y + 1];
+        float sum = 0.f;
+        if (i0 + y > 1) sum += ky[y] + kc;
+        if (i0 + y < g.ny) sum += ky[y + 2] + kc;
+        if (j > 1 || bcx0) sum += kxa[y] + kc;
+        if (j < g.nx || bcx1) sum += kxb[y] + kc;
+        if (k > 1) sum += kza[y] + kc;
+        if (k < g.nz) sum += kzb[y] + kc;
+        const float d = dg ? dga[y] + scale * sum : -scale * sum;
+        da[y] = (d != 0.f) ? 1.f / d : 0.f;
+      }
       float za[4];
       if (coarse) {
         const int xf = 1 + xl, zf = 1 + zl;
@@ -988,14 +1086,6 @@ __global__ void __launch_bounds__(256, 3)
           dst[t][2] = 0.875f * a1 + 0.125f * a2;
           dst[t][3] = 0.625f * a1 + 0.375f * a2;
         }
-        const float4 k4 = *reinterpret_cast<const float4*>(hk + idx);
-        const float4 kx0 = *reinterpret_cast<const float4*>(hk + idx - g.sx);
-        const float4 kx1 = *reinterpret_cast<const float4*>(hk + idx + g.sx);
-        const float4 kz0 = *reinterpret_cast<const float4*>(hk + idx - g.sz);
-        const float4 kz1 = *reinterpret_cast<const float4*>(hk + idx + g.sz);
-        const float ky[6] = {hk[idx - 1], k4.x, k4.y, k4.z, k4.w, hk[idx + 4]};
-        const float kxa[4] = {kx0.x, kx0.y, kx0.z, kx0.w}, kxb[4] = {kx1.x, kx1.y, kx1.z, kx1.w};
-        const float kza[4] = {kz0.x, kz0.y, kz0.z, kz0.w}, kzb[4] = {kz1.x, kz1.y, kz1.z, kz1.w};
         // ghost rules only for the cells on a domain face
         if (i0 == 1 || i0 + 3 == g.ny || j == 1 || j == g.nx || k == 1 || k == g.nz) {
           if (i0 == 1) cen[0] = cen[1];
@@ -1008,11 +1098,6 @@ __global__ void __launch_bounds__(256, 3)
             if (k == 1) zm4[y] = pc;
             if (k == g.nz) zp4[y] = pc;
           }
-        }
-        float dga[4] = {0.f, 0.f, 0.f, 0.f};
-        if (dg) {  // the CnE form: A p = diag p - scale S(p)
-          const float4 d4 = *reinterpret_cast<const float4*>(dg + idx);
-          dga[0] = d4.x; dga[1] = d4.y; dga[2] = d4.z; dga[3] = d4.w;
         }
 #pragma unroll
         for (int y = 0; y < 4; ++y) {
@@ -1031,22 +1116,14 @@ __global__ void __launch_bounds__(256, 3)
       for (int y = 0; y < 4; ++y) {
         a_zr += za[y] * ra[y];
         a_zq += za[y] * qa[y];
+        a_rr += ra[y] * ra[y];
       }
       *reinterpret_cast<float4*>(z + idx) = make_float4(za[0], za[1], za[2], za[3]);
     }
   }
-  double v[2] = {(double)a_zr, (double)a_zq}, tot[2];
-  if (grid_reduce<2>(v, partials, &st->counter[5], tot)) {
-    if (threadIdx.x == 0) {
-      const double zr = tot[0];
-      const double beta = st->initial ? 0.0 : -tot[1] / st->pq;
-      st->initial = 0;
-      st->rho = zr;
-      st->beta = beta;
-      if (*err) st->done = 5;
-      else if (!isfinite(zr) || !isfinite(beta)) st->done = 3;
-    }
-  }
+  double v[3] = {(double)a_zr, (double)a_zq, (double)a_rr}, tot[3];
+  if (grid_reduce<3>(v, partials, &st->counter[5], tot))
+    if (threadIdx.x == 0) fcg_close(st, tot[0], tot[1], tot[2], rupd, *err);
 }
 
 struct NetPc {
@@ -1055,7 +1132,8 @@ struct NetPc {
   Dims c{};   // the U-Net's grid: cv rounded up to multiples of 16 (zero padding)
   Dims cv{};  // the coarse cells of the solve's grid (fine interior / 4)
   Work* w = nullptr;
-  float* rc = nullptr;
+  float* rc = nullptr;   // R r of the current residual
+  float* rq = nullptr;   // R q of the current direction (flexible-CG direction kernel)
   float* coefc = nullptr;
   float* massc = nullptr;  // coarse means of the CnE diagonal
   float* zf = nullptr;   // FP32 z (g32 layout)
@@ -1071,13 +1149,14 @@ struct NetPc {
     delete w;
     w = nullptr;
     cudaFree(rc);
+    cudaFree(rq);
     cudaFree(coefc);
     cudaFree(massc);
     cudaFree(zf);
     cudaFree(scal);
     cudaFree(parts);
     cudaFree(cnt);
-    rc = coefc = massc = zf = scal = nullptr;
+    rc = rq = coefc = massc = zf = scal = nullptr;
     parts = nullptr;
     cnt = nullptr;
   }
@@ -1111,6 +1190,7 @@ int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, double scal
     pc->cv = cv;
     pc->w = netd::make_work(c, false, &cv);
     if (!pc->w || cudaMalloc(&pc->rc, sizeof(float) * c.v()) ||
+        cudaMalloc(&pc->rq, sizeof(float) * c.v()) ||
         cudaMalloc(&pc->coefc, sizeof(float) * c.v()) ||
         cudaMalloc(&pc->massc, sizeof(float) * c.v()) ||
         cudaMalloc(&pc->zf, sizeof(float) * g.nh) || cudaMalloc(&pc->scal, sizeof(float) * 8) ||
@@ -1127,6 +1207,8 @@ int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, double scal
     SBM_CUDA_TRY(cudaMemsetAsync(pc->cnt, 0, sizeof(unsigned) * 4, s));
     SBM_CUDA_TRY(cudaMemsetAsync(pc->scal, 0, sizeof(float) * 8, s));
   }
+  // no direction yet: the first pack applies alpha = 0 to a zero R q
+  SBM_CUDA_TRY(cudaMemsetAsync(pc->rq, 0, sizeof(float) * c.v(), s));
   pc->hk32 = hk32;
   pc->dg32 = dg32;
   pc->scale = (float)scale;
@@ -1148,6 +1230,8 @@ float* net_pc_zbuf(sbm_ctx* ctx) {
 }
 
 float* net_pc_rc(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->rc; }
+float* net_pc_rq(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->rq; }
+int64_t net_pc_ncell(sbm_ctx* ctx) { return static_cast<netd::NetPc*>(ctx->net)->cv.v(); }
 // y and x strides of the coarse arrays (the padded grid's extents)
 void net_pc_rc_strides(sbm_ctx* ctx, int* sy, int* sx) {
   const netd::NetPc* pc = static_cast<const netd::NetPc*>(ctx->net);
@@ -1161,26 +1245,26 @@ int net_pc_nodes() { return 3 + 9; }
 // The multiplicative step: tiles of 64 x 8 x 4 fine cells (the last y tile
 // may be partial), one wave of resident blocks (3 per SM at 80 registers)
 // walking them grid-stride.
-static void launch_mult(netd::NetPc* pc, const Geo& g, const float* r32, const float* iv32,
-                        const float* q32, double* partials, CgState* st, cudaStream_t s) {
+static void launch_mult(netd::NetPc* pc, const Geo& g, float* r32, const float* q32,
+                        double* partials, CgState* st, cudaStream_t s) {
   const int64_t tiles = (int64_t)((g.ny + netd::kMTY - 1) / netd::kMTY) * (g.nx / netd::kMTX) *
                         (g.nz / netd::kMTZ);
   const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
   launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, pc->c, pc->cv,
-             (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->hk32,
-             pc->dg32, pc->scale, pc->bcx0, pc->bcx1, netd::kPcOmega, pc->zf + kOff32,
+             (const float*)pc->w->out, (const float*)pc->scal, r32, q32, pc->hk32, pc->dg32,
+             pc->scale, pc->bcx0, pc->bcx1, netd::kPcOmega, pc->zf + kOff32,
              (const int*)pc->net->err, partials, st);
 }
 
-void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const float* q32,
+void net_pc_launch(sbm_ctx* ctx, float* r32, const float* iv32, const float* q32,
                    double* partials, CgState* st, cudaStream_t s) {
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   const Geo& g = ctx->g32;
   const netd::Dims& c = pc->c;
   launch_pdl(netd::k_pc_restrict, dim3(netd::grid_for(pc->cv.v())), dim3(256), 0, s, g, c, pc->cv,
-             r32, pc->rc, partials, (float*)pc->scal, st);
-  launch_pdl(netd::k_pc_pack, dim3(netd::grid_for(c.v())), dim3(256), 0, s, c.v(),
-             (const float*)pc->rc, (const float*)pc->scal, pc->w->in0, (const CgState*)st);
+             (const float*)r32, pc->rc, (const float*)pc->rq, partials, (float*)pc->scal, st);
+  launch_pdl(netd::k_pc_pack, dim3(netd::grid_for(c.v())), dim3(256), 0, s, c.v(), pc->rc,
+             (const float*)pc->rq, (const float*)pc->scal, pc->w->in0, partials, st);
   SBM_LAUNCHED(2);
   netd::forward(pc->net, *pc->w, false, &st->done, &st->pc_off, s);
   const int64_t items = (int64_t)(g.ny / 4) * g.nx * (g.nz / 4);
@@ -1195,22 +1279,19 @@ void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const floa
                (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->zf + kOff32,
                (const int*)pc->net->err, partials, st);
   } else {
-    launch_mult(pc, g, r32, iv32, q32, partials, st, s);
+    launch_mult(pc, g, r32, q32, partials, st, s);
   }
   SBM_LAUNCHED(1);
 }
 
-void net_pc_launch_part(sbm_ctx* ctx, int part, const float* r32, const float* iv32,
-                        const float* q32, double* partials, CgState* st, cudaStream_t s) {
+void net_pc_launch_part(sbm_ctx* ctx, int part, float* r32, const float* q32,
+                        double* partials, CgState* st, cudaStream_t s) {
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
-  const Geo& g = ctx->g32;
-  const netd::Dims& c = pc->c;
   if (part == 0) {
     netd::forward(pc->net, *pc->w, false, &st->done, &st->pc_off, s);
     return;
   }
-  (void)c;
-  launch_mult(pc, g, r32, iv32, q32, partials, st, s);
+  launch_mult(pc, ctx->g32, r32, q32, partials, st, s);
   SBM_LAUNCHED(1);
 }
 

@@ -19,17 +19,24 @@ bool net_pc_usable(const sbm_ctx* ctx, int form);
 int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, double scale, int bcx0,
                  int bcx1, cudaStream_t s);
 
-// z = invd*r + P(e_c), e_c from the network on the restricted residual;
-// the last block sets st->rho = z.r and st->beta (flexible CG, Notay's
-// FCG(1): beta = -z.q_old / pq_old; 0 on the first use).  No-op once
-// st->done is set.  Returns the FP32 buffer (base + kOff32) receiving z.
+// One application inside the flexible CG (no-op once st->done is set):
+// R r when stale (first use, residual replacement), R r -= alpha R q and
+// the network's input, the U-Net, then the kernel that applies the pending
+// r -= alpha q of the previous direction (not on the first residual) and
+// forms z = M(r) -- multiplicative: z1 + omega invd (r - A z1), z1 the
+// prolonged network output; additive: invd r + z1.  Its last block sets
+// st->rho = z.r and st->beta (Notay's FCG(1): beta = -z.q_old / pq_old; 0
+// on the first use) and decides the reliable-update trigger from r.r.
+// net_pc_zbuf returns the FP32 buffer (base + kOff32) receiving z.
 float* net_pc_zbuf(sbm_ctx* ctx);
-void net_pc_launch(sbm_ctx* ctx, const float* r32, const float* iv32, const float* q32,
+void net_pc_launch(sbm_ctx* ctx, float* r32, const float* iv32, const float* q32,
                    double* partials, CgState* st, cudaStream_t s);
-// Coarse residual R r and the scalars (s, 1/s, ...) the preconditioner reads;
-// the flexible-CG update kernel fills them (and marks them valid in
-// CgState.aux[1]).
+// Coarse residual R r, the direction's R q (written by the flexible-CG
+// direction kernel) and the scalars (s, 1/s, ...) the preconditioner reads.
 float* net_pc_rc(sbm_ctx* ctx);
+float* net_pc_rq(sbm_ctx* ctx);
+// valid coarse cells (fine interior / 64)
+int64_t net_pc_ncell(sbm_ctx* ctx);
 // y and x strides of the coarse arrays (R r is stored with them)
 void net_pc_rc_strides(sbm_ctx* ctx, int* sy, int* sx);
 float* net_pc_scal(sbm_ctx* ctx);
@@ -37,8 +44,8 @@ float* net_pc_scal(sbm_ctx* ctx);
 int net_pc_nodes();
 // One part of net_pc_launch for timing: 0 = the 9 U-Net convolutions on the
 // current input, 1 = the multiplicative prolongation / Jacobi step.
-void net_pc_launch_part(sbm_ctx* ctx, int part, const float* r32, const float* iv32,
-                        const float* q32, double* partials, CgState* st, cudaStream_t s);
+void net_pc_launch_part(sbm_ctx* ctx, int part, float* r32, const float* q32,
+                        double* partials, CgState* st, cudaStream_t s);
 
 void net_pc_release(sbm_ctx* ctx);
 

@@ -830,96 +830,6 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Update of the flexible CG with the learned preconditioner, walked by
-// 4x4x4 blocks: x32 += alpha p (folding into d64 after a reliable update),
-// r32 -= alpha q, r.r, and the block means rc = R r of the new residual with
-// their sum of squares, so the preconditioner needs no separate
-// restriction pass: the last block stores s = RMS(rc), 1/s and marks rc
-// valid (aux[1]; a residual replacement clears it).  Rows of the block are
-// float4 loads, consecutive threads take consecutive blocks along y.
-__global__ void __launch_bounds__(256)
-    k32_update_fcg(Geo g, Geo g64, float* __restrict__ x, const float* __restrict__ p,
-                   float* __restrict__ r, const float* __restrict__ q, double* __restrict__ d64,
-                   float* __restrict__ rc, int rcy, int rcx, float* __restrict__ scal,
-                   double* partials, CgState* st) {
-  pdl_begin();
-  if (st->done) return;
-  const bool fold = st->accum_pending != 0;
-  const float alpha = (float)st->alpha;
-  const int cny = g.ny / 4, cnx = g.nx / 4;
-  const int64_t ncell = (int64_t)cny * cnx * (g.nz / 4);
-  float a_rr = 0.f;
-  double a_rc = 0.0;
-  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < ncell;
-       u += (int64_t)gridDim.x * blockDim.x) {
-    const int ic = (int)(u % cny);
-    const int64_t rr = u / cny;
-    const int jc = (int)(rr % cnx), kc = (int)(rr / cnx);
-    const int i = 4 * ic + 1;
-    float sum = 0.f;
-#pragma unroll 4
-    for (int q16 = 0; q16 < 16; ++q16) {
-      const int j = 4 * jc + 1 + (q16 & 3), k = 4 * kc + 1 + (q16 >> 2);
-      const int64_t c = g.ix(i, j, k);
-      float4 xv = ld4(x + c);
-      const float4 pv = ld4(p + c), qv = ld4(q + c);
-      float4 rv = ld4(r + c);
-      if (fold) {
-        const int64_t c64 = g64.ix(i, j, k);
-        d64[c64] += (double)xv.x;
-        d64[c64 + 1] += (double)xv.y;
-        d64[c64 + 2] += (double)xv.z;
-        d64[c64 + 3] += (double)xv.w;
-        xv = make_float4(alpha * pv.x, alpha * pv.y, alpha * pv.z, alpha * pv.w);
-      } else {
-        xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
-      }
-      rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
-      st4(x + c, xv);
-      st4(r + c, rv);
-      a_rr += (rv.x * rv.x + rv.y * rv.y) + (rv.z * rv.z + rv.w * rv.w);
-      sum += (rv.x + rv.y) + (rv.z + rv.w);
-    }
-    const float m = sum * (1.f / 64.f);
-    rc[ic + (int64_t)rcy * (jc + (int64_t)rcx * kc)] = m;  // strides of the padded coarse grid
-    a_rc += (double)m * (double)m;
-  }
-  double v[2] = {(double)a_rr, a_rc}, tot[2];
-  if (grid_reduce<2>(v, partials, &st->counter[1], tot)) {
-    if (threadIdx.x == 0) {
-      const double rr_new = tot[0];
-      const int it = st->iter + 1;
-      st->iter = it;
-      st->accum_pending = 0;
-      const double sc = sqrt(tot[1] / (double)ncell);
-      scal[0] = (float)sc;
-      scal[1] = sc > 0.0 ? (float)(1.0 / sc) : 0.f;
-      st->aux[1] = 1.0;
-      // progress check of the learned preconditioner: the FP32 residual norm
-      // must halve within 50 iterations, else the solve continues as
-      // Jacobi-PCG (a network that does not fit the problem cannot stall it)
-      if (!st->pc_off) {
-        if (st->aux[3] <= 0.0 || rr_new < 0.25 * st->aux[3]) {
-          st->aux[3] = rr_new;
-          st->stall_iter = it;
-        } else if (it - st->stall_iter > 50) {
-          st->pc_off = 1;
-        }
-      }
-      if (!isfinite(rr_new) || !isfinite(st->alpha)) {
-        st->done = 3;
-      } else {
-        const double maxrr = fmax(st->maxrr, rr_new);
-        if ((rr_new < st->delta2 * maxrr) || (rr_new <= st->tol * st->tol * st->aux[0]) ||
-            (it >= st->max_it))
-          st->reliable = 1;
-        st->rr = rr_new;
-        st->maxrr = maxrr;
-      }
-    }
-  }
-}
-
 // Reliable update: r = r0 - A_h (d64 + x32) in FP64 (ghost rules of the
 // search direction on the correction), r32 = (float) r, z = invd*r32;
 // convergence on the FP64 norm, new rho / beta.  No-op unless flagged.
@@ -1113,11 +1023,14 @@ int flat_blocks(int64_t items) {
 struct TmaPlan;
 bool tma_supported(const Geo& g32);
 int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, const float* hk,
-             const float* iv, const float* dg, int pc, int form, int zct, TmaPlan* plan);
+             const float* iv, const float* dg, int pc, int form, int zct, int flex,
+             TmaPlan* plan);
 int tma_plan_size(void);
 int tma_init();
 void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
-                double* partials, CgState* st, cudaStream_t s, bool pdl = false);
+                double* partials, CgState* st, cudaStream_t s);
+void tma_launch_fcg(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
+                    const FcgDirArgs& fx, double* partials, CgState* st, cudaStream_t s);
 
 int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cudaGraph_t* graph_out,
                 int* nodes_out) {
@@ -1145,7 +1058,10 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   OpArgs<float> op32{g32, hk32, sp.form ? dg32 : nullptr, (float)sp.scale, sp.form, sp.bcx0,
                      sp.bcx1};
   // learned preconditioner when usable, else Jacobi (the documented fallback)
-  const bool learned = sp.precond == SBM_PC_LEARNED && net_pc_usable(ctx, sp.form) && vec == 4;
+  // the flexible-CG loop runs on the TMA-staged direction kernel (it carries
+  // the deferred x update and the restriction of q)
+  const bool learned = sp.precond == SBM_PC_LEARNED && net_pc_usable(ctx, sp.form) && vec == 4 &&
+                       tma_supported(g32);
   const bool pc = sp.precond == SBM_PC_JACOBI || (sp.precond == SBM_PC_LEARNED && !learned);
   ctx->last_precond = learned ? SBM_PC_LEARNED : (pc ? SBM_PC_JACOBI : SBM_PC_NONE);
   // Reliable-update factor: the FP64 residual replacement is an FP64-ALU-
@@ -1179,8 +1095,17 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   if (learned &&
       (rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, sp.scale, sp.bcx0, sp.bcx1, s)))
     return rc;
-  int rcy = 0, rcx = 0;
-  if (learned) net_pc_rc_strides(ctx, &rcy, &rcx);
+  FcgDirArgs fx{};
+  if (learned) {
+    fx.x32 = x32;
+    fx.d64 = ctx->d64;
+    fx.g64 = g;
+    fx.rc = net_pc_rc(ctx);
+    fx.rq = net_pc_rq(ctx);
+    fx.scal = net_pc_scal(ctx);
+    net_pc_rc_strides(ctx, &fx.rcy, &fx.rcx);
+    fx.ncell = net_pc_ncell(ctx);
+  }
   // with the learned preconditioner the direction kernels read z from its buffer
   float* const zl = learned ? net_pc_zbuf(ctx) : nullptr;
   const float* const rdir = learned ? zl : r32;
@@ -1196,8 +1121,6 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   SBM_LAUNCHED(1);
   const int64_t items = (int64_t)nchunk * g.nx * g.nz;
   const dim3 fgrid(flat_blocks(items));
-  // the learned path's update: one thread per 4x4x4 block
-  const dim3 cgrid((unsigned)std::min<int64_t>(std::max<int64_t>(items / 16 / 256, 1), 152 * 8));
   const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
   float* const pbuf[2] = {p32, ctx->rold32 + kOff32};  // alternating direction buffers
   // the replacement kernel walks its tiles grid-stride with four blocks per
@@ -1222,22 +1145,31 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
 #undef SBM_REL
   };
   // TMA-staged stencil when the layout allows it (tensor maps of this solve)
-  const bool use_tma = (vec == 4) && !ctx->no_tma && tma_supported(g32);
+  const bool use_tma = (vec == 4) && (learned || !ctx->no_tma) && tma_supported(g32);
   std::vector<unsigned char> plan_buf(use_tma ? tma_plan_size() : 1);
   TmaPlan* plan = reinterpret_cast<TmaPlan*>(plan_buf.data());
   if (use_tma) {
     if ((rc = tma_init())) return rc;
     if ((rc = tma_plan(g32, learned ? zl - kOff32 : ctx->r32, ctx->p32, ctx->rold32, ctx->hk32,
-                       ctx->z32, ctx->dg32, pc ? 1 : 0, sp.form, ctx->zc32, plan)))
+                       ctx->z32, ctx->dg32, pc ? 1 : 0, sp.form, ctx->zc32, learned ? 1 : 0,
+                       plan)))
       return rc;
   }
   // one iteration reading direction buffer `in` and writing `out`
   auto iter = [&](cudaStream_t s2, const float* in, float* out) {
-    if (learned) net_pc_launch(ctx, r32, iv32, q32, ctx->partials, ctx->st, s2);
+    if (learned) {
+      // flexible CG: R r (when stale) and R r -= alpha R q, the U-Net, the
+      // step that applies r -= alpha q and forms z, the direction kernel
+      // (which applies x += alpha p_old), then the residual replacement
+      net_pc_launch(ctx, r32, iv32, q32, ctx->partials, ctx->st, s2);
+      tma_launch_fcg(*plan, in == pbuf[0], op32, out, q32, fx, ctx->partials, ctx->st, s2);
+      rel(s2);
+      return;
+    }
 #define SBM_AD(F, P)                                                                           \
   do {                                                                                         \
     if (use_tma)                                                                               \
-      tma_launch(*plan, in == pbuf[0], op32, out, q32, ctx->partials, ctx->st, s2, learned);   \
+      tma_launch(*plan, in == pbuf[0], op32, out, q32, ctx->partials, ctx->st, s2);            \
     else if (vec == 4)                                                                         \
       k32v_apply_dir<F, P><<<vgrid, 256, 0, s2>>>(op32, nchunk, zc32, rdir, in, iv32, out, q32, \
                                                    ctx->partials, ctx->st);                    \
@@ -1255,11 +1187,7 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
 #define SBM_UP(P, V)                                                                         \
   k32_update<P, V><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, x32, out, r32, q32, iv32, ctx->d64, \
                                           ctx->partials, ctx->st)
-    if (learned) {
-      launch_pdl(k32_update_fcg, cgrid, dim3(256), 0, s2, g32, g, x32, (const float*)out, r32,
-                 (const float*)q32, ctx->d64, net_pc_rc(ctx), rcy, rcx, net_pc_scal(ctx),
-                 ctx->partials, ctx->st);
-    } else if (vec == 4) {
+    if (vec == 4) {
       if (pc) SBM_UP(true, 4); else SBM_UP(false, 4);
     } else {
       if (pc) SBM_UP(true, 1); else SBM_UP(false, 1);
@@ -1288,7 +1216,7 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
              sp.form, sp.bcx0, sp.bcx1, vec * 16 + zc32, pc, sh64.zc, clen);
   cudaGraphExec_t ex = nullptr;
   int nodes = 0;
-  rc = capture_graph(ctx, key, learned ? 2 * (3 + net_pc_nodes()) : 6, body, &ex, &nodes, clen);
+  rc = capture_graph(ctx, key, learned ? 2 * (2 + net_pc_nodes()) : 6, body, &ex, &nodes, clen);
   if (rc) return rc;
   ctx->last_op32 = op32;
   ctx->last_pc = pc ? 1 : 0;
@@ -1387,12 +1315,15 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
 
 // Times `reps` back-to-back launches of one solver kernel on the context
 // stream with CUDA events, on the buffers of the last mixed solve:
-//   which 0: the FP32 fused direction + stencil kernel (the dominant kernel)
-//   which 1: the FP32 vector update kernel
+//   which 0: the FP32 fused direction + stencil kernel (its flexible-CG
+//            variant after a learned solve)
+//   which 1: the FP32 vector update kernel (Jacobi / no preconditioner)
 //   which 2: the FP64 stencil + dot kernel of the plain CG
+//   which 3: one application of the learned preconditioner (its r update
+//            included); 5: its nine convolutions; 6: its multiplicative step
 // and reports the algorithmic bytes one launch moves.
 int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double* bytes_per_launch) {
-  if (reps < 1 || which < 0 || which > 6) return SBM_ERR_ARG;
+  if (reps < 1 || which < 0 || which > 6 || which == 4) return SBM_ERR_ARG;
   if (which != 2 && ctx->last_pc < 0) return SBM_ERR_STATE;
   if (which >= 3 && (ctx->last_precond != SBM_PC_LEARNED || !net_pc_usable(ctx, 0)))
     return SBM_ERR_STATE;
@@ -1426,21 +1357,38 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
   float* q32 = ctx->q32 + kOff32;
   float* x32 = ctx->x32 + kOff32;
   float* iv = ctx->z32 + kOff32;
-  const bool use_tma = (vec == 4) && !ctx->no_tma && tma_supported(g32);
+  // the direction kernel of the last solve: the flexible-CG variant after a
+  // learned solve (it also applies the deferred x update and restricts q)
+  const bool flex = ctx->last_precond == SBM_PC_LEARNED && net_pc_usable(ctx, op32.form);
+  const bool use_tma = (vec == 4) && (flex || !ctx->no_tma) && tma_supported(g32);
   std::vector<unsigned char> plan_buf(use_tma ? tma_plan_size() : 1);
   TmaPlan* plan = reinterpret_cast<TmaPlan*>(plan_buf.data());
+  FcgDirArgs fx{};
   if (use_tma && which == 0) {
     int rc = tma_init();
-    if (!rc) rc = tma_plan(g32, ctx->r32, ctx->p32, ctx->rold32, ctx->hk32, ctx->z32, ctx->dg32,
-                           pc ? 1 : 0, op32.form, ctx->zc32, plan);
+    if (!rc) rc = tma_plan(g32, flex ? net_pc_zbuf(ctx) - kOff32 : ctx->r32, ctx->p32,
+                           ctx->rold32, ctx->hk32, ctx->z32, ctx->dg32, pc ? 1 : 0, op32.form,
+                           ctx->zc32, flex ? 1 : 0, plan);
     if (rc) return rc;
+    if (flex) {
+      fx.x32 = x32;
+      fx.d64 = ctx->d64;
+      fx.g64 = g;
+      fx.rc = net_pc_rc(ctx);
+      fx.rq = net_pc_rq(ctx);
+      fx.scal = net_pc_scal(ctx);
+      net_pc_rc_strides(ctx, &fx.rcy, &fx.rcx);
+      fx.ncell = net_pc_ncell(ctx);
+    }
   }
   if (which == 2) {
     int rc = compute_faces(ctx, ctx->hk_gen, s);
     if (rc) return rc;
   }
   auto launch = [&]() {
-    if (which == 0 && use_tma) {
+    if (which == 0 && use_tma && flex) {
+      tma_launch_fcg(*plan, true, op32, pb, q32, fx, ctx->partials, ctx->st32, s);
+    } else if (which == 0 && use_tma) {
       tma_launch(*plan, true, op32, pb, q32, ctx->partials, ctx->st32, s);
     } else if (which == 0) {
       if (vec == 4) {
@@ -1458,14 +1406,7 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
     } else if (which == 3) {
       net_pc_launch(ctx, r32, iv, q32, ctx->partials, ctx->st32, s);
     } else if (which == 5 || which == 6) {
-      net_pc_launch_part(ctx, which - 5, r32, iv, q32, ctx->partials, ctx->st32, s);
-    } else if (which == 4) {
-      const dim3 cgrid((unsigned)std::min<int64_t>(
-          std::max<int64_t>((int64_t)nchunk * g.nx * g.nz / 16 / 256, 1), 152 * 8));
-      int rcy = 0, rcx = 0;
-      net_pc_rc_strides(ctx, &rcy, &rcx);
-      k32_update_fcg<<<cgrid, 256, 0, s>>>(g32, g, x32, pb, r32, q32, ctx->d64, net_pc_rc(ctx),
-                                          rcy, rcx, net_pc_scal(ctx), ctx->partials, ctx->st32);
+      net_pc_launch_part(ctx, which - 5, r32, q32, ctx->partials, ctx->st32, s);
     } else if (which == 1) {
       if (vec == 4) {
         if (pc) k32_update<true, 4><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);
@@ -1490,13 +1431,15 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
   SBM_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   if (ms_per_launch) *ms_per_launch = ms / reps;
   double words;
-  if (which == 0) words = 5.0 + (pc ? 1.0 : 0.0) + (op32.form ? 1.0 : 0.0);  // r,p_old,hk,[invd],[diag] -> p_new,q
-  else if (which == 1) words = 6.0 + (pc ? 1.0 : 0.0);                       // x,p,r,q,[invd] -> x,r
-  // restriction r; prolongation r,invd,q,[hk] -> z (coarse grid not counted)
-  else if (which == 3) words = ctx->pc_additive ? 5.0 : 6.0;
-  else if (which == 4) words = 6.0;  // x,p,r,q -> x,r (+ the coarse means)
+  const double dgw = op32.form ? 1.0 : 0.0;
+  if (which == 0 && flex) words = 7.0 + dgw;  // z,p_old,hk,x,[diag] -> p_new,q,x (+ R q)
+  else if (which == 0) words = 5.0 + (pc ? 1.0 : 0.0) + dgw;  // r,p_old,hk,[invd],[diag] -> p_new,q
+  else if (which == 1) words = 6.0 + (pc ? 1.0 : 0.0);        // x,p,r,q,[invd] -> x,r
+  // one application: R r (only after a replacement) and the coarse grid not
+  // counted; multiplicative r,q,hk,[diag] -> r,z; additive r,invd,q -> r,z
+  else if (which == 3) words = ctx->pc_additive ? 5.0 : 5.0 + dgw;
   else if (which == 5) words = 0.0;  // convolutions: coarse grid only (flops, not fine bytes)
-  else if (which == 6) words = 5.0;  // r,invd,q,hk -> z
+  else if (which == 6) words = 5.0 + dgw;  // r,q,hk,[diag] -> r,z
   else words = 3.0;                                                          // p,hk -> q (FP64)
   if (bytes_per_launch) *bytes_per_launch = words * (which == 2 ? 8.0 : 4.0) * n;
   return SBM_OK;

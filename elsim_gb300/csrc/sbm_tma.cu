@@ -12,6 +12,18 @@
 // shuffle).  Each thread produces four y-consecutive voxels (float4 stores
 // of p_new and q).  One block barrier per plane.
 //
+// The flexible-CG variant (FLEX, learned preconditioner) reads the
+// preconditioned residual z in place of r and also carries two passes that
+// would otherwise stream the grid on their own: the previous iteration's
+// x32 += alpha p_old (p_old of the thread's own cells is kept in registers
+// from the staged plane before it is overwritten; x32 is read early in the
+// plane step so its latency hides behind the barrier) and the 4x4x4 means
+// rq = R q of the new q (per-thread sums over the four planes of a coarse
+// slab, combined across the tile's rows through shared memory; z planes per
+// CTA are then a multiple of 4).  Its last block also sets
+// s = RMS(R r - alpha R q), the scale of the next U-Net input, from
+// |R r|^2, R r.R q and |R q|^2.
+//
 // Every mbarrier wait is bounded; on expiry the CTA records done = 5 in the
 // solver state (reported as SBM_ERR_TIMEOUT), waits (bounded) for its own
 // copies in flight and returns.  Loads use only this CTA's shared memory: no
@@ -99,18 +111,25 @@ __device__ __forceinline__ float4 lds4(const float* p) {
   return *reinterpret_cast<const float4*>(p);
 }
 
-template <int FORM, bool PC>
+template <int FORM, bool PC, bool FLEX = false>
 __global__ void __launch_bounds__(NTH)
     k32t_apply_dir(const __grid_constant__ TmaMaps maps, OpArgs<float> op, int zct,
-                   float* __restrict__ pnew, float* __restrict__ q, double* partials,
-                   CgState* st) {
+                   float* __restrict__ pnew, float* __restrict__ q, FcgDirArgs fx,
+                   double* partials, CgState* st) {
   pdl_begin();
   constexpr int NA = 3 + (PC ? 1 : 0) + (FORM == 1 ? 1 : 0);
   constexpr int A_IV = 3, A_DG = 3 + (PC ? 1 : 0);
+  constexpr int RF4 = BOXX / 4;  // float4s per staged row
   extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ float red[FLEX ? NTH / 32 : 1][16];  // FLEX: row-pair sums of q per coarse cell
   if (st->done) return;
   const Geo g = op.g;
   const float beta = (float)st->beta;
+  // FLEX: the previous iteration's x32 += alpha p_old, applied here; after a
+  // residual replacement x32 is first folded into d64 (x32 = alpha p_old)
+  const float alpha_x = FLEX ? (float)st->alpha : 0.f;
+  const bool fold = FLEX && st->accum_pending != 0;
+  const bool xupd = FLEX && (fold || alpha_x != 0.f);
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x;
   const int ntile_y = (g.ny + TX - 1) / TX;
@@ -127,6 +146,17 @@ __global__ void __launch_bounds__(NTH)
   const int i0 = TX * tyb + 4 * q4 + 1;
   const int j = TY * txb + row;
   const bool active = (i0 <= g.ny) && (j <= g.nx);
+  // staged float4s each thread turns into p_new: its own cells (row `row`,
+  // float4 column 1 + q4) and, for 52 threads, one of the halo float4s
+  // (rows 0 and BOXY-1, float4 columns 0 and RF4-1 of the rows between)
+  const int vown = row * RF4 + 1 + q4;
+  int vhalo = -1;
+  if (tid < 2 * RF4) {
+    vhalo = tid < RF4 ? tid : (BOXY - 1) * RF4 + (tid - RF4);
+  } else if (tid < 2 * RF4 + 2 * TY) {
+    const int u = tid - 2 * RF4;
+    vhalo = (1 + u % TY) * RF4 + (u < TY ? 0 : RF4 - 1);
+  }
   auto stage = [&](int s, int a) -> float* {
     return reinterpret_cast<float*>(smem + (size_t)(s * NA + a) * SLOT);
   };
@@ -157,12 +187,12 @@ __global__ void __launch_bounds__(NTH)
     return mbar_wait_bounded(&bar[m % NS], (unsigned)((m / NS) & 1), tries);
   };
   // p_new = z + beta p_old for every staged cell of plane m, written over
-  // p_old in place (stage array 1)
-  auto make_pn = [&](int m) {
+  // p_old in place (stage array 1); returns p_old of the thread's own cells
+  auto make_pn = [&](int m) -> float4 {
     const float4* R = reinterpret_cast<const float4*>(stage(m % NS, 0));
     float4* P = reinterpret_cast<float4*>(stage(m % NS, 1));
     const float4* IV = reinterpret_cast<const float4*>(stage(m % NS, PC ? A_IV : 0));
-    for (int v = tid; v < PLANE / 4; v += NTH) {
+    auto one = [&](int v) {
       const float4 rv = R[v], pv = P[v];
       float4 z = rv;
       if (PC) {
@@ -171,18 +201,48 @@ __global__ void __launch_bounds__(NTH)
       }
       P[v] = make_float4(z.x + beta * pv.x, z.y + beta * pv.y, z.z + beta * pv.z,
                          z.w + beta * pv.w);
-    }
+      return pv;
+    };
+    const float4 pold = one(vown);
+    if (vhalo >= 0) one(vhalo);
+    return pold;
   };
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 pold_nx = zero4;  // p_old of the thread's cells in the next plane
   bool ok = wait_plane(0);
   if (ok) make_pn(0);
   if (ok) ok = wait_plane(1);
-  if (ok) make_pn(1);
+  if (ok) pold_nx = make_pn(1);
   float acc = 0.f;
-  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  // FLEX: R q of the coarse cells whose 4 y x 4 x x 4 z cells lie in this
+  // tile (z planes per CTA are a multiple of 4): per-thread sums over the
+  // slab's planes, row pairs by shuffle, the two pairs through `red`
+  float rq_acc = 0.f;
+  int slab_done = -1;  // coarse z index whose row-pair sums wait in red
+  double a_cq = 0.0, a_qq = 0.0;
+  auto finish_slab = [&](int kc) {  // after a block barrier
+    if (tid < 32) {
+      const int rg = tid >> 4, qq = tid & 15;
+      const int ic = (TX / 4) * tyb + qq, jc = (TY / 4) * txb + rg;
+      if (4 * ic < g.ny && 4 * jc < g.nx) {
+        const float m = (red[2 * rg][qq] + red[2 * rg + 1][qq]) * (1.f / 64.f);
+        const int64_t cc = ic + (int64_t)fx.rcy * (jc + (int64_t)fx.rcx * kc);
+        fx.rq[cc] = m;
+        a_cq += (double)fx.rc[cc] * (double)m;
+        a_qq += (double)m * (double)m;
+      }
+    }
+  };
   const int o = row * BOXX + col;
   for (int mk = 1; mk <= nplanes - 2; ++mk) {
+    const int k = k0 - 1 + mk;
+    const int64_t c = g.ix(i0, j, k);
+    // FLEX: this plane's x32 is read before the barrier (latency hidden)
+    float4 xv = zero4;
+    if (xupd && active) xv = *reinterpret_cast<const float4*>(fx.x32 + c);
+    const float4 pold = pold_nx;
     const bool w = ok && wait_plane(mk + 1);
-    if (w) make_pn(mk + 1);
+    if (w) pold_nx = make_pn(mk + 1);
     // one barrier per plane: p_new of mk+1 is complete, and every thread has
     // finished step mk-1, so the stage of plane mk-2 can be refilled.  The
     // barrier also makes the give-up decision of the bounded waits uniform.
@@ -190,11 +250,14 @@ __global__ void __launch_bounds__(NTH)
       ok = false;
       break;
     }
+    if (FLEX && slab_done >= 0) {
+      finish_slab(slab_done);
+      slab_done = -1;
+    }
     if (tid == 0 && mk >= 2 && mk - 2 + NS < nplanes) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue(mk - 2 + NS);
     }
-    const int k = k0 - 1 + mk;
     const float* PM = stage((mk - 1) % NS, 1);
     const float* PCc = stage(mk % NS, 1);
     const float* PP = stage((mk + 1) % NS, 1);
@@ -245,10 +308,35 @@ __global__ void __launch_bounds__(NTH)
                                         pza[e]);
         qa[e] = (FORM == 0) ? op.scale * s : dg[e] * pa[e + 1] - op.scale * s;
       }
-      const int64_t c = g.ix(i0, j, k);
       *reinterpret_cast<float4*>(pnew + c) = pc;
       *reinterpret_cast<float4*>(q + c) = make_float4(qa[0], qa[1], qa[2], qa[3]);
       acc += (pa[1] * qa[0] + pa[2] * qa[1]) + (pa[3] * qa[2] + pa[4] * qa[3]);
+      if (FLEX) {
+        rq_acc += (qa[0] + qa[1]) + (qa[2] + qa[3]);
+        if (xupd) {
+          if (fold) {
+            const int64_t c64 = fx.g64.ix(i0, j, k);
+            fx.d64[c64] += (double)xv.x;
+            fx.d64[c64 + 1] += (double)xv.y;
+            fx.d64[c64 + 2] += (double)xv.z;
+            fx.d64[c64 + 3] += (double)xv.w;
+            xv = make_float4(alpha_x * pold.x, alpha_x * pold.y, alpha_x * pold.z,
+                             alpha_x * pold.w);
+          } else {
+            xv.x += alpha_x * pold.x;
+            xv.y += alpha_x * pold.y;
+            xv.z += alpha_x * pold.z;
+            xv.w += alpha_x * pold.w;
+          }
+          *reinterpret_cast<float4*>(fx.x32 + c) = xv;
+        }
+      }
+    }
+    if (FLEX && (k & 3) == 0) {  // k = 4 kc + 4 closes coarse slab kc
+      const float v = rq_acc + __shfl_xor_sync(FULL, rq_acc, 16);  // rows 2w+1 and 2w+2
+      if ((tid & 31) < 16) red[tid >> 5][tid & 15] = v;
+      rq_acc = 0.f;
+      slab_done = (k - 1) >> 2;
     }
   }
   // Every thread must agree before the reduction: a CTA whose wait expired
@@ -267,6 +355,33 @@ __global__ void __launch_bounds__(NTH)
     }
     __syncthreads();
     acc = 0.f;
+    a_cq = a_qq = 0.0;
+  } else if (FLEX && slab_done >= 0) {
+    finish_slab(slab_done);
+  }
+  if (FLEX) {
+    double v[3] = {(double)acc, a_cq, a_qq}, tot[3];
+    if (grid_reduce<3>(v, partials, &st->counter[0], tot)) {
+      if (threadIdx.x == 0) {
+        const double pq = tot[0];
+        const double alpha = st->rho / pq;
+        st->pq = pq;
+        st->alpha = alpha;
+        st->accum_pending = 0;
+        // s = RMS(R r - alpha R q) over the valid coarse cells, |R r|^2 in
+        // aux[2]: the scale of the next U-Net input
+        const double ss = (st->aux[2] - 2.0 * alpha * tot[1] + alpha * alpha * tot[2]) /
+                          (double)fx.ncell;
+        const double sc = ss > 0.0 ? sqrt(ss) : 0.0;
+        fx.scal[0] = (float)sc;
+        fx.scal[1] = sc > 0.0 ? (float)(1.0 / sc) : 0.f;
+        if (st->done == 0) {
+          if (pq == 0.0) st->done = 4;
+          else if (!isfinite(pq)) st->done = 3;
+        }
+      }
+    }
+    return;
   }
   double v[1] = {(double)acc}, tot[1];
   if (grid_reduce<1>(v, partials, &st->counter[0], tot)) {
@@ -320,26 +435,37 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-// z planes per CTA when not tuned: the launch should fill whole waves of
-// resident CTAs (a last, partly filled wave leaves SMs idle), and each CTA
-// also streams 2 halo planes, so minimise waves x (planes + 2) over 8..32.
-int auto_zct(int ntile, int nz, int pc, int form) {
-  int dev = 0, nsm = 152, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = smem_bytes(pc, form);
+// Occupancy of one instantiation of the direction kernel.
+int dir_blocks_per_sm(int pc, int form, bool flex, size_t smem) {
+  int per_sm = 0;
   cudaError_t e;
-  if (form == 0)
+  if (flex)
+    e = form ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<1, false, true>, NTH, smem)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<0, false, true>, NTH, smem);
+  else if (form == 0)
     e = pc ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<0, true>, NTH, smem)
            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<0, false>, NTH, smem);
   else
     e = pc ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<1, true>, NTH, smem)
            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k32t_apply_dir<1, false>, NTH, smem);
-  if (e != cudaSuccess || per_sm < 1) return ZCT;
+  return e == cudaSuccess ? per_sm : 0;
+}
+
+// z planes per CTA when not tuned: the launch should fill whole waves of
+// resident CTAs (a last, partly filled wave leaves SMs idle), and each CTA
+// also streams 2 halo planes, so minimise waves x (planes + 2) over 8..32
+// (multiples of 4 for the flexible-CG variant, whose CTAs own whole coarse
+// slabs).
+int auto_zct(int ntile, int nz, int pc, int form, bool flex) {
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int per_sm = dir_blocks_per_sm(pc, form, flex, smem_bytes(pc, form));
+  if (per_sm < 1) return ZCT;
   const int64_t cap = (int64_t)nsm * per_sm;
   int best = ZCT;
   int64_t best_cost = -1;
-  for (int z = 8; z <= 32; ++z) {
+  for (int z = 8; z <= 32; z += flex ? 4 : 1) {
     const int64_t ctas = (int64_t)ntile * ((nz + z - 1) / z);
     const int64_t cost = ((ctas + cap - 1) / cap) * (int64_t)(std::min(z, nz) + 2);
     if (best_cost < 0 || cost < best_cost || (cost == best_cost && z > best)) {
@@ -358,14 +484,18 @@ struct TmaPlan {
   TmaMaps fwd, bwd;  // fwd reads p buffer a, bwd reads buffer b
   dim3 grid;
   size_t smem;
-  int pc, form, zct;
+  int pc, form, zct, flex;
 };
 
 // Builds the tensor maps of one mixed solve.  Buffers are allocation bases
 // (the FP32 layout's element (i,j,k) sits at base + kOff32 + g32.ix(i,j,k)).
+// flex: the flexible-CG variant (no Jacobi array; zct a multiple of 4, and
+// every extent a multiple of 4).
 int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, const float* hk,
-             const float* iv, const float* dg, int pc, int form, int zct, TmaPlan* plan) {
+             const float* iv, const float* dg, int pc, int form, int zct, int flex,
+             TmaPlan* plan) {
   memset(plan, 0, sizeof(*plan));
+  if (flex && (pc || g32.nx % 4 || g32.nz % 4)) return SBM_ERR_STATE;
   if (!make_map(&plan->fwd.r, r, g32) || !make_map(&plan->fwd.p, pa, g32) ||
       !make_map(&plan->fwd.hk, hk, g32) || (pc && !make_map(&plan->fwd.iv, iv, g32)) ||
       (form && !make_map(&plan->fwd.dg, dg, g32)))
@@ -373,18 +503,20 @@ int tma_plan(const Geo& g32, const float* r, const float* pa, const float* pb, c
   plan->bwd = plan->fwd;
   if (!make_map(&plan->bwd.p, pb, g32)) return SBM_ERR_STATE;
   const int ntile = ((g32.ny + TX - 1) / TX) * ((g32.nx + TY - 1) / TY);
-  if (zct < 1) zct = auto_zct(ntile, g32.nz, pc, form);
+  if (zct < 1) zct = auto_zct(ntile, g32.nz, pc, form, flex != 0);
+  if (flex) zct = (zct + 3) / 4 * 4;
   plan->zct = zct;
   plan->grid = dim3((unsigned)ntile, (unsigned)((g32.nz + zct - 1) / zct));
   plan->pc = pc;
   plan->form = form;
+  plan->flex = flex;
   plan->smem = smem_bytes(pc, form);
   return SBM_OK;
 }
 
 int tma_plan_size(void) { return (int)sizeof(TmaPlan); }
 
-// Sets the dynamic shared-memory limit of the four instantiations (once).
+// Sets the dynamic shared-memory limit of the six instantiations (once).
 int tma_init() {
   static bool done = false;
   if (done) return SBM_OK;
@@ -396,27 +528,39 @@ int tma_init() {
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(0, 1)));
   SBM_CUDA_TRY(cudaFuncSetAttribute(k32t_apply_dir<1, true>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(1, 1)));
+  SBM_CUDA_TRY(cudaFuncSetAttribute(k32t_apply_dir<0, false, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(0, 0)));
+  SBM_CUDA_TRY(cudaFuncSetAttribute(k32t_apply_dir<1, false, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(0, 1)));
   done = true;
   return SBM_OK;
 }
 
 // One launch: reads p from buffer a (fwd) or b (!fwd), writes p_new to pnew.
 void tma_launch(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
-                double* partials, CgState* st, cudaStream_t s, bool pdl) {
+                double* partials, CgState* st, cudaStream_t s) {
   const TmaMaps& m = fwd ? plan.fwd : plan.bwd;
-  if (pdl && plan.form == 0 && !plan.pc) {
-    // the flexible-CG loop (learned preconditioner): programmatic launch
-    launch_pdl(k32t_apply_dir<0, false>, plan.grid, dim3(NTH), plan.smem, s, m, op, plan.zct,
-               pnew, q, partials, st);
-    return;
-  }
+  const FcgDirArgs none{};
   if (plan.form == 0) {
-    if (plan.pc) k32t_apply_dir<0, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
-    else k32t_apply_dir<0, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
+    if (plan.pc) k32t_apply_dir<0, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, none, partials, st);
+    else k32t_apply_dir<0, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, none, partials, st);
   } else {
-    if (plan.pc) k32t_apply_dir<1, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
-    else k32t_apply_dir<1, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, partials, st);
+    if (plan.pc) k32t_apply_dir<1, true><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, none, partials, st);
+    else k32t_apply_dir<1, false><<<plan.grid, NTH, plan.smem, s>>>(m, op, plan.zct, pnew, q, none, partials, st);
   }
+}
+
+// One launch of the flexible-CG variant (plan built with flex), with
+// programmatic dependent launch inside the captured loop.
+void tma_launch_fcg(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, float* pnew, float* q,
+                    const FcgDirArgs& fx, double* partials, CgState* st, cudaStream_t s) {
+  const TmaMaps& m = fwd ? plan.fwd : plan.bwd;
+  if (plan.form == 0)
+    launch_pdl(k32t_apply_dir<0, false, true>, plan.grid, dim3(NTH), plan.smem, s, m, op,
+               plan.zct, pnew, q, fx, partials, st);
+  else
+    launch_pdl(k32t_apply_dir<1, false, true>, plan.grid, dim3(NTH), plan.smem, s, m, op,
+               plan.zct, pnew, q, fx, partials, st);
 }
 
 }  // namespace sbm

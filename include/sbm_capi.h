@@ -229,11 +229,13 @@ int sbm_cg_solve(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double scale,
 /* Benchmark hook (no counterpart in the reference): times `reps` launches
  * of one solver kernel on the context stream with CUDA events, replaying the
  * arguments of the last mixed-precision solve.  which 0: FP32 fused
- * direction + stencil kernel; 1: FP32 vector update; 2: FP64 stencil + dot;
- * after a learned-preconditioner solve also 3: one application of the
- * preconditioner (restriction, U-Net, prolongation: 12 launches), 4: the
- * flexible-CG update, 5: the 9 U-Net convolutions alone (0 fine-grid
- * bytes) and 6: the multiplicative prolongation / Jacobi step alone.
+ * direction + stencil kernel (after a learned-preconditioner solve its
+ * flexible-CG variant, which also applies the deferred x update and
+ * restricts q); 1: FP32 vector update; 2: FP64 stencil + dot; after a
+ * learned-preconditioner solve also 3: one application of the
+ * preconditioner (restriction, U-Net, the step that updates r and forms z:
+ * 12 launches), 5: the 9 U-Net convolutions alone (0 fine-grid bytes) and
+ * 6: the multiplicative step alone.  which 4 is not used.
  * Reports the mean time and the algorithmic bytes one launch (one
  * application) moves on the fine grid. */
 int sbm_bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch,
