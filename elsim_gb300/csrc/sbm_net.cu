@@ -846,10 +846,9 @@ __device__ void fcg_close(CgState* st, double zr, double zq, double rr, bool rup
 // axis: fine cell e of coarse cell m lies at m - 3/8 + e/4 in coarse units.
 __device__ __forceinline__ void interp1(int fi, int n, int* lo, int* hi, float* wlo) {
   const int m = fi >> 2, e = fi & 3;
-  const float wl[4] = {0.375f, 0.125f, 0.875f, 0.625f};
   *lo = (e < 2) ? max(m - 1, 0) : m;
   *hi = (e < 2) ? m : min(m + 1, n - 1);
-  *wlo = wl[e];
+  *wlo = 0.375f - 0.25f * (float)(e & 1) + 0.5f * (float)(e >> 1);  // 3/8, 1/8, 7/8, 5/8
 }
 
 // The additive form: r -= alpha q (the pending update of the flexible CG,
@@ -1261,10 +1260,14 @@ void net_pc_launch(sbm_ctx* ctx, float* r32, const float* iv32, const float* q32
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   const Geo& g = ctx->g32;
   const netd::Dims& c = pc->c;
-  launch_pdl(netd::k_pc_restrict, dim3(netd::grid_for(pc->cv.v())), dim3(256), 0, s, g, c, pc->cv,
-             (const float*)r32, pc->rc, (const float*)pc->rq, partials, (float*)pc->scal, st);
-  launch_pdl(netd::k_pc_pack, dim3(netd::grid_for(c.v())), dim3(256), 0, s, c.v(), pc->rc,
-             (const float*)pc->rq, (const float*)pc->scal, pc->w->in0, partials, st);
+  // coarse-grid kernels with a grid reduction: two blocks per SM at most,
+  // so the last block sums few partials
+  const int rgrid = std::min(netd::grid_for(pc->cv.v()), 2 * 152);
+  const int pgrid = std::min(netd::grid_for(c.v()), 2 * 152);
+  launch_pdl(netd::k_pc_restrict, dim3(rgrid), dim3(256), 0, s, g, c, pc->cv, (const float*)r32,
+             pc->rc, (const float*)pc->rq, partials, (float*)pc->scal, st);
+  launch_pdl(netd::k_pc_pack, dim3(pgrid), dim3(256), 0, s, c.v(), pc->rc, (const float*)pc->rq,
+             (const float*)pc->scal, pc->w->in0, partials, st);
   SBM_LAUNCHED(2);
   netd::forward(pc->net, *pc->w, false, &st->done, &st->pc_off, s);
   const int64_t items = (int64_t)(g.ny / 4) * g.nx * (g.nz / 4);
