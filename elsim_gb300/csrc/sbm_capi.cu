@@ -65,8 +65,9 @@ static int dalloc(double** p, int64_t n) {
 
 int ensure_fp32_work(sbm_ctx* ctx) {
   if (ctx->hk32) return SBM_OK;
-  float** bufs[] = {&ctx->hk32, &ctx->dg32, &ctx->r32, &ctx->p32,
-                    &ctx->q32,  &ctx->x32,  &ctx->z32, &ctx->rold32};
+  float** bufs[] = {&ctx->hk32,   &ctx->dg32,   &ctx->r32,    &ctx->p32,    &ctx->q32,
+                    &ctx->x32,    &ctx->z32,    &ctx->rold32, &ctx->hklo32, &ctx->dglo32,
+                    &ctx->r0hi32, &ctx->r0lo32, &ctx->dhi32,  &ctx->dlo32};
   for (float** b : bufs) {
     cudaError_t e = cudaMalloc(b, sizeof(float) * (size_t)ctx->g32.nh);
     if (e != cudaSuccess) {
@@ -200,7 +201,9 @@ int sbm_ctx_destroy(sbm_ctx* ctx) {
                  ctx->q64,    ctx->d64,    ctx->r0,     ctx->partials, ctx->d_scal,
                  ctx->fc64};
   for (double* q : d) cudaFree(q);
-  float* fl[] = {ctx->hk32, ctx->dg32, ctx->r32, ctx->p32, ctx->q32, ctx->x32, ctx->z32, ctx->rold32};
+  float* fl[] = {ctx->hk32,   ctx->dg32,   ctx->r32,    ctx->p32,   ctx->q32,
+                 ctx->x32,    ctx->z32,    ctx->rold32, ctx->hklo32, ctx->dglo32,
+                 ctx->r0hi32, ctx->r0lo32, ctx->dhi32,  ctx->dlo32};
   for (float* q : fl) cudaFree(q);
   cudaFree(ctx->st);
   cudaFree(ctx->st32);

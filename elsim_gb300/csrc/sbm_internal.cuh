@@ -248,16 +248,60 @@ struct OpArgs {
   const T* fc = nullptr;
 };
 
+// ------------------------------------------- double-float arithmetic
+// An unevaluated sum hi + lo of two FP32 values with |lo| <= ulp(hi)/2
+// carries about 48 significant bits.  The mixed solver keeps its FP64-grade
+// quantities in this form (the correction, the initial residual, the
+// coefficients as hi + lo splits of the FP64 values) and forms the
+// residual replacement with FP32 instructions, whose rate on GB300 is
+// some 64x that of FP64.  Error-free transformations: Knuth's TwoSum,
+// Dekker's Fast2Sum (|a| >= |b|) and the FMA product error; the _rn
+// intrinsics keep the compiler from contracting or reordering them.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+  const DF s = df_two_sum(x.hi, y.hi);
+  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ DF df_sub(DF x, DF y) { return df_add(x, DF{-y.hi, -y.lo}); }
+__device__ __forceinline__ DF df_add_f(DF x, float y) {
+  const DF s = df_two_sum(x.hi, y);
+  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, x.lo));
+}
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return df_fast_two_sum(p, e);
+}
+// hi + lo split of an FP64 value (lo exact to FP32 rounding)
+__host__ __device__ __forceinline__ void df_split(double v, float* hi, float* lo) {
+  const float h = (float)v;
+  *hi = h;
+  *lo = (float)(v - (double)h);
+}
+
 // Extra operands of the flexible-CG direction kernel (learned
 // preconditioner).  That kernel also applies the previous iteration's
 // deferred x32 += alpha p_old (or, after a residual replacement, folds x32
-// into d64 first) and restricts q = A p_new to the coarse grid (rq = 4x4x4
+// into the double-float correction first) and restricts q = A p_new to the coarse grid (rq = 4x4x4
 // means, strides rcy / rcx of the coarse arrays), so that neither x nor the
 // restriction of the residual needs a pass of its own.
 struct FcgDirArgs {
   float* x32 = nullptr;       // FP32 correction (g32 layout)
-  double* d64 = nullptr;      // FP64 correction (g64 layout)
-  Geo g64{};
+  float* dhi = nullptr;       // double-float correction hi + lo (g32 layout)
+  float* dlo = nullptr;
   const float* rc = nullptr;  // R r of the current residual (coarse)
   float* rq = nullptr;        // R q of the new direction (coarse, written)
   float* scal = nullptr;      // s = RMS(R r_next), 1/s (written by the last block)
@@ -359,6 +403,11 @@ struct sbm_ctx {
   // FP32 work: half coefficient, diagonal, residual, direction, A*direction, correction, z
   float *hk32 = nullptr, *dg32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr,
         *x32 = nullptr, *z32 = nullptr, *rold32 = nullptr;
+  // double-float work (FP32 layout): low parts of the half coefficient and
+  // the diagonal (their high parts are hk32 / dg32), the initial residual
+  // and the accumulated correction of the mixed solver
+  float *hklo32 = nullptr, *dglo32 = nullptr, *r0hi32 = nullptr, *r0lo32 = nullptr,
+        *dhi32 = nullptr, *dlo32 = nullptr;
   // reductions
   double* partials = nullptr;
   sbm::CgState* st = nullptr;      // device: outer / FP64 state

@@ -554,13 +554,15 @@ int solve_fp64(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
 // layout (make_geo32); every time the FP32 recursive residual has dropped
 // by delta^2 since the last replacement -- and whenever it claims
 // convergence or the cap is reached -- the true residual
-//     r = r0 - A (d64 + x32)
-// is recomputed in FP64 from the FP64 correction d64 and the FP32 partial
-// correction x32, converted to FP32 and substituted for the recursive
-// residual; x32 is then folded into d64.  The FP32 search direction is kept
+//     r = r0 - A (d + x32)
+// is recomputed in double-float arithmetic (FP32 pairs, about 48
+// significant bits; the initial residual r0 itself comes from the FP64
+// stencil) from the double-float correction d and the FP32 partial
+// correction x32, rounded to FP32 and substituted for the recursive
+// residual; x32 is then folded into d.  The FP32 search direction is kept
 // across replacements, so the Krylov space is not restarted (unlike
-// restarted iterative refinement).  Convergence is decided only on the FP64
-// true residual: on return ||b - A x||_2 / ||b - A x0||_2 <= tol.
+// restarted iterative refinement).  Convergence is decided only on the
+// recomputed true residual: on return ||b - A x||_2 / ||b - A x0||_2 <= tol.
 
 namespace {
 
@@ -749,14 +751,14 @@ __device__ __forceinline__ int64_t item_ix(const Geo& g, int nchunk, int64_t u, 
 // x32 += alpha p; r32 -= alpha q; r.r and r.z (FP32 per thread, FP64 across
 // threads); decides whether the next step is a reliable update.  After a
 // reliable update the FP32 correction accumulated so far is first folded
-// into the FP64 one (d64 += x32, x32 = alpha p).
+// into the double-float one (d += x32, x32 = alpha p).
 // FLEX (flexible CG with the learned preconditioner): rho and beta are left
 // to the preconditioner kernel that follows.
 template <bool PC, int VEC, bool FLEX = false>
 __global__ void __launch_bounds__(256)
-    k32_update(Geo g, Geo g64, int nchunk, float* __restrict__ x, const float* __restrict__ p,
+    k32_update(Geo g, int nchunk, float* __restrict__ x, const float* __restrict__ p,
                float* __restrict__ r, const float* __restrict__ q, const float* __restrict__ invd,
-               double* __restrict__ d64, double* partials, CgState* st) {
+               float* __restrict__ dhi, float* __restrict__ dlo, double* partials, CgState* st) {
   if (st->done) return;
   const bool fold = st->accum_pending != 0;
   const float alpha = (float)st->alpha;
@@ -771,11 +773,11 @@ __global__ void __launch_bounds__(256)
       const float4 pv = ld4(p + c), qv = ld4(q + c);
       float4 rv = ld4(r + c);
       if (fold) {
-        const int64_t c64 = g64.ix(i, j, k);
-        d64[c64] += (double)xv.x;
-        d64[c64 + 1] += (double)xv.y;
-        d64[c64 + 2] += (double)xv.z;
-        d64[c64 + 3] += (double)xv.w;
+        const float4 dh = ld4(dhi + c), dl = ld4(dlo + c);
+        const DF d0 = df_add_f(DF{dh.x, dl.x}, xv.x), d1 = df_add_f(DF{dh.y, dl.y}, xv.y);
+        const DF d2 = df_add_f(DF{dh.z, dl.z}, xv.z), d3 = df_add_f(DF{dh.w, dl.w}, xv.w);
+        st4(dhi + c, make_float4(d0.hi, d1.hi, d2.hi, d3.hi));
+        st4(dlo + c, make_float4(d0.lo, d1.lo, d2.lo, d3.lo));
         xv = make_float4(alpha * pv.x, alpha * pv.y, alpha * pv.z, alpha * pv.w);
       } else {
         xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
@@ -792,7 +794,9 @@ __global__ void __launch_bounds__(256)
     } else {
       float xv = x[c];
       if (fold) {
-        d64[g64.ix(i, j, k)] += (double)xv;
+        const DF d = df_add_f(DF{dhi[c], dlo[c]}, xv);
+        dhi[c] = d.hi;
+        dlo[c] = d.lo;
         xv = alpha * p[c];
       } else {
         xv += alpha * p[c];
@@ -830,57 +834,57 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Reliable update: r = r0 - A_h (d64 + x32) in FP64 (ghost rules of the
-// search direction on the correction), r32 = (float) r, z = invd*r32;
-// convergence on the FP64 norm, new rho / beta.  No-op unless flagged.
-// FLEX: rho / beta and the first-residual flag are left to the flexible
-// preconditioner kernel that follows.
-// Tiles of BX x BY columns x zc planes are walked grid-stride by a grid of
-// a few blocks per SM (rel_grid): the launch is a no-op in most iterations,
-// and a small grid keeps that no-op cheap.
+// Operands of the double-float residual replacement (FP32 layout, base +
+// kOff32): hk = hkhi + hklo and, for the CnE form, diag = dghi + dglo split
+// from the FP64 fields; r0 = r0hi + r0lo; the correction d = dhi + dlo
+// plus x32.
+struct DfResArgs {
+  const float *hkhi, *hklo, *dghi, *dglo, *r0hi, *r0lo, *dhi, *dlo, *x32;
+  float* r32;
+  const float* invd32;
+  float scale_hi, scale_lo;
+  int bcx0, bcx1;
+};
+
+// Reliable update in double-float arithmetic: r = r0 - A (d + x32) with
+// every operand carried as an FP32 pair (about 48 significant bits, ample
+// for residuals down to 1e-8 of r0 at 256^3), r32 = the high part, z =
+// invd*r32 (Jacobi) and the norms as in k_rel_resid, whose FP64 stencil it
+// replaces in the mixed solver: about 230 FP32 instructions per voxel
+// instead of about 25 FP64 ones.  The correction V = d + x32 of each voxel
+// is formed once and shared with the plane's other threads through a
+// shared-memory tile (its column rolls along z); the half coefficients
+// come from global memory (L1 / L2).  Tiles of BX x BY columns x zc planes
+// are walked grid-stride by a few blocks per SM, as in k_rel_resid.
 template <int FORM, bool PC, bool FLEX = false>
 __global__ void __launch_bounds__(BX* BY)
-    k_rel_resid(OpArgs<double> op, Geo g32, int zc, const double* __restrict__ d64,
-                const float* __restrict__ x32, const double* __restrict__ r0,
-                float* __restrict__ r32, const float* __restrict__ invd32, double* partials,
-                CgState* st) {
+    k_rel_resid_df(Geo g, int zc, DfResArgs a, double* partials, CgState* st) {
   pdl_begin();
   if (!st->reliable || st->done) return;
-  const Geo g = op.g;
-  // the first replacement of a solve sees a zero correction (d64 and x32
-  // were just cleared): the true residual is r0 itself, no stencil needed
   const bool zero_corr = st->initial != 0;
   const int nty = (g.ny + BX - 1) / BX, ntx = (g.nx + BY - 1) / BY;
   const int ntiles = nty * ntx * ((g.nz + zc - 1) / zc);
-  double a_rr = 0.0, a_r32 = 0.0, a_rz = 0.0;
+  double a_rr = 0.0, a_rz = 0.0;
+  __shared__ float svh[BY + 2][BX + 2], svl[BY + 2][BX + 2];
+  const DF scale{a.scale_hi, a.scale_lo};
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int ib = (t % nty) * BX, jb = ((t / nty) % ntx) * BY;  // cell (ib + col, jb + row)
+    const int ib = (t % nty) * BX, jb = ((t / nty) % ntx) * BY;
     const int i = ib + threadIdx.x + 1, j = jb + threadIdx.y + 1;
     const int k0 = (t / (nty * ntx)) * zc + 1;
     const int k1 = min(k0 + zc - 1, g.nz);
     const bool active = (i <= g.ny) && (j <= g.nx);
+    float t_rr = 0.f, t_rz = 0.f;
     if (active && zero_corr) {
+      // first replacement of a solve: the correction is zero, r = r0
       for (int k = k0; k <= k1; ++k) {
-        const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
-        const double rv = r0[c];
-        const float rf = (float)rv;
-        r32[c3] = rf;
-        const float zf = PC ? invd32[c3] * rf : rf;
-        a_rr += rv * rv;
-        a_r32 += (double)rf * (double)rf;
-        a_rz += (double)rf * (double)zf;
+        const int64_t c = g.ix(i, j, k);
+        const float rf = a.r0hi[c];
+        a.r32[c] = rf;
+        const float zf = PC ? a.invd32[c] * rf : rf;
+        t_rr += rf * rf;
+        t_rz += rf * zf;
       }
     } else if (!zero_corr) {
-      // The correction V = d64 + (double)x32 of each cell is formed once: the
-      // thread's own column rolls along z (vm, vc, vp) and every plane is
-      // shared, with its in-plane halo, through shared memory, so the lateral
-      // neighbours are read instead of formed again (the same operations on
-      // the same operands: the same bits).  This cuts the FP64 instructions
-      // per cell from about 34 to about 25 (1038 -> 672 us per replacement
-      // at 256^3); the kernel is FP64-pipe bound.
-      // All threads of the block march the same planes k0..k1 (uniform
-      // barriers); 80 of them also form the halo cells of each plane.
-      __shared__ double sv[BY + 2][BX + 2];
       const int tx = threadIdx.x, ty = threadIdx.y, tf = ty * BX + tx;
       int hrow = -1, hcol = -1;
       if (tf < 2 * BX) {  // rows 0 and BY + 1 (x halo)
@@ -892,64 +896,55 @@ __global__ void __launch_bounds__(BX* BY)
         hcol = u < BY ? 0 : BX + 1;
       }
       const int hi = ib + hcol, hj = jb + hrow;
-      // only interior halo cells are ever read (the ghost rules replace the rest)
+      // only interior halo cells are read (the ghost rules replace the rest)
       const bool hact = hrow >= 0 && hi >= 1 && hi <= g.ny && hj >= 1 && hj <= g.nx;
       auto corr = [&](int ii, int jj, int kk) {
-        return d64[g.ix(ii, jj, kk)] + (double)x32[g32.ix(ii, jj, kk)];
+        const int64_t c = g.ix(ii, jj, kk);
+        return df_add_f(DF{a.dhi[c], a.dlo[c]}, a.x32[c]);
       };
-      double vc = 0.0, vm = 0.0;
+      auto hk = [&](int64_t c) { return DF{a.hkhi[c], a.hklo[c]}; };
+      DF vc{0.f, 0.f}, vm{0.f, 0.f};
       if (active) {
         vc = corr(i, j, k0);
         vm = (k0 == 1) ? vc : corr(i, j, k0 - 1);
       }
       for (int k = k0; k <= k1; ++k) {
-        double vp = 0.0, hv = 0.0;
+        DF vp{0.f, 0.f}, hv{0.f, 0.f};
         if (active) vp = (k == g.nz) ? vc : corr(i, j, k + 1);
         if (hact) hv = corr(hi, hj, k);
         __syncthreads();  // the previous plane's readers are done
-        sv[ty + 1][tx + 1] = vc;
-        if (hrow >= 0) sv[hrow][hcol] = hv;
+        svh[ty + 1][tx + 1] = vc.hi;
+        svl[ty + 1][tx + 1] = vc.lo;
+        if (hrow >= 0) {
+          svh[hrow][hcol] = hv.hi;
+          svl[hrow][hcol] = hv.lo;
+        }
         __syncthreads();
         if (active) {
-          const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
-          const double pc = vc;
-          const double pym = (i == 1) ? pc : sv[ty + 1][tx];
-          const double pyp = (i == g.ny) ? pc : sv[ty + 1][tx + 2];
-          const double pxm = (j == 1) ? (op.bcx0 ? 0.0 : pc) : sv[ty][tx + 1];
-          const double pxp = (j == g.nx) ? (op.bcx1 ? 0.0 : pc) : sv[ty + 2][tx + 1];
-          const double pzm = vm;
-          const double pzp = vp;
-          const double* hk = op.hk;
-          // With the stored faces, the diagonal form sum_f c_f p_nb - (sum_f
-          // c_f) p_c: 7 FP64 operations instead of 12 (the kernel is bound
-          // by the FP64 pipe).  A copy ghost (p_nb = p_c) still cancels in
-          // value; the residual's rounding error, about 1e-16 of sum_f c_f
-          // |p|, stays far below what the rel-res test resolves.
-          double s;
-          if (op.fc) {
-            const double* fy = op.fc;
-            const double* fx = op.fc + g.nh;
-            const double* fz = op.fc + 2 * g.nh;
-            s = fy[c] * pyp;
-            s = fma(fy[c - 1], pym, s);
-            s = fma(fx[c], pxp, s);
-            s = fma(fx[c - g.sx], pxm, s);
-            s = fma(fz[c], pzp, s);
-            s = fma(fz[c - g.sz], pzm, s);
-            s = fma(-op.fc[3 * g.nh + c], pc, s);
-          } else {
-            s = face_sum<double>(hk[c], pc, hk[c + 1], pyp, hk[c - 1], pym, hk[c + g.sx], pxp,
-                                 hk[c - g.sx], pxm, hk[c + g.sz], pzp, hk[c - g.sz], pzm);
-          }
-          const double ad = (FORM == 0) ? op.scale * s : op.diag[c] * pc - op.scale * s;
-          const double rv = r0[c] - ad;
-          const float rf = (float)rv;
-          r32[c3] = rf;
-          a_rr += rv * rv;
-          a_r32 += (double)rf * (double)rf;
+          const int64_t c = g.ix(i, j, k);
+          const DF zero{0.f, 0.f};
+          const DF vym = (i == 1) ? vc : DF{svh[ty + 1][tx], svl[ty + 1][tx]};
+          const DF vyp = (i == g.ny) ? vc : DF{svh[ty + 1][tx + 2], svl[ty + 1][tx + 2]};
+          const DF vxm = (j == 1) ? (a.bcx0 ? zero : vc) : DF{svh[ty][tx + 1], svl[ty][tx + 1]};
+          const DF vxp =
+              (j == g.nx) ? (a.bcx1 ? zero : vc) : DF{svh[ty + 2][tx + 1], svl[ty + 2][tx + 1]};
+          const DF kc = hk(c);
+          // S(V) = sum_f (hk_nb + hk_c) (V_nb - V_c), faces y+, y-, x+, x-, z+, z-
+          DF sum = df_mul(df_add(hk(c + 1), kc), df_sub(vyp, vc));
+          sum = df_add(sum, df_mul(df_add(hk(c - 1), kc), df_sub(vym, vc)));
+          sum = df_add(sum, df_mul(df_add(hk(c + g.sx), kc), df_sub(vxp, vc)));
+          sum = df_add(sum, df_mul(df_add(hk(c - g.sx), kc), df_sub(vxm, vc)));
+          sum = df_add(sum, df_mul(df_add(hk(c + g.sz), kc), df_sub(vp, vc)));
+          sum = df_add(sum, df_mul(df_add(hk(c - g.sz), kc), df_sub(vm, vc)));
+          DF av = df_mul(scale, sum);
+          if (FORM == 1) av = df_sub(df_mul(DF{a.dghi[c], a.dglo[c]}, vc), av);
+          const DF rv = df_sub(DF{a.r0hi[c], a.r0lo[c]}, av);
+          const float rf = rv.hi;
+          a.r32[c] = rf;
+          t_rr += rf * rf;
           if (!FLEX) {  // the flexible solver takes rho from its preconditioner kernel
-            const float zf = PC ? invd32[c3] * rf : rf;
-            a_rz += (double)rf * (double)zf;
+            const float zf = PC ? a.invd32[c] * rf : rf;
+            t_rz += rf * zf;
           }
         }
         vm = vc;
@@ -957,9 +952,11 @@ __global__ void __launch_bounds__(BX* BY)
       }
       __syncthreads();  // the next tile reuses the plane tile
     }
+    a_rr += (double)t_rr;
+    a_rz += (double)t_rz;
   }
-  double v[3] = {a_rr, a_r32, a_rz}, tot[3];
-  if (grid_reduce<3>(v, partials, &st->counter[3], tot)) {
+  double v[2] = {a_rr, a_rz}, tot[2];
+  if (grid_reduce<2>(v, partials, &st->counter[3], tot)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
       const double rms = (st->rr0 > 0.0) ? sqrt(tot[0] / st->rr0) : 0.0;
       st->rms = rms;
@@ -967,36 +964,39 @@ __global__ void __launch_bounds__(BX* BY)
       if (!isfinite(rms)) st->done = 3;
       else if (!(rms > st->tol)) st->done = 1;
       else if (st->iter >= st->max_it) st->done = 2;
-      if (st->initial) st->aux[0] = tot[1];
+      if (st->initial) st->aux[0] = tot[0];
       st->aux[1] = 0.0;  // the coarse residual of the learned preconditioner is stale
       if (!FLEX) {
-        st->beta = st->initial ? 0.0 : tot[2] / st->rho;
-        st->rho = tot[2];
+        st->beta = st->initial ? 0.0 : tot[1] / st->rho;
+        st->rho = tot[1];
         st->initial = 0;
       }
-      st->rr = tot[1];
-      st->maxrr = tot[1];
+      st->rr = tot[0];
+      st->maxrr = tot[0];
       st->reliable = 0;
       st->accum_pending = 1;
     }
   }
 }
 
-// x += d64 + x32 on the interior (the total correction of the mixed solve).
+// x += dhi + dlo + x32 on the interior (the total correction of the mixed
+// solve; the FP32 parts summed in FP64).
 __global__ void k_finish(Geo g, Geo g32, int zc, double* __restrict__ x,
-                         const double* __restrict__ d64, const float* __restrict__ x32) {
+                         const float* __restrict__ dhi, const float* __restrict__ dlo,
+                         const float* __restrict__ x32) {
   SBM_COLUMN_PROLOGUE(g, zc)
   if (!active) return;
   for (int k = k0; k <= k1; ++k) {
-    const int64_t c = g.ix(i, j, k);
-    x[c] = x[c] + (d64[c] + (double)x32[g32.ix(i, j, k)]);
+    const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
+    x[c] = x[c] + (((double)dhi[c3] + (double)dlo[c3]) + (double)x32[c3]);
   }
 }
 
-// hk32/dg32 = (float) hk64/diag64 over the padded domain, FP64 layout ->
-// FP32 layout.
-__global__ void k_to32(Geo g64, Geo g32, const double* __restrict__ hk, float* __restrict__ hk32,
-                       const double* __restrict__ dg, float* __restrict__ dg32) {
+// a32 = (float) a over the padded domain, FP64 layout -> FP32 layout, with
+// the low part a - a32 in alo when given (and the same for b).
+__global__ void k_to32(Geo g64, Geo g32, const double* __restrict__ a, float* __restrict__ a32,
+                       const double* __restrict__ b, float* __restrict__ b32,
+                       float* __restrict__ alo = nullptr, float* __restrict__ blo = nullptr) {
   const int64_t n = g64.nh;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x) {
@@ -1005,8 +1005,15 @@ __global__ void k_to32(Geo g64, Geo g32, const double* __restrict__ hk, float* _
     const int j = (int)(rr % (g64.nx + 2));
     const int k = (int)(rr / (g64.nx + 2));
     const int64_t c3 = g32.ix(i, j, k);
-    hk32[c3] = (float)hk[c];
-    if (dg) dg32[c3] = (float)dg[c];
+    float h, l;
+    df_split(a[c], &h, &l);
+    a32[c3] = h;
+    if (alo) alo[c3] = l;
+    if (b) {
+      df_split(b[c], &h, &l);
+      b32[c3] = h;
+      if (blo) blo[c3] = l;
+    }
   }
 }
 
@@ -1064,12 +1071,11 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
                        tma_supported(g32);
   const bool pc = sp.precond == SBM_PC_JACOBI || (sp.precond == SBM_PC_LEARNED && !learned);
   ctx->last_precond = learned ? SBM_PC_LEARNED : (pc ? SBM_PC_JACOBI : SBM_PC_NONE);
-  // Reliable-update factor: the FP64 residual replacement is an FP64-ALU-
-  // bound stencil (~0.6 ms at 256^3), so replace once the FP32 residual has
-  // fallen by 1e-2 (Jacobi / none; same iteration counts as 0.1 at 256^3)
-  // or 1e-4 (flexible CG, which converges in far fewer iterations: 256^3
-  // headline solve 29.13 / 29.51 / 28.69 / 28.67 ms at 1e-3 / 3e-4 / 1e-4 /
-  // 3e-5, 61-62 iterations each).
+  // Reliable-update factor: replace the residual once the FP32 residual
+  // has fallen by 1e-2 (Jacobi / none; same iteration counts as 0.1 at
+  // 256^3) or 1e-4 (flexible CG, which converges in far fewer iterations:
+  // 256^3 headline solve 29.13 / 29.51 / 28.69 / 28.67 ms at 1e-3 / 3e-4 /
+  // 1e-4 / 3e-5 with the FP64 replacement, 61-62 iterations each).
   const double delta = ctx->inner_tol > 0 ? ctx->inner_tol : (learned ? 1e-4 : 1e-2);
   CgState* h = &ctx->h_st[2];
   memset(h, 0, sizeof(CgState));
@@ -1081,12 +1087,14 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   h->initial = 1;
   SBM_CUDA_TRY(cudaEventRecord(ctx->ev0, s));
   SBM_CUDA_TRY(cudaMemcpyAsync(ctx->st, h, sizeof(CgState), cudaMemcpyHostToDevice, s));
-  SBM_CUDA_TRY(cudaMemsetAsync(ctx->d64, 0, sizeof(double) * g.nh, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->dhi32, 0, sizeof(float) * g32.nh, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->dlo32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->x32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->p32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->rold32, 0, sizeof(float) * g32.nh, s));
+  // FP32 coefficients and, for the double-float replacement, their low parts
   k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
-                                         dg32);
+                                         dg32, ctx->hklo32 + kOff32, ctx->dglo32 + kOff32);
   SBM_LAUNCHED(1);
   if (pc || learned) {
     k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
@@ -1098,8 +1106,8 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   FcgDirArgs fx{};
   if (learned) {
     fx.x32 = x32;
-    fx.d64 = ctx->d64;
-    fx.g64 = g;
+    fx.dhi = ctx->dhi32 + kOff32;
+    fx.dlo = ctx->dlo32 + kOff32;
     fx.rc = net_pc_rc(ctx);
     fx.rq = net_pc_rq(ctx);
     fx.scal = net_pc_scal(ctx);
@@ -1109,7 +1117,8 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   // with the learned preconditioner the direction kernels read z from its buffer
   float* const zl = learned ? net_pc_zbuf(ctx) : nullptr;
   const float* const rdir = learned ? zl : r32;
-  // r0 = b - A x0 with x0's stored ghosts (FP64); sets rr0.
+  // r0 = b - A x0 with x0's stored ghosts (FP64); sets rr0; split into the
+  // double-float pair the replacements start from
   if (sp.form == 0)
     k_residual_mem<0, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x,
                                                               ctx->r0, ctx->p64, nullptr,
@@ -1118,7 +1127,9 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
     k_residual_mem<1, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x,
                                                               ctx->r0, ctx->p64, nullptr,
                                                               ctx->partials, ctx->st);
-  SBM_LAUNCHED(1);
+  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, ctx->r0, ctx->r0hi32 + kOff32, nullptr, nullptr,
+                                         ctx->r0lo32 + kOff32, nullptr);
+  SBM_LAUNCHED(2);
   const int64_t items = (int64_t)nchunk * g.nx * g.nz;
   const dim3 fgrid(flat_blocks(items));
   const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
@@ -1127,16 +1138,27 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   // SM (four fit at its 56 registers), so its usual no-op launch is cheap
   const int64_t rel_tiles = (int64_t)sh64.grid.x * sh64.grid.y * sh64.grid.z;
   const dim3 rgrid((unsigned)std::min<int64_t>(rel_tiles, 152 * 4));
+  DfResArgs dfa{};
+  dfa.hkhi = hk32;
+  dfa.hklo = ctx->hklo32 + kOff32;
+  dfa.dghi = dg32;
+  dfa.dglo = ctx->dglo32 + kOff32;
+  dfa.r0hi = ctx->r0hi32 + kOff32;
+  dfa.r0lo = ctx->r0lo32 + kOff32;
+  dfa.dhi = ctx->dhi32 + kOff32;
+  dfa.dlo = ctx->dlo32 + kOff32;
+  dfa.x32 = x32;
+  dfa.r32 = r32;
+  dfa.invd32 = iv32;
+  df_split(sp.scale, &dfa.scale_hi, &dfa.scale_lo);
+  dfa.bcx0 = sp.bcx0;
+  dfa.bcx1 = sp.bcx1;
   auto rel = [&](cudaStream_t s2) {
-#define SBM_REL(F, P)                                                                          \
-  k_rel_resid<F, P><<<rgrid, sh64.block, 0, s2>>>(op64, g32, sh64.zc, ctx->d64, x32,          \
-                                                   ctx->r0, r32, iv32, ctx->partials,          \
-                                                   ctx->st)
+#define SBM_REL(F, P) \
+  k_rel_resid_df<F, P><<<rgrid, sh64.block, 0, s2>>>(g32, sh64.zc, dfa, ctx->partials, ctx->st)
     if (learned) {
-      launch_pdl(sp.form ? k_rel_resid<1, false, true> : k_rel_resid<0, false, true>, rgrid,
-                 sh64.block, 0, s2, op64, g32, sh64.zc, (const double*)ctx->d64,
-                 (const float*)x32, (const double*)ctx->r0, r32, (const float*)iv32,
-                 ctx->partials, ctx->st);
+      launch_pdl(sp.form ? k_rel_resid_df<1, false, true> : k_rel_resid_df<0, false, true>, rgrid,
+                 sh64.block, 0, s2, g32, sh64.zc, dfa, ctx->partials, ctx->st);
     } else if (sp.form == 0) {
       if (pc) SBM_REL(0, true); else SBM_REL(0, false);
     } else {
@@ -1185,7 +1207,8 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
     }
 #undef SBM_AD
 #define SBM_UP(P, V)                                                                         \
-  k32_update<P, V><<<fgrid, 256, 0, s2>>>(g32, g, nchunk, x32, out, r32, q32, iv32, ctx->d64, \
+  k32_update<P, V><<<fgrid, 256, 0, s2>>>(g32, nchunk, x32, out, r32, q32, iv32,               \
+                                          ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,             \
                                           ctx->partials, ctx->st)
     if (vec == 4) {
       if (pc) SBM_UP(true, 4); else SBM_UP(false, 4);
@@ -1232,8 +1255,9 @@ int mixed_end(sbm_ctx* ctx, const SolveSpec& sp, const CgState& fin, SolveResult
   cudaStream_t s = ctx->stream;
   const Shape sh64 = stencil_shape(g, pick_zc(g, ctx->zc64));
   float* const x32 = ctx->x32 + kOff32;
-  // x += d64 + x32 (interior): the ghosts of x keep their Dirichlet / flux data.
-  k_finish<<<sh64.grid, sh64.block, 0, s>>>(g, g32, sh64.zc, sp.x, ctx->d64, x32);
+  // x += d + x32 (interior): the ghosts of x keep their Dirichlet / flux data.
+  k_finish<<<sh64.grid, sh64.block, 0, s>>>(g, g32, sh64.zc, sp.x, ctx->dhi32 + kOff32,
+                                            ctx->dlo32 + kOff32, x32);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaGetLastError());
   SBM_CUDA_TRY(cudaEventRecord(ctx->ev1, s));
@@ -1372,8 +1396,8 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
     if (rc) return rc;
     if (flex) {
       fx.x32 = x32;
-      fx.d64 = ctx->d64;
-      fx.g64 = g;
+      fx.dhi = ctx->dhi32 + kOff32;
+      fx.dlo = ctx->dlo32 + kOff32;
       fx.rc = net_pc_rc(ctx);
       fx.rq = net_pc_rq(ctx);
       fx.scal = net_pc_scal(ctx);
@@ -1409,10 +1433,10 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
       net_pc_launch_part(ctx, which - 5, r32, q32, ctx->partials, ctx->st32, s);
     } else if (which == 1) {
       if (vec == 4) {
-        if (pc) k32_update<true, 4><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);
-        else k32_update<false, 4><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);
+        if (pc) k32_update<true, 4><<<fgrid, 256, 0, s>>>(g32, nchunk, x32, pb, r32, q32, iv, ctx->dhi32 + kOff32, ctx->dlo32 + kOff32, ctx->partials, ctx->st32);
+        else k32_update<false, 4><<<fgrid, 256, 0, s>>>(g32, nchunk, x32, pb, r32, q32, iv, ctx->dhi32 + kOff32, ctx->dlo32 + kOff32, ctx->partials, ctx->st32);
       } else {
-        k32_update<false, 1><<<fgrid, 256, 0, s>>>(g32, g, nchunk, x32, pb, r32, q32, iv, ctx->d64, ctx->partials, ctx->st32);
+        k32_update<false, 1><<<fgrid, 256, 0, s>>>(g32, nchunk, x32, pb, r32, q32, iv, ctx->dhi32 + kOff32, ctx->dlo32 + kOff32, ctx->partials, ctx->st32);
       }
     } else {
       OpArgs<double> op{g, ctx->hk_gen, nullptr, 1.0, 0, SBM_BC_ZERO, SBM_BC_ZERO};

@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(NTH)
   const Geo g = op.g;
   const float beta = (float)st->beta;
   // FLEX: the previous iteration's x32 += alpha p_old, applied here; after a
-  // residual replacement x32 is first folded into d64 (x32 = alpha p_old)
+  // residual replacement x32 is first folded into the double-float
+  // correction (x32 = alpha p_old)
   const float alpha_x = FLEX ? (float)st->alpha : 0.f;
   const bool fold = FLEX && st->accum_pending != 0;
   const bool xupd = FLEX && (fold || alpha_x != 0.f);
@@ -317,11 +318,12 @@ __global__ void __launch_bounds__(NTH)
         rq_acc += (qa[0] + qa[1]) + (qa[2] + qa[3]);
         if (xupd) {
           if (fold) {
-            const int64_t c64 = fx.g64.ix(i0, j, k);
-            fx.d64[c64] += (double)xv.x;
-            fx.d64[c64 + 1] += (double)xv.y;
-            fx.d64[c64 + 2] += (double)xv.z;
-            fx.d64[c64 + 3] += (double)xv.w;
+            const float4 dh = *reinterpret_cast<const float4*>(fx.dhi + c);
+            const float4 dl = *reinterpret_cast<const float4*>(fx.dlo + c);
+            const DF d0 = df_add_f(DF{dh.x, dl.x}, xv.x), d1 = df_add_f(DF{dh.y, dl.y}, xv.y);
+            const DF d2 = df_add_f(DF{dh.z, dl.z}, xv.z), d3 = df_add_f(DF{dh.w, dl.w}, xv.w);
+            *reinterpret_cast<float4*>(fx.dhi + c) = make_float4(d0.hi, d1.hi, d2.hi, d3.hi);
+            *reinterpret_cast<float4*>(fx.dlo + c) = make_float4(d0.lo, d1.lo, d2.lo, d3.lo);
             xv = make_float4(alpha_x * pold.x, alpha_x * pold.y, alpha_x * pold.z,
                              alpha_x * pold.w);
           } else {
