@@ -52,9 +52,10 @@ SEED = 1
 TOL = 1e-8
 METRIC = "sbm_potential_solve_time_256^3_relres_1e-8"
 # dram__bytes_read.sum + dram__bytes_write.sum of one k32t_apply_dir launch
-# at 256^3 (ncu): with the Jacobi read (Jacobi-PCG); the flexible-CG variant
-# (learned preconditioner) is not captured yet.
-APPLY_TRAFFIC = {1: 398.2e6}
+# at 256^3 (ncu): with the Jacobi read (Jacobi-PCG) and the flexible-CG
+# variant of the learned preconditioner (7 words: z, p_old, hk, x read;
+# p_new, q, x written).
+APPLY_TRAFFIC = {1: 398.2e6, 2: 460.5e6}
 # dram__bytes_read.sum + dram__bytes_write.sum of the 9 k_conv3_tc launches
 # of one preconditioner application at 256^3 (ncu)
 CONV_TRAFFIC = 41.56e6
@@ -542,7 +543,7 @@ def run_ours(args):
                       "z.q_old, r.r)", "ms": ms_m,
             "GB/s": bytes_m / (ms_m * 1e-3) / 1e9, "frac": bytes_m / (ms_m * 1e-3) / 1e9 / peak,
             "bound": "hbm"}
-        # the dominant kernel of the solve (32 % of its time over 9 launches
+        # the dominant kernel of the solve (36 % of its time over 9 launches
         # per iteration): the U-Net convolutions on the tensor cores
         ach = fl / (ms_cv * 1e-3) / 1e12
         roofline = {"bound": "tensor", "kernel": "k_conv3_tc (the 9 U-Net convolutions of one "
