@@ -773,31 +773,27 @@ __global__ void k_pc_restrict(Geo g, Dims c, Dims cv, const float* __restrict__ 
       const double s = sqrt(tot[0] / (double)cv.v());
       scal[0] = (float)s;
       scal[1] = s > 0.0 ? (float)(1.0 / s) : 0.f;
-      st->aux[1] = 1.0;  // rc holds R r of the current residual
+      st->aux[1] = 1.0;     // rc holds R r of the current residual
+      st->aux[2] = tot[0];  // |rc - alpha rq|^2: |rc|^2 once the pack has applied alpha
     }
   }
 }
 
 // rc -= alpha rq (R r of the updated residual, alpha the step the
-// preconditioner kernel that follows applies to r), the U-Net's residual
-// channel rc / s, and |rc|^2 (aux[2]) for the next scale.
+// preconditioner kernel that follows applies to r) and the U-Net's residual
+// channel rc / s.  |rc|^2 of the updated rc is already in aux[2] (set with
+// s by the direction kernel or the restriction).
 __global__ void k_pc_pack(int64_t V, float* __restrict__ rc, const float* __restrict__ rq,
-                          const float* scal, bf16* __restrict__ in0, double* partials,
-                          CgState* st) {
+                          const float* scal, bf16* __restrict__ in0, const CgState* st) {
   pdl_begin();
   if (st->done || st->pc_off) return;
   const float inv = scal[1];
   const float alpha = (float)st->alpha;
-  double acc = 0.0;
   NET_LOOP(V) {
     const float m = rc[t] - alpha * rq[t];
     rc[t] = m;
-    acc += (double)m * (double)m;
     in0[act_index(t, 0, V)] = __float2bfloat16_rn(m * inv);
   }
-  double v[1] = {acc}, tot[1];
-  if (grid_reduce<1>(v, partials, &st->counter[1], tot))
-    if (threadIdx.x == 0) st->aux[2] = tot[0];
 }
 
 // Last block of the flexible CG's preconditioner kernel, which also applies
@@ -1260,14 +1256,13 @@ void net_pc_launch(sbm_ctx* ctx, float* r32, const float* iv32, const float* q32
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   const Geo& g = ctx->g32;
   const netd::Dims& c = pc->c;
-  // coarse-grid kernels with a grid reduction: two blocks per SM at most,
-  // so the last block sums few partials
+  // the restriction (a grid reduction): two blocks per SM at most, so the
+  // last block sums few partials
   const int rgrid = std::min(netd::grid_for(pc->cv.v()), 2 * 152);
-  const int pgrid = std::min(netd::grid_for(c.v()), 2 * 152);
   launch_pdl(netd::k_pc_restrict, dim3(rgrid), dim3(256), 0, s, g, c, pc->cv, (const float*)r32,
              pc->rc, (const float*)pc->rq, partials, (float*)pc->scal, st);
-  launch_pdl(netd::k_pc_pack, dim3(pgrid), dim3(256), 0, s, c.v(), pc->rc, (const float*)pc->rq,
-             (const float*)pc->scal, pc->w->in0, partials, st);
+  launch_pdl(netd::k_pc_pack, dim3(netd::grid_for(c.v())), dim3(256), 0, s, c.v(), pc->rc,
+             (const float*)pc->rq, (const float*)pc->scal, pc->w->in0, (const CgState*)st);
   SBM_LAUNCHED(2);
   netd::forward(pc->net, *pc->w, false, &st->done, &st->pc_off, s);
   const int64_t items = (int64_t)(g.ny / 4) * g.nx * (g.nz / 4);

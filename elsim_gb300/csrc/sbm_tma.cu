@@ -373,10 +373,11 @@ __global__ void __launch_bounds__(NTH)
         st->alpha = alpha;
         st->accum_pending = 0;
         // s = RMS(R r - alpha R q) over the valid coarse cells, |R r|^2 in
-        // aux[2]: the scale of the next U-Net input
-        const double ss = (st->aux[2] - 2.0 * alpha * tot[1] + alpha * alpha * tot[2]) /
-                          (double)fx.ncell;
-        const double sc = ss > 0.0 ? sqrt(ss) : 0.0;
+        // aux[2]: the scale of the next U-Net input; |R r - alpha R q|^2
+        // becomes the next |R r|^2
+        const double ss2 = st->aux[2] - 2.0 * alpha * tot[1] + alpha * alpha * tot[2];
+        const double sc = ss2 > 0.0 ? sqrt(ss2 / (double)fx.ncell) : 0.0;
+        st->aux[2] = ss2 > 0.0 ? ss2 : 0.0;  // |R r|^2 after the pack applies alpha R q
         fx.scal[0] = (float)sc;
         fx.scal[1] = sc > 0.0 ? (float)(1.0 / sc) : 0.f;
         if (st->done == 0) {
