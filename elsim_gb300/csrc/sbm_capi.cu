@@ -166,7 +166,7 @@ int sbm_ctx_create(int ny, int nx, int nz, const sbm_params* p, sbm_ctx** out) {
     return fail(SBM_ERR_CUDA);
   for (int f = 0; f < SBM_F_COUNT; ++f)
     if ((rc = dalloc(&ctx->f[f], ctx->g.nh))) return fail(rc);
-  double** cg[] = {&ctx->hk_gen, &ctx->r64, &ctx->p64, &ctx->q64, &ctx->d64, &ctx->r0};
+  double** cg[] = {&ctx->hk_gen, &ctx->r64, &ctx->p64, &ctx->q64, &ctx->d64};
   for (double** b : cg)
     if ((rc = dalloc(b, ctx->g.nh))) return fail(rc);
   ctx->rhs = ctx->f[SBM_F_RHS];
@@ -198,7 +198,7 @@ int sbm_ctx_destroy(sbm_ctx* ctx) {
   double* d[] = {ctx->hk_kap, ctx->hk_pce, ctx->hk_pcc, ctx->hk_gen, ctx->dab, ctx->dab1,
                  ctx->mu,     ctx->mb,     ctx->pmn,    ctx->rhe,    ctx->rxc, ctx->kfw,
                  ctx->kbw,    ctx->ppo,    ctx->peo,    ctx->tmp,    ctx->r64, ctx->p64,
-                 ctx->q64,    ctx->d64,    ctx->r0,     ctx->partials, ctx->d_scal,
+                 ctx->q64,    ctx->d64,    ctx->partials, ctx->d_scal,
                  ctx->fc64};
   for (double* q : d) cudaFree(q);
   float* fl[] = {ctx->hk32,   ctx->dg32,   ctx->r32,    ctx->p32,   ctx->q32,

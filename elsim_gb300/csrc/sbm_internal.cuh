@@ -396,8 +396,8 @@ struct sbm_ctx {
   double *dab = nullptr, *dab1 = nullptr, *mu = nullptr, *mb = nullptr, *pmn = nullptr;
   double *rhs = nullptr, *rhe = nullptr, *rxc = nullptr, *kfw = nullptr, *kbw = nullptr;
   double *ppo = nullptr, *peo = nullptr, *tmp = nullptr;
-  // FP64 CG work: residual, direction, A*direction, IR correction, IR r0
-  double *r64 = nullptr, *p64 = nullptr, *q64 = nullptr, *d64 = nullptr, *r0 = nullptr;
+  // FP64 CG work: residual, direction, A*direction, Jacobi weight
+  double *r64 = nullptr, *p64 = nullptr, *q64 = nullptr, *d64 = nullptr;
   // stored y / x / z face coefficients of the current FP64 operator (3 nh)
   double* fc64 = nullptr;
   // FP32 work: half coefficient, diagonal, residual, direction, A*direction, correction, z

@@ -979,6 +979,109 @@ __global__ void __launch_bounds__(BX* BY)
   }
 }
 
+// Initial residual of the mixed solve in double-float arithmetic:
+// r0 = b - A x0 with x0's stored ghosts (Dirichlet / flux data: no ghost
+// rules), from the hi + lo splits of x0 (xhi, xlo) and b (bhi, blo) in the
+// FP32 layout; r0 is kept as the pair r0hi + r0lo for the replacements, and
+// the last block sets rr0 = r0.r0 and the state of a new solve (as
+// k_residual_mem does in FP64).  The operands of k_rel_resid_df, with
+// hkhi / hklo / dghi / dglo / scale / r0hi / r0lo of `a` used; same tiling.
+template <int FORM>
+__global__ void __launch_bounds__(BX* BY)
+    k_residual_df(Geo g, int zc, DfResArgs a, const float* __restrict__ xhi,
+                  const float* __restrict__ xlo, const float* __restrict__ bhi,
+                  const float* __restrict__ blo, float* __restrict__ r0hi,
+                  float* __restrict__ r0lo, double* partials, CgState* st) {
+  const int nty = (g.ny + BX - 1) / BX, ntx = (g.nx + BY - 1) / BY;
+  const int ntiles = nty * ntx * ((g.nz + zc - 1) / zc);
+  double a_rr = 0.0;
+  __shared__ float svh[BY + 2][BX + 2], svl[BY + 2][BX + 2];
+  const DF scale{a.scale_hi, a.scale_lo};
+  const int tx = threadIdx.x, ty = threadIdx.y, tf = ty * BX + tx;
+  int hrow = -1, hcol = -1;
+  if (tf < 2 * BX) {  // rows 0 and BY + 1 (x halo)
+    hcol = tf % BX + 1;
+    hrow = tf < BX ? 0 : BY + 1;
+  } else if (tf < 2 * BX + 2 * BY) {  // columns 0 and BX + 1 (y halo)
+    const int u = tf - 2 * BX;
+    hrow = u % BY + 1;
+    hcol = u < BY ? 0 : BX + 1;
+  }
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int ib = (t % nty) * BX, jb = ((t / nty) % ntx) * BY;
+    const int i = ib + tx + 1, j = jb + ty + 1;
+    const int k0 = (t / (nty * ntx)) * zc + 1;
+    const int k1 = min(k0 + zc - 1, g.nz);
+    const bool active = (i <= g.ny) && (j <= g.nx);
+    // a thread of a partial tile whose cell is in the ghost layer supplies
+    // that ghost value to its neighbours through the plane tile
+    const bool ghost = !active && (i <= g.ny + 1) && (j <= g.nx + 1);
+    const int hi = ib + hcol, hj = jb + hrow;
+    // halo cells up to and including the ghost layer: x0's ghosts are data
+    const bool hact = hrow >= 0 && hi <= g.ny + 1 && hj <= g.nx + 1;
+    auto xv = [&](int ii, int jj, int kk) {
+      const int64_t c = g.ix(ii, jj, kk);
+      return DF{xhi[c], xlo[c]};
+    };
+    auto hk = [&](int64_t c) { return DF{a.hkhi[c], a.hklo[c]}; };
+    DF vc{0.f, 0.f}, vm{0.f, 0.f};
+    if (active) {
+      vc = xv(i, j, k0);
+      vm = xv(i, j, k0 - 1);
+    }
+    float t_rr = 0.f;
+    for (int k = k0; k <= k1; ++k) {
+      DF vp{0.f, 0.f}, hv{0.f, 0.f};
+      if (active) vp = xv(i, j, k + 1);
+      else if (ghost) vc = xv(i, j, k);
+      if (hact) hv = xv(hi, hj, k);
+      __syncthreads();  // the previous plane's readers are done
+      svh[ty + 1][tx + 1] = vc.hi;
+      svl[ty + 1][tx + 1] = vc.lo;
+      if (hrow >= 0) {
+        svh[hrow][hcol] = hv.hi;
+        svl[hrow][hcol] = hv.lo;
+      }
+      __syncthreads();
+      if (active) {
+        const int64_t c = g.ix(i, j, k);
+        const DF vym{svh[ty + 1][tx], svl[ty + 1][tx]};
+        const DF vyp{svh[ty + 1][tx + 2], svl[ty + 1][tx + 2]};
+        const DF vxm{svh[ty][tx + 1], svl[ty][tx + 1]};
+        const DF vxp{svh[ty + 2][tx + 1], svl[ty + 2][tx + 1]};
+        const DF kc = hk(c);
+        DF sum = df_mul(df_add(hk(c + 1), kc), df_sub(vyp, vc));
+        sum = df_add(sum, df_mul(df_add(hk(c - 1), kc), df_sub(vym, vc)));
+        sum = df_add(sum, df_mul(df_add(hk(c + g.sx), kc), df_sub(vxp, vc)));
+        sum = df_add(sum, df_mul(df_add(hk(c - g.sx), kc), df_sub(vxm, vc)));
+        sum = df_add(sum, df_mul(df_add(hk(c + g.sz), kc), df_sub(vp, vc)));
+        sum = df_add(sum, df_mul(df_add(hk(c - g.sz), kc), df_sub(vm, vc)));
+        DF av = df_mul(scale, sum);
+        if (FORM == 1) av = df_sub(df_mul(DF{a.dghi[c], a.dglo[c]}, vc), av);
+        const DF rv = df_sub(DF{bhi[c], blo[c]}, av);
+        r0hi[c] = rv.hi;
+        r0lo[c] = rv.lo;
+        t_rr += rv.hi * rv.hi;
+      }
+      vm = vc;
+      vc = vp;
+    }
+    __syncthreads();  // the next tile reuses the plane tile
+    a_rr += (double)t_rr;
+  }
+  double v[1] = {a_rr}, tot[1];
+  if (grid_reduce<1>(v, partials, &st->counter[2], tot)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      st->rr = tot[0];
+      st->rr0 = tot[0];
+      st->rho = tot[0];
+      st->iter = 0;
+      st->rms = 1.0;
+      st->done = (st->stop_rule == SBM_STOP_REL_RES && tot[0] == 0.0) ? 1 : 0;
+    }
+  }
+}
+
 // x += dhi + dlo + x32 on the interior (the total correction of the mixed
 // solve; the FP32 parts summed in FP64).
 __global__ void k_finish(Geo g, Geo g32, int zc, double* __restrict__ x,
@@ -1059,9 +1162,6 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   float* const q32 = ctx->q32 + kOff32;
   float* const x32 = ctx->x32 + kOff32;
   float* const iv32 = ctx->z32 + kOff32;
-  OpArgs<double> op64{g, sp.hk64, sp.diag64, sp.scale, sp.form, sp.bcx0, sp.bcx1};
-  if ((rc = compute_faces(ctx, sp.hk64, s))) return rc;
-  op64.fc = ctx->fc64;
   OpArgs<float> op32{g32, hk32, sp.form ? dg32 : nullptr, (float)sp.scale, sp.form, sp.bcx0,
                      sp.bcx1};
   // learned preconditioner when usable, else Jacobi (the documented fallback)
@@ -1087,8 +1187,6 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   h->initial = 1;
   SBM_CUDA_TRY(cudaEventRecord(ctx->ev0, s));
   SBM_CUDA_TRY(cudaMemcpyAsync(ctx->st, h, sizeof(CgState), cudaMemcpyHostToDevice, s));
-  SBM_CUDA_TRY(cudaMemsetAsync(ctx->dhi32, 0, sizeof(float) * g32.nh, s));
-  SBM_CUDA_TRY(cudaMemsetAsync(ctx->dlo32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->x32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->p32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->rold32, 0, sizeof(float) * g32.nh, s));
@@ -1117,25 +1215,9 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   // with the learned preconditioner the direction kernels read z from its buffer
   float* const zl = learned ? net_pc_zbuf(ctx) : nullptr;
   const float* const rdir = learned ? zl : r32;
-  // r0 = b - A x0 with x0's stored ghosts (FP64); sets rr0; split into the
-  // double-float pair the replacements start from
-  if (sp.form == 0)
-    k_residual_mem<0, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x,
-                                                              ctx->r0, ctx->p64, nullptr,
-                                                              ctx->partials, ctx->st);
-  else
-    k_residual_mem<1, false><<<sh64.grid, sh64.block, 0, s>>>(op64, sh64.zc, sp.rhs, sp.x,
-                                                              ctx->r0, ctx->p64, nullptr,
-                                                              ctx->partials, ctx->st);
-  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, ctx->r0, ctx->r0hi32 + kOff32, nullptr, nullptr,
-                                         ctx->r0lo32 + kOff32, nullptr);
-  SBM_LAUNCHED(2);
-  const int64_t items = (int64_t)nchunk * g.nx * g.nz;
-  const dim3 fgrid(flat_blocks(items));
-  const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
-  float* const pbuf[2] = {p32, ctx->rold32 + kOff32};  // alternating direction buffers
-  // the replacement kernel walks its tiles grid-stride with four blocks per
-  // SM (four fit at its 56 registers), so its usual no-op launch is cheap
+  // the double-float residual kernels walk their tiles grid-stride with four
+  // blocks per SM (four fit at their 64 registers), so the usual no-op
+  // launch of the replacement is cheap
   const int64_t rel_tiles = (int64_t)sh64.grid.x * sh64.grid.y * sh64.grid.z;
   const dim3 rgrid((unsigned)std::min<int64_t>(rel_tiles, 152 * 4));
   DfResArgs dfa{};
@@ -1153,6 +1235,28 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   df_split(sp.scale, &dfa.scale_hi, &dfa.scale_lo);
   dfa.bcx0 = sp.bcx0;
   dfa.bcx1 = sp.bcx1;
+  // r0 = b - A x0 with x0's stored ghosts, in double-float from the hi + lo
+  // splits of x0 and b (held meanwhile in q32 / r32 and in the correction's
+  // arrays, which are cleared after it); sets rr0
+  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.x, q32, sp.rhs, ctx->dhi32 + kOff32, r32,
+                                         ctx->dlo32 + kOff32);
+  if (sp.form == 0)
+    k_residual_df<0><<<rgrid, sh64.block, 0, s>>>(g32, sh64.zc, dfa, q32, r32,
+                                                   ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,
+                                                   ctx->r0hi32 + kOff32, ctx->r0lo32 + kOff32,
+                                                   ctx->partials, ctx->st);
+  else
+    k_residual_df<1><<<rgrid, sh64.block, 0, s>>>(g32, sh64.zc, dfa, q32, r32,
+                                                   ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,
+                                                   ctx->r0hi32 + kOff32, ctx->r0lo32 + kOff32,
+                                                   ctx->partials, ctx->st);
+  SBM_LAUNCHED(2);
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->dhi32, 0, sizeof(float) * g32.nh, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->dlo32, 0, sizeof(float) * g32.nh, s));
+  const int64_t items = (int64_t)nchunk * g.nx * g.nz;
+  const dim3 fgrid(flat_blocks(items));
+  const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
+  float* const pbuf[2] = {p32, ctx->rold32 + kOff32};  // alternating direction buffers
   auto rel = [&](cudaStream_t s2) {
 #define SBM_REL(F, P) \
   k_rel_resid_df<F, P><<<rgrid, sh64.block, 0, s2>>>(g32, sh64.zc, dfa, ctx->partials, ctx->st)
