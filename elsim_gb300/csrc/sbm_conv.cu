@@ -229,6 +229,106 @@ __device__ __forceinline__ void issue_taps(uint32_t tmem, uint64_t ad, uint64_t 
   }
 }
 
+// Epilogue of one output tile: thread m (0..127) of the four warps that
+// read TMEM lanes 32 (m / 32) .. + 31 owns voxel row m (y = y0 + m % 8,
+// x = x0 + m / 8) of every plane; accumulator columns of plane pl start at
+// tacc + pl nt.  Bias, ReLU, BF16 / FP32 stores, the fused 2x2x2 pooling
+// (y and x pairs by warp shuffle), nearest upsampling into the finer
+// concat buffer and the fused 1x1 output layer.  Warp shuffles only: no
+// block barrier, so a subset of warps can run it.
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tacc, int m, int y0,
+                                              int x0, int z0, int zl, int n0, int nt, int P) {
+  const int tid = m;
+  const int warp = m >> 5;
+  const uint32_t tmem = tacc;
+  const unsigned FULL = 0xffffffffu;
+  const int64_t V = (int64_t)a.ny * a.nx * a.nz;
+  const int y = y0 + (tid & 7), x = x0 + (tid >> 3);
+  const bool valid = y < a.ny && x < a.nx;
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  float head[4] = {0.f, 0.f, 0.f, 0.f};  // fused 1x1 output layer, per plane
+  for (int c0 = 0; c0 < nt; c0 += 16) {
+    __align__(16) __nv_bfloat16 o[4][16];
+    for (int pl = 0; pl < P; ++pl) {
+      float acc[16];
+      tc_ld16(lane_base + (uint32_t)(pl * nt + c0), acc);
+      const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + pl));
+      // voxels in the zero padding of a padded grid keep zero outputs, as
+      // the zero fill beyond a grid face would present them
+      const bool live =
+          a.vny == 0 || (y < a.vny && x < a.vnx && (zl + pl) < a.vnz);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        float val = acc[q] + (a.bias ? a.bias[n0 + c0 + q] : 0.f);
+        if (a.relu) val = fmaxf(val, 0.f);
+        if (!live) val = 0.f;
+        o[pl][q] = __float2bfloat16_rn(val);
+        acc[q] = val;
+        if (a.w1x1) head[pl] += a.w1x1[n0 + c0 + q] * __bfloat162float(o[pl][q]);
+      }
+      if (!valid) continue;
+      const int ch = a.offy + n0 + c0;
+      if (a.y16) {
+        *reinterpret_cast<uint4*>(a.y16 + act_index(v, ch, V)) =
+            *reinterpret_cast<const uint4*>(&o[pl][0]);
+        *reinterpret_cast<uint4*>(a.y16 + act_index(v, ch + 8, V)) =
+            *reinterpret_cast<const uint4*>(&o[pl][8]);
+      }
+      if (a.y32) {
+        float4* d0 = reinterpret_cast<float4*>(a.y32 + act_index(v, ch, V));
+        float4* d1 = reinterpret_cast<float4*>(a.y32 + act_index(v, ch + 8, V));
+        d0[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+        d0[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+        d1[0] = make_float4(acc[8], acc[9], acc[10], acc[11]);
+        d1[1] = make_float4(acc[12], acc[13], acc[14], acc[15]);
+      }
+      if (a.up) {
+        // nearest upsampling: the 8 children in the finer grid
+        const int fy = 2 * a.ny, fx = 2 * a.nx;
+        for (int ch = 0; ch < 8; ++ch) {
+          const int cy = 2 * y + (ch & 1), cxx = 2 * x + ((ch >> 1) & 1);
+          const int czl = 2 * (zl + pl) + (ch >> 2);
+          const int64_t u = (int64_t)cy +
+                            (int64_t)fy * (cxx + (int64_t)fx * (2 * (z0 + pl) + (ch >> 2)));
+          const int cu = a.offu + n0 + c0;
+          const bool ulive = a.uvny == 0 || (cy < a.uvny && cxx < a.uvnx && czl < a.uvnz);
+          const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
+          *reinterpret_cast<uint4*>(a.up + act_index(u, cu, 8 * V)) =
+              ulive ? *reinterpret_cast<const uint4*>(&o[pl][0]) : zero4;
+          *reinterpret_cast<uint4*>(a.up + act_index(u, cu + 8, 8 * V)) =
+              ulive ? *reinterpret_cast<const uint4*>(&o[pl][8]) : zero4;
+        }
+      }
+    }
+    // 2x2x2 average: plane pairs in registers, y pairs lane^1, x pairs lane^8
+    for (int pp = 0; a.pool && pp < P; pp += 2) {
+      __align__(16) __nv_bfloat16 pv[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        float sum = __bfloat162float(o[pp][q]) + __bfloat162float(o[pp + 1][q]);
+        sum += __shfl_xor_sync(FULL, sum, 1);
+        sum += __shfl_xor_sync(FULL, sum, 8);
+        pv[q] = __float2bfloat16_rn(sum * 0.125f);
+      }
+      if (valid && (tid & 1) == 0 && ((tid >> 3) & 1) == 0) {
+        const int cy = a.ny / 2, cx = a.nx / 2;
+        const int64_t vc =
+            (int64_t)(y / 2) + (int64_t)cy * ((x / 2) + (int64_t)cx * ((z0 + pp) / 2));
+        *reinterpret_cast<uint4*>(a.pool + act_index(vc, n0 + c0, V / 8)) =
+            *reinterpret_cast<const uint4*>(&pv[0]);
+        *reinterpret_cast<uint4*>(a.pool + act_index(vc, n0 + c0 + 8, V / 8)) =
+            *reinterpret_cast<const uint4*>(&pv[8]);
+      }
+    }
+  }
+  if (a.w1x1 && valid) {
+    for (int pl = 0; pl < P; ++pl) {
+      const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + pl));
+      a.out1x1[v] = head[pl] + a.b1x1[0];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvMap m, ConvArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
   const int P = a.planes;  // z planes per CTA (1, 2 or 4), one accumulator each
@@ -350,92 +450,7 @@ __global__ void __launch_bounds__(NTHR) k_conv3_tc(const __grid_constant__ ConvM
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
-    const unsigned FULL = 0xffffffffu;
-    const int64_t V = (int64_t)a.ny * a.nx * a.nz;
-    const int y = y0 + (tid & 7), x = x0 + (tid >> 3);
-    const bool valid = y < a.ny && x < a.nx;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    float head[4] = {0.f, 0.f, 0.f, 0.f};  // fused 1x1 output layer, per plane
-    for (int c0 = 0; c0 < nt; c0 += 16) {
-      __align__(16) __nv_bfloat16 o[4][16];
-      for (int pl = 0; pl < P; ++pl) {
-        float acc[16];
-        tc_ld16(lane_base + (uint32_t)(pl * nt + c0), acc);
-        const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + pl));
-        // voxels in the zero padding of a padded grid keep zero outputs, as
-        // the zero fill beyond a grid face would present them
-        const bool live =
-            a.vny == 0 || (y < a.vny && x < a.vnx && (zl + pl) < a.vnz);
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          float val = acc[q] + (a.bias ? a.bias[n0 + c0 + q] : 0.f);
-          if (a.relu) val = fmaxf(val, 0.f);
-          if (!live) val = 0.f;
-          o[pl][q] = __float2bfloat16_rn(val);
-          acc[q] = val;
-          if (a.w1x1) head[pl] += a.w1x1[n0 + c0 + q] * __bfloat162float(o[pl][q]);
-        }
-        if (!valid) continue;
-        const int ch = a.offy + n0 + c0;
-        if (a.y16) {
-          *reinterpret_cast<uint4*>(a.y16 + act_index(v, ch, V)) =
-              *reinterpret_cast<const uint4*>(&o[pl][0]);
-          *reinterpret_cast<uint4*>(a.y16 + act_index(v, ch + 8, V)) =
-              *reinterpret_cast<const uint4*>(&o[pl][8]);
-        }
-        if (a.y32) {
-          float4* d0 = reinterpret_cast<float4*>(a.y32 + act_index(v, ch, V));
-          float4* d1 = reinterpret_cast<float4*>(a.y32 + act_index(v, ch + 8, V));
-          d0[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-          d0[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
-          d1[0] = make_float4(acc[8], acc[9], acc[10], acc[11]);
-          d1[1] = make_float4(acc[12], acc[13], acc[14], acc[15]);
-        }
-        if (a.up) {
-          // nearest upsampling: the 8 children in the finer grid
-          const int fy = 2 * a.ny, fx = 2 * a.nx;
-          for (int ch = 0; ch < 8; ++ch) {
-            const int cy = 2 * y + (ch & 1), cxx = 2 * x + ((ch >> 1) & 1);
-            const int czl = 2 * (zl + pl) + (ch >> 2);
-            const int64_t u = (int64_t)cy +
-                              (int64_t)fy * (cxx + (int64_t)fx * (2 * (z0 + pl) + (ch >> 2)));
-            const int cu = a.offu + n0 + c0;
-            const bool ulive = a.uvny == 0 || (cy < a.uvny && cxx < a.uvnx && czl < a.uvnz);
-            const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
-            *reinterpret_cast<uint4*>(a.up + act_index(u, cu, 8 * V)) =
-                ulive ? *reinterpret_cast<const uint4*>(&o[pl][0]) : zero4;
-            *reinterpret_cast<uint4*>(a.up + act_index(u, cu + 8, 8 * V)) =
-                ulive ? *reinterpret_cast<const uint4*>(&o[pl][8]) : zero4;
-          }
-        }
-      }
-      // 2x2x2 average: plane pairs in registers, y pairs lane^1, x pairs lane^8
-      for (int pp = 0; a.pool && pp < P; pp += 2) {
-        __align__(16) __nv_bfloat16 pv[16];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          float sum = __bfloat162float(o[pp][q]) + __bfloat162float(o[pp + 1][q]);
-          sum += __shfl_xor_sync(FULL, sum, 1);
-          sum += __shfl_xor_sync(FULL, sum, 8);
-          pv[q] = __float2bfloat16_rn(sum * 0.125f);
-        }
-        if (valid && (tid & 1) == 0 && ((tid >> 3) & 1) == 0) {
-          const int cy = a.ny / 2, cx = a.nx / 2;
-          const int64_t vc =
-              (int64_t)(y / 2) + (int64_t)cy * ((x / 2) + (int64_t)cx * ((z0 + pp) / 2));
-          *reinterpret_cast<uint4*>(a.pool + act_index(vc, n0 + c0, V / 8)) =
-              *reinterpret_cast<const uint4*>(&pv[0]);
-          *reinterpret_cast<uint4*>(a.pool + act_index(vc, n0 + c0 + 8, V / 8)) =
-              *reinterpret_cast<const uint4*>(&pv[8]);
-        }
-      }
-    }
-    if (a.w1x1 && valid) {
-      for (int pl = 0; pl < P; ++pl) {
-        const int64_t v = (int64_t)y + (int64_t)a.ny * (x + (int64_t)a.nx * (z0 + pl));
-        a.out1x1[v] = head[pl] + a.b1x1[0];
-      }
-    }
+    conv_epilogue(a, tmem, tid, y0, x0, z0, zl, n0, nt, P);
   } else if (tid == 0) {
     atomicExch(a.err, 1);
   }

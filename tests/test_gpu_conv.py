@@ -57,11 +57,14 @@ def run(shape, cin, cout, relu, flip, use_tc, x16, w16, bias):
 
 
 # z extents: odd -> one plane per CTA, even -> two, multiples of 4 with at
-# most 32 output channels -> four
+# most 32 output channels -> four.  The last three have more voxel tiles
+# than one wave of CTAs holds (one, two and four planes; two, three and
+# four input chunks with one pipeline stage per CTA).
 @pytest.mark.parametrize("shape,cin,cout", [((5, 6, 7), 16, 16), ((8, 8, 8), 32, 48),
                                             ((9, 4, 10), 112, 48), ((16, 16, 3), 48, 64),
                                             ((3, 3, 3), 16, 32), ((7, 9, 12), 48, 16),
-                                            ((8, 16, 8), 16, 32)])
+                                            ((8, 16, 8), 16, 32), ((48, 48, 13), 64, 32),
+                                            ((64, 64, 12), 48, 48), ((64, 64, 24), 32, 16)])
 @pytest.mark.parametrize("relu,flip", [(0, 0), (1, 0), (0, 1)])
 def test_tensor_core_conv_matches_references(built, shape, cin, cout, relu, flip):
     rng = np.random.default_rng(cin * 7 + cout + relu + 3 * flip)
