@@ -1091,22 +1091,23 @@ __global__ void k_finish(Geo g, Geo g32, int zc, double* __restrict__ x,
   if (!active) return;
   for (int k = k0; k <= k1; ++k) {
     const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
-    x[c] = x[c] + (((double)dhi[c3] + (double)dlo[c3]) + (double)x32[c3]);
+    // d + x32 in double-float on the FP32 pipe, then two FP64 additions
+    const DF d = df_add_f(DF{dhi[c3], dlo[c3]}, x32[c3]);
+    x[c] = (x[c] + (double)d.hi) + (double)d.lo;
   }
 }
 
 // a32 = (float) a over the padded domain, FP64 layout -> FP32 layout, with
 // the low part a - a32 in alo when given (and the same for b).
+// One thread per padded element: x over i, grid y / z over j / k (launch
+// with to32_grid).
 __global__ void k_to32(Geo g64, Geo g32, const double* __restrict__ a, float* __restrict__ a32,
                        const double* __restrict__ b, float* __restrict__ b32,
                        float* __restrict__ alo = nullptr, float* __restrict__ blo = nullptr) {
-  const int64_t n = g64.nh;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g64.sx);
-    const int64_t rr = c / g64.sx;
-    const int j = (int)(rr % (g64.nx + 2));
-    const int k = (int)(rr / (g64.nx + 2));
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i > g64.ny + 1) return;
+  {
+    const int64_t c = g64.ix(i, j, k);
     const int64_t c3 = g32.ix(i, j, k);
     float h, l;
     df_split(a[c], &h, &l);
@@ -1118,6 +1119,10 @@ __global__ void k_to32(Geo g64, Geo g32, const double* __restrict__ a, float* __
       if (blo) blo[c3] = l;
     }
   }
+}
+
+dim3 to32_grid(const Geo& g) {
+  return dim3((unsigned)((g.ny + 2 + 127) / 128), (unsigned)(g.nx + 2), (unsigned)(g.nz + 2));
 }
 
 int flat_blocks(int64_t items) {
@@ -1145,6 +1150,7 @@ void tma_launch_fcg(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, floa
 int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cudaGraph_t* graph_out,
                 int* nodes_out) {
   if (sp.stop_rule != SBM_STOP_REL_RES) return SBM_ERR_ARG;
+  if (ctx->g.nx + 2 > 65535 || ctx->g.nz + 2 > 65535) return SBM_ERR_ARG;  // to32_grid
   int rc = ensure_fp32_work(ctx);
   if (rc) return rc;
   const Geo& g = ctx->g;
@@ -1191,7 +1197,7 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->p32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->rold32, 0, sizeof(float) * g32.nh, s));
   // FP32 coefficients and, for the double-float replacement, their low parts
-  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
+  k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
                                          dg32, ctx->hklo32 + kOff32, ctx->dglo32 + kOff32);
   SBM_LAUNCHED(1);
   if (pc || learned) {
@@ -1238,7 +1244,7 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   // r0 = b - A x0 with x0's stored ghosts, in double-float from the hi + lo
   // splits of x0 and b (held meanwhile in q32 / r32 and in the correction's
   // arrays, which are cleared after it); sets rr0
-  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.x, q32, sp.rhs, ctx->dhi32 + kOff32, r32,
+  k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, sp.x, q32, sp.rhs, ctx->dhi32 + kOff32, r32,
                                          ctx->dlo32 + kOff32);
   if (sp.form == 0)
     k_residual_df<0><<<rgrid, sh64.block, 0, s>>>(g32, sh64.zc, dfa, q32, r32,
@@ -1383,6 +1389,7 @@ int mixed_end(sbm_ctx* ctx, const SolveSpec& sp, const CgState& fin, SolveResult
 // against an independent restatement.
 int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double* z) {
   if (!net_pc_usable(ctx, sp.form) || ctx->g.ny % 4) return SBM_ERR_STATE;
+  if (ctx->g.nx + 2 > 65535 || ctx->g.nz + 2 > 65535) return SBM_ERR_ARG;  // to32_grid
   int rc = ensure_fp32_work(ctx);
   if (rc) return rc;
   const Geo& g = ctx->g;
@@ -1396,14 +1403,14 @@ int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double*
   OpArgs<float> op32{g32, hk32, sp.form ? dg32 : nullptr, (float)sp.scale, sp.form, sp.bcx0,
                      sp.bcx1};
   const Shape sh32 = stencil_shape(g32, pick_zc(g32, ctx->zc32));
-  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
+  k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
                                          dg32);
   k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
   SBM_LAUNCHED(2);
   if ((rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, sp.scale, sp.bcx0, sp.bcx1, s)))
     return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(ctx->r64, r, sizeof(double) * g.nh, cudaMemcpyHostToDevice, s));
-  k_to32<<<flat_grid(g.nh), 256, 0, s>>>(g, g32, ctx->r64, r32, nullptr, nullptr);
+  k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, ctx->r64, r32, nullptr, nullptr);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->q32, 0, sizeof(float) * g32.nh, s));
   CgState* h = &ctx->h_st[2];

@@ -313,7 +313,7 @@ def validate(net, vals, cap: int = 2000) -> int:
 
 def train(sizes=((64, 48), (128, 96)), steps=(1500, 12000), batch=(8, 4), lr=(2e-3, 1e-3),
           seed: int = 0, eval_every: int = 500, verbose: bool = True, cne: bool = False,
-          rhs: str = "family"):
+          rhs: str = "family", cne_only: bool = False):
     """Training recipe of the stored weights: for each (n, structures) stage
     build pairs at n^3 (coarse n/4) and run Adam on the GPU (learning rate
     decayed to 0.3x and 0.1x over the last 40 % and 10 % of the stage); k_out
@@ -323,9 +323,12 @@ def train(sizes=((64, 48), (128, 96)), steps=(1500, 12000), batch=(8, 4), lr=(2e
     only a proxy for the preconditioner's quality).  With cne, every stage
     adds as many CnE-form systems (make_pairs form 1, other seeds) to the
     potential ones, the network reads the mass channel, and a CnE-form
-    solve joins the validation score.  Returns (net, info)."""
+    solve joins the validation score; with cne_only the network sees and is
+    scored on CnE-form systems alone.  Returns (net, info)."""
+    cne = cne or cne_only
     net = sbm.Net(seed=seed, mass=cne)
-    vals = validation_set(cne_cases=VALIDATION_CNE if cne else ())
+    vals = validation_set(cases=() if cne_only else VALIDATION,
+                          cne_cases=VALIDATION_CNE if cne else ())
     kout = None
     hist_all, val_hist = [], []
     best, best_p = None, None
@@ -333,7 +336,9 @@ def train(sizes=((64, 48), (128, 96)), steps=(1500, 12000), batch=(8, 4), lr=(2e
     for (n, nseeds), st, b, eta in zip(sizes, steps, batch, lr):
         t0 = time.time()
         seeds = range(seed * 1000 + n, seed * 1000 + n + nseeds)
-        feats, errs, _ = make_pairs(n, seeds, verbose=verbose, rhs=rhs)
+        feats, errs = [], []
+        if not cne_only:
+            feats, errs, _ = make_pairs(n, seeds, verbose=verbose, rhs=rhs)
         if cne:
             f1, e1, _ = make_pairs(n, range(seed * 1000 + 500 + n, seed * 1000 + 500 + n + nseeds),
                                    verbose=verbose, form=1)
@@ -368,7 +373,8 @@ def train(sizes=((64, 48), (128, 96)), steps=(1500, 12000), batch=(8, 4), lr=(2e
     for ctx, *_ in vals:
         ctx.close()
     info = dict(sizes=np.array(sizes), steps=np.array(steps), batch=np.array(batch),
-                lr=np.array(lr), seed=seed, eval_every=eval_every, cne=cne, rhs=rhs,
+                lr=np.array(lr), seed=seed, eval_every=eval_every, cne=cne, cne_only=cne_only,
+                rhs=rhs,
                 validation=np.array(VALIDATION),
                 validation_cne=np.array(VALIDATION_CNE if cne else []),
                 validation_iterations=np.array(val_hist),
@@ -382,6 +388,8 @@ def main(argv=None) -> None:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cne", action="store_true",
                     help="train on CnE-form systems too (the network then reads the mass channel)")
+    ap.add_argument("--cne-only", action="store_true",
+                    help="train and validate on CnE-form systems alone (mass channel)")
     ap.add_argument("--recipe", default="shipped", choices=["shipped", "bv64"],
                     help="shipped: the recipe of the stored weights (64^3 and 128^3 stages, "
                          "right-hand sides of several spectra); bv64: 2,000 pairs from 200 "
@@ -391,7 +399,7 @@ def main(argv=None) -> None:
         net, info = train(sizes=((64, 200),), steps=(13500,), batch=(8,), lr=(1.5e-3,),
                           seed=a.seed, cne=a.cne, rhs="bv")
     else:
-        net, info = train(seed=a.seed, cne=a.cne)
+        net, info = train(seed=a.seed, cne=a.cne, cne_only=a.cne_only)
     save(a.out, net, info)
     print("saved", a.out)
 
