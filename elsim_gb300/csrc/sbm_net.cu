@@ -34,6 +34,7 @@
 #include <tuple>
 #include <vector>
 
+#include "sbm_async.cuh"
 #include "sbm_conv.cuh"
 #include "sbm_net.cuh"
 
@@ -951,15 +952,28 @@ __global__ void __launch_bounds__(256)
 constexpr float kPcOmega = SBM_PC_OMEGA;
 constexpr int kMTY = 64, kMTX = 8, kMTZ = 4;
 constexpr int kWY = kMTY / 4 + 2;  // coarse y window
+// Tensor maps of the multiplicative step: r (64 x 8 x 4 boxes, the tile)
+// and hk (72 x 10 x 6 boxes, the tile with its one-cell halo, x-start
+// rounded down to a 16-byte boundary), over the FP32 layout.
+struct MultMaps {
+  CUtensorMap r, hk;
+};
+constexpr int kMRB = kMTY * kMTX * kMTZ * 4;                    // r box bytes (8192)
+constexpr int kMHB = (kMTY + 8) * (kMTX + 2) * (kMTZ + 2) * 4;  // hk box bytes (17280)
+constexpr int kMBuf = (kMRB + kMHB + 127) / 128 * 128;          // one staging buffer
+constexpr size_t kMultSmem = 2 * (size_t)kMBuf + 2 * sizeof(uint64_t);
+
 __global__ void __launch_bounds__(256, 3)
-    k_pc_mult_tiled(Geo g, Dims c, Dims cv, const float* __restrict__ out, const float* scal,
-                    float* __restrict__ r, const float* __restrict__ q,
-                    const float* __restrict__ hk, const float* __restrict__ dg, float scale,
+    k_pc_mult_tiled(const __grid_constant__ MultMaps maps, Geo g, Dims c, Dims cv,
+                    const float* __restrict__ out, const float* scal, float* __restrict__ r,
+                    const float* __restrict__ q, const float* __restrict__ dg, float scale,
                     int bcx0, int bcx1, float omega, float* __restrict__ z, const int* err,
                     double* partials, CgState* st) {
   __shared__ float sA[3][kMTX / 4 + 2][kWY];
   __shared__ float sB[3][kMTX + 2][kWY];
   __shared__ float sC[kMTZ + 2][kMTX + 2][kWY];
+  extern __shared__ __align__(128) unsigned char dsm[];
+  uint64_t* const bar = reinterpret_cast<uint64_t*>(dsm + 2 * kMBuf);
   pdl_begin();
   if (st->done) return;
   const bool coarse = st->pc_off == 0;  // off: z = D^-1 r (Jacobi-PCG)
@@ -971,16 +985,42 @@ __global__ void __launch_bounds__(256, 3)
   const int64_t ntiles = (int64_t)nty * ntx * (g.nz / kMTZ);
   // per-thread roles of the staging loops: (x, y) column of the windows
   const int col_y = tid % kWY, col_x = tid / kWY;  // col_x < kMTX + 2 for tid < 180
+  // thread 0 stages the r and hk boxes of a tile into buffer b
+  auto stage = [&](int64_t tile, int b) {
+    const int by = (int)(tile % nty);
+    const int bx = (int)((tile / nty) % ntx);
+    const int bz = (int)(tile / ((int64_t)nty * ntx));
+    unsigned char* B = dsm + (size_t)b * kMBuf;
+    mbar_expect_tx(&bar[b], (unsigned)(kMRB + kMHB));
+    tma_load_3d(B, &maps.r, kMTY * by + 1 + kOff32, kMTX * bx + 1, kMTZ * bz + 1, &bar[b]);
+    tma_load_3d(B + kMRB, &maps.hk, kMTY * by, kMTX * bx, kMTZ * bz, &bar[b]);
+  };
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (blockIdx.x < ntiles) stage(blockIdx.x, 0);
+  }
+  int n_issued = blockIdx.x < ntiles ? 1 : 0;  // tiles staged (thread 0's count)
   float a_zr = 0.f, a_zq = 0.f, a_rr = 0.f;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  bool ok = true;
+  int n = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++n) {
     const int by = (int)(tile % nty);
     const int bx = (int)((tile / nty) % ntx);
     const int bz = (int)(tile / ((int64_t)nty * ntx));
     const int y0 = kMTY * by + 1, x0 = kMTX * bx + 1, z0 = kMTZ * bz + 1;
     // coarse index of window entry 0 in y, x, z
     const int cy0 = (kMTY / 4) * by - 1, cx0 = (kMTX / 4) * bx - 1, cz0 = bz - 1;
+    // every thread is done with the previous tile: its buffer takes the next
+    // tile's boxes, and the coarse windows are free
+    __syncthreads();
+    if (tid == 0 && tile + gridDim.x < ntiles) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      stage(tile + gridDim.x, (n + 1) & 1);
+      ++n_issued;
+    }
     if (coarse) {
-      __syncthreads();  // the previous tile's readers are done
       if (col_x < kMTX / 4 + 2) {
         const int cy = min(max(cy0 + col_y, 0), cv.ny - 1);
         const int cx = min(max(cx0 + col_x, 0), cv.nx - 1);
@@ -1010,8 +1050,15 @@ __global__ void __launch_bounds__(256, 3)
               f * (w * sB[lo - cz0][col_x][col_y] + (1.f - w) * sB[hi - cz0][col_x][col_y]);
         }
       }
-      __syncthreads();
     }
+    // the tile's boxes have landed (the wait decision is made uniform)
+    const bool w_ok = mbar_wait_bounded(&bar[n & 1], (unsigned)((n >> 1) & 1), 1u << 20);
+    if (!__syncthreads_and(w_ok)) {
+      ok = false;
+      break;
+    }
+    const float* R = reinterpret_cast<const float*>(dsm + (size_t)(n & 1) * kMBuf);
+    const float* H = reinterpret_cast<const float*>(dsm + (size_t)(n & 1) * kMBuf + kMRB);
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
       const int u = tid + 256 * h;
@@ -1019,20 +1066,23 @@ __global__ void __launch_bounds__(256, 3)
       const int i0 = y0 + 4 * mq, j = x0 + xl, k = z0 + zl;
       if (i0 > g.ny) continue;  // beyond a partial tile (ny is a multiple of 4)
       const int64_t idx = g.ix(i0, j, k);
-      float4 rv = *reinterpret_cast<const float4*>(r + idx);
       const float4 qv = *reinterpret_cast<const float4*>(q + idx);
+      float4 rv = *reinterpret_cast<const float4*>(R + (zl * kMTX + xl) * kMTY + 4 * mq);
       if (rupd) {
         rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
         *reinterpret_cast<float4*>(r + idx) = rv;
       }
       const float ra[4] = {rv.x, rv.y, rv.z, rv.w};
       const float qa[4] = {qv.x, qv.y, qv.z, qv.w};
-      const float4 k4 = *reinterpret_cast<const float4*>(hk + idx);
-      const float4 kx0 = *reinterpret_cast<const float4*>(hk + idx - g.sx);
-      const float4 kx1 = *reinterpret_cast<const float4*>(hk + idx + g.sx);
-      const float4 kz0 = *reinterpret_cast<const float4*>(hk + idx - g.sz);
-      const float4 kz1 = *reinterpret_cast<const float4*>(hk + idx + g.sz);
-      const float ky[6] = {hk[idx - 1], k4.x, k4.y, k4.z, k4.w, hk[idx + 4]};
+      // hk box: (zl + 1, xl + 1, column 4 mq + 4) is the thread's first cell
+      const int ho = ((zl + 1) * (kMTX + 2) + xl + 1) * (kMTY + 8) + 4 * mq + 4;
+      const int hxs = kMTY + 8, hzs = (kMTY + 8) * (kMTX + 2);
+      const float4 k4 = *reinterpret_cast<const float4*>(H + ho);
+      const float4 kx0 = *reinterpret_cast<const float4*>(H + ho - hxs);
+      const float4 kx1 = *reinterpret_cast<const float4*>(H + ho + hxs);
+      const float4 kz0 = *reinterpret_cast<const float4*>(H + ho - hzs);
+      const float4 kz1 = *reinterpret_cast<const float4*>(H + ho + hzs);
+      const float ky[6] = {H[ho - 1], k4.x, k4.y, k4.z, k4.w, H[ho + 4]};
       const float kxa[4] = {kx0.x, kx0.y, kx0.z, kx0.w}, kxb[4] = {kx1.x, kx1.y, kx1.z, kx1.w};
       const float kza[4] = {kz0.x, kz0.y, kz0.z, kz0.w}, kzb[4] = {kz1.x, kz1.y, kz1.z, kz1.w};
       float dga[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1116,6 +1166,18 @@ __global__ void __launch_bounds__(256, 3)
       *reinterpret_cast<float4*>(z + idx) = make_float4(za[0], za[1], za[2], za[3]);
     }
   }
+  if (!ok) {
+    // a staging wait expired: the copies still landing are waited out
+    // (only the last staged tile of each buffer can be) and the solve stops
+    if (tid == 0) {
+      st->done = 5;
+      for (int b = 0; b < 2; ++b) {
+        const int cnt = (n_issued + 1 - b) / 2;  // tiles staged into buffer b
+        if (cnt > 0) mbar_wait_bounded(&bar[b], (unsigned)((cnt - 1) & 1), 1u << 20);
+      }
+    }
+    a_zr = a_zq = a_rr = 0.f;
+  }
   double v[3] = {(double)a_zr, (double)a_zq, (double)a_rr}, tot[3];
   if (grid_reduce<3>(v, partials, &st->counter[5], tot))
     if (threadIdx.x == 0) fcg_close(st, tot[0], tot[1], tot[2], rupd, *err);
@@ -1138,6 +1200,7 @@ struct NetPc {
   // operator of the current solve, for the multiplicative smoothing step
   const float* hk32 = nullptr;
   const float* dg32 = nullptr;  // the CnE form's diagonal (null: potential form)
+  MultMaps mmaps{};             // tensor maps of the multiplicative step (r, hk)
   float scale = 1.f;
   int bcx0 = 0, bcx1 = 0;
   void release() {
@@ -1170,11 +1233,18 @@ bool net_pc_usable(const sbm_ctx* ctx, int form) {
          g.nz % 16 == 0;
 }
 
-int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, double scale, int bcx0,
-                 int bcx1, cudaStream_t s) {
+int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, const float* r32,
+                 double scale, int bcx0, int bcx1, cudaStream_t s) {
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   int rc = conv3_init();
   if (rc) return rc;
+  static bool mult_attr = false;
+  if (!mult_attr) {
+    SBM_CUDA_TRY(cudaFuncSetAttribute(netd::k_pc_mult_tiled,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)netd::kMultSmem));
+    mult_attr = true;
+  }
   const Geo& g = ctx->g32;
   const netd::Dims cv{g.ny / 4, g.nx / 4, g.nz / 4, g.nz / 4};
   auto r16 = [](int n) { return (n + 15) / 16 * 16; };
@@ -1206,6 +1276,10 @@ int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, double scal
   SBM_CUDA_TRY(cudaMemsetAsync(pc->rq, 0, sizeof(float) * c.v(), s));
   pc->hk32 = hk32;
   pc->dg32 = dg32;
+  if (!make_map_box(&pc->mmaps.r, r32 - kOff32, g, netd::kMTY, netd::kMTX, netd::kMTZ) ||
+      !make_map_box(&pc->mmaps.hk, hk32 - kOff32, g, netd::kMTY + 8, netd::kMTX + 2,
+                    netd::kMTZ + 2))
+    return SBM_ERR_STATE;
   pc->scale = (float)scale;
   pc->bcx0 = bcx0;
   pc->bcx1 = bcx1;
@@ -1245,8 +1319,8 @@ static void launch_mult(netd::NetPc* pc, const Geo& g, float* r32, const float* 
   const int64_t tiles = (int64_t)((g.ny + netd::kMTY - 1) / netd::kMTY) * (g.nx / netd::kMTX) *
                         (g.nz / netd::kMTZ);
   const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
-  launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), 0, s, g, pc->c, pc->cv,
-             (const float*)pc->w->out, (const float*)pc->scal, r32, q32, pc->hk32, pc->dg32,
+  launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), netd::kMultSmem, s, pc->mmaps, g, pc->c,
+             pc->cv, (const float*)pc->w->out, (const float*)pc->scal, r32, q32, pc->dg32,
              pc->scale, pc->bcx0, pc->bcx1, netd::kPcOmega, pc->zf + kOff32,
              (const int*)pc->net->err, partials, st);
 }

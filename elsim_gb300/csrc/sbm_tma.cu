@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "sbm_async.cuh"
 #include "sbm_internal.cuh"
 
 namespace sbm {
@@ -68,46 +69,6 @@ __device__ unsigned g_wait_tries = kSpin;
 struct TmaMaps {
   CUtensorMap r, p, hk, iv, dg;
 };
-
-__device__ __forceinline__ uint32_t saddr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)),
-               "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(saddr(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity, unsigned tries) {
-  for (unsigned n = 0; n < tries; ++n)
-    if (mbar_try_wait(b, parity)) return true;
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(saddr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(saddr(bar))
-      : "memory");
-}
 
 __device__ __forceinline__ float4 lds4(const float* p) {
   return *reinterpret_cast<const float4*>(p);
@@ -425,6 +386,20 @@ bool make_map(CUtensorMap* m, const float* base, const Geo& g32) {
 }
 
 }  // namespace
+
+bool make_map_box(CUtensorMap* m, const float* base, const Geo& g32, int bx, int by, int bz) {
+  auto fn = tensor_map_encoder();
+  if (!fn) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)g32.sx, (cuuint64_t)(g32.nx + 2), (cuuint64_t)(g32.nz + 2)};
+  cuuint64_t strides[2] = {(cuuint64_t)g32.sx * 4, (cuuint64_t)g32.sz * 4};
+  cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
+  cuuint32_t es[3] = {1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims,
+                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
 
 // The CUDA driver API's tensor-map encoder (runtime entry-point query, once).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
