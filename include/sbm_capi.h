@@ -68,7 +68,7 @@ extern "C" {
 
 /* Solver variants (no counterpart in the reference). */
 #define SBM_PREC_FP64   0   /* plain FP64 CG: the drop-in                    */
-#define SBM_PREC_MIXED  1   /* FP32 inner CG inside FP64 iterative refinement */
+#define SBM_PREC_MIXED  1   /* FP32 inner CG, double-float residual replacement */
 
 #define SBM_PC_NONE     0
 #define SBM_PC_JACOBI   1
@@ -161,9 +161,10 @@ int sbm_ctx_destroy(sbm_ctx* ctx);
 int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p);
 /* Launch-shape and mixed-precision knobs (0 = built-in choice): z planes
  * per thread of the FP64 / FP32 stencil kernels, CG iterations per captured
- * graph chunk, and `delta` of the mixed solver (its FP64 residual is
- * recomputed whenever the FP32 residual norm has fallen by this factor;
- * default 1e-2, 1e-3 with the learned preconditioner).  flags bit 0
+ * graph chunk, and `delta` of the mixed solver (its true residual is
+ * recomputed in double-float arithmetic whenever the FP32 residual norm has
+ * fallen by this factor; default 1e-2, 1e-4 with the learned
+ * preconditioner).  flags bit 0
  * (SBM_TUNE_NO_TMA): use the register-tiled FP32 stencil instead of the
  * TMA-staged one; bit 1 (SBM_TUNE_PC_ADDITIVE): apply the learned
  * preconditioner in its additive form z = D^-1 r + P e_c instead of the
