@@ -1,8 +1,8 @@
 // sbm_async.cuh -- inline-PTX helpers of the asynchronous copies shared by
 // the TMA-staged kernels (sbm_tma.cu, sbm_net.cu): shared-memory addresses,
-// mbarriers (init, expect_tx, bounded parity waits) and 3-D tensor-map
-// loads (cp.async.bulk.tensor), plus the host-side builder of a 3-D tensor
-// map over an FP32-layout buffer.
+// mbarriers (init, expect_tx, bounded parity waits), 3-D tensor-map loads
+// (cp.async.bulk.tensor) and per-thread 4-byte cp.async copies, plus the
+// host-side builder of a 3-D tensor map over an FP32-layout buffer.
 #pragma once
 
 #include <cuda.h>
@@ -53,6 +53,19 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(saddr(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(saddr(bar))
       : "memory");
+}
+
+// Per-thread asynchronous 4-byte copy global -> shared (cp.async, cached in
+// L1), its group commit and the wait for all of the thread's groups.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(saddr(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // 3-D tensor map over an FP32-layout buffer (base = allocation start,

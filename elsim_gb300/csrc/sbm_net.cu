@@ -848,6 +848,8 @@ __device__ __forceinline__ void interp1(int fi, int n, int* lo, int* hi, float* 
   *wlo = 0.375f - 0.25f * (float)(e & 1) + 0.5f * (float)(e >> 1);  // 3/8, 1/8, 7/8, 5/8
 }
 
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
 // The additive form: r -= alpha q (the pending update of the flexible CG,
 // not on the first residual), then z = invd*r + f * P(out) over the fine
 // interior, f = s k_out / (scale c_ref); z.r, z.q_old and r.r reduced; the
@@ -928,19 +930,21 @@ __global__ void __launch_bounds__(256)
 
 // The multiplicative form z = z1 + omega*invd*(r - A z1), z1 = f P(out), by
 // tiles of 64 (y) x 8 (x) x 4 (z) fine cells, after the pending update
-// r -= alpha q of the flexible CG (not on the first residual).  The block
-// interpolates the coarse window (18 y x 4 x x 3 z cells, clamped) in x and
-// then in z onto the tile's fine x / z positions with their one-cell halo,
-// in shared memory (the order of k_pc_prolong); each thread then takes 4
-// y-consecutive cells (one coarse y cell), interpolates z1 in y for them
-// and their 6 neighbours from three coarse values per row, and applies the
-// FP32 operator with the search-direction ghost rules.  The Jacobi weight
-// invd is formed from the same half coefficients (the operations of
-// k_invdiag), so it is not read.  Global traffic per cell: r, q_old and hk
-// read, r and z written (20 B); the coarse values and the neighbours' hk
-// come from L2.  z.r, z.q_old and r.r are reduced and the last block runs
-// fcg_close.  Tiles are walked grid-stride (every block the same count: the
-// barriers are uniform).
+// r -= alpha q of the flexible CG (not on the first residual).  A tile's r
+// and q boxes and its hk box with the one-cell halo arrive by TMA, and its
+// coarse window (18 y x 4 x x 3 z cells, clamped) by per-thread cp.async,
+// into the other half of a double buffer while the block computes the tile
+// before it.  The block interpolates the window in x and then in z onto the
+// tile's fine x / z positions with their one-cell halo (the order of
+// k_pc_prolong); each thread then takes 4 y-consecutive cells (one coarse y
+// cell), interpolates z1 in y for them and their 6 neighbours from three
+// coarse values per row, and applies the FP32 operator with the
+// search-direction ghost rules.  The Jacobi weight invd is formed from the
+// same half coefficients (the operations of k_invdiag), so it is not read.
+// Global traffic per cell: r, q_old and hk read, r and z written (20 B).
+// z.r, z.q_old and r.r are reduced and the last block runs fcg_close.
+// Tiles are walked grid-stride (every block the same count: the barriers
+// are uniform); two barriers per tile.
 // Weight of the Jacobi step of the multiplicative form.  Flexible-CG
 // iterations on the GPU (256^3 headline / 128^3 and 256^3 held-out / 64^3 /
 // 128^3 structures): omega 1.5: 86/56/82/54/67, 1.9: 72/47/71/51/53,
@@ -952,26 +956,39 @@ __global__ void __launch_bounds__(256)
 constexpr float kPcOmega = SBM_PC_OMEGA;
 constexpr int kMTY = 64, kMTX = 8, kMTZ = 4;
 constexpr int kWY = kMTY / 4 + 2;  // coarse y window
-// Tensor maps of the multiplicative step: r (64 x 8 x 4 boxes, the tile)
-// and hk (72 x 10 x 6 boxes, the tile with its one-cell halo, x-start
+// Tensor maps of the multiplicative step: r and q (64 x 8 x 4 boxes, the
+// tile) and hk (72 x 10 x 6 boxes, the tile with its one-cell halo, x-start
 // rounded down to a 16-byte boundary), over the FP32 layout.
 struct MultMaps {
-  CUtensorMap r, hk;
+  CUtensorMap r, q, hk;
 };
-constexpr int kMRB = kMTY * kMTX * kMTZ * 4;                    // r box bytes (8192)
+constexpr int kMRB = kMTY * kMTX * kMTZ * 4;                    // r (and q) box bytes (8192)
 constexpr int kMHB = (kMTY + 8) * (kMTX + 2) * (kMTZ + 2) * 4;  // hk box bytes (17280)
-constexpr int kMBuf = (kMRB + kMHB + 127) / 128 * 128;          // one staging buffer
+constexpr int kMBuf = (2 * kMRB + kMHB + 127) / 128 * 128;      // one staging buffer: r, q, hk
+constexpr int kMWin = 3 * (kMTX / 4 + 2) * kWY;                 // coarse window (216 values)
 constexpr size_t kMultSmem = 2 * (size_t)kMBuf + 2 * sizeof(uint64_t);
+
+// A tile of the walk as (y, x, z) tile coordinates, y fastest.
+struct MultTile {
+  int by, bx, bz;
+};
+
+// 1 / d by the hardware reciprocal approximation (PTX rcp.approx.f32,
+// within 1 ulp): the weight of a smoothing step needs no correct rounding.
+__device__ __forceinline__ float rcp_approx(float d) {
+  float y;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(d));
+  return y;
+}
 
 __global__ void __launch_bounds__(256, 3)
     k_pc_mult_tiled(const __grid_constant__ MultMaps maps, Geo g, Dims c, Dims cv,
                     const float* __restrict__ out, const float* scal, float* __restrict__ r,
-                    const float* __restrict__ q, const float* __restrict__ dg, float scale,
+                    const float* __restrict__ dg, float scale,
                     int bcx0, int bcx1, float omega, float* __restrict__ z, const int* err,
                     double* partials, CgState* st) {
-  __shared__ float sA[3][kMTX / 4 + 2][kWY];
-  __shared__ float sB[3][kMTX + 2][kWY];
-  __shared__ float sC[kMTZ + 2][kMTX + 2][kWY];
+  __shared__ float sA[2][3][kMTX / 4 + 2][kWY];  // coarse windows, double-buffered
+  __shared__ float sC[kMTZ + 2][kMTX + 2][kWY];   // f z1 interpolated in x and z
   extern __shared__ __align__(128) unsigned char dsm[];
   uint64_t* const bar = reinterpret_cast<uint64_t*>(dsm + 2 * kMBuf);
   pdl_begin();
@@ -982,188 +999,267 @@ __global__ void __launch_bounds__(256, 3)
   const float alpha = (float)st->alpha;
   const int tid = threadIdx.x;
   const int nty = (g.ny + kMTY - 1) / kMTY, ntx = g.nx / kMTX;  // the last y tile may be partial
-  const int64_t ntiles = (int64_t)nty * ntx * (g.nz / kMTZ);
-  // per-thread roles of the staging loops: (x, y) column of the windows
-  const int col_y = tid % kWY, col_x = tid / kWY;  // col_x < kMTX + 2 for tid < 180
-  // thread 0 stages the r and hk boxes of a tile into buffer b
-  auto stage = [&](int64_t tile, int b) {
-    const int by = (int)(tile % nty);
-    const int bx = (int)((tile / nty) % ntx);
-    const int bz = (int)(tile / ((int64_t)nty * ntx));
-    unsigned char* B = dsm + (size_t)b * kMBuf;
-    mbar_expect_tx(&bar[b], (unsigned)(kMRB + kMHB));
-    tma_load_3d(B, &maps.r, kMTY * by + 1 + kOff32, kMTX * bx + 1, kMTZ * bz + 1, &bar[b]);
-    tma_load_3d(B + kMRB, &maps.hk, kMTY * by, kMTX * bx, kMTZ * bz, &bar[b]);
+  const int ntiles = nty * ntx * (g.nz / kMTZ);
+  // the walk: tile blockIdx.x, then steps of gridDim.x tiles, advanced in
+  // tile coordinates (no division per tile)
+  auto decomp = [&](int t) {
+    MultTile m;
+    m.bz = t / (nty * ntx);
+    const int rem = t - m.bz * nty * ntx;
+    m.bx = rem / nty;
+    m.by = rem - m.bx * nty;
+    return m;
   };
+  const MultTile step = decomp(gridDim.x);
+  auto advance = [&](MultTile m) {
+    m.by += step.by;
+    int carry = m.by >= nty;
+    if (carry) m.by -= nty;
+    m.bx += step.bx + carry;
+    carry = m.bx >= ntx;
+    if (carry) m.bx -= ntx;
+    m.bz += step.bz + carry;
+    return m;
+  };
+  // thread 0 stages the r, q and hk boxes of a tile into buffer b
+  auto stage = [&](MultTile m, int b) {
+    unsigned char* B = dsm + (size_t)b * kMBuf;
+    const int ry = kMTY * m.by + 1 + kOff32, rx = kMTX * m.bx + 1, rz = kMTZ * m.bz + 1;
+    mbar_expect_tx(&bar[b], (unsigned)(2 * kMRB + kMHB));
+    tma_load_3d(B, &maps.r, ry, rx, rz, &bar[b]);
+    tma_load_3d(B + kMRB, &maps.q, ry, rx, rz, &bar[b]);
+    tma_load_3d(B + 2 * kMRB, &maps.hk, kMTY * m.by, kMTX * m.bx, kMTZ * m.bz, &bar[b]);
+  };
+  // threads 0..215 fetch one value each of a tile's coarse window into sA[b]
+  // (y fastest, then x, then z; coarse indexes clamped to the grid, so the
+  // interpolation below needs no clamping of its own)
+  auto fetch_window = [&](MultTile m, int b) {
+    if (coarse && tid < kMWin) {
+      const int wy = tid % kWY, wx = (tid / kWY) % (kMTX / 4 + 2);
+      const int wz = tid / (kWY * (kMTX / 4 + 2));
+      const int cy = min(max((kMTY / 4) * m.by - 1 + wy, 0), cv.ny - 1);
+      const int cx = min(max((kMTX / 4) * m.bx - 1 + wx, 0), cv.nx - 1);
+      const int cz = min(max(m.bz - 1 + wz, 0), cv.nz - 1);
+      cp_async4(&sA[b][wz][wx][wy], out + cy + (int64_t)c.ny * (cx + (int64_t)c.nx * cz));
+    }
+    cp_async_commit();
+  };
+  MultTile cur = decomp(blockIdx.x);
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    if (blockIdx.x < ntiles) stage(blockIdx.x, 0);
+    if ((int)blockIdx.x < ntiles) stage(cur, 0);
   }
-  int n_issued = blockIdx.x < ntiles ? 1 : 0;  // tiles staged (thread 0's count)
-  float a_zr = 0.f, a_zq = 0.f, a_rr = 0.f;
+  if ((int)blockIdx.x < ntiles) fetch_window(cur, 0);
+  __syncthreads();  // the barriers' initialisation is seen by every thread
+  int n_issued = (int)blockIdx.x < ntiles ? 1 : 0;  // tiles staged (thread 0's count)
+  // Cell roles: item h of a thread is 4 y-consecutive cells (coarse y cell
+  // mq) on x row xl of plane zl + 2h; offsets of item 0 in the r / q box,
+  // the hk box and sC (item 1: + 2 planes)
+  const int mq = tid % (kMTY / 4), xl = (tid / (kMTY / 4)) % kMTX, zl = tid / ((kMTY / 4) * kMTX);
+  const int so = 4 * tid;
+  constexpr int hxs = kMTY + 8, hzs = (kMTY + 8) * (kMTX + 2), cxs = kWY, czs = kWY * (kMTX + 2);
+  const int ho = ((zl + 1) * (kMTX + 2) + xl + 1) * hxs + 4 * mq + 4;
+  const int co = ((zl + 1) * (kMTX + 2) + xl + 1) * cxs + mq;
+  // the cells' arithmetic runs on pairs of FP32 lanes (paired FMA / add /
+  // multiply), one pair per two y-consecutive cells
+  const float2 nal = make_float2(-alpha, -alpha), om2 = make_float2(omega, omega);
+  const float2 sc2 = make_float2(scale, scale), nsc2 = make_float2(-scale, -scale);
+  const float2 zero2 = make_float2(0.f, 0.f);
+  float2 acc_zr = zero2, acc_zq = zero2, acc_rr = zero2;
   bool ok = true;
   int n = 0;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++n) {
-    const int by = (int)(tile % nty);
-    const int bx = (int)((tile / nty) % ntx);
-    const int bz = (int)(tile / ((int64_t)nty * ntx));
-    const int y0 = kMTY * by + 1, x0 = kMTX * bx + 1, z0 = kMTZ * bz + 1;
-    // coarse index of window entry 0 in y, x, z
-    const int cy0 = (kMTY / 4) * by - 1, cx0 = (kMTX / 4) * bx - 1, cz0 = bz - 1;
-    // every thread is done with the previous tile: its buffer takes the next
-    // tile's boxes, and the coarse windows are free
-    __syncthreads();
-    if (tid == 0 && tile + gridDim.x < ntiles) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      stage(tile + gridDim.x, (n + 1) & 1);
-      ++n_issued;
-    }
-    if (coarse) {
-      if (col_x < kMTX / 4 + 2) {
-        const int cy = min(max(cy0 + col_y, 0), cv.ny - 1);
-        const int cx = min(max(cx0 + col_x, 0), cv.nx - 1);
-#pragma unroll
-        for (int zz = 0; zz < 3; ++zz) {
-          const int cz = min(max(cz0 + zz, 0), cv.nz - 1);
-          sA[zz][col_x][col_y] = out[cy + (int64_t)c.ny * (cx + (int64_t)c.nx * cz)];
-        }
-      }
-      __syncthreads();
-      if (col_x < kMTX + 2) {  // x interpolation to the fine x positions x0-1 .. x0+kMTX
-        int lo, hi;
-        float w;
-        interp1(x0 - 2 + col_x, cv.nx, &lo, &hi, &w);
-#pragma unroll
-        for (int zz = 0; zz < 3; ++zz)
-          sB[zz][col_x][col_y] = w * sA[zz][lo - cx0][col_y] + (1.f - w) * sA[zz][hi - cx0][col_y];
-      }
-      __syncthreads();
-      if (col_x < kMTX + 2) {  // z interpolation to the fine planes z0-1 .. z0+kMTZ
-#pragma unroll
-        for (int zf = 0; zf < kMTZ + 2; ++zf) {
-          int lo, hi;
-          float w;
-          interp1(z0 - 2 + zf, cv.nz, &lo, &hi, &w);
-          sC[zf][col_x][col_y] =
-              f * (w * sB[lo - cz0][col_x][col_y] + (1.f - w) * sB[hi - cz0][col_x][col_y]);
-        }
-      }
-    }
-    // the tile's boxes have landed (the wait decision is made uniform)
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, cur = advance(cur), ++n) {
+    const int y0 = kMTY * cur.by + 1, x0 = kMTX * cur.bx + 1, z0 = kMTZ * cur.bz + 1;
+    // the tile's boxes and window have landed (the wait decision is made
+    // uniform), and every thread is done with the previous tile: its
+    // buffer and window take the next tile's
+    cp_async_wait_all();
     const bool w_ok = mbar_wait_bounded(&bar[n & 1], (unsigned)((n >> 1) & 1), 1u << 20);
     if (!__syncthreads_and(w_ok)) {
       ok = false;
       break;
     }
+    if (tile + (int)gridDim.x < ntiles) {
+      const MultTile nxt = advance(cur);
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        stage(nxt, (n + 1) & 1);
+        ++n_issued;
+      }
+      fetch_window(nxt, (n + 1) & 1);
+    }
+    if (coarse) {
+      // x interpolation of the window's 3 z planes, then z interpolation to
+      // the fine planes z0-1 .. z0+kMTZ (fine plane zf at coarse window
+      // cells (zlo, zlo + 1) with weight wz on zlo), scaled by f
+      // (the roles are the same in every tile: tiles start at multiples of 4
+      // fine cells, so the weights repeat).  Threads 0..179 own the column
+      // (x position xf, y entry cy) of the fine x positions x0-1 ..
+      // x0+kMTX; fine x position xf lies in the window's coarse cells
+      // (xlo, xlo + 1) with weight wxl on xlo.
+      if (tid < (kMTX + 2) * kWY) {
+        const int cy = tid % kWY, xf = tid / kWY;
+        const int xe = (xf - 1) & 3, xm = (xf - 1) >> 2;  // interp1 of fine index 8 bx - 1 + xf
+        const int xlo = xe < 2 ? xm : xm + 1;
+        const float wxl = 0.375f - 0.25f * (float)(xe & 1) + 0.5f * (float)(xe >> 1);
+        const float* W = &sA[n & 1][0][0][0] + xlo * kWY + cy;
+        constexpr int wzs = (kMTX / 4 + 2) * kWY;
+        float bz3[3];
+#pragma unroll
+        for (int zz = 0; zz < 3; ++zz)
+          bz3[zz] = wxl * W[zz * wzs] + (1.f - wxl) * W[zz * wzs + kWY];
+        float* C = &sC[0][0][0] + xf * kWY + cy;
+#pragma unroll
+        for (int zf = 0; zf < kMTZ + 2; ++zf) {
+          const int ze = (zf - 1) & 3, zm = (zf - 1) >> 2;
+          const int zlo = ze < 2 ? zm : zm + 1;
+          const float wz = 0.375f - 0.25f * (float)(ze & 1) + 0.5f * (float)(ze >> 1);
+          C[zf * czs] = f * (wz * bz3[zlo] + (1.f - wz) * bz3[zlo + 1]);
+        }
+      }
+      __syncthreads();
+    }
     const float* R = reinterpret_cast<const float*>(dsm + (size_t)(n & 1) * kMBuf);
-    const float* H = reinterpret_cast<const float*>(dsm + (size_t)(n & 1) * kMBuf + kMRB);
+    const float* Q = R + kMRB / 4;
+    const float* H = R + 2 * kMRB / 4;
+    const int i0 = y0 + 4 * mq, j = x0 + xl;
+    const int64_t gbase = g.ix(i0, j, z0 + zl);
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
-      const int u = tid + 256 * h;
-      const int mq = u % (kMTY / 4), xl = (u / (kMTY / 4)) % kMTX, zl = u / ((kMTY / 4) * kMTX);
-      const int i0 = y0 + 4 * mq, j = x0 + xl, k = z0 + zl;
-      if (i0 > g.ny) continue;  // beyond a partial tile (ny is a multiple of 4)
-      const int64_t idx = g.ix(i0, j, k);
-      const float4 qv = *reinterpret_cast<const float4*>(q + idx);
-      float4 rv = *reinterpret_cast<const float4*>(R + (zl * kMTX + xl) * kMTY + 4 * mq);
+      const int k = z0 + zl + 2 * h;
+      if (i0 > g.ny) break;  // beyond a partial tile (ny is a multiple of 4)
+      const int64_t idx = gbase + 2 * h * g.sz;
+      // the thread's 4 cells as two pairs, (i0, i0+1) and (i0+2, i0+3)
+      const int sh = so + h * (2 * kMTX * kMTY);
+      const float4 qv = *reinterpret_cast<const float4*>(Q + sh);
+      const float4 rv = *reinterpret_cast<const float4*>(R + sh);
+      const float2 q0 = make_float2(qv.x, qv.y), q1 = make_float2(qv.z, qv.w);
+      float2 r0 = make_float2(rv.x, rv.y), r1 = make_float2(rv.z, rv.w);
       if (rupd) {
-        rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
-        *reinterpret_cast<float4*>(r + idx) = rv;
+        r0 = __ffma2_rn(nal, q0, r0);
+        r1 = __ffma2_rn(nal, q1, r1);
+        *reinterpret_cast<float4*>(r + idx) = make_float4(r0.x, r0.y, r1.x, r1.y);
       }
-      const float ra[4] = {rv.x, rv.y, rv.z, rv.w};
-      const float qa[4] = {qv.x, qv.y, qv.z, qv.w};
-      // hk box: (zl + 1, xl + 1, column 4 mq + 4) is the thread's first cell
-      const int ho = ((zl + 1) * (kMTX + 2) + xl + 1) * (kMTY + 8) + 4 * mq + 4;
-      const int hxs = kMTY + 8, hzs = (kMTY + 8) * (kMTX + 2);
-      const float4 k4 = *reinterpret_cast<const float4*>(H + ho);
-      const float4 kx0 = *reinterpret_cast<const float4*>(H + ho - hxs);
-      const float4 kx1 = *reinterpret_cast<const float4*>(H + ho + hxs);
-      const float4 kz0 = *reinterpret_cast<const float4*>(H + ho - hzs);
-      const float4 kz1 = *reinterpret_cast<const float4*>(H + ho + hzs);
-      const float ky[6] = {H[ho - 1], k4.x, k4.y, k4.z, k4.w, H[ho + 4]};
-      const float kxa[4] = {kx0.x, kx0.y, kx0.z, kx0.w}, kxb[4] = {kx1.x, kx1.y, kx1.z, kx1.w};
-      const float kza[4] = {kz0.x, kz0.y, kz0.z, kz0.w}, kzb[4] = {kz1.x, kz1.y, kz1.z, kz1.w};
-      float dga[4] = {0.f, 0.f, 0.f, 0.f};
+      // hk box: (zl + 2h + 1, xl + 1, column 4 mq + 4) is the first cell
+      const float* hk = H + ho + h * (2 * hzs);
+      const float4 k4 = *reinterpret_cast<const float4*>(hk);
+      const float4 kx0 = *reinterpret_cast<const float4*>(hk - hxs);
+      const float4 kx1 = *reinterpret_cast<const float4*>(hk + hxs);
+      const float4 kz0 = *reinterpret_cast<const float4*>(hk - hzs);
+      const float4 kz1 = *reinterpret_cast<const float4*>(hk + hzs);
+      const float kyl = hk[-1], kyh = hk[4];
+      const float2 kc0 = make_float2(k4.x, k4.y), kc1 = make_float2(k4.z, k4.w);
+      // face coefficients c_f = hk_nb + hk_c; the y faces of the four cells
+      // are F_t = hk(i0-1+t) + hk(i0+t), t = 0..4 (cell y: F_y below, F_y+1
+      // above).  A face outside the operator (a Neumann or copied ghost)
+      // gets c_f = 0: it then drops out of the diagonal and of S(z1), as the
+      // ghost rules make its difference vanish.
+      float2 fym0 = __fadd2_rn(make_float2(kyl, k4.x), kc0);         // F0, F1
+      const float2 fym1 = __fadd2_rn(make_float2(k4.y, k4.z), kc1);  // F2, F3
+      float f4 = kyh + k4.w;
+      if (i0 == 1) fym0.x = 0.f;
+      if (i0 + 3 == g.ny) f4 = 0.f;
+      const float2 fyp0 = make_float2(fym0.y, fym1.x), fyp1 = make_float2(fym1.y, f4);
+      float2 fxm0 = __fadd2_rn(make_float2(kx0.x, kx0.y), kc0);
+      float2 fxm1 = __fadd2_rn(make_float2(kx0.z, kx0.w), kc1);
+      float2 fxp0 = __fadd2_rn(make_float2(kx1.x, kx1.y), kc0);
+      float2 fxp1 = __fadd2_rn(make_float2(kx1.z, kx1.w), kc1);
+      float2 fzm0 = __fadd2_rn(make_float2(kz0.x, kz0.y), kc0);
+      float2 fzm1 = __fadd2_rn(make_float2(kz0.z, kz0.w), kc1);
+      float2 fzp0 = __fadd2_rn(make_float2(kz1.x, kz1.y), kc0);
+      float2 fzp1 = __fadd2_rn(make_float2(kz1.z, kz1.w), kc1);
+      if (j == 1 && !bcx0) fxm0 = fxm1 = zero2;
+      if (j == g.nx && !bcx1) fxp0 = fxp1 = zero2;
+      if (k == 1) fzm0 = fzm1 = zero2;
+      if (k == g.nz) fzp0 = fzp1 = zero2;
+      // the Jacobi weight 1 / A_cc, faces summed in k_invdiag's order
+      const float2 s0 = __fadd2_rn(
+          __fadd2_rn(__fadd2_rn(__fadd2_rn(__fadd2_rn(fym0, fyp0), fxm0), fxp0), fzm0), fzp0);
+      const float2 s1 = __fadd2_rn(
+          __fadd2_rn(__fadd2_rn(__fadd2_rn(__fadd2_rn(fym1, fyp1), fxm1), fxp1), fzm1), fzp1);
+      float2 dg0 = zero2, dg1 = zero2, d0, d1;
       if (dg) {  // the CnE form: A p = diag p - scale S(p)
         const float4 d4 = *reinterpret_cast<const float4*>(dg + idx);
-        dga[0] = d4.x; dga[1] = d4.y; dga[2] = d4.z; dga[3] = d4.w;
-      }
-      // the Jacobi weight 1 / A_cc, faces summed in k_invdiag's order
-      float da[4];
-#pragma unroll
-      for (int y = 0; y < 4; ++y) {
-        const float kc = ky[y + 1];
-        float sum = 0.f;
-        if (i0 + y > 1) sum += ky[y] + kc;
-        if (i0 + y < g.ny) sum += ky[y + 2] + kc;
-        if (j > 1 || bcx0) sum += kxa[y] + kc;
-        if (j < g.nx || bcx1) sum += kxb[y] + kc;
-        if (k > 1) sum += kza[y] + kc;
-        if (k < g.nz) sum += kzb[y] + kc;
-        const float d = dg ? dga[y] + scale * sum : -scale * sum;
-        da[y] = (d != 0.f) ? 1.f / d : 0.f;
-      }
-      float za[4];
-      if (coarse) {
-        const int xf = 1 + xl, zf = 1 + zl;
-        // y interpolation: coarse cells (m-1, m, m+1) are window entries
-        // mq, mq+1, mq+2; fine offsets -1..4 of this coarse cell
-        float cen[6], ym[4], yp[4], zm4[4], zp4[4];
-        {
-          const float a0 = sC[zf][xf][mq], a1 = sC[zf][xf][mq + 1], a2 = sC[zf][xf][mq + 2];
-          cen[0] = 0.625f * a0 + 0.375f * a1;
-          cen[1] = 0.375f * a0 + 0.625f * a1;
-          cen[2] = 0.125f * a0 + 0.875f * a1;
-          cen[3] = 0.875f * a1 + 0.125f * a2;
-          cen[4] = 0.625f * a1 + 0.375f * a2;
-          cen[5] = 0.375f * a1 + 0.625f * a2;
-        }
-        const float* rows[4] = {&sC[zf][xf - 1][0], &sC[zf][xf + 1][0], &sC[zf - 1][xf][0],
-                                &sC[zf + 1][xf][0]};
-        float* dst[4] = {ym, yp, zm4, zp4};
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const float a0 = rows[t][mq], a1 = rows[t][mq + 1], a2 = rows[t][mq + 2];
-          dst[t][0] = 0.375f * a0 + 0.625f * a1;
-          dst[t][1] = 0.125f * a0 + 0.875f * a1;
-          dst[t][2] = 0.875f * a1 + 0.125f * a2;
-          dst[t][3] = 0.625f * a1 + 0.375f * a2;
-        }
-        // ghost rules only for the cells on a domain face
-        if (i0 == 1 || i0 + 3 == g.ny || j == 1 || j == g.nx || k == 1 || k == g.nz) {
-          if (i0 == 1) cen[0] = cen[1];
-          if (i0 + 3 == g.ny) cen[5] = cen[4];
-#pragma unroll
-          for (int y = 0; y < 4; ++y) {
-            const float pc = cen[y + 1];
-            if (j == 1) ym[y] = bcx0 ? 0.f : pc;
-            if (j == g.nx) yp[y] = bcx1 ? 0.f : pc;
-            if (k == 1) zm4[y] = pc;
-            if (k == g.nz) zp4[y] = pc;
-          }
-        }
-#pragma unroll
-        for (int y = 0; y < 4; ++y) {
-          const float pc = cen[y + 1];
-          const float sv = face_sum<float>(ky[y + 1], pc, ky[y + 2], cen[y + 2], ky[y], cen[y],
-                                           kxb[y], yp[y], kxa[y], ym[y], kzb[y], zp4[y], kza[y],
-                                           zm4[y]);
-          const float az = dg ? dga[y] * pc - scale * sv : scale * sv;
-          za[y] = pc + omega * (da[y] * (ra[y] - az));
-        }
+        dg0 = make_float2(d4.x, d4.y);
+        dg1 = make_float2(d4.z, d4.w);
+        d0 = __ffma2_rn(sc2, s0, dg0);
+        d1 = __ffma2_rn(sc2, s1, dg1);
       } else {
-#pragma unroll
-        for (int y = 0; y < 4; ++y) za[y] = da[y] * ra[y];
+        d0 = __fmul2_rn(nsc2, s0);
+        d1 = __fmul2_rn(nsc2, s1);
       }
-#pragma unroll
-      for (int y = 0; y < 4; ++y) {
-        a_zr += za[y] * ra[y];
-        a_zq += za[y] * qa[y];
-        a_rr += ra[y] * ra[y];
+      const float2 da0 = make_float2(d0.x != 0.f ? rcp_approx(d0.x) : 0.f,
+                                     d0.y != 0.f ? rcp_approx(d0.y) : 0.f);
+      const float2 da1 = make_float2(d1.x != 0.f ? rcp_approx(d1.x) : 0.f,
+                                     d1.y != 0.f ? rcp_approx(d1.y) : 0.f);
+      float2 z0v, z1v;
+      if (coarse) {
+        // y interpolation: coarse cells (m-1, m, m+1) are window entries mq,
+        // mq+1, mq+2; z1 at the fine offsets -1..4 of this coarse cell as
+        // the pairs (-1, 0), (1, 2), (3, 4)
+        const float* cc0 = &sC[0][0][0] + co + h * (2 * czs);
+        const float a0 = cc0[0], a1 = cc0[1], a2 = cc0[2];
+        const float2 A1 = make_float2(a1, a1);
+        const float2 cm = __ffma2_rn(make_float2(0.625f, 0.375f), make_float2(a0, a0),
+                                     __fmul2_rn(make_float2(0.375f, 0.625f), A1));
+        const float2 cc = __ffma2_rn(make_float2(0.125f, 0.125f), make_float2(a0, a2),
+                                     __fmul2_rn(make_float2(0.875f, 0.875f), A1));
+        const float2 cp = __ffma2_rn(make_float2(0.375f, 0.625f), make_float2(a2, a2),
+                                     __fmul2_rn(make_float2(0.625f, 0.375f), A1));
+        const float2 pc0 = make_float2(cm.y, cc.x), pc1 = make_float2(cc.y, cp.x);
+        // the four neighbour rows (x-1, x+1, z-1, z+1), offsets 0..3
+        auto row = [&](const float* rp, float2& lo, float2& hi) {
+          const float b0 = rp[0], b1 = rp[1], b2 = rp[2];
+          const float2 B1 = make_float2(b1, b1);
+          lo = __ffma2_rn(make_float2(0.375f, 0.125f), make_float2(b0, b0),
+                          __fmul2_rn(make_float2(0.625f, 0.875f), B1));
+          hi = __ffma2_rn(make_float2(0.125f, 0.375f), make_float2(b2, b2),
+                          __fmul2_rn(make_float2(0.875f, 0.625f), B1));
+        };
+        float2 xm0, xm1, xp0, xp1, zm0, zm1, zp0, zp1;
+        row(cc0 - cxs, xm0, xm1);
+        row(cc0 + cxs, xp0, xp1);
+        row(cc0 - czs, zm0, zm1);
+        row(cc0 + czs, zp0, zp1);
+        // a Dirichlet x face reads a zero ghost (a Neumann one has c_f = 0)
+        if (j == 1) xm0 = xm1 = zero2;
+        if (j == g.nx) xp0 = xp1 = zero2;
+        // S(z1) = sum_f c_f (z1_nb - z1_c), faces in the order of face_sum
+        auto fsum = [&](float2 pc, float2 pyp, float2 pym, float2 pxp, float2 pxm, float2 pzp,
+                        float2 pzm, float2 cyp, float2 cym, float2 cxp, float2 cxm, float2 czp,
+                        float2 czm) {
+          float2 sv = __fmul2_rn(cyp, __fadd2_rn(pyp, neg2(pc)));
+          sv = __ffma2_rn(cym, __fadd2_rn(pym, neg2(pc)), sv);
+          sv = __ffma2_rn(cxp, __fadd2_rn(pxp, neg2(pc)), sv);
+          sv = __ffma2_rn(cxm, __fadd2_rn(pxm, neg2(pc)), sv);
+          sv = __ffma2_rn(czp, __fadd2_rn(pzp, neg2(pc)), sv);
+          return __ffma2_rn(czm, __fadd2_rn(pzm, neg2(pc)), sv);
+        };
+        const float2 sv0 = fsum(pc0, cc, cm, xp0, xm0, zp0, zm0, fyp0, fym0, fxp0, fxm0, fzp0,
+                                fzm0);
+        const float2 sv1 = fsum(pc1, cp, cc, xp1, xm1, zp1, zm1, fyp1, fym1, fxp1, fxm1, fzp1,
+                                fzm1);
+        // -A z1 = scale S(z1) - diag z1 (potential form: -scale S(z1))
+        float2 naz0, naz1;
+        if (dg) {
+          naz0 = __ffma2_rn(neg2(dg0), pc0, __fmul2_rn(sc2, sv0));
+          naz1 = __ffma2_rn(neg2(dg1), pc1, __fmul2_rn(sc2, sv1));
+        } else {
+          naz0 = __fmul2_rn(nsc2, sv0);
+          naz1 = __fmul2_rn(nsc2, sv1);
+        }
+        z0v = __ffma2_rn(om2, __fmul2_rn(da0, __fadd2_rn(r0, naz0)), pc0);
+        z1v = __ffma2_rn(om2, __fmul2_rn(da1, __fadd2_rn(r1, naz1)), pc1);
+      } else {
+        z0v = __fmul2_rn(da0, r0);
+        z1v = __fmul2_rn(da1, r1);
       }
-      *reinterpret_cast<float4*>(z + idx) = make_float4(za[0], za[1], za[2], za[3]);
+      acc_zr = __ffma2_rn(z0v, r0, __ffma2_rn(z1v, r1, acc_zr));
+      acc_zq = __ffma2_rn(z0v, q0, __ffma2_rn(z1v, q1, acc_zq));
+      acc_rr = __ffma2_rn(r0, r0, __ffma2_rn(r1, r1, acc_rr));
+      *reinterpret_cast<float4*>(z + idx) = make_float4(z0v.x, z0v.y, z1v.x, z1v.y);
     }
   }
   if (!ok) {
@@ -1176,9 +1272,12 @@ __global__ void __launch_bounds__(256, 3)
         if (cnt > 0) mbar_wait_bounded(&bar[b], (unsigned)((cnt - 1) & 1), 1u << 20);
       }
     }
-    a_zr = a_zq = a_rr = 0.f;
+    cp_async_wait_all();
+    acc_zr = acc_zq = acc_rr = zero2;
   }
-  double v[3] = {(double)a_zr, (double)a_zq, (double)a_rr}, tot[3];
+  double v[3] = {(double)acc_zr.x + acc_zr.y, (double)acc_zq.x + acc_zq.y,
+                 (double)acc_rr.x + acc_rr.y},
+         tot[3];
   if (grid_reduce<3>(v, partials, &st->counter[5], tot))
     if (threadIdx.x == 0) fcg_close(st, tot[0], tot[1], tot[2], rupd, *err);
 }
@@ -1200,7 +1299,7 @@ struct NetPc {
   // operator of the current solve, for the multiplicative smoothing step
   const float* hk32 = nullptr;
   const float* dg32 = nullptr;  // the CnE form's diagonal (null: potential form)
-  MultMaps mmaps{};             // tensor maps of the multiplicative step (r, hk)
+  MultMaps mmaps{};             // tensor maps of the multiplicative step (r, q, hk)
   float scale = 1.f;
   int bcx0 = 0, bcx1 = 0;
   void release() {
@@ -1234,7 +1333,7 @@ bool net_pc_usable(const sbm_ctx* ctx, int form) {
 }
 
 int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, const float* r32,
-                 double scale, int bcx0, int bcx1, cudaStream_t s) {
+                 const float* q32, double scale, int bcx0, int bcx1, cudaStream_t s) {
   netd::NetPc* pc = static_cast<netd::NetPc*>(ctx->net);
   int rc = conv3_init();
   if (rc) return rc;
@@ -1243,6 +1342,10 @@ int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, const float
     SBM_CUDA_TRY(cudaFuncSetAttribute(netd::k_pc_mult_tiled,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)netd::kMultSmem));
+    // three blocks of ~72 KB per SM: the largest shared-memory carveout
+    SBM_CUDA_TRY(cudaFuncSetAttribute(netd::k_pc_mult_tiled,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      (int)cudaSharedmemCarveoutMaxShared));
     mult_attr = true;
   }
   const Geo& g = ctx->g32;
@@ -1277,6 +1380,7 @@ int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, const float
   pc->hk32 = hk32;
   pc->dg32 = dg32;
   if (!make_map_box(&pc->mmaps.r, r32 - kOff32, g, netd::kMTY, netd::kMTX, netd::kMTZ) ||
+      !make_map_box(&pc->mmaps.q, q32 - kOff32, g, netd::kMTY, netd::kMTX, netd::kMTZ) ||
       !make_map_box(&pc->mmaps.hk, hk32 - kOff32, g, netd::kMTY + 8, netd::kMTX + 2,
                     netd::kMTZ + 2))
     return SBM_ERR_STATE;
@@ -1314,13 +1418,13 @@ int net_pc_nodes() { return 3 + 9; }
 // The multiplicative step: tiles of 64 x 8 x 4 fine cells (the last y tile
 // may be partial), one wave of resident blocks (3 per SM at 80 registers)
 // walking them grid-stride.
-static void launch_mult(netd::NetPc* pc, const Geo& g, float* r32, const float* q32,
-                        double* partials, CgState* st, cudaStream_t s) {
+static void launch_mult(netd::NetPc* pc, const Geo& g, float* r32, double* partials, CgState* st,
+                        cudaStream_t s) {
   const int64_t tiles = (int64_t)((g.ny + netd::kMTY - 1) / netd::kMTY) * (g.nx / netd::kMTX) *
                         (g.nz / netd::kMTZ);
   const unsigned bt = (unsigned)(tiles < 152 * 3 ? tiles : 152 * 3);
   launch_pdl(netd::k_pc_mult_tiled, dim3(bt), dim3(256), netd::kMultSmem, s, pc->mmaps, g, pc->c,
-             pc->cv, (const float*)pc->w->out, (const float*)pc->scal, r32, q32, pc->dg32,
+             pc->cv, (const float*)pc->w->out, (const float*)pc->scal, r32, pc->dg32,
              pc->scale, pc->bcx0, pc->bcx1, netd::kPcOmega, pc->zf + kOff32,
              (const int*)pc->net->err, partials, st);
 }
@@ -1351,7 +1455,7 @@ void net_pc_launch(sbm_ctx* ctx, float* r32, const float* iv32, const float* q32
                (const float*)pc->w->out, (const float*)pc->scal, r32, iv32, q32, pc->zf + kOff32,
                (const int*)pc->net->err, partials, st);
   } else {
-    launch_mult(pc, g, r32, q32, partials, st, s);
+    launch_mult(pc, g, r32, partials, st, s);
   }
   SBM_LAUNCHED(1);
 }
@@ -1363,7 +1467,7 @@ void net_pc_launch_part(sbm_ctx* ctx, int part, float* r32, const float* q32,
     netd::forward(pc->net, *pc->w, false, &st->done, &st->pc_off, s);
     return;
   }
-  launch_mult(pc, ctx->g32, r32, q32, partials, st, s);
+  launch_mult(pc, ctx->g32, r32, partials, st, s);
   SBM_LAUNCHED(1);
 }
 

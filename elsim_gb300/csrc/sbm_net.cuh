@@ -15,10 +15,11 @@ bool net_pc_usable(const sbm_ctx* ctx, int form);
 // Per-solve set-up on the context stream (static features of the coarse
 // grid from the FP32 half coefficient and, for FORM 1, the FP32 diagonal
 // dg32 -- null for FORM 0; output scaling; the tensor maps the
-// multiplicative step stages r and hk with).  hk32 / dg32 / r32 are the
-// solver's FP32 fields (base + kOff32).
+// multiplicative step stages r, q and hk with).  hk32 / dg32 / r32 / q32 are
+// the solver's FP32 fields (base + kOff32); later launches pass the same r32
+// and q32.
 int net_pc_begin(sbm_ctx* ctx, const float* hk32, const float* dg32, const float* r32,
-                 double scale, int bcx0, int bcx1, cudaStream_t s);
+                 const float* q32, double scale, int bcx0, int bcx1, cudaStream_t s);
 
 // One application inside the flexible CG (no-op once st->done is set):
 // R r when stale (first use, residual replacement), R r -= alpha R q and

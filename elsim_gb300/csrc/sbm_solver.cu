@@ -1205,8 +1205,8 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
     SBM_LAUNCHED(1);
   }
   if (learned &&
-      (rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, r32, sp.scale, sp.bcx0, sp.bcx1,
-                         s)))
+      (rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, r32, q32, sp.scale, sp.bcx0,
+                         sp.bcx1, s)))
     return rc;
   FcgDirArgs fx{};
   if (learned) {
@@ -1408,8 +1408,8 @@ int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double*
                                          dg32);
   k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
   SBM_LAUNCHED(2);
-  if ((rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, r32, sp.scale, sp.bcx0, sp.bcx1,
-                         s)))
+  if ((rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, r32, q32, sp.scale, sp.bcx0,
+                         sp.bcx1, s)))
     return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(ctx->r64, r, sizeof(double) * g.nh, cudaMemcpyHostToDevice, s));
   k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, ctx->r64, r32, nullptr, nullptr);
