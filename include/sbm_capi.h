@@ -384,9 +384,9 @@ int sbm_accdiff(int py, int px, int pz, const double* psi, double* cn,
  * library (SBM_NOALLOC_REDIST_MAX_CELLS doubles, 8 MiB, held on every GPU
  * that loads the library until exit); grids of more padded cells, or with
  * pz + 2 > 65535, are rejected with SBM_ERR_ARG and a message in
- * sbm_last_error().  It calls no cudaMalloc or cudaFree.  The first call on a
- * device looks up the scratch address on that device, so make that first
- * call before any stream capture.  All calls share the scratch: calls that
+ * sbm_last_error().  It calls no cudaMalloc or cudaFree.  Because it
+ * synchronizes the stream, no call (first or later) may be made while that
+ * stream is being captured into a graph.  All calls share the scratch: calls that
  * overlap on the GPU race.  Results are bit-identical to sbm_redist. */
 #define SBM_NOALLOC_REDIST_MAX_CELLS (1 << 20)
 int sbm_redist_noalloc(int lit, int py, int px, int pz, double dt, const double* sg, double* f,
