@@ -39,32 +39,6 @@ BatchCache g_batch;
 // and its round counters are shared by every call.
 std::mutex g_batch_mu;
 
-// Sets the WHILE condition of one volume: another round while the solve is
-// not done and fewer than `cap` rounds ran (init: before the first round).
-// Past the cap the volume is marked as stopped by the iteration cap.
-__global__ void k_batch_loop(cudaGraphConditionalHandle h, CgState* st, int* rounds, int cap,
-                             int init) {
-  if (threadIdx.x) return;
-  const int r = init ? 0 : *rounds + 1;
-  *rounds = r;
-  const bool more = st->done == 0 && r < cap;
-  if (!more && st->done == 0) st->done = 2;
-  cudaGraphSetConditional(h, more ? 1u : 0u);
-}
-
-int add_loop_kernel(cudaGraph_t g, const cudaGraphNode_t* dep, cudaGraphConditionalHandle h,
-                    CgState* st, int* rounds, int cap, int init, cudaGraphNode_t* out) {
-  void* args[] = {&h, &st, &rounds, &cap, &init};
-  cudaKernelNodeParams kp{};
-  kp.func = reinterpret_cast<void*>(k_batch_loop);
-  kp.gridDim = dim3(1);
-  kp.blockDim = dim3(32);
-  kp.sharedMemBytes = 0;
-  kp.kernelParams = args;
-  SBM_CUDA_TRY(cudaGraphAddKernelNode(out, g, dep, dep ? 1 : 0, &kp));
-  return SBM_OK;
-}
-
 }  // namespace
 
 extern "C" int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bcx0,
@@ -140,8 +114,8 @@ extern "C" int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bc
       SBM_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g_batch.parent, 0,
                                                     cudaGraphCondAssignDefault));
       cudaGraphNode_t first, loop, child, last;
-      int rc = add_loop_kernel(g_batch.parent, nullptr, h, ctxs[v]->st, g_batch.rounds + v, cap,
-                               1, &first);
+      int rc = add_graph_loop_node(g_batch.parent, nullptr, h, ctxs[v]->st, g_batch.rounds + v,
+                                   cap, 1, &first);
       if (rc) return rc;
       cudaGraphNodeParams cp{};
       cp.type = cudaGraphNodeTypeConditional;
@@ -151,8 +125,8 @@ extern "C" int sbm_batch_solve_ops(sbm_ctx** ctxs, const int* ops, const int* bc
       SBM_CUDA_TRY(cudaGraphAddNode(&loop, g_batch.parent, &first, nullptr, 1, &cp));
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       SBM_CUDA_TRY(cudaGraphAddChildGraphNode(&child, body, nullptr, 0, graphs[v]));
-      if ((rc = add_loop_kernel(body, &child, h, ctxs[v]->st, g_batch.rounds + v, cap, 0,
-                                &last)))
+      if ((rc = add_graph_loop_node(body, &child, h, ctxs[v]->st, g_batch.rounds + v, cap, 0,
+                                    &last)))
         return rc;
     }
     SBM_CUDA_TRY(cudaGraphInstantiate(&g_batch.exec, g_batch.parent, 0));

@@ -292,6 +292,56 @@ __host__ __device__ __forceinline__ void df_split(double v, float* hi, float* lo
   *lo = (float)(v - (double)h);
 }
 
+// (double)f with integer instructions for zero and normal f (exact, as the
+// conversion is); subnormal, infinite and NaN f take the conversion.
+__device__ __forceinline__ double f2d_int(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if ((u << 1) == 0) return __longlong_as_double((long long)sign);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0 || e == 0xffu) return (double)f;
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023 - 127) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// The same split with integer instructions (GB300's FP64 pipe is some 64x
+// slower than its integer and FP32 pipes): hi rounds the 53-bit significand
+// to 24 bits (to nearest, ties to even, as the conversion does), the exact
+// remainder r (|r| <= 2^28 units of the double's last place) becomes lo by
+// one int -> float conversion (round to nearest) and a power-of-two scale,
+// so hi and lo are bit-identical to df_split's.  Zero is split as 0 + 0;
+// magnitudes outside [2^-70, 2^127) (where lo could be subnormal or hi
+// could overflow) take df_split's FP64 path.
+__device__ __forceinline__ void df_split_int(double v, float* hi, float* lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const int eb = (int)((u >> 52) & 0x7ff);  // biased exponent
+  const unsigned sign = (unsigned)(u >> 63) << 31;
+  if (eb == 0 && (u << 1) == 0) {  // +-0
+    *hi = __uint_as_float(sign);
+    *lo = 0.f;
+    return;
+  }
+  const int e = eb - 1023;
+  if (e < -70 || e > 126) {
+    df_split(v, hi, lo);
+    return;
+  }
+  const unsigned long long m = (u & ((1ull << 52) - 1)) | (1ull << 52);
+  unsigned long long mh = m >> 29;
+  const unsigned long long drop = m & ((1ull << 29) - 1);
+  if (drop > (1ull << 28) || (drop == (1ull << 28) && (mh & 1))) mh += 1;
+  const int r = (int)((long long)m - (long long)(mh << 29));
+  int eh = e;
+  if (mh == (1ull << 24)) {  // rounding carried into the next binade
+    mh >>= 1;
+    eh += 1;
+  }
+  *hi = __uint_as_float(sign | ((unsigned)(eh + 127) << 23) | ((unsigned)mh & 0x7fffffu));
+  const float scale = __uint_as_float((unsigned)(e - 52 + 127) << 23);  // 2^(e-52), normal
+  // an exact split (r = 0) gives lo = +0, as v - (double)hi does
+  *lo = r == 0 ? 0.f : __uint_as_float(__float_as_uint(__int2float_rn(r) * scale) ^ sign);
+}
+
 // Extra operands of the flexible-CG direction kernel (learned
 // preconditioner).  That kernel also applies the previous iteration's
 // deferred x32 += alpha p_old (or, after a residual replacement, folds x32
@@ -428,6 +478,14 @@ struct sbm_ctx {
     int nodes;
   };
   std::map<std::string, GraphRec> graphs;
+  // device-looped runs of a chunk graph (a WHILE conditional node around
+  // it), keyed by the chunk graph, with the round cap they were built for
+  struct LoopRec {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int cap = 0;
+  };
+  std::map<cudaGraph_t, LoopRec> loops;
   // arguments of the last mixed solve, replayed by sbm_bench_kernel
   sbm::OpArgs<float> last_op32{};
   int last_pc = -1;
@@ -454,4 +512,11 @@ int bench_kernel(sbm_ctx* ctx, int which, int reps, float* ms_per_launch, double
 int ensure_fp32_work(sbm_ctx* ctx);
 int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double* z);
 void release_graphs(sbm_ctx* ctx);
+// Adds to graph g (after *dep when given) a one-thread kernel node that sets
+// the WHILE condition h: another round while st->done is clear and fewer
+// than cap rounds ran (init: before the first round, which it counts from
+// 0 in *rounds); past the cap the solve is marked as stopped by the
+// iteration cap (st->done = 2).
+int add_graph_loop_node(cudaGraph_t g, const cudaGraphNode_t* dep, cudaGraphConditionalHandle h,
+                        CgState* st, int* rounds, int cap, int init, cudaGraphNode_t* out);
 }  // namespace sbm

@@ -22,6 +22,7 @@
 //         residual is periodically recomputed in FP64 and the correction
 //         accumulated in FP64, without restarting the Krylov space.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -321,6 +322,29 @@ cudaError_t launch_half(const Geo& g, const double* k, double* hk, cudaStream_t 
 
 // ---------------------------------------------------------------- driver
 
+__global__ void k_graph_loop(cudaGraphConditionalHandle h, CgState* st, int* rounds, int cap,
+                             int init) {
+  if (threadIdx.x) return;
+  const int r = init ? 0 : *rounds + 1;
+  *rounds = r;
+  const bool more = st->done == 0 && r < cap;
+  if (!more && st->done == 0) st->done = 2;
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+int add_graph_loop_node(cudaGraph_t g, const cudaGraphNode_t* dep, cudaGraphConditionalHandle h,
+                        CgState* st, int* rounds, int cap, int init, cudaGraphNode_t* out) {
+  void* args[] = {&h, &st, &rounds, &cap, &init};
+  cudaKernelNodeParams kp{};
+  kp.func = reinterpret_cast<void*>(k_graph_loop);
+  kp.gridDim = dim3(1);
+  kp.blockDim = dim3(32);
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = args;
+  SBM_CUDA_TRY(cudaGraphAddKernelNode(out, g, dep, dep ? 1 : 0, &kp));
+  return SBM_OK;
+}
+
 namespace {
 
 template <typename T>
@@ -393,6 +417,50 @@ int capture_graph(sbm_ctx* ctx, const std::string& key, int nodes_per_iter, Body
   ctx->graphs[key] = {ex, graph, nodes_per_iter * len};
   *exec = ex;
   *nodes = nodes_per_iter * len;
+  return SBM_OK;
+}
+
+// Runs the chunk graph on the device until the state at dst reports done:
+// a parent graph (built once per chunk graph and round cap) holds a WHILE
+// conditional node whose body is the chunk followed by k_graph_loop, so the
+// loop stops after the chunk in which the solve finished, without a host
+// round trip per chunk.  The round count is kept in dst->counter[7]; the
+// final state is copied through the pinned hbuf[0] to *final_state.
+int run_loop(sbm_ctx* ctx, cudaGraph_t chunk, int nodes, int max_it, CgState* dst, CgState* hbuf,
+             CgState* final_state) {
+  cudaStream_t s = ctx->stream;
+  const int cap = max_it > INT_MAX - 2 ? INT_MAX : max_it + 2;  // each round >= 1 iteration
+  sbm_ctx::LoopRec& L = ctx->loops[chunk];
+  if (!L.exec || L.cap != cap) {
+    if (L.exec) cudaGraphExecDestroy(L.exec);
+    if (L.graph) cudaGraphDestroy(L.graph);
+    L = sbm_ctx::LoopRec();
+    SBM_CUDA_TRY(cudaGraphCreate(&L.graph, 0));
+    cudaGraphConditionalHandle h;
+    SBM_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, L.graph, 0, cudaGraphCondAssignDefault));
+    int* rounds = reinterpret_cast<int*>(&dst->counter[7]);
+    cudaGraphNode_t first, loop, child, last;
+    int rc = add_graph_loop_node(L.graph, nullptr, h, dst, rounds, cap, 1, &first);
+    if (rc) return rc;
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    SBM_CUDA_TRY(cudaGraphAddNode(&loop, L.graph, &first, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    SBM_CUDA_TRY(cudaGraphAddChildGraphNode(&child, body, nullptr, 0, chunk));
+    if ((rc = add_graph_loop_node(body, &child, h, dst, rounds, cap, 0, &last))) return rc;
+    SBM_CUDA_TRY(cudaGraphInstantiate(&L.exec, L.graph, 0));
+    L.cap = cap;
+  }
+  SBM_CUDA_TRY(cudaGraphLaunch(L.exec, s));
+  SBM_CUDA_TRY(cudaMemcpyAsync(&hbuf[0], dst, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+  SBM_CUDA_TRY(cudaEventRecord(ctx->evq[0], s));
+  SBM_CUDA_TRY(cudaEventSynchronize(ctx->evq[0]));
+  *final_state = hbuf[0];
+  const int rounds = (int)hbuf[0].counter[7];
+  SBM_LAUNCHED((int64_t)rounds * (nodes + 1) + 1);
   return SBM_OK;
 }
 
@@ -861,7 +929,6 @@ __global__ void __launch_bounds__(BX* BY)
     k_rel_resid_df(Geo g, int zc, DfResArgs a, double* partials, CgState* st) {
   pdl_begin();
   if (!st->reliable || st->done) return;
-  const bool zero_corr = st->initial != 0;
   const int nty = (g.ny + BX - 1) / BX, ntx = (g.nx + BY - 1) / BY;
   const int ntiles = nty * ntx * ((g.nz + zc - 1) / zc);
   double a_rr = 0.0, a_rz = 0.0;
@@ -874,17 +941,7 @@ __global__ void __launch_bounds__(BX* BY)
     const int k1 = min(k0 + zc - 1, g.nz);
     const bool active = (i <= g.ny) && (j <= g.nx);
     float t_rr = 0.f, t_rz = 0.f;
-    if (active && zero_corr) {
-      // first replacement of a solve: the correction is zero, r = r0
-      for (int k = k0; k <= k1; ++k) {
-        const int64_t c = g.ix(i, j, k);
-        const float rf = a.r0hi[c];
-        a.r32[c] = rf;
-        const float zf = PC ? a.invd32[c] * rf : rf;
-        t_rr += rf * rf;
-        t_rz += rf * zf;
-      }
-    } else if (!zero_corr) {
+    {
       const int tx = threadIdx.x, ty = threadIdx.y, tf = ty * BX + tx;
       int hrow = -1, hcol = -1;
       if (tf < 2 * BX) {  // rows 0 and BY + 1 (x halo)
@@ -964,12 +1021,10 @@ __global__ void __launch_bounds__(BX* BY)
       if (!isfinite(rms)) st->done = 3;
       else if (!(rms > st->tol)) st->done = 1;
       else if (st->iter >= st->max_it) st->done = 2;
-      if (st->initial) st->aux[0] = tot[0];
       st->aux[1] = 0.0;  // the coarse residual of the learned preconditioner is stale
       if (!FLEX) {
-        st->beta = st->initial ? 0.0 : tot[1] / st->rho;
+        st->beta = tot[1] / st->rho;
         st->rho = tot[1];
-        st->initial = 0;
       }
       st->rr = tot[0];
       st->maxrr = tot[0];
@@ -982,11 +1037,16 @@ __global__ void __launch_bounds__(BX* BY)
 // Initial residual of the mixed solve in double-float arithmetic:
 // r0 = b - A x0 with x0's stored ghosts (Dirichlet / flux data: no ghost
 // rules), from the hi + lo splits of x0 (xhi, xlo) and b (bhi, blo) in the
-// FP32 layout; r0 is kept as the pair r0hi + r0lo for the replacements, and
-// the last block sets rr0 = r0.r0 and the state of a new solve (as
-// k_residual_mem does in FP64).  The operands of k_rel_resid_df, with
-// hkhi / hklo / dghi / dglo / scale / r0hi / r0lo of `a` used; same tiling.
-template <int FORM>
+// FP32 layout; r0 is kept as the pair r0hi + r0lo for the replacements and
+// its high part starts the FP32 residual (a.r32).  The last block sets
+// rr0 = r0.r0 and the state of a new solve, including what the first
+// residual replacement of k_rel_resid_df would set (the correction is still
+// zero, so that replacement is this kernel's own result): the stopping
+// norm, rho = r.z (PC: z = invd r; not FLEX, whose preconditioner kernel
+// forms rho) and the replacement bookkeeping.  The operands of
+// k_rel_resid_df, with hkhi / hklo / dghi / dglo / scale / r32 / invd32 of
+// `a` used; same tiling.
+template <int FORM, bool PC, bool FLEX>
 __global__ void __launch_bounds__(BX* BY)
     k_residual_df(Geo g, int zc, DfResArgs a, const float* __restrict__ xhi,
                   const float* __restrict__ xlo, const float* __restrict__ bhi,
@@ -994,7 +1054,7 @@ __global__ void __launch_bounds__(BX* BY)
                   float* __restrict__ r0lo, double* partials, CgState* st) {
   const int nty = (g.ny + BX - 1) / BX, ntx = (g.nx + BY - 1) / BY;
   const int ntiles = nty * ntx * ((g.nz + zc - 1) / zc);
-  double a_rr = 0.0;
+  double a_rr = 0.0, a_rz = 0.0;
   __shared__ float svh[BY + 2][BX + 2], svl[BY + 2][BX + 2];
   const DF scale{a.scale_hi, a.scale_lo};
   const int tx = threadIdx.x, ty = threadIdx.y, tf = ty * BX + tx;
@@ -1029,7 +1089,7 @@ __global__ void __launch_bounds__(BX* BY)
       vc = xv(i, j, k0);
       vm = xv(i, j, k0 - 1);
     }
-    float t_rr = 0.f;
+    float t_rr = 0.f, t_rz = 0.f;
     for (int k = k0; k <= k1; ++k) {
       DF vp{0.f, 0.f}, hv{0.f, 0.f};
       if (active) vp = xv(i, j, k + 1);
@@ -1061,23 +1121,46 @@ __global__ void __launch_bounds__(BX* BY)
         const DF rv = df_sub(DF{bhi[c], blo[c]}, av);
         r0hi[c] = rv.hi;
         r0lo[c] = rv.lo;
-        t_rr += rv.hi * rv.hi;
+        const float rf = rv.hi;
+        a.r32[c] = rf;
+        t_rr += rf * rf;
+        if (!FLEX) {
+          const float zf = PC ? a.invd32[c] * rf : rf;
+          t_rz += rf * zf;
+        }
       }
       vm = vc;
       vc = vp;
     }
     __syncthreads();  // the next tile reuses the plane tile
     a_rr += (double)t_rr;
+    a_rz += (double)t_rz;
   }
-  double v[1] = {a_rr}, tot[1];
-  if (grid_reduce<1>(v, partials, &st->counter[2], tot)) {
+  double v[2] = {a_rr, a_rz}, tot[2];
+  if (grid_reduce<2>(v, partials, &st->counter[2], tot)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-      st->rr = tot[0];
-      st->rr0 = tot[0];
-      st->rho = tot[0];
+      const double rr = tot[0];
+      // ||r|| / ||r0|| = 1 (0 for a zero residual; the non-finite value itself)
+      const double rms = !isfinite(rr) ? rr : (rr > 0.0 ? 1.0 : 0.0);
+      st->rr0 = rr;
       st->iter = 0;
-      st->rms = 1.0;
-      st->done = (st->stop_rule == SBM_STOP_REL_RES && tot[0] == 0.0) ? 1 : 0;
+      st->rms = rms;
+      st->n_reliable = 1;
+      st->done = 0;
+      if (!isfinite(rr)) st->done = 3;
+      else if (!(rms > st->tol)) st->done = 1;
+      else if (st->max_it <= 0) st->done = 2;
+      st->aux[0] = rr;
+      st->aux[1] = 0.0;  // the learned preconditioner's coarse residual is stale
+      st->rho = FLEX ? rr : tot[1];
+      if (!FLEX) {
+        st->beta = 0.0;
+        st->initial = 0;
+      }
+      st->rr = rr;
+      st->maxrr = rr;
+      st->reliable = 0;
+      st->accum_pending = 1;
     }
   }
 }
@@ -1089,40 +1172,60 @@ __global__ void k_finish(Geo g, Geo g32, int zc, double* __restrict__ x,
                          const float* __restrict__ x32) {
   SBM_COLUMN_PROLOGUE(g, zc)
   if (!active) return;
+#pragma unroll 2
   for (int k = k0; k <= k1; ++k) {
     const int64_t c = g.ix(i, j, k), c3 = g32.ix(i, j, k);
-    // d + x32 in double-float on the FP32 pipe, then two FP64 additions
+    // d + x32 in double-float on the FP32 pipe, widened to FP64 with integer
+    // instructions, then two FP64 additions
     const DF d = df_add_f(DF{dhi[c3], dlo[c3]}, x32[c3]);
-    x[c] = (x[c] + (double)d.hi) + (double)d.lo;
+    x[c] = (x[c] + f2d_int(d.hi)) + f2d_int(d.lo);
   }
 }
 
 // a32 = (float) a over the padded domain, FP64 layout -> FP32 layout, with
 // the low part a - a32 in alo when given (and the same for b).
-// One thread per padded element: x over i, grid y / z over j / k (launch
-// with to32_grid).
-__global__ void k_to32(Geo g64, Geo g32, const double* __restrict__ a, float* __restrict__ a32,
-                       const double* __restrict__ b, float* __restrict__ b32,
-                       float* __restrict__ alo = nullptr, float* __restrict__ blo = nullptr) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-  if (i > g64.ny + 1) return;
-  {
-    const int64_t c = g64.ix(i, j, k);
-    const int64_t c3 = g32.ix(i, j, k);
+// A block of 64 x 2 threads takes two padded rows (j, k): each thread
+// walks its row with stride 64, several independent loads in flight
+// (launch with to32_grid / kTo32Block).
+constexpr int kTo32Row = 64;
+const dim3 kTo32Block(kTo32Row, 2);
+__global__ void __launch_bounds__(2 * kTo32Row)
+    k_to32(Geo g64, Geo g32, const double* __restrict__ a, float* __restrict__ a32,
+           const double* __restrict__ b, float* __restrict__ b32, float* __restrict__ alo = nullptr,
+           float* __restrict__ blo = nullptr) {
+  const int j = 2 * blockIdx.x + threadIdx.y, k = blockIdx.y;
+  if (j > g64.nx + 1) return;
+  const int64_t c0 = g64.ix(0, j, k), c30 = g32.ix(0, j, k);
+  const int n = g64.ny + 2;
+#pragma unroll 4
+  for (int i = threadIdx.x; i < n; i += kTo32Row) {
+    const int64_t c = c0 + i, c3 = c30 + i;
     float h, l;
-    df_split(a[c], &h, &l);
+    df_split_int(a[c], &h, &l);
     a32[c3] = h;
     if (alo) alo[c3] = l;
     if (b) {
-      df_split(b[c], &h, &l);
+      df_split_int(b[c], &h, &l);
       b32[c3] = h;
       if (blo) blo[c3] = l;
     }
   }
 }
 
+// hi + lo splits of n FP64 values (sbm_split_f64), grid-stride.
+__global__ void k_split_f64(int64_t n, const double* __restrict__ x, float* __restrict__ hi,
+                            float* __restrict__ lo) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    float h, l;
+    df_split_int(x[t], &h, &l);
+    hi[t] = h;
+    lo[t] = l;
+  }
+}
+
 dim3 to32_grid(const Geo& g) {
-  return dim3((unsigned)((g.ny + 2 + 127) / 128), (unsigned)(g.nx + 2), (unsigned)(g.nz + 2));
+  return dim3((unsigned)((g.nx + 2 + 1) / 2), (unsigned)(g.nz + 2));
 }
 
 int flat_blocks(int64_t items) {
@@ -1150,7 +1253,7 @@ void tma_launch_fcg(const TmaPlan& plan, bool fwd, const OpArgs<float>& op, floa
 int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cudaGraph_t* graph_out,
                 int* nodes_out) {
   if (sp.stop_rule != SBM_STOP_REL_RES) return SBM_ERR_ARG;
-  if (ctx->g.nx + 2 > 65535 || ctx->g.nz + 2 > 65535) return SBM_ERR_ARG;  // to32_grid
+  if (ctx->g.nz + 2 > 65535) return SBM_ERR_ARG;  // to32_grid
   int rc = ensure_fp32_work(ctx);
   if (rc) return rc;
   const Geo& g = ctx->g;
@@ -1193,14 +1296,16 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   h->initial = 1;
   SBM_CUDA_TRY(cudaEventRecord(ctx->ev0, s));
   SBM_CUDA_TRY(cudaMemcpyAsync(ctx->st, h, sizeof(CgState), cudaMemcpyHostToDevice, s));
-  SBM_CUDA_TRY(cudaMemsetAsync(ctx->x32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->p32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->rold32, 0, sizeof(float) * g32.nh, s));
   // FP32 coefficients and, for the double-float replacement, their low parts
-  k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
-                                         dg32, ctx->hklo32 + kOff32, ctx->dglo32 + kOff32);
+  k_to32<<<to32_grid(g), kTo32Block, 0, s>>>(g, g32, sp.hk64, hk32,
+                                              sp.form ? sp.diag64 : nullptr, dg32,
+                                              ctx->hklo32 + kOff32, ctx->dglo32 + kOff32);
   SBM_LAUNCHED(1);
-  if (pc || learned) {
+  // the Jacobi weight: Jacobi-PCG and the learned preconditioner's additive
+  // form read it (the multiplicative form forms it from hk itself)
+  if (pc || (learned && ctx->pc_additive)) {
     k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
     SBM_LAUNCHED(1);
   }
@@ -1243,23 +1348,30 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   dfa.bcx0 = sp.bcx0;
   dfa.bcx1 = sp.bcx1;
   // r0 = b - A x0 with x0's stored ghosts, in double-float from the hi + lo
-  // splits of x0 and b (held meanwhile in q32 / r32 and in the correction's
-  // arrays, which are cleared after it); sets rr0
-  k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, sp.x, q32, sp.rhs, ctx->dhi32 + kOff32, r32,
-                                         ctx->dlo32 + kOff32);
-  if (sp.form == 0)
-    k_residual_df<0><<<rgrid, sh64.block, 0, s>>>(g32, sh64.zc, dfa, q32, r32,
-                                                   ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,
-                                                   ctx->r0hi32 + kOff32, ctx->r0lo32 + kOff32,
-                                                   ctx->partials, ctx->st);
-  else
-    k_residual_df<1><<<rgrid, sh64.block, 0, s>>>(g32, sh64.zc, dfa, q32, r32,
-                                                   ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,
-                                                   ctx->r0hi32 + kOff32, ctx->r0lo32 + kOff32,
-                                                   ctx->partials, ctx->st);
+  // splits of x0 (held meanwhile in q32 / x32) and b (in the correction's
+  // arrays); x32 and the correction are cleared after it.  The initial
+  // residual is also the first residual replacement: it writes r32 = r0's
+  // high part (r32 is none of its inputs) and sets the stopping norm and rho.
+  k_to32<<<to32_grid(g), kTo32Block, 0, s>>>(g, g32, sp.x, q32, sp.rhs, ctx->dhi32 + kOff32,
+                                              x32, ctx->dlo32 + kOff32);
+#define SBM_RES0(F, P, X)                                                                     \
+  k_residual_df<F, P, X><<<rgrid, sh64.block, 0, s>>>(                                      \
+      g32, sh64.zc, dfa, q32, x32, ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,                 \
+      ctx->r0hi32 + kOff32, ctx->r0lo32 + kOff32, ctx->partials, ctx->st)
+  if (sp.form == 0) {
+    if (learned) SBM_RES0(0, false, true);
+    else if (pc) SBM_RES0(0, true, false);
+    else SBM_RES0(0, false, false);
+  } else {
+    if (learned) SBM_RES0(1, false, true);
+    else if (pc) SBM_RES0(1, true, false);
+    else SBM_RES0(1, false, false);
+  }
+#undef SBM_RES0
   SBM_LAUNCHED(2);
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->dhi32, 0, sizeof(float) * g32.nh, s));
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->dlo32, 0, sizeof(float) * g32.nh, s));
+  SBM_CUDA_TRY(cudaMemsetAsync(ctx->x32, 0, sizeof(float) * g32.nh, s));
   const int64_t items = (int64_t)nchunk * g.nx * g.nz;
   const dim3 fgrid(flat_blocks(items));
   const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
@@ -1334,10 +1446,8 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
     iter(s2, pbuf[0], pbuf[1]);
     iter(s2, pbuf[1], pbuf[0]);
   };
-  // first residual replacement: r32 = r0, rho, beta = 0 (p32 = 0 so the
-  // first p_new = z)
-  rel(s);
-  SBM_LAUNCHED(1);
+  // (the first residual replacement -- r32 = r0, rho, beta = 0, with p32 = 0
+  // so that the first p_new = z -- was made by k_residual_df)
   SBM_CUDA_TRY(cudaGetLastError());
   // bodies of 2 iterations per captured chunk: the flexible CG converges in
   // ~10x fewer iterations, so shorter chunks trim the no-op tail (256^3,
@@ -1390,7 +1500,7 @@ int mixed_end(sbm_ctx* ctx, const SolveSpec& sp, const CgState& fin, SolveResult
 // against an independent restatement.
 int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double* z) {
   if (!net_pc_usable(ctx, sp.form) || ctx->g.ny % 4) return SBM_ERR_STATE;
-  if (ctx->g.nx + 2 > 65535 || ctx->g.nz + 2 > 65535) return SBM_ERR_ARG;  // to32_grid
+  if (ctx->g.nz + 2 > 65535) return SBM_ERR_ARG;  // to32_grid
   int rc = ensure_fp32_work(ctx);
   if (rc) return rc;
   const Geo& g = ctx->g;
@@ -1404,15 +1514,15 @@ int learned_pc_apply(sbm_ctx* ctx, const SolveSpec& sp, const double* r, double*
   OpArgs<float> op32{g32, hk32, sp.form ? dg32 : nullptr, (float)sp.scale, sp.form, sp.bcx0,
                      sp.bcx1};
   const Shape sh32 = stencil_shape(g32, pick_zc(g32, ctx->zc32));
-  k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, sp.hk64, hk32, sp.form ? sp.diag64 : nullptr,
-                                         dg32);
+  k_to32<<<to32_grid(g), kTo32Block, 0, s>>>(g, g32, sp.hk64, hk32,
+                                              sp.form ? sp.diag64 : nullptr, dg32);
   k_invdiag<float><<<sh32.grid, sh32.block, 0, s>>>(op32, sh32.zc, iv32);
   SBM_LAUNCHED(2);
   if ((rc = net_pc_begin(ctx, hk32, sp.form ? dg32 : nullptr, r32, q32, sp.scale, sp.bcx0,
                          sp.bcx1, s)))
     return rc;
   SBM_CUDA_TRY(cudaMemcpyAsync(ctx->r64, r, sizeof(double) * g.nh, cudaMemcpyHostToDevice, s));
-  k_to32<<<to32_grid(g), 128, 0, s>>>(g, g32, ctx->r64, r32, nullptr, nullptr);
+  k_to32<<<to32_grid(g), kTo32Block, 0, s>>>(g, g32, ctx->r64, r32, nullptr, nullptr);
   SBM_LAUNCHED(1);
   SBM_CUDA_TRY(cudaMemsetAsync(ctx->q32, 0, sizeof(float) * g32.nh, s));
   CgState* h = &ctx->h_st[2];
@@ -1444,7 +1554,7 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   int rc = mixed_begin(ctx, sp, &ex, &graph, &nodes);
   if (rc) return rc;
   CgState fin;
-  rc = run_chunks(ctx, ex, nodes, ctx->st, ctx->h_st, &fin);
+  rc = run_loop(ctx, graph, nodes, sp.max_it, ctx->st, ctx->h_st, &fin);
   if (rc) return rc;
   return mixed_end(ctx, sp, fin, out);
 }
@@ -1589,6 +1699,11 @@ int solve(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
 }
 
 void release_graphs(sbm_ctx* ctx) {
+  for (auto& kv : ctx->loops) {
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  ctx->loops.clear();
   for (auto& kv : ctx->graphs) {
     cudaGraphExecDestroy(kv.second.exec);
     cudaGraphDestroy(kv.second.graph);
@@ -1599,3 +1714,13 @@ void release_graphs(sbm_ctx* ctx) {
 int status_of_done(int done) { return status_of(done); }
 
 }  // namespace sbm
+
+extern "C" int sbm_split_f64(int64_t n, const double* x, float* hi, float* lo, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !hi || !lo))) return SBM_ERR_ARG;
+  if (n == 0) return SBM_OK;
+  const int64_t b = std::min<int64_t>((n + 255) / 256, 152 * 16);
+  sbm::k_split_f64<<<(unsigned)b, 256, 0, static_cast<cudaStream_t>(stream)>>>(n, x, hi, lo);
+  SBM_LAUNCHED(1);
+  SBM_CUDA_TRY(cudaGetLastError());
+  return SBM_OK;
+}

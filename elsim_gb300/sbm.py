@@ -166,6 +166,7 @@ def load_library(path: os.PathLike | None = None) -> C.CDLL:
         "sbm_redist_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
         "sbm_set_wait_limit": (C.c_int, [C.c_int]),
+        "sbm_split_f64": (C.c_int, [i64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
         "sbm_rm_mask": (C.c_int, [i64, dp, dp, dp]),
         "sbm_sign": (C.c_int, [i64, dp, C.c_double, dp]),
         "sbm_net_param_count": (i64, []),

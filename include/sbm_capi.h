@@ -505,6 +505,15 @@ int sbm_learned_pc_apply_op(sbm_ctx* ctx, int op, int bc_x0, int bc_x1, double s
  * it only while no solve runs. */
 int sbm_set_wait_limit(int tries);
 
+/* Double-float split (no counterpart in the reference): hi[i] = (float)x[i]
+ * and lo[i] = (float)(x[i] - hi[i]) for n FP64 values, the hi + lo pairs
+ * (about 48 significant bits) in which the mixed-precision solver carries
+ * the operator, the initial iterate and the right-hand side.  Computed with
+ * integer instructions, bit-identical to those FP64 expressions.  DEVICE
+ * pointers; enqueued on `stream` (a cudaStream_t; NULL = the default
+ * stream), asynchronous. */
+int sbm_split_f64(int64_t n, const double* x, float* hi, float* lo, void* stream);
+
 /* Version string of the compiled library. */
 const char* sbm_version(void);
 /* Number of kernel launches this process has issued through the library. */
