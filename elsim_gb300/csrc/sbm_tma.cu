@@ -443,6 +443,18 @@ int auto_zct(int ntile, int nz, int pc, int form, bool flex) {
   const int per_sm = dir_blocks_per_sm(pc, form, flex, smem_bytes(pc, form));
   if (per_sm < 1) return ZCT;
   const int64_t cap = (int64_t)nsm * per_sm;
+  // One wave when the columns allow it: the most z chunks whose CTAs are all
+  // resident at once (a partly filled last wave runs at a fraction of the
+  // bandwidth; 256^3 flexible-CG direction kernel: 0.0978 ms with 5 chunks
+  // of 52 planes, one wave of 640 CTAs, against 0.1047 ms with 11 chunks of
+  // 24 in 1.85 waves, 0.111 / 0.115 ms with 16 / 32 planes).  At least 8
+  // planes per CTA, so that the two halo planes stay a small part of it.
+  const int64_t chunks = cap / ntile;
+  if (chunks >= 1) {
+    int z = (int)((nz + chunks - 1) / chunks);
+    if (flex) z = (z + 3) / 4 * 4;
+    return z >= 8 ? z : 8;
+  }
   int best = ZCT;
   int64_t best_cost = -1;
   for (int z = 8; z <= 32; z += flex ? 4 : 1) {
