@@ -285,6 +285,42 @@ __device__ __forceinline__ DF df_mul(DF x, DF y) {
   e = __fmaf_rn(x.lo, y.hi, e);
   return df_fast_two_sum(p, e);
 }
+// The same operations on pairs of FP32 lanes (paired add / multiply /
+// FMA), one double-float value per lane, each lane bit-identical to the
+// scalar forms above.
+struct DF2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ float2 f2_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ DF2 df2_two_sum(float2 a, float2 b) {
+  const float2 s = __fadd2_rn(a, b);
+  const float2 bb = __fadd2_rn(s, f2_neg(a));
+  return {s, __fadd2_rn(__fadd2_rn(a, f2_neg(__fadd2_rn(s, f2_neg(bb)))),
+                        __fadd2_rn(b, f2_neg(bb)))};
+}
+__device__ __forceinline__ DF2 df2_fast_two_sum(float2 a, float2 b) {
+  const float2 s = __fadd2_rn(a, b);
+  return {s, __fadd2_rn(b, f2_neg(__fadd2_rn(s, f2_neg(a))))};
+}
+__device__ __forceinline__ DF2 df2_add(DF2 x, DF2 y) {
+  const DF2 s = df2_two_sum(x.hi, y.hi);
+  return df2_fast_two_sum(s.hi, __fadd2_rn(s.lo, __fadd2_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ DF2 df2_sub(DF2 x, DF2 y) {
+  return df2_add(x, DF2{f2_neg(y.hi), f2_neg(y.lo)});
+}
+__device__ __forceinline__ DF2 df2_add_f(DF2 x, float2 y) {
+  const DF2 s = df2_two_sum(x.hi, y);
+  return df2_fast_two_sum(s.hi, __fadd2_rn(s.lo, x.lo));
+}
+__device__ __forceinline__ DF2 df2_mul(DF2 x, DF2 y) {
+  const float2 p = __fmul2_rn(x.hi, y.hi);
+  float2 e = __ffma2_rn(x.hi, y.hi, f2_neg(p));
+  e = __ffma2_rn(x.hi, y.lo, e);
+  e = __ffma2_rn(x.lo, y.hi, e);
+  return df2_fast_two_sum(p, e);
+}
+
 // hi + lo split of an FP64 value (lo exact to FP32 rounding)
 __host__ __device__ __forceinline__ void df_split(double v, float* hi, float* lo) {
   const float h = (float)v;

@@ -914,6 +914,58 @@ struct DfResArgs {
   int bcx0, bcx1;
 };
 
+// Last-block bookkeeping of a residual replacement (tot = r.r, r.z): the
+// stopping norm ||r|| / ||r0||, beta and rho (not FLEX, whose
+// preconditioner kernel forms them), the replacement counters.
+template <bool FLEX>
+__device__ void df_rel_close(CgState* st, const double (&tot)[2]) {
+  const double rms = (st->rr0 > 0.0) ? sqrt(tot[0] / st->rr0) : 0.0;
+  st->rms = rms;
+  st->n_reliable += 1;
+  if (!isfinite(rms)) st->done = 3;
+  else if (!(rms > st->tol)) st->done = 1;
+  else if (st->iter >= st->max_it) st->done = 2;
+  st->aux[1] = 0.0;  // the coarse residual of the learned preconditioner is stale
+  if (!FLEX) {
+    st->beta = tot[1] / st->rho;
+    st->rho = tot[1];
+  }
+  st->rr = tot[0];
+  st->maxrr = tot[0];
+  st->reliable = 0;
+  st->accum_pending = 1;
+}
+
+// Last-block state of a new solve after its initial residual (tot = r0.r0,
+// r0.z0), which is also the solve's first residual replacement (the
+// correction is still zero): rr0, the stopping norm (1, or 0 for a zero
+// residual, or the non-finite value itself), rho and beta = 0 (not FLEX)
+// and the replacement bookkeeping.
+template <bool FLEX>
+__device__ void df_init_close(CgState* st, const double (&tot)[2]) {
+  const double rr = tot[0];
+  const double rms = !isfinite(rr) ? rr : (rr > 0.0 ? 1.0 : 0.0);
+  st->rr0 = rr;
+  st->iter = 0;
+  st->rms = rms;
+  st->n_reliable = 1;
+  st->done = 0;
+  if (!isfinite(rr)) st->done = 3;
+  else if (!(rms > st->tol)) st->done = 1;
+  else if (st->max_it <= 0) st->done = 2;
+  st->aux[0] = rr;
+  st->aux[1] = 0.0;  // the learned preconditioner's coarse residual is stale
+  st->rho = FLEX ? rr : tot[1];
+  if (!FLEX) {
+    st->beta = 0.0;
+    st->initial = 0;
+  }
+  st->rr = rr;
+  st->maxrr = rr;
+  st->reliable = 0;
+  st->accum_pending = 1;
+}
+
 // Reliable update in double-float arithmetic: r = r0 - A (d + x32) with
 // every operand carried as an FP32 pair (about 48 significant bits, ample
 // for residuals down to 1e-8 of r0 at 256^3), r32 = the high part, z =
@@ -1013,25 +1065,8 @@ __global__ void __launch_bounds__(BX* BY)
     a_rz += (double)t_rz;
   }
   double v[2] = {a_rr, a_rz}, tot[2];
-  if (grid_reduce<2>(v, partials, &st->counter[3], tot)) {
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-      const double rms = (st->rr0 > 0.0) ? sqrt(tot[0] / st->rr0) : 0.0;
-      st->rms = rms;
-      st->n_reliable += 1;
-      if (!isfinite(rms)) st->done = 3;
-      else if (!(rms > st->tol)) st->done = 1;
-      else if (st->iter >= st->max_it) st->done = 2;
-      st->aux[1] = 0.0;  // the coarse residual of the learned preconditioner is stale
-      if (!FLEX) {
-        st->beta = tot[1] / st->rho;
-        st->rho = tot[1];
-      }
-      st->rr = tot[0];
-      st->maxrr = tot[0];
-      st->reliable = 0;
-      st->accum_pending = 1;
-    }
-  }
+  if (grid_reduce<2>(v, partials, &st->counter[3], tot))
+    if (threadIdx.x == 0 && threadIdx.y == 0) df_rel_close<FLEX>(st, tot);
 }
 
 // Initial residual of the mixed solve in double-float arithmetic:
@@ -1137,32 +1172,217 @@ __global__ void __launch_bounds__(BX* BY)
     a_rz += (double)t_rz;
   }
   double v[2] = {a_rr, a_rz}, tot[2];
-  if (grid_reduce<2>(v, partials, &st->counter[2], tot)) {
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-      const double rr = tot[0];
-      // ||r|| / ||r0|| = 1 (0 for a zero residual; the non-finite value itself)
-      const double rms = !isfinite(rr) ? rr : (rr > 0.0 ? 1.0 : 0.0);
-      st->rr0 = rr;
-      st->iter = 0;
-      st->rms = rms;
-      st->n_reliable = 1;
-      st->done = 0;
-      if (!isfinite(rr)) st->done = 3;
-      else if (!(rms > st->tol)) st->done = 1;
-      else if (st->max_it <= 0) st->done = 2;
-      st->aux[0] = rr;
-      st->aux[1] = 0.0;  // the learned preconditioner's coarse residual is stale
-      st->rho = FLEX ? rr : tot[1];
-      if (!FLEX) {
-        st->beta = 0.0;
-        st->initial = 0;
-      }
-      st->rr = rr;
-      st->maxrr = rr;
-      st->reliable = 0;
-      st->accum_pending = 1;
-    }
+  if (grid_reduce<2>(v, partials, &st->counter[2], tot))
+    if (threadIdx.x == 0 && threadIdx.y == 0) df_init_close<FLEX>(st, tot);
+}
+
+// The double-float residuals for grids whose y extent is a multiple of 4:
+// INIT the initial residual of k_residual_df (from the splits of x0 and b,
+// x0's ghosts read as data; also writes r0hi / r0lo and sets the state of
+// the first replacement), else the replacement of k_rel_resid_df
+// (V = d + x32 with the ghost rules of the correction).  Tiles of 64 (y) x
+// 8 (x) cells x zc planes walked grid-stride by 128-thread blocks; each
+// thread takes four y-consecutive cells (float4 loads of V, hk, the
+// right-hand side) and runs the double-float arithmetic on pairs of FP32
+// lanes: r (and r0) bit-identical to the one-cell kernels' (the same
+// operations per cell), the norms summed in another order.  V of the
+// plane's x / y neighbours comes from a shared-memory tile
+// (12 lanes of every warp load its halo), V of the z neighbours rolls in
+// registers, hk comes from global memory (L1 / L2).
+constexpr int kDfTX = 64, kDfTY = 8, kDfThreads = kDfTX / 4 * kDfTY;
+template <int FORM, bool PC, bool FLEX, bool INIT>
+__global__ void __launch_bounds__(kDfThreads, 4)
+    k_df_res4(Geo g, int zc, DfResArgs a, const float* __restrict__ xhi,
+              const float* __restrict__ xlo, const float* __restrict__ bhi,
+              const float* __restrict__ blo, float* __restrict__ r0hi, float* __restrict__ r0lo,
+              double* partials, CgState* st) {
+  if (!INIT) {
+    pdl_begin();
+    if (!st->reliable || st->done) return;
   }
+  constexpr int Q = kDfTX / 4;  // float4 columns of the tile (16)
+  constexpr int RF4 = Q + 2;    // with the y halo columns
+  __shared__ float4 svh[kDfTY + 2][RF4], svl[kDfTY + 2][RF4];
+  const int tid = threadIdx.x;
+  const int q4 = tid % Q, row = tid / Q;
+  const int nty = (g.ny + kDfTX - 1) / kDfTX, ntx = (g.nx + kDfTY - 1) / kDfTY;
+  const int ntiles = nty * ntx * ((g.nz + zc - 1) / zc);
+  // this thread's halo float4 (12 lanes of each warp): rows 0 / TY+1 at
+  // columns 1..Q (the x neighbours of the tile's edge rows), columns 0 /
+  // RF4-1 at rows 1..TY (the y neighbours of the row ends)
+  constexpr int NH = 2 * Q + 2 * kDfTY;
+  constexpr int HPW = NH / (kDfThreads / 32);
+  const int hh = (tid & 31) < HPW ? (tid >> 5) * HPW + (tid & 31) : NH;
+  int hrow = -1, hcol = -1;
+  if (hh < 2 * Q) {
+    hrow = hh < Q ? 0 : kDfTY + 1;
+    hcol = hh % Q + 1;
+  } else if (hh < NH) {
+    const int u = hh - 2 * Q;
+    hrow = u % kDfTY + 1;
+    hcol = u < kDfTY ? 0 : RF4 - 1;
+  }
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto lo2 = [](float4 v) { return make_float2(v.x, v.y); };
+  auto hi2 = [](float4 v) { return make_float2(v.z, v.w); };
+  // V (x0, or the correction d + x32) of the float4 starting at c
+  auto vat = [&](int64_t c, float4& vh, float4& vl) {
+    if (INIT) {
+      vh = *reinterpret_cast<const float4*>(xhi + c);
+      vl = *reinterpret_cast<const float4*>(xlo + c);
+    } else {
+      const float4 dh = *reinterpret_cast<const float4*>(a.dhi + c);
+      const float4 dl = *reinterpret_cast<const float4*>(a.dlo + c);
+      const float4 xx = *reinterpret_cast<const float4*>(a.x32 + c);
+      const DF2 p0 = df2_add_f(DF2{lo2(dh), lo2(dl)}, lo2(xx));
+      const DF2 p1 = df2_add_f(DF2{hi2(dh), hi2(dl)}, hi2(xx));
+      vh = make_float4(p0.hi.x, p0.hi.y, p1.hi.x, p1.hi.y);
+      vl = make_float4(p0.lo.x, p0.lo.y, p1.lo.x, p1.lo.y);
+    }
+  };
+  auto hk2 = [&](int64_t c, float2* h0, float2* h1) {  // hk pairs (cells 0-1, 2-3) at c
+    const float4 h = *reinterpret_cast<const float4*>(a.hkhi + c);
+    const float4 l = *reinterpret_cast<const float4*>(a.hklo + c);
+    h0[0] = lo2(h);
+    h0[1] = lo2(l);
+    h1[0] = hi2(h);
+    h1[1] = hi2(l);
+  };
+  const DF2 scale2{make_float2(a.scale_hi, a.scale_hi), make_float2(a.scale_lo, a.scale_lo)};
+  double a_rr = 0.0, a_rz = 0.0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tyb = t % nty, txb = (t / nty) % ntx, tzb = t / (nty * ntx);
+    const int i0 = kDfTX * tyb + 4 * q4 + 1, j = kDfTY * txb + row + 1;
+    const int k0 = tzb * zc + 1, k1 = min(k0 + zc - 1, g.nz);
+    // the own float4 lies in the padded layout (rows end at ny + 4), and
+    // its cells are interior
+    const bool inrow = i0 <= g.ny + 1 && j <= g.nx + 1;
+    const bool active = i0 <= g.ny && j <= g.nx;
+    const int hi_i = kDfTX * tyb + 4 * (hcol - 1) + 1, hj = kDfTY * txb + hrow;
+    const bool hload = hrow >= 0 && hi_i <= g.ny + 1 && hj <= g.nx + 1;
+    float4 vch = z4, vcl = z4, vmh = z4, vml = z4;
+    if (inrow) {
+      vat(g.ix(i0, j, k0), vch, vcl);
+      vat(g.ix(i0, j, k0 - 1), vmh, vml);
+    }
+    float2 t_rr = make_float2(0.f, 0.f), t_rz = t_rr;
+    for (int k = k0; k <= k1; ++k) {
+      const int64_t c = g.ix(i0, j, k);
+      float4 vph = z4, vpl = z4, hvh = z4, hvl = z4;
+      if (inrow) vat(c + g.sz, vph, vpl);
+      if (hload) vat(g.ix(hi_i, hj, k), hvh, hvl);
+      __syncthreads();  // the previous plane's readers are done
+      svh[row + 1][q4 + 1] = vch;
+      svl[row + 1][q4 + 1] = vcl;
+      if (hrow >= 0) {
+        svh[hrow][hcol] = hvh;
+        svl[hrow][hcol] = hvl;
+      }
+      __syncthreads();
+      if (active) {
+        // neighbours of V: y from the tile row, x from the rows beside, z in
+        // registers; INIT reads x0's ghosts as data, otherwise the ghost
+        // rules of the correction apply
+        float ylh = svh[row + 1][q4].w, yll = svl[row + 1][q4].w;
+        float yrh = svh[row + 1][q4 + 2].x, yrl = svl[row + 1][q4 + 2].x;
+        float4 xmh = svh[row][q4 + 1], xml = svl[row][q4 + 1];
+        float4 xph = svh[row + 2][q4 + 1], xpl = svl[row + 2][q4 + 1];
+        float4 zmh = vmh, zml = vml, zph = vph, zpl = vpl;
+        if (!INIT) {
+          if (i0 == 1) {
+            ylh = vch.x;
+            yll = vcl.x;
+          }
+          if (i0 + 3 == g.ny) {
+            yrh = vch.w;
+            yrl = vcl.w;
+          }
+          if (j == 1) {
+            xmh = a.bcx0 ? z4 : vch;
+            xml = a.bcx0 ? z4 : vcl;
+          }
+          if (j == g.nx) {
+            xph = a.bcx1 ? z4 : vch;
+            xpl = a.bcx1 ? z4 : vcl;
+          }
+          if (k == 1) {
+            zmh = vch;
+            zml = vcl;
+          }
+          if (k == g.nz) {
+            zph = vch;
+            zpl = vcl;
+          }
+        }
+        const DF2 vc0{lo2(vch), lo2(vcl)}, vc1{hi2(vch), hi2(vcl)};
+        float2 kc0[2], kc1[2], n0[2], n1[2];
+        hk2(c, kc0, kc1);
+        const DF2 k0v{kc0[0], kc0[1]}, k1v{kc1[0], kc1[1]};
+        // S(V) = sum_f (hk_nb + hk_c) (V_nb - V_c), faces y+, y-, x+, x-, z+, z-
+        const float klh = a.hkhi[c - 1], kll = a.hklo[c - 1];
+        const float krh = a.hkhi[c + 4], krl = a.hklo[c + 4];
+        DF2 s0 = df2_mul(df2_add(DF2{make_float2(kc0[0].y, kc1[0].x), make_float2(kc0[1].y, kc1[1].x)}, k0v),
+                         df2_sub(DF2{make_float2(vch.y, vch.z), make_float2(vcl.y, vcl.z)}, vc0));
+        DF2 s1 = df2_mul(df2_add(DF2{make_float2(kc1[0].y, krh), make_float2(kc1[1].y, krl)}, k1v),
+                         df2_sub(DF2{make_float2(vch.w, yrh), make_float2(vcl.w, yrl)}, vc1));
+        s0 = df2_add(s0, df2_mul(df2_add(DF2{make_float2(klh, kc0[0].x), make_float2(kll, kc0[1].x)}, k0v),
+                                 df2_sub(DF2{make_float2(ylh, vch.x), make_float2(yll, vcl.x)}, vc0)));
+        s1 = df2_add(s1, df2_mul(df2_add(DF2{make_float2(kc0[0].y, kc1[0].x), make_float2(kc0[1].y, kc1[1].x)}, k1v),
+                                 df2_sub(DF2{make_float2(vch.y, vch.z), make_float2(vcl.y, vcl.z)}, vc1)));
+        auto face = [&](int64_t cn, float4 nh, float4 nl) {
+          hk2(cn, n0, n1);
+          s0 = df2_add(s0, df2_mul(df2_add(DF2{n0[0], n0[1]}, k0v),
+                                   df2_sub(DF2{lo2(nh), lo2(nl)}, vc0)));
+          s1 = df2_add(s1, df2_mul(df2_add(DF2{n1[0], n1[1]}, k1v),
+                                   df2_sub(DF2{hi2(nh), hi2(nl)}, vc1)));
+        };
+        face(c + g.sx, xph, xpl);
+        face(c - g.sx, xmh, xml);
+        face(c + g.sz, zph, zpl);
+        face(c - g.sz, zmh, zml);
+        DF2 av0 = df2_mul(scale2, s0), av1 = df2_mul(scale2, s1);
+        if (FORM == 1) {
+          const float4 dh = *reinterpret_cast<const float4*>(a.dghi + c);
+          const float4 dl = *reinterpret_cast<const float4*>(a.dglo + c);
+          av0 = df2_sub(df2_mul(DF2{lo2(dh), lo2(dl)}, vc0), av0);
+          av1 = df2_sub(df2_mul(DF2{hi2(dh), hi2(dl)}, vc1), av1);
+        }
+        const float* rh = INIT ? bhi : a.r0hi;
+        const float* rl = INIT ? blo : a.r0lo;
+        const float4 bh = *reinterpret_cast<const float4*>(rh + c);
+        const float4 bl = *reinterpret_cast<const float4*>(rl + c);
+        const DF2 rv0 = df2_sub(DF2{lo2(bh), lo2(bl)}, av0);
+        const DF2 rv1 = df2_sub(DF2{hi2(bh), hi2(bl)}, av1);
+        if (INIT) {
+          *reinterpret_cast<float4*>(r0hi + c) = make_float4(rv0.hi.x, rv0.hi.y, rv1.hi.x, rv1.hi.y);
+          *reinterpret_cast<float4*>(r0lo + c) = make_float4(rv0.lo.x, rv0.lo.y, rv1.lo.x, rv1.lo.y);
+        }
+        *reinterpret_cast<float4*>(a.r32 + c) = make_float4(rv0.hi.x, rv0.hi.y, rv1.hi.x, rv1.hi.y);
+        t_rr = __ffma2_rn(rv1.hi, rv1.hi, __ffma2_rn(rv0.hi, rv0.hi, t_rr));
+        if (!FLEX) {
+          float2 z0 = rv0.hi, z1 = rv1.hi;
+          if (PC) {
+            const float4 iv = *reinterpret_cast<const float4*>(a.invd32 + c);
+            z0 = __fmul2_rn(lo2(iv), z0);
+            z1 = __fmul2_rn(hi2(iv), z1);
+          }
+          t_rz = __ffma2_rn(rv1.hi, z1, __ffma2_rn(rv0.hi, z0, t_rz));
+        }
+      }
+      vmh = vch;
+      vml = vcl;
+      vch = vph;
+      vcl = vpl;
+    }
+    a_rr += (double)t_rr.x + (double)t_rr.y;
+    a_rz += (double)t_rz.x + (double)t_rz.y;
+  }
+  double v[2] = {a_rr, a_rz}, tot[2];
+  if (grid_reduce<2>(v, partials, &st->counter[INIT ? 2 : 3], tot))
+    if (threadIdx.x == 0) {
+      if (INIT) df_init_close<FLEX>(st, tot);
+      else df_rel_close<FLEX>(st, tot);
+    }
 }
 
 // x += dhi + dlo + x32 on the interior (the total correction of the mixed
@@ -1332,6 +1552,13 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   // launch of the replacement is cheap
   const int64_t rel_tiles = (int64_t)sh64.grid.x * sh64.grid.y * sh64.grid.z;
   const dim3 rgrid((unsigned)std::min<int64_t>(rel_tiles, 152 * 4));
+  // the four-cell form when rows are whole float4s: tiles of 64 x 8 cells x
+  // 16 planes, four 128-thread blocks per SM at most
+  const bool df4 = vec == 4;
+  constexpr int kDfZc = 16;
+  const int64_t df_tiles = (int64_t)((g32.ny + kDfTX - 1) / kDfTX) *
+                           ((g32.nx + kDfTY - 1) / kDfTY) * ((g32.nz + kDfZc - 1) / kDfZc);
+  const dim3 dgrid((unsigned)std::min<int64_t>(df_tiles, 152 * 4));
   DfResArgs dfa{};
   dfa.hkhi = hk32;
   dfa.hklo = ctx->hklo32 + kOff32;
@@ -1354,10 +1581,17 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   // high part (r32 is none of its inputs) and sets the stopping norm and rho.
   k_to32<<<to32_grid(g), kTo32Block, 0, s>>>(g, g32, sp.x, q32, sp.rhs, ctx->dhi32 + kOff32,
                                               x32, ctx->dlo32 + kOff32);
-#define SBM_RES0(F, P, X)                                                                     \
-  k_residual_df<F, P, X><<<rgrid, sh64.block, 0, s>>>(                                      \
-      g32, sh64.zc, dfa, q32, x32, ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,                 \
-      ctx->r0hi32 + kOff32, ctx->r0lo32 + kOff32, ctx->partials, ctx->st)
+#define SBM_RES0(F, P, X)                                                                    \
+  do {                                                                                       \
+    if (df4)                                                                                 \
+      k_df_res4<F, P, X, true><<<dgrid, kDfThreads, 0, s>>>(                                 \
+          g32, kDfZc, dfa, q32, x32, ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,               \
+          ctx->r0hi32 + kOff32, ctx->r0lo32 + kOff32, ctx->partials, ctx->st);               \
+    else                                                                                     \
+      k_residual_df<F, P, X><<<rgrid, sh64.block, 0, s>>>(                                  \
+          g32, sh64.zc, dfa, q32, x32, ctx->dhi32 + kOff32, ctx->dlo32 + kOff32,             \
+          ctx->r0hi32 + kOff32, ctx->r0lo32 + kOff32, ctx->partials, ctx->st);               \
+  } while (0)
   if (sp.form == 0) {
     if (learned) SBM_RES0(0, false, true);
     else if (pc) SBM_RES0(0, true, false);
@@ -1377,11 +1611,21 @@ int mixed_begin(sbm_ctx* ctx, const SolveSpec& sp, cudaGraphExec_t* ex_out, cuda
   const dim3 vgrid((unsigned)(((int64_t)nchunk * g.nx + 255) / 256), (g.nz + zc32 - 1) / zc32);
   float* const pbuf[2] = {p32, ctx->rold32 + kOff32};  // alternating direction buffers
   auto rel = [&](cudaStream_t s2) {
-#define SBM_REL(F, P) \
-  k_rel_resid_df<F, P><<<rgrid, sh64.block, 0, s2>>>(g32, sh64.zc, dfa, ctx->partials, ctx->st)
+    const float* nf = nullptr;
+    float* nw = nullptr;
+#define SBM_REL(F, P)                                                                          \
+  do {                                                                                         \
+    if (df4)                                                                                   \
+      k_df_res4<F, P, false, false><<<dgrid, kDfThreads, 0, s2>>>(                             \
+          g32, kDfZc, dfa, nf, nf, nf, nf, nw, nw, ctx->partials, ctx->st);                    \
+    else                                                                                       \
+      k_rel_resid_df<F, P><<<rgrid, sh64.block, 0, s2>>>(g32, sh64.zc, dfa, ctx->partials,     \
+                                                         ctx->st);                             \
+  } while (0)
     if (learned) {
-      launch_pdl(sp.form ? k_rel_resid_df<1, false, true> : k_rel_resid_df<0, false, true>, rgrid,
-                 sh64.block, 0, s2, g32, sh64.zc, dfa, ctx->partials, ctx->st);
+      launch_pdl(sp.form ? k_df_res4<1, false, true, false> : k_df_res4<0, false, true, false>,
+                 dgrid, dim3(kDfThreads), 0, s2, g32, kDfZc, dfa, nf, nf, nf, nf, nw, nw,
+                 ctx->partials, ctx->st);
     } else if (sp.form == 0) {
       if (pc) SBM_REL(0, true); else SBM_REL(0, false);
     } else {

@@ -114,8 +114,10 @@ def _distances(shape, seed):
 
 
 @pytest.mark.parametrize("precond", [sbm.PC_NONE, sbm.PC_JACOBI])
-def test_mixed_precision_matches_fp64(built, precond):
-    shape = (48, 48, 48)
+@pytest.mark.parametrize("shape", [(48, 48, 48), (44, 30, 21), (42, 36, 40)])
+def test_mixed_precision_matches_fp64(built, precond, shape):
+    # y extents a multiple of 4 (the four-cell double-float residual
+    # kernels; 44 x 30: partial tiles in y and x) and not (the one-cell ones)
     m, prob = _problem(shape, 13, tunnel=True)
     xo, io = orc.cg(prob["coef"], prob["rhs"], prob["x"], 1.0, sbm.BC_ZERO, sbm.BC_ZERO,
                     sbm.STOP_REL_RES, 1e-12, 50000)
