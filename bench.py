@@ -1050,7 +1050,10 @@ def run_step128(args):
 
 def run_profile(args):
     """The production solve alone (no FP64 baseline, no CPU leg), `steps`
-    times after `warmup` solves: the command the ncu summaries profile."""
+    times after `warmup` solves: the command the ncu summaries profile.  Its
+    iteration chunks are driven from the host (the same kernels): ncu does
+    not profile kernels inside the conditional graph that loops them on the
+    device."""
     import __graft_entry__
     __graft_entry__.build()
     from elsim_gb300 import sbm, synth
@@ -1061,6 +1064,7 @@ def run_profile(args):
     with sbm.Context(n, n, n) as ctx:
         for k in ("coef", "x", "rhs", "weight"):
             ctx.upload(k, prob[k])
+        ctx.set_tuning(host_loop=True)
         if pc == sbm.PC_LEARNED:
             from elsim_gb300 import learned
             net = learned.load()

@@ -227,7 +227,8 @@ int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p) {
 
 int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta, int flags) {
   if (!ctx || zc64 < 0 || zc32 < 0 || chunk < 0 || zc64 > 64 || zc32 > 64 || chunk > 1024 ||
-      !(delta >= 0.0 && delta < 1.0) || (flags & ~(SBM_TUNE_NO_TMA | SBM_TUNE_PC_ADDITIVE)))
+      !(delta >= 0.0 && delta < 1.0) ||
+      (flags & ~(SBM_TUNE_NO_TMA | SBM_TUNE_PC_ADDITIVE | SBM_TUNE_HOST_LOOP)))
     return SBM_ERR_ARG;
   const int no_tma = (flags & SBM_TUNE_NO_TMA) ? 1 : 0;
   const int pc_add = (flags & SBM_TUNE_PC_ADDITIVE) ? 1 : 0;
@@ -242,6 +243,7 @@ int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta
   ctx->inner_tol = delta;
   ctx->no_tma = no_tma;
   ctx->pc_additive = pc_add;
+  ctx->host_loop = (flags & SBM_TUNE_HOST_LOOP) ? 1 : 0;
   return SBM_OK;
 }
 

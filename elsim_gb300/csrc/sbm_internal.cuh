@@ -527,6 +527,7 @@ struct sbm_ctx {
   int last_pc = -1;
   int no_tma = 0;  // tuning flag: use the register-tiled FP32 stencil instead of TMA
   int pc_additive = 0;  // tuning flag: additive learned preconditioner (no smoothing step)
+  int host_loop = 0;    // tuning flag: mixed-solver chunks driven from the host
   // learned preconditioner plan (opaque; owned by sbm_net.cu) and the
   // preconditioner the last mixed solve actually used
   void* net = nullptr;

@@ -1798,7 +1798,8 @@ int solve_mixed(sbm_ctx* ctx, const SolveSpec& sp, SolveResult* out) {
   int rc = mixed_begin(ctx, sp, &ex, &graph, &nodes);
   if (rc) return rc;
   CgState fin;
-  rc = run_loop(ctx, graph, nodes, sp.max_it, ctx->st, ctx->h_st, &fin);
+  rc = ctx->host_loop ? run_chunks(ctx, ex, nodes, ctx->st, ctx->h_st, &fin)
+                      : run_loop(ctx, graph, nodes, sp.max_it, ctx->st, ctx->h_st, &fin);
   if (rc) return rc;
   return mixed_end(ctx, sp, fin, out);
 }

@@ -35,6 +35,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_MAXIT, ERR_NONFINITE, ERR_BREAKDOWN, ERR_NOMEM, ERR_S
     0, -1, -2, -3, -4, -5, -6, -7, -8)
 TUNE_NO_TMA = 1
 TUNE_PC_ADDITIVE = 2
+TUNE_HOST_LOOP = 4
 BC_COPY, BC_ZERO = 0, 1
 OP_CNE, OP_PHP, OP_PHE, OP_GENERIC, OP_GENERIC_DIAG = 0, 1, 2, 3, 4
 STOP_REF_UPDATE, STOP_REF_RESID, STOP_REL_RES = 0, 1, 2
@@ -318,11 +319,14 @@ class Context:
         _check(self.lib.sbm_ctx_set_params(self._h, C.byref(params)), "sbm_ctx_set_params")
 
     def set_tuning(self, zc64=0, zc32=0, chunk=0, delta=0.0, no_tma=False,
-                   pc_additive=False) -> None:
+                   pc_additive=False, host_loop=False) -> None:
         """Launch-shape knobs (0 = built-in), the reliable-update factor, the
-        choice of the register-tiled instead of the TMA-staged stencil and of
-        the additive instead of the multiplicative learned preconditioner."""
-        flags = (TUNE_NO_TMA if no_tma else 0) | (TUNE_PC_ADDITIVE if pc_additive else 0)
+        choice of the register-tiled instead of the TMA-staged stencil, of
+        the additive instead of the multiplicative learned preconditioner and
+        of host-driven instead of device-looped iteration chunks (for
+        profilers that cannot see kernels inside conditional graphs)."""
+        flags = ((TUNE_NO_TMA if no_tma else 0) | (TUNE_PC_ADDITIVE if pc_additive else 0) |
+                 (TUNE_HOST_LOOP if host_loop else 0))
         _check(self.lib.sbm_ctx_set_tuning(self._h, zc64, zc32, chunk, delta, flags),
                "sbm_ctx_set_tuning")
 

@@ -168,10 +168,16 @@ int sbm_ctx_set_params(sbm_ctx* ctx, const sbm_params* p);
  * (SBM_TUNE_NO_TMA): use the register-tiled FP32 stencil instead of the
  * TMA-staged one; bit 1 (SBM_TUNE_PC_ADDITIVE): apply the learned
  * preconditioner in its additive form z = D^-1 r + P e_c instead of the
- * default multiplicative one z = z1 + 2.3 D^-1 (r - A z1), z1 = P e_c.
+ * default multiplicative one z = z1 + 2.3 D^-1 (r - A z1), z1 = P e_c;
+ * bit 2 (SBM_TUNE_HOST_LOOP): drive the mixed solver's captured iteration
+ * chunks from the host (one chunk in flight while the host reads the
+ * previous one's state) instead of looping them on the device in a
+ * conditional graph node -- the same kernels, for profilers that cannot
+ * see kernels inside conditional graphs.
  * No counterpart in the reference. */
 #define SBM_TUNE_NO_TMA 1
 #define SBM_TUNE_PC_ADDITIVE 2
+#define SBM_TUNE_HOST_LOOP 4
 int sbm_ctx_set_tuning(sbm_ctx* ctx, int zc64, int zc32, int chunk, double delta, int flags);
 /* The context's CUDA stream as an opaque handle (cudaStream_t), and a wait
  * for everything enqueued on it (no counterpart in the reference: its work
