@@ -196,3 +196,27 @@ def test_expired_device_wait_reports_timeout_and_the_context_recovers(built):
         x = ctx.download("x")
     assert info["status"] == 0
     assert _true_relres(prob, x) <= 1.05e-8
+
+
+@pytest.mark.parametrize("precond", [sbm.PC_JACOBI, sbm.PC_NONE])
+def test_host_driven_chunks_equal_the_device_loop(built, precond):
+    """The mixed solver loops its captured chunk on the device (a WHILE
+    conditional node); SBM_TUNE_HOST_LOOP drives the same chunk from the host
+    (for profilers).  Both run the same kernels on the same state, so the
+    iterations and the solution agree bit for bit."""
+    shape = (48, 40, 36)
+    m, prob = _problem(shape, 23, tunnel=True)
+    out = []
+    with sbm.Context(*shape) as ctx:
+        _load(ctx, prob)
+        for host in (False, True, False):
+            ctx.set_tuning(host_loop=host)
+            ctx.upload("x", prob["x"])
+            info = ctx.cg_solve(op=sbm.OP_GENERIC, bc_x0=sbm.BC_ZERO, bc_x1=sbm.BC_ZERO,
+                                scale=1.0, tol=1e-8, max_it=50000, stop_rule=sbm.STOP_REL_RES,
+                                precision=sbm.PREC_MIXED, precond=precond)
+            assert info["status"] == 0
+            out.append((info["iters"], info["final_res"], ctx.download("x")))
+    for iters, res, x in out[1:]:
+        assert iters == out[0][0] and res == out[0][1]
+        np.testing.assert_array_equal(x, out[0][2])
