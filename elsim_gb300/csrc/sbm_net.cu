@@ -1126,7 +1126,9 @@ __global__ void __launch_bounds__(256, 3)
     const float* H = R + 2 * kMRB / 4;
     const int i0 = y0 + 4 * mq, j = x0 + xl;
     const int64_t gbase = g.ix(i0, j, z0 + zl);
-#pragma unroll 1
+    // both items unrolled: their independent chains interleave, and the
+    // register allocation has no spills (0.088 -> 0.072 ms at 256^3)
+#pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int k = z0 + zl + 2 * h;
       if (i0 > g.ny) break;  // beyond a partial tile (ny is a multiple of 4)

@@ -305,3 +305,38 @@ def test_cne_form_preconditioner_matches_oracle(built):
                             scale=5.0, tol=1e-8, max_it=20000, stop_rule=sbm.STOP_REL_RES,
                             precision=sbm.PREC_MIXED, precond=sbm.PC_LEARNED)
         assert info["status"] == sbm.OK and ctx.last_precond() == sbm.PC_JACOBI
+
+
+def test_learned_cne_form_solve_matches_fp64(built):
+    """A mixed-precision solve of the CnE form with a network flagged as
+    reading the mass channel (random weights): the flexible-CG path of the
+    CnE form -- its double-float initial residual and replacements, the
+    multiplicative step's diagonal term, the direction kernel's CnE form --
+    reaches the FP64 CG's solution (a network that does not fit is switched
+    off by the progress check, so the solve still converges)."""
+    shape = (48, 64, 32)
+    ms = synth.microstructure(shape, seed=71, solid_fraction=0.6)
+    prob = learned.cne_problem(ms["psi"], np.random.default_rng(75))
+    net = sbm.Net(seed=76, mass=True)
+    net.out_scale = 0.5
+    rng = np.random.default_rng(77)
+    with sbm.Context(*shape) as ctx:
+        for f in ("coef", "weight", "diag"):
+            ctx.upload(f, prob[f])
+        rhs = np.zeros(ctx.hshape, order="F")
+        rhs[1:-1, 1:-1, 1:-1] = rng.normal(size=shape)
+        ctx.upload("rhs", rhs)
+        ctx.set_net(net)
+
+        def solve(precision, pc, tol):
+            ctx.upload("x", np.zeros(ctx.hshape, order="F"))
+            info = ctx.cg_solve(op=sbm.OP_GENERIC_DIAG, bc_x0=sbm.BC_COPY, bc_x1=sbm.BC_COPY,
+                                scale=5.0, tol=tol, max_it=20000, stop_rule=sbm.STOP_REL_RES,
+                                precision=precision, precond=pc)
+            return info, ctx.download("x")[1:-1, 1:-1, 1:-1]
+
+        ref, xr = solve(sbm.PREC_FP64, sbm.PC_NONE, 1e-12)
+        got, xg = solve(sbm.PREC_MIXED, sbm.PC_LEARNED, 1e-8)
+    assert ref["status"] == sbm.OK and got["status"] == sbm.OK
+    assert got["final_res"] <= 1e-8
+    assert _rel(xg, xr) <= 1e-6
