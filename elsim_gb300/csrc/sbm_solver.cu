@@ -13,6 +13,10 @@
 // computes alpha / beta / the stopping norm in a fixed summation order
 // (deterministic).  Chunks of iterations are captured once into a CUDA
 // graph and replayed; a `done` flag turns the rest of a chunk into no-ops.
+// The FP64 solver replays its chunk from the host (one chunk in flight
+// while the host reads the previous one's state); the mixed solver loops
+// its chunk on the device in a WHILE conditional node (one graph launch per
+// solve), or from the host under SBM_TUNE_HOST_LOOP.
 //
 // Two precisions:
 //   FP64  the drop-in: the reference's CG and stopping rules.
