@@ -940,7 +940,9 @@ __global__ void __launch_bounds__(256)
 // cell), interpolates z1 in y for them and their 6 neighbours from three
 // coarse values per row, and applies the FP32 operator with the
 // search-direction ghost rules.  The Jacobi weight invd is formed from the
-// same half coefficients (the operations of k_invdiag), so it is not read.
+// same half coefficients (k_invdiag's face sums; the reciprocal within
+// 1 ulp), so it is not read.  The cells' arithmetic runs on pairs of FP32
+// lanes, and a thread's two items (planes zl and zl + 2) are unrolled.
 // Global traffic per cell: r, q_old and hk read, r and z written (20 B).
 // z.r, z.q_old and r.r are reduced and the last block runs fcg_close.
 // Tiles are walked grid-stride (every block the same count: the barriers
