@@ -1,0 +1,356 @@
+"""Golden vectors of the reference's own Fortran, run by tests/golden/fortran_subset.py.
+
+TEST INFRASTRUCTURE ONLY.  Run where the reference sources are present:
+
+    python tests/golden/make_reference_golden.py [--reference DIR]
+
+(DIR defaults to /root/reference; the sources are read from DIR/src/frtrn and
+nothing is copied from them).  Writes tests/golden/reference_v1.npz, read by
+tests/test_oracle_reference.py.  Every case runs one routine or one main
+program of the reference, statement by statement, on seeded inputs of a
+small size; a main program's fixed production sizes are replaced by the
+interpreter's overrides (its PARAMETERs or the assignments of its sizes),
+its input files by read hooks, and its output files are captured from the
+write hooks.  Cases:
+
+  ls_absgrd   LevelSet_3D.f90 AbsGrd3DUW_XYZ on random sg in {-1, 0, 1}, f
+  ls_redist   LevelSet_3D.f90 ReDist3D_XYZ (dt = 1.0d-1), 175 steps
+  rm_redist   RM_UCNCT_3D.f90 ReDist3D_XYZ (dt = 1.0e-1, REAL(4)), 60 steps
+  ls_front    LevelSet_3D.f90 main program from the NoGrdBc3D call after the
+              stacking to the ReDist3D_XYZ call: Allen-Cahn (50 steps), sign,
+              reinitialisation (175 steps) of a voxel field
+  accdiff     AccDiff_3D.f90 main program, first frame: solid and electrolyte
+              connectivity fields after 1500 sweeps
+  rm          RM_UCNCT_3D.f90 main program, first frame: the solid and
+              electrolyte distances with the disconnected regions removed
+  tbl         SBMES Tbl_Chk_Pln_3DA on values in and outside [0, 1],
+              on the grid points and between them
+  dmn         SBMES MyDmnCmpn_YZ for several global sizes and rank grids
+  cmbn        SBMES_3D_Cmbn_MPI_v2.f90 main program: the combined field of
+              every rank's dump, for four field prefixes
+  sbmes       SBMES main program: set-up (psi, AvP, the constants and the
+              tables) and three time steps (Cahn-Hilliard, the CnE solve,
+              the Butler-Volmer Picard loop with the phP and phE solves, the
+              voltage control) on a 9 x 11 x 7 grid, one rank
+  sbmesp      the same with the SUM reductions in the C oracle's order (a
+              partial per z plane, then the partials): shows that the order
+              of the reductions is the only difference between the oracle
+              and the reference
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(HERE))
+sys.path.insert(0, str(ROOT))
+
+from fortran_subset import Interp, Stop  # noqa: E402
+
+from elsim_gb300 import synth  # noqa: E402
+from oracle import sbm_oracle as orc  # noqa: E402  (distances of the synthetic geometry)
+
+DEFAULT_REFERENCE = "/root/reference"
+SBMES = "SBMES_3D_MPI_CH_Gr_CONJG_VD_T05_01_BQ_hx3.f90"
+SBMES_MAIN = "SBMES_3D_MPI_CarGr_ConjG_v01"
+
+
+def _F(a, dtype=np.float64):
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+def _distance(shape, seed, solid_fraction=0.5, rmin=2.0, rmax=3.5):
+    """Signed distance (interior, positive in the solid) of a seeded sphere
+    packing, by 175 reinitialisation steps from zero."""
+    solid = synth.spheres(shape, seed, solid_fraction, rmin=rmin, rmax=rmax)
+    sg = synth.sign_field(solid)
+    d = orc.redist(175, sg, np.zeros_like(sg), 1.0e-1)
+    return d[1:-1, 1:-1, 1:-1].copy(order="F"), solid
+
+
+def case_absgrd_redist(src, out):
+    L, RM = src / "LevelSet_3D.f90", src / "RM_UCNCT_3D.f90"
+    it_l, it_r = Interp([L]), Interp([RM])
+    rng = np.random.default_rng(101)
+    py, px, pz = 7, 6, 5
+    sg = _F(rng.integers(-1, 2, size=(py + 2, px + 2, pz + 2)))
+    f = _F(rng.standard_normal((py + 2, px + 2, pz + 2)) * 2.0)
+    gr = _F(np.zeros((py, px, pz)))
+    it_l.call(L, "AbsGrd3DUW_XYZ", py, px, pz, sg, f, gr)
+    out.update(ls_absgrd_sg=sg, ls_absgrd_f=f, ls_absgrd_gr=gr)
+
+    d, solid = _distance((py, px, pz), 11)
+    sg = synth.sign_field(solid)
+    sg[3, 2, 2] = 0.0  # a cell with sg = 0 (no propagation)
+    f0 = _F(rng.standard_normal((py + 2, px + 2, pz + 2)))
+    f = f0.copy(order="F")
+    it_l.call(L, "ReDist3D_XYZ", 175, py, px, pz, sg, f)
+    out.update(ls_redist_sg=sg, ls_redist_f0=f0, ls_redist_f=f, ls_redist_lit=175)
+
+    py, px, pz = 6, 5, 4
+    sg = _F(np.where(rng.random((py + 2, px + 2, pz + 2)) < 0.45, 1.0, -1.0))
+    f0 = _F(rng.standard_normal((py + 2, px + 2, pz + 2)) * 0.5)
+    f = f0.copy(order="F")
+    it_r.call(RM, "ReDist3D_XYZ", 60, py, px, pz, sg, f)
+    out.update(rm_redist_sg=sg, rm_redist_f0=f0, rm_redist_f=f, rm_redist_lit=60)
+
+
+def case_ls_front(src, out):
+    L = src / "LevelSet_3D.f90"
+    yg, xg, zg = 8, 7, 6
+    it = Interp([L], overrides={"LevelSet_3D": dict(yg=yg, xg=xg, zg=zg, yo=yg, xo=xg, zo=zg)})
+    first = it.line_of(L, r"CALL\s+NoGrdBc3D\(py,\s*px,\s*pz,\s*dsF",
+                       start=it.line_of(L, r"dsF\(1:yg,561:730"))
+    last = it.line_of(L, r"CALL\s+ReDist3D_XYZ\(175", start=first)
+    solid = synth.spheres((yg, xg, zg), 21, 0.5, rmin=2.0, rmax=3.0)
+    ds = np.zeros((yg + 2, xg + 2, zg + 2), order="F")
+    ds[1:-1, 1:-1, 1:-1] = solid
+    fr = it.exec_lines(L, "LevelSet_3D", first, last,
+                       dict(py=yg, px=xg, pz=zg, dsF=ds))
+    out.update(ls_front_ds0=ds, ls_front_ds=fr.v["DSF"].a.copy(order="F"),
+               ls_front_lines=np.array([first, last]))
+
+
+def case_accdiff(src, out):
+    A = src / "AccDiff_3D.f90"
+    yg, xg, zg = 9, 8, 7
+    it = Interp([A], overrides={"AccDiff_3D": dict(yg=yg, xg=xg, zg=zg)})
+    d, _ = _distance((yg, xg, zg), 31, 0.5)
+    cap = {}
+
+    def on_read(fname, shape, dtype):
+        assert "L24Z" in fname, fname
+        return d
+
+    def on_write(fname, values):
+        tag = "solid" if "SOD_3D_CN" in fname else "elec"
+        cap[tag] = np.asarray(values[0]).copy(order="F")
+        if tag == "elec":
+            raise Stop
+
+    it.on_read, it.on_write = on_read, on_write
+    it.run_program(A, "AccDiff_3D")
+    out.update(accdiff_dist=d, accdiff_cn_solid=cap["solid"], accdiff_cn_elec=cap["elec"])
+
+
+def case_rm(src, out):
+    R = src / "RM_UCNCT_3D.f90"
+    yg, xg, zg = 7, 6, 5
+    it = Interp([R], overrides={"RM_UCNCT_3D": dict(yg=yg, xg=xg, zg=zg)})
+    d, _ = _distance((yg, xg, zg), 41, 0.5)
+    rng = np.random.default_rng(43)
+    cs = _F(np.where(rng.random((yg, xg, zg)) < 0.3, 0.0, rng.uniform(0.0, 1.0, (yg, xg, zg))))
+    ce = _F(np.where(rng.random((yg, xg, zg)) < 0.3, 5.0e-5, rng.uniform(0.0, 1.0, (yg, xg, zg))))
+    cap = {}
+
+    def on_read(fname, shape, dtype):
+        if "SOD_3D_CN" in fname:
+            return cs
+        if "LIQ_3D_CN" in fname:
+            return ce
+        assert "L24Z" in fname, fname
+        return d
+
+    def on_write(fname, values):
+        tag = "solid" if "GRP_LS" in fname else "elec"
+        cap[tag] = np.asarray(values[0]).copy(order="F")
+        if tag == "elec":
+            raise Stop
+
+    it.on_read, it.on_write = on_read, on_write
+    it.run_program(R, "RM_UCNCT_3D")
+    out.update(rm_dist=d, rm_cn_solid=cs, rm_cn_elec=ce, rm_ds_solid=cap["solid"],
+               rm_ds_elec=cap["elec"])
+
+
+def case_tbl(src, out):
+    S = src / SBMES
+    it = Interp([S])
+    rng = np.random.default_rng(51)
+    edges = [-0.5, -1e-300, 0.0, 1e-7, 0.005, 0.01, 0.0099999999, 0.0100000001, 0.07, 0.5,
+             0.555, 0.99, 0.995, 0.99999999, 1.0, 1.0000001, 2.0, 0.29, 0.57, 0.58]
+    cn = np.concatenate([edges, rng.uniform(-0.1, 1.1, 300), np.arange(101) / 100.0])
+    for sz in (101, 51):
+        cord = np.array([float(f"{t / (sz - 1):.6f}") for t in range(sz)])
+        vals = rng.standard_normal(sz)
+        fn = np.zeros(cn.size)
+        it.call(S, "Tbl_Chk_Pln_3DA", cn.size, 1, 1, sz, cord, vals, cn.copy(), fn)
+        out.update({f"tbl{sz}_cord": cord, f"tbl{sz}_vals": vals, f"tbl{sz}_cn": cn,
+                    f"tbl{sz}_fn": fn})
+
+
+def case_dmn(src, out):
+    S = src / SBMES
+    it = Interp([S])
+    rows = []
+    for gy, gz, rnb, cnb in ((186, 320, 12, 16), (9, 7, 3, 2), (10, 13, 4, 3), (5, 5, 1, 1),
+                             (17, 23, 5, 4)):
+        for rank in range(rnb * cnb):
+            r = it.call(S, "MyDmnCmpn_YZ", rank, gy, gz, rnb, cnb, 0, 0, 0, 0, 0, 0, 0, 0)
+            # (ddR, ddC, py, lwy, upy, pz, lwz, upz)
+            rows.append([gy, gz, rnb, cnb, rank] + [int(v) for v in r[5:]])
+    out["dmn"] = np.array(rows, dtype=np.int64)
+
+
+def case_cmbn(src, out):
+    C = src / "SBMES_3D_Cmbn_MPI_v2.f90"
+    gy, gx, gz, rnb, cnb = 9, 5, 7, 3, 2
+    it = Interp([C], overrides={"SBMES_3D_Cmbn_MPI_v1": dict(gy=gy, gx=gx, gz=gz, rnb=rnb,
+                                                             cnb=cnb)})
+    rng = np.random.default_rng(61)
+    fields = {p: _F(rng.standard_normal((gy, gx, gz)), np.float32) for p in ("CP", "CE", "PE", "PP")}
+    dec = {}
+    tmp = Interp([src / SBMES])
+    for rank in range(rnb * cnb):
+        r = tmp.call(src / SBMES, "MyDmnCmpn_YZ", rank, gy, gz, rnb, cnb, 0, 0, 0, 0, 0, 0, 0, 0)
+        _, _, py, lwy, upy, pz, lwz, upz = r[5:]
+        dec[rank] = (lwy, upy, lwz, upz)
+    cap = {}
+
+    def on_read(fname, shape, dtype):
+        base = Path(fname).name
+        pred, rank = base[:2], int(base[2:6]) - 1000
+        lwy, upy, lwz, upz = dec[rank]
+        return fields[pred][lwy - 1:upy, :, lwz - 1:upz]
+
+    def on_write(fname, values):
+        cap[Path(fname).name] = np.asarray(values[0]).copy(order="F")
+
+    it.on_read, it.on_write = on_read, on_write
+    fr = it.run_program(C, "SBMES_3D_Cmbn_MPI_v1")
+    for p, f in fields.items():
+        out[f"cmbn_in_{p}"] = f
+        out[f"cmbn_out_{p}"] = cap[f"{p}ASMB1135.dat"]
+    out["cmbn_idx"] = fr.v["IDXARY"].a.copy()
+    out["cmbn_dims"] = np.array([gy, gx, gz, rnb, cnb])
+
+
+def case_sbmes(src, out, steps=3, sum_order="sequential", pre="sbmes"):
+    S = src / SBMES
+    gy, gx, gz = 9, 11, 7
+    it = Interp([S], overrides={SBMES_MAIN: dict(gy=gy, gx=gx, gz=gz, rnb=1, cnb=1)},
+                sum_order=sum_order)
+    dist, _ = _distance((gy, gx, gz), 71, 0.5)
+    dist_p = _F(dist, np.float32)
+    dist_e = _F(-dist, np.float32)
+    x = np.array([float(f"{t / 100:.2f}") for t in range(101)])
+    tables = {
+        "C_Li_X_101": x,
+        "C_Li_M6_101": 0.05 * (2.0 * x - 1.0) + 0.02 * np.sin(6.0 * np.pi * x),
+        "C_Li_Mb5_101": 1.5e-11 * (1.0 + x),
+        "C_Li_J2_101": 1.0 + 0.5 * x * (1.0 - x),
+        "C_Li_O3_101": 0.2 - 0.1 * x,
+    }
+
+    def on_read(fname, shape, dtype):
+        if "GrMic_II_DS" in fname:
+            return dist_p
+        if "GrMic_II_DL" in fname:
+            return dist_e
+        for k, v in tables.items():
+            if k in fname:
+                return v
+        raise AssertionError(fname)
+
+    writes = []
+
+    def on_write(fname, values):
+        writes.append((Path(fname).name, [np.array(v, copy=True) for v in values]))
+
+    it.on_read, it.on_write = on_read, on_write
+    L_dc = it.line_of(S, r"^\s*dCrnt\s*=\s*ABS\(trgI-sCrnt\)")
+    L_cne = it.line_of(S, r"CALL BcMpiYZ\(.*CnE\(0:ny\+1",
+                       start=it.line_of(S, r"IF \( itlp > 50000 \) EXIT"))
+    L_it = it.line_of(S, r"^\s*iter\s*=\s*iter\s*\+\s*1\s*$")
+    rec = {"start": [], "cne_its": [], "end": []}
+    arr = lambda fr, n: np.array(fr.v[n].a, copy=True, order="F")
+
+    def at_start(fr):
+        if not rec["start"]:
+            for n in ("PSP", "PSE", "AVP", "AVPX", "CNP", "CNE", "PHP", "PHE"):
+                out[f"{pre}_setup_{n.lower()}"] = arr(fr, n)
+            for n in ("TBL", "DTBL", "ITBL", "OTBL"):
+                out[f"{pre}_{n.lower()}"] = arr(fr, n)
+            consts = ("DX", "DT", "RHO", "CST1", "FRD", "BVP", "BVE", "VSR", "VSR0", "DE", "DMP",
+                      "KPL", "T_MINUS", "D0", "TC1", "TC2", "EPS", "ZETA", "CRTE", "CRTP", "CRTL",
+                      "TPP", "TPE", "XRF", "TRGI", "SCRNT")
+            out[f"{pre}_const_names"] = np.array(consts)
+            out[f"{pre}_const"] = np.array([float(fr.v[n]) for n in consts])
+        rec["start"].append([float(fr.v["XRF"]), float(fr.v["SCRNT"]), float(fr.v["TRGI"])])
+
+    def at_cne(fr):
+        rec["cne_its"].append(int(fr.v["ITLP"]))
+
+    def at_end(fr):
+        e = {n: arr(fr, n) for n in ("CNP", "CNE", "PHP", "PHE", "RXN")}
+        sc = [float(fr.v[n]) for n in ("XRF", "SCRNT", "BVE", "TM", "DT", "VSR", "INFX", "CVGP",
+                                       "CVGL")]
+        ints = [int(fr.v[n]) for n in ("ITER", "NLP", "ITLP", "ITLE", "CNT")]
+        rec["end"].append((e, sc, ints))
+        if len(rec["end"]) == steps:
+            raise Stop
+
+    it.line_hooks[L_dc] = (at_start, None)
+    it.line_hooks[L_cne] = (at_cne, None)
+    it.line_hooks[L_it] = (None, at_end)
+    it.run_program(S, SBMES_MAIN)
+    if len(rec["end"]) != steps:
+        raise RuntimeError(f"the program ended after {len(rec['end'])} steps")
+    out[f"{pre}_dims"] = np.array([gy, gx, gz, steps])
+    out[f"{pre}_dist_p"], out[f"{pre}_dist_e"] = dist_p, dist_e
+    out[f"{pre}_raw_tables"] = np.stack([tables[k] for k in ("C_Li_X_101", "C_Li_M6_101",
+                                                              "C_Li_Mb5_101", "C_Li_J2_101",
+                                                              "C_Li_O3_101")])
+    out[f"{pre}_step_start"] = np.array(rec["start"])
+    out[f"{pre}_cne_its"] = np.array(rec["cne_its"])
+    for k, (e, sc, ints) in enumerate(rec["end"], 1):
+        for n, a in e.items():
+            out[f"{pre}_s{k}_{n.lower()}"] = a
+        out[f"{pre}_s{k}_scal"] = np.array(sc)
+        out[f"{pre}_s{k}_ints"] = np.array(ints)
+    out[f"{pre}_scal_names"] = np.array(["XRF", "SCRNT", "BVE", "TM", "DT", "VSR", "INFX", "CVGP",
+                                        "CVGL"])
+    out[f"{pre}_int_names"] = np.array(["ITER", "NLP", "ITLP", "ITLE", "CNT"])
+    for name, vals in writes:
+        if name.endswith(".dat"):
+            out[f"{pre}_file_{name[:-4]}"] = np.asarray(vals[0])
+        else:
+            out[f"{pre}_file_{name.replace('.', '_')}"] = np.array(
+                [float(v) for v in vals], dtype=np.float64)
+
+
+def case_sbmes_planes(src, out):
+    """The same three steps with the C oracle's order of the SUM reductions."""
+    case_sbmes(src, out, sum_order="planes", pre="sbmesp")
+
+
+CASES = [case_tbl, case_dmn, case_absgrd_redist, case_accdiff, case_rm, case_ls_front,
+         case_cmbn, case_sbmes, case_sbmes_planes]
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--reference", default=DEFAULT_REFERENCE)
+    ap.add_argument("--out", default=str(HERE / "reference_v1.npz"))
+    ap.add_argument("--only", nargs="*")
+    a = ap.parse_args(argv)
+    src = Path(a.reference) / "src" / "frtrn"
+    out = {}
+    for case in CASES:
+        if a.only and case.__name__[5:] not in a.only:
+            continue
+        t = time.time()
+        case(src, out)
+        print(f"{case.__name__}: {time.time() - t:.1f} s", flush=True)
+    np.savez_compressed(a.out, **out)
+    print("wrote", a.out, len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,226 @@
+"""The oracle and the host code against the reference's own results.  CPU only.
+
+tests/golden/reference_v1.npz holds what the reference's Fortran computes,
+statement by statement, on small seeded inputs (tests/golden/
+make_reference_golden.py runs its source files with the interpreter
+tests/golden/fortran_subset.py; the reference has no compiler here).  The
+element-wise routines must agree bit for bit.  The coupled time step must
+agree bit for bit once the interpreter sums in the oracle's order (a partial
+per z plane, then the partials: the 'sbmesp' run); with the reference's own
+sequential SUM the iteration counts agree exactly and the fields to the
+tolerances below, which are the rounding of one summation order against
+another, amplified through about 80 CG iterations of an ill-conditioned
+system (the concentration system's psE spans 1e-6 .. 1).
+"""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import sbm_oracle as orc
+
+G = np.load(Path(__file__).resolve().parent / "golden" / "reference_v1.npz")
+
+# field id of sbm_oracle.State / include/sbm_capi.h
+F_PSP, F_PSE, F_AVP, F_AVPX, F_CNP, F_CNE, F_PHP, F_PHE, F_RXN = range(9)
+
+
+def inner(a):
+    return a[1:-1, 1:-1, 1:-1]
+
+
+def test_table_lookup_matches_reference():
+    """Tbl_Chk_Pln_3DA (SBMES:987-1028): clamping below 0 and above 1, the
+    FLOOR segment with its end fix-ups, values on and between grid points."""
+    for sz in (101, 51):
+        fn = orc.table(G[f"tbl{sz}_cord"], G[f"tbl{sz}_vals"], G[f"tbl{sz}_cn"])
+        assert np.array_equal(fn, G[f"tbl{sz}_fn"]), sz
+
+
+def test_absgrd_and_redist_match_reference():
+    """AbsGrd3DUW_XYZ and ReDist3D_XYZ of LevelSet_3D.f90 (dt = 1.0d-1) and of
+    RM_UCNCT_3D.f90 (dt = 1.0e-1, a REAL(4) literal)."""
+    gr = orc.absgrd(G["ls_absgrd_sg"], G["ls_absgrd_f"])
+    assert np.array_equal(inner(gr), G["ls_absgrd_gr"])
+    f = orc.redist(int(G["ls_redist_lit"]), G["ls_redist_sg"], G["ls_redist_f0"], 1.0e-1)
+    assert np.array_equal(f, G["ls_redist_f"])
+    f = orc.redist(int(G["rm_redist_lit"]), G["rm_redist_sg"], G["rm_redist_f0"],
+                   float(np.float32(1.0e-1)))
+    assert np.array_equal(f, G["rm_redist_f"])
+
+
+def test_geometry_front_end_matches_reference():
+    """LevelSet_3D.f90 from the boundary fill after the stacking to the
+    reinitialisation: 50 Allen-Cahn steps, the sign field, 175 ReDist steps."""
+    ds = orc.allen_cahn(50, orc.nogrdbc(G["ls_front_ds0"]))
+    sg = orc.sign(ds.ravel(order="F")).reshape(ds.shape, order="F")
+    f = orc.redist(175, np.asfortranarray(sg), np.zeros_like(ds, order="F"), 1.0e-1)
+    assert np.array_equal(f, G["ls_front_ds"])
+
+
+def test_connectivity_matches_reference():
+    """AccDiff_3D.f90, one frame: 1500 accelerated-diffusion sweeps of the
+    solid and of the electrolyte phase."""
+    cs, ce = orc.connectivity(G["accdiff_dist"], 0.75, 1501)
+    assert np.array_equal(inner(cs), G["accdiff_cn_solid"])
+    assert np.array_equal(inner(ce), G["accdiff_cn_elec"])
+    assert 0.2 < (G["accdiff_cn_solid"] > 0).mean() < 0.9  # a non-trivial case
+
+
+def test_disconnected_region_removal_matches_reference():
+    """RM_UCNCT_3D.f90, one frame: mask, sign, 175 reinitialisation steps per phase."""
+    s, e = orc.rm_ucnct(G["rm_dist"], G["rm_cn_solid"], G["rm_cn_elec"], 175)
+    assert np.array_equal(inner(s), G["rm_ds_solid"])
+    assert np.array_equal(inner(e), G["rm_ds_elec"])
+
+
+def test_rank_decomposition_and_combine_match_reference(tmp_path):
+    """MyDmnCmpn_YZ (SBMES:947-982) and the combine program
+    (SBMES_3D_Cmbn_MPI_v2.f90) against elsim_gb300.fortran_io."""
+    from elsim_gb300 import fortran_io as fio
+    for row in G["dmn"]:
+        gy, gz, rnb, cnb, rank, ddr, ddc, py, lwy, upy, pz, lwz, upz = (int(v) for v in row)
+        assert tuple(fio.rank_decomposition(gy, gz, rnb, cnb)[rank]) == (lwy, upy, py, lwz, upz, pz)
+    gy, gx, gz, rnb, cnb = (int(v) for v in G["cmbn_dims"])
+    assert np.array_equal(G["cmbn_idx"], fio.rank_decomposition(gy, gz, rnb, cnb))
+    for p in ("CP", "CE", "PE", "PP"):
+        fio.write_rank_outputs(135, p, G[f"cmbn_in_{p}"], rnb, cnb, tmp_path)
+        und, path = fio.combine(135, p, gy, gx, gz, rnb, cnb, tmp_path)
+        assert np.array_equal(und, G[f"cmbn_out_{p}"])
+        assert np.array_equal(fio.read_array(path, np.float32, (gy, gx, gz)), G[f"cmbn_out_{p}"])
+
+
+def _consts(pre="sbmes"):
+    return {str(k): float(v) for k, v in zip(G[f"{pre}_const_names"], G[f"{pre}_const"])}
+
+
+def test_constants_match_reference(built):
+    """The set-up block's constants (SBMES:86-136), REAL(4) literals and
+    all, in the oracle and in the CUDA library's parameter defaults."""
+    from elsim_gb300 import sbm
+    c = _consts()
+    for p in (orc.params_reference(), sbm.reference_params()):
+        assert p.dx == c["DX"] and p.rho == c["RHO"] and p.eps == c["EPS"]
+        assert p.cst1 == c["CST1"] and p.frd == c["FRD"]
+        assert p.bvp == c["BVP"] and p.bve == c["BVE"]
+        assert p.t_minus == c["T_MINUS"] and p.d0 == c["D0"]
+        assert p.tc1 == c["TC1"] and p.tc2 == c["TC2"]
+        assert p.crt_cne == c["CRTE"] and p.crt_php == c["CRTP"] and p.crt_phe == c["CRTL"]
+
+
+def _state(pre):
+    gy, gx, gz, _ = (int(v) for v in G[f"{pre}_dims"])
+    p = orc.params_reference()
+    p.set_table("tbl_x", G[f"{pre}_tbl"][0])
+    p.set_table("tbl_mu", G[f"{pre}_tbl"][1])
+    p.set_table("tbl_mb", G[f"{pre}_dtbl"][1])  # scaled by 1.0d2*2/3 as SBMES:242 does
+    p.set_table("tbl_i0", G[f"{pre}_itbl"][1])
+    p.set_table("tbl_ocv", G[f"{pre}_otbl"][1])
+    st = orc.State(gy, gx, gz, p)
+    sc = st.setup_domain(G[f"{pre}_dist_p"], G[f"{pre}_dist_e"])
+    return st, sc
+
+
+def test_mobility_table_scaling_matches_reference():
+    raw = G["sbmes_raw_tables"]
+    assert np.array_equal(G["sbmes_dtbl"][1], raw[2] * 1.0e2 * 2 / 3)
+    assert np.array_equal(G["sbmes_tbl"], raw[:2])
+
+
+@pytest.mark.parametrize("pre", ["sbmes", "sbmesp"])
+def test_setup_matches_reference(pre):
+    """psi from the distances, the 1e-7 / 1e-6 floors, AvP and AvPx, the
+    initial fields (SBMES:138-351); the global sums to 1e-13 with the
+    reference's order of summation and exactly with the oracle's."""
+    st, sc = _state(pre)
+    for fid, n in ((F_PSP, "psp"), (F_PSE, "pse"), (F_CNP, "cnp"), (F_CNE, "cne"),
+                   (F_PHP, "php"), (F_PHE, "phe")):
+        assert np.array_equal(st.field(fid), G[f"{pre}_setup_{n}"]), n
+    for fid, n in ((F_AVP, "avp"), (F_AVPX, "avpx")):
+        assert np.array_equal(inner(st.field(fid)), G[f"{pre}_setup_{n}"]), n
+    c = _consts(pre)
+    for k, n in (("tPP", "TPP"), ("tPE", "TPE"), ("xrf", "XRF"), ("trgI", "TRGI")):
+        if pre == "sbmesp":
+            assert sc[k] == c[n], k
+        else:
+            assert abs(sc[k] - c[n]) <= 1e-13 * abs(c[n]), k
+
+
+# tolerance of the oracle's time step against the reference's, summation
+# order aside: max |difference| / max |reference| per field, relative for
+# the scalars (measured: cne 5.0e-5, rxn 1.6e-5, phe 2.6e-6, scrnt 2.3e-6,
+# cnp 1.8e-8, php 1.3e-12 by the third step)
+FIELD_TOL = {"cnp": 1e-7, "cne": 2e-4, "php": 1e-10, "phe": 1e-5, "rxn": 1e-4}
+SCALAR_TOL = {"XRF": 1e-12, "SCRNT": 1e-5, "BVE": 1e-12, "INFX": 1e-8}
+
+
+@pytest.mark.parametrize("pre", ["sbmes", "sbmesp"])
+def test_time_steps_match_reference(pre):
+    """Three passes of the time loop (SBMES:357-877) with the reference's own
+    dt and scan rate: Cahn-Hilliard, the CnE solve (skipped on the first
+    step), the Butler-Volmer Picard loop with its phP and phE solves, the
+    voltage control.  Every solve's iteration count and the Picard count are
+    the reference's; with the oracle's summation order every value is."""
+    st, _ = _state(pre)
+    exact = pre == "sbmesp"
+    names = [str(n) for n in G[f"{pre}_scal_names"]]
+    inames = [str(n) for n in G[f"{pre}_int_names"]]
+    steps = int(G[f"{pre}_dims"][3])
+    for k in range(1, steps + 1):
+        s = dict(zip(names, (float(v) for v in G[f"{pre}_s{k}_scal"])))
+        ii = dict(zip(inames, (int(v) for v in G[f"{pre}_s{k}_ints"])))
+        r = st.time_step(k, s["DT"], s["VSR"])
+        # the reference's counters run one past the iterations done
+        assert r["it_cne"] == int(G[f"{pre}_cne_its"][k - 1]) - 1, k
+        assert r["n_picard"] == ii["NLP"] - 1, k
+        assert r["it_php"] == ii["ITLP"] - 1 and r["it_phe"] == ii["ITLE"] - 1, k
+        fields = {"cnp": st.field(F_CNP), "cne": st.field(F_CNE), "php": st.field(F_PHP),
+                  "phe": st.field(F_PHE), "rxn": inner(st.field(F_RXN))}
+        for n, a in fields.items():
+            b = G[f"{pre}_s{k}_{n}"]
+            if exact:
+                assert np.array_equal(a, b), (k, n)
+            else:
+                assert np.abs(a - b).max() <= FIELD_TOL[n] * np.abs(b).max(), (k, n)
+        got = {"XRF": r["xrf"], "SCRNT": r["scrnt"], "BVE": r["bve"], "INFX": r["infx"],
+               "CVGP": r["cvgp"], "CVGL": r["cvgl"]}
+        for n, tol in SCALAR_TOL.items():
+            if exact:
+                assert got[n] == s[n], (k, n)
+            else:
+                assert abs(got[n] - s[n]) <= tol * max(abs(s[n]), 1e-300), (k, n)
+        if exact:
+            assert got["CVGP"] == s["CVGP"] and got["CVGL"] == s["CVGL"], k
+    assert steps == 3
+
+
+def test_step_schedule_matches_reference():
+    """dt and the voltage scan rate the time loop picks (SBMES:360-383) from
+    the Li fraction and the current error, REAL(4) literals and all."""
+    from elsim_gb300 import synth
+    names = [str(n) for n in G["sbmes_scal_names"]]
+    for k, (xrf, scrnt, trgi) in enumerate(G["sbmes_step_start"], 1):
+        s = dict(zip(names, (float(v) for v in G[f"sbmes_s{k}_scal"])))
+        dt, vsr = synth.step_schedule(float(xrf), abs(float(trgi) - float(scrnt)), float(trgi))
+        assert dt == s["DT"] and vsr == s["VSR"], k
+
+
+def test_output_files_match_reference(tmp_path):
+    """OutPut3D_A (SBMES:892-919, SNGL of the field) and ReC_TmFX
+    (SBMES:922-943) as elsim_gb300.fortran_io writes them, against what the
+    reference wrote at the set-up and at the end of the first step."""
+    from elsim_gb300 import fortran_io as fio
+    gy, gx, gz, _ = (int(v) for v in G["sbmes_dims"])
+    fields = {"PS": inner(G["sbmes_setup_psp"]), "PL": inner(G["sbmes_setup_pse"]),
+              "CP": inner(G["sbmes_s1_cnp"]), "CE": inner(G["sbmes_s1_cne"]),
+              "PP": inner(G["sbmes_s1_php"]), "PE": inner(G["sbmes_s1_phe"])}
+    for pred, a in fields.items():
+        path = fio.output3d_a(1, pred + "1000", a, tmp_path)
+        ref = G[f"sbmes_file_{pred}10001001"]
+        assert ref.dtype == np.float32
+        assert np.array_equal(fio.read_array(path, np.float32, (gy, gx, gz)), ref), pred
+    rec = G["sbmes_file_GBQ105TmFx_txt"]  # fr, iter, tm, Xrf, sCrnt, trgI, BvE
+    path = fio.rec_tmfx(int(rec[0]), "GBQ105", int(rec[1]), *rec[2:], directory=tmp_path)
+    assert np.array_equal(fio.read_tmfx(path)[0], rec)
