@@ -3,8 +3,9 @@
  *
  * A line-by-line FP64 restatement of the reference Fortran, used only as the
  * checker (tests/, __graft_entry__.smoke(), bench.py's CPU baseline leg).
- * Parity is UNPINNED by reference vectors (the reference has none and cannot
- * be compiled here); see sbm_oracle.h for the rules this file keeps.
+ * Pinned against the reference's own Fortran, run by an interpreter
+ * (tests/golden/reference_v1.npz); see sbm_oracle.h for the rules this file
+ * keeps.
  *
  * File references are to AffanMalik90/Elsim:
  *   SBMES = src/frtrn/SBMES_3D_MPI_CH_Gr_CONJG_VD_T05_01_BQ_hx3.f90

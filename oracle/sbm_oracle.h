@@ -6,11 +6,16 @@
  * checker by tests/, by __graft_entry__.smoke() and by bench.py's CPU
  * baseline leg.  The product path (elsim_gb300) never links or calls it.
  *
- * PARITY UNPINNED: the reference ships no tests, golden vectors or fixtures,
- * and it cannot be compiled here (no Fortran compiler, no MPI).  The
- * restatement is instead pinned by analytic known-answer tests (linear
- * Laplace solution, planar signed distance, flood-fill connectivity,
- * symmetric operator) in tests/test_oracle_pins.py.
+ * PARITY PINNED by the reference's own code: the reference ships no tests
+ * or golden vectors and cannot be compiled here (no Fortran compiler, no
+ * MPI), so tests/golden/fortran_subset.py interprets its Fortran sources
+ * and tests/golden/reference_v1.npz holds what they compute on small seeded
+ * cases.  This restatement matches them bit for bit (tests/
+ * test_oracle_reference.py): every element-wise routine, and the coupled
+ * time step too once the reference's SUMs run in this file's order of
+ * reduction (below); with the reference's sequential SUMs the iteration
+ * counts are identical and the fields agree to the solves' rounding.
+ * Analytic known-answer tests (tests/test_oracle_pins.py) pin it as well.
  *
  * Rules kept from the reference:
  *   - Fortran evaluation order of every expression (left to right for

@@ -2,9 +2,10 @@
 
 Imported by tests/, __graft_entry__.smoke() and bench.py's CPU baseline leg
 as the checker; the product (elsim_gb300) never imports it.  The oracle is a
-line-by-line FP64 C restatement of the reference Fortran; parity is
-unpinned by reference vectors (the reference has none and cannot be
-compiled here) and is pinned instead by analytic known-answer tests.
+line-by-line FP64 C restatement of the reference Fortran, pinned against the
+reference's own results on small seeded cases (its Fortran sources run by
+the interpreter tests/golden/fortran_subset.py, fixtures
+tests/golden/reference_v1.npz) and by analytic known-answer tests.
 """
 from __future__ import annotations
 

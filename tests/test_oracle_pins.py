@@ -1,7 +1,9 @@
 """Analytic known-answer tests of the C oracle (CPU only).
 
-The reference ships no test vectors, so the restatement is pinned by cases
-whose answer is known in closed form or by an independent direct solver.
+The reference ships no test vectors; besides its own results run by the
+Fortran-subset interpreter (tests/test_oracle_reference.py), the restatement
+is pinned here by cases whose answer is known in closed form or by an
+independent direct solver.
 """
 import numpy as np
 import pytest
