@@ -36,6 +36,8 @@ write hooks.  Cases:
               partial per z plane, then the partials): shows that the order
               of the reductions is the only difference between the oracle
               and the reference
+  sbmest      four steps on a 16 x 16 x 16 grid with the CG tolerances
+              tightened to 1e-11 (fields of the last step only)
 """
 from __future__ import annotations
 
@@ -231,12 +233,15 @@ def case_cmbn(src, out):
     out["cmbn_dims"] = np.array([gy, gx, gz, rnb, cnb])
 
 
-def case_sbmes(src, out, steps=3, sum_order="sequential", pre="sbmes"):
+def case_sbmes(src, out, steps=3, sum_order="sequential", pre="sbmes", shape=(9, 11, 7),
+               seed=71, crt=None, last_fields_only=False):
     S = src / SBMES
-    gy, gx, gz = 9, 11, 7
-    it = Interp([S], overrides={SBMES_MAIN: dict(gy=gy, gx=gx, gz=gz, rnb=1, cnb=1)},
-                sum_order=sum_order)
-    dist, _ = _distance((gy, gx, gz), 71, 0.5)
+    gy, gx, gz = shape
+    ovr = dict(gy=gy, gx=gx, gz=gz, rnb=1, cnb=1)
+    if crt is not None:  # the three CG stopping tolerances (SBMES:96-98)
+        ovr.update(crte=crt, crtp=crt, crtl=crt)
+    it = Interp([S], overrides={SBMES_MAIN: ovr}, sum_order=sum_order)
+    dist, _ = _distance((gy, gx, gz), seed, 0.5)
     dist_p = _F(dist, np.float32)
     dist_e = _F(-dist, np.float32)
     x = np.array([float(f"{t / 100:.2f}") for t in range(101)])
@@ -311,7 +316,8 @@ def case_sbmes(src, out, steps=3, sum_order="sequential", pre="sbmes"):
     out[f"{pre}_cne_its"] = np.array(rec["cne_its"])
     for k, (e, sc, ints) in enumerate(rec["end"], 1):
         for n, a in e.items():
-            out[f"{pre}_s{k}_{n.lower()}"] = a
+            if k == steps or not last_fields_only:
+                out[f"{pre}_s{k}_{n.lower()}"] = a
         out[f"{pre}_s{k}_scal"] = np.array(sc)
         out[f"{pre}_s{k}_ints"] = np.array(ints)
     out[f"{pre}_scal_names"] = np.array(["XRF", "SCRNT", "BVE", "TM", "DT", "VSR", "INFX", "CVGP",
@@ -330,8 +336,16 @@ def case_sbmes_planes(src, out):
     case_sbmes(src, out, sum_order="planes", pre="sbmesp")
 
 
+def case_sbmes_tight(src, out):
+    """Four steps on 16 x 16 x 16 with the CG tolerances at 1e-11, the
+    comparison case of solvers that stop on their own criteria (the GPU's
+    mixed-precision stage solves); fields of the last step only."""
+    case_sbmes(src, out, steps=4, pre="sbmest", shape=(16, 16, 16), seed=73, crt=1.0e-11,
+               last_fields_only=True)
+
+
 CASES = [case_tbl, case_dmn, case_absgrd_redist, case_accdiff, case_rm, case_ls_front,
-         case_cmbn, case_sbmes, case_sbmes_planes]
+         case_cmbn, case_sbmes, case_sbmes_planes, case_sbmes_tight]
 
 
 def main(argv=None):
