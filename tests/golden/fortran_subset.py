@@ -1037,7 +1037,7 @@ def _store_scalar(v, kind, clen):
 
 
 # ------------------------------------------------------------- statements
-_SIG_EXIT, _SIG_CYCLE, _SIG_RETURN = "EXIT", "CYCLE", "RETURN"
+_SIG_EXIT, _SIG_RETURN = "EXIT", "RETURN"  # CYCLE ends the body like a normal pass
 
 
 class _Builder:
@@ -1626,14 +1626,11 @@ class Interp:
             d = u.decls[dn]
             if d.dims is None:
                 fr.v[dn] = _store_scalar(r.get(caller), d.kind, d.clen)
-        arrays = []
         for dn, r in pairs:
             d = u.decls[dn]
             if d.dims is None:
                 continue
-            # shapes may use PARAMETERs of the callee, so evaluate them in a
-            # frame holding the scalars bound so far
-            shape, lb = _eval_dims(d.dims, fr)
+            shape, lb = _eval_dims(d.dims, fr)  # explicit shape from the scalar dummies
             view = r.view(caller) if r.view else None
             if view is None:
                 view = np.asarray(r.get(caller))
@@ -1645,7 +1642,6 @@ class Interp:
                 raise FortranError(f"{u.name}: actual {dn} has {flat.size} elements, dummy {n}")
             data = np.array(flat[:n], dtype=_NP[d.kind]).reshape(shape, order="F")
             fr.v[dn] = FArr(data, lb, d.kind)
-            arrays.append((dn, r, d))
         full = self._frame(u, bind=dict(fr.v))
         _run(u.body, full)
         for dn, r in pairs:
