@@ -26,6 +26,8 @@ write hooks.  Cases:
   tbl         SBMES Tbl_Chk_Pln_3DA on values in and outside [0, 1],
               on the grid points and between them
   dmn         SBMES MyDmnCmpn_YZ for several global sizes and rank grids
+  sched       SBMES time loop: the dt / scan-rate choice over a grid of Li
+              fractions and current errors, on and off its REAL(4) thresholds
   cmbn        SBMES_3D_Cmbn_MPI_v2.f90 main program: the combined field of
               every rank's dump, for four field prefixes
   sbmes       SBMES main program: set-up (psi, AvP, the constants and the
@@ -331,6 +333,33 @@ def case_sbmes(src, out, steps=3, sum_order="sequential", pre="sbmes", shape=(9,
                 [float(v) for v in vals], dtype=np.float64)
 
 
+def case_schedule(src, out):
+    """The time loop's choice of dt and scan rate (its two IF blocks after
+    dCrnt = ABS(trgI-sCrnt)) over a grid of Li fractions and current
+    errors, including values on the REAL(4) thresholds."""
+    S = src / SBMES
+    it = Interp([S])
+    first = it.line_of(S, r"^\s*dCrnt\s*=\s*ABS\(trgI-sCrnt\)")
+    last = it.line_of(S, r"Vsr\s*=\s*Vsr\*15", start=first) + 1  # its ENDIF
+    f4 = lambda v: float(np.float32(v))
+    trgi = 0.017946869136805158
+    vsr0 = 1.0e-2 * 1.0e1 / f4(3.25 ** 2) * f4(2.5)
+    xrfs = [0.0202, 0.05, f4(0.12) - 1e-12, f4(0.12), 0.12, 0.15, f4(0.20), 0.2, 0.5, 0.97]
+    ratios = [0.0, 0.05, f4(0.07), 0.07, 0.1, f4(0.20), 0.3, f4(0.40), 0.6, f4(0.75), 0.9, 2.5]
+    rows = []
+    for xrf in xrfs:
+        for r in ratios:
+            for sign in (1.0, -1.0):
+                scrnt = trgi - sign * r * trgi
+                fr = it.exec_lines(S, SBMES_MAIN, first, last,
+                                   dict(xrf=xrf, trgi=trgi, scrnt=scrnt, vsr0=vsr0, vsr=0.0,
+                                        dt=0.0))
+                rows.append([xrf, trgi, scrnt, float(fr.v["DCRNT"]), float(fr.v["DT"]),
+                             float(fr.v["VSR"])])
+    out["sched"] = np.array(rows)
+    out["sched_lines"] = np.array([first, last])
+
+
 def case_sbmes_planes(src, out):
     """The same three steps with the C oracle's order of the SUM reductions."""
     case_sbmes(src, out, sum_order="planes", pre="sbmesp")
@@ -344,7 +373,7 @@ def case_sbmes_tight(src, out):
                last_fields_only=True)
 
 
-CASES = [case_tbl, case_dmn, case_absgrd_redist, case_accdiff, case_rm, case_ls_front,
+CASES = [case_tbl, case_dmn, case_schedule, case_absgrd_redist, case_accdiff, case_rm, case_ls_front,
          case_cmbn, case_sbmes, case_sbmes_planes, case_sbmes_tight]
 
 

@@ -205,6 +205,12 @@ def test_step_schedule_matches_reference():
         s = dict(zip(names, (float(v) for v in G[f"sbmes_s{k}_scal"])))
         dt, vsr = synth.step_schedule(float(xrf), abs(float(trgi) - float(scrnt)), float(trgi))
         assert dt == s["DT"] and vsr == s["VSR"], k
+    # every branch, on and off the REAL(4) thresholds (0.07, 0.20, 0.40,
+    # 0.75 of the target current; Li fraction 0.12, 0.20)
+    for xrf, trgi, scrnt, dcrnt, dt, vsr in G["sched"]:
+        assert abs(trgi - scrnt) == dcrnt
+        assert synth.step_schedule(xrf, dcrnt, trgi) == (dt, vsr), (xrf, dcrnt / trgi)
+    assert len(set(G["sched"][:, 5])) == 14
 
 
 def test_output_files_match_reference(tmp_path):
