@@ -669,7 +669,7 @@ int step_voltage(sbm_ctx* ctx, double dt, double vsr, sbm_scalars* out) {
   if ((rc = fetch_scalars(ctx, 8))) return rc;
   ctx->sc.scrnt = ctx->h_scal[7];                                      // :826-828
   const double d = ctx->sc.trgI - ctx->sc.scrnt;
-  const double sv = (d >= 0.0) ? fabs(vsr) : -fabs(vsr);                // DSIGN
+  const double sv = copysign(fabs(vsr), d);  // DSIGN(Vsr, d): a -0.0 difference is negative
   ctx->sc.bve = ctx->sc.bve + sv * dt;                                 // :830
   k_shift<<<flat(g.ninterior()), 256, 0, ctx->stream>>>(g, ctx->f[SBM_F_PHE], -(sv * dt));
   SBM_LAUNCHED(1);

@@ -1039,7 +1039,7 @@ int orc_voltage_step(orc_state* s, double dt, double vsr, sbm_scalars* sc) {
   double* phe = s->f[SBM_F_PHE];
   s->scrnt = sum_prod(ny, nx, nz, s->f[SBM_F_RXN], s->f[SBM_F_AVPX]);
   const double d = s->trgI - s->scrnt;
-  const double sv = (d >= 0.0) ? fabs(vsr) : -fabs(vsr);      /* DSIGN */
+  const double sv = copysign(fabs(vsr), d); /* DSIGN: the sign of d, -0.0 negative */
   s->bve = s->bve + sv * dt;
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= nx; ++j)

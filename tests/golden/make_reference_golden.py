@@ -118,7 +118,8 @@ def case_ls_front(src, out):
     fr = it.exec_lines(L, "LevelSet_3D", first, last,
                        dict(py=yg, px=xg, pz=zg, dsF=ds))
     out.update(ls_front_ds0=ds, ls_front_ds=fr.v["DSF"].a.copy(order="F"),
-               ls_front_lines=np.array([first, last]))
+               ls_front_lines=np.array([first, last]),
+               ls_turd=fr.v["TURD"].a.copy())  # the DATA table of tunnel radii
 
 
 def case_accdiff(src, out):

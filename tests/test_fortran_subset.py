@@ -178,6 +178,26 @@ END PROGRAM T
     assert v["S"] == "1024"
 
 
+def test_data_sign_and_floor(tmp_path):
+    _, _, v = run(tmp_path, """
+PROGRAM T
+IMPLICIT NONE
+REAL(KIND=8), DIMENSION(0:2) :: t
+REAL(KIND=8) :: a, b, c
+INTEGER :: f1, f2
+DATA t / 0, 6.3826e+00, -1.5d0 /
+a = DSIGN(2.0d0, -0.0d0)
+b = DSIGN(-3.0d0, 1.0d0)
+c = MAX(1, 2.5, 0.5d0)
+f1 = FLOOR(-0.5d0)
+f2 = FLOOR(2.999d0)
+END PROGRAM T
+""")
+    assert list(v["T"].a) == [0.0, float(f32(6.3826)), -1.5]  # REAL(4) literal widened
+    assert v["A"] == -2.0 and math.copysign(1.0, v["A"]) < 0 and v["B"] == 3.0
+    assert v["C"] == 2.5 and (v["F1"], v["F2"]) == (-1, 2)
+
+
 def test_out_of_bounds_access_raises(tmp_path):
     p = tmp_path / "t.f90"
     p.write_text("""

@@ -60,6 +60,13 @@ def test_geometry_front_end_matches_reference():
     assert np.array_equal(f, G["ls_front_ds"])
 
 
+def test_tunnel_radii_match_reference():
+    """LevelSet_3D.f90's DATA table of tunnel radii: REAL(4) literals stored
+    into a REAL(8) array, as elsim_gb300.geometry keeps them."""
+    from elsim_gb300 import geometry
+    assert np.array_equal(geometry.TUNNEL_RADII, G["ls_turd"])
+
+
 def test_connectivity_matches_reference():
     """AccDiff_3D.f90, one frame: 1500 accelerated-diffusion sweeps of the
     solid and of the electrolyte phase."""
