@@ -32,7 +32,9 @@ floating-point operations (no -ffast-math, no FMA contraction):
   association (column-major) and copied back unless the dummy is
   INTENT(IN); a scalar variable actual is copied back likewise.
 * subscripts are bounds-checked: an access outside a declared extent raises
-  FortranError instead of aliasing other memory.
+  FortranError instead of aliasing other memory -- unless the Interp is made
+  with bounds="linear", which addresses such an element of a rank-3 array by
+  its column-major offset, as compiled code without bounds checks does.
 * main-program arrays and ALLOCATE start as zeros (static storage and fresh
   pages); a procedure's automatic arrays and real scalars start as NaN, so
   that a value read before it is written shows in the results.
@@ -926,7 +928,8 @@ class Unit:
                     return lambda fr: _elem1(fr.v[name], f0(fr), name)
                 if len(fs) == 3:
                     f0, f1, f2 = fs
-                    return lambda fr: _elem3(fr.v[name], f0(fr), f1(fr), f2(fr), name)
+                    return lambda fr: _elem3(fr.v[name], f0(fr), f1(fr), f2(fr), name,
+                                             fr.interp.linear)
                 return lambda fr: (lambda A: A.a[_idx(A, [f(fr) for f in fs], name)])(fr.v[name])
             sec = self._section(subs)
             return lambda fr: (lambda A: A.a[_slices(A, sec(fr), name)])(fr.v[name])
@@ -1017,14 +1020,35 @@ def _elem1(A, i, name):
     return A.a[j]
 
 
-def _elem3(A, i, j, k, name):
+def _elem3(A, i, j, k, name, linear=False):
     a = A.a
     lb = A.lb
     i0, j0, k0 = i - lb[0], j - lb[1], k - lb[2]
     s = a.shape
     if not (0 <= i0 < s[0] and 0 <= j0 < s[1] and 0 <= k0 < s[2]):
-        raise FortranError(f"{name}({i},{j},{k}) outside its bounds")
+        if not linear:
+            raise FortranError(f"{name}({i},{j},{k}) outside its bounds")
+        return _flat(A, name)[_linear_offset(A, (i0, j0, k0), name)]
     return a[i0, j0, k0]
+
+
+def _linear_offset(A, idx0, name):
+    """Column-major offset of the 0-based subscripts idx0 in A's storage, as
+    code compiled without bounds checks addresses an element whose
+    subscript leaves its dimension; FortranError when it leaves the storage."""
+    off, stride = 0, 1
+    for d, i in enumerate(idx0):
+        off += i * stride
+        stride *= A.a.shape[d]
+    if not 0 <= off < A.a.size:
+        raise FortranError(f"{name}: element outside the array's storage")
+    return off
+
+
+def _flat(A, name):
+    if not A.a.flags.f_contiguous:
+        raise FortranError(f"{name}: linear addressing of a non-contiguous array")
+    return A.a.reshape(-1, order="F")
 
 
 def _store_scalar(v, kind, clen):
@@ -1374,7 +1398,10 @@ class _Builder:
                 i, j, kk = f0(fr) - A.lb[0], f1(fr) - A.lb[1], f2(fr) - A.lb[2]
                 s = A.a.shape
                 if not (0 <= i < s[0] and 0 <= j < s[1] and 0 <= kk < s[2]):
-                    raise FortranError(f"{name}: store outside its bounds")
+                    if not fr.interp.linear:
+                        raise FortranError(f"{name}: store outside its bounds")
+                    _flat(A, name)[_linear_offset(A, (i, j, kk), name)] = convert(v, A.kind)
+                    return None
                 A.a[i, j, kk] = convert(v, A.kind)
                 return None
 
@@ -1520,9 +1547,16 @@ class Interp:
     call_hooks {name: f(frame, refs)} for CALLs, line_hooks {line: (before,
     after)} on the statements starting at a line.  sum_order "sequential"
     (the compiled reference's) or "planes" (the C oracle's, see _sum_planes).
+    bounds "check" (a subscript outside its dimension raises) or "linear"
+    (an element of a rank-3 array whose subscript leaves its dimension is
+    addressed by its column-major offset, as compiled code without bounds
+    checks does, as long as that stays inside the array's storage).
     """
 
-    def __init__(self, paths, overrides=None, sum_order="sequential"):
+    def __init__(self, paths, overrides=None, sum_order="sequential", bounds="check"):
+        if bounds not in ("check", "linear"):
+            raise ValueError(f"bounds {bounds!r}")
+        self.linear = bounds == "linear"
         self.overrides = {k.upper(): {n.upper(): v for n, v in d.items()}
                           for k, d in (overrides or {}).items()}
         self.intrinsics = dict(INTRINSICS)

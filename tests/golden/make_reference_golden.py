@@ -19,6 +19,10 @@ write hooks.  Cases:
   ls_front    LevelSet_3D.f90 main program from the NoGrdBc3D call after the
               stacking to the ReDist3D_XYZ call: Allen-Cahn (50 steps), sign,
               reinitialisation (175 steps) of a voxel field
+  ls_geom     LevelSet_3D.f90 main program at its own size (93 x 730 x 160),
+              first frame: reorientation, tunnels (with the loop's stores
+              beyond TmpB's second extent addressed as compiled code does),
+              stacking, NoGrdBc3D, 50 Allen-Cahn steps; SHA-256 of the fields
   accdiff     AccDiff_3D.f90 main program, first frame: solid and electrolyte
               connectivity fields after 1500 sweeps
   rm          RM_UCNCT_3D.f90 main program, first frame: the solid and
@@ -44,6 +48,7 @@ write hooks.  Cases:
 from __future__ import annotations
 
 import argparse
+import hashlib
 import sys
 import time
 from pathlib import Path
@@ -120,6 +125,42 @@ def case_ls_front(src, out):
     out.update(ls_front_ds0=ds, ls_front_ds=fr.v["DSF"].a.copy(order="F"),
                ls_front_lines=np.array([first, last]),
                ls_turd=fr.v["TURD"].a.copy())  # the DATA table of tunnel radii
+
+
+def _sha(a):
+    return hashlib.sha256(np.asfortranarray(a).tobytes(order="F")).hexdigest()
+
+
+def case_ls_geometry(src, out):
+    """LevelSet_3D.f90's main program at its own size, first frame (tunnel
+    radius TuRd(3)), from 500 x 520 x 170 seeded voxels: reorientation, the
+    two tunnels -- whose loop over j = 1..730 stores TmpB(i,j,k) beyond
+    TmpB's second extent (170), an element compiled code addresses by its
+    column-major offset (bounds="linear") -- the stacking of four
+    thicknesses, NoGrdBc3D, then 50 Allen-Cahn steps.  The fields hold 11 M
+    values, so their SHA-256 (column-major float64 bytes) and sums are kept."""
+    L = src / "LevelSet_3D.f90"
+    it = Interp([L], bounds="linear")
+    vox = np.asfortranarray(synth.spheres((500, 520, 170), 81, 0.6).astype(np.float64))
+    it.on_read = lambda fname, shape, dtype: vox
+    first = it.line_of(L, r"CALL\s+NoGrdBc3D\(py,\s*px,\s*pz,\s*dsF",
+                       start=it.line_of(L, r"dsF\(1:yg,561:730"))
+    ac = it.line_of(L, r"^\s*DO\s+iter\s*=\s*1\s*,\s*50", start=first)
+
+    def stacked(fr):
+        a = fr.v["DSF"].a
+        out.update(ls_geom_sha=np.array(_sha(a)), ls_geom_sum=np.array(float(a.sum())))
+
+    def smoothed(fr):
+        a = fr.v["DSF"].a
+        out.update(ls_geom_ac_sha=np.array(_sha(a)), ls_geom_ac_sum=np.array(float(a.sum())),
+                   ls_geom_tr=np.array(float(fr.v["TR"])))
+        raise Stop
+
+    it.line_hooks[first] = (None, stacked)
+    it.line_hooks[ac] = (None, smoothed)
+    it.run_program(L, "LevelSet_3D")
+    out["ls_geom_vox_sha"] = np.array(_sha(vox))
 
 
 def case_accdiff(src, out):
@@ -375,7 +416,7 @@ def case_sbmes_tight(src, out):
 
 
 CASES = [case_tbl, case_dmn, case_schedule, case_absgrd_redist, case_accdiff, case_rm, case_ls_front,
-         case_cmbn, case_sbmes, case_sbmes_planes, case_sbmes_tight]
+         case_cmbn, case_sbmes, case_sbmes_planes, case_sbmes_tight, case_ls_geometry]
 
 
 def main(argv=None):

@@ -279,3 +279,24 @@ def test_fixture_reproduces_from_the_reference_sources():
     for k, a in out.items():
         assert k in G.files, k
         assert np.array_equal(np.asarray(a), G[k]), k
+
+
+def test_linear_addressing_of_an_element_outside_its_dimension(tmp_path):
+    src = """
+PROGRAM T
+IMPLICIT NONE
+REAL(KIND=8), DIMENSION(2,3,4) :: a
+REAL(KIND=8) :: r
+a = 0.0
+a(1,5,1) = 7.0
+r = a(2,4,1)
+END PROGRAM T
+"""
+    p = tmp_path / "t.f90"
+    p.write_text(src)
+    with pytest.raises(fs.FortranError):
+        fs.Interp([p]).run_program(p, "T")
+    v = fs.Interp([p], bounds="linear").run_program(p, "T").v
+    a = v["A"].a
+    # (1,5,1) is offset 0 + 2*4 = 8, i.e. element (1,2,2); (2,4,1) is (2,1,2)
+    assert a[0, 1, 1] == 7.0 and np.count_nonzero(a) == 1 and v["R"] == 0.0

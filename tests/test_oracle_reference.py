@@ -14,6 +14,7 @@ system (the concentration system's psE spans 1e-6 .. 1).
 """
 from __future__ import annotations
 
+import hashlib
 from pathlib import Path
 
 import numpy as np
@@ -65,6 +66,27 @@ def test_tunnel_radii_match_reference():
     into a REAL(8) array, as elsim_gb300.geometry keeps them."""
     from elsim_gb300 import geometry
     assert np.array_equal(geometry.TUNNEL_RADII, G["ls_turd"])
+
+
+def _sha(a):
+    return hashlib.sha256(np.asfortranarray(a).tobytes(order="F")).hexdigest()
+
+
+def test_full_size_geometry_matches_reference():
+    """LevelSet_3D.f90's own frame at its own size (93 x 730 x 160 from
+    500 x 520 x 170 voxels, tunnel radius TuRd(3)): reorientation, the
+    tunnels -- their loop stores TmpB(i,j,k) for j up to 730 beyond TmpB's
+    second extent of 170, addressed by column-major offset as the compiled
+    reference does -- the four stacked thicknesses and NoGrdBc3D, then 50
+    Allen-Cahn steps; bit for bit, by SHA-256 of the 11 M values."""
+    from elsim_gb300 import geometry, synth
+    vox = np.asfortranarray(synth.spheres((500, 520, 170), 81, 0.6).astype(np.float64))
+    assert _sha(vox) == str(G["ls_geom_vox_sha"])
+    tr = float(G["ls_geom_tr"])
+    assert tr == geometry.TUNNEL_RADII[3]
+    ds = orc.ls_geometry(vox, 93, 160, 50, 4, tr)
+    assert _sha(ds) == str(G["ls_geom_sha"])
+    assert _sha(orc.allen_cahn(50, ds)) == str(G["ls_geom_ac_sha"])
 
 
 def test_connectivity_matches_reference():
