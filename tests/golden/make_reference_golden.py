@@ -42,6 +42,9 @@ write hooks.  Cases:
               partial per z plane, then the partials): shows that the order
               of the reductions is the only difference between the oracle
               and the reference
+  sbmesl      101 steps of the 9 x 11 x 7 case with a smaller mobility (the
+              mean correction at step 101), fields of the last step; sbmeslp
+              the same in the oracle's order of summation
   sbmest      four steps on a 16 x 16 x 16 grid with the CG tolerances
               tightened to 1e-11 (fields of the last step only)
 """
@@ -278,7 +281,7 @@ def case_cmbn(src, out):
 
 
 def case_sbmes(src, out, steps=3, sum_order="sequential", pre="sbmes", shape=(9, 11, 7),
-               seed=71, crt=None, last_fields_only=False):
+               seed=71, crt=None, last_fields_only=False, mobility=1.5e-11):
     S = src / SBMES
     gy, gx, gz = shape
     ovr = dict(gy=gy, gx=gx, gz=gz, rnb=1, cnb=1)
@@ -292,7 +295,7 @@ def case_sbmes(src, out, steps=3, sum_order="sequential", pre="sbmes", shape=(9,
     tables = {
         "C_Li_X_101": x,
         "C_Li_M6_101": 0.05 * (2.0 * x - 1.0) + 0.02 * np.sin(6.0 * np.pi * x),
-        "C_Li_Mb5_101": 1.5e-11 * (1.0 + x),
+        "C_Li_Mb5_101": mobility * (1.0 + x),
         "C_Li_J2_101": 1.0 + 0.5 * x * (1.0 - x),
         "C_Li_O3_101": 0.2 - 0.1 * x,
     }
@@ -407,6 +410,16 @@ def case_sbmes_planes(src, out):
     case_sbmes(src, out, sum_order="planes", pre="sbmesp")
 
 
+def case_sbmes_long(src, out):
+    """101 steps on the 9 x 11 x 7 grid (the CnE mean correction runs again
+    at step 101), with a mobility table 100 times smaller so that the
+    explicit Cahn-Hilliard update stays stable that long; fields of the last
+    step only; with the reference's and with the oracle's summation order."""
+    for order, pre in (("sequential", "sbmesl"), ("planes", "sbmeslp")):
+        case_sbmes(src, out, steps=101, sum_order=order, pre=pre, last_fields_only=True,
+                   mobility=1.5e-13)
+
+
 def case_sbmes_tight(src, out):
     """Four steps on 16 x 16 x 16 with the CG tolerances at 1e-11, the
     comparison case of solvers that stop on their own criteria (the GPU's
@@ -416,7 +429,8 @@ def case_sbmes_tight(src, out):
 
 
 CASES = [case_tbl, case_dmn, case_schedule, case_absgrd_redist, case_accdiff, case_rm, case_ls_front,
-         case_cmbn, case_sbmes, case_sbmes_planes, case_sbmes_tight, case_ls_geometry]
+         case_cmbn, case_sbmes, case_sbmes_planes, case_sbmes_long, case_sbmes_tight,
+         case_ls_geometry]
 
 
 def main(argv=None):
