@@ -196,8 +196,12 @@ def _math1(name):
     def g8(v):
         try:
             return f8(v)
-        except (ValueError, OverflowError):
-            return float("nan") if name != "exp" else (math.inf if v > 0 else 0.0)
+        except (ValueError, OverflowError):  # libm's IEEE results where Python raises
+            if name == "exp":
+                return math.inf
+            if name == "log" and v == 0.0:
+                return -math.inf
+            return float("nan")
 
     def f(x):
         k = kind_of(x)

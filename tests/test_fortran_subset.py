@@ -198,6 +198,13 @@ END PROGRAM T
     assert v["C"] == 2.5 and (v["F1"], v["F2"]) == (-1, 2)
 
 
+def test_ieee_results_where_python_raises():
+    f = fs.INTRINSICS
+    assert f["LOG"](0.0) == -math.inf and math.isnan(f["LOG"](-1.0))
+    assert f["EXP"](1000.0) == math.inf and f["EXP"](-1000.0) == 0.0
+    assert math.isnan(f["SQRT"](-1.0))
+
+
 def test_out_of_bounds_access_raises(tmp_path):
     p = tmp_path / "t.f90"
     p.write_text("""
