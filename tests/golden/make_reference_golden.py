@@ -30,6 +30,9 @@ write hooks.  Cases:
   tbl         SBMES Tbl_Chk_Pln_3DA on values in and outside [0, 1],
               on the grid points and between them
   dmn         SBMES MyDmnCmpn_YZ for several global sizes and rank grids
+  loop        SBMES main program's loop control with the Li fraction, the
+              current and BvE forced to a script after each step: dt, scan
+              rate, tm, every file written and when, ReC_TmFX lines, the stop
   sched       SBMES time loop: the dt / scan-rate choice over a grid of Li
               fractions and current errors, on and off its REAL(4) thresholds
   cmbn        SBMES_3D_Cmbn_MPI_v2.f90 main program: the combined field of
@@ -405,6 +408,89 @@ def case_schedule(src, out):
     out["sched_lines"] = np.array([first, last])
 
 
+def loop_script(k):
+    """Li fraction, current and BvE forced after step k of the loop case:
+    Xrf rises 0.0029 per step (past every output threshold, the dt
+    thresholds 0.12 and 0.20), the current error cycles through the scan-rate
+    branches, BvE rises 0.0051 per step to the stop condition at step 70."""
+    trgi = 0.017946869136805158
+    r = (0.01, 0.1, 0.3, 0.5, 0.9, 1.5)[k % 6]
+    return 0.0202 + 0.0029 * k, trgi * (1.0 - r), -0.4495 + 0.0051 * k
+
+
+def case_loop(src, out):
+    """The SBMES main program's loop control (SBMES:351-877) on 9 x 11 x 7:
+    after each step's own Xrf, sCrnt and BvE are computed, hooks replace them
+    with loop_script(iter), so that the run crosses the output thresholds,
+    the dt and scan-rate branches and the stop condition; recorded: each
+    step's dt, scan rate and tm, every file the program writes with the step
+    it writes it in, the ReC_TmFX lines, the step at which the loop ends."""
+    S = src / SBMES
+    it = Interp([S], overrides={SBMES_MAIN: dict(gy=9, gx=11, gz=7, rnb=1, cnb=1)})
+    dist, _ = _distance((9, 11, 7), 71, 0.5)
+    x = np.array([float(f"{t / 100:.2f}") for t in range(101)])
+    tables = {"C_Li_X_101": x,
+              "C_Li_M6_101": 0.05 * (2.0 * x - 1.0) + 0.02 * np.sin(6.0 * np.pi * x),
+              "C_Li_Mb5_101": 1.5e-13 * (1.0 + x),
+              "C_Li_J2_101": 1.0 + 0.5 * x * (1.0 - x),
+              "C_Li_O3_101": 0.2 - 0.1 * x}
+
+    def on_read(fname, shape, dtype):
+        if "GrMic_II_DS" in fname:
+            return _F(dist, np.float32)
+        if "GrMic_II_DL" in fname:
+            return _F(-dist, np.float32)
+        return next(v for k, v in tables.items() if k in fname)
+
+    cur = {"iter": 0}
+    writes, tmfx, steps = [], [], []
+
+    def on_write(fname, values):
+        name = Path(fname).name
+        writes.append((name, cur["iter"]))
+        if "TmFx" in name:
+            tmfx.append([float(v) for v in values])
+
+    it.on_read, it.on_write = on_read, on_write
+    loop = it.line_of(S, r"^\s*DO WHILE \( Xrf < 0\.971 \)")
+    lines = dict(
+        dc=it.line_of(S, r"^\s*dCrnt\s*=\s*ABS\(trgI-sCrnt\)"),
+        xrf=it.line_of(S, r"^\s*Xrf\s*=\s*SUM\(VaER\(0:np-1\)\)/tPP", start=loop),
+        scrnt=it.line_of(S, r"^\s*sCrnt\s*=\s*SUM\(VaER\(0:np-1\)\)", start=loop),
+        bve=it.line_of(S, r"^\s*BvE\s*=\s*BvE\s*\+\s*DSIGN", start=loop),
+        it=it.line_of(S, r"^\s*iter\s*=\s*iter\s*\+\s*1\s*$"))
+    init = {}
+
+    def at_dc(fr):
+        cur["iter"] = int(fr.v["ITER"])
+        if not init:
+            init.update(xrf=float(fr.v["XRF"]), scrnt=float(fr.v["SCRNT"]),
+                        trgi=float(fr.v["TRGI"]), bve=float(fr.v["BVE"]))
+
+    def force(name, idx):
+        def hook(fr):
+            fr.v[name] = float(loop_script(int(fr.v["ITER"]))[idx])
+        return hook
+
+    def at_end(fr):
+        steps.append([int(fr.v["ITER"]) - 1, float(fr.v["DT"]), float(fr.v["VSR"]),
+                      float(fr.v["TM"])])
+
+    it.line_hooks[lines["dc"]] = (at_dc, None)
+    it.line_hooks[lines["xrf"]] = (None, force("XRF", 0))
+    it.line_hooks[lines["scrnt"]] = (None, force("SCRNT", 1))
+    it.line_hooks[lines["bve"]] = (None, force("BVE", 2))
+    it.line_hooks[lines["it"]] = (None, at_end)
+    fr = it.run_program(S, SBMES_MAIN)
+    out["loop_init"] = np.array([init["xrf"], init["scrnt"], init["trgi"], init["bve"]])
+    out["loop_steps"] = np.array(steps)
+    out["loop_end_iter"] = np.array(int(fr.v["ITER"]))
+    out["loop_write_names"] = np.array([w[0] for w in writes])
+    out["loop_write_iters"] = np.array([w[1] for w in writes])
+    out["loop_tmfx"] = np.array(tmfx)
+    out["loop_script"] = np.array([loop_script(k) for k in range(1, int(fr.v["ITER"]) + 1)])
+
+
 def case_sbmes_planes(src, out):
     """The same three steps with the C oracle's order of the SUM reductions."""
     case_sbmes(src, out, sum_order="planes", pre="sbmesp")
@@ -428,7 +514,7 @@ def case_sbmes_tight(src, out):
                last_fields_only=True)
 
 
-CASES = [case_tbl, case_dmn, case_schedule, case_absgrd_redist, case_accdiff, case_rm, case_ls_front,
+CASES = [case_tbl, case_dmn, case_schedule, case_loop, case_absgrd_redist, case_accdiff, case_rm, case_ls_front,
          case_cmbn, case_sbmes, case_sbmes_planes, case_sbmes_long, case_sbmes_tight,
          case_ls_geometry]
 

@@ -341,3 +341,55 @@ def test_101_steps_match_reference(pre):
 # max |reference| (measured: cne 1.2e-4, rxn 7.5e-6, cnp 2.7e-6, phe 2.5e-6,
 # php 1.1e-11)
 LONG_TOL = {"cnp": 2e-5, "cne": 1e-3, "php": 1e-9, "phe": 2e-5, "rxn": 5e-5}
+
+
+class _ScriptedContext:
+    """Stands in for sbm.Context in the loop-control test: after step k it
+    holds the Li fraction, current and BvE the reference was forced to."""
+
+    def __init__(self, init, script):
+        self.s = dict(xrf=init[0], scrnt=init[1], trgI=init[2], bve=init[3])
+        self.script = script
+
+    def scalars(self):
+        return dict(self.s)
+
+    def time_step(self, it, dt, vsr, precision=0):
+        x, c, b = (float(v) for v in self.script[it - 1])
+        self.s.update(xrf=x, scrnt=c, bve=b)
+        return dict(self.s)
+
+    def download(self, fid, haloed=True):
+        return np.full((9, 11, 7), float(fid))
+
+
+def test_cell_loop_matches_reference(tmp_path):
+    """elsim_gb300.cell against the reference main program's own loop control
+    (SBMES:351-877) with the same Li fraction, current and BvE after every
+    step: each step's dt and scan rate, tm, every file written and in which
+    step, the ReC_TmFX lines (and the file they make), the step that ends
+    the loop."""
+    from elsim_gb300 import cell
+    from elsim_gb300 import fortran_io as fio
+    ctx = _ScriptedContext([float(v) for v in G["loop_init"]], G["loop_script"])
+    cell.write_setup(ctx, tmp_path)
+    res = cell.run(ctx, directory=tmp_path)
+    assert res["why"] == "stop" and res["iter"] == int(G["loop_end_iter"])
+    steps = [e for e in res["events"] if e[0] == "step"]
+    assert len(steps) == res["iter"]
+    tm = 0.0
+    for (_, k, dt, vsr), (rk, rdt, rvsr, rtm) in zip(steps, G["loop_steps"]):
+        tm = tm + dt
+        assert (k, dt, vsr, tm) == (int(rk), rdt, rvsr, rtm), k
+    names = [("PS10001001.dat", 0), ("PL10001001.dat", 0)]
+    for e in res["events"]:
+        if e[0] == "dump":
+            names.append((f"{e[1]}1000{1000 + e[2]:4d}.dat", e[3]))
+        elif e[0] == "tmfx":
+            names.append(("GBQ105TmFx.txt", e[2]))
+    assert names == [(str(n), int(i)) for n, i in zip(G["loop_write_names"], G["loop_write_iters"])]
+    rows = np.array([e[1:] for e in res["events"] if e[0] == "tmfx"], dtype=np.float64)
+    assert np.array_equal(rows, G["loop_tmfx"])
+    assert np.array_equal(fio.read_tmfx(tmp_path / "GBQ105TmFx.txt"), G["loop_tmfx"])
+    assert sorted(p.name for p in tmp_path.glob("*.dat")) == sorted(
+        {str(n) for n in G["loop_write_names"] if str(n).endswith(".dat")})
